@@ -1,0 +1,274 @@
+/*
+ * grisrt.h — C ABI of the GB300-native ReSTIR PT (GRIS) pass.
+ *
+ * Drop-in boundary for the reference's GRISReSTIR pass (src/GRISReSTIR.h:24-26):
+ *   GRISReSTIR::createPipeline(ShaderManager*, descLayouts)      -> grisCreate / grisSceneCreate
+ *   GRISReSTIR::render(cmd, extent, DescriptorSetBindingMap)     -> grisPassRender (caller-owned
+ *                                                                    device buffers, like the
+ *                                                                    descriptor sets) or
+ *                                                                    grisFrameRender (library-owned
+ *                                                                    frame buffers with the
+ *                                                                    renderer's ping-pong)
+ * and for its input producers:
+ *   GBufferPass::render (src/GBufferPass.cpp:22-55, raster)      -> grisPassGBuffer / grisFrameGBuffer
+ *   DeviceScene ctor + createAccelerationStructure
+ *     (src/Scene.cpp:324-330, 448-547)                           -> grisSceneCreate (8-wide BVH)
+ *   Scene::buildLightDataStructure (src/Scene.cpp:309-322)       -> grisBuildLightTable
+ *   Camera::update (src/Camera.cpp:78-98)                        -> grisCameraSetup
+ *
+ * Conventions: every call returns GRIS_OK (0) or a negative GRIS_ERR_* code and never
+ * throws; grisGetError() gives the context's last message. Work is enqueued on the
+ * context's CUDA stream and the call returns after enqueue; grisSync() waits. A context
+ * is used by one host thread at a time. All structs below are the reference's std430
+ * layouts, byte for byte (sizes are checked at compile time in the library).
+ */
+#ifndef GRISRT_H
+#define GRISRT_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define GRIS_OK 0
+#define GRIS_ERR_INVALID_ARGUMENT (-1)
+#define GRIS_ERR_CUDA (-2)
+#define GRIS_ERR_OUT_OF_MEMORY (-3)
+#define GRIS_ERR_UNSUPPORTED (-4)
+#define GRIS_ERR_DEVICE_FAULT (-5)   /* a kernel raised its error word (e.g. a bounded wait ran out) */
+#define GRIS_ERR_TOO_LARGE (-6)
+
+/* ---------------------------------------------------------------- layouts */
+
+/* reference: Material, src/shader/layouts.glsl:6-25 (RESTIR_PT_MATERIAL = 1, 32 B).
+ * type: 1 Lambert, 2 MetallicWorkflow, 3 Metal, 4 Dielectric, 6 Fake (material.glsl:13-20). */
+typedef struct GrisMaterial {
+    float baseColor[3];
+    uint32_t type;
+    uint32_t textureIdx;     /* 0xffffffff: no texture (textures are not supported) */
+    float metallic;
+    float roughness;
+    float ior;
+} GrisMaterial;
+
+/* reference: MeshVertex, layouts.glsl:53-58 (32 B) */
+typedef struct GrisMeshVertex {
+    float pos[3];
+    float uvx;
+    float norm[3];
+    float uvy;
+} GrisMeshVertex;
+
+/* reference: ObjectInstance, layouts.glsl:60-72 (224 B). Matrices are column-major. */
+typedef struct GrisObjectInstance {
+    float transform[16];
+    float transformInv[16];
+    float transformInvT[16];
+    float radiance[3];
+    float pad0;
+    uint32_t indexOffset;
+    uint32_t indexCount;
+    uint32_t matIndex;
+    float pad2;
+} GrisObjectInstance;
+
+/* reference: TriangleLight, layouts.glsl:74-83 (64 B) */
+typedef struct GrisTriangleLight {
+    float v0[3]; float nx;
+    float v1[3]; float ny;
+    float v2[3]; float nz;
+    float radiance[3]; float area;
+} GrisTriangleLight;
+
+/* reference: LightSampleTableElement, layouts.glsl:85-88 (8 B). Entry 0 = {sumPower, count};
+ * entry i+1 = {prob, failId (1-based)} (src/util/AliasTable.h:26-71). */
+typedef struct GrisLightTableEntry {
+    float prob;
+    uint32_t failId;
+} GrisLightTableEntry;
+
+/* reference: Camera, layouts.glsl:27-51 (352 B, the camera UBO element) */
+typedef struct GrisCamera {
+    float view[16];
+    float proj[16];
+    float projView[16];
+    float lastProjView[16];
+    float pos[3]; float FOV;
+    float angle[3]; float nearZ;
+    float front[3]; float farZ;
+    float right[3]; float lensRadius;
+    float up[3]; float focalDist;
+    uint32_t filmSize[2];
+    uint32_t frameIndex;     /* bit 31: clear flag (camera.glsl:6-7) */
+    uint32_t seed;
+} GrisCamera;
+
+/* reference: Intersection, layouts.glsl:90-94 (16 B) */
+typedef struct GrisIntersection {
+    float bary[2];
+    uint32_t instanceIdx;    /* 0: light instance; 0xffffffff: miss; 0xfffffffe: primary (bary = uv) */
+    uint32_t triangleIdx;
+} GrisIntersection;
+
+/* reference: GRISPathSample + GRISReservoir, layouts.glsl:132-156 (96 B) */
+typedef struct GrisReservoir {
+    GrisIntersection rcIsec;
+    float rcLi[3]; uint32_t rcRng;
+    float rcWi[3]; uint32_t flags;   /* bits 0-7 rcVertexId, 8-15 pathLength, 16-23 rcVertexType */
+    float pad[2]; float rcPrevSamplePdf; float rcJacobian;
+    float F[3]; uint32_t primaryRng;
+    float sampleCount;
+    float resampleWeight;
+    float contribWeight;
+    float pad0;
+} GrisReservoir;
+
+/* reference: GRISReSTIR::Settings (src/GRISReSTIR.h:11-17, the 20-byte push constant) followed by
+ * the constants the reference hard-codes, as parameters (defaults = reference values). */
+typedef struct GrisSettings {
+    uint32_t shiftType;         /* 0 Reconnection, 1 Replay, 2 Hybrid (GRISReSTIR.h:9) */
+    float rrScale;              /* 1.0 */
+    uint32_t temporalReuse;     /* bool */
+    uint32_t spatialReuse;      /* bool */
+    uint32_t cap;               /* M cap, 20 */
+    uint32_t maxDepth;          /* MaxTracingDepth, gris_path_trace.glsl:46 (15) */
+    uint32_t spatialNeighbors;  /* ResampleNum, gris_resample_spatial.glsl:65 (3) */
+    float spatialRadius;        /* ResampleRadius in pixels, gris_resample_spatial.glsl:66 (20) */
+    float envRadiance[3];       /* extension: constant environment (0 = the reference: a miss ends the path) */
+    uint32_t reserved[5];
+} GrisSettings;
+
+/* Host-side scene arrays (what DeviceScene uploads, src/Scene.cpp:368-446). */
+typedef struct GrisSceneDesc {
+    const GrisMeshVertex* vertices; uint64_t vertexCount;
+    const uint32_t* indices; uint64_t indexCount;
+    const GrisObjectInstance* instances; uint64_t instanceCount;
+    const GrisMaterial* materials; uint64_t materialCount;
+    const int32_t* materialIndices; uint64_t materialIndexCount;   /* one per triangle: [indexOffset/3 + tri] */
+    const GrisTriangleLight* lights; uint64_t lightCount;
+    const GrisLightTableEntry* lightTable; uint64_t lightTableCount;  /* lightCount + 1 */
+} GrisSceneDesc;
+
+/* Device buffers of one GRISReSTIR::render call: descriptor set 2 of the reference
+ * (layouts.glsl:180-195, bound per frame by Renderer.cpp:329-347). W x H pixels, row-major. */
+typedef struct GrisPassBindings {
+    uint32_t width, height;
+    const float* depthNormal;        /* float4: depth, normal.xyz (RGBA32F) */
+    const float* depthNormalPrev;
+    const uint32_t* albedoMatId;     /* uint2: unorm4x8 albedo, matIndex<<16 | instanceIdx (RG32UI) */
+    const uint32_t* albedoMatIdPrev;
+    const uint16_t* motion;          /* half2 (RG16F) */
+    GrisReservoir* reservoirThis;
+    const GrisReservoir* reservoirPrev;
+    GrisReservoir* reservoirTemp;
+    float* output;                   /* float4 RGBA32F, running mean (indirect output) */
+} GrisPassBindings;
+
+/* Device buffers written by the G-buffer pass (GBufferPass.h:23-26 formats). */
+typedef struct GrisGBufferBindings {
+    uint32_t width, height;
+    float* depthNormal;
+    uint32_t* albedoMatId;
+    uint16_t* motion;
+} GrisGBufferBindings;
+
+typedef struct GrisSceneStats {
+    uint64_t triangleCount;          /* light + object triangles in the BVH */
+    uint64_t nodeCount;              /* 8-wide nodes (80 B each) */
+    uint64_t nodeBytes, triangleBytes;
+    uint32_t maxDepth;               /* deepest 8-wide level */
+    uint32_t reserved;
+    double buildSeconds;
+} GrisSceneStats;
+
+/* Ray counters (device-side, exact): index 0 closest-hit rays, 1 shadow/visibility rays,
+ * 2 G-buffer primary rays, 3 error word (0 = none). */
+#define GRIS_COUNTER_CLOSEST 0
+#define GRIS_COUNTER_SHADOW 1
+#define GRIS_COUNTER_PRIMARY 2
+#define GRIS_COUNTER_ERROR 3
+
+typedef struct GrisContext GrisContext;
+typedef struct GrisScene GrisScene;
+typedef struct GrisFrame GrisFrame;
+typedef struct GrisHostScene GrisHostScene;
+
+/* ---------------------------------------------------------------- context */
+int grisCreate(int device, GrisContext** out);
+int grisDestroy(GrisContext* ctx);
+const char* grisGetError(const GrisContext* ctx);
+int grisSync(GrisContext* ctx);
+void* grisGetStream(GrisContext* ctx);                    /* cudaStream_t */
+int grisReadCounters(GrisContext* ctx, uint64_t out[4], int reset);
+int grisGetVersion(void);
+size_t grisSizeof(int which);   /* 0 camera, 1 reservoir, 2 material, 3 vertex, 4 instance, 5 light, 6 table entry, 7 settings */
+
+/* ---------------------------------------------------------------- host helpers (no GPU) */
+/* reference: DiscreteSampler1D::build, src/util/AliasTable.h:26-71 (table of n+1 entries). */
+int grisBuildLightTable(const float* distribution, uint32_t n, GrisLightTableEntry* out);
+/* reference: Camera::update (src/Camera.cpp:78-98) + the per-frame fields; angle in degrees
+ * (yaw, pitch, roll), FOV in degrees; frameIndex = 0, seed = 0, lastProjView = projView. */
+int grisCameraSetup(GrisCamera* cam, const float pos[3], const float angle[3], float fovDeg,
+                    uint32_t width, uint32_t height);
+/* reference: Camera::setDir (src/Camera.cpp:39-48) then update(). */
+int grisCameraLookAt(GrisCamera* cam, const float pos[3], const float target[3], float fovDeg,
+                     uint32_t width, uint32_t height);
+/* Synthetic scenes. kind 0: closed box of 12 quads + ceiling quad light (radiance 15, 1/16 of the
+ * ceiling area), Lambertian walls with albedo ~ U[0.2,0.8]^3; kind 1: fBm heightfield (gridN x gridN
+ * vertices) + `spheres` instanced icospheres (subdivision 2) with radii log-uniform [0.1, 2], GGX
+ * MetallicWorkflow materials, 4 quad lights; kind 2: glossy variant of kind 1 (roughness U[0.02,0.3],
+ * 70% metallic, occluders over the lights). The camera for frame f of the scene's orbit comes from
+ * grisHostSceneCamera. */
+int grisHostSceneCreate(int kind, uint64_t seed, uint32_t gridN, uint32_t spheres, GrisHostScene** out);
+int grisHostSceneDesc(const GrisHostScene* hs, GrisSceneDesc* out);
+int grisHostSceneCamera(const GrisHostScene* hs, uint32_t frame, uint32_t frames, uint32_t width,
+                        uint32_t height, GrisCamera* out);
+int grisHostSceneDestroy(GrisHostScene* hs);
+
+/* ---------------------------------------------------------------- scene */
+/* Copies the arrays to the device and builds the 8-wide BVH over lights (instance 0) and every
+ * instance's world-space triangles. */
+int grisSceneCreate(GrisContext* ctx, const GrisSceneDesc* desc, GrisScene** out);
+int grisSceneDestroy(GrisScene* scene);
+int grisSceneGetStats(const GrisScene* scene, GrisSceneStats* out);
+/* Builder check: closest-hit / any-hit of n rays (float[8] each: org.xyz, tmin, dir.xyz, tmax)
+ * through the BVH on the host or on the device (dev pointers). hits: float[4] per ray
+ * {t, u, v, bitcast instanceIdx} and uint triangleIdx in a second array. anyHit != 0: shadow query. */
+/* Builder check without a GPU: builds the BVH on the host only (no context, no upload); the
+ * result serves grisDebugTraceHost / grisSceneGetStats and is freed by grisSceneDestroy. */
+int grisDebugHostSceneCreate(const GrisSceneDesc* desc, GrisScene** out);
+int grisDebugTraceHost(const GrisScene* scene, const float* rays, uint64_t n, int anyHit,
+                       float* hitTUV, uint32_t* hitInst, uint32_t* hitTri);
+int grisDebugTraceDevice(GrisContext* ctx, const GrisScene* scene, const float* dRays, uint64_t n,
+                         int anyHit, float* dHitTUV, uint32_t* dHitInst, uint32_t* dHitTri);
+
+/* ---------------------------------------------------------------- passes on caller buffers */
+int grisPassGBuffer(GrisContext* ctx, const GrisScene* scene, const GrisGBufferBindings* b,
+                    const GrisCamera* cam);
+/* GRISReSTIR::render: path trace -> temporal reuse -> spatial reuse + final shading. passes:
+ * bit 0 path trace, bit 1 temporal, bit 2 spatial (7 = the full pass). */
+int grisPassRender(GrisContext* ctx, const GrisScene* scene, const GrisPassBindings* b,
+                   const GrisCamera* cam, const GrisCamera* prevCam, const GrisSettings* settings,
+                   int passes);
+
+/* ---------------------------------------------------------------- frames (library-owned buffers) */
+/* G-buffer cur/prev, reservoirs This[2]/Temp, output: the renderer's per-frame resources
+ * (src/Renderer.cpp:193-257) with its ping-pong (Renderer.cpp:329-347, 567). */
+int grisFrameCreate(GrisContext* ctx, uint32_t width, uint32_t height, GrisFrame** out);
+int grisFrameDestroy(GrisFrame* frame);
+/* G-buffer into the current slot, then GRISReSTIR::render on the current slot, then swap. */
+int grisFrameRender(GrisContext* ctx, const GrisScene* scene, GrisFrame* frame, const GrisCamera* cam,
+                    const GrisCamera* prevCam, const GrisSettings* settings);
+/* which: 0 depthNormal, 1 albedoMatId, 2 motion, 3 reservoir, 4 temp reservoir, 5 output.
+ * slot: 0 = the slot the last grisFrameRender wrote (current), 1 = the other one. */
+int grisFrameGetBuffer(const GrisFrame* frame, int which, int slot, void** devPtr, size_t* bytes);
+int grisFrameDownload(GrisContext* ctx, const GrisFrame* frame, int which, int slot, void* host, size_t bytes);
+int grisFrameUpload(GrisContext* ctx, GrisFrame* frame, int which, int slot, const void* host, size_t bytes);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif

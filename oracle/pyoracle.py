@@ -1,0 +1,117 @@
+"""Python driver of the CPU oracle (oracle/_build/liboracle.so) and of the compiled reference
+shaders (oracle/_ref/libgrisref.so).
+
+TEST INFRASTRUCTURE: only tests/, __graft_entry__.smoke() and bench.py's CPU legs import it.
+
+Both libraries expose the same entry points (prefix `oracle_` / `gref_`); `run_sequence`
+replays the renderer's frame loop (src/Renderer.cpp:329-347 ping-pong, 539-569 draw order):
+G-buffer into slot j, GRISReSTIR::render with This = R[j], Prev = R[j^1], then j ^= 1.
+All frame buffers start zeroed, as on the GPU side.
+"""
+import ctypes
+import os
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ORACLE_LIB = os.path.join(HERE, "_build", "liboracle.so")
+REF_LIB = os.path.join(HERE, "_ref", "libgrisref.so")
+
+
+class CpuImpl:
+    def __init__(self, path, prefix):
+        if not os.path.exists(path):
+            raise FileNotFoundError(path)
+        self.lib = ctypes.CDLL(path)
+        self.prefix = prefix
+        vp, u64 = ctypes.c_void_p, ctypes.c_ulonglong
+        self._fn("scene_set", ctypes.c_int, [vp, u64] * 7)
+        self._fn("gbuffer", None, [vp, ctypes.c_uint32, ctypes.c_uint32, vp, vp, vp])
+        self._fn("gris_frame", None, [vp] * 12 + [ctypes.c_int])
+        self._fn("counters", None, [vp, ctypes.c_int])
+        self._fn("trace", None, [vp, u64, ctypes.c_int, vp, vp, vp])
+        self._fn("sizeof", ctypes.c_int, [ctypes.c_int])
+        self._arrays = None
+
+    def _fn(self, name, res, args):
+        f = getattr(self.lib, self.prefix + name)
+        f.restype, f.argtypes = res, args
+        setattr(self, name, f)
+
+    def set_scene(self, host_scene):
+        arrs = [np.ascontiguousarray(a) for a in host_scene.arrays()]
+        self._arrays = arrs   # keep alive (the reference harness binds the arrays in place)
+        args = []
+        for a in arrs:
+            args += [a.ctypes.data, len(a)]
+        return self.scene_set(*args)
+
+    def set_traversal(self, use_bvh):
+        f = getattr(self.lib, self.prefix + "set_traversal", None)
+        if f is not None:
+            f.argtypes = [ctypes.c_int]
+            f(int(use_bvh))
+
+    def read_counters(self, reset=True):
+        out = (ctypes.c_ulonglong * 4)()
+        self.counters(out, int(reset))
+        return list(out)
+
+    def trace_rays(self, rays, any_hit=False):
+        rays = np.ascontiguousarray(rays, dtype=np.float32).reshape(-1, 8)
+        n = len(rays)
+        tuv = np.zeros((n, 4), np.float32)
+        inst = np.zeros(n, np.uint32)
+        tri = np.zeros(n, np.uint32)
+        self.trace(rays.ctypes.data, n, int(any_hit), tuv.ctypes.data, inst.ctypes.data, tri.ctypes.data)
+        return tuv, inst, tri
+
+
+def oracle():
+    return CpuImpl(ORACLE_LIB, "oracle_")
+
+
+def reference():
+    return CpuImpl(REF_LIB, "gref_")
+
+
+def _p(a):
+    return ctypes.c_void_p(a.ctypes.data)
+
+
+def run_sequence(impl, cams, prevs, settings, width, height, frames=None, record=("resv", "temp", "out", "dn", "am", "mv")):
+    """Runs len(cams) frames; returns a list of dicts of per-frame buffer copies."""
+    from grisrt import RESERVOIR
+    n = width * height
+    dn = [np.zeros((n, 4), np.float32) for _ in range(2)]
+    am = [np.zeros((n, 2), np.uint32) for _ in range(2)]
+    mv = np.zeros((n, 2), np.uint16)
+    resv = [np.zeros(n, RESERVOIR) for _ in range(2)]
+    temp = np.zeros(n, RESERVOIR)
+    out = np.zeros((n, 4), np.float32)
+    sbytes = bytes(memoryview(settings))
+    sbuf = np.frombuffer(sbytes, dtype=np.uint8).copy()
+    results = []
+    j = 0
+    for f in range(len(cams)):
+        cb = np.frombuffer(cams[f].tobytes(), np.uint8).copy()
+        pb = np.frombuffer(prevs[f].tobytes(), np.uint8).copy()
+        impl.gbuffer(_p(cb), width, height, _p(dn[j]), _p(am[j]), _p(mv))
+        impl.gris_frame(_p(cb), _p(pb), _p(sbuf), _p(dn[j]), _p(dn[j ^ 1]), _p(am[j]), _p(am[j ^ 1]), _p(mv),
+                        _p(resv[j]), _p(resv[j ^ 1]), _p(temp), _p(out), 7)
+        rec = {}
+        if "resv" in record:
+            rec["resv"] = resv[j].copy()
+        if "temp" in record:
+            rec["temp"] = temp.copy()
+        if "out" in record:
+            rec["out"] = out.copy()
+        if "dn" in record:
+            rec["dn"] = dn[j].copy()
+        if "am" in record:
+            rec["am"] = am[j].copy()
+        if "mv" in record:
+            rec["mv"] = mv.copy()
+        results.append(rec)
+        j ^= 1
+    return results

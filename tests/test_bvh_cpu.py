@@ -1,0 +1,84 @@
+"""The 8-wide BVH on the host (same traversal code as the kernels) against the oracle's
+brute-force ray queries: closest hits must match bit for bit, any-hit booleans exactly."""
+import numpy as np
+import pytest
+
+import grisrt as G
+from oracle import pyoracle
+
+
+def _rays(scene, n, seed, mode):
+    rng = np.random.default_rng(seed)
+    v = scene.vertices["pos"]
+    lo, hi = v.min(0) - 1.0, v.max(0) + 1.0
+    if scene.instances.size:
+        t = scene.instances["transform"][:, 12:15]
+        lo, hi = np.minimum(lo, t.min(0) - 2), np.maximum(hi, t.max(0) + 2)
+    o = rng.uniform(lo, hi, (n, 3))
+    d = rng.normal(size=(n, 3))
+    if mode == "axis":
+        k = rng.integers(0, 3, n)
+        d[:] = 0
+        d[np.arange(n), k] = rng.choice([-1.0, 1.0], n)
+    elif mode == "grazing":
+        d[:, 2] *= 1e-3
+    d /= np.linalg.norm(d, axis=1, keepdims=True)
+    rays = np.zeros((n, 8), np.float32)
+    rays[:, 0:3], rays[:, 3], rays[:, 4:7], rays[:, 7] = o, 1e-4, d, 1e7
+    if mode == "short":
+        rays[:, 7] = rng.uniform(0.0, 3.0, n)
+    return rays
+
+
+@pytest.fixture(scope="module")
+def oracle_bf():
+    return pyoracle.oracle()
+
+
+@pytest.mark.parametrize("kind,grid,spheres", [(0, 0, 0), (1, 48, 60), (2, 40, 40)])
+@pytest.mark.parametrize("mode", ["random", "axis", "grazing", "short"])
+def test_bvh_closest_and_any_hit_match_brute_force(kind, grid, spheres, mode, oracle_bf):
+    hs = G.HostScene(kind, seed=3, grid=grid, spheres=spheres)
+    bvh = G.load()
+    # build the BVH without a device: the host trace entry point needs only the host copy,
+    # but grisSceneCreate uploads; emulate by building through a context only when possible
+    scene = _host_scene(hs)
+    oracle_bf.set_scene(hs)
+    oracle_bf.set_traversal(False)
+    rays = _rays(hs, 4000, 11 + kind, mode)
+    t1, i1, r1 = scene.trace_host(rays)
+    t2, i2, r2 = oracle_bf.trace_rays(rays)
+    assert np.array_equal(i1, i2) and np.array_equal(r1, r2)
+    assert t1.tobytes() == t2.tobytes()
+    a1, _, _ = scene.trace_host(rays, any_hit=True)
+    a2, _, _ = oracle_bf.trace_rays(rays, any_hit=True)
+    assert np.array_equal(a1[:, 0] > 0, a2[:, 0] > 0)
+    # the oracle's own binary BVH (used for CPU timing) agrees too
+    oracle_bf.set_traversal(True)
+    t3, i3, r3 = oracle_bf.trace_rays(rays)
+    oracle_bf.set_traversal(False)
+    assert np.array_equal(i3, i2) and t3.tobytes() == t2.tobytes()
+
+
+class _HostOnlyScene:
+    """BVH built by the library's host builder, traced on the host (no GPU needed)."""
+
+    def __init__(self, hs):
+        import ctypes
+        lib = G.load()
+        self._lib = lib
+        self._desc = hs.desc()
+        h = ctypes.c_void_p()
+        rc = lib.grisDebugHostSceneCreate(ctypes.byref(self._desc), ctypes.byref(h))
+        assert rc == 0
+        self.h = h
+
+    def trace_host(self, rays, any_hit=False):
+        return G.Scene.trace_host(self, rays, any_hit)
+
+    def __del__(self):
+        self._lib.grisSceneDestroy(self.h)
+
+
+def _host_scene(hs):
+    return _HostOnlyScene(hs)

@@ -1,0 +1,158 @@
+"""GPU parity: the CUDA path through the C ABI against the oracle, bit for bit (reservoir
+selections, M, weights, G-buffer, output radiance, ray counts)."""
+import ctypes
+
+import numpy as np
+import pytest
+
+import grisrt as G
+from oracle import pyoracle as O
+
+pytestmark = pytest.mark.gpu
+
+CASES = [
+    ("box_config1", 0, 0, 0, 64, 48, 8, dict(maxDepth=3, spatialRadius=30.0)),
+    ("box_reference_defaults", 0, 0, 0, 40, 40, 3, dict()),
+    ("box_reconnection", 0, 0, 0, 32, 24, 3, dict(shiftType=0, maxDepth=6)),
+    ("box_no_temporal", 0, 0, 0, 24, 24, 3, dict(temporalReuse=False, maxDepth=4)),
+    ("box_no_spatial_cap5", 0, 0, 0, 24, 24, 4, dict(spatialReuse=False, cap=5, maxDepth=4)),
+    ("terrain_depth8", 1, 48, 60, 48, 40, 4, dict(maxDepth=8, spatialRadius=30.0)),
+    ("glossy_depth8", 2, 48, 60, 48, 40, 4, dict(maxDepth=8, spatialRadius=30.0)),
+    ("glossy_rr", 2, 24, 30, 32, 24, 3, dict(maxDepth=12, rrScale=0.5, spatialNeighbors=5)),
+    ("odd_size", 1, 32, 20, 37, 23, 3, dict(maxDepth=5)),
+]
+
+
+@pytest.fixture(scope="module")
+def ctx():
+    c = G.Context(0)
+    yield c
+    c.close()
+
+
+@pytest.fixture(scope="module")
+def ora():
+    return O.oracle()
+
+
+def gpu_sequence(ctx, hs, cams, prevs, st, W, H):
+    scene = G.Scene(ctx, hs)
+    fr = G.Frame(ctx, W, H)
+    ctx.counters(reset=True)
+    out = []
+    for f in range(len(cams)):
+        fr.render(scene, cams[f], prevs[f], st)
+        out.append({"resv": fr.download(G.BUF_RESERVOIR), "temp": fr.download(G.BUF_TEMP),
+                    "out": fr.download(G.BUF_OUTPUT), "dn": fr.download(G.BUF_DEPTH_NORMAL),
+                    "am": fr.download(G.BUF_ALBEDO_MATID), "mv": fr.download(G.BUF_MOTION)})
+    ctx.sync()
+    counters = ctx.counters(reset=True)
+    fr.close()
+    scene.close()
+    return out, counters
+
+
+@pytest.mark.parametrize("case", CASES, ids=[c[0] for c in CASES])
+def test_gpu_matches_oracle_bit_exact(case, ctx, ora):
+    name, kind, grid, spheres, W, H, frames, kw = case
+    hs = G.HostScene(kind, seed=2, grid=grid, spheres=spheres)
+    cams, prevs = G.sequence_cameras(hs, frames, W, H, seed=11)
+    st = G.Settings.make(**kw)
+    got, gc = gpu_sequence(ctx, hs, cams, prevs, st, W, H)
+    ora.set_scene(hs)
+    ora.read_counters(reset=True)
+    want = O.run_sequence(ora, cams, prevs, st, W, H)
+    oc = ora.read_counters()
+    for f in range(frames):
+        for k in ("dn", "am", "mv", "resv", "temp", "out"):
+            g, w = got[f][k], want[f][k]
+            if g.tobytes() != w.tobytes():
+                gv = g.view(np.uint32).reshape(len(g), -1)
+                wv = w.view(np.uint32).reshape(len(w), -1)
+                bad = np.nonzero((gv != wv).any(1))[0]
+                pytest.fail("%s: frame %d buffer %s differs at %d pixels, first %s:\n gpu %s\n oracle %s" % (
+                    name, f, k, len(bad), bad[:8], g[bad[0]], w[bad[0]]))
+    assert gc[0] == oc[0] and gc[1] == oc[1] and gc[2] == oc[2], (gc, oc)
+    assert gc[3] == 0
+
+
+def test_device_traversal_matches_host(ctx):
+    hs = G.HostScene(1, seed=4, grid=64, spheres=100)
+    scene = G.Scene(ctx, hs)
+    rng = np.random.default_rng(5)
+    n = 50000
+    rays = np.zeros((n, 8), np.float32)
+    rays[:, 0:3] = rng.uniform([-55, -55, -5], [55, 55, 25], (n, 3))
+    d = rng.normal(size=(n, 3))
+    rays[:, 4:7] = d / np.linalg.norm(d, axis=1, keepdims=True)
+    rays[:, 3], rays[:, 7] = 1e-4, 1e7
+    import torch
+    dr = torch.from_numpy(rays).cuda()
+    tuv = torch.zeros((n, 4), dtype=torch.float32, device="cuda")
+    inst = torch.zeros(n, dtype=torch.int32, device="cuda")
+    tri = torch.zeros(n, dtype=torch.int32, device="cuda")
+    for any_hit in (0, 1):
+        torch.cuda.synchronize()
+        ctx.check(G.load().grisDebugTraceDevice(ctx.h, scene.h, dr.data_ptr(), n, any_hit, tuv.data_ptr(),
+                                                inst.data_ptr(), tri.data_ptr()), "grisDebugTraceDevice")
+        ctx.sync()
+        h_tuv, h_inst, h_tri = scene.trace_host(rays, any_hit=bool(any_hit))
+        if any_hit:
+            assert np.array_equal(tuv[:, 0].cpu().numpy() > 0, h_tuv[:, 0] > 0)
+        else:
+            assert np.array_equal(inst.cpu().numpy().view(np.uint32), h_inst)
+            assert np.array_equal(tri.cpu().numpy().view(np.uint32), h_tri)
+            assert tuv.cpu().numpy().tobytes() == h_tuv.tobytes()
+    scene.close()
+
+
+def test_pass_bindings_api_matches_frame_api(ctx, ora):
+    """grisPassGBuffer + grisPassRender on caller-owned device buffers (the descriptor-set form)."""
+    import torch
+    W, H, frames = 40, 32, 3
+    hs = G.HostScene(0, seed=3)
+    cams, prevs = G.sequence_cameras(hs, frames, W, H, seed=5)
+    st = G.Settings.make(maxDepth=4, spatialRadius=30.0)
+    scene = G.Scene(ctx, hs)
+    n = W * H
+    dn = [torch.zeros((n, 4), dtype=torch.float32, device="cuda") for _ in range(2)]
+    am = [torch.zeros((n, 2), dtype=torch.int32, device="cuda") for _ in range(2)]
+    mv = torch.zeros((n, 2), dtype=torch.int16, device="cuda")
+    resv = [torch.zeros((n, 24), dtype=torch.int32, device="cuda") for _ in range(2)]
+    temp = torch.zeros((n, 24), dtype=torch.int32, device="cuda")
+    out = torch.zeros((n, 4), dtype=torch.float32, device="cuda")
+    torch.cuda.synchronize()
+    lib = G.load()
+    want = O.run_sequence(ora if ora.set_scene(hs) else ora, cams, prevs, st, W, H, record=("resv", "out"))
+    j = 0
+    for f in range(frames):
+        gb = G.GBufferBindings(W, H, dn[j].data_ptr(), am[j].data_ptr(), mv.data_ptr())
+        ctx.check(lib.grisPassGBuffer(ctx.h, scene.h, ctypes.byref(gb), ctypes.byref(cams[f])), "grisPassGBuffer")
+        b = G.PassBindings(W, H, dn[j].data_ptr(), dn[j ^ 1].data_ptr(), am[j].data_ptr(), am[j ^ 1].data_ptr(),
+                           mv.data_ptr(), resv[j].data_ptr(), resv[j ^ 1].data_ptr(), temp.data_ptr(), out.data_ptr())
+        ctx.check(lib.grisPassRender(ctx.h, scene.h, ctypes.byref(b), ctypes.byref(cams[f]), ctypes.byref(prevs[f]),
+                                     ctypes.byref(st), 7), "grisPassRender")
+        ctx.sync()
+        assert resv[j].cpu().numpy().tobytes() == want[f]["resv"].tobytes()
+        assert out.cpu().numpy().tobytes() == want[f]["out"].tobytes()
+        j ^= 1
+    scene.close()
+
+
+def test_invalid_arguments_are_rejected(ctx):
+    lib = G.load()
+    hs = G.HostScene(0, seed=1)
+    scene = G.Scene(ctx, hs)
+    cam = hs.camera(0, 1, 16, 16)
+    st = G.Settings.make()
+    b = G.PassBindings()
+    b.width, b.height = 16, 16
+    assert lib.grisPassRender(ctx.h, scene.h, ctypes.byref(b), ctypes.byref(cam), ctypes.byref(cam), ctypes.byref(st), 7) == -1
+    st.maxDepth = 0
+    assert lib.grisFrameRender(ctx.h, scene.h, None, ctypes.byref(cam), ctypes.byref(cam), ctypes.byref(st)) == -1
+    bad = G.HostScene(0, seed=1)
+    bad.materials["textureIdx"][0] = 3
+    h = ctypes.c_void_p()
+    d = bad.desc()
+    assert lib.grisSceneCreate(ctx.h, ctypes.byref(d), ctypes.byref(h)) == -4
+    scene.close()

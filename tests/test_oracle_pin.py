@@ -1,0 +1,47 @@
+"""Pins the oracle restatement against the reference's own shader code compiled as C++
+(oracle/_ref): every buffer of every frame must be bit-identical. Runs where the
+reference sources were available to build oracle/_ref (skipped elsewhere)."""
+import numpy as np
+import pytest
+
+import grisrt as G
+from oracle import pyoracle as O
+
+CASES = [
+    # (name, kind, grid, spheres, W, H, frames, settings kwargs)
+    ("box_config1", 0, 0, 0, 48, 40, 5, dict(maxDepth=3, spatialRadius=30.0)),
+    ("box_reference_defaults", 0, 0, 0, 32, 32, 3, dict()),
+    ("box_reconnection", 0, 0, 0, 32, 24, 3, dict(shiftType=0, maxDepth=6)),
+    ("box_no_temporal", 0, 0, 0, 24, 24, 3, dict(temporalReuse=False, maxDepth=4)),
+    ("box_no_spatial_cap5", 0, 0, 0, 24, 24, 4, dict(spatialReuse=False, cap=5, maxDepth=4)),
+    ("terrain_depth8", 1, 40, 40, 40, 32, 3, dict(maxDepth=8, spatialRadius=30.0)),
+    ("glossy_depth8", 2, 40, 40, 40, 32, 3, dict(maxDepth=8, spatialRadius=30.0)),
+    ("glossy_rr", 2, 24, 30, 32, 24, 3, dict(maxDepth=12, rrScale=0.5, spatialNeighbors=5)),
+]
+
+
+@pytest.fixture(scope="module")
+def impls(ref_available):
+    if not ref_available:
+        pytest.skip("oracle/_ref not built (reference sources absent)")
+    return O.reference(), O.oracle()
+
+
+@pytest.mark.parametrize("case", CASES, ids=[c[0] for c in CASES])
+def test_oracle_matches_compiled_reference(case, impls):
+    name, kind, grid, spheres, W, H, frames, kw = case
+    ref, ora = impls
+    hs = G.HostScene(kind, seed=2, grid=grid, spheres=spheres)
+    cams, prevs = G.sequence_cameras(hs, frames, W, H, seed=11)
+    st = G.Settings.make(**kw)
+    for impl in impls:
+        impl.set_scene(hs)
+        impl.read_counters(reset=True)
+    a = O.run_sequence(ref, cams, prevs, st, W, H)
+    ca = ref.read_counters()
+    b = O.run_sequence(ora, cams, prevs, st, W, H)
+    cb = ora.read_counters()
+    for f in range(frames):
+        for k in a[f]:
+            assert a[f][k].tobytes() == b[f][k].tobytes(), "frame %d buffer %s differs" % (f, k)
+    assert ca[:3] == cb[:3]

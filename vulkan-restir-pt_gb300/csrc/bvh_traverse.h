@@ -1,0 +1,246 @@
+/*
+ * bvh_traverse.h — 8-wide compressed BVH layout and traversal (closest hit / any hit).
+ *
+ * Replaces the reference's hardware ray queries (src/shader/ray_query.glsl:6-70:
+ * traceClosestHit, traceShadow) with a software walk of a compressed wide BVH in the form
+ * published by Ylitie, Karras & Laine, "Efficient Incoherent Ray Traversal on GPUs Through
+ * Compressed Wide BVHs", HPG 2017 — 80-byte nodes holding 8 child boxes quantised to 8 bits
+ * per plane against a per-node origin and power-of-two scale, child slots ordered so that
+ * visiting slot (position XOR ray octant) is approximately near-to-far.
+ *
+ * Node = 20 x u32:
+ *   [0..2]  origin p (float)       [3] ex | ey<<8 | ez<<16 | imask<<24   (scale = 2^(e-127))
+ *   [4]     first child node       [5] first triangle
+ *   [6..7]  meta[8]: 0 empty; 0x80|rank (internal child, rank among internal slots);
+ *           0x80 | count<<5 | offset (leaf child: `count` triangles from first+offset)
+ *   [8..19] qlo_x[8] qlo_y[8] qlo_z[8] qhi_x[8] qhi_y[8] qhi_z[8] (bytes)
+ * Triangle = 12 x f32: v0.xyz, instanceIdx | e1.xyz, triangleIdx | e2.xyz, 0  (e = v - v0).
+ *
+ * Hit semantics (the same everywhere in this project): Moller-Trumbore, two-sided, hits with t
+ * in [tmin, tmax]; the closest hit is the smallest t, ties broken by the smaller
+ * (instanceIdx, triangleIdx). Box tests only decide what is visited; boxes are padded and
+ * rounded outward at build time so that every triangle the test would accept is reached.
+ */
+#ifndef GRISRT_BVH_TRAVERSE_H
+#define GRISRT_BVH_TRAVERSE_H
+
+#include <stdint.h>
+
+#ifdef __CUDACC__
+#define GRIS_HD __host__ __device__ __forceinline__
+#else
+#define GRIS_HD static inline
+#endif
+
+#define GRIS_BVH_STACK 64
+#define GRIS_NODE_WORDS 20
+#define GRIS_TRI_FLOATS 12
+#define GRIS_INVALID_HIT 0xffffffffu
+
+struct GrisRayHit {
+    float t, u, v;
+    uint32_t inst, tri;
+};
+
+GRIS_HD float gris_fma(float a, float b, float c) {
+#ifdef __CUDA_ARCH__
+    return __fmaf_rn(a, b, c);
+#else
+    return __builtin_fmaf(a, b, c);
+#endif
+}
+GRIS_HD float gris_fmin(float a, float b) {
+#ifdef __CUDA_ARCH__
+    return fminf(a, b);
+#else
+    return __builtin_fminf(a, b);
+#endif
+}
+GRIS_HD float gris_fmax(float a, float b) {
+#ifdef __CUDA_ARCH__
+    return fmaxf(a, b);
+#else
+    return __builtin_fmaxf(a, b);
+#endif
+}
+GRIS_HD float gris_u2f(uint32_t u) {
+#ifdef __CUDA_ARCH__
+    return __uint_as_float(u);
+#else
+    union { uint32_t u; float f; } c; c.u = u; return c.f;
+#endif
+}
+GRIS_HD uint32_t gris_f2u(float f) {
+#ifdef __CUDA_ARCH__
+    return __float_as_uint(f);
+#else
+    union { uint32_t u; float f; } c; c.f = f; return c.u;
+#endif
+}
+GRIS_HD int gris_popc(uint32_t x) {
+#ifdef __CUDA_ARCH__
+    return __popc(x);
+#else
+    return __builtin_popcount(x);
+#endif
+}
+GRIS_HD int gris_ffs(uint32_t x) {   /* index of the lowest set bit; x != 0 */
+#ifdef __CUDA_ARCH__
+    return __ffs(x) - 1;
+#else
+    return __builtin_ctz(x);
+#endif
+}
+
+/* The project's ray/triangle test (exact IEEE sequence; no fused operations). */
+GRIS_HD bool gris_tri_test(const float* T, float ox, float oy, float oz, float dx, float dy, float dz,
+                           float tmin, float tmax, float* tOut, float* uOut, float* vOut) {
+    float e1x = T[4], e1y = T[5], e1z = T[6];
+    float e2x = T[8], e2y = T[9], e2z = T[10];
+    float pvx = dy * e2z - dz * e2y, pvy = dz * e2x - dx * e2z, pvz = dx * e2y - dy * e2x;
+    float det = (e1x * pvx + e1y * pvy) + e1z * pvz;
+    if (det == 0.0f) return false;
+    float inv = 1.0f / det;
+    float tvx = ox - T[0], tvy = oy - T[1], tvz = oz - T[2];
+    float u = ((tvx * pvx + tvy * pvy) + tvz * pvz) * inv;
+    if (!(u >= 0.0f) || !(u <= 1.0f)) return false;
+    float qvx = tvy * e1z - tvz * e1y, qvy = tvz * e1x - tvx * e1z, qvz = tvx * e1y - tvy * e1x;
+    float v = ((dx * qvx + dy * qvy) + dz * qvz) * inv;
+    if (!(v >= 0.0f) || !(u + v <= 1.0f)) return false;
+    float t = ((e2x * qvx + e2y * qvy) + e2z * qvz) * inv;
+    if (!(t >= tmin) || !(t <= tmax)) return false;
+    *tOut = t; *uOut = u; *vOut = v;
+    return true;
+}
+
+GRIS_HD uint32_t gris_byte(uint32_t w, int i) { return (w >> (i * 8)) & 0xffu; }
+
+/*
+ * Walks the BVH. ANY: return at the first accepted hit (shadow rays). skipInst0: ignore the
+ * light instance (the G-buffer is rasterised without lights). Returns true if a hit was
+ * found; `hit` receives the closest one. *err is set to 1 if the stack limit was reached (the
+ * builder guarantees it is not: tree depth <= GRIS_BVH_STACK).
+ */
+template <bool ANY>
+GRIS_HD bool gris_bvh_trace(const uint32_t* __restrict__ nodes, const float* __restrict__ tris,
+                            float ox, float oy, float oz, float dx, float dy, float dz,
+                            float tmin, float tmax, bool skipInst0, GrisRayHit* hit, int* err,
+                            uint32_t* nodeVisits) {
+    const float tiny = 1e-30f;
+    float idx = 1.0f / ((dx > tiny || dx < -tiny) ? dx : (dx < 0.0f ? -tiny : tiny));
+    float idy = 1.0f / ((dy > tiny || dy < -tiny) ? dy : (dy < 0.0f ? -tiny : tiny));
+    float idz = 1.0f / ((dz > tiny || dz < -tiny) ? dz : (dz < 0.0f ? -tiny : tiny));
+    uint32_t oct = (dx < 0.0f ? 1u : 0u) | (dy < 0.0f ? 2u : 0u) | (dz < 0.0f ? 4u : 0u);
+    float bestT = tmax;
+    uint32_t bestInst = GRIS_INVALID_HIT, bestTri = GRIS_INVALID_HIT;
+    float bestU = 0.0f, bestV = 0.0f;
+    bool found = false;
+
+    uint32_t stackBase[GRIS_BVH_STACK];
+    uint32_t stackBits[GRIS_BVH_STACK];
+    int sp = 0;
+    uint32_t grpBase = 0, grpHits = 0, grpImask = 0;
+    uint32_t nodeIdx = 0;
+    bool haveNode = true;
+    uint32_t visits = 0;
+
+    while (true) {
+        if (haveNode) {
+            const uint32_t* N = nodes + (uint64_t)nodeIdx * GRIS_NODE_WORDS;
+#ifdef __CUDA_ARCH__
+            uint4 w0 = __ldg(reinterpret_cast<const uint4*>(N) + 0);
+            uint4 w1 = __ldg(reinterpret_cast<const uint4*>(N) + 1);
+            uint4 w2 = __ldg(reinterpret_cast<const uint4*>(N) + 2);
+            uint4 w3 = __ldg(reinterpret_cast<const uint4*>(N) + 3);
+            uint4 w4 = __ldg(reinterpret_cast<const uint4*>(N) + 4);
+            uint32_t W[20] = {w0.x, w0.y, w0.z, w0.w, w1.x, w1.y, w1.z, w1.w, w2.x, w2.y,
+                              w2.z, w2.w, w3.x, w3.y, w3.z, w3.w, w4.x, w4.y, w4.z, w4.w};
+#else
+            uint32_t W[20];
+            for (int i = 0; i < 20; i++) W[i] = N[i];
+#endif
+            visits++;
+            float px = gris_u2f(W[0]), py = gris_u2f(W[1]), pz = gris_u2f(W[2]);
+            uint32_t e = W[3];
+            float sx = gris_u2f((e & 0xffu) << 23), sy = gris_u2f(((e >> 8) & 0xffu) << 23),
+                  sz = gris_u2f(((e >> 16) & 0xffu) << 23);
+            uint32_t imask = e >> 24;
+            float ax = sx * idx, ay = sy * idy, az = sz * idz;
+            float bx = (px - ox) * idx, by = (py - oy) * idy, bz = (pz - oz) * idz;
+            uint32_t innerHits = 0, triHits = 0;
+#pragma unroll
+            for (int s = 0; s < 8; s++) {
+                uint32_t meta = gris_byte(W[6 + (s >> 2)], s & 3);
+                if (meta == 0) continue;
+                int wi = s >> 2, bi = s & 3;
+                float lx = gris_fma((float)gris_byte(W[8 + wi], bi), ax, bx);
+                float ly = gris_fma((float)gris_byte(W[10 + wi], bi), ay, by);
+                float lz = gris_fma((float)gris_byte(W[12 + wi], bi), az, bz);
+                float hx = gris_fma((float)gris_byte(W[14 + wi], bi), ax, bx);
+                float hy = gris_fma((float)gris_byte(W[16 + wi], bi), ay, by);
+                float hz = gris_fma((float)gris_byte(W[18 + wi], bi), az, bz);
+                float tn = gris_fmax(gris_fmax(gris_fmin(lx, hx), gris_fmin(ly, hy)), gris_fmax(gris_fmin(lz, hz), tmin));
+                float tf = gris_fmin(gris_fmin(gris_fmax(lx, hx), gris_fmax(ly, hy)), gris_fmin(gris_fmax(lz, hz), bestT));
+                if (!(tn <= tf)) continue;
+                if (imask & (1u << s)) innerHits |= 1u << (s ^ oct);
+                else {
+                    uint32_t cnt = (meta >> 5) & 3u, off = meta & 31u;
+                    triHits |= ((1u << cnt) - 1u) << off;
+                }
+            }
+            uint32_t triBase = W[5];
+            while (triHits) {
+                int b = gris_ffs(triHits);
+                triHits &= triHits - 1u;
+                const float* T = tris + (uint64_t)(triBase + (uint32_t)b) * GRIS_TRI_FLOATS;
+#ifdef __CUDA_ARCH__
+                float4 t0 = __ldg(reinterpret_cast<const float4*>(T) + 0);
+                float4 t1 = __ldg(reinterpret_cast<const float4*>(T) + 1);
+                float4 t2 = __ldg(reinterpret_cast<const float4*>(T) + 2);
+                float TT[12] = {t0.x, t0.y, t0.z, t0.w, t1.x, t1.y, t1.z, t1.w, t2.x, t2.y, t2.z, t2.w};
+#else
+                float TT[12];
+                for (int i = 0; i < 12; i++) TT[i] = T[i];
+#endif
+                uint32_t inst = gris_f2u(TT[3]), tri = gris_f2u(TT[7]);
+                if (skipInst0 && inst == 0u) continue;
+                float t, u, v;
+                if (!gris_tri_test(TT, ox, oy, oz, dx, dy, dz, tmin, bestT, &t, &u, &v)) continue;
+                if (ANY) {
+                    hit->t = t; hit->u = u; hit->v = v; hit->inst = inst; hit->tri = tri;
+                    if (nodeVisits) *nodeVisits += visits;
+                    return true;
+                }
+                /* t <= bestT here (the test used bestT as tmax) */
+                bool keyLess = inst < bestInst || (inst == bestInst && tri < bestTri);
+                bool better = t < bestT || (t == bestT && keyLess);
+                if (better) {
+                    bestT = t; bestU = u; bestV = v; bestInst = inst; bestTri = tri; found = true;
+                }
+            }
+            if (innerHits) {
+                if (grpHits) {
+                    if (sp >= GRIS_BVH_STACK) { *err = 1; break; }
+                    stackBase[sp] = grpBase; stackBits[sp] = grpHits | (grpImask << 8); sp++;
+                }
+                grpBase = W[4]; grpHits = innerHits; grpImask = imask;
+            }
+            haveNode = false;
+        }
+        if (grpHits == 0) {
+            if (sp == 0) break;
+            sp--;
+            grpBase = stackBase[sp]; grpHits = stackBits[sp] & 0xffu; grpImask = stackBits[sp] >> 8;
+        }
+        int pos = gris_ffs(grpHits);
+        grpHits &= grpHits - 1u;
+        uint32_t slot = (uint32_t)pos ^ oct;
+        nodeIdx = grpBase + (uint32_t)gris_popc(grpImask & ((1u << slot) - 1u));
+        haveNode = true;
+    }
+    if (nodeVisits) *nodeVisits += visits;
+    if (found) { hit->t = bestT; hit->u = bestU; hit->v = bestV; hit->inst = bestInst; hit->tri = bestTri; }
+    return found;
+}
+
+#endif

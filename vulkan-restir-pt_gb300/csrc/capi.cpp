@@ -1,0 +1,397 @@
+/*
+ * capi.cpp — the grisrt C ABI (include/grisrt.h): contexts, scene upload + BVH build,
+ * caller-bound passes, library-owned frames with the renderer's ping-pong.
+ *
+ * Reference roles: GRISReSTIR::createPipeline / render (src/GRISReSTIR.cpp:9-67),
+ * DeviceScene (src/Scene.cpp:324-446), Renderer's per-frame resources and ping-pong
+ * (src/Renderer.cpp:193-257, 329-347, 539-569).
+ */
+#include <cuda_runtime.h>
+#include <string.h>
+
+#include <string>
+#include <vector>
+
+#include "../../include/grisrt.h"
+#include "bvh_traverse.h"
+#include "gris_kernels.h"
+#include "grisrt_internal.h"
+
+static_assert(sizeof(GrisMaterial) == 32, "Material is 32 B (layouts.glsl:6-25)");
+static_assert(sizeof(GrisMeshVertex) == 32, "MeshVertex is 32 B");
+static_assert(sizeof(GrisObjectInstance) == 224, "ObjectInstance is 224 B");
+static_assert(sizeof(GrisTriangleLight) == 64, "TriangleLight is 64 B");
+static_assert(sizeof(GrisLightTableEntry) == 8, "LightSampleTableElement is 8 B");
+static_assert(sizeof(GrisCamera) == 352, "Camera is 352 B");
+static_assert(sizeof(GrisReservoir) == 96, "GRISReservoir is 96 B");
+static_assert(sizeof(GrisSettings) == 64, "GrisSettings is 64 B");
+
+struct GrisContext {
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    unsigned long long* dCounters = nullptr;
+    unsigned long long* hCounters = nullptr;   /* pinned */
+    std::string err;
+};
+
+struct GrisScene {
+    GrisContext* ctx = nullptr;
+    std::vector<void*> allocations;
+    grisrt::DeviceSceneView view{};
+    grisrt::BvhHost bvh;
+    GrisSceneStats stats{};
+};
+
+struct GrisFrame {
+    GrisContext* ctx = nullptr;
+    uint32_t w = 0, h = 0;
+    float* depthNormal[2] = {nullptr, nullptr};
+    uint32_t* albedoMatId[2] = {nullptr, nullptr};
+    uint16_t* motion = nullptr;
+    GrisReservoir* resv[2] = {nullptr, nullptr};
+    GrisReservoir* temp = nullptr;
+    float* output = nullptr;
+    int next = 0;   /* slot the next render writes */
+};
+
+namespace {
+
+int fail(GrisContext* ctx, int code, const std::string& msg) {
+    if (ctx) ctx->err = msg;
+    return code;
+}
+int cuda_fail(GrisContext* ctx, cudaError_t e, const char* what) {
+    return fail(ctx, e == cudaErrorMemoryAllocation ? GRIS_ERR_OUT_OF_MEMORY : GRIS_ERR_CUDA,
+                std::string(what) + ": " + cudaGetErrorString(e));
+}
+#define GRIS_CK(ctx, call)                                   \
+    do {                                                     \
+        cudaError_t e_ = (call);                             \
+        if (e_ != cudaSuccess) return cuda_fail(ctx, e_, #call); \
+    } while (0)
+
+template <typename T>
+int upload(GrisContext* ctx, GrisScene* s, const T* src, uint64_t n, const T** dst) {
+    size_t bytes = (size_t)n * sizeof(T);
+    void* p = nullptr;
+    GRIS_CK(ctx, cudaMalloc(&p, bytes < 256 ? 256 : bytes));
+    s->allocations.push_back(p);
+    if (bytes) GRIS_CK(ctx, cudaMemcpyAsync(p, src, bytes, cudaMemcpyHostToDevice, ctx->stream));
+    *dst = (const T*)p;
+    return GRIS_OK;
+}
+
+grisrt::DeviceSceneView scene_view(const GrisScene* s) { return s->view; }
+
+}  // namespace
+
+extern "C" {
+
+int grisGetVersion(void) { return 1; }
+
+size_t grisSizeof(int which) {
+    switch (which) {
+    case 0: return sizeof(GrisCamera);
+    case 1: return sizeof(GrisReservoir);
+    case 2: return sizeof(GrisMaterial);
+    case 3: return sizeof(GrisMeshVertex);
+    case 4: return sizeof(GrisObjectInstance);
+    case 5: return sizeof(GrisTriangleLight);
+    case 6: return sizeof(GrisLightTableEntry);
+    case 7: return sizeof(GrisSettings);
+    }
+    return 0;
+}
+
+int grisCreate(int device, GrisContext** out) {
+    if (!out) return GRIS_ERR_INVALID_ARGUMENT;
+    *out = nullptr;
+    int count = 0;
+    cudaError_t e = cudaGetDeviceCount(&count);
+    if (e != cudaSuccess || count == 0) return GRIS_ERR_CUDA;
+    if (device < 0 || device >= count) return GRIS_ERR_INVALID_ARGUMENT;
+    GrisContext* ctx = new GrisContext();
+    ctx->device = device;
+    if (cudaSetDevice(device) != cudaSuccess || cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaMalloc(&ctx->dCounters, 8 * sizeof(unsigned long long)) != cudaSuccess ||
+        cudaMallocHost(&ctx->hCounters, 8 * sizeof(unsigned long long)) != cudaSuccess ||
+        cudaMemset(ctx->dCounters, 0, 8 * sizeof(unsigned long long)) != cudaSuccess) {
+        delete ctx;
+        return GRIS_ERR_CUDA;
+    }
+    *out = ctx;
+    return GRIS_OK;
+}
+
+int grisDestroy(GrisContext* ctx) {
+    if (!ctx) return GRIS_ERR_INVALID_ARGUMENT;
+    cudaSetDevice(ctx->device);
+    if (ctx->stream) cudaStreamSynchronize(ctx->stream);
+    cudaFree(ctx->dCounters);
+    cudaFreeHost(ctx->hCounters);
+    if (ctx->stream) cudaStreamDestroy(ctx->stream);
+    delete ctx;
+    return GRIS_OK;
+}
+
+const char* grisGetError(const GrisContext* ctx) { return ctx ? ctx->err.c_str() : "null context"; }
+
+void* grisGetStream(GrisContext* ctx) { return ctx ? (void*)ctx->stream : nullptr; }
+
+int grisReadCounters(GrisContext* ctx, uint64_t out[4], int reset) {
+    if (!ctx || !out) return GRIS_ERR_INVALID_ARGUMENT;
+    cudaSetDevice(ctx->device);
+    GRIS_CK(ctx, cudaMemcpyAsync(ctx->hCounters, ctx->dCounters, 4 * sizeof(unsigned long long), cudaMemcpyDeviceToHost, ctx->stream));
+    if (reset) GRIS_CK(ctx, cudaMemsetAsync(ctx->dCounters, 0, 4 * sizeof(unsigned long long), ctx->stream));
+    GRIS_CK(ctx, cudaStreamSynchronize(ctx->stream));
+    for (int i = 0; i < 4; i++) out[i] = ctx->hCounters[i];
+    return GRIS_OK;
+}
+
+int grisSync(GrisContext* ctx) {
+    if (!ctx) return GRIS_ERR_INVALID_ARGUMENT;
+    cudaSetDevice(ctx->device);
+    GRIS_CK(ctx, cudaStreamSynchronize(ctx->stream));
+    GRIS_CK(ctx, cudaMemcpy(ctx->hCounters + 3, ctx->dCounters + 3, sizeof(unsigned long long), cudaMemcpyDeviceToHost));
+    if (ctx->hCounters[3]) return fail(ctx, GRIS_ERR_DEVICE_FAULT, "a kernel raised the error word (traversal stack limit)");
+    return GRIS_OK;
+}
+
+/* ------------------------------------------------------------------ scene */
+int grisSceneCreate(GrisContext* ctx, const GrisSceneDesc* d, GrisScene** out) {
+    if (!ctx || !d || !out) return fail(ctx, GRIS_ERR_INVALID_ARGUMENT, "null argument");
+    *out = nullptr;
+    if ((d->vertexCount && !d->vertices) || (d->indexCount && !d->indices) || (d->instanceCount && !d->instances) ||
+        (d->materialCount && !d->materials) || (d->materialIndexCount && !d->materialIndices) ||
+        (d->lightCount && !d->lights) || (d->lightTableCount && !d->lightTable))
+        return fail(ctx, GRIS_ERR_INVALID_ARGUMENT, "array pointer is null but its count is not");
+    if (d->lightCount && d->lightTableCount != d->lightCount + 1)
+        return fail(ctx, GRIS_ERR_INVALID_ARGUMENT, "light table needs lightCount + 1 entries");
+    for (uint64_t i = 0; i < d->materialCount; i++)
+        if (d->materials[i].textureIdx != 0xffffffffu)
+            return fail(ctx, GRIS_ERR_UNSUPPORTED, "textured materials are not supported");
+    cudaSetDevice(ctx->device);
+    GrisScene* s = new GrisScene();
+    s->ctx = ctx;
+    std::string err;
+    if (!grisrt::build_bvh(*d, s->bvh, err)) { delete s; return fail(ctx, GRIS_ERR_INVALID_ARGUMENT, err); }
+    int rc = GRIS_OK;
+#define UP(src, n, dst) if (rc == GRIS_OK) rc = upload(ctx, s, src, n, dst)
+    UP(d->vertices, d->vertexCount, &s->view.vertices);
+    UP(d->indices, d->indexCount, &s->view.indices);
+    UP(d->instances, d->instanceCount, &s->view.instances);
+    UP(d->materials, d->materialCount, &s->view.materials);
+    UP(d->materialIndices, d->materialIndexCount, &s->view.matIndices);
+    UP(d->lights, d->lightCount, &s->view.lights);
+    UP(d->lightTable, d->lightTableCount, &s->view.table);
+    UP(s->bvh.nodes.data(), (uint64_t)s->bvh.nodes.size(), &s->view.nodes);
+    UP(s->bvh.tris.data(), (uint64_t)s->bvh.tris.size(), &s->view.tris);
+#undef UP
+    if (rc == GRIS_OK) {
+        cudaError_t e = cudaStreamSynchronize(ctx->stream);
+        if (e != cudaSuccess) rc = cuda_fail(ctx, e, "scene upload");
+    }
+    if (rc != GRIS_OK) { grisSceneDestroy(s); return rc; }
+    s->view.nVertices = d->vertexCount; s->view.nIndices = d->indexCount; s->view.nInstances = d->instanceCount;
+    s->view.nMaterials = d->materialCount; s->view.nMatIndices = d->materialIndexCount;
+    s->view.nLights = d->lightCount; s->view.nTable = d->lightTableCount;
+    s->stats.triangleCount = s->bvh.triangleCount;
+    s->stats.nodeCount = s->bvh.nodes.size() / GRIS_NODE_WORDS;
+    s->stats.nodeBytes = s->bvh.nodes.size() * 4ull;
+    s->stats.triangleBytes = s->bvh.tris.size() * 4ull;
+    s->stats.maxDepth = s->bvh.maxDepth;
+    s->stats.buildSeconds = s->bvh.buildSeconds;
+    *out = s;
+    return GRIS_OK;
+}
+
+int grisSceneDestroy(GrisScene* s) {
+    if (!s) return GRIS_ERR_INVALID_ARGUMENT;
+    if (s->ctx) {
+        cudaSetDevice(s->ctx->device);
+        cudaStreamSynchronize(s->ctx->stream);
+    }
+    for (void* p : s->allocations) cudaFree(p);
+    delete s;
+    return GRIS_OK;
+}
+
+int grisDebugHostSceneCreate(const GrisSceneDesc* d, GrisScene** out) {
+    if (!d || !out) return GRIS_ERR_INVALID_ARGUMENT;
+    *out = nullptr;
+    GrisScene* s = new GrisScene();
+    std::string err;
+    if (!grisrt::build_bvh(*d, s->bvh, err)) { delete s; return GRIS_ERR_INVALID_ARGUMENT; }
+    s->stats.triangleCount = s->bvh.triangleCount;
+    s->stats.nodeCount = s->bvh.nodes.size() / GRIS_NODE_WORDS;
+    s->stats.nodeBytes = s->bvh.nodes.size() * 4ull;
+    s->stats.triangleBytes = s->bvh.tris.size() * 4ull;
+    s->stats.maxDepth = s->bvh.maxDepth;
+    s->stats.buildSeconds = s->bvh.buildSeconds;
+    *out = s;
+    return GRIS_OK;
+}
+
+int grisSceneGetStats(const GrisScene* s, GrisSceneStats* out) {
+    if (!s || !out) return GRIS_ERR_INVALID_ARGUMENT;
+    *out = s->stats;
+    return GRIS_OK;
+}
+
+int grisDebugTraceHost(const GrisScene* s, const float* rays, uint64_t n, int anyHit, float* hitTUV, uint32_t* hitInst,
+                       uint32_t* hitTri) {
+    if (!s || (n && (!rays || !hitTUV || !hitInst || !hitTri))) return GRIS_ERR_INVALID_ARGUMENT;
+    const uint32_t* nodes = s->bvh.nodes.data();
+    const float* tris = s->bvh.tris.data();
+    int anyErr = 0;
+#pragma omp parallel for schedule(dynamic, 256) reduction(| : anyErr)
+    for (int64_t i = 0; i < (int64_t)n; i++) {
+        const float* r = rays + i * 8;
+        GrisRayHit h;
+        int err = 0;
+        bool hit = anyHit ? gris_bvh_trace<true>(nodes, tris, r[0], r[1], r[2], r[4], r[5], r[6], r[3], r[7], false, &h, &err, nullptr)
+                          : gris_bvh_trace<false>(nodes, tris, r[0], r[1], r[2], r[4], r[5], r[6], r[3], r[7], false, &h, &err, nullptr);
+        anyErr |= err;
+        if (hit) { hitTUV[i * 4] = h.t; hitTUV[i * 4 + 1] = h.u; hitTUV[i * 4 + 2] = h.v; hitTUV[i * 4 + 3] = 0.0f; hitInst[i] = h.inst; hitTri[i] = h.tri; }
+        else { hitTUV[i * 4] = -1.0f; hitTUV[i * 4 + 1] = 0.0f; hitTUV[i * 4 + 2] = 0.0f; hitTUV[i * 4 + 3] = 0.0f; hitInst[i] = GRIS_INVALID_HIT; hitTri[i] = GRIS_INVALID_HIT; }
+    }
+    return anyErr ? GRIS_ERR_DEVICE_FAULT : GRIS_OK;
+}
+
+int grisDebugTraceDevice(GrisContext* ctx, const GrisScene* s, const float* dRays, uint64_t n, int anyHit, float* dHitTUV,
+                         uint32_t* dHitInst, uint32_t* dHitTri) {
+    if (!ctx || !s) return GRIS_ERR_INVALID_ARGUMENT;
+    cudaSetDevice(ctx->device);
+    GRIS_CK(ctx, grisrt::launch_debug_trace(s->view.nodes, s->view.tris, dRays, n, anyHit, dHitTUV, dHitInst, dHitTri,
+                                            ctx->dCounters, ctx->stream));
+    return GRIS_OK;
+}
+
+/* ------------------------------------------------------------------ passes on caller buffers */
+int grisPassGBuffer(GrisContext* ctx, const GrisScene* s, const GrisGBufferBindings* b, const GrisCamera* cam) {
+    if (!ctx || !s || !b || !cam) return fail(ctx, GRIS_ERR_INVALID_ARGUMENT, "null argument");
+    if (!b->depthNormal || !b->albedoMatId || !b->motion || b->width == 0 || b->height == 0)
+        return fail(ctx, GRIS_ERR_INVALID_ARGUMENT, "G-buffer bindings incomplete");
+    if (cam->filmSize[0] != b->width || cam->filmSize[1] != b->height)
+        return fail(ctx, GRIS_ERR_INVALID_ARGUMENT, "camera filmSize differs from the bound extent");
+    cudaSetDevice(ctx->device);
+    GRIS_CK(ctx, grisrt::launch_gbuffer(scene_view(s), *b, *cam, ctx->dCounters, ctx->stream));
+    return GRIS_OK;
+}
+
+int grisPassRender(GrisContext* ctx, const GrisScene* s, const GrisPassBindings* b, const GrisCamera* cam,
+                   const GrisCamera* prevCam, const GrisSettings* set, int passes) {
+    if (!ctx || !s || !b || !cam || !prevCam || !set) return fail(ctx, GRIS_ERR_INVALID_ARGUMENT, "null argument");
+    if (b->width == 0 || b->height == 0 || !b->depthNormal || !b->albedoMatId || !b->reservoirThis || !b->reservoirTemp ||
+        ((passes & 2) && (!b->depthNormalPrev || !b->albedoMatIdPrev || !b->motion || !b->reservoirPrev)) ||
+        ((passes & 4) && !b->output))
+        return fail(ctx, GRIS_ERR_INVALID_ARGUMENT, "pass bindings incomplete");
+    if (cam->filmSize[0] != b->width || cam->filmSize[1] != b->height)
+        return fail(ctx, GRIS_ERR_INVALID_ARGUMENT, "camera filmSize differs from the bound extent");
+    if (set->maxDepth == 0 || set->maxDepth > 255) return fail(ctx, GRIS_ERR_INVALID_ARGUMENT, "maxDepth must be 1..255");
+    if (set->spatialNeighbors > 64) return fail(ctx, GRIS_ERR_INVALID_ARGUMENT, "spatialNeighbors must be <= 64");
+    cudaSetDevice(ctx->device);
+    GRIS_CK(ctx, grisrt::launch_gris(scene_view(s), *b, *cam, *prevCam, *set, passes & 7, ctx->dCounters, ctx->stream));
+    return GRIS_OK;
+}
+
+/* ------------------------------------------------------------------ frames */
+int grisFrameCreate(GrisContext* ctx, uint32_t w, uint32_t h, GrisFrame** out) {
+    if (!ctx || !out || w == 0 || h == 0) return fail(ctx, GRIS_ERR_INVALID_ARGUMENT, "bad frame size");
+    *out = nullptr;
+    cudaSetDevice(ctx->device);
+    GrisFrame* f = new GrisFrame();
+    f->ctx = ctx; f->w = w; f->h = h;
+    size_t n = (size_t)w * h;
+    cudaError_t e = cudaSuccess;
+    auto alloc = [&](void** p, size_t bytes) {
+        if (e == cudaSuccess) e = cudaMalloc(p, bytes);
+        if (e == cudaSuccess) e = cudaMemsetAsync(*p, 0, bytes, ctx->stream);
+    };
+    for (int i = 0; i < 2; i++) {
+        alloc((void**)&f->depthNormal[i], n * 16);
+        alloc((void**)&f->albedoMatId[i], n * 8);
+        alloc((void**)&f->resv[i], n * sizeof(GrisReservoir));
+    }
+    alloc((void**)&f->motion, n * 4);
+    alloc((void**)&f->temp, n * sizeof(GrisReservoir));
+    alloc((void**)&f->output, n * 16);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+    if (e != cudaSuccess) { grisFrameDestroy(f); return cuda_fail(ctx, e, "frame allocation"); }
+    *out = f;
+    return GRIS_OK;
+}
+
+int grisFrameDestroy(GrisFrame* f) {
+    if (!f) return GRIS_ERR_INVALID_ARGUMENT;
+    cudaSetDevice(f->ctx->device);
+    cudaStreamSynchronize(f->ctx->stream);
+    for (int i = 0; i < 2; i++) { cudaFree(f->depthNormal[i]); cudaFree(f->albedoMatId[i]); cudaFree(f->resv[i]); }
+    cudaFree(f->motion); cudaFree(f->temp); cudaFree(f->output);
+    delete f;
+    return GRIS_OK;
+}
+
+int grisFrameRender(GrisContext* ctx, const GrisScene* s, GrisFrame* f, const GrisCamera* cam, const GrisCamera* prevCam,
+                    const GrisSettings* set) {
+    if (!ctx || !s || !f || !cam || !prevCam || !set) return fail(ctx, GRIS_ERR_INVALID_ARGUMENT, "null argument");
+    int j = f->next;
+    GrisGBufferBindings gb;
+    gb.width = f->w; gb.height = f->h;
+    gb.depthNormal = f->depthNormal[j]; gb.albedoMatId = f->albedoMatId[j]; gb.motion = f->motion;
+    int rc = grisPassGBuffer(ctx, s, &gb, cam);
+    if (rc != GRIS_OK) return rc;
+    GrisPassBindings b;
+    b.width = f->w; b.height = f->h;
+    b.depthNormal = f->depthNormal[j]; b.depthNormalPrev = f->depthNormal[j ^ 1];
+    b.albedoMatId = f->albedoMatId[j]; b.albedoMatIdPrev = f->albedoMatId[j ^ 1];
+    b.motion = f->motion;
+    b.reservoirThis = f->resv[j]; b.reservoirPrev = f->resv[j ^ 1]; b.reservoirTemp = f->temp;
+    b.output = f->output;
+    rc = grisPassRender(ctx, s, &b, cam, prevCam, set, 7);
+    if (rc != GRIS_OK) return rc;
+    f->next = j ^ 1;
+    return GRIS_OK;
+}
+
+int grisFrameGetBuffer(const GrisFrame* f, int which, int slot, void** devPtr, size_t* bytes) {
+    if (!f || !devPtr || slot < 0 || slot > 1) return GRIS_ERR_INVALID_ARGUMENT;
+    int j = (f->next ^ 1) ^ slot;   /* slot 0: written by the last render */
+    size_t n = (size_t)f->w * f->h;
+    void* p = nullptr;
+    size_t sz = 0;
+    switch (which) {
+    case 0: p = f->depthNormal[j]; sz = n * 16; break;
+    case 1: p = f->albedoMatId[j]; sz = n * 8; break;
+    case 2: p = f->motion; sz = n * 4; break;
+    case 3: p = f->resv[j]; sz = n * sizeof(GrisReservoir); break;
+    case 4: p = f->temp; sz = n * sizeof(GrisReservoir); break;
+    case 5: p = f->output; sz = n * 16; break;
+    default: return GRIS_ERR_INVALID_ARGUMENT;
+    }
+    *devPtr = p;
+    if (bytes) *bytes = sz;
+    return GRIS_OK;
+}
+
+int grisFrameDownload(GrisContext* ctx, const GrisFrame* f, int which, int slot, void* host, size_t bytes) {
+    void* p; size_t sz;
+    int rc = grisFrameGetBuffer(f, which, slot, &p, &sz);
+    if (rc != GRIS_OK || !ctx || !host || bytes != sz) return fail(ctx, GRIS_ERR_INVALID_ARGUMENT, "bad download request");
+    cudaSetDevice(ctx->device);
+    GRIS_CK(ctx, cudaMemcpyAsync(host, p, sz, cudaMemcpyDeviceToHost, ctx->stream));
+    GRIS_CK(ctx, cudaStreamSynchronize(ctx->stream));
+    return GRIS_OK;
+}
+
+int grisFrameUpload(GrisContext* ctx, GrisFrame* f, int which, int slot, const void* host, size_t bytes) {
+    void* p; size_t sz;
+    int rc = grisFrameGetBuffer(f, which, slot, &p, &sz);
+    if (rc != GRIS_OK || !ctx || !host || bytes != sz) return fail(ctx, GRIS_ERR_INVALID_ARGUMENT, "bad upload request");
+    cudaSetDevice(ctx->device);
+    GRIS_CK(ctx, cudaMemcpyAsync(p, host, sz, cudaMemcpyHostToDevice, ctx->stream));
+    GRIS_CK(ctx, cudaStreamSynchronize(ctx->stream));
+    return GRIS_OK;
+}
+
+}  /* extern "C" */

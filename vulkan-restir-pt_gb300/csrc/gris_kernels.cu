@@ -1,0 +1,716 @@
+/*
+ * gris_kernels.cu — the GRIS hot path on sm_103a.
+ *
+ *   k_gbuffer      GBuffer.vert/.frag (raster) as one primary ray per pixel over the BVH
+ *   k_path_trace   gris_path_trace.comp / tracePath (gris_path_trace.glsl:45-306)
+ *   k_temporal     gris_resample_temporal.comp / temporalReuse (gris_resample_temporal.glsl:36-83)
+ *   k_spatial      gris_resample_spatial.comp / spatialReuse + final shading + running mean
+ *                  (gris_resample_spatial.glsl:36-135, gris_resample_spatial.comp:14-28)
+ * with the hybrid shift traceReplayPathForHybridShift / GRISReservoirReuseAndMerge
+ * (gris_retrace.glsl:42-236) shared by the two reuse kernels.
+ *
+ * One thread per pixel, 16 x 8 pixel tiles; traversal is the 8-wide BVH walk of
+ * bvh_traverse.h. Ray counts are accumulated per thread and added once per warp.
+ */
+#include <cuda_fp16.h>
+#include <cuda_runtime.h>
+
+#include "gris_device.cuh"
+#include "gris_kernels.h"
+
+namespace grisrt {
+
+struct PassCtx {
+    DevScene sc;
+    CamD cam, prev;
+    GrisSettings set;
+    GrisPassBindings b;
+    unsigned long long* counters;
+};
+
+/* ------------------------------------------------------------------ ray queries */
+struct RayCount { uint32_t closest, shadow; };
+
+GD Isec traceClosestHit(const DevScene& sc, V3 o, V3 d, float tmin, float tmax, RayCount& rc, int& err) {
+    rc.closest++;
+    GrisRayHit h;
+    Isec r;
+    if (gris_bvh_trace<false>(sc.nodes, sc.tris, o.x, o.y, o.z, d.x, d.y, d.z, tmin, tmax, false, &h, &err, nullptr)) {
+        r.bx = h.u; r.by = h.v; r.inst = h.inst; r.tri = h.tri;
+    } else {
+        r.bx = 0.0f; r.by = 0.0f; r.inst = kInvalidHit; r.tri = 0u;
+    }
+    return r;
+}
+GD bool traceShadow(const DevScene& sc, V3 o, float tmin, V3 d, float tmax, RayCount& rc, int& err) {
+    rc.shadow++;
+    GrisRayHit h;
+    return gris_bvh_trace<true>(sc.nodes, sc.tris, o.x, o.y, o.z, d.x, d.y, d.z, tmin, tmax, false, &h, &err, nullptr);
+}
+/* ray_query.glsl:29-39 */
+GD bool traceVisibility(const DevScene& sc, V3 from, V3 to, RayCount& rc, int& err) {
+    return !traceShadow(sc, from, kMinRayDistance, normalize3(to - from), distance3(to, from) - kMinRayDistance, rc, err);
+}
+
+GD void flush_counts(unsigned long long* counters, const RayCount& rc, int err) {
+    unsigned int c = __reduce_add_sync(0xffffffffu, rc.closest);
+    unsigned int s = __reduce_add_sync(0xffffffffu, rc.shadow);
+    unsigned int e = __reduce_or_sync(0xffffffffu, (unsigned)err);
+    if (((threadIdx.y * blockDim.x + threadIdx.x) & 31u) == 0u) {
+        if (c) atomicAdd(counters + GRIS_COUNTER_CLOSEST, (unsigned long long)c);
+        if (s) atomicAdd(counters + GRIS_COUNTER_SHADOW, (unsigned long long)s);
+        if (e) atomicOr(counters + GRIS_COUNTER_ERROR, (unsigned long long)e);
+    }
+}
+
+/* ------------------------------------------------------------------ path sampling */
+struct Stream { PathSample ps; float weight, sumWeight; uint32_t sampleCount; };       /* gris_path_trace.glsl:10-23 */
+GD void addStream(Stream& r, const PathSample& ps, float weight, float rnd) {           /* :25-33 */
+    r.sumWeight += weight;
+    if (rnd * r.sumWeight < weight) { r.weight = weight; r.ps = ps; r.sampleCount++; }
+}
+GD uint32_t nextRcVertexSampleState(uint32_t state, bool connectible) {                 /* :35-43 */
+    if (state == 2u) return 2u;
+    if (!connectible) return 0u;
+    return state + (connectible ? 1u : 0u);
+}
+
+/* tracePath (gris_path_trace.glsl:45-306); writes the canonical reservoir of the pixel. */
+GD void tracePath(const PassCtx& P, uint32_t ix, uint32_t iy, RayCount& rc, int& err) {
+    const DevScene& sc = P.sc;
+    const int W = (int)P.b.width, H = (int)P.b.height;
+    V2 uv = v2(((float)ix + 0.5f) / (float)W, ((float)iy + 0.5f) / (float)H);
+    float depth = 0.0f; V3 norm = v3s(0.0f), albedo = v3s(0.0f); int matMeshId = 0;
+    float4 dn = texture_bilinear(reinterpret_cast<const float4*>(P.b.depthNormal), W, H, uv);
+    uint2 am = fetch_am(reinterpret_cast<const uint2*>(P.b.albedoMatId), W, H, (int)ix, (int)iy);
+    if (!unpackGBuffer(dn, am, depth, norm, albedo, matMeshId)) return;
+    int matId = matMeshId >> 16;
+    Ray3 ray = pinholeCameraSampleRay(P.cam, v2(uv.x, 1.0f - uv.y));
+    uint32_t rng = makeSeed2(P.cam.seed, ix, iy);
+
+    V3 radiance = v3s(0.0f);
+    V3 throughput = v3s(1.0f);
+    V3 rcThroughput = v3s(0.0f);
+    V3 wo = -ray.dir;
+    V3 lastPos = v3s(0.0f);
+    bool isLastVertexConnectible = false;
+    uint32_t sampleState = 0u, lastSampleState = 0u;
+
+    Surf surf = surf_zero();
+    surf.pos = ray.ori + ray.dir * (depth - 1e-4f);
+    surf.norm = norm;
+    surf.albedo = albedo;
+    surf.isLight = false;
+
+    Mat mat = load_material(sc, (uint32_t)matId);
+    BsdfSample s = bs_zero();
+    Isec isec = isec_zero();
+
+    PathSample pathSample = ps_zero();
+    pathSampleReset(pathSample);
+    pathSample.primaryRng = rng;
+
+    Resv resv = resv_zero();
+    resvReset(resv);
+    Stream stream;
+    stream.ps = ps_zero(); stream.weight = 0.0f; stream.sumWeight = 0.0f; stream.sampleCount = 0u;
+
+    const int maxDepth = (int)P.set.maxDepth;
+    for (int bounce = 0; bounce < maxDepth; bounce++) {
+        if (bounce > 0) {
+            isec = traceClosestHit(sc, ray.ori, ray.dir, kMinRayDistance, kMaxRayDistance, rc, err);
+            if (isec.inst == kInvalidHit) break;
+            loadSurfaceInfo(sc, isec, surf);
+            mat = load_material(sc, surf.matIndex);
+        }
+        setPathLength(pathSample.flags, (uint32_t)bounce + 1u);
+
+        float cosPrevWi = dot3(ray.dir, surf.norm);
+        float distToPrev = distance3(lastPos, surf.pos);
+        float geometryJacobian = fabsf(cosPrevWi) / square(distToPrev);
+
+        bool isThisVertexConnectible = surf.isLight || isBSDFConnectible(mat);
+
+        lastSampleState = sampleState;
+        sampleState = nextRcVertexSampleState(sampleState, isThisVertexConnectible);
+
+        if (P.set.shiftType == kShiftReconnection && bounce == 1 && !surf.isLight) {
+            sampleState = 2u;
+            lastSampleState = 1u;
+        }
+        float resvRandSample = sample1f(rng);
+
+        if (surf.isLight) {
+            if (bounce > 1 && cosPrevWi < 0.0f) {
+                float weight = 1.0f;
+                float sumPower = load_table(sc, 0).prob;
+                float lightPdf = luminance(surf.albedo) / sumPower / geometryJacobian;
+                if (!isSampleTypeDelta(s.type)) weight = MISWeight(s.pdf, lightPdf);
+                V3 weightedLi = surf.albedo * weight;
+                if (sampleState == 2u && lastSampleState == 2u) {
+                    pathSample.rcLi = pathSample.rcLi + weightedLi * rcThroughput;
+                    pathSample.F = pathSample.F + weightedLi * throughput;
+                } else if ((sampleState == 2u && lastSampleState == 1u) && isLastVertexConnectible &&
+                           distToPrev > kDistanceThreshold) {
+                    pathSample.rcIsec = isec;
+                    pathSample.rcRng = rng;
+                    pathSample.rcPrevSamplePdf = s.pdf;
+                    pathSample.rcJacobian = geometryJacobian;
+                    pathSample.rcLi = weightedLi;
+                    pathSample.rcWi = v3s(0.0f);
+                    pathSample.F = weightedLi * throughput;
+                    setRcVertexId(pathSample.flags, (uint32_t)bounce);
+                    setRcVertexType(pathSample.flags, kRcLightScattered);
+                    addStream(stream, pathSample, luminance(pathSample.F), resvRandSample);
+                }
+                radiance = radiance + weightedLi * throughput;
+            }
+            break;
+        }
+
+        bool connectible = isThisVertexConnectible && isLastVertexConnectible && distToPrev > kDistanceThreshold;
+
+        if ((sampleState == 2u && lastSampleState == 1u) && (connectible || P.set.shiftType == kShiftReconnection)) {
+            pathSample.rcIsec = isec;
+            pathSample.rcRng = rng;
+            pathSample.rcPrevSamplePdf = s.pdf;
+            pathSample.rcJacobian = geometryJacobian;
+            setRcVertexId(pathSample.flags, (uint32_t)bounce);
+            setRcVertexType(pathSample.flags, kRcSurface);
+            rcThroughput = v3s(1.0f);
+        }
+
+        V4 lightRandSample = sample4f(rng);
+        resvRandSample = sample1f(rng);
+
+        if (bounce > 0 && !isBSDFDelta(mat)) {
+            V3 lightDir; V2 lightBary; float lightDist, lightPdf, lightJacobian; uint32_t lightId;
+            V3 lightRadiance = sampleLightByPower(sc, surf.pos, lightDir, lightDist, lightPdf, lightJacobian, lightBary,
+                                                  lightId, lightRandSample);
+            bool shadowed = traceShadow(sc, surf.pos, kMinRayDistance, lightDir, lightDist - kMinRayDistance, rc, err);
+            if (!shadowed && lightPdf > 1e-6f) {
+                float bsdfPdf = absDot(surf.norm, lightDir) * kPiInv;
+                float weight = MISWeight(lightPdf, bsdfPdf);
+                V3 scatterTerm = evalBSDF(mat, surf.albedo, surf.norm, wo, lightDir) * satDot(surf.norm, lightDir);
+                V3 weightedLi = lightRadiance / lightPdf * weight;
+                if (sampleState == 2u && lastSampleState == 2u) {
+                    pathSample.rcLi = pathSample.rcLi + weightedLi * scatterTerm * rcThroughput;
+                    pathSample.F = pathSample.F + weightedLi * scatterTerm * throughput;
+                } else if (sampleState == 2u && lastSampleState == 1u) {
+                    pathSample.rcLi = weightedLi;
+                    pathSample.rcWi = lightDir;
+                    pathSample.F = weightedLi * scatterTerm * throughput;
+                    addStream(stream, pathSample, luminance(pathSample.F), resvRandSample);
+                } else if ((sampleState == 1u) && isThisVertexConnectible && lightDist > kDistanceThreshold) {
+                    pathSample.rcIsec.bx = lightBary.x; pathSample.rcIsec.by = lightBary.y;
+                    pathSample.rcIsec.inst = 0u; pathSample.rcIsec.tri = lightId;
+                    pathSample.rcRng = rng;
+                    pathSample.rcPrevSamplePdf = lightPdf;
+                    pathSample.rcJacobian = lightJacobian;
+                    pathSample.rcLi = lightRadiance * weight;
+                    pathSample.rcWi = v3s(0.0f);
+                    pathSample.F = weightedLi * scatterTerm * throughput;
+                    setRcVertexId(pathSample.flags, (uint32_t)bounce + 1u);
+                    setRcVertexType(pathSample.flags, kRcLightSampled);
+                    addStream(stream, pathSample, luminance(pathSample.F), resvRandSample);
+                }
+                radiance = radiance + weightedLi * scatterTerm * throughput;
+            }
+        }
+
+        if (bounce > 4) {
+            float pdfTerminate = fmaxf(1.0f - luminance(throughput) * P.set.rrScale, 0.0f);
+            if (sample1f(rng) < pdfTerminate) break;
+            throughput = throughput / (1.0f - pdfTerminate);
+            rcThroughput = rcThroughput / (1.0f - pdfTerminate);
+        }
+
+        if (!sampleBSDF(mat, surf.albedo, surf.norm, wo, sample3f(rng), s) || s.pdf < 1e-6f) break;
+
+        float cosTheta = isSampleTypeDelta(s.type) ? 1.0f : absDot(surf.norm, s.wi);
+        V3 scatterTerm = s.bsdf * cosTheta / s.pdf;
+        throughput = throughput * scatterTerm;
+
+        if (sampleState == 2u && lastSampleState == 2u) {
+            rcThroughput = rcThroughput * scatterTerm;
+        } else if (sampleState == 2u && lastSampleState == 1u) {
+            pathSample.rcLi = v3s(0.0f);
+            pathSample.rcWi = s.wi;
+            pathSample.F = v3s(0.0f);
+            rcThroughput = rcThroughput / s.pdf;
+        }
+
+        lastPos = surf.pos;
+        wo = -s.wi;
+        ray.dir = s.wi;
+        ray.ori = surf.pos + ray.dir * 1e-4f;
+        isLastVertexConnectible = isThisVertexConnectible;
+    }
+
+    if (sampleState == 2u && lastSampleState == 2u) addStream(stream, pathSample, luminance(pathSample.F), sample1f(rng));
+
+    pathSample = stream.ps;
+    if (stream.sumWeight > 0.0f && stream.weight > 0.0f) {
+        pathSample.F = pathSample.F * (stream.sumWeight / stream.weight);
+        pathSample.rcLi = pathSample.rcLi * (stream.sumWeight / stream.weight);
+        resv.resampleWeight = luminance(pathSample.F);
+    } else {
+        pathSample.rcIsec.inst = kInvalidHit;
+        pathSample.F = v3s(0.0f);
+    }
+    resv.s = pathSample;
+    resv.sampleCount = 1.0f;
+    store_resv(P.b.reservoirThis, (uint64_t)iy * (uint64_t)W + ix, resv);
+    (void)radiance;
+}
+
+/* ------------------------------------------------------------------ hybrid shift (gris_retrace.glsl) */
+/* traceReplayPathForHybridShift (:42-136) */
+GD void traceReplay(const PassCtx& P, Isec isec, Surf surf, Ray3 ray, uint32_t targetFlags, uint32_t rng, RcData& rcData,
+                    RayCount& rc, int& err) {
+    const DevScene& sc = P.sc;
+    V3 throughput = v3s(1.0f);
+    V3 wo = -ray.dir;
+    Mat mat = load_material(sc, surf.matIndex);
+    BsdfSample s = bs_zero();
+    rcData.rcPrevThroughput = v3s(0.0f);
+    rcData.rcPrevIsec.inst = kInvalidHit;
+    uint32_t targetId = rcVertexId(targetFlags);
+    if (targetId == 1u) {
+        rcData.rcPrevIsec = isec;
+        rcData.rcPrevWo = wo;
+        rcData.rcPrevThroughput = throughput;
+        return;
+    }
+    const int maxDepth = (int)P.set.maxDepth;
+    for (int bounce = 0; bounce < maxDepth; bounce++) {
+        if (bounce > 0) {
+            isec = traceClosestHit(sc, ray.ori, ray.dir, kMinRayDistance, kMaxRayDistance, rc, err);
+            if (isec.inst == kInvalidHit) break;
+            loadSurfaceInfo(sc, isec, surf);
+            mat = load_material(sc, surf.matIndex);
+        }
+        bool isThisVertexConnectible = isBSDFConnectible(mat);
+        float resvRandSample = sample1f(rng);
+        (void)resvRandSample;
+        if (surf.isLight) break;
+        if ((uint32_t)bounce == targetId - 1u) {
+            if (isThisVertexConnectible) {
+                rcData.rcPrevIsec = isec;
+                rcData.rcPrevWo = wo;
+                rcData.rcPrevThroughput = throughput;
+            }
+            break;
+        }
+        V4 lightRandSample = sample4f(rng);
+        (void)lightRandSample;
+        resvRandSample = sample1f(rng);
+        if (bounce > 4) {
+            float pdfTerminate = fmaxf(1.0f - luminance(throughput) * P.set.rrScale, 0.0f);
+            if (sample1f(rng) < pdfTerminate) break;
+            throughput = throughput / (1.0f - pdfTerminate);
+        }
+        if (!sampleBSDF(mat, surf.albedo, surf.norm, wo, sample3f(rng), s) || s.pdf < 1e-6f) break;
+        float cosTheta = isSampleTypeDelta(s.type) ? 1.0f : absDot(surf.norm, s.wi);
+        V3 scatterTerm = s.bsdf * cosTheta / s.pdf;
+        throughput = throughput * scatterTerm;
+        wo = -s.wi;
+        ray.dir = s.wi;
+        ray.ori = surf.pos + ray.dir * 1e-4f;
+    }
+}
+
+/* GRISReservoirReuseAndMerge (:138-236) */
+GD void reuseAndMerge(const PassCtx& P, Resv& dstResv, const Surf& dstPrimarySurf, const Isec& dstPrimaryIsec,
+                      const Ray3& primaryRay, Resv srcResv, uint32_t& rng, RayCount& rc, int& err) {
+    const DevScene& sc = P.sc;
+    PathSample srcSample = srcResv.s;
+    RcData dstRcData;
+    dstRcData.rcPrevIsec = isec_zero(); dstRcData.rcPrevWo = v3s(0.0f); dstRcData.rcPrevThroughput = v3s(0.0f);
+    Surf rcPrevSurf = surf_zero(), rcSurf = surf_zero();
+    Mat rcMat = load_material(sc, 0xffffffffu), rcPrevMat = rcMat;
+    V3 wi = v3s(0.0f);
+    V3 Li = v3s(0.0f);
+    bool srcSampleValid = false;
+    float dstJacobian = 0.0f, jacobian = 0.0f, dist = 0.0f, dstPHat = 0.0f, dstSamplePdf = 0.0f;
+
+    if (srcSample.rcIsec.inst != kInvalidHit) {
+        traceReplay(P, dstPrimaryIsec, dstPrimarySurf, primaryRay, srcSample.flags, srcSample.primaryRng, dstRcData, rc, err);
+        if (dstRcData.rcPrevIsec.inst != kInvalidHit) {
+            if (dstRcData.rcPrevIsec.inst == kSpecialHit) rcPrevSurf = dstPrimarySurf;
+            else loadSurfaceInfo(sc, dstRcData.rcPrevIsec, rcPrevSurf);
+            loadSurfaceInfo(sc, srcSample.rcIsec, rcSurf);
+            rcMat = load_material(sc, rcSurf.matIndex);
+            rcPrevMat = load_material(sc, rcPrevSurf.matIndex);
+            dist = distance3(rcPrevSurf.pos, rcSurf.pos);
+            wi = normalize3(rcSurf.pos - rcPrevSurf.pos);
+            float cosTheta = -dot3(rcSurf.norm, wi);
+            dstJacobian = fabsf(cosTheta) / square(dist);
+            jacobian = dstJacobian / srcSample.rcJacobian;
+            if (dist > kDistanceThreshold && cosTheta > 0.0f && !isnan(jacobian) && srcSample.rcJacobian > 0.0f &&
+                isBSDFConnectible(rcPrevMat)) {
+                if (traceVisibility(sc, rcPrevSurf.pos, rcSurf.pos, rc, err)) srcSampleValid = true;
+            }
+        }
+    }
+
+    if (srcSampleValid) {
+        uint32_t rcType = rcVertexType(srcSample.flags);
+        if (!isnan(srcSample.rcPrevSamplePdf) && srcSample.rcPrevSamplePdf > 1e-6f) {
+            Li = srcSample.rcLi;
+            if (rcType == kRcSurface && length3(srcSample.rcWi) > 0.5f) {
+                Li = Li * (evalBSDF(rcMat, rcSurf.albedo, rcSurf.norm, -wi, srcSample.rcWi) * satDot(rcSurf.norm, srcSample.rcWi));
+            }
+            Li = Li * (evalBSDF(rcPrevMat, rcPrevSurf.albedo, rcPrevSurf.norm, dstRcData.rcPrevWo, wi) * satDot(rcPrevSurf.norm, wi));
+            Li = Li * dstRcData.rcPrevThroughput;
+            Li = Li / srcSample.rcPrevSamplePdf;
+            if (!isBlack(Li) && !isnan3(Li)) dstPHat = luminance(Li * jacobian);
+            if (rcType == kRcLightSampled) {
+                float sumPower = load_table(sc, 0).prob;
+                dstSamplePdf = luminance(rcSurf.albedo) / sumPower / dstJacobian;
+            } else {
+                dstSamplePdf = evalPdf(rcPrevMat, rcPrevSurf.norm, dstRcData.rcPrevWo, wi);
+            }
+        }
+        float srcPHat = luminance(srcSample.F);
+        srcSample.rcJacobian = dstJacobian;
+        srcSample.rcPrevSamplePdf = dstSamplePdf;
+        srcSample.F = Li;
+        if (srcSample.rcPrevSamplePdf < 1e-6f || isnan(srcSample.rcPrevSamplePdf)) srcSample.rcPrevSamplePdf = 0.0f;
+        srcResv.s = srcSample;
+        srcResv.resampleWeight *= dstPHat / srcPHat;
+    } else {
+        srcResv.resampleWeight = 0.0f;
+    }
+    if (resvIsValid(srcResv)) resvMerge(dstResv, srcResv, sample1f(rng));
+    resvCap(dstResv, (float)P.set.cap);
+}
+
+/* ------------------------------------------------------------------ temporal reuse */
+GD void temporalReuse(const PassCtx& P, uint32_t ix, uint32_t iy, RayCount& rc, int& err) {
+    const DevScene& sc = P.sc;
+    const int W = (int)P.b.width, H = (int)P.b.height;
+    const uint64_t n = (uint64_t)W * (uint64_t)H;
+    V2 uv = v2(((float)ix + 0.5f) / (float)W, ((float)iy + 0.5f) / (float)H);
+    float depth = 0.0f; V3 norm = v3s(0.0f), albedo = v3s(0.0f); int matMeshId = 0;
+    float4 dn = texture_bilinear(reinterpret_cast<const float4*>(P.b.depthNormal), W, H, uv);
+    uint2 am = fetch_am(reinterpret_cast<const uint2*>(P.b.albedoMatId), W, H, (int)ix, (int)iy);
+    if (!unpackGBuffer(dn, am, depth, norm, albedo, matMeshId)) return;
+    const __half2* mv = reinterpret_cast<const __half2*>(P.b.motion);
+    float2 motion = __half22float2(mv[(uint64_t)iy * W + ix]);
+    int matId = matMeshId >> 16;
+    Ray3 ray = pinholeCameraSampleRay(P.cam, v2(uv.x, 1.0f - uv.y));
+    uint32_t rng = makeSeed2(P.cam.seed, ix, iy) ^ 1u;
+    uint32_t resvRng = ~rng;
+    V3 pos = ray.ori + ray.dir * (depth - 1e-4f);
+
+    uint64_t idx = (uint64_t)iy * W + ix;
+    Resv resv = load_resv(P.b.reservoirThis, idx, n);
+    Isec dstPrimaryIsec; dstPrimaryIsec.bx = uv.x; dstPrimaryIsec.by = uv.y; dstPrimaryIsec.inst = kSpecialHit; dstPrimaryIsec.tri = 0u;
+
+    if (P.set.temporalReuse) {
+        Resv temporalResv = resv_zero();
+        resvReset(temporalResv);
+        Surf dstPrimarySurf; dstPrimarySurf.pos = pos; dstPrimarySurf.norm = norm; dstPrimarySurf.albedo = albedo;
+        dstPrimarySurf.matIndex = (uint32_t)matId; dstPrimarySurf.isLight = false;
+        if ((P.cam.frameIndex & kCameraClearFlag) == 0u) {
+            /* findPreviousReservoir (gris_resample_temporal.glsl:11-34) */
+            V2 puv = v2(uv.x + motion.x, uv.y + motion.y);
+            bool found = false;
+            if (!(puv.x < 0.0f || puv.y < 0.0f || puv.x > 1.0f || puv.y > 1.0f)) {
+                int px = (int)(puv.x * (float)P.cam.w), py = (int)(puv.y * (float)P.cam.h);
+                float depthPrev = 0.0f; V3 normalPrev = v3s(0.0f), albedoPrev = v3s(0.0f); int matMeshIdPrev = 0;
+                float4 pdn = texture_bilinear(reinterpret_cast<const float4*>(P.b.depthNormalPrev), W, H, puv);
+                uint2 pam = fetch_am(reinterpret_cast<const uint2*>(P.b.albedoMatIdPrev), W, H, px, py);
+                if (unpackGBuffer(pdn, pam, depthPrev, normalPrev, albedoPrev, matMeshIdPrev)) {
+                    Ray3 pray = pinholeCameraSampleRay(P.prev, v2(puv.x, 1.0f - puv.y));
+                    V3 posPrev = pray.ori + pray.dir * (depthPrev - 1e-4f);
+                    if (!(matMeshIdPrev != matMeshId || dot3(normalPrev, norm) < 0.95f || distance3(pos, posPrev) > 0.5f)) {
+                        uint32_t pidx = (uint32_t)P.cam.w * (uint32_t)py + (uint32_t)px;
+                        temporalResv = load_resv(P.b.reservoirPrev, pidx, n);
+                        found = true;
+                    }
+                }
+            }
+            if (found && resvIsValid(temporalResv))
+                reuseAndMerge(P, resv, dstPrimarySurf, dstPrimaryIsec, ray, temporalResv, resvRng, rc, err);
+        }
+    }
+    resvResetIfInvalid(resv);
+    store_resv(P.b.reservoirTemp, idx, resv);
+}
+
+/* ------------------------------------------------------------------ spatial reuse + final shading */
+GD V3 spatialReuse(const PassCtx& P, uint32_t ix, uint32_t iy, RayCount& rc, int& err, bool& wrote) {
+    const DevScene& sc = P.sc;
+    const int W = (int)P.b.width, H = (int)P.b.height;
+    const uint64_t n = (uint64_t)W * (uint64_t)H;
+    V2 uv = v2(((float)ix + 0.5f) / (float)W, ((float)iy + 0.5f) / (float)H);
+    float depth = 0.0f; V3 norm = v3s(0.0f), albedo = v3s(0.0f); int matMeshId = 0;
+    const float4* dnT = reinterpret_cast<const float4*>(P.b.depthNormal);
+    const uint2* amT = reinterpret_cast<const uint2*>(P.b.albedoMatId);
+    float4 dn = texture_bilinear(dnT, W, H, uv);
+    uint2 am = fetch_am(amT, W, H, (int)ix, (int)iy);
+    wrote = false;
+    if (!unpackGBuffer(dn, am, depth, norm, albedo, matMeshId)) return v3s(0.0f);
+    uint32_t rng = makeSeed2(P.cam.seed, ix, iy) ^ 2u;
+    Ray3 ray = pinholeCameraSampleRay(P.cam, v2(uv.x, 1.0f - uv.y));
+    V3 pos = ray.ori + ray.dir * (depth - 1e-4f);
+    int matId = matMeshId >> 16;
+    V3 radiance = v3s(0.0f);
+    uint64_t idx = (uint64_t)iy * W + ix;
+    Resv resv = load_resv(P.b.reservoirTemp, idx, n);
+    Isec dstPrimaryIsec; dstPrimaryIsec.bx = uv.x; dstPrimaryIsec.by = uv.y; dstPrimaryIsec.inst = kSpecialHit; dstPrimaryIsec.tri = 0u;
+    Surf dstPrimarySurf; dstPrimarySurf.pos = pos; dstPrimarySurf.norm = norm; dstPrimarySurf.albedo = albedo;
+    dstPrimarySurf.matIndex = (uint32_t)matId; dstPrimarySurf.isLight = false;
+
+    if (P.set.spatialReuse) {
+        const uint32_t resampleNum = P.set.spatialNeighbors;
+        const float resampleRadius = P.set.spatialRadius;
+        float tx = 1.0f / (float)W, ty = 1.0f / (float)H;
+        for (uint32_t i = 0; i < resampleNum; i++) {
+            V2 d = toConcentricDisk(sample2f(rng));
+            V2 nb = v2(uv.x + d.x * resampleRadius * tx, uv.y + d.y * resampleRadius * ty);
+            Resv neighborResv = resv_zero();
+            resvReset(neighborResv);
+            /* findNeighborReservoir (gris_resample_spatial.glsl:11-34) */
+            if (nb.x < 0.0f || nb.y < 0.0f || nb.x > 1.0f || nb.y > 1.0f) continue;
+            int px = (int)(nb.x * (float)P.cam.w), py = (int)(nb.y * (float)P.cam.h);
+            float depthN = 0.0f; V3 normalN = v3s(0.0f), albedoN = v3s(0.0f); int matMeshIdN = 0;
+            float4 ndn = texture_bilinear(dnT, W, H, nb);
+            uint2 nam = fetch_am(amT, W, H, px, py);
+            if (!unpackGBuffer(ndn, nam, depthN, normalN, albedoN, matMeshIdN)) continue;
+            Ray3 nray = pinholeCameraSampleRay(P.cam, v2(nb.x, 1.0f - nb.y));
+            V3 posN = nray.ori + nray.dir * (depthN - 1e-4f);
+            if (dot3(normalN, norm) < 0.9f || distance3(pos, posN) > 0.4f) continue;
+            uint32_t nidx = (uint32_t)P.cam.w * (uint32_t)py + (uint32_t)px;
+            neighborResv = load_resv(P.b.reservoirTemp, nidx, n);
+            if (resvIsValid(neighborResv))
+                reuseAndMerge(P, resv, dstPrimarySurf, dstPrimaryIsec, ray, neighborResv, rng, rc, err);
+        }
+    }
+    resvResetIfInvalid(resv);
+    store_resv(P.b.reservoirThis, idx, resv);
+    wrote = true;
+
+    if (resvIsValid(resv) && resv.sampleCount > 0.0f) {
+        PathSample pathSample = resv.s;
+        if (pathSample.rcIsec.inst != kInvalidHit) {
+            RcData rcData;
+            rcData.rcPrevIsec = isec_zero(); rcData.rcPrevWo = v3s(0.0f); rcData.rcPrevThroughput = v3s(0.0f);
+            traceReplay(P, dstPrimaryIsec, dstPrimarySurf, ray, pathSample.flags, pathSample.primaryRng, rcData, rc, err);
+            if (rcData.rcPrevIsec.inst != kInvalidHit) {
+                Surf rcPrevSurf = surf_zero(), rcSurf = surf_zero();
+                if (rcData.rcPrevIsec.inst == kSpecialHit) rcPrevSurf = dstPrimarySurf;
+                else loadSurfaceInfo(sc, rcData.rcPrevIsec, rcPrevSurf);
+                loadSurfaceInfo(sc, pathSample.rcIsec, rcSurf);
+                Mat rcMat = load_material(sc, rcSurf.matIndex);
+                Mat rcPrevMat = load_material(sc, rcPrevSurf.matIndex);
+                V3 Li = pathSample.rcLi;
+                uint32_t rcType = rcVertexType(pathSample.flags);
+                V3 wi = normalize3(rcSurf.pos - rcPrevSurf.pos);
+                if (rcType == kRcSurface && length3(pathSample.rcWi) > 0.5f)
+                    Li = Li * (evalBSDF(rcMat, rcSurf.albedo, rcSurf.norm, -wi, pathSample.rcWi) * satDot(rcSurf.norm, pathSample.rcWi));
+                Li = Li * (evalBSDF(rcPrevMat, rcPrevSurf.albedo, rcPrevSurf.norm, rcData.rcPrevWo, wi) * satDot(rcPrevSurf.norm, wi));
+                Li = Li * rcData.rcPrevThroughput;
+                Li = Li / pathSample.rcPrevSamplePdf;
+                if (!isBlack(Li) && !isnan3(Li)) radiance = Li / luminance(Li) * resv.resampleWeight / resv.sampleCount;
+            }
+        }
+    }
+    return clampColor(radiance);
+}
+
+/* ------------------------------------------------------------------ kernels */
+__global__ void __launch_bounds__(128) k_path_trace(PassCtx P) {
+    uint32_t x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y * blockDim.y + threadIdx.y;
+    RayCount rc = {0u, 0u};
+    int err = 0;
+    if (x < P.b.width && y < P.b.height) tracePath(P, x, y, rc, err);
+    flush_counts(P.counters, rc, err);
+}
+
+__global__ void __launch_bounds__(128) k_temporal(PassCtx P) {
+    uint32_t x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y * blockDim.y + threadIdx.y;
+    RayCount rc = {0u, 0u};
+    int err = 0;
+    if (x < P.b.width && y < P.b.height) temporalReuse(P, x, y, rc, err);
+    flush_counts(P.counters, rc, err);
+}
+
+__global__ void __launch_bounds__(128) k_spatial(PassCtx P) {
+    uint32_t x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y * blockDim.y + threadIdx.y;
+    RayCount rc = {0u, 0u};
+    int err = 0;
+    if (x < P.b.width && y < P.b.height) {
+        bool wrote;
+        V3 color = spatialReuse(P, x, y, rc, err, wrote);
+        /* gris_resample_spatial.comp:21-27: running mean over frameIndex & mask frames */
+        float frameCount = (float)(P.cam.frameIndex & kCameraFrameIndexMask);
+        float4* out = reinterpret_cast<float4*>(P.b.output) + (uint64_t)y * P.b.width + x;
+        float4 o = *out;
+        V3 acc = v3(o.x, o.y, o.z);
+        acc = (acc * frameCount + color) / (frameCount + 1.0f);
+        *out = make_float4(acc.x, acc.y, acc.z, 1.0f);
+    }
+    flush_counts(P.counters, rc, err);
+}
+
+/* G-buffer (GBuffer.vert:16-28, GBuffer.frag:21-54) by primary rays that ignore instance 0. */
+struct GBufCtx {
+    DevScene sc;
+    CamD cam;
+    float lastProjView[16];
+    GrisGBufferBindings b;
+    unsigned long long* counters;
+};
+
+GD uint32_t packUnorm1(float c) { return (uint32_t)floorf(fminf(fmaxf(c, 0.0f), 1.0f) * 255.0f + 0.5f); }
+
+__global__ void __launch_bounds__(128) k_gbuffer(GBufCtx G) {
+    uint32_t x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y * blockDim.y + threadIdx.y;
+    int err = 0;
+    uint32_t primary = 0;
+    if (x < G.b.width && y < G.b.height) {
+        const DevScene& sc = G.sc;
+        uint64_t p = (uint64_t)y * G.b.width + x;
+        V2 uv = v2(((float)x + 0.5f) / (float)G.b.width, ((float)y + 0.5f) / (float)G.b.height);
+        Ray3 ray = pinholeCameraSampleRay(G.cam, v2(uv.x, 1.0f - uv.y));
+        GrisRayHit h;
+        primary = 1;
+        bool hit = gris_bvh_trace<false>(sc.nodes, sc.tris, ray.ori.x, ray.ori.y, ray.ori.z, ray.dir.x, ray.dir.y,
+                                          ray.dir.z, kMinRayDistance, kMaxRayDistance, true, &h, &err, nullptr);
+        float4* dnOut = reinterpret_cast<float4*>(G.b.depthNormal) + p;
+        uint2* amOut = reinterpret_cast<uint2*>(G.b.albedoMatId) + p;
+        __half2* mvOut = reinterpret_cast<__half2*>(G.b.motion) + p;
+        if (!hit) {
+            *dnOut = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+            *amOut = make_uint2(0u, 0u);
+            *mvOut = __halves2half2(__ushort_as_half(0), __ushort_as_half(0));
+        } else {
+            uint64_t k = (uint64_t)h.inst - 1u;
+            float T[16], TI[16];
+            uint32_t indexOffset = 0u;
+            if (k < sc.nInstances) {
+                load_mat4(sc.instances[k].transform, T);
+                load_mat4(sc.instances[k].transformInvT, TI);
+                indexOffset = ldu(&sc.instances[k].indexOffset);
+            } else {
+                for (int i = 0; i < 16; i++) { T[i] = 0.0f; TI[i] = 0.0f; }
+            }
+            V3 b = v3(1.0f - h.u - h.v, h.u, h.v);
+            V3 Pj[3], Nj[3];
+            for (int j = 0; j < 3; j++) {
+                V3 vp, vn;
+                load_vertex(sc, load_index(sc, (uint64_t)(indexOffset + h.tri * 3u + (uint32_t)j)), vp, vn);
+                Pj[j] = m4mul_point(T, vp, 1.0f);
+                V3 c0 = v3(TI[0], TI[1], TI[2]), c1 = v3(TI[4], TI[5], TI[6]), c2 = v3(TI[8], TI[9], TI[10]);
+                Nj[j] = normalize3((c0 * vn.x + c1 * vn.y) + c2 * vn.z);
+            }
+            V3 pos = (Pj[0] * b.x + Pj[1] * b.y) + Pj[2] * b.z;
+            V3 nor = normalize3((Nj[0] * b.x + Nj[1] * b.y) + Nj[2] * b.z);
+            uint64_t mi = (uint64_t)(indexOffset / 3u + h.tri);
+            uint32_t matIndex = (uint32_t)(mi < sc.nMatIndices ? (int32_t)ldu(reinterpret_cast<const uint32_t*>(sc.matIndices + mi)) : 0);
+            V3 albedo = load_material(sc, matIndex).baseColor;
+            const float* M = G.lastProjView;
+            float lx = ((M[0] * pos.x + M[4] * pos.y) + M[8] * pos.z) + M[12] * 1.0f;
+            float ly = ((M[1] * pos.x + M[5] * pos.y) + M[9] * pos.z) + M[13] * 1.0f;
+            float lw = ((M[3] * pos.x + M[7] * pos.y) + M[11] * pos.z) + M[15] * 1.0f;
+            lx = lx / lw; ly = ly / lw;
+            lx = lx * 0.5f + 0.5f; ly = ly * 0.5f + 0.5f;
+            float tx = ((float)x + 0.5f) / (float)G.b.width, ty = ((float)y + 0.5f) / (float)G.b.height;
+            float mx = lx - tx, my = ly - ty;
+            *dnOut = make_float4(length3(G.cam.pos - pos), nor.x, nor.y, nor.z);
+            uint32_t packed = packUnorm1(albedo.x) | (packUnorm1(albedo.y) << 8) | (packUnorm1(albedo.z) << 16) | (packUnorm1(1.0f) << 24);
+            *amOut = make_uint2(packed, (matIndex << 16) | (uint32_t)k);
+            *mvOut = __halves2half2(__float2half_rn(mx), __float2half_rn(my));
+        }
+    }
+    unsigned int c = __reduce_add_sync(0xffffffffu, primary);
+    unsigned int e = __reduce_or_sync(0xffffffffu, (unsigned)err);
+    if (((threadIdx.y * blockDim.x + threadIdx.x) & 31u) == 0u) {
+        if (c) atomicAdd(G.counters + GRIS_COUNTER_PRIMARY, (unsigned long long)c);
+        if (e) atomicOr(G.counters + GRIS_COUNTER_ERROR, (unsigned long long)e);
+    }
+}
+
+/* Builder check: one ray per thread. */
+__global__ void k_debug_trace(const uint32_t* nodes, const float* tris, const float* rays, uint64_t n, int anyHit,
+                              float* hitTUV, uint32_t* hitInst, uint32_t* hitTri, unsigned long long* counters) {
+    uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const float* r = rays + i * 8;
+    GrisRayHit h;
+    int err = 0;
+    bool hit = anyHit ? gris_bvh_trace<true>(nodes, tris, r[0], r[1], r[2], r[4], r[5], r[6], r[3], r[7], false, &h, &err, nullptr)
+                      : gris_bvh_trace<false>(nodes, tris, r[0], r[1], r[2], r[4], r[5], r[6], r[3], r[7], false, &h, &err, nullptr);
+    if (hit) { hitTUV[i * 4] = h.t; hitTUV[i * 4 + 1] = h.u; hitTUV[i * 4 + 2] = h.v; hitTUV[i * 4 + 3] = 0.0f; hitInst[i] = h.inst; hitTri[i] = h.tri; }
+    else { hitTUV[i * 4] = -1.0f; hitTUV[i * 4 + 1] = 0.0f; hitTUV[i * 4 + 2] = 0.0f; hitTUV[i * 4 + 3] = 0.0f; hitInst[i] = GRIS_INVALID_HIT; hitTri[i] = GRIS_INVALID_HIT; }
+    if (err) atomicOr(counters + GRIS_COUNTER_ERROR, 1ull);
+}
+
+/* ------------------------------------------------------------------ launchers */
+static CamD make_cam(const GrisCamera& c) {
+    CamD d;
+    d.pos.x = c.pos[0]; d.pos.y = c.pos[1]; d.pos.z = c.pos[2];
+    d.front.x = c.front[0]; d.front.y = c.front[1]; d.front.z = c.front[2];
+    d.right.x = c.right[0]; d.right.y = c.right[1]; d.right.z = c.right[2];
+    d.up.x = c.up[0]; d.up.y = c.up[1]; d.up.z = c.up[2];
+    d.FOV = c.FOV;
+    d.w = c.filmSize[0]; d.h = c.filmSize[1];
+    d.frameIndex = c.frameIndex; d.seed = c.seed;
+    return d;
+}
+
+static DevScene to_dev(const DeviceSceneView& v) {
+    DevScene s;
+    s.vertices = v.vertices; s.nVertices = v.nVertices;
+    s.indices = v.indices; s.nIndices = v.nIndices;
+    s.instances = v.instances; s.nInstances = v.nInstances;
+    s.materials = v.materials; s.nMaterials = v.nMaterials;
+    s.matIndices = v.matIndices; s.nMatIndices = v.nMatIndices;
+    s.lights = v.lights; s.nLights = v.nLights;
+    s.table = v.table; s.nTable = v.nTable;
+    s.nodes = v.nodes; s.tris = v.tris;
+    return s;
+}
+
+cudaError_t launch_gbuffer(const DeviceSceneView& scene, const GrisGBufferBindings& b, const GrisCamera& cam,
+                           unsigned long long* counters, cudaStream_t stream) {
+    GBufCtx G;
+    G.sc = to_dev(scene);
+    G.cam = make_cam(cam);
+    for (int i = 0; i < 16; i++) G.lastProjView[i] = cam.lastProjView[i];
+    G.b = b;
+    G.counters = counters;
+    dim3 block(16, 8), grid((b.width + 15) / 16, (b.height + 7) / 8);
+    k_gbuffer<<<grid, block, 0, stream>>>(G);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_gris(const DeviceSceneView& scene, const GrisPassBindings& b, const GrisCamera& cam,
+                        const GrisCamera& prevCam, const GrisSettings& set, int passes, unsigned long long* counters,
+                        cudaStream_t stream) {
+    PassCtx P;
+    P.sc = to_dev(scene);
+    P.cam = make_cam(cam);
+    P.prev = make_cam(prevCam);
+    P.set = set;
+    P.b = b;
+    P.counters = counters;
+    dim3 block(16, 8), grid((b.width + 15) / 16, (b.height + 7) / 8);
+    if (passes & 1) k_path_trace<<<grid, block, 0, stream>>>(P);
+    if (passes & 2) k_temporal<<<grid, block, 0, stream>>>(P);
+    if (passes & 4) k_spatial<<<grid, block, 0, stream>>>(P);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_debug_trace(const uint32_t* nodes, const float* tris, const float* rays, uint64_t n, int anyHit,
+                               float* hitTUV, uint32_t* hitInst, uint32_t* hitTri, unsigned long long* counters,
+                               cudaStream_t stream) {
+    if (n == 0) return cudaSuccess;
+    k_debug_trace<<<(unsigned)((n + 127) / 128), 128, 0, stream>>>(nodes, tris, rays, n, anyHit, hitTUV, hitInst, hitTri, counters);
+    return cudaGetLastError();
+}
+
+}  // namespace grisrt

@@ -1,0 +1,35 @@
+/*
+ * grisrt_internal.h — internal declarations shared by the grisrt translation units.
+ */
+#ifndef GRISRT_INTERNAL_H
+#define GRISRT_INTERNAL_H
+
+#include <stdint.h>
+
+#include <string>
+#include <vector>
+
+#include "../../include/grisrt.h"
+
+namespace grisrt {
+
+/* Host copy of the 8-wide BVH (layout in bvh_traverse.h). */
+struct BvhHost {
+    std::vector<uint32_t> nodes;   /* GRIS_NODE_WORDS per node */
+    std::vector<float> tris;       /* GRIS_TRI_FLOATS per triangle, in leaf order */
+    uint32_t maxDepth = 0;
+    uint64_t triangleCount = 0;
+    double buildSeconds = 0.0;
+};
+
+/* World-space triangles of the scene as every ray query sees them: light triangles
+ * (instance 0, index = light index) then each object instance k (instance k+1, index = local
+ * triangle), vertex = vec3(transform * vec4(pos, 1)) evaluated column by column. */
+void world_triangles(const GrisSceneDesc& d, std::vector<float>& v012, std::vector<uint32_t>& ids);
+
+/* Builds the BVH; returns false with a message on failure. */
+bool build_bvh(const GrisSceneDesc& d, BvhHost& out, std::string& err);
+
+}  // namespace grisrt
+
+#endif

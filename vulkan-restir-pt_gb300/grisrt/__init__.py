@@ -1,0 +1,393 @@
+"""grisrt — Python bindings (ctypes) over the C ABI in include/grisrt.h.
+
+The library is libgrisrt.so next to this file (built by vulkan-restir-pt_gb300/build.py).
+There is no fallback: every GPU entry point goes to the CUDA kernels, and loading fails
+loudly when the library is missing.
+
+Numpy dtypes below are the reference's std430 layouts (src/shader/layouts.glsl), byte for
+byte, so host arrays pass straight through the ABI.
+"""
+import ctypes
+import os
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_HERE, "libgrisrt.so")
+
+# ---------------------------------------------------------------- layouts (numpy)
+MATERIAL = np.dtype([("baseColor", "<f4", 3), ("type", "<u4"), ("textureIdx", "<u4"), ("metallic", "<f4"),
+                     ("roughness", "<f4"), ("ior", "<f4")])
+VERTEX = np.dtype([("pos", "<f4", 3), ("uvx", "<f4"), ("norm", "<f4", 3), ("uvy", "<f4")])
+INSTANCE = np.dtype([("transform", "<f4", 16), ("transformInv", "<f4", 16), ("transformInvT", "<f4", 16),
+                     ("radiance", "<f4", 3), ("pad0", "<f4"), ("indexOffset", "<u4"), ("indexCount", "<u4"),
+                     ("matIndex", "<u4"), ("pad2", "<f4")])
+LIGHT = np.dtype([("v0", "<f4", 3), ("nx", "<f4"), ("v1", "<f4", 3), ("ny", "<f4"), ("v2", "<f4", 3), ("nz", "<f4"),
+                  ("radiance", "<f4", 3), ("area", "<f4")])
+TABLE = np.dtype([("prob", "<f4"), ("failId", "<u4")])
+RESERVOIR = np.dtype([("bary", "<f4", 2), ("instanceIdx", "<u4"), ("triangleIdx", "<u4"),
+                      ("rcLi", "<f4", 3), ("rcRng", "<u4"), ("rcWi", "<f4", 3), ("flags", "<u4"),
+                      ("pad", "<f4", 2), ("rcPrevSamplePdf", "<f4"), ("rcJacobian", "<f4"),
+                      ("F", "<f4", 3), ("primaryRng", "<u4"),
+                      ("sampleCount", "<f4"), ("resampleWeight", "<f4"), ("contribWeight", "<f4"), ("pad0", "<f4")])
+assert MATERIAL.itemsize == 32 and VERTEX.itemsize == 32 and INSTANCE.itemsize == 224
+assert LIGHT.itemsize == 64 and TABLE.itemsize == 8 and RESERVOIR.itemsize == 96
+
+INVALID_HIT = 0xFFFFFFFF
+CLEAR_FLAG = 0x80000000
+
+
+class Camera(ctypes.Structure):
+    """reference: Camera, layouts.glsl:27-51 (352 B)."""
+    _fields_ = [("view", ctypes.c_float * 16), ("proj", ctypes.c_float * 16), ("projView", ctypes.c_float * 16),
+                ("lastProjView", ctypes.c_float * 16), ("pos", ctypes.c_float * 3), ("FOV", ctypes.c_float),
+                ("angle", ctypes.c_float * 3), ("nearZ", ctypes.c_float), ("front", ctypes.c_float * 3),
+                ("farZ", ctypes.c_float), ("right", ctypes.c_float * 3), ("lensRadius", ctypes.c_float),
+                ("up", ctypes.c_float * 3), ("focalDist", ctypes.c_float), ("filmSize", ctypes.c_uint32 * 2),
+                ("frameIndex", ctypes.c_uint32), ("seed", ctypes.c_uint32)]
+
+    def copy(self):
+        c = Camera()
+        ctypes.memmove(ctypes.byref(c), ctypes.byref(self), ctypes.sizeof(Camera))
+        return c
+
+    def tobytes(self):
+        return bytes(memoryview(self))
+
+
+class Settings(ctypes.Structure):
+    """GRISReSTIR::Settings (src/GRISReSTIR.h:11-17) + the reference's hard-coded constants."""
+    _fields_ = [("shiftType", ctypes.c_uint32), ("rrScale", ctypes.c_float), ("temporalReuse", ctypes.c_uint32),
+                ("spatialReuse", ctypes.c_uint32), ("cap", ctypes.c_uint32), ("maxDepth", ctypes.c_uint32),
+                ("spatialNeighbors", ctypes.c_uint32), ("spatialRadius", ctypes.c_float),
+                ("envRadiance", ctypes.c_float * 3), ("reserved", ctypes.c_uint32 * 5)]
+
+    @classmethod
+    def make(cls, shiftType=2, rrScale=1.0, temporalReuse=True, spatialReuse=True, cap=20, maxDepth=15,
+             spatialNeighbors=3, spatialRadius=20.0):
+        s = cls()
+        s.shiftType, s.rrScale, s.temporalReuse, s.spatialReuse = shiftType, rrScale, int(temporalReuse), int(spatialReuse)
+        s.cap, s.maxDepth, s.spatialNeighbors, s.spatialRadius = cap, maxDepth, spatialNeighbors, spatialRadius
+        return s
+
+
+class SceneDesc(ctypes.Structure):
+    _fields_ = [("vertices", ctypes.c_void_p), ("vertexCount", ctypes.c_uint64),
+                ("indices", ctypes.c_void_p), ("indexCount", ctypes.c_uint64),
+                ("instances", ctypes.c_void_p), ("instanceCount", ctypes.c_uint64),
+                ("materials", ctypes.c_void_p), ("materialCount", ctypes.c_uint64),
+                ("materialIndices", ctypes.c_void_p), ("materialIndexCount", ctypes.c_uint64),
+                ("lights", ctypes.c_void_p), ("lightCount", ctypes.c_uint64),
+                ("lightTable", ctypes.c_void_p), ("lightTableCount", ctypes.c_uint64)]
+
+
+class PassBindings(ctypes.Structure):
+    _fields_ = [("width", ctypes.c_uint32), ("height", ctypes.c_uint32),
+                ("depthNormal", ctypes.c_void_p), ("depthNormalPrev", ctypes.c_void_p),
+                ("albedoMatId", ctypes.c_void_p), ("albedoMatIdPrev", ctypes.c_void_p),
+                ("motion", ctypes.c_void_p), ("reservoirThis", ctypes.c_void_p), ("reservoirPrev", ctypes.c_void_p),
+                ("reservoirTemp", ctypes.c_void_p), ("output", ctypes.c_void_p)]
+
+
+class GBufferBindings(ctypes.Structure):
+    _fields_ = [("width", ctypes.c_uint32), ("height", ctypes.c_uint32), ("depthNormal", ctypes.c_void_p),
+                ("albedoMatId", ctypes.c_void_p), ("motion", ctypes.c_void_p)]
+
+
+class SceneStats(ctypes.Structure):
+    _fields_ = [("triangleCount", ctypes.c_uint64), ("nodeCount", ctypes.c_uint64), ("nodeBytes", ctypes.c_uint64),
+                ("triangleBytes", ctypes.c_uint64), ("maxDepth", ctypes.c_uint32), ("reserved", ctypes.c_uint32),
+                ("buildSeconds", ctypes.c_double)]
+
+
+EXPORTS = [
+    "grisCreate", "grisDestroy", "grisGetError", "grisSync", "grisGetStream", "grisReadCounters", "grisGetVersion",
+    "grisSizeof", "grisBuildLightTable", "grisCameraSetup", "grisCameraLookAt", "grisHostSceneCreate",
+    "grisHostSceneDesc", "grisHostSceneCamera", "grisHostSceneDestroy", "grisSceneCreate", "grisSceneDestroy",
+    "grisSceneGetStats", "grisDebugHostSceneCreate", "grisDebugTraceHost", "grisDebugTraceDevice", "grisPassGBuffer", "grisPassRender",
+    "grisFrameCreate", "grisFrameDestroy", "grisFrameRender", "grisFrameGetBuffer", "grisFrameDownload",
+    "grisFrameUpload",
+]
+
+_lib = None
+
+
+def load(path=None):
+    """Loads libgrisrt.so (raises if it is missing — there is no fallback)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    p = path or LIB_PATH
+    if not os.path.exists(p):
+        raise RuntimeError("libgrisrt.so not found at %s: run vulkan-restir-pt_gb300/build.py" % p)
+    lib = ctypes.CDLL(p)
+    vp, u32, u64, i32 = ctypes.c_void_p, ctypes.c_uint32, ctypes.c_uint64, ctypes.c_int
+    sig = {
+        "grisCreate": (i32, [i32, ctypes.POINTER(vp)]),
+        "grisDestroy": (i32, [vp]),
+        "grisGetError": (ctypes.c_char_p, [vp]),
+        "grisSync": (i32, [vp]),
+        "grisGetStream": (vp, [vp]),
+        "grisReadCounters": (i32, [vp, ctypes.POINTER(u64), i32]),
+        "grisGetVersion": (i32, []),
+        "grisSizeof": (ctypes.c_size_t, [i32]),
+        "grisBuildLightTable": (i32, [vp, u32, vp]),
+        "grisCameraSetup": (i32, [ctypes.POINTER(Camera), vp, vp, ctypes.c_float, u32, u32]),
+        "grisCameraLookAt": (i32, [ctypes.POINTER(Camera), vp, vp, ctypes.c_float, u32, u32]),
+        "grisHostSceneCreate": (i32, [i32, u64, u32, u32, ctypes.POINTER(vp)]),
+        "grisHostSceneDesc": (i32, [vp, ctypes.POINTER(SceneDesc)]),
+        "grisHostSceneCamera": (i32, [vp, u32, u32, u32, u32, ctypes.POINTER(Camera)]),
+        "grisHostSceneDestroy": (i32, [vp]),
+        "grisSceneCreate": (i32, [vp, ctypes.POINTER(SceneDesc), ctypes.POINTER(vp)]),
+        "grisSceneDestroy": (i32, [vp]),
+        "grisSceneGetStats": (i32, [vp, ctypes.POINTER(SceneStats)]),
+        "grisDebugHostSceneCreate": (i32, [ctypes.POINTER(SceneDesc), ctypes.POINTER(vp)]),
+        "grisDebugTraceHost": (i32, [vp, vp, u64, i32, vp, vp, vp]),
+        "grisDebugTraceDevice": (i32, [vp, vp, vp, u64, i32, vp, vp, vp]),
+        "grisPassGBuffer": (i32, [vp, vp, ctypes.POINTER(GBufferBindings), ctypes.POINTER(Camera)]),
+        "grisPassRender": (i32, [vp, vp, ctypes.POINTER(PassBindings), ctypes.POINTER(Camera), ctypes.POINTER(Camera),
+                                 ctypes.POINTER(Settings), i32]),
+        "grisFrameCreate": (i32, [vp, u32, u32, ctypes.POINTER(vp)]),
+        "grisFrameDestroy": (i32, [vp]),
+        "grisFrameRender": (i32, [vp, vp, vp, ctypes.POINTER(Camera), ctypes.POINTER(Camera), ctypes.POINTER(Settings)]),
+        "grisFrameGetBuffer": (i32, [vp, i32, i32, ctypes.POINTER(vp), ctypes.POINTER(ctypes.c_size_t)]),
+        "grisFrameDownload": (i32, [vp, vp, i32, i32, vp, ctypes.c_size_t]),
+        "grisFrameUpload": (i32, [vp, vp, i32, i32, vp, ctypes.c_size_t]),
+    }
+    for name, (res, args) in sig.items():
+        f = getattr(lib, name)
+        f.restype, f.argtypes = res, args
+    _lib = lib
+    return lib
+
+
+class GrisError(RuntimeError):
+    pass
+
+
+def _check(rc, ctx=None, what=""):
+    if rc != 0:
+        msg = ""
+        if ctx is not None:
+            m = load().grisGetError(ctx)
+            msg = m.decode() if m else ""
+        raise GrisError("%s failed (%d): %s" % (what, rc, msg))
+
+
+# ---------------------------------------------------------------- host helpers
+def build_light_table(distribution):
+    d = np.ascontiguousarray(distribution, dtype=np.float32)
+    out = np.zeros(len(d) + 1, dtype=TABLE)
+    _check(load().grisBuildLightTable(d.ctypes.data, len(d), out.ctypes.data), what="grisBuildLightTable")
+    return out
+
+
+def camera_setup(pos, angle, fov, width, height):
+    c = Camera()
+    p = np.asarray(pos, np.float32)
+    a = np.asarray(angle, np.float32)
+    _check(load().grisCameraSetup(ctypes.byref(c), p.ctypes.data, a.ctypes.data, fov, width, height), what="grisCameraSetup")
+    return c
+
+
+class HostScene:
+    """Synthetic scene (kind 0 box, 1 terrain + spheres, 2 glossy terrain) as reference-layout arrays."""
+
+    def __init__(self, kind=0, seed=1, grid=512, spheres=2000):
+        lib = load()
+        h = ctypes.c_void_p()
+        _check(lib.grisHostSceneCreate(kind, seed, grid, spheres, ctypes.byref(h)), what="grisHostSceneCreate")
+        self._h = h
+        d = SceneDesc()
+        _check(lib.grisHostSceneDesc(h, ctypes.byref(d)), what="grisHostSceneDesc")
+
+        def arr(ptr, n, dt):
+            if n == 0:
+                return np.zeros(0, dtype=dt)
+            buf = (ctypes.c_uint8 * (n * np.dtype(dt).itemsize)).from_address(ptr)
+            return np.frombuffer(buf, dtype=dt).copy()
+
+        self.vertices = arr(d.vertices, d.vertexCount, VERTEX)
+        self.indices = arr(d.indices, d.indexCount, np.uint32)
+        self.instances = arr(d.instances, d.instanceCount, INSTANCE)
+        self.materials = arr(d.materials, d.materialCount, MATERIAL)
+        self.material_indices = arr(d.materialIndices, d.materialIndexCount, np.int32)
+        self.lights = arr(d.lights, d.lightCount, LIGHT)
+        self.light_table = arr(d.lightTable, d.lightTableCount, TABLE)
+
+    def camera(self, frame, frames, width, height):
+        c = Camera()
+        _check(load().grisHostSceneCamera(self._h, frame, frames, width, height, ctypes.byref(c)), what="grisHostSceneCamera")
+        return c
+
+    def desc(self):
+        d = SceneDesc()
+        d.vertices, d.vertexCount = self.vertices.ctypes.data, len(self.vertices)
+        d.indices, d.indexCount = self.indices.ctypes.data, len(self.indices)
+        d.instances, d.instanceCount = self.instances.ctypes.data, len(self.instances)
+        d.materials, d.materialCount = self.materials.ctypes.data, len(self.materials)
+        d.materialIndices, d.materialIndexCount = self.material_indices.ctypes.data, len(self.material_indices)
+        d.lights, d.lightCount = self.lights.ctypes.data, len(self.lights)
+        d.lightTable, d.lightTableCount = self.light_table.ctypes.data, len(self.light_table)
+        return d
+
+    def arrays(self):
+        return (self.vertices, self.indices, self.instances, self.materials, self.material_indices, self.lights,
+                self.light_table)
+
+    def triangle_count(self):
+        return len(self.lights) + int(sum(int(i["indexCount"]) // 3 for i in self.instances))
+
+    def __del__(self):
+        if getattr(self, "_h", None) and _lib is not None:
+            _lib.grisHostSceneDestroy(self._h)
+            self._h = None
+
+
+def frame_seed(base, frame):
+    """Per-frame camera seed (the reference draws it from std::default_random_engine in
+    Camera::nextFrame, src/Camera.cpp:68-72; here a splitmix64 stream of the config seed)."""
+    z = (int(base) * 0x9E3779B97F4A7C15 + (frame + 1) * 0xBF58476D1CE4E5B9) & 0xFFFFFFFFFFFFFFFF
+    z = ((z ^ (z >> 30)) * 0xBF58476D1CE4E5B9) & 0xFFFFFFFFFFFFFFFF
+    z = ((z ^ (z >> 27)) * 0x94D049BB133111EB) & 0xFFFFFFFFFFFFFFFF
+    return (z ^ (z >> 31)) >> 32
+
+
+def sequence_cameras(host_scene, frames, width, height, seed=1, accumulate=False, orbit_frames=None):
+    """Cameras of a frame sequence with the renderer's per-frame fields
+    (src/Renderer.cpp:358-363, 654-660; src/Camera.cpp:68-98):
+      seed         drawn per frame;
+      frameIndex   clear flag on the first frame (no previous reservoirs), then 0 — or the
+                   frame count when accumulating (running mean over frames);
+      lastProjView the previous frame's projView (motion vectors);
+      prev camera  the camera of the previous frame.
+    Returns (cams, prevs)."""
+    cams, prevs = [], []
+    n = orbit_frames or frames
+    for f in range(frames):
+        c = host_scene.camera(f, n, width, height)
+        c.seed = frame_seed(seed, f)
+        if f > 0:
+            ctypes.memmove(c.lastProjView, cams[f - 1].projView, 64)
+        c.frameIndex = f if accumulate else (CLEAR_FLAG if f == 0 else 0)
+        if accumulate and f == 0:
+            c.frameIndex = CLEAR_FLAG
+        cams.append(c)
+        prevs.append(cams[f - 1].copy() if f > 0 else c.copy())
+    return cams, prevs
+
+
+# ---------------------------------------------------------------- device side
+class Context:
+    def __init__(self, device=0):
+        lib = load()
+        h = ctypes.c_void_p()
+        _check(lib.grisCreate(device, ctypes.byref(h)), what="grisCreate")
+        self.h = h
+
+    def check(self, rc, what):
+        _check(rc, self.h, what)
+
+    def sync(self):
+        self.check(load().grisSync(self.h), "grisSync")
+
+    def stream(self):
+        return load().grisGetStream(self.h)
+
+    def counters(self, reset=False):
+        out = (ctypes.c_uint64 * 4)()
+        self.check(load().grisReadCounters(self.h, out, int(reset)), "grisReadCounters")
+        return list(out)
+
+    def close(self):
+        if self.h:
+            load().grisDestroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class Scene:
+    def __init__(self, ctx, host_scene):
+        self.ctx = ctx
+        self.host = host_scene
+        self._desc = host_scene.desc()
+        h = ctypes.c_void_p()
+        ctx.check(load().grisSceneCreate(ctx.h, ctypes.byref(self._desc), ctypes.byref(h)), "grisSceneCreate")
+        self.h = h
+
+    def stats(self):
+        s = SceneStats()
+        self.ctx.check(load().grisSceneGetStats(self.h, ctypes.byref(s)), "grisSceneGetStats")
+        return s
+
+    def trace_host(self, rays, any_hit=False):
+        rays = np.ascontiguousarray(rays, dtype=np.float32).reshape(-1, 8)
+        n = len(rays)
+        tuv = np.zeros((n, 4), np.float32)
+        inst = np.zeros(n, np.uint32)
+        tri = np.zeros(n, np.uint32)
+        rc = load().grisDebugTraceHost(self.h, rays.ctypes.data, n, int(any_hit), tuv.ctypes.data, inst.ctypes.data,
+                                       tri.ctypes.data)
+        _check(rc, what="grisDebugTraceHost")
+        return tuv, inst, tri
+
+    def close(self):
+        if self.h:
+            load().grisSceneDestroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+BUF_DEPTH_NORMAL, BUF_ALBEDO_MATID, BUF_MOTION, BUF_RESERVOIR, BUF_TEMP, BUF_OUTPUT = range(6)
+_BUF_DTYPE = {0: (np.float32, 4), 1: (np.uint32, 2), 2: (np.uint16, 2), 3: (RESERVOIR, None),
+              4: (RESERVOIR, None), 5: (np.float32, 4)}
+
+
+class Frame:
+    """Library-owned frame resources with the renderer's ping-pong (grisFrame*)."""
+
+    def __init__(self, ctx, width, height):
+        self.ctx, self.w, self.h = ctx, width, height
+        h = ctypes.c_void_p()
+        ctx.check(load().grisFrameCreate(ctx.h, width, height, ctypes.byref(h)), "grisFrameCreate")
+        self.handle = h
+
+    def render(self, scene, cam, prev_cam, settings):
+        self.ctx.check(load().grisFrameRender(self.ctx.h, scene.h, self.handle, ctypes.byref(cam), ctypes.byref(prev_cam),
+                                              ctypes.byref(settings)), "grisFrameRender")
+
+    def device_ptr(self, which, slot=0):
+        p = ctypes.c_void_p()
+        n = ctypes.c_size_t()
+        self.ctx.check(load().grisFrameGetBuffer(self.handle, which, slot, ctypes.byref(p), ctypes.byref(n)),
+                       "grisFrameGetBuffer")
+        return p.value, n.value
+
+    def download(self, which, slot=0):
+        dt, ch = _BUF_DTYPE[which]
+        n = self.w * self.h
+        arr = np.zeros((n, ch) if ch else n, dtype=dt)
+        self.ctx.check(load().grisFrameDownload(self.ctx.h, self.handle, which, slot, arr.ctypes.data, arr.nbytes),
+                       "grisFrameDownload")
+        return arr
+
+    def close(self):
+        if self.handle:
+            load().grisFrameDestroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
