@@ -203,6 +203,14 @@ int grisSync(GrisContext* ctx);
 void* grisGetStream(GrisContext* ctx);                    /* cudaStream_t */
 int grisReadCounters(GrisContext* ctx, uint64_t out[4], int reset);
 int grisGetVersion(void);
+/* Per-kernel timing (CUDA events around every launch on the context stream while enabled).
+ * Kernels: 0 G-buffer, 1 path trace, 2 temporal reuse, 3 spatial reuse + final shading. */
+int grisSetProfiling(GrisContext* ctx, int enable);
+int grisReadProfile(GrisContext* ctx, double msTotal[4], uint64_t launches[4], int reset);
+/* Traversal work per kernel while enabled: BVH nodes intersected, triangles tested and
+ * closest-hit rays (primary rays for the G-buffer); shadow rays are in grisReadCounters. */
+int grisSetWorkCounting(GrisContext* ctx, int enable);
+int grisReadWorkCounters(GrisContext* ctx, uint64_t nodes[4], uint64_t tris[4], uint64_t closestRays[4], int reset);
 size_t grisSizeof(int which);   /* 0 camera, 1 reservoir, 2 material, 3 vertex, 4 instance, 5 light, 6 table entry, 7 settings */
 
 /* ---------------------------------------------------------------- host helpers (no GPU) */

@@ -27,6 +27,8 @@
 #include <algorithm>
 #include <vector>
 
+#include <omp.h>
+
 #include "detmath.h"
 
 namespace oracle {
@@ -101,6 +103,7 @@ struct Scene {
 };
 static Scene g;
 static unsigned long long g_counts[4];
+static int g_row0 = 0, g_row1 = 1 << 30;   /* rows processed by the passes (a bounded CPU sample) */
 
 template <typename T> static inline T at(const std::vector<T>& v, uint64_t i) {
     if (i < v.size()) return v[i];
@@ -957,6 +960,17 @@ int oracle_scene_set(void* vertices, unsigned long long nv, void* indices, unsig
 
 void oracle_set_traversal(int useBvh) { g.useBvh = useBvh; }
 
+/* Restricts the G-buffer and the three passes to rows [y0, y1) (a bounded sample of a frame). */
+void oracle_set_rows(int y0, int y1) { g_row0 = y0; g_row1 = y1; }
+
+int oracle_threads(void) {
+    int n = 1;
+#pragma omp parallel
+#pragma omp single
+    n = omp_get_num_threads();
+    return n;
+}
+
 void oracle_counters(unsigned long long* out, int reset) {
     for (int i = 0; i < 4; i++) { out[i] = g_counts[i]; if (reset) g_counts[i] = 0; }
 }
@@ -982,8 +996,9 @@ void oracle_trace(const float* rays, unsigned long long n, int anyHit, float* tu
 /* G-buffer (GBuffer.vert:16-28 / GBuffer.frag:21-54 restated as a ray cast without the lights) */
 void oracle_gbuffer(const void* camera, uint32_t W, uint32_t H, float* dn, uint32_t* am, uint16_t* mv) {
     Camera cam; memcpy(&cam, camera, sizeof(cam));
+    int y0 = std::max(0, g_row0), y1 = std::min((int)H, g_row1);
 #pragma omp parallel for schedule(dynamic, 4)
-    for (int y = 0; y < (int)H; y++)
+    for (int y = y0; y < y1; y++)
         for (int x = 0; x < (int)W; x++) {
             size_t p = (size_t)y * W + x;
             F2 uv = pixelUV(x, y, (int)W, (int)H);
@@ -1038,18 +1053,19 @@ void oracle_gris_frame(const void* camera, const void* prevCamera, const void* s
     P.motion.resize(P.n * 2);
     for (uint64_t i = 0; i < P.n * 2; i++) P.motion[i] = fromHalf(motion[i]);
     P.self = (Reservoir*)resvThis; P.previous = (Reservoir*)resvPrev; P.temp = (Reservoir*)resvTemp;
+    int y0 = std::max(0, g_row0), y1 = std::min(P.H, g_row1);
     if (passes & 1) {
 #pragma omp parallel for schedule(dynamic, 2)
-        for (int y = 0; y < P.H; y++) for (int x = 0; x < P.W; x++) pathTracePixel(P, x, y);
+        for (int y = y0; y < y1; y++) for (int x = 0; x < P.W; x++) pathTracePixel(P, x, y);
     }
     if (passes & 2) {
 #pragma omp parallel for schedule(dynamic, 2)
-        for (int y = 0; y < P.H; y++) for (int x = 0; x < P.W; x++) temporalPixel(P, x, y);
+        for (int y = y0; y < y1; y++) for (int x = 0; x < P.W; x++) temporalPixel(P, x, y);
     }
     if (passes & 4) {
         float n = (float)(P.cam.frameIndex & 0x7fffffffu);
 #pragma omp parallel for schedule(dynamic, 2)
-        for (int y = 0; y < P.H; y++)
+        for (int y = y0; y < y1; y++)
             for (int x = 0; x < P.W; x++) {
                 F3 c = spatialPixel(P, x, y);
                 float* o = output + ((size_t)y * P.W + x) * 4;

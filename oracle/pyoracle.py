@@ -52,6 +52,14 @@ class CpuImpl:
             f.argtypes = [ctypes.c_int]
             f(int(use_bvh))
 
+    def set_rows(self, y0, y1):
+        f = self.lib.oracle_set_rows
+        f.argtypes = [ctypes.c_int, ctypes.c_int]
+        f(int(y0), int(y1))
+
+    def threads(self):
+        return int(self.lib.oracle_threads())
+
     def read_counters(self, reset=True):
         out = (ctypes.c_ulonglong * 4)()
         self.counters(out, int(reset))

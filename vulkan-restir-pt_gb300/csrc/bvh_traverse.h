@@ -42,6 +42,11 @@ struct GrisRayHit {
     uint32_t inst, tri;
 };
 
+/* Work done by one or more traversals: nodes intersected, triangles tested. */
+struct GrisWork {
+    uint32_t nodes, tris;
+};
+
 GRIS_HD float gris_fma(float a, float b, float c) {
 #ifdef __CUDA_ARCH__
     return __fmaf_rn(a, b, c);
@@ -125,7 +130,7 @@ template <bool ANY>
 GRIS_HD bool gris_bvh_trace(const uint32_t* __restrict__ nodes, const float* __restrict__ tris,
                             float ox, float oy, float oz, float dx, float dy, float dz,
                             float tmin, float tmax, bool skipInst0, GrisRayHit* hit, int* err,
-                            uint32_t* nodeVisits) {
+                            GrisWork* work) {
     const float tiny = 1e-30f;
     float idx = 1.0f / ((dx > tiny || dx < -tiny) ? dx : (dx < 0.0f ? -tiny : tiny));
     float idy = 1.0f / ((dy > tiny || dy < -tiny) ? dy : (dy < 0.0f ? -tiny : tiny));
@@ -142,7 +147,7 @@ GRIS_HD bool gris_bvh_trace(const uint32_t* __restrict__ nodes, const float* __r
     uint32_t grpBase = 0, grpHits = 0, grpImask = 0;
     uint32_t nodeIdx = 0;
     bool haveNode = true;
-    uint32_t visits = 0;
+    uint32_t visits = 0, tests = 0;
 
     while (true) {
         if (haveNode) {
@@ -204,11 +209,12 @@ GRIS_HD bool gris_bvh_trace(const uint32_t* __restrict__ nodes, const float* __r
 #endif
                 uint32_t inst = gris_f2u(TT[3]), tri = gris_f2u(TT[7]);
                 if (skipInst0 && inst == 0u) continue;
+                tests++;
                 float t, u, v;
                 if (!gris_tri_test(TT, ox, oy, oz, dx, dy, dz, tmin, bestT, &t, &u, &v)) continue;
                 if (ANY) {
                     hit->t = t; hit->u = u; hit->v = v; hit->inst = inst; hit->tri = tri;
-                    if (nodeVisits) *nodeVisits += visits;
+                    if (work) { work->nodes += visits; work->tris += tests; }
                     return true;
                 }
                 /* t <= bestT here (the test used bestT as tmax) */
@@ -238,7 +244,7 @@ GRIS_HD bool gris_bvh_trace(const uint32_t* __restrict__ nodes, const float* __r
         nodeIdx = grpBase + (uint32_t)gris_popc(grpImask & ((1u << slot) - 1u));
         haveNode = true;
     }
-    if (nodeVisits) *nodeVisits += visits;
+    if (work) { work->nodes += visits; work->tris += tests; }
     if (found) { hit->t = bestT; hit->u = bestU; hit->v = bestV; hit->inst = bestInst; hit->tri = bestTri; }
     return found;
 }

@@ -26,11 +26,59 @@ static_assert(sizeof(GrisCamera) == 352, "Camera is 352 B");
 static_assert(sizeof(GrisReservoir) == 96, "GRISReservoir is 96 B");
 static_assert(sizeof(GrisSettings) == 64, "GrisSettings is 64 B");
 
+/* Per-kernel CUDA-event timing of every launch while enabled (events recorded on the
+ * launch stream around each kernel; read back and summed on request). */
+struct Profiler : grisrt::KernelTimer {
+    bool enabled = false;
+    struct Pair { cudaEvent_t a, b; int kernel; };
+    std::vector<Pair> pending, free;
+    double ms[4] = {0, 0, 0, 0};
+    uint64_t launches[4] = {0, 0, 0, 0};
+    Pair open{};
+    void mark(int kernel, bool begin, cudaStream_t stream) override {
+        if (!enabled) return;
+        if (begin) {
+            if (free.empty()) {
+                Pair p{};
+                cudaEventCreate(&p.a);
+                cudaEventCreate(&p.b);
+                free.push_back(p);
+            }
+            open = free.back();
+            free.pop_back();
+            open.kernel = kernel;
+            cudaEventRecord(open.a, stream);
+        } else {
+            cudaEventRecord(open.b, stream);
+            pending.push_back(open);
+        }
+    }
+    void collect() {
+        for (Pair& p : pending) {
+            float t = 0.0f;
+            cudaEventSynchronize(p.b);
+            cudaEventElapsedTime(&t, p.a, p.b);
+            ms[p.kernel] += t;
+            launches[p.kernel]++;
+            free.push_back(p);
+        }
+        pending.clear();
+    }
+    ~Profiler() override {
+        for (Pair& p : pending) { cudaEventDestroy(p.a); cudaEventDestroy(p.b); }
+        for (Pair& p : free) { cudaEventDestroy(p.a); cudaEventDestroy(p.b); }
+    }
+};
+
+#define GRIS_NUM_COUNTERS 32
+
 struct GrisContext {
     int device = 0;
     cudaStream_t stream = nullptr;
     unsigned long long* dCounters = nullptr;
     unsigned long long* hCounters = nullptr;   /* pinned */
+    int countWork = 0;
+    Profiler prof;
     std::string err;
 };
 
@@ -113,9 +161,9 @@ int grisCreate(int device, GrisContext** out) {
     GrisContext* ctx = new GrisContext();
     ctx->device = device;
     if (cudaSetDevice(device) != cudaSuccess || cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking) != cudaSuccess ||
-        cudaMalloc(&ctx->dCounters, 8 * sizeof(unsigned long long)) != cudaSuccess ||
-        cudaMallocHost(&ctx->hCounters, 8 * sizeof(unsigned long long)) != cudaSuccess ||
-        cudaMemset(ctx->dCounters, 0, 8 * sizeof(unsigned long long)) != cudaSuccess) {
+        cudaMalloc(&ctx->dCounters, GRIS_NUM_COUNTERS * sizeof(unsigned long long)) != cudaSuccess ||
+        cudaMallocHost(&ctx->hCounters, GRIS_NUM_COUNTERS * sizeof(unsigned long long)) != cudaSuccess ||
+        cudaMemset(ctx->dCounters, 0, GRIS_NUM_COUNTERS * sizeof(unsigned long long)) != cudaSuccess) {
         delete ctx;
         return GRIS_ERR_CUDA;
     }
@@ -145,6 +193,45 @@ int grisReadCounters(GrisContext* ctx, uint64_t out[4], int reset) {
     if (reset) GRIS_CK(ctx, cudaMemsetAsync(ctx->dCounters, 0, 4 * sizeof(unsigned long long), ctx->stream));
     GRIS_CK(ctx, cudaStreamSynchronize(ctx->stream));
     for (int i = 0; i < 4; i++) out[i] = ctx->hCounters[i];
+    return GRIS_OK;
+}
+
+int grisSetProfiling(GrisContext* ctx, int enable) {
+    if (!ctx) return GRIS_ERR_INVALID_ARGUMENT;
+    ctx->prof.enabled = enable != 0;
+    return GRIS_OK;
+}
+
+int grisReadProfile(GrisContext* ctx, double msTotal[4], uint64_t launches[4], int reset) {
+    if (!ctx || !msTotal || !launches) return GRIS_ERR_INVALID_ARGUMENT;
+    cudaSetDevice(ctx->device);
+    ctx->prof.collect();
+    for (int k = 0; k < 4; k++) {
+        msTotal[k] = ctx->prof.ms[k];
+        launches[k] = ctx->prof.launches[k];
+        if (reset) { ctx->prof.ms[k] = 0.0; ctx->prof.launches[k] = 0; }
+    }
+    return GRIS_OK;
+}
+
+int grisSetWorkCounting(GrisContext* ctx, int enable) {
+    if (!ctx) return GRIS_ERR_INVALID_ARGUMENT;
+    ctx->countWork = enable != 0;
+    return GRIS_OK;
+}
+
+int grisReadWorkCounters(GrisContext* ctx, uint64_t nodes[4], uint64_t tris[4], uint64_t rays[4], int reset) {
+    if (!ctx || !nodes || !tris || !rays) return GRIS_ERR_INVALID_ARGUMENT;
+    cudaSetDevice(ctx->device);
+    GRIS_CK(ctx, cudaMemcpyAsync(ctx->hCounters + 8, ctx->dCounters + 8, 16 * sizeof(unsigned long long),
+                                 cudaMemcpyDeviceToHost, ctx->stream));
+    if (reset) GRIS_CK(ctx, cudaMemsetAsync(ctx->dCounters + 8, 0, 16 * sizeof(unsigned long long), ctx->stream));
+    GRIS_CK(ctx, cudaStreamSynchronize(ctx->stream));
+    for (int k = 0; k < 4; k++) {
+        nodes[k] = ctx->hCounters[8 + 2 * k];
+        tris[k] = ctx->hCounters[9 + 2 * k];
+        rays[k] = ctx->hCounters[16 + k];
+    }
     return GRIS_OK;
 }
 
@@ -275,7 +362,7 @@ int grisPassGBuffer(GrisContext* ctx, const GrisScene* s, const GrisGBufferBindi
     if (cam->filmSize[0] != b->width || cam->filmSize[1] != b->height)
         return fail(ctx, GRIS_ERR_INVALID_ARGUMENT, "camera filmSize differs from the bound extent");
     cudaSetDevice(ctx->device);
-    GRIS_CK(ctx, grisrt::launch_gbuffer(scene_view(s), *b, *cam, ctx->dCounters, ctx->stream));
+    GRIS_CK(ctx, grisrt::launch_gbuffer(scene_view(s), *b, *cam, ctx->dCounters, ctx->countWork, &ctx->prof, ctx->stream));
     return GRIS_OK;
 }
 
@@ -291,7 +378,8 @@ int grisPassRender(GrisContext* ctx, const GrisScene* s, const GrisPassBindings*
     if (set->maxDepth == 0 || set->maxDepth > 255) return fail(ctx, GRIS_ERR_INVALID_ARGUMENT, "maxDepth must be 1..255");
     if (set->spatialNeighbors > 64) return fail(ctx, GRIS_ERR_INVALID_ARGUMENT, "spatialNeighbors must be <= 64");
     cudaSetDevice(ctx->device);
-    GRIS_CK(ctx, grisrt::launch_gris(scene_view(s), *b, *cam, *prevCam, *set, passes & 7, ctx->dCounters, ctx->stream));
+    GRIS_CK(ctx, grisrt::launch_gris(scene_view(s), *b, *cam, *prevCam, *set, passes & 7, ctx->dCounters, ctx->countWork,
+                                     &ctx->prof, ctx->stream));
     return GRIS_OK;
 }
 

@@ -26,16 +26,24 @@ struct PassCtx {
     GrisSettings set;
     GrisPassBindings b;
     unsigned long long* counters;
+    int countWork;
 };
 
 /* ------------------------------------------------------------------ ray queries */
-struct RayCount { uint32_t closest, shadow; };
+/* Per-thread ray counts, plus traversal work when the pass counts it (ctx work counting). */
+struct RayCount { uint32_t closest, shadow; GrisWork work; };
+
+GD RayCount ray_count() {
+    RayCount rc;
+    rc.closest = 0u; rc.shadow = 0u; rc.work.nodes = 0u; rc.work.tris = 0u;
+    return rc;
+}
 
 GD Isec traceClosestHit(const DevScene& sc, V3 o, V3 d, float tmin, float tmax, RayCount& rc, int& err) {
     rc.closest++;
     GrisRayHit h;
     Isec r;
-    if (gris_bvh_trace<false>(sc.nodes, sc.tris, o.x, o.y, o.z, d.x, d.y, d.z, tmin, tmax, false, &h, &err, nullptr)) {
+    if (gris_bvh_trace<false>(sc.nodes, sc.tris, o.x, o.y, o.z, d.x, d.y, d.z, tmin, tmax, false, &h, &err, &rc.work)) {
         r.bx = h.u; r.by = h.v; r.inst = h.inst; r.tri = h.tri;
     } else {
         r.bx = 0.0f; r.by = 0.0f; r.inst = kInvalidHit; r.tri = 0u;
@@ -45,21 +53,34 @@ GD Isec traceClosestHit(const DevScene& sc, V3 o, V3 d, float tmin, float tmax, 
 GD bool traceShadow(const DevScene& sc, V3 o, float tmin, V3 d, float tmax, RayCount& rc, int& err) {
     rc.shadow++;
     GrisRayHit h;
-    return gris_bvh_trace<true>(sc.nodes, sc.tris, o.x, o.y, o.z, d.x, d.y, d.z, tmin, tmax, false, &h, &err, nullptr);
+    return gris_bvh_trace<true>(sc.nodes, sc.tris, o.x, o.y, o.z, d.x, d.y, d.z, tmin, tmax, false, &h, &err, &rc.work);
 }
 /* ray_query.glsl:29-39 */
 GD bool traceVisibility(const DevScene& sc, V3 from, V3 to, RayCount& rc, int& err) {
     return !traceShadow(sc, from, kMinRayDistance, normalize3(to - from), distance3(to, from) - kMinRayDistance, rc, err);
 }
 
-GD void flush_counts(unsigned long long* counters, const RayCount& rc, int err) {
+/* counters: [0] closest, [1] shadow, [2] primary, [3] error word,
+ * [8+2k] nodes and [9+2k] triangles of kernel k, [16+k] closest-hit rays of kernel k
+ * (k: 0 G-buffer, 1 path trace, 2 temporal, 3 spatial). */
+GD void flush_counts(unsigned long long* counters, const RayCount& rc, int err, int kernel, int countWork) {
     unsigned int c = __reduce_add_sync(0xffffffffu, rc.closest);
     unsigned int s = __reduce_add_sync(0xffffffffu, rc.shadow);
     unsigned int e = __reduce_or_sync(0xffffffffu, (unsigned)err);
+    unsigned long long nodes = 0, tris = 0;
+    if (countWork) {
+        nodes = __reduce_add_sync(0xffffffffu, rc.work.nodes);
+        tris = __reduce_add_sync(0xffffffffu, rc.work.tris);
+    }
     if (((threadIdx.y * blockDim.x + threadIdx.x) & 31u) == 0u) {
         if (c) atomicAdd(counters + GRIS_COUNTER_CLOSEST, (unsigned long long)c);
         if (s) atomicAdd(counters + GRIS_COUNTER_SHADOW, (unsigned long long)s);
         if (e) atomicOr(counters + GRIS_COUNTER_ERROR, (unsigned long long)e);
+        if (countWork) {
+            atomicAdd(counters + 8 + 2 * kernel, nodes);
+            atomicAdd(counters + 9 + 2 * kernel, tris);
+            atomicAdd(counters + 16 + kernel, (unsigned long long)c);
+        }
     }
 }
 
@@ -524,23 +545,23 @@ GD V3 spatialReuse(const PassCtx& P, uint32_t ix, uint32_t iy, RayCount& rc, int
 /* ------------------------------------------------------------------ kernels */
 __global__ void __launch_bounds__(128) k_path_trace(PassCtx P) {
     uint32_t x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y * blockDim.y + threadIdx.y;
-    RayCount rc = {0u, 0u};
+    RayCount rc = ray_count();
     int err = 0;
     if (x < P.b.width && y < P.b.height) tracePath(P, x, y, rc, err);
-    flush_counts(P.counters, rc, err);
+    flush_counts(P.counters, rc, err, 1, P.countWork);
 }
 
 __global__ void __launch_bounds__(128) k_temporal(PassCtx P) {
     uint32_t x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y * blockDim.y + threadIdx.y;
-    RayCount rc = {0u, 0u};
+    RayCount rc = ray_count();
     int err = 0;
     if (x < P.b.width && y < P.b.height) temporalReuse(P, x, y, rc, err);
-    flush_counts(P.counters, rc, err);
+    flush_counts(P.counters, rc, err, 2, P.countWork);
 }
 
 __global__ void __launch_bounds__(128) k_spatial(PassCtx P) {
     uint32_t x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y * blockDim.y + threadIdx.y;
-    RayCount rc = {0u, 0u};
+    RayCount rc = ray_count();
     int err = 0;
     if (x < P.b.width && y < P.b.height) {
         bool wrote;
@@ -553,7 +574,7 @@ __global__ void __launch_bounds__(128) k_spatial(PassCtx P) {
         acc = (acc * frameCount + color) / (frameCount + 1.0f);
         *out = make_float4(acc.x, acc.y, acc.z, 1.0f);
     }
-    flush_counts(P.counters, rc, err);
+    flush_counts(P.counters, rc, err, 3, P.countWork);
 }
 
 /* G-buffer (GBuffer.vert:16-28, GBuffer.frag:21-54) by primary rays that ignore instance 0. */
@@ -563,6 +584,7 @@ struct GBufCtx {
     float lastProjView[16];
     GrisGBufferBindings b;
     unsigned long long* counters;
+    int countWork;
 };
 
 GD uint32_t packUnorm1(float c) { return (uint32_t)floorf(fminf(fmaxf(c, 0.0f), 1.0f) * 255.0f + 0.5f); }
@@ -571,6 +593,7 @@ __global__ void __launch_bounds__(128) k_gbuffer(GBufCtx G) {
     uint32_t x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y * blockDim.y + threadIdx.y;
     int err = 0;
     uint32_t primary = 0;
+    GrisWork work; work.nodes = 0u; work.tris = 0u;
     if (x < G.b.width && y < G.b.height) {
         const DevScene& sc = G.sc;
         uint64_t p = (uint64_t)y * G.b.width + x;
@@ -579,7 +602,8 @@ __global__ void __launch_bounds__(128) k_gbuffer(GBufCtx G) {
         GrisRayHit h;
         primary = 1;
         bool hit = gris_bvh_trace<false>(sc.nodes, sc.tris, ray.ori.x, ray.ori.y, ray.ori.z, ray.dir.x, ray.dir.y,
-                                          ray.dir.z, kMinRayDistance, kMaxRayDistance, true, &h, &err, nullptr);
+                                          ray.dir.z, kMinRayDistance, kMaxRayDistance, true, &h, &err,
+                                          &work);
         float4* dnOut = reinterpret_cast<float4*>(G.b.depthNormal) + p;
         uint2* amOut = reinterpret_cast<uint2*>(G.b.albedoMatId) + p;
         __half2* mvOut = reinterpret_cast<__half2*>(G.b.motion) + p;
@@ -628,9 +652,19 @@ __global__ void __launch_bounds__(128) k_gbuffer(GBufCtx G) {
     }
     unsigned int c = __reduce_add_sync(0xffffffffu, primary);
     unsigned int e = __reduce_or_sync(0xffffffffu, (unsigned)err);
+    unsigned long long nodes = 0, tris = 0;
+    if (G.countWork) {
+        nodes = __reduce_add_sync(0xffffffffu, work.nodes);
+        tris = __reduce_add_sync(0xffffffffu, work.tris);
+    }
     if (((threadIdx.y * blockDim.x + threadIdx.x) & 31u) == 0u) {
         if (c) atomicAdd(G.counters + GRIS_COUNTER_PRIMARY, (unsigned long long)c);
         if (e) atomicOr(G.counters + GRIS_COUNTER_ERROR, (unsigned long long)e);
+        if (G.countWork) {
+            atomicAdd(G.counters + 8, nodes);
+            atomicAdd(G.counters + 9, tris);
+            atomicAdd(G.counters + 16, (unsigned long long)c);
+        }
     }
 }
 
@@ -676,22 +710,26 @@ static DevScene to_dev(const DeviceSceneView& v) {
 }
 
 cudaError_t launch_gbuffer(const DeviceSceneView& scene, const GrisGBufferBindings& b, const GrisCamera& cam,
-                           unsigned long long* counters, cudaStream_t stream) {
+                           unsigned long long* counters, int countWork, KernelTimer* timer, cudaStream_t stream) {
     GBufCtx G;
+    G.countWork = countWork;
     G.sc = to_dev(scene);
     G.cam = make_cam(cam);
     for (int i = 0; i < 16; i++) G.lastProjView[i] = cam.lastProjView[i];
     G.b = b;
     G.counters = counters;
     dim3 block(16, 8), grid((b.width + 15) / 16, (b.height + 7) / 8);
+    if (timer) timer->mark(0, true, stream);
     k_gbuffer<<<grid, block, 0, stream>>>(G);
+    if (timer) timer->mark(0, false, stream);
     return cudaGetLastError();
 }
 
 cudaError_t launch_gris(const DeviceSceneView& scene, const GrisPassBindings& b, const GrisCamera& cam,
                         const GrisCamera& prevCam, const GrisSettings& set, int passes, unsigned long long* counters,
-                        cudaStream_t stream) {
+                        int countWork, KernelTimer* timer, cudaStream_t stream) {
     PassCtx P;
+    P.countWork = countWork;
     P.sc = to_dev(scene);
     P.cam = make_cam(cam);
     P.prev = make_cam(prevCam);
@@ -699,9 +737,21 @@ cudaError_t launch_gris(const DeviceSceneView& scene, const GrisPassBindings& b,
     P.b = b;
     P.counters = counters;
     dim3 block(16, 8), grid((b.width + 15) / 16, (b.height + 7) / 8);
-    if (passes & 1) k_path_trace<<<grid, block, 0, stream>>>(P);
-    if (passes & 2) k_temporal<<<grid, block, 0, stream>>>(P);
-    if (passes & 4) k_spatial<<<grid, block, 0, stream>>>(P);
+    if (passes & 1) {
+        if (timer) timer->mark(1, true, stream);
+        k_path_trace<<<grid, block, 0, stream>>>(P);
+        if (timer) timer->mark(1, false, stream);
+    }
+    if (passes & 2) {
+        if (timer) timer->mark(2, true, stream);
+        k_temporal<<<grid, block, 0, stream>>>(P);
+        if (timer) timer->mark(2, false, stream);
+    }
+    if (passes & 4) {
+        if (timer) timer->mark(3, true, stream);
+        k_spatial<<<grid, block, 0, stream>>>(P);
+        if (timer) timer->mark(3, false, stream);
+    }
     return cudaGetLastError();
 }
 

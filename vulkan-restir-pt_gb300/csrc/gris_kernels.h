@@ -24,11 +24,18 @@ struct DeviceSceneView {
     const float* tris;
 };
 
+/* Receives a mark before (begin = true) and after each kernel launch, on the launch stream. */
+struct KernelTimer {
+    virtual void mark(int kernel, bool begin, cudaStream_t stream) = 0;
+    virtual ~KernelTimer() {}
+};
+
+/* kernels: 0 G-buffer, 1 path trace, 2 temporal reuse, 3 spatial reuse */
 cudaError_t launch_gbuffer(const DeviceSceneView& scene, const GrisGBufferBindings& b, const GrisCamera& cam,
-                           unsigned long long* counters, cudaStream_t stream);
+                           unsigned long long* counters, int countWork, KernelTimer* timer, cudaStream_t stream);
 cudaError_t launch_gris(const DeviceSceneView& scene, const GrisPassBindings& b, const GrisCamera& cam,
                         const GrisCamera& prevCam, const GrisSettings& set, int passes, unsigned long long* counters,
-                        cudaStream_t stream);
+                        int countWork, KernelTimer* timer, cudaStream_t stream);
 cudaError_t launch_debug_trace(const uint32_t* nodes, const float* tris, const float* rays, uint64_t n, int anyHit,
                                float* hitTUV, uint32_t* hitInst, uint32_t* hitTri, unsigned long long* counters,
                                cudaStream_t stream);

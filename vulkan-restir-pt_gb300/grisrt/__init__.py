@@ -102,6 +102,7 @@ class SceneStats(ctypes.Structure):
 
 EXPORTS = [
     "grisCreate", "grisDestroy", "grisGetError", "grisSync", "grisGetStream", "grisReadCounters", "grisGetVersion",
+    "grisSetProfiling", "grisReadProfile", "grisSetWorkCounting", "grisReadWorkCounters",
     "grisSizeof", "grisBuildLightTable", "grisCameraSetup", "grisCameraLookAt", "grisHostSceneCreate",
     "grisHostSceneDesc", "grisHostSceneCamera", "grisHostSceneDestroy", "grisSceneCreate", "grisSceneDestroy",
     "grisSceneGetStats", "grisDebugHostSceneCreate", "grisDebugTraceHost", "grisDebugTraceDevice", "grisPassGBuffer", "grisPassRender",
@@ -130,6 +131,10 @@ def load(path=None):
         "grisGetStream": (vp, [vp]),
         "grisReadCounters": (i32, [vp, ctypes.POINTER(u64), i32]),
         "grisGetVersion": (i32, []),
+        "grisSetProfiling": (i32, [vp, i32]),
+        "grisReadProfile": (i32, [vp, ctypes.POINTER(ctypes.c_double), ctypes.POINTER(u64), i32]),
+        "grisSetWorkCounting": (i32, [vp, i32]),
+        "grisReadWorkCounters": (i32, [vp, ctypes.POINTER(u64), ctypes.POINTER(u64), ctypes.POINTER(u64), i32]),
         "grisSizeof": (ctypes.c_size_t, [i32]),
         "grisBuildLightTable": (i32, [vp, u32, vp]),
         "grisCameraSetup": (i32, [ctypes.POINTER(Camera), vp, vp, ctypes.c_float, u32, u32]),
@@ -298,6 +303,25 @@ class Context:
         out = (ctypes.c_uint64 * 4)()
         self.check(load().grisReadCounters(self.h, out, int(reset)), "grisReadCounters")
         return list(out)
+
+    def set_profiling(self, enable):
+        self.check(load().grisSetProfiling(self.h, int(enable)), "grisSetProfiling")
+
+    def profile(self, reset=False):
+        """(ms per kernel, launches per kernel) for G-buffer, path trace, temporal, spatial."""
+        ms = (ctypes.c_double * 4)()
+        n = (ctypes.c_uint64 * 4)()
+        self.check(load().grisReadProfile(self.h, ms, n, int(reset)), "grisReadProfile")
+        return list(ms), list(n)
+
+    def set_work_counting(self, enable):
+        self.check(load().grisSetWorkCounting(self.h, int(enable)), "grisSetWorkCounting")
+
+    def work(self, reset=False):
+        """(nodes, triangles, closest-hit rays) per kernel."""
+        a, b, c = (ctypes.c_uint64 * 4)(), (ctypes.c_uint64 * 4)(), (ctypes.c_uint64 * 4)()
+        self.check(load().grisReadWorkCounters(self.h, a, b, c, int(reset)), "grisReadWorkCounters")
+        return list(a), list(b), list(c)
 
     def close(self):
         if self.h:
