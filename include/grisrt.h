@@ -261,6 +261,23 @@ int grisPassRender(GrisContext* ctx, const GrisScene* scene, const GrisPassBindi
                    const GrisCamera* cam, const GrisCamera* prevCam, const GrisSettings* settings,
                    int passes);
 
+/* No counterpart in the reference. The GRIS pass for callers that cannot allocate device memory
+ * while they render (for example a host callback or plugin that must not call cudaMalloc, or a
+ * process whose device allocator belongs to another framework). The temporary reservoirs that
+ * carry the temporal result to the spatial kernel, and the ray-counter words, live in one static
+ * device array of GRIS_NOALLOC_MAX_PIXELS x 96 B + 256 B (about 6.3 MB) that every GPU loading
+ * the library holds until exit. The caller passes inputs and outputs as for grisPassRender, with
+ * reservoirTemp = NULL, and a CUDA stream (NULL = the default stream); all three passes run.
+ * Frames larger than GRIS_NOALLOC_MAX_PIXELS return GRIS_ERR_TOO_LARGE before any work. The
+ * call allocates nothing: it clears the part of the array it uses (so its result equals
+ * grisPassRender's with a zero-filled reservoirTemp), then launches. The first call on a device
+ * looks up the array's device address (cudaGetSymbolAddress, with that device current); make
+ * that first call before any stream capture. Every call shares the one array: calls that overlap
+ * on the GPU (other streams, other threads) race on it. */
+#define GRIS_NOALLOC_MAX_PIXELS 65536
+int grisPassRenderNoAlloc(const GrisScene* scene, const GrisPassBindings* b, const GrisCamera* cam,
+                          const GrisCamera* prevCam, const GrisSettings* settings, void* stream);
+
 /* ---------------------------------------------------------------- frames (library-owned buffers) */
 /* G-buffer cur/prev, reservoirs This[2]/Temp, output: the renderer's per-frame resources
  * (src/Renderer.cpp:193-257) with its ping-pong (Renderer.cpp:329-347, 567). */

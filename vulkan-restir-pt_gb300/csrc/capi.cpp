@@ -133,6 +133,13 @@ grisrt::DeviceSceneView scene_view(const GrisScene* s) { return s->view; }
 
 }  // namespace
 
+bool grisrt::scene_device(const GrisScene* s, grisrt::DeviceSceneView* view, int* device) {
+    if (!s || !s->ctx) return false;
+    *view = s->view;
+    *device = s->ctx->device;
+    return true;
+}
+
 extern "C" {
 
 int grisGetVersion(void) { return 1; }

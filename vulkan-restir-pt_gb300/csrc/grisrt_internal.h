@@ -30,6 +30,10 @@ void world_triangles(const GrisSceneDesc& d, std::vector<float>& v012, std::vect
 /* Builds the BVH; returns false with a message on failure. */
 bool build_bvh(const GrisSceneDesc& d, BvhHost& out, std::string& err);
 
+struct DeviceSceneView;
+/* Device view and device ordinal of an uploaded scene; false for a host-only scene. */
+bool scene_device(const GrisScene* s, DeviceSceneView* view, int* device);
+
 }  // namespace grisrt
 
 #endif

@@ -34,6 +34,7 @@ assert MATERIAL.itemsize == 32 and VERTEX.itemsize == 32 and INSTANCE.itemsize =
 assert LIGHT.itemsize == 64 and TABLE.itemsize == 8 and RESERVOIR.itemsize == 96
 
 INVALID_HIT = 0xFFFFFFFF
+NOALLOC_MAX_PIXELS = 65536
 CLEAR_FLAG = 0x80000000
 
 
@@ -105,7 +106,7 @@ EXPORTS = [
     "grisSetProfiling", "grisReadProfile", "grisSetWorkCounting", "grisReadWorkCounters",
     "grisSizeof", "grisBuildLightTable", "grisCameraSetup", "grisCameraLookAt", "grisHostSceneCreate",
     "grisHostSceneDesc", "grisHostSceneCamera", "grisHostSceneDestroy", "grisSceneCreate", "grisSceneDestroy",
-    "grisSceneGetStats", "grisDebugHostSceneCreate", "grisDebugTraceHost", "grisDebugTraceDevice", "grisPassGBuffer", "grisPassRender",
+    "grisSceneGetStats", "grisDebugHostSceneCreate", "grisDebugTraceHost", "grisDebugTraceDevice", "grisPassGBuffer", "grisPassRender", "grisPassRenderNoAlloc",
     "grisFrameCreate", "grisFrameDestroy", "grisFrameRender", "grisFrameGetBuffer", "grisFrameDownload",
     "grisFrameUpload",
 ]
@@ -152,6 +153,8 @@ def load(path=None):
         "grisPassGBuffer": (i32, [vp, vp, ctypes.POINTER(GBufferBindings), ctypes.POINTER(Camera)]),
         "grisPassRender": (i32, [vp, vp, ctypes.POINTER(PassBindings), ctypes.POINTER(Camera), ctypes.POINTER(Camera),
                                  ctypes.POINTER(Settings), i32]),
+        "grisPassRenderNoAlloc": (i32, [vp, ctypes.POINTER(PassBindings), ctypes.POINTER(Camera), ctypes.POINTER(Camera),
+                                        ctypes.POINTER(Settings), vp]),
         "grisFrameCreate": (i32, [vp, u32, u32, ctypes.POINTER(vp)]),
         "grisFrameDestroy": (i32, [vp]),
         "grisFrameRender": (i32, [vp, vp, vp, ctypes.POINTER(Camera), ctypes.POINTER(Camera), ctypes.POINTER(Settings)]),
