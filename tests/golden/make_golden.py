@@ -1,0 +1,75 @@
+#!/usr/bin/env python3
+"""Generates the golden vectors in tests/golden/ from the reference's own shader code compiled
+as C++ (oracle/_ref, built by oracle/ref/make_ref.py where the reference sources are present).
+
+For each case the file stores the scene-array hash, the cameras and settings used, the ray
+counts, and per frame the SHA-256 digest of every buffer (G-buffer, motion, reservoirs,
+temporary reservoirs, output) plus, for the small cases, full copies of the reservoirs and the
+output radiance (for diagnostics).
+Usage: python tests/golden/make_golden.py
+"""
+import hashlib
+import os
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+REPO = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, os.path.join(REPO, "vulkan-restir-pt_gb300"))
+sys.path.insert(0, REPO)
+
+import grisrt as G                      # noqa: E402
+from oracle import pyoracle as O        # noqa: E402
+
+BUFFERS = ("dn", "am", "mv", "resv", "temp", "out")
+# name: (kind, grid, spheres, W, H, frames, settings, store full arrays)
+CASES = {
+    "box_32x32_c1": (0, 0, 0, 32, 32, 3, dict(maxDepth=3, spatialRadius=30.0), True),
+    "terrain_24x20_d8": (1, 24, 12, 24, 20, 2, dict(maxDepth=8, spatialRadius=30.0), True),
+    "glossy_24x20_d8": (2, 24, 12, 24, 20, 2, dict(maxDepth=8), True),
+    "box_256x256_c1_8frames": (0, 0, 0, 256, 256, 8, dict(maxDepth=3, spatialRadius=30.0), False),
+}
+
+
+def scene_hash(hs):
+    h = hashlib.sha256()
+    for a in hs.arrays():
+        h.update(np.ascontiguousarray(a).tobytes())
+    return h.hexdigest()
+
+
+def digest(a):
+    return hashlib.sha256(np.ascontiguousarray(a).tobytes()).hexdigest()
+
+
+def make(name):
+    kind, grid, spheres, W, H, frames, kw, full = CASES[name]
+    G.load()
+    hs = G.HostScene(kind, seed=3, grid=grid, spheres=spheres)
+    cams, prevs = G.sequence_cameras(hs, frames, W, H, seed=21)
+    st = G.Settings.make(**kw)
+    ref = O.reference()
+    ref.set_scene(hs)
+    ref.read_counters(reset=True)
+    res = O.run_sequence(ref, cams, prevs, st, W, H)
+    cnt = ref.read_counters(reset=True)
+    out = {"scene_sha256": np.array(scene_hash(hs)), "settings": np.frombuffer(bytes(memoryview(st)), np.uint8),
+           "cams": np.stack([np.frombuffer(c.tobytes(), np.uint8) for c in cams]),
+           "prevs": np.stack([np.frombuffer(c.tobytes(), np.uint8) for c in prevs]),
+           "counters": np.array(cnt[:3], np.uint64), "meta": np.array([kind, grid, spheres, W, H, frames], np.int64)}
+    for f in range(frames):
+        for k in BUFFERS:
+            if full and k in ("resv", "out"):
+                out["%s_%d" % (k, f)] = res[f][k]
+            out["%s_%d_sha256" % (k, f)] = np.array(digest(res[f][k]))
+    path = os.path.join(HERE, name + ".npz")
+    np.savez_compressed(path, **out)
+    return path
+
+
+if __name__ == "__main__":
+    if not os.path.exists(O.REF_LIB):
+        sys.exit("oracle/_ref/libgrisref.so missing: run oracle/ref/make_ref.py (needs the reference sources)")
+    for n in (sys.argv[1:] or CASES):
+        print(make(n), os.path.getsize(os.path.join(HERE, n + ".npz")))
