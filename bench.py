@@ -63,6 +63,7 @@ def parse():
     ap.add_argument("--depth", type=int, default=8)
     ap.add_argument("--seed", type=int, default=1)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--launch-mode", default="persistent", choices=["persistent", "grid"])
     ap.add_argument("--cpu-seconds", type=float, default=20.0, help="target CPU work of the baseline sample")
     return ap.parse_args()
 
@@ -206,6 +207,8 @@ def main():
     hs = G.HostScene(1, seed=args.seed, grid=args.grid, spheres=args.spheres)
     config["triangles"] = hs.triangle_count()
     ctx = G.Context(local)
+    ctx.set_launch_mode(G.LAUNCH_PERSISTENT if args.launch_mode == "persistent" else G.LAUNCH_GRID)
+    config["launch"] = args.launch_mode
     scene = G.Scene(ctx, hs)
     stats = scene.stats()
     frame = G.Frame(ctx, W, H)

@@ -210,6 +210,12 @@ int grisReadProfile(GrisContext* ctx, double msTotal[4], uint64_t launches[4], i
 /* Traversal work per kernel while enabled: BVH nodes intersected, triangles tested and
  * closest-hit rays (primary rays for the G-buffer); shadow rays are in grisReadCounters. */
 int grisSetWorkCounting(GrisContext* ctx, int enable);
+/* Launch form of the three GRIS passes: GRIS_LAUNCH_GRID (one thread per pixel of a 16 x 8 tile)
+ * or GRIS_LAUNCH_PERSISTENT (default: resident warps take 16 x 16 pixel tiles and refill idle
+ * lanes pixel by pixel). Results are identical; only speed differs. */
+#define GRIS_LAUNCH_GRID 0
+#define GRIS_LAUNCH_PERSISTENT 1
+int grisSetLaunchMode(GrisContext* ctx, int mode);
 int grisReadWorkCounters(GrisContext* ctx, uint64_t nodes[4], uint64_t tris[4], uint64_t closestRays[4], int reset);
 size_t grisSizeof(int which);   /* 0 camera, 1 reservoir, 2 material, 3 vertex, 4 instance, 5 light, 6 table entry, 7 settings */
 

@@ -35,7 +35,8 @@ def ora():
     return O.oracle()
 
 
-def gpu_sequence(ctx, hs, cams, prevs, st, W, H):
+def gpu_sequence(ctx, hs, cams, prevs, st, W, H, mode=G.LAUNCH_PERSISTENT):
+    ctx.set_launch_mode(mode)
     scene = G.Scene(ctx, hs)
     fr = G.Frame(ctx, W, H)
     ctx.counters(reset=True)
@@ -52,13 +53,18 @@ def gpu_sequence(ctx, hs, cams, prevs, st, W, H):
     return out, counters
 
 
+MODES = [G.LAUNCH_PERSISTENT, G.LAUNCH_GRID]
+
+
+@pytest.mark.parametrize("mode", MODES, ids=["persistent", "grid"])
 @pytest.mark.parametrize("case", CASES, ids=[c[0] for c in CASES])
-def test_gpu_matches_oracle_bit_exact(case, ctx, ora):
+def test_gpu_matches_oracle_bit_exact(case, mode, ctx, ora):
     name, kind, grid, spheres, W, H, frames, kw = case
     hs = G.HostScene(kind, seed=2, grid=grid, spheres=spheres)
     cams, prevs = G.sequence_cameras(hs, frames, W, H, seed=11)
     st = G.Settings.make(**kw)
-    got, gc = gpu_sequence(ctx, hs, cams, prevs, st, W, H)
+    got, gc = gpu_sequence(ctx, hs, cams, prevs, st, W, H, mode)
+    ctx.set_launch_mode(G.LAUNCH_PERSISTENT)
     ora.set_scene(hs)
     ora.read_counters(reset=True)
     want = O.run_sequence(ora, cams, prevs, st, W, H)
@@ -123,7 +129,8 @@ def test_pass_bindings_api_matches_frame_api(ctx, ora):
     out = torch.zeros((n, 4), dtype=torch.float32, device="cuda")
     torch.cuda.synchronize()
     lib = G.load()
-    want = O.run_sequence(ora if ora.set_scene(hs) else ora, cams, prevs, st, W, H, record=("resv", "out"))
+    ora.set_scene(hs)
+    want = O.run_sequence(ora, cams, prevs, st, W, H, record=("resv", "out"))
     j = 0
     for f in range(frames):
         gb = G.GBufferBindings(W, H, dn[j].data_ptr(), am[j].data_ptr(), mv.data_ptr())

@@ -78,6 +78,7 @@ struct GrisContext {
     unsigned long long* dCounters = nullptr;
     unsigned long long* hCounters = nullptr;   /* pinned */
     int countWork = 0;
+    int launchMode = GRIS_LAUNCH_PERSISTENT;
     Profiler prof;
     std::string err;
 };
@@ -218,6 +219,12 @@ int grisReadProfile(GrisContext* ctx, double msTotal[4], uint64_t launches[4], i
         launches[k] = ctx->prof.launches[k];
         if (reset) { ctx->prof.ms[k] = 0.0; ctx->prof.launches[k] = 0; }
     }
+    return GRIS_OK;
+}
+
+int grisSetLaunchMode(GrisContext* ctx, int mode) {
+    if (!ctx || (mode != GRIS_LAUNCH_GRID && mode != GRIS_LAUNCH_PERSISTENT)) return GRIS_ERR_INVALID_ARGUMENT;
+    ctx->launchMode = mode;
     return GRIS_OK;
 }
 
@@ -386,7 +393,7 @@ int grisPassRender(GrisContext* ctx, const GrisScene* s, const GrisPassBindings*
     if (set->spatialNeighbors > 64) return fail(ctx, GRIS_ERR_INVALID_ARGUMENT, "spatialNeighbors must be <= 64");
     cudaSetDevice(ctx->device);
     GRIS_CK(ctx, grisrt::launch_gris(scene_view(s), *b, *cam, *prevCam, *set, passes & 7, ctx->dCounters, ctx->countWork,
-                                     &ctx->prof, ctx->stream));
+                                     &ctx->prof, ctx->stream, ctx->launchMode));
     return GRIS_OK;
 }
 

@@ -96,51 +96,65 @@ GD uint32_t nextRcVertexSampleState(uint32_t state, bool connectible) {         
     return state + (connectible ? 1u : 0u);
 }
 
-/* tracePath (gris_path_trace.glsl:45-306); writes the canonical reservoir of the pixel. */
-GD void tracePath(const PassCtx& P, uint32_t ix, uint32_t iy, RayCount& rc, int& err) {
-    const DevScene& sc = P.sc;
-    const int W = (int)P.b.width, H = (int)P.b.height;
-    V2 uv = v2(((float)ix + 0.5f) / (float)W, ((float)iy + 0.5f) / (float)H);
-    float depth = 0.0f; V3 norm = v3s(0.0f), albedo = v3s(0.0f); int matMeshId = 0;
-    float4 dn = texture_bilinear(reinterpret_cast<const float4*>(P.b.depthNormal), W, H, uv);
-    uint2 am = fetch_am(reinterpret_cast<const uint2*>(P.b.albedoMatId), W, H, (int)ix, (int)iy);
-    if (!unpackGBuffer(dn, am, depth, norm, albedo, matMeshId)) return;
-    int matId = matMeshId >> 16;
-    Ray3 ray = pinholeCameraSampleRay(P.cam, v2(uv.x, 1.0f - uv.y));
-    uint32_t rng = makeSeed2(P.cam.seed, ix, iy);
-
-    V3 radiance = v3s(0.0f);
-    V3 throughput = v3s(1.0f);
-    V3 rcThroughput = v3s(0.0f);
-    V3 wo = -ray.dir;
-    V3 lastPos = v3s(0.0f);
-    bool isLastVertexConnectible = false;
-    uint32_t sampleState = 0u, lastSampleState = 0u;
-
-    Surf surf = surf_zero();
-    surf.pos = ray.ori + ray.dir * (depth - 1e-4f);
-    surf.norm = norm;
-    surf.albedo = albedo;
-    surf.isLight = false;
-
-    Mat mat = load_material(sc, (uint32_t)matId);
-    BsdfSample s = bs_zero();
-    Isec isec = isec_zero();
-
-    PathSample pathSample = ps_zero();
-    pathSampleReset(pathSample);
-    pathSample.primaryRng = rng;
-
-    Resv resv = resv_zero();
-    resvReset(resv);
+/* tracePath (gris_path_trace.glsl:45-306) as a state machine: begin() is the prologue up to the
+ * bounce loop, step() one iteration of the loop (false where the reference breaks), end() the
+ * epilogue that writes the canonical reservoir. Driving begin / step until false or maxDepth /
+ * end performs exactly the reference's sequence of operations for the pixel. */
+struct PathTracer {
+    uint32_t ix, iy;
+    int bounce;
+    uint32_t rng;
+    V3 throughput, rcThroughput, wo, lastPos;
+    bool isLastVertexConnectible;
+    uint32_t sampleState, lastSampleState;
+    Surf surf;
+    Mat mat;
+    BsdfSample s;
+    Isec isec;
+    PathSample pathSample;
     Stream stream;
-    stream.ps = ps_zero(); stream.weight = 0.0f; stream.sumWeight = 0.0f; stream.sampleCount = 0u;
+    Ray3 ray;
 
-    const int maxDepth = (int)P.set.maxDepth;
-    for (int bounce = 0; bounce < maxDepth; bounce++) {
+    GD bool begin(const PassCtx& P, uint32_t px, uint32_t py) {
+        const DevScene& sc = P.sc;
+        const int W = (int)P.b.width, H = (int)P.b.height;
+        ix = px; iy = py;
+        V2 uv = v2(((float)ix + 0.5f) / (float)W, ((float)iy + 0.5f) / (float)H);
+        float depth = 0.0f; V3 norm = v3s(0.0f), albedo = v3s(0.0f); int matMeshId = 0;
+        float4 dn = texture_bilinear(reinterpret_cast<const float4*>(P.b.depthNormal), W, H, uv);
+        uint2 am = fetch_am(reinterpret_cast<const uint2*>(P.b.albedoMatId), W, H, (int)ix, (int)iy);
+        if (!unpackGBuffer(dn, am, depth, norm, albedo, matMeshId)) return false;
+        int matId = matMeshId >> 16;
+        ray = pinholeCameraSampleRay(P.cam, v2(uv.x, 1.0f - uv.y));
+        rng = makeSeed2(P.cam.seed, ix, iy);
+        throughput = v3s(1.0f);
+        rcThroughput = v3s(0.0f);
+        wo = -ray.dir;
+        lastPos = v3s(0.0f);
+        isLastVertexConnectible = false;
+        sampleState = 0u; lastSampleState = 0u;
+        surf = surf_zero();
+        surf.pos = ray.ori + ray.dir * (depth - 1e-4f);
+        surf.norm = norm;
+        surf.albedo = albedo;
+        surf.isLight = false;
+        mat = load_material(sc, (uint32_t)matId);
+        s = bs_zero();
+        isec = isec_zero();
+        pathSample = ps_zero();
+        pathSampleReset(pathSample);
+        pathSample.primaryRng = rng;
+        stream.ps = ps_zero(); stream.weight = 0.0f; stream.sumWeight = 0.0f; stream.sampleCount = 0u;
+        bounce = 0;
+        return true;
+    }
+
+    /* one iteration of the bounce loop (gris_path_trace.glsl:91-258) */
+    GD bool step(const PassCtx& P, RayCount& rc, int& err) {
+        const DevScene& sc = P.sc;
         if (bounce > 0) {
             isec = traceClosestHit(sc, ray.ori, ray.dir, kMinRayDistance, kMaxRayDistance, rc, err);
-            if (isec.inst == kInvalidHit) break;
+            if (isec.inst == kInvalidHit) return false;
             loadSurfaceInfo(sc, isec, surf);
             mat = load_material(sc, surf.matIndex);
         }
@@ -184,9 +198,8 @@ GD void tracePath(const PassCtx& P, uint32_t ix, uint32_t iy, RayCount& rc, int&
                     setRcVertexType(pathSample.flags, kRcLightScattered);
                     addStream(stream, pathSample, luminance(pathSample.F), resvRandSample);
                 }
-                radiance = radiance + weightedLi * throughput;
-            }
-            break;
+                        }
+            return false;
         }
 
         bool connectible = isThisVertexConnectible && isLastVertexConnectible && distToPrev > kDistanceThreshold;
@@ -235,18 +248,17 @@ GD void tracePath(const PassCtx& P, uint32_t ix, uint32_t iy, RayCount& rc, int&
                     setRcVertexType(pathSample.flags, kRcLightSampled);
                     addStream(stream, pathSample, luminance(pathSample.F), resvRandSample);
                 }
-                radiance = radiance + weightedLi * scatterTerm * throughput;
-            }
+                        }
         }
 
         if (bounce > 4) {
             float pdfTerminate = fmaxf(1.0f - luminance(throughput) * P.set.rrScale, 0.0f);
-            if (sample1f(rng) < pdfTerminate) break;
+            if (sample1f(rng) < pdfTerminate) return false;
             throughput = throughput / (1.0f - pdfTerminate);
             rcThroughput = rcThroughput / (1.0f - pdfTerminate);
         }
 
-        if (!sampleBSDF(mat, surf.albedo, surf.norm, wo, sample3f(rng), s) || s.pdf < 1e-6f) break;
+        if (!sampleBSDF(mat, surf.albedo, surf.norm, wo, sample3f(rng), s) || s.pdf < 1e-6f) return false;
 
         float cosTheta = isSampleTypeDelta(s.type) ? 1.0f : absDot(surf.norm, s.wi);
         V3 scatterTerm = s.bsdf * cosTheta / s.pdf;
@@ -266,24 +278,31 @@ GD void tracePath(const PassCtx& P, uint32_t ix, uint32_t iy, RayCount& rc, int&
         ray.dir = s.wi;
         ray.ori = surf.pos + ray.dir * 1e-4f;
         isLastVertexConnectible = isThisVertexConnectible;
+        return true;
     }
 
-    if (sampleState == 2u && lastSampleState == 2u) addStream(stream, pathSample, luminance(pathSample.F), sample1f(rng));
+    /* after the loop (gris_path_trace.glsl:260-278) */
+    GD void end(const PassCtx& P) {
+        const int W = (int)P.b.width;
+        Resv resv = resv_zero();
+        resvReset(resv);
+        if (sampleState == 2u && lastSampleState == 2u) addStream(stream, pathSample, luminance(pathSample.F), sample1f(rng));
 
-    pathSample = stream.ps;
-    if (stream.sumWeight > 0.0f && stream.weight > 0.0f) {
-        pathSample.F = pathSample.F * (stream.sumWeight / stream.weight);
-        pathSample.rcLi = pathSample.rcLi * (stream.sumWeight / stream.weight);
-        resv.resampleWeight = luminance(pathSample.F);
-    } else {
-        pathSample.rcIsec.inst = kInvalidHit;
-        pathSample.F = v3s(0.0f);
+        pathSample = stream.ps;
+        if (stream.sumWeight > 0.0f && stream.weight > 0.0f) {
+            pathSample.F = pathSample.F * (stream.sumWeight / stream.weight);
+            pathSample.rcLi = pathSample.rcLi * (stream.sumWeight / stream.weight);
+            resv.resampleWeight = luminance(pathSample.F);
+        } else {
+            pathSample.rcIsec.inst = kInvalidHit;
+            pathSample.F = v3s(0.0f);
+        }
+        resv.s = pathSample;
+        resv.sampleCount = 1.0f;
+        store_resv(P.b.reservoirThis, (uint64_t)iy * (uint64_t)W + ix, resv);
+
     }
-    resv.s = pathSample;
-    resv.sampleCount = 1.0f;
-    store_resv(P.b.reservoirThis, (uint64_t)iy * (uint64_t)W + ix, resv);
-    (void)radiance;
-}
+};
 
 /* ------------------------------------------------------------------ hybrid shift (gris_retrace.glsl) */
 /* traceReplayPathForHybridShift (:42-136) */
@@ -408,165 +427,90 @@ GD void reuseAndMerge(const PassCtx& P, Resv& dstResv, const Surf& dstPrimarySur
 }
 
 /* ------------------------------------------------------------------ temporal reuse */
-GD void temporalReuse(const PassCtx& P, uint32_t ix, uint32_t iy, RayCount& rc, int& err) {
-    const DevScene& sc = P.sc;
-    const int W = (int)P.b.width, H = (int)P.b.height;
-    const uint64_t n = (uint64_t)W * (uint64_t)H;
-    V2 uv = v2(((float)ix + 0.5f) / (float)W, ((float)iy + 0.5f) / (float)H);
-    float depth = 0.0f; V3 norm = v3s(0.0f), albedo = v3s(0.0f); int matMeshId = 0;
-    float4 dn = texture_bilinear(reinterpret_cast<const float4*>(P.b.depthNormal), W, H, uv);
-    uint2 am = fetch_am(reinterpret_cast<const uint2*>(P.b.albedoMatId), W, H, (int)ix, (int)iy);
-    if (!unpackGBuffer(dn, am, depth, norm, albedo, matMeshId)) return;
-    const __half2* mv = reinterpret_cast<const __half2*>(P.b.motion);
-    float2 motion = __half22float2(mv[(uint64_t)iy * W + ix]);
-    int matId = matMeshId >> 16;
-    Ray3 ray = pinholeCameraSampleRay(P.cam, v2(uv.x, 1.0f - uv.y));
-    uint32_t rng = makeSeed2(P.cam.seed, ix, iy) ^ 1u;
-    uint32_t resvRng = ~rng;
-    V3 pos = ray.ori + ray.dir * (depth - 1e-4f);
+/* temporalReuse (gris_resample_temporal.glsl:36-83): begin() finds the previous reservoir
+ * (findPreviousReservoir, :11-34) and finishes the pixel when there is nothing to merge;
+ * step() shifts and merges it and writes the temporary reservoir. */
+struct TemporalTask {
+    uint64_t idx;
+    Resv resv, src;
+    Surf dst;
+    Isec dstIsec;
+    Ray3 ray;
+    uint32_t resvRng;
 
-    uint64_t idx = (uint64_t)iy * W + ix;
-    Resv resv = load_resv(P.b.reservoirThis, idx, n);
-    Isec dstPrimaryIsec; dstPrimaryIsec.bx = uv.x; dstPrimaryIsec.by = uv.y; dstPrimaryIsec.inst = kSpecialHit; dstPrimaryIsec.tri = 0u;
+    GD void finish(const PassCtx& P) {
+        resvResetIfInvalid(resv);
+        store_resv(P.b.reservoirTemp, idx, resv);
+    }
 
-    if (P.set.temporalReuse) {
-        Resv temporalResv = resv_zero();
-        resvReset(temporalResv);
-        Surf dstPrimarySurf; dstPrimarySurf.pos = pos; dstPrimarySurf.norm = norm; dstPrimarySurf.albedo = albedo;
-        dstPrimarySurf.matIndex = (uint32_t)matId; dstPrimarySurf.isLight = false;
-        if ((P.cam.frameIndex & kCameraClearFlag) == 0u) {
-            /* findPreviousReservoir (gris_resample_temporal.glsl:11-34) */
-            V2 puv = v2(uv.x + motion.x, uv.y + motion.y);
-            bool found = false;
-            if (!(puv.x < 0.0f || puv.y < 0.0f || puv.x > 1.0f || puv.y > 1.0f)) {
-                int px = (int)(puv.x * (float)P.cam.w), py = (int)(puv.y * (float)P.cam.h);
-                float depthPrev = 0.0f; V3 normalPrev = v3s(0.0f), albedoPrev = v3s(0.0f); int matMeshIdPrev = 0;
-                float4 pdn = texture_bilinear(reinterpret_cast<const float4*>(P.b.depthNormalPrev), W, H, puv);
-                uint2 pam = fetch_am(reinterpret_cast<const uint2*>(P.b.albedoMatIdPrev), W, H, px, py);
-                if (unpackGBuffer(pdn, pam, depthPrev, normalPrev, albedoPrev, matMeshIdPrev)) {
-                    Ray3 pray = pinholeCameraSampleRay(P.prev, v2(puv.x, 1.0f - puv.y));
-                    V3 posPrev = pray.ori + pray.dir * (depthPrev - 1e-4f);
-                    if (!(matMeshIdPrev != matMeshId || dot3(normalPrev, norm) < 0.95f || distance3(pos, posPrev) > 0.5f)) {
-                        uint32_t pidx = (uint32_t)P.cam.w * (uint32_t)py + (uint32_t)px;
-                        temporalResv = load_resv(P.b.reservoirPrev, pidx, n);
-                        found = true;
+    GD bool begin(const PassCtx& P, uint32_t ix, uint32_t iy, RayCount&, int&) {
+        const int W = (int)P.b.width, H = (int)P.b.height;
+        const uint64_t n = (uint64_t)W * (uint64_t)H;
+        V2 uv = v2(((float)ix + 0.5f) / (float)W, ((float)iy + 0.5f) / (float)H);
+        float depth = 0.0f; V3 norm = v3s(0.0f), albedo = v3s(0.0f); int matMeshId = 0;
+        float4 dn = texture_bilinear(reinterpret_cast<const float4*>(P.b.depthNormal), W, H, uv);
+        uint2 am = fetch_am(reinterpret_cast<const uint2*>(P.b.albedoMatId), W, H, (int)ix, (int)iy);
+        if (!unpackGBuffer(dn, am, depth, norm, albedo, matMeshId)) return false;
+        const __half2* mv = reinterpret_cast<const __half2*>(P.b.motion);
+        float2 motion = __half22float2(mv[(uint64_t)iy * W + ix]);
+        int matId = matMeshId >> 16;
+        ray = pinholeCameraSampleRay(P.cam, v2(uv.x, 1.0f - uv.y));
+        uint32_t rng = makeSeed2(P.cam.seed, ix, iy) ^ 1u;
+        resvRng = ~rng;
+        V3 pos = ray.ori + ray.dir * (depth - 1e-4f);
+        idx = (uint64_t)iy * W + ix;
+        resv = load_resv(P.b.reservoirThis, idx, n);
+        dstIsec.bx = uv.x; dstIsec.by = uv.y; dstIsec.inst = kSpecialHit; dstIsec.tri = 0u;
+        if (P.set.temporalReuse) {
+            src = resv_zero();
+            resvReset(src);
+            dst.pos = pos; dst.norm = norm; dst.albedo = albedo; dst.matIndex = (uint32_t)matId; dst.isLight = false;
+            if ((P.cam.frameIndex & kCameraClearFlag) == 0u) {
+                V2 puv = v2(uv.x + motion.x, uv.y + motion.y);
+                bool found = false;
+                if (!(puv.x < 0.0f || puv.y < 0.0f || puv.x > 1.0f || puv.y > 1.0f)) {
+                    int px = (int)(puv.x * (float)P.cam.w), py = (int)(puv.y * (float)P.cam.h);
+                    float depthPrev = 0.0f; V3 normalPrev = v3s(0.0f), albedoPrev = v3s(0.0f); int matMeshIdPrev = 0;
+                    float4 pdn = texture_bilinear(reinterpret_cast<const float4*>(P.b.depthNormalPrev), W, H, puv);
+                    uint2 pam = fetch_am(reinterpret_cast<const uint2*>(P.b.albedoMatIdPrev), W, H, px, py);
+                    if (unpackGBuffer(pdn, pam, depthPrev, normalPrev, albedoPrev, matMeshIdPrev)) {
+                        Ray3 pray = pinholeCameraSampleRay(P.prev, v2(puv.x, 1.0f - puv.y));
+                        V3 posPrev = pray.ori + pray.dir * (depthPrev - 1e-4f);
+                        if (!(matMeshIdPrev != matMeshId || dot3(normalPrev, norm) < 0.95f || distance3(pos, posPrev) > 0.5f)) {
+                            uint32_t pidx = (uint32_t)P.cam.w * (uint32_t)py + (uint32_t)px;
+                            src = load_resv(P.b.reservoirPrev, pidx, n);
+                            found = true;
+                        }
                     }
                 }
+                if (found && resvIsValid(src)) return true;
             }
-            if (found && resvIsValid(temporalResv))
-                reuseAndMerge(P, resv, dstPrimarySurf, dstPrimaryIsec, ray, temporalResv, resvRng, rc, err);
         }
+        finish(P);
+        return false;
     }
-    resvResetIfInvalid(resv);
-    store_resv(P.b.reservoirTemp, idx, resv);
-}
+
+    GD bool step(const PassCtx& P, RayCount& rc, int& err) {
+        reuseAndMerge(P, resv, dst, dstIsec, ray, src, resvRng, rc, err);
+        finish(P);
+        return false;
+    }
+};
 
 /* ------------------------------------------------------------------ spatial reuse + final shading */
-GD V3 spatialReuse(const PassCtx& P, uint32_t ix, uint32_t iy, RayCount& rc, int& err, bool& wrote) {
-    const DevScene& sc = P.sc;
-    const int W = (int)P.b.width, H = (int)P.b.height;
-    const uint64_t n = (uint64_t)W * (uint64_t)H;
-    V2 uv = v2(((float)ix + 0.5f) / (float)W, ((float)iy + 0.5f) / (float)H);
-    float depth = 0.0f; V3 norm = v3s(0.0f), albedo = v3s(0.0f); int matMeshId = 0;
-    const float4* dnT = reinterpret_cast<const float4*>(P.b.depthNormal);
-    const uint2* amT = reinterpret_cast<const uint2*>(P.b.albedoMatId);
-    float4 dn = texture_bilinear(dnT, W, H, uv);
-    uint2 am = fetch_am(amT, W, H, (int)ix, (int)iy);
-    wrote = false;
-    if (!unpackGBuffer(dn, am, depth, norm, albedo, matMeshId)) return v3s(0.0f);
-    uint32_t rng = makeSeed2(P.cam.seed, ix, iy) ^ 2u;
-    Ray3 ray = pinholeCameraSampleRay(P.cam, v2(uv.x, 1.0f - uv.y));
-    V3 pos = ray.ori + ray.dir * (depth - 1e-4f);
-    int matId = matMeshId >> 16;
-    V3 radiance = v3s(0.0f);
-    uint64_t idx = (uint64_t)iy * W + ix;
-    Resv resv = load_resv(P.b.reservoirTemp, idx, n);
-    Isec dstPrimaryIsec; dstPrimaryIsec.bx = uv.x; dstPrimaryIsec.by = uv.y; dstPrimaryIsec.inst = kSpecialHit; dstPrimaryIsec.tri = 0u;
-    Surf dstPrimarySurf; dstPrimarySurf.pos = pos; dstPrimarySurf.norm = norm; dstPrimarySurf.albedo = albedo;
-    dstPrimarySurf.matIndex = (uint32_t)matId; dstPrimarySurf.isLight = false;
+/* spatialReuse (gris_resample_spatial.glsl:36-135) + the running mean of
+ * gris_resample_spatial.comp:21-27. begin() reads the pixel (a background pixel only updates the
+ * running mean); each step() handles one neighbour (findNeighborReservoir, :11-34, then the shift
+ * and merge); the last step writes the reservoir, shades and accumulates. */
+struct SpatialTask {
+    uint32_t ix, iy, i, rng;
+    uint64_t idx;
+    Resv resv;
+    Surf dst;
+    Isec dstIsec;
+    Ray3 ray;
 
-    if (P.set.spatialReuse) {
-        const uint32_t resampleNum = P.set.spatialNeighbors;
-        const float resampleRadius = P.set.spatialRadius;
-        float tx = 1.0f / (float)W, ty = 1.0f / (float)H;
-        for (uint32_t i = 0; i < resampleNum; i++) {
-            V2 d = toConcentricDisk(sample2f(rng));
-            V2 nb = v2(uv.x + d.x * resampleRadius * tx, uv.y + d.y * resampleRadius * ty);
-            Resv neighborResv = resv_zero();
-            resvReset(neighborResv);
-            /* findNeighborReservoir (gris_resample_spatial.glsl:11-34) */
-            if (nb.x < 0.0f || nb.y < 0.0f || nb.x > 1.0f || nb.y > 1.0f) continue;
-            int px = (int)(nb.x * (float)P.cam.w), py = (int)(nb.y * (float)P.cam.h);
-            float depthN = 0.0f; V3 normalN = v3s(0.0f), albedoN = v3s(0.0f); int matMeshIdN = 0;
-            float4 ndn = texture_bilinear(dnT, W, H, nb);
-            uint2 nam = fetch_am(amT, W, H, px, py);
-            if (!unpackGBuffer(ndn, nam, depthN, normalN, albedoN, matMeshIdN)) continue;
-            Ray3 nray = pinholeCameraSampleRay(P.cam, v2(nb.x, 1.0f - nb.y));
-            V3 posN = nray.ori + nray.dir * (depthN - 1e-4f);
-            if (dot3(normalN, norm) < 0.9f || distance3(pos, posN) > 0.4f) continue;
-            uint32_t nidx = (uint32_t)P.cam.w * (uint32_t)py + (uint32_t)px;
-            neighborResv = load_resv(P.b.reservoirTemp, nidx, n);
-            if (resvIsValid(neighborResv))
-                reuseAndMerge(P, resv, dstPrimarySurf, dstPrimaryIsec, ray, neighborResv, rng, rc, err);
-        }
-    }
-    resvResetIfInvalid(resv);
-    store_resv(P.b.reservoirThis, idx, resv);
-    wrote = true;
-
-    if (resvIsValid(resv) && resv.sampleCount > 0.0f) {
-        PathSample pathSample = resv.s;
-        if (pathSample.rcIsec.inst != kInvalidHit) {
-            RcData rcData;
-            rcData.rcPrevIsec = isec_zero(); rcData.rcPrevWo = v3s(0.0f); rcData.rcPrevThroughput = v3s(0.0f);
-            traceReplay(P, dstPrimaryIsec, dstPrimarySurf, ray, pathSample.flags, pathSample.primaryRng, rcData, rc, err);
-            if (rcData.rcPrevIsec.inst != kInvalidHit) {
-                Surf rcPrevSurf = surf_zero(), rcSurf = surf_zero();
-                if (rcData.rcPrevIsec.inst == kSpecialHit) rcPrevSurf = dstPrimarySurf;
-                else loadSurfaceInfo(sc, rcData.rcPrevIsec, rcPrevSurf);
-                loadSurfaceInfo(sc, pathSample.rcIsec, rcSurf);
-                Mat rcMat = load_material(sc, rcSurf.matIndex);
-                Mat rcPrevMat = load_material(sc, rcPrevSurf.matIndex);
-                V3 Li = pathSample.rcLi;
-                uint32_t rcType = rcVertexType(pathSample.flags);
-                V3 wi = normalize3(rcSurf.pos - rcPrevSurf.pos);
-                if (rcType == kRcSurface && length3(pathSample.rcWi) > 0.5f)
-                    Li = Li * (evalBSDF(rcMat, rcSurf.albedo, rcSurf.norm, -wi, pathSample.rcWi) * satDot(rcSurf.norm, pathSample.rcWi));
-                Li = Li * (evalBSDF(rcPrevMat, rcPrevSurf.albedo, rcPrevSurf.norm, rcData.rcPrevWo, wi) * satDot(rcPrevSurf.norm, wi));
-                Li = Li * rcData.rcPrevThroughput;
-                Li = Li / pathSample.rcPrevSamplePdf;
-                if (!isBlack(Li) && !isnan3(Li)) radiance = Li / luminance(Li) * resv.resampleWeight / resv.sampleCount;
-            }
-        }
-    }
-    return clampColor(radiance);
-}
-
-/* ------------------------------------------------------------------ kernels */
-__global__ void __launch_bounds__(128) k_path_trace(PassCtx P) {
-    uint32_t x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y * blockDim.y + threadIdx.y;
-    RayCount rc = ray_count();
-    int err = 0;
-    if (x < P.b.width && y < P.b.height) tracePath(P, x, y, rc, err);
-    flush_counts(P.counters, rc, err, 1, P.countWork);
-}
-
-__global__ void __launch_bounds__(128) k_temporal(PassCtx P) {
-    uint32_t x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y * blockDim.y + threadIdx.y;
-    RayCount rc = ray_count();
-    int err = 0;
-    if (x < P.b.width && y < P.b.height) temporalReuse(P, x, y, rc, err);
-    flush_counts(P.counters, rc, err, 2, P.countWork);
-}
-
-__global__ void __launch_bounds__(128) k_spatial(PassCtx P) {
-    uint32_t x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y * blockDim.y + threadIdx.y;
-    RayCount rc = ray_count();
-    int err = 0;
-    if (x < P.b.width && y < P.b.height) {
-        bool wrote;
-        V3 color = spatialReuse(P, x, y, rc, err, wrote);
-        /* gris_resample_spatial.comp:21-27: running mean over frameIndex & mask frames */
+    GD static void accumulate(const PassCtx& P, uint32_t x, uint32_t y, V3 color) {
         float frameCount = (float)(P.cam.frameIndex & kCameraFrameIndexMask);
         float4* out = reinterpret_cast<float4*>(P.b.output) + (uint64_t)y * P.b.width + x;
         float4 o = *out;
@@ -574,7 +518,169 @@ __global__ void __launch_bounds__(128) k_spatial(PassCtx P) {
         acc = (acc * frameCount + color) / (frameCount + 1.0f);
         *out = make_float4(acc.x, acc.y, acc.z, 1.0f);
     }
-    flush_counts(P.counters, rc, err, 3, P.countWork);
+
+    GD bool begin(const PassCtx& P, uint32_t px, uint32_t py, RayCount&, int&) {
+        const int W = (int)P.b.width, H = (int)P.b.height;
+        ix = px; iy = py;
+        V2 uv = v2(((float)ix + 0.5f) / (float)W, ((float)iy + 0.5f) / (float)H);
+        float depth = 0.0f; V3 norm = v3s(0.0f), albedo = v3s(0.0f); int matMeshId = 0;
+        float4 dn = texture_bilinear(reinterpret_cast<const float4*>(P.b.depthNormal), W, H, uv);
+        uint2 am = fetch_am(reinterpret_cast<const uint2*>(P.b.albedoMatId), W, H, (int)ix, (int)iy);
+        if (!unpackGBuffer(dn, am, depth, norm, albedo, matMeshId)) {
+            accumulate(P, ix, iy, v3s(0.0f));
+            return false;
+        }
+        rng = makeSeed2(P.cam.seed, ix, iy) ^ 2u;
+        ray = pinholeCameraSampleRay(P.cam, v2(uv.x, 1.0f - uv.y));
+        V3 pos = ray.ori + ray.dir * (depth - 1e-4f);
+        int matId = matMeshId >> 16;
+        idx = (uint64_t)iy * W + ix;
+        resv = load_resv(P.b.reservoirTemp, idx, (uint64_t)W * (uint64_t)H);
+        dstIsec.bx = uv.x; dstIsec.by = uv.y; dstIsec.inst = kSpecialHit; dstIsec.tri = 0u;
+        dst.pos = pos; dst.norm = norm; dst.albedo = albedo; dst.matIndex = (uint32_t)matId; dst.isLight = false;
+        i = 0;
+        return true;
+    }
+
+    GD bool step(const PassCtx& P, RayCount& rc, int& err) {
+        const DevScene& sc = P.sc;
+        const int W = (int)P.b.width, H = (int)P.b.height;
+        const uint64_t n = (uint64_t)W * (uint64_t)H;
+        if (P.set.spatialReuse && i < P.set.spatialNeighbors) {
+            i++;
+            const float resampleRadius = P.set.spatialRadius;
+            float tx = 1.0f / (float)W, ty = 1.0f / (float)H;
+            V2 uv = v2(dstIsec.bx, dstIsec.by);
+            V2 d = toConcentricDisk(sample2f(rng));
+            V2 nb = v2(uv.x + d.x * resampleRadius * tx, uv.y + d.y * resampleRadius * ty);
+            if (nb.x < 0.0f || nb.y < 0.0f || nb.x > 1.0f || nb.y > 1.0f) return true;
+            int px = (int)(nb.x * (float)P.cam.w), py = (int)(nb.y * (float)P.cam.h);
+            float depthN = 0.0f; V3 normalN = v3s(0.0f), albedoN = v3s(0.0f); int matMeshIdN = 0;
+            float4 ndn = texture_bilinear(reinterpret_cast<const float4*>(P.b.depthNormal), W, H, nb);
+            uint2 nam = fetch_am(reinterpret_cast<const uint2*>(P.b.albedoMatId), W, H, px, py);
+            if (!unpackGBuffer(ndn, nam, depthN, normalN, albedoN, matMeshIdN)) return true;
+            Ray3 nray = pinholeCameraSampleRay(P.cam, v2(nb.x, 1.0f - nb.y));
+            V3 posN = nray.ori + nray.dir * (depthN - 1e-4f);
+            if (dot3(normalN, dst.norm) < 0.9f || distance3(dst.pos, posN) > 0.4f) return true;
+            uint32_t nidx = (uint32_t)P.cam.w * (uint32_t)py + (uint32_t)px;
+            Resv neighborResv = load_resv(P.b.reservoirTemp, nidx, n);
+            if (resvIsValid(neighborResv)) reuseAndMerge(P, resv, dst, dstIsec, ray, neighborResv, rng, rc, err);
+            return true;
+        }
+        resvResetIfInvalid(resv);
+        store_resv(P.b.reservoirThis, idx, resv);
+        V3 radiance = v3s(0.0f);
+        if (resvIsValid(resv) && resv.sampleCount > 0.0f) {
+            PathSample pathSample = resv.s;
+            if (pathSample.rcIsec.inst != kInvalidHit) {
+                RcData rcData;
+                rcData.rcPrevIsec = isec_zero(); rcData.rcPrevWo = v3s(0.0f); rcData.rcPrevThroughput = v3s(0.0f);
+                traceReplay(P, dstIsec, dst, ray, pathSample.flags, pathSample.primaryRng, rcData, rc, err);
+                if (rcData.rcPrevIsec.inst != kInvalidHit) {
+                    Surf rcPrevSurf = surf_zero(), rcSurf = surf_zero();
+                    if (rcData.rcPrevIsec.inst == kSpecialHit) rcPrevSurf = dst;
+                    else loadSurfaceInfo(sc, rcData.rcPrevIsec, rcPrevSurf);
+                    loadSurfaceInfo(sc, pathSample.rcIsec, rcSurf);
+                    Mat rcMat = load_material(sc, rcSurf.matIndex);
+                    Mat rcPrevMat = load_material(sc, rcPrevSurf.matIndex);
+                    V3 Li = pathSample.rcLi;
+                    uint32_t rcType = rcVertexType(pathSample.flags);
+                    V3 wi = normalize3(rcSurf.pos - rcPrevSurf.pos);
+                    if (rcType == kRcSurface && length3(pathSample.rcWi) > 0.5f)
+                        Li = Li * (evalBSDF(rcMat, rcSurf.albedo, rcSurf.norm, -wi, pathSample.rcWi) * satDot(rcSurf.norm, pathSample.rcWi));
+                    Li = Li * (evalBSDF(rcPrevMat, rcPrevSurf.albedo, rcPrevSurf.norm, rcData.rcPrevWo, wi) * satDot(rcPrevSurf.norm, wi));
+                    Li = Li * rcData.rcPrevThroughput;
+                    Li = Li / pathSample.rcPrevSamplePdf;
+                    if (!isBlack(Li) && !isnan3(Li)) radiance = Li / luminance(Li) * resv.resampleWeight / resv.sampleCount;
+                }
+            }
+        }
+        accumulate(P, ix, iy, clampColor(radiance));
+        return false;
+    }
+};
+
+struct PathTask {
+    PathTracer t;
+    GD bool begin(const PassCtx& P, uint32_t x, uint32_t y, RayCount&, int&) { return t.begin(P, x, y); }
+    GD bool step(const PassCtx& P, RayCount& rc, int& err) {
+        if (!t.step(P, rc, err) || ++t.bounce >= (int)P.set.maxDepth) {
+            t.end(P);
+            return false;
+        }
+        return true;
+    }
+};
+
+/* ------------------------------------------------------------------ launch forms */
+/* Grid form: one thread per pixel of a 16 x 8 tile. */
+template <typename Task>
+GD void run_grid(const PassCtx& P, RayCount& rc, int& err) {
+    uint32_t x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y * blockDim.y + threadIdx.y;
+    if (x >= P.b.width || y >= P.b.height) return;
+    Task t;
+    if (t.begin(P, x, y, rc, err))
+        while (t.step(P, rc, err)) {}
+}
+
+/* Persistent form: warps take 16 x 16 pixel tiles from a global cursor (one atomic per tile);
+ * whenever lanes are idle (path ended, background pixel) they take the tile's next pixels, so a
+ * warp's lanes stay busy while they run paths of different lengths. Per-pixel arithmetic is the
+ * same as in the grid form; only the assignment of pixels to lanes differs. */
+constexpr uint32_t kTileSide = 16;
+constexpr uint32_t kTilePixels = kTileSide * kTileSide;
+
+template <typename Task>
+GD void run_persistent(const PassCtx& P, unsigned int* cursor, RayCount& rc, int& err) {
+    const uint32_t W = P.b.width, H = P.b.height;
+    const uint32_t tilesX = (W + kTileSide - 1) / kTileSide;
+    const uint32_t numTiles = tilesX * ((H + kTileSide - 1) / kTileSide);
+    const uint32_t lane = threadIdx.x & 31u;
+    const unsigned lanesBelow = (1u << lane) - 1u;
+    uint32_t tile = 0, next = kTilePixels;   /* warp-uniform; next == kTilePixels: no current tile */
+    bool active = false, more = true;
+    Task t;
+    while (true) {
+        unsigned idle = __ballot_sync(0xffffffffu, !active);
+        while (idle && more) {
+            if (next >= kTilePixels) {
+                unsigned int v = 0;
+                if (lane == 0) v = atomicAdd(cursor, 1u);
+                tile = __shfl_sync(0xffffffffu, v, 0);
+                next = 0;
+                if (tile >= numTiles) { more = false; break; }
+            }
+            uint32_t n = min((uint32_t)__popc(idle), kTilePixels - next);
+            uint32_t rank = (uint32_t)__popc(idle & lanesBelow);
+            if (!active && rank < n) {
+                uint32_t k = next + rank;
+                uint32_t px = (tile % tilesX) * kTileSide + (k % kTileSide);
+                uint32_t py = (tile / tilesX) * kTileSide + (k / kTileSide);
+                if (px < W && py < H) active = t.begin(P, px, py, rc, err);
+            }
+            next += n;
+            idle = __ballot_sync(0xffffffffu, !active);
+        }
+        if (__ballot_sync(0xffffffffu, active) == 0u) break;
+        if (active) active = t.step(P, rc, err);
+    }
+}
+
+/* ------------------------------------------------------------------ kernels */
+template <typename Task, int KERNEL>
+__global__ void __launch_bounds__(128) k_pass_grid(PassCtx P) {
+    RayCount rc = ray_count();
+    int err = 0;
+    run_grid<Task>(P, rc, err);
+    flush_counts(P.counters, rc, err, KERNEL, P.countWork);
+}
+
+template <typename Task, int KERNEL>
+__global__ void __launch_bounds__(128) k_pass_persistent(PassCtx P) {
+    RayCount rc = ray_count();
+    int err = 0;
+    run_persistent<Task>(P, reinterpret_cast<unsigned int*>(P.counters + 24) + KERNEL, rc, err);
+    flush_counts(P.counters, rc, err, KERNEL, P.countWork);
 }
 
 /* G-buffer (GBuffer.vert:16-28, GBuffer.frag:21-54) by primary rays that ignore instance 0. */
@@ -727,7 +833,7 @@ cudaError_t launch_gbuffer(const DeviceSceneView& scene, const GrisGBufferBindin
 
 cudaError_t launch_gris(const DeviceSceneView& scene, const GrisPassBindings& b, const GrisCamera& cam,
                         const GrisCamera& prevCam, const GrisSettings& set, int passes, unsigned long long* counters,
-                        int countWork, KernelTimer* timer, cudaStream_t stream) {
+                        int countWork, KernelTimer* timer, cudaStream_t stream, int launchMode) {
     PassCtx P;
     P.countWork = countWork;
     P.sc = to_dev(scene);
@@ -737,19 +843,40 @@ cudaError_t launch_gris(const DeviceSceneView& scene, const GrisPassBindings& b,
     P.b = b;
     P.counters = counters;
     dim3 block(16, 8), grid((b.width + 15) / 16, (b.height + 7) / 8);
+    bool persistent = launchMode == GRIS_LAUNCH_PERSISTENT;
+    int blocksPT = 0, blocksT = 0, blocksS = 0;
+    if (persistent) {
+        static int smCount = 0, occ[3] = {0, 0, 0};
+        if (smCount == 0) {
+            int dev = 0;
+            cudaGetDevice(&dev);
+            cudaDeviceGetAttribute(&smCount, cudaDevAttrMultiProcessorCount, dev);
+            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ[0], k_pass_persistent<PathTask, 1>, 128, 0);
+            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ[1], k_pass_persistent<TemporalTask, 2>, 128, 0);
+            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ[2], k_pass_persistent<SpatialTask, 3>, 128, 0);
+        }
+        blocksPT = smCount * (occ[0] > 0 ? occ[0] : 1);
+        blocksT = smCount * (occ[1] > 0 ? occ[1] : 1);
+        blocksS = smCount * (occ[2] > 0 ? occ[2] : 1);
+        cudaError_t e = cudaMemsetAsync(counters + 24, 0, 2 * sizeof(unsigned long long), stream);
+        if (e != cudaSuccess) return e;
+    }
     if (passes & 1) {
         if (timer) timer->mark(1, true, stream);
-        k_path_trace<<<grid, block, 0, stream>>>(P);
+        if (persistent) k_pass_persistent<PathTask, 1><<<blocksPT, 128, 0, stream>>>(P);
+        else k_pass_grid<PathTask, 1><<<grid, block, 0, stream>>>(P);
         if (timer) timer->mark(1, false, stream);
     }
     if (passes & 2) {
         if (timer) timer->mark(2, true, stream);
-        k_temporal<<<grid, block, 0, stream>>>(P);
+        if (persistent) k_pass_persistent<TemporalTask, 2><<<blocksT, 128, 0, stream>>>(P);
+        else k_pass_grid<TemporalTask, 2><<<grid, block, 0, stream>>>(P);
         if (timer) timer->mark(2, false, stream);
     }
     if (passes & 4) {
         if (timer) timer->mark(3, true, stream);
-        k_spatial<<<grid, block, 0, stream>>>(P);
+        if (persistent) k_pass_persistent<SpatialTask, 3><<<blocksS, 128, 0, stream>>>(P);
+        else k_pass_grid<SpatialTask, 3><<<grid, block, 0, stream>>>(P);
         if (timer) timer->mark(3, false, stream);
     }
     return cudaGetLastError();

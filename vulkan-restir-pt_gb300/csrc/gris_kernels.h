@@ -35,7 +35,7 @@ cudaError_t launch_gbuffer(const DeviceSceneView& scene, const GrisGBufferBindin
                            unsigned long long* counters, int countWork, KernelTimer* timer, cudaStream_t stream);
 cudaError_t launch_gris(const DeviceSceneView& scene, const GrisPassBindings& b, const GrisCamera& cam,
                         const GrisCamera& prevCam, const GrisSettings& set, int passes, unsigned long long* counters,
-                        int countWork, KernelTimer* timer, cudaStream_t stream);
+                        int countWork, KernelTimer* timer, cudaStream_t stream, int launchMode = GRIS_LAUNCH_PERSISTENT);
 cudaError_t launch_debug_trace(const uint32_t* nodes, const float* tris, const float* rays, uint64_t n, int anyHit,
                                float* hitTUV, uint32_t* hitInst, uint32_t* hitTri, unsigned long long* counters,
                                cudaStream_t stream);

@@ -34,6 +34,7 @@ assert MATERIAL.itemsize == 32 and VERTEX.itemsize == 32 and INSTANCE.itemsize =
 assert LIGHT.itemsize == 64 and TABLE.itemsize == 8 and RESERVOIR.itemsize == 96
 
 INVALID_HIT = 0xFFFFFFFF
+LAUNCH_GRID, LAUNCH_PERSISTENT = 0, 1
 NOALLOC_MAX_PIXELS = 65536
 CLEAR_FLAG = 0x80000000
 
@@ -103,7 +104,7 @@ class SceneStats(ctypes.Structure):
 
 EXPORTS = [
     "grisCreate", "grisDestroy", "grisGetError", "grisSync", "grisGetStream", "grisReadCounters", "grisGetVersion",
-    "grisSetProfiling", "grisReadProfile", "grisSetWorkCounting", "grisReadWorkCounters",
+    "grisSetProfiling", "grisReadProfile", "grisSetWorkCounting", "grisReadWorkCounters", "grisSetLaunchMode",
     "grisSizeof", "grisBuildLightTable", "grisCameraSetup", "grisCameraLookAt", "grisHostSceneCreate",
     "grisHostSceneDesc", "grisHostSceneCamera", "grisHostSceneDestroy", "grisSceneCreate", "grisSceneDestroy",
     "grisSceneGetStats", "grisDebugHostSceneCreate", "grisDebugTraceHost", "grisDebugTraceDevice", "grisPassGBuffer", "grisPassRender", "grisPassRenderNoAlloc",
@@ -135,6 +136,7 @@ def load(path=None):
         "grisSetProfiling": (i32, [vp, i32]),
         "grisReadProfile": (i32, [vp, ctypes.POINTER(ctypes.c_double), ctypes.POINTER(u64), i32]),
         "grisSetWorkCounting": (i32, [vp, i32]),
+        "grisSetLaunchMode": (i32, [vp, i32]),
         "grisReadWorkCounters": (i32, [vp, ctypes.POINTER(u64), ctypes.POINTER(u64), ctypes.POINTER(u64), i32]),
         "grisSizeof": (ctypes.c_size_t, [i32]),
         "grisBuildLightTable": (i32, [vp, u32, vp]),
@@ -316,6 +318,10 @@ class Context:
         n = (ctypes.c_uint64 * 4)()
         self.check(load().grisReadProfile(self.h, ms, n, int(reset)), "grisReadProfile")
         return list(ms), list(n)
+
+    def set_launch_mode(self, mode):
+        """0: grid (one thread per pixel), 1: persistent with per-lane refill (default)."""
+        self.check(load().grisSetLaunchMode(self.h, int(mode)), "grisSetLaunchMode")
 
     def set_work_counting(self, enable):
         self.check(load().grisSetWorkCounting(self.h, int(enable)), "grisSetWorkCounting")
