@@ -445,7 +445,11 @@ void build_terrain(GrisHostScene& s, uint32_t gridN, uint32_t spheres, bool glos
         if (gi >= gridN) gi = gridN - 1;
         if (gj >= gridN) gj = gridN - 1;
         float pz = hgt[(size_t)gj * gridN + gi] + radius * 0.7f;
-        H3 col = h3(0.2f + 0.75f * rng.uniform(), 0.2f + 0.75f * rng.uniform(), 0.2f + 0.75f * rng.uniform());
+        /* one draw per statement: the order of evaluation of function arguments is unspecified */
+        float cr = 0.2f + 0.75f * rng.uniform();
+        float cg = 0.2f + 0.75f * rng.uniform();
+        float cb = 0.2f + 0.75f * rng.uniform();
+        H3 col = h3(cr, cg, cb);
         float rough, metal;
         if (glossy) { rough = 0.02f + 0.28f * rng.uniform(); metal = rng.uniform() < 0.7f ? 1.0f : 0.0f; }
         else { rough = 0.05f + 0.95f * rng.uniform(); metal = rng.uniform() < 0.3f ? 1.0f : 0.0f; }
@@ -455,8 +459,8 @@ void build_terrain(GrisHostScene& s, uint32_t gridN, uint32_t spheres, bool glos
         for (uint32_t f : SF) s.indices.push_back(sBase + f);
         for (size_t f = 0; f < SF.size() / 3; f++) s.materialIndices.push_back((int32_t)mat);
         s.instances.emplace_back();
-        set_instance(s.instances.back(), m4_translate_scale_rotz(h3(px, py, pz), radius, 6.2831853f * rng.uniform()),
-                     off, (uint32_t)SF.size(), mat);
+        float rot = 6.2831853f * rng.uniform();
+        set_instance(s.instances.back(), m4_translate_scale_rotz(h3(px, py, pz), radius, rot), off, (uint32_t)SF.size(), mat);
     }
     /* four 8 x 8 quad lights at height 22, facing down */
     H3 lightPos[4] = {h3(-20, -20, 22), h3(20, -20, 22), h3(20, 20, 22), h3(-20, 20, 22)};
