@@ -9,6 +9,7 @@ byte, so host arrays pass straight through the ABI.
 """
 import ctypes
 import os
+import sys
 
 import numpy as np
 
@@ -249,7 +250,7 @@ class HostScene:
         return len(self.lights) + int(sum(int(i["indexCount"]) // 3 for i in self.instances))
 
     def __del__(self):
-        if getattr(self, "_h", None) and _lib is not None:
+        if getattr(self, "_h", None) and _lib is not None and not sys.is_finalizing():
             _lib.grisHostSceneDestroy(self._h)
             self._h = None
 
@@ -338,6 +339,9 @@ class Context:
             self.h = None
 
     def __del__(self):
+        # at interpreter exit the CUDA runtime may already be torn down: leave it to the driver
+        if sys.is_finalizing():
+            return
         try:
             self.close()
         except Exception:
@@ -375,6 +379,9 @@ class Scene:
             self.h = None
 
     def __del__(self):
+        # at interpreter exit the CUDA runtime may already be torn down: leave it to the driver
+        if sys.is_finalizing():
+            return
         try:
             self.close()
         except Exception:
@@ -420,6 +427,9 @@ class Frame:
             self.handle = None
 
     def __del__(self):
+        # at interpreter exit the CUDA runtime may already be torn down: leave it to the driver
+        if sys.is_finalizing():
+            return
         try:
             self.close()
         except Exception:
