@@ -120,15 +120,6 @@ GRIS_HD bool gris_tri_test(const float* T, float ox, float oy, float oz, float d
 
 GRIS_HD uint32_t gris_byte(uint32_t w, int i) { return (w >> (i * 8)) & 0xffu; }
 
-/* byte i of w as a float, exactly: the byte is placed in the low mantissa bits of 2^23 */
-GRIS_HD float gris_qbyte(uint32_t w, int i) {
-#ifdef __CUDA_ARCH__
-    return __uint_as_float(__byte_perm(w, 0x4B000000u, 0x7440u | (uint32_t)i)) - 8388608.0f;
-#else
-    return (float)gris_byte(w, i);
-#endif
-}
-
 /*
  * Walks the BVH. ANY: return at the first accepted hit (shadow rays). skipInst0: ignore the
  * light instance (the G-buffer is rasterised without lights). Returns true if a hit was
@@ -182,25 +173,25 @@ GRIS_HD bool gris_bvh_trace(const uint32_t* __restrict__ nodes, const float* __r
             float ax = sx * idx, ay = sy * idy, az = sz * idz;
             float bx = (px - ox) * idx, by = (py - oy) * idy, bz = (pz - oz) * idz;
             uint32_t innerHits = 0, triHits = 0;
-            /* all 8 slots without branches (lanes visiting different nodes stay converged);
-             * a quantised byte q becomes the float q exactly as (2^23 + q) - 2^23 */
 #pragma unroll
             for (int s = 0; s < 8; s++) {
-                const int wi = s >> 2, bi = s & 3;
-                uint32_t meta = gris_byte(W[6 + wi], bi);
-                float lx = gris_fma(gris_qbyte(W[8 + wi], bi), ax, bx);
-                float ly = gris_fma(gris_qbyte(W[10 + wi], bi), ay, by);
-                float lz = gris_fma(gris_qbyte(W[12 + wi], bi), az, bz);
-                float hx = gris_fma(gris_qbyte(W[14 + wi], bi), ax, bx);
-                float hy = gris_fma(gris_qbyte(W[16 + wi], bi), ay, by);
-                float hz = gris_fma(gris_qbyte(W[18 + wi], bi), az, bz);
+                uint32_t meta = gris_byte(W[6 + (s >> 2)], s & 3);
+                if (meta == 0) continue;
+                int wi = s >> 2, bi = s & 3;
+                float lx = gris_fma((float)gris_byte(W[8 + wi], bi), ax, bx);
+                float ly = gris_fma((float)gris_byte(W[10 + wi], bi), ay, by);
+                float lz = gris_fma((float)gris_byte(W[12 + wi], bi), az, bz);
+                float hx = gris_fma((float)gris_byte(W[14 + wi], bi), ax, bx);
+                float hy = gris_fma((float)gris_byte(W[16 + wi], bi), ay, by);
+                float hz = gris_fma((float)gris_byte(W[18 + wi], bi), az, bz);
                 float tn = gris_fmax(gris_fmax(gris_fmin(lx, hx), gris_fmin(ly, hy)), gris_fmax(gris_fmin(lz, hz), tmin));
                 float tf = gris_fmin(gris_fmin(gris_fmax(lx, hx), gris_fmax(ly, hy)), gris_fmin(gris_fmax(lz, hz), bestT));
-                bool hit = (meta != 0u) && (tn <= tf);
-                bool inner = (imask >> s) & 1u;
-                uint32_t cnt = (meta >> 5) & 3u, off = meta & 31u;
-                innerHits |= (hit && inner) ? (1u << (s ^ oct)) : 0u;
-                triHits |= (hit && !inner) ? (((1u << cnt) - 1u) << off) : 0u;
+                if (!(tn <= tf)) continue;
+                if (imask & (1u << s)) innerHits |= 1u << (s ^ oct);
+                else {
+                    uint32_t cnt = (meta >> 5) & 3u, off = meta & 31u;
+                    triHits |= ((1u << cnt) - 1u) << off;
+                }
             }
             uint32_t triBase = W[5];
             while (triHits) {

@@ -14,7 +14,8 @@ import sys
 import numpy as np
 
 _HERE = os.path.dirname(os.path.abspath(__file__))
-LIB_PATH = os.path.join(_HERE, "libgrisrt.so")
+# GRISRT_LIBRARY selects another build of the library (e.g. a variant being compared).
+LIB_PATH = os.environ.get("GRISRT_LIBRARY") or os.path.join(_HERE, "libgrisrt.so")
 
 # ---------------------------------------------------------------- layouts (numpy)
 MATERIAL = np.dtype([("baseColor", "<f4", 3), ("type", "<u4"), ("textureIdx", "<u4"), ("metallic", "<f4"),
