@@ -63,7 +63,10 @@ def parse():
     ap.add_argument("--depth", type=int, default=8)
     ap.add_argument("--seed", type=int, default=1)
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--launch-mode", default="persistent", choices=["persistent", "grid"])
+    ap.add_argument("--launch-mode", default="grid", choices=["persistent", "grid"])
+    ap.add_argument("--api", default="batch", choices=["batch", "frame"],
+                    help="grisBatchRender (one-view batch) or grisFrameRender")
+    ap.add_argument("--path-form", default="wavefront", choices=["wavefront", "megakernel"])
     ap.add_argument("--cpu-seconds", type=float, default=20.0, help="target CPU work of the baseline sample")
     return ap.parse_args()
 
@@ -208,10 +211,14 @@ def main():
     config["triangles"] = hs.triangle_count()
     ctx = G.Context(local)
     ctx.set_launch_mode(G.LAUNCH_PERSISTENT if args.launch_mode == "persistent" else G.LAUNCH_GRID)
-    config["launch"] = args.launch_mode
+    ctx.set_path_form(G.PATH_WAVEFRONT if args.path_form == "wavefront" else G.PATH_MEGAKERNEL)
+    config["api"] = args.api
+    config["launch"] = args.launch_mode if args.api == "frame" else "batch tiles"
+    config["path_form"] = args.path_form if args.api == "batch" else "megakernel"
     scene = G.Scene(ctx, hs)
     stats = scene.stats()
-    frame = G.Frame(ctx, W, H)
+    frame = G.Frame(ctx, W, H) if args.api == "frame" else None
+    batch = G.Batch(ctx, [scene], [(W, H)]) if args.api == "batch" else None
     total = WU + 2 * K + 4
     cams, prevs = G.sequence_cameras(hs, total, W, H, seed=args.seed, orbit_frames=60)
     stream = torch.cuda.ExternalStream(ctx.stream(), device=torch.device("cuda", local))
@@ -219,7 +226,13 @@ def main():
     fi = 0
 
     def render(i):
-        frame.render(scene, cams[i], prevs[i], settings)
+        if batch is not None:
+            batch.render([cams[i]], [prevs[i]], [settings])
+        else:
+            frame.render(scene, cams[i], prevs[i], settings)
+
+    def output_ptr():
+        return batch.device_ptr(0, G.BUF_OUTPUT)[0] if batch is not None else frame.device_ptr(G.BUF_OUTPUT)[0]
 
     for _ in range(WU):
         render(fi)
@@ -253,6 +266,9 @@ def main():
     clocks = sampler.stop()
     ms = sum(a.elapsed_time(b) for a, b in events)
     kms, klaunch = ctx.profile(reset=True)
+    # kernels per frame: G-buffer, temporal, spatial + the path tracer (one kernel, or the
+    # wavefront's begin + 4 stages for each further bounce)
+    launches_per_frame = 4 if (args.api == "frame" or args.path_form == "megakernel") else 3 + 1 + 4 * (args.depth - 1)
     ctx.set_profiling(False)
     cnt = ctx.counters(reset=True)
     ctx.sync()
@@ -277,13 +293,16 @@ def main():
 
     # ---------------- end to end through the C ABI with host buffers
     out_host = torch.empty((W * H * 4,), dtype=torch.float32, pin_memory=True)
-    lib = G.load()
+    cudart = torch.cuda.cudart()
     barrier()
     t0 = time.perf_counter()
     for _ in range(K):
         render(fi)
-        ctx.check(lib.grisFrameDownload(ctx.h, frame.handle, G.BUF_OUTPUT, 0, ctypes.c_void_p(out_host.data_ptr()),
-                                        W * H * 16), "grisFrameDownload")
+        # the frame's radiance to pinned host memory, on the library's stream, then wait for it
+        rc = cudart.cudaMemcpyAsync(out_host.data_ptr(), output_ptr(), W * H * 16, 2, ctx.stream())
+        if int(rc) != 0:
+            raise RuntimeError("cudaMemcpyAsync failed")
+        ctx.sync()
         fi += 1
     barrier()
     e2e_s = time.perf_counter() - t0
@@ -338,7 +357,8 @@ def main():
                 "mrays_per_s": mrays, "rays_per_frame": rays / K,
                 "bvh": {"nodes": stats.nodeCount, "node_mb": stats.nodeBytes / 1e6, "tri_mb": stats.triangleBytes / 1e6,
                         "depth": stats.maxDepth, "build_s": stats.buildSeconds},
-                "clocks": clocks, "e2e": e2e, "gpu_launches": 4 * K, "roofline": roofline, "cpu_baseline": cpu}
+                "clocks": clocks, "e2e": e2e, "gpu_launches": launches_per_frame * K, "roofline": roofline,
+                "cpu_baseline": cpu}
         print(json.dumps(line))
     if world > 1:
         torch.distributed.destroy_process_group()

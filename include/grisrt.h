@@ -210,9 +210,9 @@ int grisReadProfile(GrisContext* ctx, double msTotal[4], uint64_t launches[4], i
 /* Traversal work per kernel while enabled: BVH nodes intersected, triangles tested and
  * closest-hit rays (primary rays for the G-buffer); shadow rays are in grisReadCounters. */
 int grisSetWorkCounting(GrisContext* ctx, int enable);
-/* Launch form of the three GRIS passes: GRIS_LAUNCH_GRID (one thread per pixel of a 16 x 8 tile)
- * or GRIS_LAUNCH_PERSISTENT (default: resident warps take 16 x 16 pixel tiles and refill idle
- * lanes pixel by pixel). Results are identical; only speed differs. */
+/* Launch form of the three GRIS passes: GRIS_LAUNCH_GRID (default: one thread per pixel of a
+ * 16 x 8 tile) or GRIS_LAUNCH_PERSISTENT (resident warps take 16 x 16 pixel tiles and refill
+ * idle lanes pixel by pixel). Results are identical; only speed differs. */
 #define GRIS_LAUNCH_GRID 0
 #define GRIS_LAUNCH_PERSISTENT 1
 int grisSetLaunchMode(GrisContext* ctx, int mode);
@@ -283,6 +283,27 @@ int grisPassRender(GrisContext* ctx, const GrisScene* scene, const GrisPassBindi
 #define GRIS_NOALLOC_MAX_PIXELS 65536
 int grisPassRenderNoAlloc(const GrisScene* scene, const GrisPassBindings* b, const GrisCamera* cam,
                           const GrisCamera* prevCam, const GrisSettings* settings, void* stream);
+
+/* ---------------------------------------------------------------- batches of views */
+/* A batch renders many independent views per frame — each with its own scene, resolution,
+ * cameras and settings (depth, reuse, ...) — with one launch per pass for all of them (the
+ * per-frame view table lives in device memory). Buffers are library-owned per view, with the
+ * renderer's ping-pong, as for grisFrame*. The path tracer runs either as one kernel per frame
+ * (GRIS_PATH_MEGAKERNEL) or as wavefront stages per bounce — closest hits, shading, shadow
+ * queries, NEE + BSDF sampling — over queues of live paths compacted at every bounce
+ * (GRIS_PATH_WAVEFRONT, default). Results are identical either way. */
+#define GRIS_PATH_MEGAKERNEL 0
+#define GRIS_PATH_WAVEFRONT 1
+typedef struct GrisBatch GrisBatch;
+int grisSetPathForm(GrisContext* ctx, int form);
+int grisBatchCreate(GrisContext* ctx, uint32_t nViews, const GrisScene* const* scenes, const uint32_t* widths,
+                    const uint32_t* heights, GrisBatch** out);
+int grisBatchDestroy(GrisBatch* batch);
+/* cams, prevCams, settings: nViews entries each (filmSize must match the view's size). */
+int grisBatchRender(GrisContext* ctx, GrisBatch* batch, const GrisCamera* cams, const GrisCamera* prevCams,
+                    const GrisSettings* settings);
+/* which / slot as in grisFrameGetBuffer, for one view. */
+int grisBatchGetBuffer(const GrisBatch* batch, uint32_t view, int which, int slot, void** devPtr, size_t* bytes);
 
 /* ---------------------------------------------------------------- frames (library-owned buffers) */
 /* G-buffer cur/prev, reservoirs This[2]/Temp, output: the renderer's per-frame resources

@@ -1,0 +1,73 @@
+"""Batches (grisBatch*): many views with their own scene, size, depth and reuse settings rendered
+with one launch per pass, by the megakernel and by the wavefront path tracer (per-bounce
+compacted queues). Every buffer of every view must equal the oracle's, bit for bit."""
+import numpy as np
+import pytest
+
+import grisrt as G
+from oracle import pyoracle as O
+
+pytestmark = pytest.mark.gpu
+
+VIEWS = [   # kind, grid, spheres, W, H, settings
+    (0, 0, 0, 40, 32, dict(maxDepth=3, spatialRadius=30.0)),
+    (1, 40, 30, 64, 48, dict(maxDepth=8)),
+    (2, 32, 24, 24, 24, dict(maxDepth=10, rrScale=0.5)),
+    (0, 0, 0, 16, 16, dict(maxDepth=2, temporalReuse=False)),
+    (1, 24, 10, 33, 17, dict(maxDepth=5, spatialNeighbors=5, cap=7)),
+    (2, 40, 40, 48, 40, dict(maxDepth=6, shiftType=0)),
+]
+FRAMES = 3
+
+
+@pytest.fixture(scope="module")
+def setup():
+    ctx = G.Context(0)
+    hss = [G.HostScene(k, seed=10 + i, grid=g, spheres=sp) for i, (k, g, sp, W, H, kw) in enumerate(VIEWS)]
+    scenes = [G.Scene(ctx, hs) for hs in hss]
+    seqs = [G.sequence_cameras(hs, FRAMES, W, H, seed=30 + i) for i, (hs, (k, g, sp, W, H, kw)) in enumerate(zip(hss, VIEWS))]
+    settings = [G.Settings.make(**kw) for (k, g, sp, W, H, kw) in VIEWS]
+    ora = O.oracle()
+    want = []
+    for i, (k, g, sp, W, H, kw) in enumerate(VIEWS):
+        ora.set_scene(hss[i])
+        want.append(O.run_sequence(ora, seqs[i][0], seqs[i][1], settings[i], W, H))
+    yield ctx, hss, scenes, seqs, settings, want
+    for sc in scenes:
+        sc.close()
+    ctx.close()
+
+
+@pytest.mark.parametrize("form", [G.PATH_WAVEFRONT, G.PATH_MEGAKERNEL], ids=["wavefront", "megakernel"])
+def test_batch_views_match_oracle(setup, form):
+    ctx, hss, scenes, seqs, settings, want = setup
+    ctx.set_path_form(form)
+    batch = G.Batch(ctx, scenes, [(W, H) for (k, g, sp, W, H, kw) in VIEWS])
+    ctx.counters(reset=True)
+    keys = {"resv": G.BUF_RESERVOIR, "temp": G.BUF_TEMP, "out": G.BUF_OUTPUT, "dn": G.BUF_DEPTH_NORMAL,
+            "am": G.BUF_ALBEDO_MATID, "mv": G.BUF_MOTION}
+    for f in range(FRAMES):
+        batch.render([seqs[v][0][f] for v in range(len(VIEWS))], [seqs[v][1][f] for v in range(len(VIEWS))], settings)
+        for v in range(len(VIEWS)):
+            for k, which in keys.items():
+                got = batch.download(v, which)
+                w = want[v][f][k]
+                assert got.tobytes() == w.tobytes(), "form %d frame %d view %d buffer %s differs" % (form, f, v, k)
+    ctx.sync()
+    assert ctx.counters()[3] == 0
+    batch.close()
+    ctx.set_path_form(G.PATH_WAVEFRONT)
+
+
+def test_single_view_batch_equals_frame_api(setup):
+    ctx, hss, scenes, seqs, settings, want = setup
+    k, g, sp, W, H, kw = VIEWS[1]
+    batch = G.Batch(ctx, [scenes[1]], [(W, H)])
+    fr = G.Frame(ctx, W, H)
+    for f in range(FRAMES):
+        batch.render([seqs[1][0][f]], [seqs[1][1][f]], [settings[1]])
+        fr.render(scenes[1], seqs[1][0][f], seqs[1][1][f], settings[1])
+        assert batch.download(0, G.BUF_RESERVOIR).tobytes() == fr.download(G.BUF_RESERVOIR).tobytes()
+        assert batch.download(0, G.BUF_OUTPUT).tobytes() == fr.download(G.BUF_OUTPUT).tobytes()
+    fr.close()
+    batch.close()

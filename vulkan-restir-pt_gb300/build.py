@@ -20,7 +20,7 @@ LIB = os.path.join(OUT_DIR, "libgrisrt.so")
 BUILD = os.path.join(HERE, "_build")
 
 CUDA_SOURCES = ["gris_kernels.cu", "noalloc.cu"]
-HOST_SOURCES = ["capi.cpp", "host_scene.cpp", "bvh_build.cpp"]
+HOST_SOURCES = ["capi.cpp", "batch.cpp", "host_scene.cpp", "bvh_build.cpp"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 

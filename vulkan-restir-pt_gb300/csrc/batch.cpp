@@ -1,0 +1,185 @@
+/*
+ * batch.cpp — batches of views rendered with one launch per pass (C ABI: grisBatch*).
+ *
+ * The per-view buffers are the renderer's per-frame resources (src/Renderer.cpp:193-257) with
+ * its ping-pong (Renderer.cpp:329-347, 567), laid out view after view in one allocation per
+ * buffer kind; the wavefront path tracer's state and queues are sized for all views' pixels.
+ */
+#include <cuda_runtime.h>
+#include <string.h>
+
+#include <string>
+#include <vector>
+
+#include "../../include/grisrt.h"
+#include "gris_kernels.h"
+#include "grisrt_internal.h"
+
+struct GrisBatch {
+    GrisContext* ctx = nullptr;
+    uint32_t n = 0;
+    std::vector<const GrisScene*> scenes;
+    std::vector<uint32_t> w, h;
+    std::vector<uint64_t> base;   /* first pixel of each view */
+    uint64_t pixels = 0;
+    /* per-view frame buffers, view after view */
+    float* depthNormal[2] = {nullptr, nullptr};
+    uint32_t* albedoMatId[2] = {nullptr, nullptr};
+    uint16_t* motion = nullptr;
+    GrisReservoir* resv[2] = {nullptr, nullptr};
+    GrisReservoir* temp = nullptr;
+    float* output = nullptr;
+    /* wavefront path tracer */
+    grisrt::WaveBuffers wave{};
+    std::vector<void*> allocations;
+    /* view table: device copy, double-buffered pinned staging guarded by events */
+    void* dViews = nullptr;
+    void* hViews[2] = {nullptr, nullptr};
+    cudaEvent_t staged[2] = {nullptr, nullptr};
+    int stage = 0;
+    int next = 0;
+};
+
+using namespace grisrt;
+
+extern "C" {
+
+int grisBatchCreate(GrisContext* ctx, uint32_t n, const GrisScene* const* scenes, const uint32_t* widths,
+                    const uint32_t* heights, GrisBatch** out) {
+    if (!ctx || !out || !scenes || !widths || !heights || n == 0 || n > 4096)
+        return ctx_fail(ctx, GRIS_ERR_INVALID_ARGUMENT, "bad batch description");
+    *out = nullptr;
+    cudaSetDevice(ctx_device(ctx));
+    GrisBatch* b = new GrisBatch();
+    b->ctx = ctx;
+    b->n = n;
+    for (uint32_t i = 0; i < n; i++) {
+        DeviceSceneView v;
+        int dev = -1;
+        if (!scenes[i] || !scene_device(scenes[i], &v, &dev) || dev != ctx_device(ctx) || widths[i] == 0 || heights[i] == 0) {
+            delete b;
+            return ctx_fail(ctx, GRIS_ERR_INVALID_ARGUMENT, "batch view " + std::to_string(i) + ": bad scene or size");
+        }
+        b->scenes.push_back(scenes[i]);
+        b->w.push_back(widths[i]);
+        b->h.push_back(heights[i]);
+        b->base.push_back(b->pixels);
+        b->pixels += (uint64_t)widths[i] * heights[i];
+    }
+    if (b->pixels >= 0xffffffffull) { delete b; return ctx_fail(ctx, GRIS_ERR_TOO_LARGE, "batch has too many pixels"); }
+    cudaError_t e = cudaSuccess;
+    cudaStream_t st = ctx_stream(ctx);
+    auto alloc = [&](void** p, size_t bytes, bool zero) {
+        if (e != cudaSuccess) return;
+        e = cudaMalloc(p, bytes < 256 ? 256 : bytes);
+        if (e == cudaSuccess) b->allocations.push_back(*p);
+        if (e == cudaSuccess && zero) e = cudaMemsetAsync(*p, 0, bytes, st);
+    };
+    size_t P = (size_t)b->pixels;
+    for (int i = 0; i < 2; i++) {
+        alloc((void**)&b->depthNormal[i], P * 16, true);
+        alloc((void**)&b->albedoMatId[i], P * 8, true);
+        alloc((void**)&b->resv[i], P * sizeof(GrisReservoir), true);
+    }
+    alloc((void**)&b->motion, P * 4, true);
+    alloc((void**)&b->temp, P * sizeof(GrisReservoir), true);
+    alloc((void**)&b->output, P * 16, true);
+    size_t per = wave_bytes_per_path();
+    (void)per;
+    alloc(&b->wave.state, P * 272, false);
+    alloc(&b->wave.nee, P * 96, false);
+    alloc(&b->wave.hit, P * 16, false);
+    alloc((void**)&b->wave.blocked, P, false);
+    alloc((void**)&b->wave.queue[0], P * 4, false);
+    alloc((void**)&b->wave.queue[1], P * 4, false);
+    alloc((void**)&b->wave.shadowQueue, P * 4, false);
+    alloc((void**)&b->wave.counts, 512 * 4, true);
+    b->wave.capacity = P;
+    alloc(&b->dViews, view_entry_bytes() * n, false);
+    for (int i = 0; i < 2 && e == cudaSuccess; i++) {
+        e = cudaMallocHost(&b->hViews[i], view_entry_bytes() * n);
+        if (e == cudaSuccess) e = cudaEventCreateWithFlags(&b->staged[i], cudaEventDisableTiming);
+    }
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    if (e != cudaSuccess) {
+        grisBatchDestroy(b);
+        return ctx_fail(ctx, e == cudaErrorMemoryAllocation ? GRIS_ERR_OUT_OF_MEMORY : GRIS_ERR_CUDA,
+                        std::string("batch allocation: ") + cudaGetErrorString(e));
+    }
+    *out = b;
+    return GRIS_OK;
+}
+
+int grisBatchDestroy(GrisBatch* b) {
+    if (!b) return GRIS_ERR_INVALID_ARGUMENT;
+    cudaSetDevice(ctx_device(b->ctx));
+    cudaStreamSynchronize(ctx_stream(b->ctx));
+    for (void* p : b->allocations) cudaFree(p);
+    for (int i = 0; i < 2; i++) {
+        if (b->hViews[i]) cudaFreeHost(b->hViews[i]);
+        if (b->staged[i]) cudaEventDestroy(b->staged[i]);
+    }
+    delete b;
+    return GRIS_OK;
+}
+
+int grisBatchRender(GrisContext* ctx, GrisBatch* b, const GrisCamera* cams, const GrisCamera* prevCams,
+                    const GrisSettings* settings) {
+    if (!ctx || !b || !cams || !prevCams || !settings || b->ctx != ctx)
+        return ctx_fail(ctx, GRIS_ERR_INVALID_ARGUMENT, "null argument");
+    cudaSetDevice(ctx_device(ctx));
+    std::vector<BatchView> views(b->n);
+    int j = b->next;
+    for (uint32_t i = 0; i < b->n; i++) {
+        if (cams[i].filmSize[0] != b->w[i] || cams[i].filmSize[1] != b->h[i])
+            return ctx_fail(ctx, GRIS_ERR_INVALID_ARGUMENT, "view " + std::to_string(i) + ": camera filmSize differs from the view size");
+        if (settings[i].maxDepth == 0 || settings[i].maxDepth > 255 || settings[i].spatialNeighbors > 64)
+            return ctx_fail(ctx, GRIS_ERR_INVALID_ARGUMENT, "view " + std::to_string(i) + ": bad settings");
+        BatchView& v = views[i];
+        int dummy = 0;
+        scene_device(b->scenes[i], &v.scene, &dummy);
+        uint64_t o = b->base[i];
+        v.b.width = b->w[i]; v.b.height = b->h[i];
+        v.b.depthNormal = b->depthNormal[j] + o * 4; v.b.depthNormalPrev = b->depthNormal[j ^ 1] + o * 4;
+        v.b.albedoMatId = b->albedoMatId[j] + o * 2; v.b.albedoMatIdPrev = b->albedoMatId[j ^ 1] + o * 2;
+        v.b.motion = b->motion + o * 2;
+        v.b.reservoirThis = b->resv[j] + o; v.b.reservoirPrev = b->resv[j ^ 1] + o; v.b.reservoirTemp = b->temp + o;
+        v.b.output = b->output + o * 4;
+        v.gb.width = b->w[i]; v.gb.height = b->h[i];
+        v.gb.depthNormal = b->depthNormal[j] + o * 4; v.gb.albedoMatId = b->albedoMatId[j] + o * 2; v.gb.motion = b->motion + o * 2;
+        v.cam = cams[i]; v.prev = prevCams[i]; v.set = settings[i];
+    }
+    int k = b->stage;
+    cudaError_t e = cudaEventSynchronize(b->staged[k]);   /* the staging slot's previous copy is done */
+    if (e == cudaSuccess)
+        e = launch_batch(views.data(), (int)b->n, b->dViews, b->hViews[k], b->wave, ctx_counters(ctx), ctx_count_work(ctx),
+                         ctx_timer(ctx), ctx_stream(ctx), ctx_path_form(ctx), 15);
+    if (e == cudaSuccess) e = cudaEventRecord(b->staged[k], ctx_stream(ctx));
+    if (e != cudaSuccess) return ctx_fail(ctx, GRIS_ERR_CUDA, std::string("grisBatchRender: ") + cudaGetErrorString(e));
+    b->stage ^= 1;
+    b->next ^= 1;
+    return GRIS_OK;
+}
+
+int grisBatchGetBuffer(const GrisBatch* b, uint32_t view, int which, int slot, void** devPtr, size_t* bytes) {
+    if (!b || !devPtr || view >= b->n || slot < 0 || slot > 1) return GRIS_ERR_INVALID_ARGUMENT;
+    int j = (b->next ^ 1) ^ slot;
+    size_t n = (size_t)b->w[view] * b->h[view];
+    uint64_t o = b->base[view];
+    void* p = nullptr;
+    size_t sz = 0;
+    switch (which) {
+    case 0: p = b->depthNormal[j] + o * 4; sz = n * 16; break;
+    case 1: p = b->albedoMatId[j] + o * 2; sz = n * 8; break;
+    case 2: p = b->motion + o * 2; sz = n * 4; break;
+    case 3: p = b->resv[j] + o; sz = n * sizeof(GrisReservoir); break;
+    case 4: p = b->temp + o; sz = n * sizeof(GrisReservoir); break;
+    case 5: p = b->output + o * 4; sz = n * 16; break;
+    default: return GRIS_ERR_INVALID_ARGUMENT;
+    }
+    *devPtr = p;
+    if (bytes) *bytes = sz;
+    return GRIS_OK;
+}
+
+}  /* extern "C" */

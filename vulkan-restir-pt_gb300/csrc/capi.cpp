@@ -78,7 +78,8 @@ struct GrisContext {
     unsigned long long* dCounters = nullptr;
     unsigned long long* hCounters = nullptr;   /* pinned */
     int countWork = 0;
-    int launchMode = GRIS_LAUNCH_PERSISTENT;
+    int launchMode = GRIS_LAUNCH_GRID;
+    int pathForm = GRIS_PATH_WAVEFRONT;
     Profiler prof;
     std::string err;
 };
@@ -133,6 +134,14 @@ int upload(GrisContext* ctx, GrisScene* s, const T* src, uint64_t n, const T** d
 grisrt::DeviceSceneView scene_view(const GrisScene* s) { return s->view; }
 
 }  // namespace
+
+int grisrt::ctx_device(GrisContext* ctx) { return ctx->device; }
+cudaStream_t grisrt::ctx_stream(GrisContext* ctx) { return ctx->stream; }
+unsigned long long* grisrt::ctx_counters(GrisContext* ctx) { return ctx->dCounters; }
+int grisrt::ctx_count_work(GrisContext* ctx) { return ctx->countWork; }
+int grisrt::ctx_path_form(GrisContext* ctx) { return ctx->pathForm; }
+grisrt::KernelTimer* grisrt::ctx_timer(GrisContext* ctx) { return &ctx->prof; }
+int grisrt::ctx_fail(GrisContext* ctx, int code, const std::string& msg) { return fail(ctx, code, msg); }
 
 bool grisrt::scene_device(const GrisScene* s, grisrt::DeviceSceneView* view, int* device) {
     if (!s || !s->ctx) return false;
@@ -225,6 +234,12 @@ int grisReadProfile(GrisContext* ctx, double msTotal[4], uint64_t launches[4], i
 int grisSetLaunchMode(GrisContext* ctx, int mode) {
     if (!ctx || (mode != GRIS_LAUNCH_GRID && mode != GRIS_LAUNCH_PERSISTENT)) return GRIS_ERR_INVALID_ARGUMENT;
     ctx->launchMode = mode;
+    return GRIS_OK;
+}
+
+int grisSetPathForm(GrisContext* ctx, int form) {
+    if (!ctx || (form != GRIS_PATH_MEGAKERNEL && form != GRIS_PATH_WAVEFRONT)) return GRIS_ERR_INVALID_ARGUMENT;
+    ctx->pathForm = form;
     return GRIS_OK;
 }
 

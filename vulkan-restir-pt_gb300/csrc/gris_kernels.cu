@@ -114,6 +114,13 @@ struct PathTracer {
     PathSample pathSample;
     Stream stream;
     Ray3 ray;
+    /* carried from shade() to post() of the same bounce */
+    bool isThisVertexConnectible, nee;
+    float resvRandSample;
+    V3 lightRadiance, lightDir;
+    V2 lightBary;
+    float lightDist, lightPdf, lightJacobian;
+    uint32_t lightId;
 
     GD bool begin(const PassCtx& P, uint32_t px, uint32_t py) {
         const DevScene& sc = P.sc;
@@ -149,12 +156,17 @@ struct PathTracer {
         return true;
     }
 
-    /* one iteration of the bounce loop (gris_path_trace.glsl:91-258) */
-    GD bool step(const PassCtx& P, RayCount& rc, int& err) {
+    /* One iteration of the bounce loop (gris_path_trace.glsl:91-258) in two parts around the
+     * NEE shadow query. shade() takes the closest hit of `ray` (bounce > 0) and runs up to the
+     * light sample: kShadow asks the caller for the shadow query (surf.pos along lightDir, up to
+     * lightDist - MinRayDistance) and then post(shadowed); kNext / kEnd report a vertex without
+     * NEE whose post() already ran (continue / the reference breaks). */
+    static constexpr int kEnd = 0, kShadow = 1, kNext = 2;
+    GD int shade(const PassCtx& P, const Isec& hit) {
         const DevScene& sc = P.sc;
         if (bounce > 0) {
-            isec = traceClosestHit(sc, ray.ori, ray.dir, kMinRayDistance, kMaxRayDistance, rc, err);
-            if (isec.inst == kInvalidHit) return false;
+            isec = hit;
+            if (isec.inst == kInvalidHit) return kEnd;
             loadSurfaceInfo(sc, isec, surf);
             mat = load_material(sc, surf.matIndex);
         }
@@ -164,7 +176,7 @@ struct PathTracer {
         float distToPrev = distance3(lastPos, surf.pos);
         float geometryJacobian = fabsf(cosPrevWi) / square(distToPrev);
 
-        bool isThisVertexConnectible = surf.isLight || isBSDFConnectible(mat);
+        isThisVertexConnectible = surf.isLight || isBSDFConnectible(mat);
 
         lastSampleState = sampleState;
         sampleState = nextRcVertexSampleState(sampleState, isThisVertexConnectible);
@@ -173,7 +185,7 @@ struct PathTracer {
             sampleState = 2u;
             lastSampleState = 1u;
         }
-        float resvRandSample = sample1f(rng);
+        resvRandSample = sample1f(rng);
 
         if (surf.isLight) {
             if (bounce > 1 && cosPrevWi < 0.0f) {
@@ -199,7 +211,7 @@ struct PathTracer {
                     addStream(stream, pathSample, luminance(pathSample.F), resvRandSample);
                 }
                         }
-            return false;
+            return kEnd;
         }
 
         bool connectible = isThisVertexConnectible && isLastVertexConnectible && distToPrev > kDistanceThreshold;
@@ -217,11 +229,19 @@ struct PathTracer {
         V4 lightRandSample = sample4f(rng);
         resvRandSample = sample1f(rng);
 
-        if (bounce > 0 && !isBSDFDelta(mat)) {
-            V3 lightDir; V2 lightBary; float lightDist, lightPdf, lightJacobian; uint32_t lightId;
-            V3 lightRadiance = sampleLightByPower(sc, surf.pos, lightDir, lightDist, lightPdf, lightJacobian, lightBary,
-                                                  lightId, lightRandSample);
-            bool shadowed = traceShadow(sc, surf.pos, kMinRayDistance, lightDir, lightDist - kMinRayDistance, rc, err);
+        nee = bounce > 0 && !isBSDFDelta(mat);
+        if (nee) {
+            lightRadiance = sampleLightByPower(sc, surf.pos, lightDir, lightDist, lightPdf, lightJacobian, lightBary,
+                                               lightId, lightRandSample);
+            return kShadow;
+        }
+        return post(P, false) ? kNext : kEnd;
+    }
+
+    /* second part: the NEE contribution (when shade() sampled a light), Russian roulette, BSDF
+     * sampling; true = the path continues */
+    GD bool post(const PassCtx& P, bool shadowed) {
+        if (nee) {
             if (!shadowed && lightPdf > 1e-6f) {
                 float bsdfPdf = absDot(surf.norm, lightDir) * kPiInv;
                 float weight = MISWeight(lightPdf, bsdfPdf);
@@ -248,7 +268,7 @@ struct PathTracer {
                     setRcVertexType(pathSample.flags, kRcLightSampled);
                     addStream(stream, pathSample, luminance(pathSample.F), resvRandSample);
                 }
-                        }
+            }
         }
 
         if (bounce > 4) {
@@ -279,6 +299,17 @@ struct PathTracer {
         ray.ori = surf.pos + ray.dir * 1e-4f;
         isLastVertexConnectible = isThisVertexConnectible;
         return true;
+    }
+
+
+    /* the whole iteration with the ray queries inline (grid and persistent forms) */
+    GD bool step(const PassCtx& P, RayCount& rc, int& err) {
+        Isec hit = isec_zero();
+        if (bounce > 0) hit = traceClosestHit(P.sc, ray.ori, ray.dir, kMinRayDistance, kMaxRayDistance, rc, err);
+        int r = shade(P, hit);
+        if (r != kShadow) return r == kNext;
+        bool shadowed = traceShadow(P.sc, surf.pos, kMinRayDistance, lightDir, lightDist - kMinRayDistance, rc, err);
+        return post(P, shadowed);
     }
 
     /* after the loop (gris_path_trace.glsl:260-278) */
@@ -667,8 +698,12 @@ GD void run_persistent(const PassCtx& P, unsigned int* cursor, RayCount& rc, int
 }
 
 /* ------------------------------------------------------------------ kernels */
+/* Resident blocks per SM requested from the compiler for the grid form: the reuse passes run
+ * faster at 5 blocks (96 registers) despite a few spills; the path tracer at its natural 3. */
+template <int KERNEL> struct GridMinBlocks { static constexpr int value = KERNEL == 1 ? 1 : 5; };
+
 template <typename Task, int KERNEL>
-__global__ void __launch_bounds__(128) k_pass_grid(PassCtx P) {
+__global__ void __launch_bounds__(128, GridMinBlocks<KERNEL>::value) k_pass_grid(PassCtx P) {
     RayCount rc = ray_count();
     int err = 0;
     run_grid<Task>(P, rc, err);
@@ -695,83 +730,89 @@ struct GBufCtx {
 
 GD uint32_t packUnorm1(float c) { return (uint32_t)floorf(fminf(fmaxf(c, 0.0f), 1.0f) * 255.0f + 0.5f); }
 
+/* One pixel of the G-buffer; returns 1 (a primary ray was cast). */
+GD uint32_t gbuffer_pixel(const GBufCtx& G, uint32_t x, uint32_t y, int& err, GrisWork& work) {
+    const DevScene& sc = G.sc;
+    uint64_t p = (uint64_t)y * G.b.width + x;
+    V2 uv = v2(((float)x + 0.5f) / (float)G.b.width, ((float)y + 0.5f) / (float)G.b.height);
+    Ray3 ray = pinholeCameraSampleRay(G.cam, v2(uv.x, 1.0f - uv.y));
+    GrisRayHit h;
+    bool hit = gris_bvh_trace<false>(sc.nodes, sc.tris, ray.ori.x, ray.ori.y, ray.ori.z, ray.dir.x, ray.dir.y,
+                                      ray.dir.z, kMinRayDistance, kMaxRayDistance, true, &h, &err, &work);
+    float4* dnOut = reinterpret_cast<float4*>(G.b.depthNormal) + p;
+    uint2* amOut = reinterpret_cast<uint2*>(G.b.albedoMatId) + p;
+    __half2* mvOut = reinterpret_cast<__half2*>(G.b.motion) + p;
+    if (!hit) {
+        *dnOut = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+        *amOut = make_uint2(0u, 0u);
+        *mvOut = __halves2half2(__ushort_as_half(0), __ushort_as_half(0));
+        return 1u;
+    }
+    uint64_t k = (uint64_t)h.inst - 1u;
+    float T[16], TI[16];
+    uint32_t indexOffset = 0u;
+    if (k < sc.nInstances) {
+        load_mat4(sc.instances[k].transform, T);
+        load_mat4(sc.instances[k].transformInvT, TI);
+        indexOffset = ldu(&sc.instances[k].indexOffset);
+    } else {
+        for (int i = 0; i < 16; i++) { T[i] = 0.0f; TI[i] = 0.0f; }
+    }
+    V3 b = v3(1.0f - h.u - h.v, h.u, h.v);
+    V3 Pj[3], Nj[3];
+    for (int j = 0; j < 3; j++) {
+        V3 vp, vn;
+        load_vertex(sc, load_index(sc, (uint64_t)(indexOffset + h.tri * 3u + (uint32_t)j)), vp, vn);
+        Pj[j] = m4mul_point(T, vp, 1.0f);
+        V3 c0 = v3(TI[0], TI[1], TI[2]), c1 = v3(TI[4], TI[5], TI[6]), c2 = v3(TI[8], TI[9], TI[10]);
+        Nj[j] = normalize3((c0 * vn.x + c1 * vn.y) + c2 * vn.z);
+    }
+    V3 pos = (Pj[0] * b.x + Pj[1] * b.y) + Pj[2] * b.z;
+    V3 nor = normalize3((Nj[0] * b.x + Nj[1] * b.y) + Nj[2] * b.z);
+    uint64_t mi = (uint64_t)(indexOffset / 3u + h.tri);
+    uint32_t matIndex = (uint32_t)(mi < sc.nMatIndices ? (int32_t)ldu(reinterpret_cast<const uint32_t*>(sc.matIndices + mi)) : 0);
+    V3 albedo = load_material(sc, matIndex).baseColor;
+    const float* M = G.lastProjView;
+    float lx = ((M[0] * pos.x + M[4] * pos.y) + M[8] * pos.z) + M[12] * 1.0f;
+    float ly = ((M[1] * pos.x + M[5] * pos.y) + M[9] * pos.z) + M[13] * 1.0f;
+    float lw = ((M[3] * pos.x + M[7] * pos.y) + M[11] * pos.z) + M[15] * 1.0f;
+    lx = lx / lw; ly = ly / lw;
+    lx = lx * 0.5f + 0.5f; ly = ly * 0.5f + 0.5f;
+    float tx = ((float)x + 0.5f) / (float)G.b.width, ty = ((float)y + 0.5f) / (float)G.b.height;
+    float mx = lx - tx, my = ly - ty;
+    *dnOut = make_float4(length3(G.cam.pos - pos), nor.x, nor.y, nor.z);
+    uint32_t packed = packUnorm1(albedo.x) | (packUnorm1(albedo.y) << 8) | (packUnorm1(albedo.z) << 16) | (packUnorm1(1.0f) << 24);
+    *amOut = make_uint2(packed, (matIndex << 16) | (uint32_t)k);
+    *mvOut = __halves2half2(__float2half_rn(mx), __float2half_rn(my));
+    return 1u;
+}
+
+GD void flush_gbuffer_counts(unsigned long long* counters, uint32_t primary, int err, const GrisWork& work, int countWork) {
+    unsigned int c = __reduce_add_sync(0xffffffffu, primary);
+    unsigned int e = __reduce_or_sync(0xffffffffu, (unsigned)err);
+    unsigned long long nodes = 0, tris = 0;
+    if (countWork) {
+        nodes = __reduce_add_sync(0xffffffffu, work.nodes);
+        tris = __reduce_add_sync(0xffffffffu, work.tris);
+    }
+    if (((threadIdx.y * blockDim.x + threadIdx.x) & 31u) == 0u) {
+        if (c) atomicAdd(counters + GRIS_COUNTER_PRIMARY, (unsigned long long)c);
+        if (e) atomicOr(counters + GRIS_COUNTER_ERROR, (unsigned long long)e);
+        if (countWork) {
+            atomicAdd(counters + 8, nodes);
+            atomicAdd(counters + 9, tris);
+            atomicAdd(counters + 16, (unsigned long long)c);
+        }
+    }
+}
+
 __global__ void __launch_bounds__(128) k_gbuffer(GBufCtx G) {
     uint32_t x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y * blockDim.y + threadIdx.y;
     int err = 0;
     uint32_t primary = 0;
     GrisWork work; work.nodes = 0u; work.tris = 0u;
-    if (x < G.b.width && y < G.b.height) {
-        const DevScene& sc = G.sc;
-        uint64_t p = (uint64_t)y * G.b.width + x;
-        V2 uv = v2(((float)x + 0.5f) / (float)G.b.width, ((float)y + 0.5f) / (float)G.b.height);
-        Ray3 ray = pinholeCameraSampleRay(G.cam, v2(uv.x, 1.0f - uv.y));
-        GrisRayHit h;
-        primary = 1;
-        bool hit = gris_bvh_trace<false>(sc.nodes, sc.tris, ray.ori.x, ray.ori.y, ray.ori.z, ray.dir.x, ray.dir.y,
-                                          ray.dir.z, kMinRayDistance, kMaxRayDistance, true, &h, &err,
-                                          &work);
-        float4* dnOut = reinterpret_cast<float4*>(G.b.depthNormal) + p;
-        uint2* amOut = reinterpret_cast<uint2*>(G.b.albedoMatId) + p;
-        __half2* mvOut = reinterpret_cast<__half2*>(G.b.motion) + p;
-        if (!hit) {
-            *dnOut = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-            *amOut = make_uint2(0u, 0u);
-            *mvOut = __halves2half2(__ushort_as_half(0), __ushort_as_half(0));
-        } else {
-            uint64_t k = (uint64_t)h.inst - 1u;
-            float T[16], TI[16];
-            uint32_t indexOffset = 0u;
-            if (k < sc.nInstances) {
-                load_mat4(sc.instances[k].transform, T);
-                load_mat4(sc.instances[k].transformInvT, TI);
-                indexOffset = ldu(&sc.instances[k].indexOffset);
-            } else {
-                for (int i = 0; i < 16; i++) { T[i] = 0.0f; TI[i] = 0.0f; }
-            }
-            V3 b = v3(1.0f - h.u - h.v, h.u, h.v);
-            V3 Pj[3], Nj[3];
-            for (int j = 0; j < 3; j++) {
-                V3 vp, vn;
-                load_vertex(sc, load_index(sc, (uint64_t)(indexOffset + h.tri * 3u + (uint32_t)j)), vp, vn);
-                Pj[j] = m4mul_point(T, vp, 1.0f);
-                V3 c0 = v3(TI[0], TI[1], TI[2]), c1 = v3(TI[4], TI[5], TI[6]), c2 = v3(TI[8], TI[9], TI[10]);
-                Nj[j] = normalize3((c0 * vn.x + c1 * vn.y) + c2 * vn.z);
-            }
-            V3 pos = (Pj[0] * b.x + Pj[1] * b.y) + Pj[2] * b.z;
-            V3 nor = normalize3((Nj[0] * b.x + Nj[1] * b.y) + Nj[2] * b.z);
-            uint64_t mi = (uint64_t)(indexOffset / 3u + h.tri);
-            uint32_t matIndex = (uint32_t)(mi < sc.nMatIndices ? (int32_t)ldu(reinterpret_cast<const uint32_t*>(sc.matIndices + mi)) : 0);
-            V3 albedo = load_material(sc, matIndex).baseColor;
-            const float* M = G.lastProjView;
-            float lx = ((M[0] * pos.x + M[4] * pos.y) + M[8] * pos.z) + M[12] * 1.0f;
-            float ly = ((M[1] * pos.x + M[5] * pos.y) + M[9] * pos.z) + M[13] * 1.0f;
-            float lw = ((M[3] * pos.x + M[7] * pos.y) + M[11] * pos.z) + M[15] * 1.0f;
-            lx = lx / lw; ly = ly / lw;
-            lx = lx * 0.5f + 0.5f; ly = ly * 0.5f + 0.5f;
-            float tx = ((float)x + 0.5f) / (float)G.b.width, ty = ((float)y + 0.5f) / (float)G.b.height;
-            float mx = lx - tx, my = ly - ty;
-            *dnOut = make_float4(length3(G.cam.pos - pos), nor.x, nor.y, nor.z);
-            uint32_t packed = packUnorm1(albedo.x) | (packUnorm1(albedo.y) << 8) | (packUnorm1(albedo.z) << 16) | (packUnorm1(1.0f) << 24);
-            *amOut = make_uint2(packed, (matIndex << 16) | (uint32_t)k);
-            *mvOut = __halves2half2(__float2half_rn(mx), __float2half_rn(my));
-        }
-    }
-    unsigned int c = __reduce_add_sync(0xffffffffu, primary);
-    unsigned int e = __reduce_or_sync(0xffffffffu, (unsigned)err);
-    unsigned long long nodes = 0, tris = 0;
-    if (G.countWork) {
-        nodes = __reduce_add_sync(0xffffffffu, work.nodes);
-        tris = __reduce_add_sync(0xffffffffu, work.tris);
-    }
-    if (((threadIdx.y * blockDim.x + threadIdx.x) & 31u) == 0u) {
-        if (c) atomicAdd(G.counters + GRIS_COUNTER_PRIMARY, (unsigned long long)c);
-        if (e) atomicOr(G.counters + GRIS_COUNTER_ERROR, (unsigned long long)e);
-        if (G.countWork) {
-            atomicAdd(G.counters + 8, nodes);
-            atomicAdd(G.counters + 9, tris);
-            atomicAdd(G.counters + 16, (unsigned long long)c);
-        }
-    }
+    if (x < G.b.width && y < G.b.height) primary = gbuffer_pixel(G, x, y, err, work);
+    flush_gbuffer_counts(G.counters, primary, err, work, G.countWork);
 }
 
 /* Builder check: one ray per thread. */
@@ -887,6 +928,397 @@ cudaError_t launch_debug_trace(const uint32_t* nodes, const float* tris, const f
                                cudaStream_t stream) {
     if (n == 0) return cudaSuccess;
     k_debug_trace<<<(unsigned)((n + 127) / 128), 128, 0, stream>>>(nodes, tris, rays, n, anyHit, hitTUV, hitInst, hitTri, counters);
+    return cudaGetLastError();
+}
+
+}  // namespace grisrt
+
+/* ==================================================================================================
+ * Batches: many views (each with its own scene, size, cameras and settings) in one launch per
+ * pass, and the wavefront form of the path tracer with per-bounce compacted queues.
+ * ================================================================================================== */
+namespace grisrt {
+
+/* One view of a batch, as the kernels read it from the device view table. */
+struct ViewEntry {
+    PassCtx P;
+    GBufCtx G;
+    uint32_t tileBase;   /* first 16 x 8 tile of the view in the batch's tile space */
+    uint32_t tilesX;
+    uint32_t pixelBase;  /* first path id of the view */
+    uint32_t pad;
+};
+
+size_t view_entry_bytes() { return sizeof(ViewEntry); }
+
+GD int find_view_by_tile(const ViewEntry* V, int n, uint32_t tile) {
+    int lo = 0, hi = n - 1;
+    while (lo < hi) {
+        int mid = (lo + hi + 1) >> 1;
+        if (V[mid].tileBase <= tile) lo = mid; else hi = mid - 1;
+    }
+    return lo;
+}
+GD int find_view_by_pixel(const ViewEntry* V, int n, uint32_t id) {
+    int lo = 0, hi = n - 1;
+    while (lo < hi) {
+        int mid = (lo + hi + 1) >> 1;
+        if (V[mid].pixelBase <= id) lo = mid; else hi = mid - 1;
+    }
+    return lo;
+}
+
+/* G-buffer, temporal and spatial passes over every view: one 16 x 8 block per tile. */
+__global__ void __launch_bounds__(128) k_batch_gbuffer(const ViewEntry* __restrict__ V, int n) {
+    int v = find_view_by_tile(V, n, blockIdx.x);
+    const GBufCtx& G = V[v].G;
+    uint32_t t = blockIdx.x - V[v].tileBase;
+    uint32_t x = (t % V[v].tilesX) * 16u + threadIdx.x, y = (t / V[v].tilesX) * 8u + threadIdx.y;
+    int err = 0;
+    uint32_t primary = 0;
+    GrisWork work; work.nodes = 0u; work.tris = 0u;
+    if (x < G.b.width && y < G.b.height) primary = gbuffer_pixel(G, x, y, err, work);
+    flush_gbuffer_counts(G.counters, primary, err, work, G.countWork);
+}
+
+template <typename Task, int KERNEL>
+__global__ void __launch_bounds__(128, GridMinBlocks<KERNEL>::value) k_batch_pass(const ViewEntry* __restrict__ V, int n) {
+    int v = find_view_by_tile(V, n, blockIdx.x);
+    const PassCtx& P = V[v].P;
+    uint32_t t = blockIdx.x - V[v].tileBase;
+    uint32_t x = (t % V[v].tilesX) * 16u + threadIdx.x, y = (t / V[v].tilesX) * 8u + threadIdx.y;
+    RayCount rc = ray_count();
+    int err = 0;
+    if (x < P.b.width && y < P.b.height) {
+        Task task;
+        if (task.begin(P, x, y, rc, err))
+            while (task.step(P, rc, err)) {}
+    }
+    flush_counts(P.counters, rc, err, KERNEL, P.countWork);
+}
+
+/* ------------------------------------------------------------------ wavefront path tracer */
+/* Path state between kernels, per path id: the loop-carried members of PathTracer (17 x 16 B)
+ * and the part of a bounce carried from shade() to post() across the shadow query (6 x 16 B). */
+struct WaveRec { uint4 w[17]; };
+struct NeeRec { uint4 w[6]; };
+
+GD uint4 u4f(float a, float b, float c, float d) {
+    return make_uint4(__float_as_uint(a), __float_as_uint(b), __float_as_uint(c), __float_as_uint(d));
+}
+GD void ps_to_words(const PathSample& p, uint4* w) {
+    w[0] = make_uint4(__float_as_uint(p.rcIsec.bx), __float_as_uint(p.rcIsec.by), p.rcIsec.inst, p.rcIsec.tri);
+    w[1] = make_uint4(__float_as_uint(p.rcLi.x), __float_as_uint(p.rcLi.y), __float_as_uint(p.rcLi.z), p.rcRng);
+    w[2] = make_uint4(__float_as_uint(p.rcWi.x), __float_as_uint(p.rcWi.y), __float_as_uint(p.rcWi.z), p.flags);
+    w[3] = u4f(p.pad0, p.pad1, p.rcPrevSamplePdf, p.rcJacobian);
+    w[4] = make_uint4(__float_as_uint(p.F.x), __float_as_uint(p.F.y), __float_as_uint(p.F.z), p.primaryRng);
+}
+GD void ps_from_words(PathSample& p, const uint4* w) {
+    p.rcIsec.bx = __uint_as_float(w[0].x); p.rcIsec.by = __uint_as_float(w[0].y); p.rcIsec.inst = w[0].z; p.rcIsec.tri = w[0].w;
+    p.rcLi = v3(__uint_as_float(w[1].x), __uint_as_float(w[1].y), __uint_as_float(w[1].z)); p.rcRng = w[1].w;
+    p.rcWi = v3(__uint_as_float(w[2].x), __uint_as_float(w[2].y), __uint_as_float(w[2].z)); p.flags = w[2].w;
+    p.pad0 = __uint_as_float(w[3].x); p.pad1 = __uint_as_float(w[3].y);
+    p.rcPrevSamplePdf = __uint_as_float(w[3].z); p.rcJacobian = __uint_as_float(w[3].w);
+    p.F = v3(__uint_as_float(w[4].x), __uint_as_float(w[4].y), __uint_as_float(w[4].z)); p.primaryRng = w[4].w;
+}
+GD void save_wave(WaveRec* __restrict__ dst, const PathTracer& t) {
+    uint4 w[17];
+    w[0] = make_uint4(t.rng, t.sampleState | (t.lastSampleState << 8) | ((t.isLastVertexConnectible ? 1u : 0u) << 16),
+                      t.surf.matIndex, t.s.type);
+    w[1] = u4f(t.throughput.x, t.throughput.y, t.throughput.z, t.s.pdf);
+    w[2] = u4f(t.rcThroughput.x, t.rcThroughput.y, t.rcThroughput.z, t.stream.weight);
+    w[3] = u4f(t.lastPos.x, t.lastPos.y, t.lastPos.z, t.stream.sumWeight);
+    w[4] = make_uint4(__float_as_uint(t.ray.ori.x), __float_as_uint(t.ray.ori.y), __float_as_uint(t.ray.ori.z), t.stream.sampleCount);
+    w[5] = u4f(t.ray.dir.x, t.ray.dir.y, t.ray.dir.z, 0.0f);
+    ps_to_words(t.pathSample, w + 6);
+    ps_to_words(t.stream.ps, w + 11);
+    w[16] = make_uint4(0u, 0u, 0u, 0u);
+    for (int i = 0; i < 17; i++) dst->w[i] = w[i];
+}
+GD void load_wave(const WaveRec* __restrict__ src, PathTracer& t) {
+    uint4 w[17];
+    for (int i = 0; i < 16; i++) w[i] = src->w[i];
+    t.rng = w[0].x;
+    t.sampleState = w[0].y & 0xffu; t.lastSampleState = (w[0].y >> 8) & 0xffu; t.isLastVertexConnectible = (w[0].y >> 16) & 1u;
+    t.surf.matIndex = w[0].z; t.s.type = w[0].w;
+    t.throughput = v3(__uint_as_float(w[1].x), __uint_as_float(w[1].y), __uint_as_float(w[1].z)); t.s.pdf = __uint_as_float(w[1].w);
+    t.rcThroughput = v3(__uint_as_float(w[2].x), __uint_as_float(w[2].y), __uint_as_float(w[2].z)); t.stream.weight = __uint_as_float(w[2].w);
+    t.lastPos = v3(__uint_as_float(w[3].x), __uint_as_float(w[3].y), __uint_as_float(w[3].z)); t.stream.sumWeight = __uint_as_float(w[3].w);
+    t.ray.ori = v3(__uint_as_float(w[4].x), __uint_as_float(w[4].y), __uint_as_float(w[4].z)); t.stream.sampleCount = w[4].w;
+    t.ray.dir = v3(__uint_as_float(w[5].x), __uint_as_float(w[5].y), __uint_as_float(w[5].z));
+    ps_from_words(t.pathSample, w + 6);
+    ps_from_words(t.stream.ps, w + 11);
+    t.wo = -t.ray.dir;   /* wo = -ray.dir holds at every bounce boundary */
+    t.s.wi = v3s(0.0f); t.s.bsdf = v3s(0.0f);
+    t.surf.isLight = false;
+}
+GD void save_nee(NeeRec* __restrict__ dst, const PathTracer& t) {
+    dst->w[0] = make_uint4(__float_as_uint(t.surf.pos.x), __float_as_uint(t.surf.pos.y), __float_as_uint(t.surf.pos.z),
+                           __float_as_uint(t.resvRandSample));
+    dst->w[1] = make_uint4(__float_as_uint(t.surf.norm.x), __float_as_uint(t.surf.norm.y), __float_as_uint(t.surf.norm.z),
+                           t.isThisVertexConnectible ? 1u : 0u);
+    dst->w[2] = make_uint4(__float_as_uint(t.surf.albedo.x), __float_as_uint(t.surf.albedo.y), __float_as_uint(t.surf.albedo.z), t.lightId);
+    dst->w[3] = u4f(t.lightRadiance.x, t.lightRadiance.y, t.lightRadiance.z, t.lightDist);
+    dst->w[4] = u4f(t.lightDir.x, t.lightDir.y, t.lightDir.z, t.lightPdf);
+    dst->w[5] = u4f(t.lightBary.x, t.lightBary.y, t.lightJacobian, 0.0f);
+}
+GD void load_nee(const NeeRec* __restrict__ src, PathTracer& t) {
+    uint4 w[6];
+    for (int i = 0; i < 6; i++) w[i] = src->w[i];
+    t.surf.pos = v3(__uint_as_float(w[0].x), __uint_as_float(w[0].y), __uint_as_float(w[0].z)); t.resvRandSample = __uint_as_float(w[0].w);
+    t.surf.norm = v3(__uint_as_float(w[1].x), __uint_as_float(w[1].y), __uint_as_float(w[1].z)); t.isThisVertexConnectible = w[1].w != 0u;
+    t.surf.albedo = v3(__uint_as_float(w[2].x), __uint_as_float(w[2].y), __uint_as_float(w[2].z)); t.lightId = w[2].w;
+    t.lightRadiance = v3(__uint_as_float(w[3].x), __uint_as_float(w[3].y), __uint_as_float(w[3].z)); t.lightDist = __uint_as_float(w[3].w);
+    t.lightDir = v3(__uint_as_float(w[4].x), __uint_as_float(w[4].y), __uint_as_float(w[4].z)); t.lightPdf = __uint_as_float(w[4].w);
+    t.lightBary = v2(__uint_as_float(w[5].x), __uint_as_float(w[5].y)); t.lightJacobian = __uint_as_float(w[5].z);
+    t.nee = true;
+}
+
+struct WaveCtx {
+    const ViewEntry* V;
+    int nViews;
+    uint32_t totalPixels;
+    WaveRec* state;
+    NeeRec* nee;
+    Isec* hit;
+    unsigned char* blocked;
+    uint32_t* queue[2];
+    uint32_t* shadowQueue;
+    uint32_t* counts;   /* [level] path count of level, [256 + level] shadow-query count of level */
+    unsigned long long* counters;
+    int countWork;
+};
+
+/* Appends `id` (for lanes with `push`) to a queue with one atomic per warp. */
+GD void warp_push(uint32_t* queue, uint32_t* count, bool push, uint32_t id) {
+    unsigned m = __ballot_sync(0xffffffffu, push);
+    if (!m) return;
+    uint32_t lane = threadIdx.x & 31u;
+    uint32_t leader = __ffs(m) - 1;
+    uint32_t base = 0;
+    if (lane == leader) base = atomicAdd(count, (uint32_t)__popc(m));
+    base = __shfl_sync(0xffffffffu, base, leader);
+    if (push) queue[base + __popc(m & ((1u << lane) - 1u))] = id;
+}
+
+GD void path_coords(const WaveCtx& C, uint32_t id, int& v, uint32_t& x, uint32_t& y) {
+    v = find_view_by_pixel(C.V, C.nViews, id);
+    uint32_t px = id - C.V[v].pixelBase;
+    x = px % C.V[v].P.b.width;
+    y = px / C.V[v].P.b.width;
+}
+
+/* After a bounce's post(): the next level or the end of the path. */
+GD void wave_continue(const WaveCtx& C, const PassCtx& P, PathTracer& t, uint32_t id, bool cont, int level, bool& push) {
+    push = false;
+    if (cont) {
+        t.bounce++;
+        if (t.bounce < (int)P.set.maxDepth) {
+            save_wave(C.state + id, t);
+            push = true;
+            return;
+        }
+    }
+    t.end(P);
+}
+
+/* level 0: begin() + the primary vertex for every pixel of every view */
+__global__ void __launch_bounds__(128) k_wave_begin(WaveCtx C) {
+    uint32_t id = blockIdx.x * blockDim.x + threadIdx.x;
+    bool push = false;
+    RayCount rc = ray_count();
+    if (id < C.totalPixels) {
+        int v; uint32_t x, y;
+        path_coords(C, id, v, x, y);
+        const PassCtx& P = C.V[v].P;
+        PathTracer t;
+        if (t.begin(P, x, y)) {
+            int r = t.shade(P, isec_zero());   /* no NEE at bounce 0 */
+            wave_continue(C, P, t, id, r == PathTracer::kNext, 0, push);
+        }
+    }
+    warp_push(C.queue[1], C.counts + 1, push, id);
+}
+
+/* closest hits of the level's paths */
+__global__ void __launch_bounds__(128) k_wave_extend(WaveCtx C, int level) {
+    const uint32_t n = C.counts[level];
+    const uint32_t* q = C.queue[level & 1];
+    RayCount rc = ray_count();
+    int err = 0;
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i - threadIdx.x < n; i += gridDim.x * blockDim.x) {
+        if (i < n) {
+            uint32_t id = q[i];
+            const uint4* w = C.state[id].w;
+            uint4 a = w[4], b = w[5];
+            V3 o = v3(__uint_as_float(a.x), __uint_as_float(a.y), __uint_as_float(a.z));
+            V3 d = v3(__uint_as_float(b.x), __uint_as_float(b.y), __uint_as_float(b.z));
+            int v = find_view_by_pixel(C.V, C.nViews, id);
+            C.hit[id] = traceClosestHit(C.V[v].P.sc, o, d, kMinRayDistance, kMaxRayDistance, rc, err);
+        }
+    }
+    flush_counts(C.counters, rc, err, 1, C.countWork);
+}
+
+/* shade() of the level's paths: the end, the next level, or a shadow query */
+__global__ void __launch_bounds__(128) k_wave_shade(WaveCtx C, int level) {
+    const uint32_t n = C.counts[level];
+    const uint32_t* q = C.queue[level & 1];
+    for (uint32_t i0 = blockIdx.x * blockDim.x; i0 < n; i0 += gridDim.x * blockDim.x) {
+        uint32_t i = i0 + threadIdx.x;
+        bool pushNext = false, pushShadow = false;
+        uint32_t id = 0;
+        if (i < n) {
+            id = q[i];
+            int v; uint32_t x, y;
+            path_coords(C, id, v, x, y);
+            const PassCtx& P = C.V[v].P;
+            PathTracer t;
+            load_wave(C.state + id, t);
+            t.ix = x; t.iy = y; t.bounce = level;
+            t.mat = load_material(P.sc, t.surf.matIndex);
+            int r = t.shade(P, C.hit[id]);
+            if (r == PathTracer::kShadow) {
+                save_wave(C.state + id, t);
+                save_nee(C.nee + id, t);
+                pushShadow = true;
+            } else {
+                wave_continue(C, P, t, id, r == PathTracer::kNext, level, pushNext);
+            }
+        }
+        warp_push(C.queue[(level + 1) & 1], C.counts + level + 1, pushNext, id);
+        warp_push(C.shadowQueue, C.counts + 256 + level, pushShadow, id);
+    }
+}
+
+/* the shadow queries of the level */
+__global__ void __launch_bounds__(128) k_wave_shadow(WaveCtx C, int level) {
+    const uint32_t n = C.counts[256 + level];
+    RayCount rc = ray_count();
+    int err = 0;
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i - threadIdx.x < n; i += gridDim.x * blockDim.x) {
+        if (i < n) {
+            uint32_t id = C.shadowQueue[i];
+            const uint4* w = C.nee[id].w;
+            uint4 a = w[0], d4 = w[4], r3 = w[3];
+            V3 o = v3(__uint_as_float(a.x), __uint_as_float(a.y), __uint_as_float(a.z));
+            V3 d = v3(__uint_as_float(d4.x), __uint_as_float(d4.y), __uint_as_float(d4.z));
+            float dist = __uint_as_float(r3.w);
+            int v = find_view_by_pixel(C.V, C.nViews, id);
+            C.blocked[id] = traceShadow(C.V[v].P.sc, o, kMinRayDistance, d, dist - kMinRayDistance, rc, err) ? 1 : 0;
+        }
+    }
+    flush_counts(C.counters, rc, err, 1, C.countWork);
+}
+
+/* post() of the paths that made a shadow query */
+__global__ void __launch_bounds__(128) k_wave_post(WaveCtx C, int level) {
+    const uint32_t n = C.counts[256 + level];
+    for (uint32_t i0 = blockIdx.x * blockDim.x; i0 < n; i0 += gridDim.x * blockDim.x) {
+        uint32_t i = i0 + threadIdx.x;
+        bool push = false;
+        uint32_t id = 0;
+        if (i < n) {
+            id = C.shadowQueue[i];
+            int v; uint32_t x, y;
+            path_coords(C, id, v, x, y);
+            const PassCtx& P = C.V[v].P;
+            PathTracer t;
+            load_wave(C.state + id, t);
+            load_nee(C.nee + id, t);
+            t.ix = x; t.iy = y; t.bounce = level;
+            t.mat = load_material(P.sc, t.surf.matIndex);
+            bool cont = t.post(P, C.blocked[id] != 0);
+            wave_continue(C, P, t, id, cont, level, push);
+        }
+        warp_push(C.queue[(level + 1) & 1], C.counts + level + 1, push, id);
+    }
+}
+
+size_t wave_bytes_per_path() { return sizeof(WaveRec) + sizeof(NeeRec) + sizeof(Isec) + 1 + 3 * sizeof(uint32_t); }
+
+cudaError_t launch_batch(const BatchView* views, int n, void* dViews, void* hViews, const WaveBuffers& wb,
+                         unsigned long long* counters, int countWork, KernelTimer* timer, cudaStream_t stream,
+                         int pathForm, int passes) {
+    if (n <= 0 || n > 4096) return cudaErrorInvalidValue;
+    ViewEntry* H = reinterpret_cast<ViewEntry*>(hViews);
+    uint32_t tiles = 0, pixels = 0;
+    int maxDepth = 0;
+    for (int i = 0; i < n; i++) {
+        const BatchView& bv = views[i];
+        ViewEntry& e = H[i];
+        memset(&e, 0, sizeof(e));
+        e.P.countWork = countWork;
+        e.P.sc = to_dev(bv.scene);
+        e.P.cam = make_cam(bv.cam);
+        e.P.prev = make_cam(bv.prev);
+        e.P.set = bv.set;
+        e.P.b = bv.b;
+        e.P.counters = counters;
+        e.G.sc = e.P.sc;
+        e.G.cam = e.P.cam;
+        for (int k = 0; k < 16; k++) e.G.lastProjView[k] = bv.cam.lastProjView[k];
+        e.G.b = bv.gb;
+        e.G.counters = counters;
+        e.G.countWork = countWork;
+        e.tilesX = (bv.b.width + 15) / 16;
+        e.tileBase = tiles;
+        e.pixelBase = pixels;
+        tiles += e.tilesX * ((bv.b.height + 7) / 8);
+        pixels += bv.b.width * bv.b.height;
+        if ((int)bv.set.maxDepth > maxDepth) maxDepth = (int)bv.set.maxDepth;
+    }
+    if ((uint64_t)pixels > wb.capacity) return cudaErrorInvalidValue;
+    cudaError_t e = cudaMemcpyAsync(dViews, hViews, sizeof(ViewEntry) * (size_t)n, cudaMemcpyHostToDevice, stream);
+    if (e != cudaSuccess) return e;
+    const ViewEntry* V = reinterpret_cast<const ViewEntry*>(dViews);
+    dim3 blk(16, 8);
+    if (passes & 8) {
+        if (timer) timer->mark(0, true, stream);
+        k_batch_gbuffer<<<tiles, blk, 0, stream>>>(V, n);
+        if (timer) timer->mark(0, false, stream);
+    }
+    if (passes & 1) {
+        if (timer) timer->mark(1, true, stream);
+        if (pathForm == GRIS_PATH_WAVEFRONT) {
+            WaveCtx C;
+            C.V = V; C.nViews = n; C.totalPixels = pixels;
+            C.state = reinterpret_cast<WaveRec*>(wb.state);
+            C.nee = reinterpret_cast<NeeRec*>(wb.nee);
+            C.hit = reinterpret_cast<Isec*>(wb.hit);
+            C.blocked = wb.blocked;
+            C.queue[0] = wb.queue[0]; C.queue[1] = wb.queue[1];
+            C.shadowQueue = wb.shadowQueue;
+            C.counts = wb.counts;
+            C.counters = counters;
+            C.countWork = countWork;
+            e = cudaMemsetAsync(wb.counts, 0, 512 * sizeof(uint32_t), stream);
+            if (e != cudaSuccess) return e;
+            static int sm = 0;
+            if (sm == 0) { int dev = 0; cudaGetDevice(&dev); cudaDeviceGetAttribute(&sm, cudaDevAttrMultiProcessorCount, dev); }
+            const int gridShade = sm * 8, gridTrace = sm * 16;
+            k_wave_begin<<<(pixels + 127) / 128, 128, 0, stream>>>(C);
+            for (int level = 1; level < maxDepth; level++) {
+                k_wave_extend<<<gridTrace, 128, 0, stream>>>(C, level);
+                k_wave_shade<<<gridShade, 128, 0, stream>>>(C, level);
+                k_wave_shadow<<<gridTrace, 128, 0, stream>>>(C, level);
+                k_wave_post<<<gridShade, 128, 0, stream>>>(C, level);
+            }
+        } else {
+            k_batch_pass<PathTask, 1><<<tiles, blk, 0, stream>>>(V, n);
+        }
+        if (timer) timer->mark(1, false, stream);
+    }
+    if (passes & 2) {
+        if (timer) timer->mark(2, true, stream);
+        k_batch_pass<TemporalTask, 2><<<tiles, blk, 0, stream>>>(V, n);
+        if (timer) timer->mark(2, false, stream);
+    }
+    if (passes & 4) {
+        if (timer) timer->mark(3, true, stream);
+        k_batch_pass<SpatialTask, 3><<<tiles, blk, 0, stream>>>(V, n);
+        if (timer) timer->mark(3, false, stream);
+    }
     return cudaGetLastError();
 }
 

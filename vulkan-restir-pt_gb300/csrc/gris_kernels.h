@@ -36,6 +36,36 @@ cudaError_t launch_gbuffer(const DeviceSceneView& scene, const GrisGBufferBindin
 cudaError_t launch_gris(const DeviceSceneView& scene, const GrisPassBindings& b, const GrisCamera& cam,
                         const GrisCamera& prevCam, const GrisSettings& set, int passes, unsigned long long* counters,
                         int countWork, KernelTimer* timer, cudaStream_t stream, int launchMode = GRIS_LAUNCH_PERSISTENT);
+/* One view of a batch for one frame: its scene, this frame's buffers (ping-pong resolved),
+ * cameras and settings. */
+struct BatchView {
+    DeviceSceneView scene;
+    GrisPassBindings b;
+    GrisGBufferBindings gb;
+    GrisCamera cam, prev;
+    GrisSettings set;
+};
+
+/* Device buffers of the wavefront path tracer, for up to `capacity` paths (pixels of a batch). */
+struct WaveBuffers {
+    void* state;
+    void* nee;
+    void* hit;
+    unsigned char* blocked;
+    uint32_t* queue[2];
+    uint32_t* shadowQueue;
+    uint32_t* counts;   /* 512 words */
+    uint64_t capacity;
+};
+size_t wave_bytes_per_path();
+size_t view_entry_bytes();
+
+/* passes: bit 3 G-buffer, bit 0 path trace, bit 1 temporal, bit 2 spatial. pathForm:
+ * GRIS_PATH_MEGAKERNEL or GRIS_PATH_WAVEFRONT. hViews: pinned staging for the view table. */
+cudaError_t launch_batch(const BatchView* views, int n, void* dViews, void* hViews, const WaveBuffers& wb,
+                         unsigned long long* counters, int countWork, KernelTimer* timer, cudaStream_t stream,
+                         int pathForm, int passes);
+
 cudaError_t launch_debug_trace(const uint32_t* nodes, const float* tris, const float* rays, uint64_t n, int anyHit,
                                float* hitTUV, uint32_t* hitInst, uint32_t* hitTri, unsigned long long* counters,
                                cudaStream_t stream);

@@ -4,6 +4,7 @@
 #ifndef GRISRT_INTERNAL_H
 #define GRISRT_INTERNAL_H
 
+#include <cuda_runtime.h>
 #include <stdint.h>
 
 #include <string>
@@ -31,6 +32,14 @@ void world_triangles(const GrisSceneDesc& d, std::vector<float>& v012, std::vect
 bool build_bvh(const GrisSceneDesc& d, BvhHost& out, std::string& err);
 
 struct DeviceSceneView;
+struct KernelTimer;
+int ctx_device(GrisContext* ctx);
+cudaStream_t ctx_stream(GrisContext* ctx);
+unsigned long long* ctx_counters(GrisContext* ctx);
+int ctx_count_work(GrisContext* ctx);
+int ctx_path_form(GrisContext* ctx);
+KernelTimer* ctx_timer(GrisContext* ctx);
+int ctx_fail(GrisContext* ctx, int code, const std::string& msg);
 /* Device view and device ordinal of an uploaded scene; false for a host-only scene. */
 bool scene_device(const GrisScene* s, DeviceSceneView* view, int* device);
 

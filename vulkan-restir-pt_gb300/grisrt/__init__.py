@@ -37,6 +37,7 @@ assert LIGHT.itemsize == 64 and TABLE.itemsize == 8 and RESERVOIR.itemsize == 96
 
 INVALID_HIT = 0xFFFFFFFF
 LAUNCH_GRID, LAUNCH_PERSISTENT = 0, 1
+PATH_MEGAKERNEL, PATH_WAVEFRONT = 0, 1
 NOALLOC_MAX_PIXELS = 65536
 CLEAR_FLAG = 0x80000000
 
@@ -111,7 +112,7 @@ EXPORTS = [
     "grisHostSceneDesc", "grisHostSceneCamera", "grisHostSceneDestroy", "grisSceneCreate", "grisSceneDestroy",
     "grisSceneGetStats", "grisDebugHostSceneCreate", "grisDebugTraceHost", "grisDebugTraceDevice", "grisPassGBuffer", "grisPassRender", "grisPassRenderNoAlloc",
     "grisFrameCreate", "grisFrameDestroy", "grisFrameRender", "grisFrameGetBuffer", "grisFrameDownload",
-    "grisFrameUpload",
+    "grisFrameUpload", "grisSetPathForm", "grisBatchCreate", "grisBatchDestroy", "grisBatchRender", "grisBatchGetBuffer",
 ]
 
 _lib = None
@@ -165,6 +166,11 @@ def load(path=None):
         "grisFrameGetBuffer": (i32, [vp, i32, i32, ctypes.POINTER(vp), ctypes.POINTER(ctypes.c_size_t)]),
         "grisFrameDownload": (i32, [vp, vp, i32, i32, vp, ctypes.c_size_t]),
         "grisFrameUpload": (i32, [vp, vp, i32, i32, vp, ctypes.c_size_t]),
+        "grisSetPathForm": (i32, [vp, i32]),
+        "grisBatchCreate": (i32, [vp, u32, ctypes.POINTER(vp), ctypes.POINTER(u32), ctypes.POINTER(u32), ctypes.POINTER(vp)]),
+        "grisBatchDestroy": (i32, [vp]),
+        "grisBatchRender": (i32, [vp, vp, ctypes.POINTER(Camera), ctypes.POINTER(Camera), ctypes.POINTER(Settings)]),
+        "grisBatchGetBuffer": (i32, [vp, u32, i32, i32, ctypes.POINTER(vp), ctypes.POINTER(ctypes.c_size_t)]),
     }
     for name, (res, args) in sig.items():
         f = getattr(lib, name)
@@ -322,8 +328,12 @@ class Context:
         return list(ms), list(n)
 
     def set_launch_mode(self, mode):
-        """0: grid (one thread per pixel), 1: persistent with per-lane refill (default)."""
+        """0: grid (one thread per pixel, default), 1: persistent with per-lane refill."""
         self.check(load().grisSetLaunchMode(self.h, int(mode)), "grisSetLaunchMode")
+
+    def set_path_form(self, form):
+        """0: megakernel path tracer, 1: wavefront stages with per-bounce queues (batches)."""
+        self.check(load().grisSetPathForm(self.h, int(form)), "grisSetPathForm")
 
     def set_work_counting(self, enable):
         self.check(load().grisSetWorkCounting(self.h, int(enable)), "grisSetWorkCounting")
@@ -429,6 +439,64 @@ class Frame:
 
     def __del__(self):
         # at interpreter exit the CUDA runtime may already be torn down: leave it to the driver
+        if sys.is_finalizing():
+            return
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class Batch:
+    """Many views (own scene, size, cameras, settings) rendered with one launch per pass (grisBatch*)."""
+
+    def __init__(self, ctx, scenes, sizes):
+        self.ctx = ctx
+        self.scenes = list(scenes)
+        self.sizes = [(int(w), int(h)) for w, h in sizes]
+        n = len(self.scenes)
+        sh = (ctypes.c_void_p * n)(*[sc.h.value for sc in self.scenes])
+        ws = (ctypes.c_uint32 * n)(*[w for w, _ in self.sizes])
+        hs = (ctypes.c_uint32 * n)(*[h for _, h in self.sizes])
+        h = ctypes.c_void_p()
+        ctx.check(load().grisBatchCreate(ctx.h, n, sh, ws, hs, ctypes.byref(h)), "grisBatchCreate")
+        self.handle = h
+
+    def render(self, cams, prev_cams, settings):
+        n = len(self.scenes)
+        c = (Camera * n)(*cams)
+        p = (Camera * n)(*prev_cams)
+        s = (Settings * n)(*settings)
+        self.ctx.check(load().grisBatchRender(self.ctx.h, self.handle, c, p, s), "grisBatchRender")
+
+    def device_ptr(self, view, which, slot=0):
+        p = ctypes.c_void_p()
+        n = ctypes.c_size_t()
+        self.ctx.check(load().grisBatchGetBuffer(self.handle, view, which, slot, ctypes.byref(p), ctypes.byref(n)),
+                       "grisBatchGetBuffer")
+        return p.value, n.value
+
+    def download(self, view, which, slot=0):
+        """Copies one view's buffer to the host (synchronises the context stream)."""
+        import torch
+        ptr, nbytes = self.device_ptr(view, which, slot)
+        self.ctx.sync()
+        dt, ch = _BUF_DTYPE[which]
+        w, h = self.sizes[view]
+        out = np.zeros((w * h, ch) if ch else w * h, dtype=dt)
+        host = torch.from_numpy(out.view(np.uint8).reshape(-1))
+        cudart = torch.cuda.cudart()
+        rc = cudart.cudaMemcpy(host.data_ptr(), ptr, nbytes, 2)   # device to host
+        if int(rc) != 0:
+            raise GrisError("cudaMemcpy failed (%s)" % rc)
+        return out
+
+    def close(self):
+        if self.handle:
+            load().grisBatchDestroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
         if sys.is_finalizing():
             return
         try:
