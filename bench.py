@@ -231,9 +231,6 @@ def main():
         else:
             frame.render(scene, cams[i], prevs[i], settings)
 
-    def output_ptr():
-        return batch.device_ptr(0, G.BUF_OUTPUT)[0] if batch is not None else frame.device_ptr(G.BUF_OUTPUT)[0]
-
     for _ in range(WU):
         render(fi)
         fi += 1
@@ -293,16 +290,17 @@ def main():
 
     # ---------------- end to end through the C ABI with host buffers
     out_host = torch.empty((W * H * 4,), dtype=torch.float32, pin_memory=True)
-    cudart = torch.cuda.cudart()
+    lib = G.load()
     barrier()
     t0 = time.perf_counter()
     for _ in range(K):
         render(fi)
-        # the frame's radiance to pinned host memory, on the library's stream, then wait for it
-        rc = cudart.cudaMemcpyAsync(out_host.data_ptr(), output_ptr(), W * H * 16, 2, ctx.stream())
-        if int(rc) != 0:
-            raise RuntimeError("cudaMemcpyAsync failed")
-        ctx.sync()
+        # the frame's radiance into pinned host memory through the C ABI (copy + wait)
+        if batch is not None:
+            batch.download(0, G.BUF_OUTPUT, out=(out_host.data_ptr(), W * H * 16))
+        else:
+            ctx.check(lib.grisFrameDownload(ctx.h, frame.handle, G.BUF_OUTPUT, 0, ctypes.c_void_p(out_host.data_ptr()),
+                                            W * H * 16), "grisFrameDownload")
         fi += 1
     barrier()
     e2e_s = time.perf_counter() - t0

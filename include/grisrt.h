@@ -304,6 +304,9 @@ int grisBatchRender(GrisContext* ctx, GrisBatch* batch, const GrisCamera* cams, 
                     const GrisSettings* settings);
 /* which / slot as in grisFrameGetBuffer, for one view. */
 int grisBatchGetBuffer(const GrisBatch* batch, uint32_t view, int which, int slot, void** devPtr, size_t* bytes);
+/* Copies one view's buffer to host memory on the context stream and waits for it. */
+int grisBatchDownload(GrisContext* ctx, const GrisBatch* batch, uint32_t view, int which, int slot, void* host,
+                      size_t bytes);
 
 /* ---------------------------------------------------------------- frames (library-owned buffers) */
 /* G-buffer cur/prev, reservoirs This[2]/Temp, output: the renderer's per-frame resources

@@ -182,4 +182,16 @@ int grisBatchGetBuffer(const GrisBatch* b, uint32_t view, int which, int slot, v
     return GRIS_OK;
 }
 
+int grisBatchDownload(GrisContext* ctx, const GrisBatch* b, uint32_t view, int which, int slot, void* host, size_t bytes) {
+    void* p = nullptr;
+    size_t sz = 0;
+    if (!ctx || !host || grisBatchGetBuffer(b, view, which, slot, &p, &sz) != GRIS_OK || bytes != sz)
+        return ctx_fail(ctx, GRIS_ERR_INVALID_ARGUMENT, "bad download request");
+    cudaSetDevice(ctx_device(ctx));
+    cudaError_t e = cudaMemcpyAsync(host, p, sz, cudaMemcpyDeviceToHost, ctx_stream(ctx));
+    if (e == cudaSuccess) e = cudaStreamSynchronize(ctx_stream(ctx));
+    if (e != cudaSuccess) return ctx_fail(ctx, GRIS_ERR_CUDA, std::string("grisBatchDownload: ") + cudaGetErrorString(e));
+    return GRIS_OK;
+}
+
 }  /* extern "C" */

@@ -113,6 +113,7 @@ EXPORTS = [
     "grisSceneGetStats", "grisDebugHostSceneCreate", "grisDebugTraceHost", "grisDebugTraceDevice", "grisPassGBuffer", "grisPassRender", "grisPassRenderNoAlloc",
     "grisFrameCreate", "grisFrameDestroy", "grisFrameRender", "grisFrameGetBuffer", "grisFrameDownload",
     "grisFrameUpload", "grisSetPathForm", "grisBatchCreate", "grisBatchDestroy", "grisBatchRender", "grisBatchGetBuffer",
+    "grisBatchDownload",
 ]
 
 _lib = None
@@ -171,6 +172,7 @@ def load(path=None):
         "grisBatchDestroy": (i32, [vp]),
         "grisBatchRender": (i32, [vp, vp, ctypes.POINTER(Camera), ctypes.POINTER(Camera), ctypes.POINTER(Settings)]),
         "grisBatchGetBuffer": (i32, [vp, u32, i32, i32, ctypes.POINTER(vp), ctypes.POINTER(ctypes.c_size_t)]),
+        "grisBatchDownload": (i32, [vp, vp, u32, i32, i32, vp, ctypes.c_size_t]),
     }
     for name, (res, args) in sig.items():
         f = getattr(lib, name)
@@ -476,19 +478,17 @@ class Batch:
                        "grisBatchGetBuffer")
         return p.value, n.value
 
-    def download(self, view, which, slot=0):
-        """Copies one view's buffer to the host (synchronises the context stream)."""
-        import torch
-        ptr, nbytes = self.device_ptr(view, which, slot)
-        self.ctx.sync()
+    def download(self, view, which, slot=0, out=None):
+        """Copies one view's buffer to the host (waits on the context stream)."""
         dt, ch = _BUF_DTYPE[which]
         w, h = self.sizes[view]
-        out = np.zeros((w * h, ch) if ch else w * h, dtype=dt)
-        host = torch.from_numpy(out.view(np.uint8).reshape(-1))
-        cudart = torch.cuda.cudart()
-        rc = cudart.cudaMemcpy(host.data_ptr(), ptr, nbytes, 2)   # device to host
-        if int(rc) != 0:
-            raise GrisError("cudaMemcpy failed (%s)" % rc)
+        if out is None:
+            out = np.zeros((w * h, ch) if ch else w * h, dtype=dt)
+            ptr, nbytes = out.ctypes.data, out.nbytes
+        else:   # caller-provided host buffer (e.g. pinned): (pointer, bytes)
+            ptr, nbytes = out
+        self.ctx.check(load().grisBatchDownload(self.ctx.h, self.handle, view, which, slot, ctypes.c_void_p(ptr), nbytes),
+                       "grisBatchDownload")
         return out
 
     def close(self):
