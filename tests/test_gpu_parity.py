@@ -35,8 +35,9 @@ def ora():
     return O.oracle()
 
 
-def gpu_sequence(ctx, hs, cams, prevs, st, W, H, mode=G.LAUNCH_PERSISTENT):
-    ctx.set_launch_mode(mode)
+def gpu_sequence(ctx, hs, cams, prevs, st, W, H, mode=(G.PATH_WAVEFRONT, G.LAUNCH_GRID)):
+    ctx.set_path_form(mode[0])
+    ctx.set_launch_mode(mode[1])
     scene = G.Scene(ctx, hs)
     fr = G.Frame(ctx, W, H)
     ctx.counters(reset=True)
@@ -53,10 +54,10 @@ def gpu_sequence(ctx, hs, cams, prevs, st, W, H, mode=G.LAUNCH_PERSISTENT):
     return out, counters
 
 
-MODES = [G.LAUNCH_PERSISTENT, G.LAUNCH_GRID]
+MODES = [(G.PATH_WAVEFRONT, G.LAUNCH_GRID), (G.PATH_MEGAKERNEL, G.LAUNCH_GRID), (G.PATH_MEGAKERNEL, G.LAUNCH_PERSISTENT)]
 
 
-@pytest.mark.parametrize("mode", MODES, ids=["persistent", "grid"])
+@pytest.mark.parametrize("mode", MODES, ids=["wavefront", "megakernel-grid", "megakernel-persistent"])
 @pytest.mark.parametrize("case", CASES, ids=[c[0] for c in CASES])
 def test_gpu_matches_oracle_bit_exact(case, mode, ctx, ora):
     name, kind, grid, spheres, W, H, frames, kw = case
@@ -64,7 +65,8 @@ def test_gpu_matches_oracle_bit_exact(case, mode, ctx, ora):
     cams, prevs = G.sequence_cameras(hs, frames, W, H, seed=11)
     st = G.Settings.make(**kw)
     got, gc = gpu_sequence(ctx, hs, cams, prevs, st, W, H, mode)
-    ctx.set_launch_mode(G.LAUNCH_PERSISTENT)
+    ctx.set_path_form(G.PATH_WAVEFRONT)
+    ctx.set_launch_mode(G.LAUNCH_GRID)
     ora.set_scene(hs)
     ora.read_counters(reset=True)
     want = O.run_sequence(ora, cams, prevs, st, W, H)

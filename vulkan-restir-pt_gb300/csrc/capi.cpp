@@ -72,8 +72,30 @@ struct Profiler : grisrt::KernelTimer {
 
 #define GRIS_NUM_COUNTERS 32
 
+/* Scratch of the wavefront path tracer for the single-view entry points, grown on demand. */
+struct WaveScratch {
+    grisrt::WaveBuffers wb{};
+    std::vector<void*> allocations;
+    void* dViews = nullptr;
+    void* hViews[2] = {nullptr, nullptr};
+    cudaEvent_t staged[2] = {nullptr, nullptr};
+    int stage = 0;
+    void release() {
+        for (void* p : allocations) cudaFree(p);
+        allocations.clear();
+        for (int i = 0; i < 2; i++) {
+            if (hViews[i]) cudaFreeHost(hViews[i]);
+            if (staged[i]) cudaEventDestroy(staged[i]);
+            hViews[i] = nullptr; staged[i] = nullptr;
+        }
+        dViews = nullptr;
+        wb = grisrt::WaveBuffers{};
+    }
+};
+
 struct GrisContext {
     int device = 0;
+    WaveScratch wave;
     cudaStream_t stream = nullptr;
     unsigned long long* dCounters = nullptr;
     unsigned long long* hCounters = nullptr;   /* pinned */
@@ -192,6 +214,7 @@ int grisDestroy(GrisContext* ctx) {
     if (!ctx) return GRIS_ERR_INVALID_ARGUMENT;
     cudaSetDevice(ctx->device);
     if (ctx->stream) cudaStreamSynchronize(ctx->stream);
+    ctx->wave.release();
     cudaFree(ctx->dCounters);
     cudaFreeHost(ctx->hCounters);
     if (ctx->stream) cudaStreamDestroy(ctx->stream);
@@ -407,6 +430,48 @@ int grisPassRender(GrisContext* ctx, const GrisScene* s, const GrisPassBindings*
     if (set->maxDepth == 0 || set->maxDepth > 255) return fail(ctx, GRIS_ERR_INVALID_ARGUMENT, "maxDepth must be 1..255");
     if (set->spatialNeighbors > 64) return fail(ctx, GRIS_ERR_INVALID_ARGUMENT, "spatialNeighbors must be <= 64");
     cudaSetDevice(ctx->device);
+    if (ctx->pathForm == GRIS_PATH_WAVEFRONT && (passes & 1)) {
+        /* the wavefront path tracer through the batch launcher, as a one-view batch */
+        uint64_t pixels = (uint64_t)b->width * b->height;
+        WaveScratch& w = ctx->wave;
+        if (w.wb.capacity < pixels) {
+            cudaStreamSynchronize(ctx->stream);
+            w.release();
+            cudaError_t e = cudaSuccess;
+            auto alloc = [&](void** p, size_t bytes) {
+                if (e == cudaSuccess) e = cudaMalloc(p, bytes < 256 ? 256 : bytes);
+                if (e == cudaSuccess) w.allocations.push_back(*p);
+            };
+            size_t P = (size_t)pixels;
+            alloc(&w.wb.state, P * 272);
+            alloc(&w.wb.nee, P * 96);
+            alloc(&w.wb.hit, P * 16);
+            alloc((void**)&w.wb.blocked, P);
+            alloc((void**)&w.wb.queue[0], P * 4);
+            alloc((void**)&w.wb.queue[1], P * 4);
+            alloc((void**)&w.wb.shadowQueue, P * 4);
+            alloc((void**)&w.wb.counts, 512 * 4);
+            alloc(&w.dViews, grisrt::view_entry_bytes());
+            for (int i = 0; i < 2 && e == cudaSuccess; i++) {
+                e = cudaMallocHost(&w.hViews[i], grisrt::view_entry_bytes());
+                if (e == cudaSuccess) e = cudaEventCreateWithFlags(&w.staged[i], cudaEventDisableTiming);
+            }
+            if (e != cudaSuccess) { w.release(); return cuda_fail(ctx, e, "wavefront scratch"); }
+            w.wb.capacity = pixels;
+        }
+        grisrt::BatchView v;
+        memset(&v, 0, sizeof(v));
+        v.scene = scene_view(s);
+        v.b = *b;
+        v.cam = *cam; v.prev = *prevCam; v.set = *set;
+        int k = w.stage;
+        GRIS_CK(ctx, cudaEventSynchronize(w.staged[k]));
+        GRIS_CK(ctx, grisrt::launch_batch(&v, 1, w.dViews, w.hViews[k], w.wb, ctx->dCounters, ctx->countWork, &ctx->prof,
+                                          ctx->stream, GRIS_PATH_WAVEFRONT, passes & 7));
+        GRIS_CK(ctx, cudaEventRecord(w.staged[k], ctx->stream));
+        w.stage ^= 1;
+        return GRIS_OK;
+    }
     GRIS_CK(ctx, grisrt::launch_gris(scene_view(s), *b, *cam, *prevCam, *set, passes & 7, ctx->dCounters, ctx->countWork,
                                      &ctx->prof, ctx->stream, ctx->launchMode));
     return GRIS_OK;
