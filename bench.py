@@ -1,23 +1,29 @@
 #!/usr/bin/env python3
-"""bench.py — ReSTIR PT (GRIS) frames/s and Mrays/s at 1920x1080 on the ~1.16M-triangle
-synthetic scene (512x512 fBm heightfield + 2000 instanced icospheres, GGX materials, 4 quad
-lights), max depth 8, temporal + spatial reuse (hybrid shift), camera orbit (60 frames per
-quarter turn).
+"""bench.py — ReSTIR PT (GRIS) frames/s and Mrays/s on one GB300.
 
-One step = one frame: G-buffer + path trace + temporal reuse + spatial reuse / final shading.
+Workloads (--workload):
+  c2  (default) 1920x1080, the ~1.16M-triangle synthetic scene (512x512 fBm heightfield + 2000
+      instanced icospheres, GGX materials, 4 quad lights), max depth 8, temporal + spatial
+      reuse (hybrid shift), camera orbit (60 frames per quarter turn);
+  c3  64 independent views in one batch: resolutions from {64,128,256,512}^2, each with its own
+      box-or-terrain scene of 10k-200k triangles, max depth uniform in [2, 10].
 
-  value   frames/s timed on the device with CUDA events on the library's stream, scene and
+One step = one frame of every view: G-buffer + path trace + temporal reuse + spatial reuse /
+final shading, rendered through grisBatchRender (a captured CUDA graph replayed per frame; the
+launch configuration picked by grisBatchAutotune first).
+
+  value   frames/s timed on the device with CUDA events on the library's stream, scenes and
           frame buffers resident in HBM, L2 flushed (256 MiB write) between frames outside the
           timed events;
   e2e     frames/s through the C ABI from the host: the per-frame cameras and settings come
-          from host memory (kernel parameters) and each frame's RGBA32F radiance is read back
-          into pinned host memory, wall-clock timed;
-  roofline  the dominant kernel's algorithmic bytes per launch (BVH nodes x 80 B + triangles
-          x 48 B + surface fetches + the per-pixel G-buffer / reservoir bytes, counted on the
-          same frames) over its average CUDA-event launch time, against the measured HBM copy
-          bandwidth;
+          from host memory and every view's RGBA32F radiance is read back into pinned host
+          memory each frame, wall-clock timed;
+  roofline  the kernel with the largest share of the frame: its algorithmic bytes per launch
+          (BVH nodes x 80 B + triangles x 48 B + per-ray / per-pixel record bytes, counted on the
+          same frames) over its average CUDA-event launch time (a separate profiled pass, eager
+          launches), against the measured HBM copy bandwidth;
   cpu_baseline  the oracle restatement (C++, OpenMP, binary BVH) on this host's cores on a
-          band of rows of the same frames, scaled to frames/s.
+          band of rows of every view, scaled to frames/s.
 
 --impl reference times that CPU implementation alone (rank 0), the reference's own GLSL
 path being unavailable on this machine (no graphics stack).
@@ -26,6 +32,7 @@ Multi-GPU: replicas (each rank renders the same workload; no collective in the p
 import argparse
 import ctypes
 import json
+import math
 import os
 import statistics
 import subprocess
@@ -39,15 +46,45 @@ for p in (PKG, REPO):
     if p not in sys.path:
         sys.path.insert(0, p)
 
-METRIC = "ReSTIR PT frames/s at 1080p (1.16M-tri synthetic scene, depth 8, temporal+spatial reuse)"
+METRICS = {
+    "c2": "ReSTIR PT frames/s at 1080p (1.16M-tri synthetic scene, depth 8, temporal+spatial reuse)",
+    "c3": "Batched ReSTIR PT frames/s (64 views of {64..512}^2, 10k-200k tris each, depth 2-10)",
+}
 UNIT = "frames/s"
-KERNELS = ["k_gbuffer", "k_path_trace", "k_temporal", "k_spatial"]
-# Fixed G-buffer / reservoir bytes per pixel and kernel (28 B G-buffer texel, 96 B reservoir):
-#   G-buffer write 28; path trace 24 read + 96 write; temporal 24+4+24 G-buffer + 2 x 96 reservoir
-#   read + 96 write; spatial 4 x 24 + 4 x 96 read + 96 write + 32 output read/write.
-PIXEL_BYTES = [28, 120, 340, 608]
 NODE_BYTES, TRI_BYTES = 80, 48
-SURFACE_BYTES = 264   # per closest hit: 3 vertices (96) + transform and inverse-transpose (128) + offsets (8) + material (32)
+SURFACE_BYTES = 264   # per closest hit shaded: 3 vertices (96) + transform and inverse-transpose (128) + offsets (8) + material (32)
+WAVE_STATE = 272      # one path's wavefront record (17 x 16 B)
+NEE_STATE = 96        # one shadow query's record (6 x 16 B)
+
+
+def alg_bytes(slot, w, px):
+    """Algorithmic bytes of one frame of kernel `slot` (work `w` per frame, `px` pixels):
+      gbuffer      traversal + 28 B G-buffer texel + a surface fetch per primary hit
+      path_trace   (megakernel) traversal + 24 B G-buffer read + 96 B reservoir write + surface fetches
+      temporal     traversal + 24+4+24 B G-buffer + 2 x 96 B reservoir reads + 96 B write + surface fetches
+      spatial      traversal + 4 x 24 B G-buffer + 4 x 96 B reservoir reads + 96 B write + 32 B output r/w
+                   + surface fetches
+      wave_begin   24 B G-buffer read + a path record write + a 4 B queue entry per pixel
+      wave_extend  per ray: 32 B ray + 16 B hit + 4 B queue entry, plus traversal
+      wave_shade   per path: record read and write + 16 B hit + a surface fetch + 4 B queue entry
+      wave_shadow  per shadow ray: 48 B query + 1 B verdict + 4 B queue entry, plus traversal
+      wave_post    per shadow query: record read and write + query read + verdict + queue entry"""
+    trav = w["nodes"] * NODE_BYTES + w["tris"] * TRI_BYTES
+    r = w["rays"]
+    per_px = {"gbuffer": 28, "path_trace": 120, "temporal": 340, "spatial": 608, "wave_begin": 24 + WAVE_STATE + 4}
+    if slot in ("gbuffer", "path_trace", "temporal", "spatial"):
+        return trav + per_px[slot] * px + SURFACE_BYTES * r
+    if slot == "wave_begin":
+        return per_px[slot] * px
+    if slot == "wave_extend":
+        return trav + 52 * r
+    if slot == "wave_shade":
+        return w["paths"] * (2 * WAVE_STATE + 16 + SURFACE_BYTES + 4)
+    if slot == "wave_shadow":
+        return trav + 53 * r
+    if slot == "wave_post":
+        return w["shadow_paths"] * (2 * WAVE_STATE + NEE_STATE + 1 + 4)
+    return 0
 
 
 def parse():
@@ -56,17 +93,22 @@ def parse():
     ap.add_argument("--steps", type=int, default=30)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="grisrt", choices=["grisrt", "reference"])
+    ap.add_argument("--workload", default="c2", choices=["c2", "c3"])
     ap.add_argument("--width", type=int, default=1920)
     ap.add_argument("--height", type=int, default=1080)
     ap.add_argument("--grid", type=int, default=512)
     ap.add_argument("--spheres", type=int, default=2000)
     ap.add_argument("--depth", type=int, default=8)
+    ap.add_argument("--views", type=int, default=64, help="views of the c3 workload")
     ap.add_argument("--seed", type=int, default=1)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-autotune", action="store_true")
+    ap.add_argument("--no-graphs", action="store_true")
     ap.add_argument("--launch-mode", default="grid", choices=["persistent", "grid"])
     ap.add_argument("--api", default="batch", choices=["batch", "frame"],
-                    help="grisBatchRender (one-view batch) or grisFrameRender")
-    ap.add_argument("--path-form", default="wavefront", choices=["wavefront", "megakernel"])
+                    help="grisBatchRender or grisFrameRender (c2 only)")
+    ap.add_argument("--path-form", default="wavefront", choices=["wavefront", "megakernel"],
+                    help="starting form (the autotuner may switch)")
     ap.add_argument("--cpu-seconds", type=float, default=20.0, help="target CPU work of the baseline sample")
     return ap.parse_args()
 
@@ -129,37 +171,96 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
-def cpu_oracle_run(hs, cams, prevs, settings, width, height, target_seconds, frames=2):
-    """Times the oracle on a band of rows of `frames` frames; returns (frames/s, threads, sample, rays/s)."""
-    import numpy as np
+class View:
+    def __init__(self, hs, width, height, settings, frames, seed):
+        import grisrt as G
+        self.hs, self.w, self.h, self.settings = hs, width, height, settings
+        self.cams, self.prevs = G.sequence_cameras(hs, frames, width, height, seed=seed, orbit_frames=60)
+
+
+def make_views(args, frames):
+    """The workload's views with `frames` cameras each, and its config dict."""
+    import grisrt as G
+    from grisrt import workloads
+
+    def settings(depth):
+        return G.Settings.make(shiftType=2, rrScale=1.0, temporalReuse=True, spatialReuse=True, cap=20,
+                               maxDepth=depth, spatialNeighbors=3, spatialRadius=20.0)
+    common = {"spatial_neighbors": 3, "spatial_radius_px": 20.0, "cap": 20, "shift": "hybrid",
+              "l2": "flushed between frames (256 MiB write outside the timed events)"}
+    if args.workload == "c2":
+        hs = G.HostScene(1, seed=args.seed, grid=args.grid, spheres=args.spheres)
+        views = [View(hs, args.width, args.height, settings(args.depth), frames, args.seed)]
+        config = {"workload": "C2: %dx%d, %d^2 fBm heightfield + %d icospheres (%d tris), depth %d, orbit" % (
+            args.width, args.height, args.grid, args.spheres, hs.triangle_count(), args.depth),
+            "width": args.width, "height": args.height, "triangles": hs.triangle_count(), "max_depth": args.depth}
+    else:
+        specs = workloads.batched_views(args.views, seed=args.seed + 6)
+        views = []
+        for i, s in enumerate(specs):
+            hs = G.HostScene(s["kind"], seed=s["seed"], grid=s["grid"], spheres=s["spheres"])
+            views.append(View(hs, s["width"], s["height"], settings(s["maxDepth"]), frames, args.seed + i))
+        tris = [v.hs.triangle_count() for v in views]
+        px = sum(v.w * v.h for v in views)
+        config = {"workload": "C3: %d views, {64,128,256,512}^2 (%d px), box-or-terrain scenes %d-%d tris (%d total), "
+                              "depth 2-10" % (len(views), px, min(tris), max(tris), sum(tris)),
+                  "views": len(views), "pixels": px, "triangles": sum(tris),
+                  "max_depth": [v.settings.maxDepth for v in views]}
+    config.update(common)
+    return views, config
+
+
+def cpu_oracle_run(views, target_seconds, frames=2, ora=None, plan=None):
+    """Times the oracle on a band of rows of every view over `frames` frames; the band is
+    calibrated so the sample takes about `target_seconds` (pass `plan` to repeat a calibrated
+    sample). Returns (frames/s, threads, sample text, rays/s, plan)."""
     from oracle import pyoracle as O
-    ora = O.oracle()
-    ora.set_scene(hs)
-    ora.set_traversal(True)
+    if ora is None:
+        ora = O.oracle()
+        ora.set_traversal(True)
+        for i, v in enumerate(views):
+            ora.select_scene(i)
+            ora.set_scene(v.hs)
     threads = ora.threads()
-    n = width * height
-    rows = max(8, height // 32)
-    # calibrate the band: one frame of `rows` rows
-    results = None
-    for attempt in range(3):
-        ora.set_rows(0, rows)
+    max_frames = min(len(v.cams) for v in views)
+
+    def run(frac, nf):
+        t_sample, t_full = 0.0, 0.0
         ora.read_counters(reset=True)
-        t0 = time.perf_counter()
-        O.run_sequence(ora, cams[:frames], prevs[:frames], settings, width, height, record=())
-        dt = time.perf_counter() - t0
-        if dt * (height / rows) >= target_seconds * 0.5 or rows >= height or dt > target_seconds / 2:
-            results = dt
-            break
-        rows = min(height, int(rows * max(2.0, min(8.0, target_seconds / 2 / max(dt, 1e-3)))))
-    if results is None:
-        results = dt
-    cnt = ora.read_counters(reset=True)
-    ora.set_rows(0, 1 << 30)
-    frac = rows / height
-    fps = frames * frac / results
-    rays = (cnt[0] + cnt[1] + cnt[2]) / results
-    sample = "%d frames x rows [0,%d) of %dx%d (%.1f%% of each frame), %.2f s" % (frames, rows, width, height, 100 * frac, results)
-    return fps, threads, sample, rays
+        for i, v in enumerate(views):
+            rows = max(1, min(v.h, int(round(v.h * frac))))
+            ora.select_scene(i)
+            ora.set_rows(0, rows)
+            t0 = time.perf_counter()
+            O.run_sequence(ora, v.cams[:nf], v.prevs[:nf], v.settings, v.w, v.h, record=())
+            dt = time.perf_counter() - t0
+            t_sample += dt
+            t_full += dt * v.h / rows
+        cnt = ora.read_counters(reset=True)
+        ora.set_rows(0, 1 << 30)
+        return t_sample, t_full, cnt[0] + cnt[1] + cnt[2]
+
+    if plan is None:
+        frac, nf = 1.0 / 32.0, min(frames, max_frames)
+        for _ in range(6):
+            t_sample, t_full, rays = run(frac, nf)
+            if t_sample >= 0.5 * target_seconds:
+                break
+            grow = max(2.0, min(16.0, target_seconds / max(t_sample, 1e-3)))
+            if frac < 1.0:
+                frac = min(1.0, frac * grow)
+            elif nf < max_frames:
+                nf = min(max_frames, int(math.ceil(nf * grow)))
+            else:
+                break
+        plan = (frac, nf)
+    else:
+        t_sample, t_full, rays = run(*plan)
+    frac, nf = plan
+    fps = nf / t_full
+    sample = "%d frame(s) x the first %.1f%% of the rows of each of %d view(s), %.2f s of CPU time" % (
+        nf, 100.0 * min(1.0, frac), len(views), t_sample)
+    return fps, threads, sample, rays / t_sample, plan, ora
 
 
 def main():
@@ -167,30 +268,27 @@ def main():
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
     local = int(os.environ.get("LOCAL_RANK", "0"))
-    W, H, K, WU = args.width, args.height, args.steps, max(args.warmup, 0)
+    K, WU = args.steps, max(args.warmup, 0)
+    if args.workload == "c3":
+        args.api = "batch"
     import grisrt as G
-    settings = G.Settings.make(shiftType=2, rrScale=1.0, temporalReuse=True, spatialReuse=True, cap=20,
-                               maxDepth=args.depth, spatialNeighbors=3, spatialRadius=20.0)
-    config = {"workload": "C2: %dx%d, 512^2 fBm heightfield + %d icospheres (~1.16M tris), depth %d, orbit" % (
-        W, H, args.spheres, args.depth), "width": W, "height": H, "triangles": None, "max_depth": args.depth,
-        "spatial_neighbors": 3, "spatial_radius_px": 20.0, "cap": 20, "shift": "hybrid",
-        "l2": "flushed between frames (256 MiB write outside the timed events)", "parallelism": "replicas" if world > 1 else "1 GPU"}
+    metric = METRICS[args.workload]
 
     if args.impl == "reference":
         if rank != 0:
             return 0
-        hs = G.HostScene(1, seed=args.seed, grid=args.grid, spheres=args.spheres)
-        config["triangles"] = hs.triangle_count()
-        cams, prevs = G.sequence_cameras(hs, 2, W, H, seed=args.seed, orbit_frames=60)
+        views, config = make_views(args, 16)
+        config["parallelism"] = "host cores (OpenMP)"
         budget = max(5.0, min(60.0, 150.0 / max(1, K + WU)))
         vals = []
+        plan, ora = None, None
         threads, sample = 0, ""
         for step in range(WU + K):
-            fps, threads, sample, rays = cpu_oracle_run(hs, cams, prevs, settings, W, H, budget)
+            fps, threads, sample, rays, plan, ora = cpu_oracle_run(views, budget, ora=ora, plan=plan)
             if step >= WU:
                 vals.append(fps)
         value = statistics.median(vals) if vals else 0.0
-        line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus, "steps": K, "warmup": WU,
+        line = {"metric": metric, "value": value, "unit": UNIT, "n_gpus": args.gpus, "steps": K, "warmup": WU,
                 "ms_per_step": 1000.0 / value if value else None, "higher_is_better": True, "scaling": "weak",
                 "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded scene generator)", "config": config,
                 "impl": "reference",
@@ -207,44 +305,58 @@ def main():
     if world > 1:
         import torch.distributed as dist
         dist.init_process_group("nccl", device_id=torch.device("cuda", local))
-    hs = G.HostScene(1, seed=args.seed, grid=args.grid, spheres=args.spheres)
-    config["triangles"] = hs.triangle_count()
+    total = WU + 3 * K + 8
+    views, config = make_views(args, total)
+    config["parallelism"] = "replicas" if world > 1 else "1 GPU"
+    n = len(views)
+    px = sum(v.w * v.h for v in views)
     ctx = G.Context(local)
     ctx.set_launch_mode(G.LAUNCH_PERSISTENT if args.launch_mode == "persistent" else G.LAUNCH_GRID)
     ctx.set_path_form(G.PATH_WAVEFRONT if args.path_form == "wavefront" else G.PATH_MEGAKERNEL)
+    ctx.set_graphs(not args.no_graphs)
+    scenes = [G.Scene(ctx, v.hs) for v in views]
+    stats = [sc.stats() for sc in scenes]
+    batch = G.Batch(ctx, scenes, [(v.w, v.h) for v in views]) if args.api == "batch" else None
+    frame = G.Frame(ctx, views[0].w, views[0].h) if args.api == "frame" else None
     config["api"] = args.api
-    config["launch"] = args.launch_mode if args.api == "frame" else "batch tiles"
-    config["path_form"] = args.path_form if args.api == "batch" else "megakernel"
-    scene = G.Scene(ctx, hs)
-    stats = scene.stats()
-    frame = G.Frame(ctx, W, H) if args.api == "frame" else None
-    batch = G.Batch(ctx, [scene], [(W, H)]) if args.api == "batch" else None
-    total = WU + 2 * K + 4
-    cams, prevs = G.sequence_cameras(hs, total, W, H, seed=args.seed, orbit_frames=60)
     stream = torch.cuda.ExternalStream(ctx.stream(), device=torch.device("cuda", local))
     flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
     fi = 0
 
     def render(i):
         if batch is not None:
-            batch.render([cams[i]], [prevs[i]], [settings])
+            batch.render([v.cams[i] for v in views], [v.prevs[i] for v in views], [v.settings for v in views])
         else:
-            frame.render(scene, cams[i], prevs[i], settings)
+            v = views[0]
+            frame.render(scenes[0], v.cams[i], v.prevs[i], v.settings)
 
     for _ in range(WU):
         render(fi)
         fi += 1
     ctx.sync()
+    tune = None
+    if batch is not None and not args.no_autotune:
+        r = batch.autotune([v.cams[fi] for v in views], [v.prevs[fi] for v in views], [v.settings for v in views],
+                           frames=3)
+        fi += 1
+        names = ["megakernel"] + ["wavefront t%d s%d" % (t, s) for t in (8, 16, 32) for s in (4, 8, 16)]
+        tune = {"chosen": "megakernel" if r.pathForm == G.PATH_MEGAKERNEL else
+                "wavefront t%d s%d" % (r.traceBlocksPerSM, r.shadeBlocksPerSM),
+                "ms": {names[i]: round(r.candidateMs[i], 3) for i in range(r.candidates)}}
+        form = r.pathForm
+    else:
+        form = G.PATH_WAVEFRONT if args.path_form == "wavefront" else G.PATH_MEGAKERNEL
+    config["path_form"] = ("wavefront" if form == G.PATH_WAVEFRONT else "megakernel") if batch is not None else "megakernel"
+    config["graphs"] = batch is not None and not args.no_graphs
+    config["autotune"] = tune
 
     def barrier():
         torch.cuda.synchronize()
         if world > 1:
             torch.distributed.barrier()
 
-    # ---------------- device-timed frames
+    # ---------------- device-timed frames (graph replays, no per-kernel events)
     ctx.counters(reset=True)
-    ctx.set_profiling(True)
-    ctx.profile(reset=True)
     sampler = ClockSampler(local)
     sampler.start()
     time.sleep(0.3)
@@ -262,11 +374,6 @@ def main():
     barrier()
     clocks = sampler.stop()
     ms = sum(a.elapsed_time(b) for a, b in events)
-    kms, klaunch = ctx.profile(reset=True)
-    # kernels per frame: G-buffer, temporal, spatial + the path tracer (one kernel, or the
-    # wavefront's begin + 4 stages for each further bounce)
-    launches_per_frame = 4 if (args.api == "frame" or args.path_form == "megakernel") else 3 + 1 + 4 * (args.depth - 1)
-    ctx.set_profiling(False)
     cnt = ctx.counters(reset=True)
     ctx.sync()
     t_max = ms
@@ -278,29 +385,50 @@ def main():
     rays = cnt[0] + cnt[1] + cnt[2]
     mrays = world * rays / (t_max / 1000.0) / 1e6
 
+    # ---------------- per-kernel profile of the same frames (eager launches with events)
+    fi_p = fi - K
+    ctx.set_profiling(True)
+    ctx.kernel_profile(reset=True)
+    with torch.cuda.stream(stream):
+        for i in range(K):
+            flush.zero_()
+            render(fi_p + i)
+    ctx.sync()
+    prof = ctx.kernel_profile(reset=True)
+    ctx.set_profiling(False)
     # ---------------- work counting on the same frames (untimed)
     ctx.set_work_counting(True)
-    ctx.work(reset=True)
-    fi_c = fi - K
+    ctx.kernel_profile(reset=True)
     for i in range(K):
-        render(fi_c + i)
+        render(fi_p + i)
     ctx.sync()
-    nodes, tris, kr = ctx.work(reset=True)
+    work = ctx.kernel_profile(reset=True)
     ctx.set_work_counting(False)
 
+    wave = config["path_form"] == "wavefront"
+    slots = (["gbuffer", "temporal", "spatial", "wave_begin", "wave_extend", "wave_shade", "wave_shadow", "wave_post"]
+             if wave else ["gbuffer", "path_trace", "temporal", "spatial"])
+    launches_per_frame = sum(prof[s]["launches"] for s in slots) / K
+
     # ---------------- end to end through the C ABI with host buffers
-    out_host = torch.empty((W * H * 4,), dtype=torch.float32, pin_memory=True)
+    out_host = torch.empty((px * 4,), dtype=torch.float32, pin_memory=True)
     lib = G.load()
+    offs, o = [], 0
+    for v in views:
+        offs.append(o)
+        o += v.w * v.h * 16
     barrier()
     t0 = time.perf_counter()
     for _ in range(K):
         render(fi)
-        # the frame's radiance into pinned host memory through the C ABI (copy + wait)
-        if batch is not None:
-            batch.download(0, G.BUF_OUTPUT, out=(out_host.data_ptr(), W * H * 16))
-        else:
-            ctx.check(lib.grisFrameDownload(ctx.h, frame.handle, G.BUF_OUTPUT, 0, ctypes.c_void_p(out_host.data_ptr()),
-                                            W * H * 16), "grisFrameDownload")
+        # every view's radiance into pinned host memory through the C ABI (copy + wait)
+        for vi, v in enumerate(views):
+            ptr = out_host.data_ptr() + offs[vi]
+            if batch is not None:
+                batch.download(vi, G.BUF_OUTPUT, out=(ptr, v.w * v.h * 16))
+            else:
+                ctx.check(lib.grisFrameDownload(ctx.h, frame.handle, G.BUF_OUTPUT, 0, ctypes.c_void_p(ptr),
+                                                v.w * v.h * 16), "grisFrameDownload")
         fi += 1
     barrier()
     e2e_s = time.perf_counter() - t0
@@ -308,55 +436,62 @@ def main():
         t = torch.tensor([e2e_s], device="cuda")
         torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
         e2e_s = float(t.item())
-    e2e = {"value": world * K / e2e_s, "unit": UNIT, "h2d_bytes_per_step": 2 * 352 + 64,
-           "d2h_bytes_per_step": W * H * 16}
+    e2e = {"value": world * K / e2e_s, "unit": UNIT, "h2d_bytes_per_step": n * (2 * 352 + 64),
+           "d2h_bytes_per_step": px * 16}
 
-    # ---------------- roofline of the dominant kernel
+    # ---------------- roofline of the kernel with the largest share
     peak, peak_kind = load_peaks()
-    k = max(range(4), key=lambda i: kms[i])
-    launches = max(1, klaunch[k])
-    avg_s = kms[k] / launches / 1000.0
-    px = W * H
-    alg = (nodes[k] * NODE_BYTES + tris[k] * TRI_BYTES) / K + PIXEL_BYTES[k] * px
-    # surface fetches: closest hits of the kernel (primary hits for the G-buffer)
-    alg += SURFACE_BYTES * (kr[k] / K)
-    achieved = alg / avg_s / 1e9
+    per_kernel = {}
+    for s in slots:
+        L = max(1, prof[s]["launches"])
+        w = {k: work[s][k] / K for k in ("nodes", "tris", "rays")}
+        w["paths"] = work["wave_extend"]["rays"] / K
+        w["shadow_paths"] = work["wave_shadow"]["rays"] / K
+        alg_frame = alg_bytes(s, w, px)
+        avg_ms = prof[s]["ms"] / L
+        per_kernel[s] = {"ms_per_frame": prof[s]["ms"] / K, "launches_per_frame": prof[s]["launches"] / K,
+                         "avg_launch_ms": avg_ms, "alg_bytes_per_launch": alg_frame * K / L,
+                         "gbs": (alg_frame * K / L) / (avg_ms / 1000.0) / 1e9 if avg_ms > 0 else None,
+                         "nodes_per_frame": w["nodes"], "tris_per_frame": w["tris"], "rays_per_frame": w["rays"]}
+    top = max(slots, key=lambda s: prof[s]["ms"])
+    pk = per_kernel[top]
+    achieved = pk["gbs"] or 0.0
     traffic = None
     tfile = os.path.join(REPO, "profiles", "ncu_dram_traffic.json")
     if os.path.exists(tfile):
         try:
-            tj = json.load(open(tfile))
-            e = tj.get(KERNELS[k])
+            tj = json.load(open(tfile)).get(args.workload, {})
+            e = tj.get(top)
             if e:
                 traffic = float(e["bytes_per_launch"]) * (px / float(e.get("pixels", px)))
         except Exception:
             traffic = None
-    roofline = {"bound": "hbm", "kernel": KERNELS[k], "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
+    roofline = {"bound": "hbm", "kernel": top, "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
                 "frac": round(achieved / peak, 4), "peak_source": peak_kind, "traffic": traffic,
-                "algorithmic_bytes_per_launch": alg, "avg_launch_ms": avg_s * 1000.0,
-                "per_kernel_ms_per_frame": {KERNELS[i]: kms[i] / max(1, klaunch[i]) for i in range(4)},
-                "nodes_per_frame": [n / K for n in nodes], "tris_per_frame": [t / K for t in tris],
-                "closest_rays_per_frame": [r / K for r in kr]}
+                "algorithmic_bytes_per_launch": pk["alg_bytes_per_launch"], "avg_launch_ms": pk["avg_launch_ms"],
+                "share_of_frame": round(prof[top]["ms"] / max(1e-9, sum(prof[s]["ms"] for s in slots)), 3),
+                "kernels": per_kernel}
 
     # ---------------- CPU baseline (rank 0)
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
         try:
-            fps, threads, sample, rps = cpu_oracle_run(hs, cams[:2], prevs[:2], settings, W, H, args.cpu_seconds)
+            fps, threads, sample, rps, _, _ = cpu_oracle_run(views, args.cpu_seconds)
             cpu = {"value": fps, "unit": UNIT, "cores": threads, "kind": "port", "sample": sample,
                    "mrays_per_s": rps / 1e6}
         except Exception as ex:   # the baseline is reported, never required
             cpu = {"value": None, "unit": UNIT, "cores": 0, "kind": "port", "sample": "failed: %s" % ex}
 
     if rank == 0:
-        line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": K, "warmup": WU,
+        line = {"metric": metric, "value": value, "unit": UNIT, "n_gpus": world, "steps": K, "warmup": WU,
                 "ms_per_step": t_max / K, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
                 "dtype": "f32", "data": "synthetic (seeded scene generator, no dataset)", "config": config,
                 "mrays_per_s": mrays, "rays_per_frame": rays / K,
-                "bvh": {"nodes": stats.nodeCount, "node_mb": stats.nodeBytes / 1e6, "tri_mb": stats.triangleBytes / 1e6,
-                        "depth": stats.maxDepth, "build_s": stats.buildSeconds},
-                "clocks": clocks, "e2e": e2e, "gpu_launches": launches_per_frame * K, "roofline": roofline,
-                "cpu_baseline": cpu}
+                "bvh": {"nodes": sum(s.nodeCount for s in stats), "node_mb": sum(s.nodeBytes for s in stats) / 1e6,
+                        "tri_mb": sum(s.triangleBytes for s in stats) / 1e6, "depth": max(s.maxDepth for s in stats),
+                        "build_s": sum(s.buildSeconds for s in stats)},
+                "clocks": clocks, "e2e": e2e, "gpu_launches": int(round(launches_per_frame * K)),
+                "roofline": roofline, "cpu_baseline": cpu}
         print(json.dumps(line))
     if world > 1:
         torch.distributed.destroy_process_group()

@@ -217,6 +217,22 @@ int grisSetWorkCounting(GrisContext* ctx, int enable);
 #define GRIS_LAUNCH_PERSISTENT 1
 int grisSetLaunchMode(GrisContext* ctx, int mode);
 int grisReadWorkCounters(GrisContext* ctx, uint64_t nodes[4], uint64_t tris[4], uint64_t closestRays[4], int reset);
+/* Per-kernel profile with the wavefront stages on their own: slots 0-3 as grisReadProfile (slot 1
+ * spans the whole path tracer), then the wavefront's begin, extension (closest hits), shading,
+ * shadow and post stages. ms/launches while profiling is on; nodes/tris/rays while work counting
+ * is on, for the slots that traverse (rays: closest-hit rays, shadow rays for the shadow stage). */
+#define GRIS_PROFILE_SLOTS 9
+#define GRIS_SLOT_WAVE_BEGIN 4
+#define GRIS_SLOT_WAVE_EXTEND 5
+#define GRIS_SLOT_WAVE_SHADE 6
+#define GRIS_SLOT_WAVE_SHADOW 7
+#define GRIS_SLOT_WAVE_POST 8
+typedef struct GrisKernelProfile {
+    double ms;
+    uint64_t launches;
+    uint64_t nodes, tris, rays;
+} GrisKernelProfile;
+int grisReadKernelProfile(GrisContext* ctx, GrisKernelProfile out[GRIS_PROFILE_SLOTS], int reset);
 size_t grisSizeof(int which);   /* 0 camera, 1 reservoir, 2 material, 3 vertex, 4 instance, 5 light, 6 table entry, 7 settings */
 
 /* ---------------------------------------------------------------- host helpers (no GPU) */
@@ -233,8 +249,9 @@ int grisCameraLookAt(GrisCamera* cam, const float pos[3], const float target[3],
  * ceiling area), Lambertian walls with albedo ~ U[0.2,0.8]^3; kind 1: fBm heightfield (gridN x gridN
  * vertices) + `spheres` instanced icospheres (subdivision 2) with radii log-uniform [0.1, 2], GGX
  * MetallicWorkflow materials, 4 quad lights; kind 2: glossy variant of kind 1 (roughness U[0.02,0.3],
- * 70% metallic, occluders over the lights). The camera for frame f of the scene's orbit comes from
- * grisHostSceneCamera. */
+ * 70% metallic, occluders over the lights); kind 3: the kind 0 box furnished with `spheres`
+ * instanced icospheres (320 triangles each, radii U[0.02,0.12], Lambertian or GGX). The camera for
+ * frame f of the scene's orbit comes from grisHostSceneCamera. */
 int grisHostSceneCreate(int kind, uint64_t seed, uint32_t gridN, uint32_t spheres, GrisHostScene** out);
 int grisHostSceneDesc(const GrisHostScene* hs, GrisSceneDesc* out);
 int grisHostSceneCamera(const GrisHostScene* hs, uint32_t frame, uint32_t frames, uint32_t width,
@@ -296,6 +313,22 @@ int grisPassRenderNoAlloc(const GrisScene* scene, const GrisPassBindings* b, con
 #define GRIS_PATH_WAVEFRONT 1
 typedef struct GrisBatch GrisBatch;
 int grisSetPathForm(GrisContext* ctx, int form);
+/* Batch frames are captured once into a CUDA graph (per staging slot and frame shape) and
+ * replayed (default on; off while per-kernel profiling is on). */
+int grisSetGraphs(GrisContext* ctx, int enable);
+/* Grid sizes of the wavefront kernels, in 128-thread blocks per SM (defaults 16 and 8). */
+int grisSetWaveLaunch(GrisContext* ctx, int traceBlocksPerSM, int shadeBlocksPerSM);
+/* Times candidate configurations — the megakernel path tracer and the wavefront one with trace
+ * grids of 8/16/32 and shading grids of 4/8/16 blocks per SM — over `frames` frames each on the
+ * given views (those frames are rendered: reservoirs and output change), keeps the fastest in
+ * the context and reports it. */
+typedef struct GrisTuneResult {
+    int pathForm;
+    int traceBlocksPerSM, shadeBlocksPerSM;
+    int candidates;
+    double msPerFrame;            /* of the chosen configuration */
+    double candidateMs[16];       /* per candidate, in the order above */
+} GrisTuneResult;
 int grisBatchCreate(GrisContext* ctx, uint32_t nViews, const GrisScene* const* scenes, const uint32_t* widths,
                     const uint32_t* heights, GrisBatch** out);
 int grisBatchDestroy(GrisBatch* batch);
@@ -307,6 +340,8 @@ int grisBatchGetBuffer(const GrisBatch* batch, uint32_t view, int which, int slo
 /* Copies one view's buffer to host memory on the context stream and waits for it. */
 int grisBatchDownload(GrisContext* ctx, const GrisBatch* batch, uint32_t view, int which, int slot, void* host,
                       size_t bytes);
+int grisBatchAutotune(GrisContext* ctx, GrisBatch* batch, const GrisCamera* cams, const GrisCamera* prevCams,
+                      const GrisSettings* settings, int frames, GrisTuneResult* out);
 
 /* ---------------------------------------------------------------- frames (library-owned buffers) */
 /* G-buffer cur/prev, reservoirs This[2]/Temp, output: the renderer's per-frame resources

@@ -960,6 +960,22 @@ int oracle_scene_set(void* vertices, unsigned long long nv, void* indices, unsig
 
 void oracle_set_traversal(int useBvh) { g.useBvh = useBvh; }
 
+/* Keeps several scenes resident: slot `slot` becomes the current scene (empty until
+ * oracle_scene_set fills it); the previous current scene stays in its own slot. */
+static std::vector<Scene> g_slots(1);
+static int g_slot = 0;
+int oracle_scene_select(int slot) {
+    if (slot < 0 || slot >= 4096) return -1;
+    if (slot == g_slot) return 0;
+    if ((size_t)slot >= g_slots.size()) g_slots.resize((size_t)slot + 1);
+    int useBvh = g.useBvh;
+    std::swap(g, g_slots[(size_t)g_slot]);
+    std::swap(g, g_slots[(size_t)slot]);
+    g.useBvh = useBvh;
+    g_slot = slot;
+    return 0;
+}
+
 /* Restricts the G-buffer and the three passes to rows [y0, y1) (a bounded sample of a frame). */
 void oracle_set_rows(int y0, int y1) { g_row0 = y0; g_row1 = y1; }
 

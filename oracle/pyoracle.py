@@ -57,6 +57,13 @@ class CpuImpl:
         f.argtypes = [ctypes.c_int, ctypes.c_int]
         f(int(y0), int(y1))
 
+    def select_scene(self, slot):
+        """Makes scene slot `slot` current (the oracle keeps several scenes resident)."""
+        f = self.lib.oracle_scene_select
+        f.argtypes, f.restype = [ctypes.c_int], ctypes.c_int
+        if f(int(slot)) != 0:
+            raise ValueError("bad scene slot %d" % slot)
+
     def threads(self):
         return int(self.lib.oracle_threads())
 

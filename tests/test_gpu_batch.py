@@ -38,10 +38,16 @@ def setup():
     ctx.close()
 
 
-@pytest.mark.parametrize("form", [G.PATH_WAVEFRONT, G.PATH_MEGAKERNEL], ids=["wavefront", "megakernel"])
-def test_batch_views_match_oracle(setup, form):
+@pytest.mark.parametrize("form,graphs,wave", [
+    (G.PATH_WAVEFRONT, True, (16, 8)), (G.PATH_WAVEFRONT, False, (16, 8)), (G.PATH_WAVEFRONT, True, (8, 4)),
+    (G.PATH_WAVEFRONT, True, (32, 16)), (G.PATH_MEGAKERNEL, True, (16, 8)), (G.PATH_MEGAKERNEL, False, (16, 8))],
+    ids=["wavefront-graph", "wavefront-eager", "wavefront-small-grids", "wavefront-large-grids", "megakernel-graph",
+         "megakernel-eager"])
+def test_batch_views_match_oracle(setup, form, graphs, wave):
     ctx, hss, scenes, seqs, settings, want = setup
     ctx.set_path_form(form)
+    ctx.set_graphs(graphs)
+    ctx.set_wave_launch(*wave)
     batch = G.Batch(ctx, scenes, [(W, H) for (k, g, sp, W, H, kw) in VIEWS])
     ctx.counters(reset=True)
     keys = {"resv": G.BUF_RESERVOIR, "temp": G.BUF_TEMP, "out": G.BUF_OUTPUT, "dn": G.BUF_DEPTH_NORMAL,
@@ -57,6 +63,33 @@ def test_batch_views_match_oracle(setup, form):
     assert ctx.counters()[3] == 0
     batch.close()
     ctx.set_path_form(G.PATH_WAVEFRONT)
+    ctx.set_graphs(True)
+    ctx.set_wave_launch(16, 8)
+
+
+def test_autotune_picks_a_candidate_and_results_stay_exact(setup):
+    """The autotuner renders frames with every candidate configuration and keeps the fastest;
+    a fresh batch rendered with the chosen configuration still matches the oracle."""
+    ctx, hss, scenes, seqs, settings, want = setup
+    sizes = [(W, H) for (k, g, sp, W, H, kw) in VIEWS]
+    n = len(VIEWS)
+    tb = G.Batch(ctx, scenes, sizes)
+    r = tb.autotune([seqs[v][0][1] for v in range(n)], [seqs[v][1][1] for v in range(n)], settings, frames=2)
+    tb.close()
+    assert r.candidates == 10
+    ms = list(r.candidateMs)[:r.candidates]
+    assert all(m > 0 for m in ms)
+    assert r.msPerFrame == min(ms)
+    assert r.pathForm in (G.PATH_MEGAKERNEL, G.PATH_WAVEFRONT)
+    batch = G.Batch(ctx, scenes, sizes)
+    for f in range(FRAMES):
+        batch.render([seqs[v][0][f] for v in range(n)], [seqs[v][1][f] for v in range(n)], settings)
+        for v in range(n):
+            assert batch.download(v, G.BUF_RESERVOIR).tobytes() == want[v][f]["resv"].tobytes()
+            assert batch.download(v, G.BUF_OUTPUT).tobytes() == want[v][f]["out"].tobytes()
+    batch.close()
+    ctx.set_path_form(G.PATH_WAVEFRONT)
+    ctx.set_wave_launch(16, 8)
 
 
 def test_single_view_batch_equals_frame_api(setup):
@@ -71,3 +104,32 @@ def test_single_view_batch_equals_frame_api(setup):
         assert batch.download(0, G.BUF_OUTPUT).tobytes() == fr.download(G.BUF_OUTPUT).tobytes()
     fr.close()
     batch.close()
+
+
+def test_batched_workload_views_match_oracle():
+    """Views drawn by the batched-views workload generator (box-with-spheres and terrain scenes of
+    10k-200k triangles, uneven depths), at small resolutions, through graphs and the wavefront."""
+    from grisrt import workloads
+    specs = workloads.batched_views(5, seed=11, resolutions=(16, 24, 40))
+    ctx = G.Context(0)
+    ctx.set_path_form(G.PATH_WAVEFRONT)
+    hss = [G.HostScene(s["kind"], seed=s["seed"], grid=s["grid"], spheres=s["spheres"]) for s in specs]
+    assert {s["kind"] for s in specs} == {1, 3}
+    scenes = [G.Scene(ctx, hs) for hs in hss]
+    sets = [G.Settings.make(maxDepth=s["maxDepth"], spatialRadius=20.0) for s in specs]
+    seqs = [G.sequence_cameras(hs, 2, s["width"], s["height"], seed=60 + i) for i, (hs, s) in enumerate(zip(hss, specs))]
+    ora = O.oracle()
+    batch = G.Batch(ctx, scenes, [(s["width"], s["height"]) for s in specs])
+    want = []
+    for i, s in enumerate(specs):
+        ora.set_scene(hss[i])
+        want.append(O.run_sequence(ora, seqs[i][0], seqs[i][1], sets[i], s["width"], s["height"], record=("resv", "out")))
+    for f in range(2):
+        batch.render([q[0][f] for q in seqs], [q[1][f] for q in seqs], sets)
+        for v in range(len(specs)):
+            assert batch.download(v, G.BUF_RESERVOIR).tobytes() == want[v][f]["resv"].tobytes(), (f, v)
+            assert batch.download(v, G.BUF_OUTPUT).tobytes() == want[v][f]["out"].tobytes(), (f, v)
+    batch.close()
+    for sc in scenes:
+        sc.close()
+    ctx.close()

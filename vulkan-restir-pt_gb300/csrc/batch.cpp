@@ -38,7 +38,20 @@ struct GrisBatch {
     cudaEvent_t staged[2] = {nullptr, nullptr};
     int stage = 0;
     int next = 0;
+    /* captured frames, one per staging slot, valid for one frame shape */
+    struct Graph {
+        cudaGraphExec_t exec = nullptr;
+        int pathForm = -1, maxDepth = -1, trace = 0, shade = 0, countWork = -1;
+        uint32_t pixels = 0, tiles = 0;
+    } graph[2];
 };
+
+static void drop_graphs(GrisBatch* b) {
+    for (auto& g : b->graph) {
+        if (g.exec) cudaGraphExecDestroy(g.exec);
+        g = GrisBatch::Graph();
+    }
+}
 
 using namespace grisrt;
 
@@ -114,6 +127,7 @@ int grisBatchDestroy(GrisBatch* b) {
     if (!b) return GRIS_ERR_INVALID_ARGUMENT;
     cudaSetDevice(ctx_device(b->ctx));
     cudaStreamSynchronize(ctx_stream(b->ctx));
+    drop_graphs(b);
     for (void* p : b->allocations) cudaFree(p);
     for (int i = 0; i < 2; i++) {
         if (b->hViews[i]) cudaFreeHost(b->hViews[i]);
@@ -150,11 +164,37 @@ int grisBatchRender(GrisContext* ctx, GrisBatch* b, const GrisCamera* cams, cons
         v.cam = cams[i]; v.prev = prevCams[i]; v.set = settings[i];
     }
     int k = b->stage;
+    cudaStream_t st = ctx_stream(ctx);
     cudaError_t e = cudaEventSynchronize(b->staged[k]);   /* the staging slot's previous copy is done */
-    if (e == cudaSuccess)
-        e = launch_batch(views.data(), (int)b->n, b->dViews, b->hViews[k], b->wave, ctx_counters(ctx), ctx_count_work(ctx),
-                         ctx_timer(ctx), ctx_stream(ctx), ctx_path_form(ctx), 15);
-    if (e == cudaSuccess) e = cudaEventRecord(b->staged[k], ctx_stream(ctx));
+    if (e != cudaSuccess) return ctx_fail(ctx, GRIS_ERR_CUDA, std::string("grisBatchRender: ") + cudaGetErrorString(e));
+    BatchShape sh = fill_view_table(views.data(), (int)b->n, b->hViews[k], ctx_counters(ctx), ctx_count_work(ctx));
+    int form = ctx_path_form(ctx);
+    WaveLaunch wl = ctx_wave_launch(ctx);
+    if (ctx_graphs(ctx)) {
+        GrisBatch::Graph& g = b->graph[k];
+        if (!g.exec || g.pathForm != form || g.maxDepth != sh.maxDepth || g.pixels != sh.pixels || g.tiles != sh.tiles ||
+            g.trace != wl.traceBlocksPerSM || g.shade != wl.shadeBlocksPerSM || g.countWork != ctx_count_work(ctx)) {
+            if (g.exec) { cudaGraphExecDestroy(g.exec); g.exec = nullptr; }
+            cudaGraph_t graph = nullptr;
+            e = cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal);
+            if (e == cudaSuccess) {
+                cudaError_t ee = enqueue_batch(sh, b->dViews, b->hViews[k], b->wave, ctx_counters(ctx), ctx_count_work(ctx),
+                                               nullptr, st, form, 15, wl);
+                e = cudaStreamEndCapture(st, &graph);
+                if (e == cudaSuccess) e = ee;
+            }
+            if (e == cudaSuccess) e = cudaGraphInstantiate(&g.exec, graph, 0);
+            if (graph) cudaGraphDestroy(graph);
+            if (e != cudaSuccess) return ctx_fail(ctx, GRIS_ERR_CUDA, std::string("graph capture: ") + cudaGetErrorString(e));
+            g.pathForm = form; g.maxDepth = sh.maxDepth; g.pixels = sh.pixels; g.tiles = sh.tiles;
+            g.trace = wl.traceBlocksPerSM; g.shade = wl.shadeBlocksPerSM; g.countWork = ctx_count_work(ctx);
+        }
+        e = cudaGraphLaunch(g.exec, st);
+    } else {
+        e = enqueue_batch(sh, b->dViews, b->hViews[k], b->wave, ctx_counters(ctx), ctx_count_work(ctx), ctx_timer(ctx), st,
+                          form, 15, wl);
+    }
+    if (e == cudaSuccess) e = cudaEventRecord(b->staged[k], st);
     if (e != cudaSuccess) return ctx_fail(ctx, GRIS_ERR_CUDA, std::string("grisBatchRender: ") + cudaGetErrorString(e));
     b->stage ^= 1;
     b->next ^= 1;
@@ -179,6 +219,54 @@ int grisBatchGetBuffer(const GrisBatch* b, uint32_t view, int which, int slot, v
     }
     *devPtr = p;
     if (bytes) *bytes = sz;
+    return GRIS_OK;
+}
+
+int grisBatchAutotune(GrisContext* ctx, GrisBatch* b, const GrisCamera* cams, const GrisCamera* prevCams,
+                      const GrisSettings* settings, int frames, GrisTuneResult* out) {
+    if (!ctx || !b || !out || frames < 1) return ctx_fail(ctx, GRIS_ERR_INVALID_ARGUMENT, "bad autotune request");
+    cudaSetDevice(ctx_device(ctx));
+    struct Cand { int form, trace, shade; };
+    std::vector<Cand> cands = {{GRIS_PATH_MEGAKERNEL, 16, 8}};
+    for (int t : {8, 16, 32})
+        for (int sh : {4, 8, 16}) cands.push_back({GRIS_PATH_WAVEFRONT, t, sh});
+    memset(out, 0, sizeof(*out));
+    cudaStream_t st = ctx_stream(ctx);
+    cudaEvent_t e0, e1;
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    int savedForm = ctx_path_form(ctx);
+    WaveLaunch savedWl = ctx_wave_launch(ctx);
+    double best = 1e30;
+    int bestI = 0;
+    int rc = GRIS_OK;
+    for (size_t i = 0; i < cands.size() && i < 16 && rc == GRIS_OK; i++) {
+        WaveLaunch wl;
+        wl.traceBlocksPerSM = cands[i].trace;
+        wl.shadeBlocksPerSM = cands[i].shade;
+        ctx_set_tuning(ctx, cands[i].form, wl);
+        rc = grisBatchRender(ctx, b, cams, prevCams, settings);   /* warm-up (and graph capture) */
+        cudaEventRecord(e0, st);
+        for (int f = 0; f < frames && rc == GRIS_OK; f++) rc = grisBatchRender(ctx, b, cams, prevCams, settings);
+        cudaEventRecord(e1, st);
+        cudaEventSynchronize(e1);
+        float ms = 0.0f;
+        cudaEventElapsedTime(&ms, e0, e1);
+        out->candidateMs[i] = ms / frames;
+        out->candidates = (int)i + 1;
+        if (ms / frames < best) { best = ms / frames; bestI = (int)i; }
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    if (rc != GRIS_OK) { ctx_set_tuning(ctx, savedForm, savedWl); return rc; }
+    WaveLaunch wl;
+    wl.traceBlocksPerSM = cands[bestI].trace;
+    wl.shadeBlocksPerSM = cands[bestI].shade;
+    ctx_set_tuning(ctx, cands[bestI].form, wl);
+    out->pathForm = cands[bestI].form;
+    out->traceBlocksPerSM = wl.traceBlocksPerSM;
+    out->shadeBlocksPerSM = wl.shadeBlocksPerSM;
+    out->msPerFrame = best;
     return GRIS_OK;
 }
 

@@ -29,14 +29,15 @@ static_assert(sizeof(GrisSettings) == 64, "GrisSettings is 64 B");
 /* Per-kernel CUDA-event timing of every launch while enabled (events recorded on the
  * launch stream around each kernel; read back and summed on request). */
 struct Profiler : grisrt::KernelTimer {
+    static const int kSlots = GRIS_PROFILE_SLOTS;
     bool enabled = false;
     struct Pair { cudaEvent_t a, b; int kernel; };
     std::vector<Pair> pending, free;
-    double ms[4] = {0, 0, 0, 0};
-    uint64_t launches[4] = {0, 0, 0, 0};
-    Pair open{};
+    double ms[kSlots] = {};
+    uint64_t launches[kSlots] = {};
+    Pair open[kSlots] = {};   /* slots nest (the wavefront stages inside the path-trace span) */
     void mark(int kernel, bool begin, cudaStream_t stream) override {
-        if (!enabled) return;
+        if (!enabled || kernel < 0 || kernel >= kSlots) return;
         if (begin) {
             if (free.empty()) {
                 Pair p{};
@@ -44,13 +45,13 @@ struct Profiler : grisrt::KernelTimer {
                 cudaEventCreate(&p.b);
                 free.push_back(p);
             }
-            open = free.back();
+            open[kernel] = free.back();
             free.pop_back();
-            open.kernel = kernel;
-            cudaEventRecord(open.a, stream);
+            open[kernel].kernel = kernel;
+            cudaEventRecord(open[kernel].a, stream);
         } else {
-            cudaEventRecord(open.b, stream);
-            pending.push_back(open);
+            cudaEventRecord(open[kernel].b, stream);
+            pending.push_back(open[kernel]);
         }
     }
     void collect() {
@@ -63,6 +64,9 @@ struct Profiler : grisrt::KernelTimer {
             free.push_back(p);
         }
         pending.clear();
+    }
+    void reset() {
+        for (int k = 0; k < kSlots; k++) { ms[k] = 0.0; launches[k] = 0; }
     }
     ~Profiler() override {
         for (Pair& p : pending) { cudaEventDestroy(p.a); cudaEventDestroy(p.b); }
@@ -102,6 +106,8 @@ struct GrisContext {
     int countWork = 0;
     int launchMode = GRIS_LAUNCH_GRID;
     int pathForm = GRIS_PATH_WAVEFRONT;
+    int useGraphs = 1;
+    grisrt::WaveLaunch waveLaunch;
     Profiler prof;
     std::string err;
 };
@@ -164,6 +170,9 @@ int grisrt::ctx_count_work(GrisContext* ctx) { return ctx->countWork; }
 int grisrt::ctx_path_form(GrisContext* ctx) { return ctx->pathForm; }
 grisrt::KernelTimer* grisrt::ctx_timer(GrisContext* ctx) { return &ctx->prof; }
 int grisrt::ctx_fail(GrisContext* ctx, int code, const std::string& msg) { return fail(ctx, code, msg); }
+bool grisrt::ctx_graphs(GrisContext* ctx) { return ctx->useGraphs && !ctx->prof.enabled; }
+grisrt::WaveLaunch grisrt::ctx_wave_launch(GrisContext* ctx) { return ctx->waveLaunch; }
+void grisrt::ctx_set_tuning(GrisContext* ctx, int pathForm, grisrt::WaveLaunch wl) { ctx->pathForm = pathForm; ctx->waveLaunch = wl; }
 
 bool grisrt::scene_device(const GrisScene* s, grisrt::DeviceSceneView* view, int* device) {
     if (!s || !s->ctx) return false;
@@ -249,14 +258,52 @@ int grisReadProfile(GrisContext* ctx, double msTotal[4], uint64_t launches[4], i
     for (int k = 0; k < 4; k++) {
         msTotal[k] = ctx->prof.ms[k];
         launches[k] = ctx->prof.launches[k];
-        if (reset) { ctx->prof.ms[k] = 0.0; ctx->prof.launches[k] = 0; }
     }
+    if (reset) ctx->prof.reset();
+    return GRIS_OK;
+}
+
+int grisReadKernelProfile(GrisContext* ctx, GrisKernelProfile out[GRIS_PROFILE_SLOTS], int reset) {
+    if (!ctx || !out) return GRIS_ERR_INVALID_ARGUMENT;
+    cudaSetDevice(ctx->device);
+    ctx->prof.collect();
+    GRIS_CK(ctx, cudaMemcpyAsync(ctx->hCounters + 8, ctx->dCounters + 8, 18 * sizeof(unsigned long long),
+                                 cudaMemcpyDeviceToHost, ctx->stream));
+    if (reset) GRIS_CK(ctx, cudaMemsetAsync(ctx->dCounters + 8, 0, 18 * sizeof(unsigned long long), ctx->stream));
+    GRIS_CK(ctx, cudaStreamSynchronize(ctx->stream));
+    const unsigned long long* c = ctx->hCounters;
+    for (int k = 0; k < GRIS_PROFILE_SLOTS; k++) {
+        GrisKernelProfile& o = out[k];
+        o.ms = ctx->prof.ms[k];
+        o.launches = ctx->prof.launches[k];
+        o.nodes = o.tris = o.rays = 0;
+        if (k < 4) { o.nodes = c[8 + 2 * k]; o.tris = c[9 + 2 * k]; o.rays = c[16 + k]; }
+        if (k == GRIS_SLOT_WAVE_EXTEND || k == GRIS_SLOT_WAVE_SHADOW) {
+            int s = k == GRIS_SLOT_WAVE_EXTEND ? 0 : 1;
+            o.nodes = c[20 + 3 * s]; o.tris = c[21 + 3 * s]; o.rays = c[22 + 3 * s];
+        }
+    }
+    if (reset) ctx->prof.reset();
     return GRIS_OK;
 }
 
 int grisSetLaunchMode(GrisContext* ctx, int mode) {
     if (!ctx || (mode != GRIS_LAUNCH_GRID && mode != GRIS_LAUNCH_PERSISTENT)) return GRIS_ERR_INVALID_ARGUMENT;
     ctx->launchMode = mode;
+    return GRIS_OK;
+}
+
+int grisSetGraphs(GrisContext* ctx, int enable) {
+    if (!ctx) return GRIS_ERR_INVALID_ARGUMENT;
+    ctx->useGraphs = enable != 0;
+    return GRIS_OK;
+}
+
+int grisSetWaveLaunch(GrisContext* ctx, int traceBlocksPerSM, int shadeBlocksPerSM) {
+    if (!ctx || traceBlocksPerSM < 1 || traceBlocksPerSM > 64 || shadeBlocksPerSM < 1 || shadeBlocksPerSM > 64)
+        return GRIS_ERR_INVALID_ARGUMENT;
+    ctx->waveLaunch.traceBlocksPerSM = traceBlocksPerSM;
+    ctx->waveLaunch.shadeBlocksPerSM = shadeBlocksPerSM;
     return GRIS_OK;
 }
 
@@ -277,7 +324,7 @@ int grisReadWorkCounters(GrisContext* ctx, uint64_t nodes[4], uint64_t tris[4], 
     cudaSetDevice(ctx->device);
     GRIS_CK(ctx, cudaMemcpyAsync(ctx->hCounters + 8, ctx->dCounters + 8, 16 * sizeof(unsigned long long),
                                  cudaMemcpyDeviceToHost, ctx->stream));
-    if (reset) GRIS_CK(ctx, cudaMemsetAsync(ctx->dCounters + 8, 0, 16 * sizeof(unsigned long long), ctx->stream));
+    if (reset) GRIS_CK(ctx, cudaMemsetAsync(ctx->dCounters + 8, 0, 18 * sizeof(unsigned long long), ctx->stream));
     GRIS_CK(ctx, cudaStreamSynchronize(ctx->stream));
     for (int k = 0; k < 4; k++) {
         nodes[k] = ctx->hCounters[8 + 2 * k];
@@ -467,7 +514,7 @@ int grisPassRender(GrisContext* ctx, const GrisScene* s, const GrisPassBindings*
         int k = w.stage;
         GRIS_CK(ctx, cudaEventSynchronize(w.staged[k]));
         GRIS_CK(ctx, grisrt::launch_batch(&v, 1, w.dViews, w.hViews[k], w.wb, ctx->dCounters, ctx->countWork, &ctx->prof,
-                                          ctx->stream, GRIS_PATH_WAVEFRONT, passes & 7));
+                                          ctx->stream, GRIS_PATH_WAVEFRONT, passes & 7, ctx->waveLaunch));
         GRIS_CK(ctx, cudaEventRecord(w.staged[k], ctx->stream));
         w.stage ^= 1;
         return GRIS_OK;

@@ -62,8 +62,11 @@ GD bool traceVisibility(const DevScene& sc, V3 from, V3 to, RayCount& rc, int& e
 
 /* counters: [0] closest, [1] shadow, [2] primary, [3] error word,
  * [8+2k] nodes and [9+2k] triangles of kernel k, [16+k] closest-hit rays of kernel k
- * (k: 0 G-buffer, 1 path trace, 2 temporal, 3 spatial). */
-GD void flush_counts(unsigned long long* counters, const RayCount& rc, int err, int kernel, int countWork) {
+ * (k: 0 G-buffer, 1 path trace, 2 temporal, 3 spatial); the wavefront's traversal stages also
+ * count on their own: [20+3s] nodes, [21+3s] triangles, [22+3s] rays (closest for s = 0, the
+ * extension stage; shadow for s = 1, the shadow stage). */
+GD void flush_counts(unsigned long long* counters, const RayCount& rc, int err, int kernel, int countWork,
+                     int stage = -1) {
     unsigned int c = __reduce_add_sync(0xffffffffu, rc.closest);
     unsigned int s = __reduce_add_sync(0xffffffffu, rc.shadow);
     unsigned int e = __reduce_or_sync(0xffffffffu, (unsigned)err);
@@ -80,6 +83,11 @@ GD void flush_counts(unsigned long long* counters, const RayCount& rc, int err, 
             atomicAdd(counters + 8 + 2 * kernel, nodes);
             atomicAdd(counters + 9 + 2 * kernel, tris);
             atomicAdd(counters + 16 + kernel, (unsigned long long)c);
+            if (stage >= 0) {
+                atomicAdd(counters + 20 + 3 * stage, nodes);
+                atomicAdd(counters + 21 + 3 * stage, tris);
+                atomicAdd(counters + 22 + 3 * stage, (unsigned long long)(stage == 0 ? c : s));
+            }
         }
     }
 }
@@ -1157,7 +1165,7 @@ __global__ void __launch_bounds__(128) k_wave_extend(WaveCtx C, int level) {
             C.hit[id] = traceClosestHit(C.V[v].P.sc, o, d, kMinRayDistance, kMaxRayDistance, rc, err);
         }
     }
-    flush_counts(C.counters, rc, err, 1, C.countWork);
+    flush_counts(C.counters, rc, err, 1, C.countWork, 0);
 }
 
 /* shade() of the level's paths: the end, the next level, or a shadow query */
@@ -1208,7 +1216,7 @@ __global__ void __launch_bounds__(128) k_wave_shadow(WaveCtx C, int level) {
             C.blocked[id] = traceShadow(C.V[v].P.sc, o, kMinRayDistance, d, dist - kMinRayDistance, rc, err) ? 1 : 0;
         }
     }
-    flush_counts(C.counters, rc, err, 1, C.countWork);
+    flush_counts(C.counters, rc, err, 1, C.countWork, 1);
 }
 
 /* post() of the paths that made a shadow query */
@@ -1237,13 +1245,10 @@ __global__ void __launch_bounds__(128) k_wave_post(WaveCtx C, int level) {
 
 size_t wave_bytes_per_path() { return sizeof(WaveRec) + sizeof(NeeRec) + sizeof(Isec) + 1 + 3 * sizeof(uint32_t); }
 
-cudaError_t launch_batch(const BatchView* views, int n, void* dViews, void* hViews, const WaveBuffers& wb,
-                         unsigned long long* counters, int countWork, KernelTimer* timer, cudaStream_t stream,
-                         int pathForm, int passes) {
-    if (n <= 0 || n > 4096) return cudaErrorInvalidValue;
+BatchShape fill_view_table(const BatchView* views, int n, void* hViews, unsigned long long* counters, int countWork) {
+    BatchShape sh;
+    sh.n = n; sh.tiles = 0; sh.pixels = 0; sh.maxDepth = 0;
     ViewEntry* H = reinterpret_cast<ViewEntry*>(hViews);
-    uint32_t tiles = 0, pixels = 0;
-    int maxDepth = 0;
     for (int i = 0; i < n; i++) {
         const BatchView& bv = views[i];
         ViewEntry& e = H[i];
@@ -1262,16 +1267,25 @@ cudaError_t launch_batch(const BatchView* views, int n, void* dViews, void* hVie
         e.G.counters = counters;
         e.G.countWork = countWork;
         e.tilesX = (bv.b.width + 15) / 16;
-        e.tileBase = tiles;
-        e.pixelBase = pixels;
-        tiles += e.tilesX * ((bv.b.height + 7) / 8);
-        pixels += bv.b.width * bv.b.height;
-        if ((int)bv.set.maxDepth > maxDepth) maxDepth = (int)bv.set.maxDepth;
+        e.tileBase = sh.tiles;
+        e.pixelBase = sh.pixels;
+        sh.tiles += e.tilesX * ((bv.b.height + 7) / 8);
+        sh.pixels += bv.b.width * bv.b.height;
+        if ((int)bv.set.maxDepth > sh.maxDepth) sh.maxDepth = (int)bv.set.maxDepth;
     }
-    if ((uint64_t)pixels > wb.capacity) return cudaErrorInvalidValue;
+    return sh;
+}
+
+cudaError_t enqueue_batch(const BatchShape& sh, void* dViews, const void* hViews, const WaveBuffers& wb,
+                          unsigned long long* counters, int countWork, KernelTimer* timer, cudaStream_t stream,
+                          int pathForm, int passes, const WaveLaunch& wl) {
+    const int n = sh.n;
+    if (n <= 0 || n > 4096) return cudaErrorInvalidValue;
+    if ((uint64_t)sh.pixels > wb.capacity && pathForm == GRIS_PATH_WAVEFRONT && (passes & 1)) return cudaErrorInvalidValue;
     cudaError_t e = cudaMemcpyAsync(dViews, hViews, sizeof(ViewEntry) * (size_t)n, cudaMemcpyHostToDevice, stream);
     if (e != cudaSuccess) return e;
     const ViewEntry* V = reinterpret_cast<const ViewEntry*>(dViews);
+    const uint32_t tiles = sh.tiles, pixels = sh.pixels;
     dim3 blk(16, 8);
     if (passes & 8) {
         if (timer) timer->mark(0, true, stream);
@@ -1296,13 +1310,26 @@ cudaError_t launch_batch(const BatchView* views, int n, void* dViews, void* hVie
             if (e != cudaSuccess) return e;
             static int sm = 0;
             if (sm == 0) { int dev = 0; cudaGetDevice(&dev); cudaDeviceGetAttribute(&sm, cudaDevAttrMultiProcessorCount, dev); }
-            const int gridShade = sm * 8, gridTrace = sm * 16;
+            const int gridShade = sm * (wl.shadeBlocksPerSM > 0 ? wl.shadeBlocksPerSM : 8);
+            const int gridTrace = sm * (wl.traceBlocksPerSM > 0 ? wl.traceBlocksPerSM : 16);
+            /* timer slots 4..8: begin, extend, shade, shadow, post */
+            auto mark = [&](int slot, bool begin) { if (timer) timer->mark(slot, begin, stream); };
+            mark(4, true);
             k_wave_begin<<<(pixels + 127) / 128, 128, 0, stream>>>(C);
-            for (int level = 1; level < maxDepth; level++) {
+            mark(4, false);
+            for (int level = 1; level < sh.maxDepth; level++) {
+                mark(5, true);
                 k_wave_extend<<<gridTrace, 128, 0, stream>>>(C, level);
+                mark(5, false);
+                mark(6, true);
                 k_wave_shade<<<gridShade, 128, 0, stream>>>(C, level);
+                mark(6, false);
+                mark(7, true);
                 k_wave_shadow<<<gridTrace, 128, 0, stream>>>(C, level);
+                mark(7, false);
+                mark(8, true);
                 k_wave_post<<<gridShade, 128, 0, stream>>>(C, level);
+                mark(8, false);
             }
         } else {
             k_batch_pass<PathTask, 1><<<tiles, blk, 0, stream>>>(V, n);
@@ -1320,6 +1347,14 @@ cudaError_t launch_batch(const BatchView* views, int n, void* dViews, void* hVie
         if (timer) timer->mark(3, false, stream);
     }
     return cudaGetLastError();
+}
+
+cudaError_t launch_batch(const BatchView* views, int n, void* dViews, void* hViews, const WaveBuffers& wb,
+                         unsigned long long* counters, int countWork, KernelTimer* timer, cudaStream_t stream,
+                         int pathForm, int passes, const WaveLaunch& wl) {
+    if (n <= 0 || n > 4096) return cudaErrorInvalidValue;
+    BatchShape sh = fill_view_table(views, n, hViews, counters, countWork);
+    return enqueue_batch(sh, dViews, hViews, wb, counters, countWork, timer, stream, pathForm, passes, wl);
 }
 
 }  // namespace grisrt

@@ -60,11 +60,29 @@ struct WaveBuffers {
 size_t wave_bytes_per_path();
 size_t view_entry_bytes();
 
-/* passes: bit 3 G-buffer, bit 0 path trace, bit 1 temporal, bit 2 spatial. pathForm:
- * GRIS_PATH_MEGAKERNEL or GRIS_PATH_WAVEFRONT. hViews: pinned staging for the view table. */
+/* Grid sizes of the wavefront kernels, in blocks of 128 threads per SM. */
+struct WaveLaunch {
+    int traceBlocksPerSM = 16;
+    int shadeBlocksPerSM = 8;
+};
+
+struct BatchShape {
+    int n;
+    uint32_t tiles, pixels;
+    int maxDepth;
+};
+
+/* Writes the view table of a frame into hViews (pinned host memory). */
+BatchShape fill_view_table(const BatchView* views, int n, void* hViews, unsigned long long* counters, int countWork);
+/* Enqueues one batch frame: copy of the view table, then the kernels. passes: bit 3 G-buffer,
+ * bit 0 path trace, bit 1 temporal, bit 2 spatial. pathForm: GRIS_PATH_MEGAKERNEL or
+ * GRIS_PATH_WAVEFRONT. Only stream operations: it can be captured into a CUDA graph. */
+cudaError_t enqueue_batch(const BatchShape& sh, void* dViews, const void* hViews, const WaveBuffers& wb,
+                          unsigned long long* counters, int countWork, KernelTimer* timer, cudaStream_t stream,
+                          int pathForm, int passes, const WaveLaunch& wl);
 cudaError_t launch_batch(const BatchView* views, int n, void* dViews, void* hViews, const WaveBuffers& wb,
                          unsigned long long* counters, int countWork, KernelTimer* timer, cudaStream_t stream,
-                         int pathForm, int passes);
+                         int pathForm, int passes, const WaveLaunch& wl);
 
 cudaError_t launch_debug_trace(const uint32_t* nodes, const float* tris, const float* rays, uint64_t n, int anyHit,
                                float* hitTUV, uint32_t* hitInst, uint32_t* hitTri, unsigned long long* counters,

@@ -40,6 +40,10 @@ int ctx_count_work(GrisContext* ctx);
 int ctx_path_form(GrisContext* ctx);
 KernelTimer* ctx_timer(GrisContext* ctx);
 int ctx_fail(GrisContext* ctx, int code, const std::string& msg);
+struct WaveLaunch;
+bool ctx_graphs(GrisContext* ctx);            /* graphs enabled and per-kernel profiling off */
+WaveLaunch ctx_wave_launch(GrisContext* ctx);
+void ctx_set_tuning(GrisContext* ctx, int pathForm, WaveLaunch wl);
 /* Device view and device ordinal of an uploaded scene; false for a host-only scene. */
 bool scene_device(const GrisScene* s, DeviceSceneView* view, int* device);
 

@@ -387,6 +387,43 @@ void icosphere(int level, std::vector<H3>& V, std::vector<uint32_t>& F) {
     }
 }
 
+/* kind 3: the box room of kind 0 furnished with `spheres` instanced level-2 icospheres (320
+ * triangles each) resting at random places inside it, Lambertian or GGX. */
+void build_box_spheres(GrisHostScene& s, uint32_t spheres) {
+    build_box(s);
+    Rng rng{s.seed * 0x9e3779b97f4a7c15ull + 3};
+    std::vector<H3> SV; std::vector<uint32_t> SF;
+    icosphere(2, SV, SF);
+    uint32_t sBase = (uint32_t)s.vertices.size();
+    for (H3 p : SV) {
+        GrisMeshVertex v;
+        v.pos[0] = p.x; v.pos[1] = p.y; v.pos[2] = p.z;
+        v.norm[0] = p.x; v.norm[1] = p.y; v.norm[2] = p.z;
+        v.uvx = 0.0f; v.uvy = 0.0f;
+        s.vertices.push_back(v);
+    }
+    for (uint32_t k = 0; k < spheres; k++) {
+        float radius = 0.02f + 0.1f * rng.uniform();
+        float px = -0.9f + 1.8f * rng.uniform();
+        float py = -0.9f + 1.8f * rng.uniform();
+        float pz = -1.0f + radius + 1.4f * rng.uniform();
+        float cr = 0.2f + 0.75f * rng.uniform();
+        float cg = 0.2f + 0.75f * rng.uniform();
+        float cb = 0.2f + 0.75f * rng.uniform();
+        float rough = 0.05f + 0.95f * rng.uniform();
+        float metal = rng.uniform() < 0.3f ? 1.0f : 0.0f;
+        uint32_t type = rng.uniform() < 0.5f ? 1u : 2u;
+        uint32_t mat = (uint32_t)s.materials.size();
+        s.materials.push_back(make_material(type, h3(cr, cg, cb), metal, rough));
+        uint32_t off = (uint32_t)s.indices.size();
+        for (uint32_t f : SF) s.indices.push_back(sBase + f);
+        for (size_t f = 0; f < SF.size() / 3; f++) s.materialIndices.push_back((int32_t)mat);
+        s.instances.emplace_back();
+        float rot = 6.2831853f * rng.uniform();
+        set_instance(s.instances.back(), m4_translate_scale_rotz(h3(px, py, pz), radius, rot), off, (uint32_t)SF.size(), mat);
+    }
+}
+
 /* kind 1 / 2: heightfield + instanced icospheres + 4 quad lights. */
 void build_terrain(GrisHostScene& s, uint32_t gridN, uint32_t spheres, bool glossy) {
     Rng rng{s.seed * 0x9e3779b97f4a7c15ull + 7};
@@ -490,10 +527,11 @@ void build_terrain(GrisHostScene& s, uint32_t gridN, uint32_t spheres, bool glos
 }  // namespace
 
 extern "C" int grisHostSceneCreate(int kind, uint64_t seed, uint32_t gridN, uint32_t spheres, GrisHostScene** out) {
-    if (!out || kind < 0 || kind > 2) return GRIS_ERR_INVALID_ARGUMENT;
+    if (!out || kind < 0 || kind > 3) return GRIS_ERR_INVALID_ARGUMENT;
     GrisHostScene* s = new GrisHostScene();
     s->kind = kind; s->seed = seed;
     if (kind == 0) build_box(*s);
+    else if (kind == 3) build_box_spheres(*s, spheres);
     else build_terrain(*s, gridN ? gridN : 512, spheres, kind == 2);
     *out = s;
     return GRIS_OK;

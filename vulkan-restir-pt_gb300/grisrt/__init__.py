@@ -105,6 +105,20 @@ class SceneStats(ctypes.Structure):
                 ("buildSeconds", ctypes.c_double)]
 
 
+class KernelProfile(ctypes.Structure):
+    _fields_ = [("ms", ctypes.c_double), ("launches", ctypes.c_uint64), ("nodes", ctypes.c_uint64),
+                ("tris", ctypes.c_uint64), ("rays", ctypes.c_uint64)]
+
+
+PROFILE_SLOTS = ["gbuffer", "path_trace", "temporal", "spatial", "wave_begin", "wave_extend", "wave_shade",
+                 "wave_shadow", "wave_post"]
+
+
+class TuneResult(ctypes.Structure):
+    _fields_ = [("pathForm", ctypes.c_int), ("traceBlocksPerSM", ctypes.c_int), ("shadeBlocksPerSM", ctypes.c_int),
+                ("candidates", ctypes.c_int), ("msPerFrame", ctypes.c_double), ("candidateMs", ctypes.c_double * 16)]
+
+
 EXPORTS = [
     "grisCreate", "grisDestroy", "grisGetError", "grisSync", "grisGetStream", "grisReadCounters", "grisGetVersion",
     "grisSetProfiling", "grisReadProfile", "grisSetWorkCounting", "grisReadWorkCounters", "grisSetLaunchMode",
@@ -113,7 +127,8 @@ EXPORTS = [
     "grisSceneGetStats", "grisDebugHostSceneCreate", "grisDebugTraceHost", "grisDebugTraceDevice", "grisPassGBuffer", "grisPassRender", "grisPassRenderNoAlloc",
     "grisFrameCreate", "grisFrameDestroy", "grisFrameRender", "grisFrameGetBuffer", "grisFrameDownload",
     "grisFrameUpload", "grisSetPathForm", "grisBatchCreate", "grisBatchDestroy", "grisBatchRender", "grisBatchGetBuffer",
-    "grisBatchDownload",
+    "grisBatchDownload", "grisSetGraphs", "grisSetWaveLaunch", "grisBatchAutotune",
+    "grisReadKernelProfile",
 ]
 
 _lib = None
@@ -173,6 +188,11 @@ def load(path=None):
         "grisBatchRender": (i32, [vp, vp, ctypes.POINTER(Camera), ctypes.POINTER(Camera), ctypes.POINTER(Settings)]),
         "grisBatchGetBuffer": (i32, [vp, u32, i32, i32, ctypes.POINTER(vp), ctypes.POINTER(ctypes.c_size_t)]),
         "grisBatchDownload": (i32, [vp, vp, u32, i32, i32, vp, ctypes.c_size_t]),
+        "grisSetGraphs": (i32, [vp, i32]),
+        "grisReadKernelProfile": (i32, [vp, ctypes.POINTER(KernelProfile), i32]),
+        "grisSetWaveLaunch": (i32, [vp, i32, i32]),
+        "grisBatchAutotune": (i32, [vp, vp, ctypes.POINTER(Camera), ctypes.POINTER(Camera), ctypes.POINTER(Settings), i32,
+                                    ctypes.POINTER(TuneResult)]),
     }
     for name, (res, args) in sig.items():
         f = getattr(lib, name)
@@ -329,6 +349,13 @@ class Context:
         self.check(load().grisReadProfile(self.h, ms, n, int(reset)), "grisReadProfile")
         return list(ms), list(n)
 
+    def kernel_profile(self, reset=False):
+        """{slot name: dict(ms, launches, nodes, tris, rays)} over PROFILE_SLOTS."""
+        out = (KernelProfile * len(PROFILE_SLOTS))()
+        self.check(load().grisReadKernelProfile(self.h, out, int(reset)), "grisReadKernelProfile")
+        return {name: dict(ms=o.ms, launches=o.launches, nodes=o.nodes, tris=o.tris, rays=o.rays)
+                for name, o in zip(PROFILE_SLOTS, out)}
+
     def set_launch_mode(self, mode):
         """0: grid (one thread per pixel, default), 1: persistent with per-lane refill."""
         self.check(load().grisSetLaunchMode(self.h, int(mode)), "grisSetLaunchMode")
@@ -336,6 +363,14 @@ class Context:
     def set_path_form(self, form):
         """0: megakernel path tracer, 1: wavefront stages with per-bounce queues (batches)."""
         self.check(load().grisSetPathForm(self.h, int(form)), "grisSetPathForm")
+
+    def set_graphs(self, enable):
+        """Batch frames replay a captured CUDA graph (default on; off while profiling)."""
+        self.check(load().grisSetGraphs(self.h, int(enable)), "grisSetGraphs")
+
+    def set_wave_launch(self, trace_blocks_per_sm, shade_blocks_per_sm):
+        self.check(load().grisSetWaveLaunch(self.h, int(trace_blocks_per_sm), int(shade_blocks_per_sm)),
+                   "grisSetWaveLaunch")
 
     def set_work_counting(self, enable):
         self.check(load().grisSetWorkCounting(self.h, int(enable)), "grisSetWorkCounting")
@@ -470,6 +505,18 @@ class Batch:
         p = (Camera * n)(*prev_cams)
         s = (Settings * n)(*settings)
         self.ctx.check(load().grisBatchRender(self.ctx.h, self.handle, c, p, s), "grisBatchRender")
+
+    def autotune(self, cams, prev_cams, settings, frames=3):
+        """Times the candidate launch configurations on these views (rendering frames), keeps the
+        fastest in the context and returns the TuneResult."""
+        n = len(self.scenes)
+        c = (Camera * n)(*cams)
+        p = (Camera * n)(*prev_cams)
+        s = (Settings * n)(*settings)
+        r = TuneResult()
+        self.ctx.check(load().grisBatchAutotune(self.ctx.h, self.handle, c, p, s, int(frames), ctypes.byref(r)),
+                       "grisBatchAutotune")
+        return r
 
     def device_ptr(self, view, which, slot=0):
         p = ctypes.c_void_p()
