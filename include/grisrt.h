@@ -249,7 +249,8 @@ int grisCameraLookAt(GrisCamera* cam, const float pos[3], const float target[3],
  * ceiling area), Lambertian walls with albedo ~ U[0.2,0.8]^3; kind 1: fBm heightfield (gridN x gridN
  * vertices) + `spheres` instanced icospheres (subdivision 2) with radii log-uniform [0.1, 2], GGX
  * MetallicWorkflow materials, 4 quad lights; kind 2: glossy variant of kind 1 (roughness U[0.02,0.3],
- * 70% metallic, occluders over the lights); kind 3: the kind 0 box furnished with `spheres`
+ * 70% metallic, the lights facing up under white Lambertian bounce panels: no direct light on the
+ * ground); kind 3: the kind 0 box furnished with `spheres`
  * instanced icospheres (320 triangles each, radii U[0.02,0.12], Lambertian or GGX). The camera for
  * frame f of the scene's orbit comes from grisHostSceneCamera. */
 int grisHostSceneCreate(int kind, uint64_t seed, uint32_t gridN, uint32_t spheres, GrisHostScene** out);
@@ -257,6 +258,34 @@ int grisHostSceneDesc(const GrisHostScene* hs, GrisSceneDesc* out);
 int grisHostSceneCamera(const GrisHostScene* hs, uint32_t frame, uint32_t frames, uint32_t width,
                         uint32_t height, GrisCamera* out);
 int grisHostSceneDestroy(GrisHostScene* hs);
+
+/* ---------------------------------------------------------------- converged image */
+/* The converged image the GRIS path converges to, for quality measurement (relMSE): per pixel,
+ * FP64 sums over independent samples of the path tracer (FP32 path arithmetic, as the GRIS
+ * passes) from the pixel's G-buffer surface. Estimator GRIS_ESTIMATOR_CANDIDATES sums the
+ * contributions the path tracer gives its reservoir stream as candidates (what ReSTIR PT's
+ * output converges to); GRIS_ESTIMATOR_INDIRECT sums every NEE and light-hit contribution
+ * (gi_naive.glsl:28-149's indirect illumination, with the GRIS path's MIS weights). Each
+ * sample is clamped as clampColor before it is added. No counterpart in the reference's GRIS
+ * pass; it replaces the reference's accumulation of many frames. */
+#define GRIS_ESTIMATOR_CANDIDATES 0
+#define GRIS_ESTIMATOR_INDIRECT 1
+typedef struct GrisConvergedBindings {
+    uint32_t width, height;
+    const float* depthNormal;     /* the G-buffer of `cam` (grisPassGBuffer) */
+    const uint32_t* albedoMatId;
+    double* sum;                  /* 3 doubles per pixel, added to */
+    double* sumSq;                /* optional (NULL): per-channel sums of squares, added to */
+} GrisConvergedBindings;
+/* Adds samples [sppBegin, sppBegin + sppCount) of every pixel (enqueued on the context stream). */
+int grisConvergedAccumulate(GrisContext* ctx, const GrisScene* scene, const GrisConvergedBindings* b,
+                            const GrisCamera* cam, const GrisSettings* settings, uint32_t sppBegin, uint32_t sppCount,
+                            int estimator);
+/* relMSE = mean over pixels and RGB of (image - ref)^2 / (ref^2 + eps) and MSE = mean of
+ * (image - ref)^2 with ref = refSum * refScale (device pointers: RGBA32F image, 3 doubles per
+ * pixel), reduced in FP64 on the device in a fixed order; waits and writes {relMSE, MSE}. */
+int grisRelMSE(GrisContext* ctx, const float* image, const double* refSum, double refScale, uint64_t pixels,
+               double eps, double out[2]);
 
 /* ---------------------------------------------------------------- scene */
 /* Copies the arrays to the device and builds the 8-wide BVH over lights (instance 0) and every

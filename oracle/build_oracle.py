@@ -13,7 +13,7 @@ import sys
 HERE = os.path.dirname(os.path.abspath(__file__))
 OUT = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT, "liboracle.so")
-SOURCES = ["gris_oracle.cpp"]
+SOURCES = ["gris_oracle.cpp", "converged_fp64.cpp"]
 
 
 def build(force=False):

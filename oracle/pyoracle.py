@@ -130,3 +130,46 @@ def run_sequence(impl, cams, prevs, settings, width, height, frames=None, record
         results.append(rec)
         j ^= 1
     return results
+
+
+class ConvergedFP64:
+    """The FP64 CPU oracle of the converged image (oracle/converged_fp64.cpp): per-pixel mean and
+    variance over `spp` independent paths of estimator 0 (the GRIS candidate sum) or 1 (the full
+    indirect illumination), from a G-buffer (dn: float32 [H*W, 4], am: uint32 [H*W, 2])."""
+
+    def __init__(self):
+        from . import build_oracle
+        self.lib = ctypes.CDLL(build_oracle.build())
+        vp, u64 = ctypes.c_void_p, ctypes.c_ulonglong
+        self.lib.fp64_scene_set.argtypes = [vp, u64] * 7
+        self.lib.fp64_scene_set.restype = ctypes.c_int
+        self.lib.fp64_render.argtypes = [vp, vp, ctypes.c_uint32, ctypes.c_uint32, vp, vp, ctypes.c_int, ctypes.c_int,
+                                         ctypes.c_int, ctypes.c_int, u64, u64, u64, ctypes.c_int, vp, vp]
+        self.lib.fp64_render.restype = None
+
+    def set_scene(self, host_scene):
+        arrs = [np.ascontiguousarray(a) for a in host_scene.arrays()]
+        args = []
+        for a in arrs:
+            args += [a.ctypes.data, len(a)]
+        n = self.lib.fp64_scene_set(*args)
+        if n < 0:
+            raise ValueError("scene not supported by the FP64 oracle (%d)" % n)
+        return n
+
+    def render(self, cam, settings, W, H, dn, am, rect=None, spp=256, seed=1, estimator=0, spp_begin=0):
+        """Returns (mean [h*w, 3], variance of one sample [h*w, 3]) over the rectangle
+        (x0, y0, x1, y1) (default: the whole frame)."""
+        x0, y0, x1, y1 = rect or (0, 0, W, H)
+        n = (x1 - x0) * (y1 - y0)
+        s = np.zeros((n, 3), np.float64)
+        q = np.zeros((n, 3), np.float64)
+        dn = np.ascontiguousarray(dn, np.float32)
+        am = np.ascontiguousarray(am, np.uint32)
+        cb = np.frombuffer(cam.tobytes(), np.uint8).copy()
+        sb = np.frombuffer(bytes(memoryview(settings)), np.uint8).copy()
+        self.lib.fp64_render(_p(cb), _p(sb), W, H, _p(dn), _p(am), x0, y0, x1, y1, spp_begin, spp, seed, estimator,
+                             _p(s), _p(q))
+        mean = s / spp
+        var = np.maximum(q / spp - mean * mean, 0.0) * spp / max(1, spp - 1)
+        return mean, var

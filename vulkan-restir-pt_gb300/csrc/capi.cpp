@@ -108,6 +108,7 @@ struct GrisContext {
     int pathForm = GRIS_PATH_WAVEFRONT;
     int useGraphs = 1;
     grisrt::WaveLaunch waveLaunch;
+    double* dReduce = nullptr;      /* relMSE partial sums (allocated on first use) */
     Profiler prof;
     std::string err;
 };
@@ -224,6 +225,7 @@ int grisDestroy(GrisContext* ctx) {
     cudaSetDevice(ctx->device);
     if (ctx->stream) cudaStreamSynchronize(ctx->stream);
     ctx->wave.release();
+    if (ctx->dReduce) cudaFree(ctx->dReduce);
     cudaFree(ctx->dCounters);
     cudaFreeHost(ctx->hCounters);
     if (ctx->stream) cudaStreamDestroy(ctx->stream);
@@ -267,9 +269,12 @@ int grisReadKernelProfile(GrisContext* ctx, GrisKernelProfile out[GRIS_PROFILE_S
     if (!ctx || !out) return GRIS_ERR_INVALID_ARGUMENT;
     cudaSetDevice(ctx->device);
     ctx->prof.collect();
-    GRIS_CK(ctx, cudaMemcpyAsync(ctx->hCounters + 8, ctx->dCounters + 8, 18 * sizeof(unsigned long long),
+    GRIS_CK(ctx, cudaMemcpyAsync(ctx->hCounters + 8, ctx->dCounters + 8, 24 * sizeof(unsigned long long),
                                  cudaMemcpyDeviceToHost, ctx->stream));
-    if (reset) GRIS_CK(ctx, cudaMemsetAsync(ctx->dCounters + 8, 0, 18 * sizeof(unsigned long long), ctx->stream));
+    if (reset) {
+        GRIS_CK(ctx, cudaMemsetAsync(ctx->dCounters + 8, 0, 16 * sizeof(unsigned long long), ctx->stream));
+        GRIS_CK(ctx, cudaMemsetAsync(ctx->dCounters + 26, 0, 6 * sizeof(unsigned long long), ctx->stream));
+    }
     GRIS_CK(ctx, cudaStreamSynchronize(ctx->stream));
     const unsigned long long* c = ctx->hCounters;
     for (int k = 0; k < GRIS_PROFILE_SLOTS; k++) {
@@ -280,7 +285,7 @@ int grisReadKernelProfile(GrisContext* ctx, GrisKernelProfile out[GRIS_PROFILE_S
         if (k < 4) { o.nodes = c[8 + 2 * k]; o.tris = c[9 + 2 * k]; o.rays = c[16 + k]; }
         if (k == GRIS_SLOT_WAVE_EXTEND || k == GRIS_SLOT_WAVE_SHADOW) {
             int s = k == GRIS_SLOT_WAVE_EXTEND ? 0 : 1;
-            o.nodes = c[20 + 3 * s]; o.tris = c[21 + 3 * s]; o.rays = c[22 + 3 * s];
+            o.nodes = c[26 + 3 * s]; o.tris = c[27 + 3 * s]; o.rays = c[28 + 3 * s];
         }
     }
     if (reset) ctx->prof.reset();
@@ -324,7 +329,10 @@ int grisReadWorkCounters(GrisContext* ctx, uint64_t nodes[4], uint64_t tris[4], 
     cudaSetDevice(ctx->device);
     GRIS_CK(ctx, cudaMemcpyAsync(ctx->hCounters + 8, ctx->dCounters + 8, 16 * sizeof(unsigned long long),
                                  cudaMemcpyDeviceToHost, ctx->stream));
-    if (reset) GRIS_CK(ctx, cudaMemsetAsync(ctx->dCounters + 8, 0, 18 * sizeof(unsigned long long), ctx->stream));
+    if (reset) {
+        GRIS_CK(ctx, cudaMemsetAsync(ctx->dCounters + 8, 0, 16 * sizeof(unsigned long long), ctx->stream));
+        GRIS_CK(ctx, cudaMemsetAsync(ctx->dCounters + 26, 0, 6 * sizeof(unsigned long long), ctx->stream));
+    }
     GRIS_CK(ctx, cudaStreamSynchronize(ctx->stream));
     for (int k = 0; k < 4; k++) {
         nodes[k] = ctx->hCounters[8 + 2 * k];
@@ -462,6 +470,39 @@ int grisPassGBuffer(GrisContext* ctx, const GrisScene* s, const GrisGBufferBindi
         return fail(ctx, GRIS_ERR_INVALID_ARGUMENT, "camera filmSize differs from the bound extent");
     cudaSetDevice(ctx->device);
     GRIS_CK(ctx, grisrt::launch_gbuffer(scene_view(s), *b, *cam, ctx->dCounters, ctx->countWork, &ctx->prof, ctx->stream));
+    return GRIS_OK;
+}
+
+int grisConvergedAccumulate(GrisContext* ctx, const GrisScene* s, const GrisConvergedBindings* b, const GrisCamera* cam,
+                            const GrisSettings* set, uint32_t sppBegin, uint32_t sppCount, int estimator) {
+    if (!ctx || !s || !b || !cam || !set) return fail(ctx, GRIS_ERR_INVALID_ARGUMENT, "null argument");
+    if (b->width == 0 || b->height == 0 || !b->depthNormal || !b->albedoMatId || !b->sum)
+        return fail(ctx, GRIS_ERR_INVALID_ARGUMENT, "converged bindings incomplete");
+    if (cam->filmSize[0] != b->width || cam->filmSize[1] != b->height)
+        return fail(ctx, GRIS_ERR_INVALID_ARGUMENT, "camera filmSize differs from the bound extent");
+    if (set->maxDepth == 0 || set->maxDepth > 255) return fail(ctx, GRIS_ERR_INVALID_ARGUMENT, "maxDepth must be 1..255");
+    if (estimator != GRIS_ESTIMATOR_CANDIDATES && estimator != GRIS_ESTIMATOR_INDIRECT)
+        return fail(ctx, GRIS_ERR_INVALID_ARGUMENT, "unknown estimator");
+    if ((uint64_t)sppBegin + sppCount > 0xffffffffull) return fail(ctx, GRIS_ERR_INVALID_ARGUMENT, "sample range overflows");
+    if (sppCount == 0) return GRIS_OK;
+    cudaSetDevice(ctx->device);
+    GRIS_CK(ctx, grisrt::launch_converged(scene_view(s), *b, *cam, *set, sppBegin, sppCount, estimator, ctx->dCounters,
+                                          ctx->stream));
+    return GRIS_OK;
+}
+
+int grisRelMSE(GrisContext* ctx, const float* image, const double* refSum, double refScale, uint64_t pixels, double eps,
+               double out[2]) {
+    if (!ctx || !image || !refSum || !out || !(eps >= 0.0)) return fail(ctx, GRIS_ERR_INVALID_ARGUMENT, "bad relMSE arguments");
+    cudaSetDevice(ctx->device);
+    if (!ctx->dReduce)
+        GRIS_CK(ctx, cudaMalloc(&ctx->dReduce, grisrt::relmse_scratch_doubles() * sizeof(double)));
+    GRIS_CK(ctx, grisrt::launch_relmse(image, refSum, refScale, pixels, eps, ctx->dReduce, ctx->stream));
+    double h[2] = {0.0, 0.0};
+    GRIS_CK(ctx, cudaMemcpyAsync(h, ctx->dReduce, sizeof(h), cudaMemcpyDeviceToHost, ctx->stream));
+    GRIS_CK(ctx, cudaStreamSynchronize(ctx->stream));
+    out[0] = h[0];
+    out[1] = h[1];
     return GRIS_OK;
 }
 

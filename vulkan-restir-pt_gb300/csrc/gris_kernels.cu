@@ -63,8 +63,9 @@ GD bool traceVisibility(const DevScene& sc, V3 from, V3 to, RayCount& rc, int& e
 /* counters: [0] closest, [1] shadow, [2] primary, [3] error word,
  * [8+2k] nodes and [9+2k] triangles of kernel k, [16+k] closest-hit rays of kernel k
  * (k: 0 G-buffer, 1 path trace, 2 temporal, 3 spatial); the wavefront's traversal stages also
- * count on their own: [20+3s] nodes, [21+3s] triangles, [22+3s] rays (closest for s = 0, the
- * extension stage; shadow for s = 1, the shadow stage). */
+ * count on their own: [26+3s] nodes, [27+3s] triangles, [28+3s] rays (closest for s = 0, the
+ * extension stage; shadow for s = 1, the shadow stage); words 24-25 hold the persistent form's
+ * tile cursors. */
 GD void flush_counts(unsigned long long* counters, const RayCount& rc, int err, int kernel, int countWork,
                      int stage = -1) {
     unsigned int c = __reduce_add_sync(0xffffffffu, rc.closest);
@@ -84,9 +85,9 @@ GD void flush_counts(unsigned long long* counters, const RayCount& rc, int err, 
             atomicAdd(counters + 9 + 2 * kernel, tris);
             atomicAdd(counters + 16 + kernel, (unsigned long long)c);
             if (stage >= 0) {
-                atomicAdd(counters + 20 + 3 * stage, nodes);
-                atomicAdd(counters + 21 + 3 * stage, tris);
-                atomicAdd(counters + 22 + 3 * stage, (unsigned long long)(stage == 0 ? c : s));
+                atomicAdd(counters + 26 + 3 * stage, nodes);
+                atomicAdd(counters + 27 + 3 * stage, tris);
+                atomicAdd(counters + 28 + 3 * stage, (unsigned long long)(stage == 0 ? c : s));
             }
         }
     }
@@ -107,8 +108,11 @@ GD uint32_t nextRcVertexSampleState(uint32_t state, bool connectible) {         
 /* tracePath (gris_path_trace.glsl:45-306) as a state machine: begin() is the prologue up to the
  * bounce loop, step() one iteration of the loop (false where the reference breaks), end() the
  * epilogue that writes the canonical reservoir. Driving begin / step until false or maxDepth /
- * end performs exactly the reference's sequence of operations for the pixel. */
-struct PathTracer {
+ * end performs exactly the reference's sequence of operations for the pixel.
+ * kAcc (the converged-image estimators) also sums, per path, the candidate contributions given
+ * to the reservoir stream (accCand) and every NEE / light-hit contribution (accAll). */
+template <bool kAcc>
+struct PathTracerT {
     uint32_t ix, iy;
     int bounce;
     uint32_t rng;
@@ -129,8 +133,15 @@ struct PathTracer {
     V2 lightBary;
     float lightDist, lightPdf, lightJacobian;
     uint32_t lightId;
+    V3 accCand, accAll;
 
-    GD bool begin(const PassCtx& P, uint32_t px, uint32_t py) {
+    GD void candidate() {
+        addStream(stream, pathSample, luminance(pathSample.F), resvRandSample);
+        if constexpr (kAcc) accCand = accCand + pathSample.F;
+    }
+
+    GD bool begin(const PassCtx& P, uint32_t px, uint32_t py) { return begin(P, px, py, P.cam.seed); }
+    GD bool begin(const PassCtx& P, uint32_t px, uint32_t py, uint32_t frameSeed) {
         const DevScene& sc = P.sc;
         const int W = (int)P.b.width, H = (int)P.b.height;
         ix = px; iy = py;
@@ -141,7 +152,8 @@ struct PathTracer {
         if (!unpackGBuffer(dn, am, depth, norm, albedo, matMeshId)) return false;
         int matId = matMeshId >> 16;
         ray = pinholeCameraSampleRay(P.cam, v2(uv.x, 1.0f - uv.y));
-        rng = makeSeed2(P.cam.seed, ix, iy);
+        rng = makeSeed2(frameSeed, ix, iy);
+        if constexpr (kAcc) { accCand = v3s(0.0f); accAll = v3s(0.0f); }
         throughput = v3s(1.0f);
         rcThroughput = v3s(0.0f);
         wo = -ray.dir;
@@ -202,6 +214,7 @@ struct PathTracer {
                 float lightPdf = luminance(surf.albedo) / sumPower / geometryJacobian;
                 if (!isSampleTypeDelta(s.type)) weight = MISWeight(s.pdf, lightPdf);
                 V3 weightedLi = surf.albedo * weight;
+                if constexpr (kAcc) accAll = accAll + weightedLi * throughput;
                 if (sampleState == 2u && lastSampleState == 2u) {
                     pathSample.rcLi = pathSample.rcLi + weightedLi * rcThroughput;
                     pathSample.F = pathSample.F + weightedLi * throughput;
@@ -216,7 +229,7 @@ struct PathTracer {
                     pathSample.F = weightedLi * throughput;
                     setRcVertexId(pathSample.flags, (uint32_t)bounce);
                     setRcVertexType(pathSample.flags, kRcLightScattered);
-                    addStream(stream, pathSample, luminance(pathSample.F), resvRandSample);
+                    candidate();
                 }
                         }
             return kEnd;
@@ -255,6 +268,7 @@ struct PathTracer {
                 float weight = MISWeight(lightPdf, bsdfPdf);
                 V3 scatterTerm = evalBSDF(mat, surf.albedo, surf.norm, wo, lightDir) * satDot(surf.norm, lightDir);
                 V3 weightedLi = lightRadiance / lightPdf * weight;
+                if constexpr (kAcc) accAll = accAll + weightedLi * scatterTerm * throughput;
                 if (sampleState == 2u && lastSampleState == 2u) {
                     pathSample.rcLi = pathSample.rcLi + weightedLi * scatterTerm * rcThroughput;
                     pathSample.F = pathSample.F + weightedLi * scatterTerm * throughput;
@@ -262,7 +276,7 @@ struct PathTracer {
                     pathSample.rcLi = weightedLi;
                     pathSample.rcWi = lightDir;
                     pathSample.F = weightedLi * scatterTerm * throughput;
-                    addStream(stream, pathSample, luminance(pathSample.F), resvRandSample);
+                    candidate();
                 } else if ((sampleState == 1u) && isThisVertexConnectible && lightDist > kDistanceThreshold) {
                     pathSample.rcIsec.bx = lightBary.x; pathSample.rcIsec.by = lightBary.y;
                     pathSample.rcIsec.inst = 0u; pathSample.rcIsec.tri = lightId;
@@ -274,7 +288,7 @@ struct PathTracer {
                     pathSample.F = weightedLi * scatterTerm * throughput;
                     setRcVertexId(pathSample.flags, (uint32_t)bounce + 1u);
                     setRcVertexType(pathSample.flags, kRcLightSampled);
-                    addStream(stream, pathSample, luminance(pathSample.F), resvRandSample);
+                    candidate();
                 }
             }
         }
@@ -320,6 +334,11 @@ struct PathTracer {
         return post(P, shadowed);
     }
 
+    /* the converged-image estimators' epilogue: the last candidate, without the stream */
+    GD void finish() {
+        if (sampleState == 2u && lastSampleState == 2u) accCand = accCand + pathSample.F;
+    }
+
     /* after the loop (gris_path_trace.glsl:260-278) */
     GD void end(const PassCtx& P) {
         const int W = (int)P.b.width;
@@ -339,9 +358,9 @@ struct PathTracer {
         resv.s = pathSample;
         resv.sampleCount = 1.0f;
         store_resv(P.b.reservoirThis, (uint64_t)iy * (uint64_t)W + ix, resv);
-
     }
 };
+using PathTracer = PathTracerT<false>;
 
 /* ------------------------------------------------------------------ hybrid shift (gris_retrace.glsl) */
 /* traceReplayPathForHybridShift (:42-136) */
@@ -930,6 +949,111 @@ cudaError_t launch_gris(const DeviceSceneView& scene, const GrisPassBindings& b,
     }
     return cudaGetLastError();
 }
+
+/* ------------------------------------------------------------------ converged image */
+/* Seed of sample s of a pixel's sequence: a hash of the frame seed and the sample index, so
+ * the samples are streams of makeSeed like the frames of the renderer. */
+GD uint32_t sample_seed(uint32_t frameSeed, uint32_t s) { return hash2(frameSeed ^ hash2(s * 0x9e3779b9u + 0x7f4a7c15u)); }
+
+/* `sppN` independent paths per pixel (samples [spp0, spp0 + sppN)) of the path tracer from the
+ * pixel's G-buffer surface; each path's estimate (estimator 0: the sum of its reservoir
+ * candidates; 1: every NEE and light-hit contribution) is clamped as clampColor and added in
+ * FP64 to sum (and its square to sumSq). One thread per pixel: no two threads touch one pixel. */
+__global__ void __launch_bounds__(128) k_converged(PassCtx P, double* sum, double* sumSq, uint32_t spp0, uint32_t sppN,
+                                                   int estimator) {
+    const uint32_t x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y * blockDim.y + threadIdx.y;
+    if (x >= P.b.width || y >= P.b.height) return;
+    RayCount rc = ray_count();
+    int err = 0;
+    double a0 = 0.0, a1 = 0.0, a2 = 0.0, q0 = 0.0, q1 = 0.0, q2 = 0.0;
+    for (uint32_t s = spp0; s < spp0 + sppN; s++) {
+        PathTracerT<true> t;
+        if (!t.begin(P, x, y, sample_seed(P.cam.seed, s))) break;   /* background: the same for every sample */
+        while (t.step(P, rc, err) && ++t.bounce < (int)P.set.maxDepth) {}
+        t.finish();
+        V3 c = clampColor(estimator == 0 ? t.accCand : t.accAll);
+        a0 += (double)c.x; a1 += (double)c.y; a2 += (double)c.z;
+        q0 += (double)c.x * (double)c.x; q1 += (double)c.y * (double)c.y; q2 += (double)c.z * (double)c.z;
+    }
+    const size_t i = ((size_t)y * P.b.width + x) * 3;
+    sum[i] += a0; sum[i + 1] += a1; sum[i + 2] += a2;
+    if (sumSq) { sumSq[i] += q0; sumSq[i + 1] += q1; sumSq[i + 2] += q2; }
+    if (err) atomicOr(P.counters + GRIS_COUNTER_ERROR, (unsigned long long)err);
+}
+
+cudaError_t launch_converged(const DeviceSceneView& scene, const GrisConvergedBindings& b, const GrisCamera& cam,
+                             const GrisSettings& set, uint32_t sppBegin, uint32_t sppCount, int estimator,
+                             unsigned long long* counters, cudaStream_t stream) {
+    PassCtx P;
+    P.countWork = 0;
+    P.sc = to_dev(scene);
+    P.cam = make_cam(cam);
+    P.prev = P.cam;
+    P.set = set;
+    memset(&P.b, 0, sizeof(P.b));
+    P.b.width = b.width; P.b.height = b.height;
+    P.b.depthNormal = b.depthNormal;
+    P.b.albedoMatId = b.albedoMatId;
+    P.counters = counters;
+    dim3 block(16, 8), grid((b.width + 15) / 16, (b.height + 7) / 8);
+    /* about 2^23 paths per launch keeps every launch short */
+    const uint64_t px = (uint64_t)b.width * b.height;
+    uint32_t chunk = (uint32_t)std::max<uint64_t>(1, std::min<uint64_t>(sppCount, (1ull << 23) / std::max<uint64_t>(1, px)));
+    for (uint32_t s = 0; s < sppCount; s += chunk) {
+        uint32_t n = std::min(chunk, sppCount - s);
+        k_converged<<<grid, block, 0, stream>>>(P, b.sum, b.sumSq, sppBegin + s, n, estimator);
+        cudaError_t e = cudaGetLastError();
+        if (e != cudaSuccess) return e;
+    }
+    return cudaSuccess;
+}
+
+/* relMSE = mean over pixels and channels of (img - ref)^2 / (ref^2 + eps), MSE = mean of
+ * (img - ref)^2, ref = refSum * refScale; FP64 sums in a fixed order (grid-stride per thread,
+ * then a fixed shuffle and block tree, then one block over the partials): deterministic. */
+constexpr int kReduceBlocks = 304, kReduceThreads = 256;
+__global__ void __launch_bounds__(kReduceThreads) k_relmse_partial(const float4* img, const double* refSum, double refScale,
+                                                                   uint64_t n, double eps, double* partial) {
+    double rel = 0.0, sq = 0.0;
+    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x) {
+        float4 v = img[i];
+        const double c[3] = {(double)v.x, (double)v.y, (double)v.z};
+        for (int k = 0; k < 3; k++) {
+            double r = refSum[i * 3 + k] * refScale, d = c[k] - r;
+            rel += d * d / (r * r + eps);
+            sq += d * d;
+        }
+    }
+    __shared__ double sr[kReduceThreads / 32], ss[kReduceThreads / 32];
+    for (int o = 16; o > 0; o >>= 1) {
+        rel += __shfl_down_sync(0xffffffffu, rel, o);
+        sq += __shfl_down_sync(0xffffffffu, sq, o);
+    }
+    if ((threadIdx.x & 31) == 0) { sr[threadIdx.x >> 5] = rel; ss[threadIdx.x >> 5] = sq; }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double a = 0.0, b = 0.0;
+        for (int w = 0; w < kReduceThreads / 32; w++) { a += sr[w]; b += ss[w]; }
+        partial[2 * blockIdx.x] = a;
+        partial[2 * blockIdx.x + 1] = b;
+    }
+}
+__global__ void k_relmse_final(const double* partial, int blocks, uint64_t n, double* out) {
+    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    double a = 0.0, b = 0.0;
+    for (int i = 0; i < blocks; i++) { a += partial[2 * i]; b += partial[2 * i + 1]; }
+    out[0] = n ? a / (3.0 * (double)n) : 0.0;
+    out[1] = n ? b / (3.0 * (double)n) : 0.0;
+}
+
+cudaError_t launch_relmse(const float* image, const double* refSum, double refScale, uint64_t pixels, double eps,
+                          double* scratch, cudaStream_t stream) {
+    k_relmse_partial<<<kReduceBlocks, kReduceThreads, 0, stream>>>(reinterpret_cast<const float4*>(image), refSum,
+                                                                    refScale, pixels, eps, scratch + 2);
+    k_relmse_final<<<1, 32, 0, stream>>>(scratch + 2, kReduceBlocks, pixels, scratch);
+    return cudaGetLastError();
+}
+size_t relmse_scratch_doubles() { return 2 + 2 * (size_t)kReduceBlocks; }
 
 cudaError_t launch_debug_trace(const uint32_t* nodes, const float* tris, const float* rays, uint64_t n, int anyHit,
                                float* hitTUV, uint32_t* hitInst, uint32_t* hitTri, unsigned long long* counters,

@@ -36,6 +36,13 @@ cudaError_t launch_gbuffer(const DeviceSceneView& scene, const GrisGBufferBindin
 cudaError_t launch_gris(const DeviceSceneView& scene, const GrisPassBindings& b, const GrisCamera& cam,
                         const GrisCamera& prevCam, const GrisSettings& set, int passes, unsigned long long* counters,
                         int countWork, KernelTimer* timer, cudaStream_t stream, int launchMode = GRIS_LAUNCH_PERSISTENT);
+/* converged image: FP64 sums of independent paths per pixel; relMSE / MSE reduction */
+cudaError_t launch_converged(const DeviceSceneView& scene, const GrisConvergedBindings& b, const GrisCamera& cam,
+                             const GrisSettings& set, uint32_t sppBegin, uint32_t sppCount, int estimator,
+                             unsigned long long* counters, cudaStream_t stream);
+cudaError_t launch_relmse(const float* image, const double* refSum, double refScale, uint64_t pixels, double eps,
+                          double* scratch, cudaStream_t stream);
+size_t relmse_scratch_doubles();
 /* One view of a batch for one frame: its scene, this frame's buffers (ping-pong resolved),
  * cameras and settings. */
 struct BatchView {

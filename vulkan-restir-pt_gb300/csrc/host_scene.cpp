@@ -499,25 +499,29 @@ void build_terrain(GrisHostScene& s, uint32_t gridN, uint32_t spheres, bool glos
         float rot = 6.2831853f * rng.uniform();
         set_instance(s.instances.back(), m4_translate_scale_rotz(h3(px, py, pz), radius, rot), off, (uint32_t)SF.size(), mat);
     }
-    /* four 8 x 8 quad lights at height 22, facing down */
+    /* four 8 x 8 quad lights at height 22: facing down; in the glossy variant facing up under a
+     * white Lambertian bounce panel, so no light reaches the ground directly and the energy
+     * arrives after 2+ bounces */
     H3 lightPos[4] = {h3(-20, -20, 22), h3(20, -20, 22), h3(20, 20, 22), h3(-20, 20, 22)};
     H3 lightCol[4] = {h3(40, 36, 30), h3(30, 34, 40), h3(40, 40, 40), h3(36, 30, 40)};
     for (int l = 0; l < 4; l++) {
         H3 c = lightPos[l];
         float h = 4.0f;
-        add_quad_light(s, h3(c.x - h, c.y - h, c.z), h3(c.x - h, c.y + h, c.z), h3(c.x + h, c.y + h, c.z),
-                       h3(c.x + h, c.y - h, c.z), lightCol[l]);
-        if (glossy) {
-            /* occluder plate just under the light, so most energy arrives after 2+ bounces */
-            uint32_t mat = (uint32_t)s.materials.size();
-            s.materials.push_back(make_material(2u, h3(0.9f, 0.9f, 0.9f), 1.0f, 0.1f));
-            uint32_t off = (uint32_t)s.indices.size();
-            float ph = h * 1.6f, pz = c.z - 1.5f;
-            add_quad(s, h3(c.x - ph, c.y - ph, pz), h3(c.x + ph, c.y - ph, pz), h3(c.x + ph, c.y + ph, pz),
-                     h3(c.x - ph, c.y + ph, pz), h3(0, 0, 1), (int32_t)mat);
-            s.instances.emplace_back();
-            set_instance(s.instances.back(), m4_identity(), off, 6, mat);
+        if (!glossy) {
+            add_quad_light(s, h3(c.x - h, c.y - h, c.z), h3(c.x - h, c.y + h, c.z), h3(c.x + h, c.y + h, c.z),
+                           h3(c.x + h, c.y - h, c.z), lightCol[l]);
+            continue;
         }
+        add_quad_light(s, h3(c.x - h, c.y - h, c.z), h3(c.x + h, c.y - h, c.z), h3(c.x + h, c.y + h, c.z),
+                       h3(c.x - h, c.y + h, c.z), lightCol[l] * 4.0f);
+        uint32_t mat = (uint32_t)s.materials.size();
+        s.materials.push_back(make_material(1u, h3(0.85f, 0.85f, 0.85f), 0.0f, 1.0f));
+        uint32_t off = (uint32_t)s.indices.size();
+        float ph = 12.0f, pz = c.z + 4.0f;
+        add_quad(s, h3(c.x - ph, c.y - ph, pz), h3(c.x - ph, c.y + ph, pz), h3(c.x + ph, c.y + ph, pz),
+                 h3(c.x + ph, c.y - ph, pz), h3(0, 0, -1), (int32_t)mat);
+        s.instances.emplace_back();
+        set_instance(s.instances.back(), m4_identity(), off, 6, mat);
     }
     build_light_table(s);
     s.center[0] = 0.0f; s.center[1] = 0.0f; s.center[2] = 0.0f;

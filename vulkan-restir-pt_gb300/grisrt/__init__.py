@@ -105,6 +105,14 @@ class SceneStats(ctypes.Structure):
                 ("buildSeconds", ctypes.c_double)]
 
 
+class ConvergedBindings(ctypes.Structure):
+    _fields_ = [("width", ctypes.c_uint32), ("height", ctypes.c_uint32), ("depthNormal", ctypes.c_void_p),
+                ("albedoMatId", ctypes.c_void_p), ("sum", ctypes.c_void_p), ("sumSq", ctypes.c_void_p)]
+
+
+ESTIMATOR_CANDIDATES, ESTIMATOR_INDIRECT = 0, 1
+
+
 class KernelProfile(ctypes.Structure):
     _fields_ = [("ms", ctypes.c_double), ("launches", ctypes.c_uint64), ("nodes", ctypes.c_uint64),
                 ("tris", ctypes.c_uint64), ("rays", ctypes.c_uint64)]
@@ -128,7 +136,7 @@ EXPORTS = [
     "grisFrameCreate", "grisFrameDestroy", "grisFrameRender", "grisFrameGetBuffer", "grisFrameDownload",
     "grisFrameUpload", "grisSetPathForm", "grisBatchCreate", "grisBatchDestroy", "grisBatchRender", "grisBatchGetBuffer",
     "grisBatchDownload", "grisSetGraphs", "grisSetWaveLaunch", "grisBatchAutotune",
-    "grisReadKernelProfile",
+    "grisReadKernelProfile", "grisConvergedAccumulate", "grisRelMSE",
 ]
 
 _lib = None
@@ -189,6 +197,9 @@ def load(path=None):
         "grisBatchGetBuffer": (i32, [vp, u32, i32, i32, ctypes.POINTER(vp), ctypes.POINTER(ctypes.c_size_t)]),
         "grisBatchDownload": (i32, [vp, vp, u32, i32, i32, vp, ctypes.c_size_t]),
         "grisSetGraphs": (i32, [vp, i32]),
+        "grisConvergedAccumulate": (i32, [vp, vp, ctypes.POINTER(ConvergedBindings), ctypes.POINTER(Camera),
+                                          ctypes.POINTER(Settings), u32, u32, i32]),
+        "grisRelMSE": (i32, [vp, vp, vp, ctypes.c_double, u64, ctypes.c_double, ctypes.POINTER(ctypes.c_double)]),
         "grisReadKernelProfile": (i32, [vp, ctypes.POINTER(KernelProfile), i32]),
         "grisSetWaveLaunch": (i32, [vp, i32, i32]),
         "grisBatchAutotune": (i32, [vp, vp, ctypes.POINTER(Camera), ctypes.POINTER(Camera), ctypes.POINTER(Settings), i32,
@@ -356,6 +367,13 @@ class Context:
         return {name: dict(ms=o.ms, launches=o.launches, nodes=o.nodes, tris=o.tris, rays=o.rays)
                 for name, o in zip(PROFILE_SLOTS, out)}
 
+    def relmse(self, image_ptr, ref_sum_ptr, ref_scale, pixels, eps=1e-2):
+        """(relMSE, MSE) of an RGBA32F device image against ref_sum * ref_scale (device FP64)."""
+        out = (ctypes.c_double * 2)()
+        self.check(load().grisRelMSE(self.h, ctypes.c_void_p(image_ptr), ctypes.c_void_p(ref_sum_ptr), float(ref_scale),
+                                     int(pixels), float(eps), out), "grisRelMSE")
+        return out[0], out[1]
+
     def set_launch_mode(self, mode):
         """0: grid (one thread per pixel, default), 1: persistent with per-lane refill."""
         self.check(load().grisSetLaunchMode(self.h, int(mode)), "grisSetLaunchMode")
@@ -409,6 +427,15 @@ class Scene:
         s = SceneStats()
         self.ctx.check(load().grisSceneGetStats(self.h, ctypes.byref(s)), "grisSceneGetStats")
         return s
+
+    def converged(self, cam, settings, width, height, depth_normal, albedo_matid, sum_ptr, sumsq_ptr=None,
+                  spp_begin=0, spp=1, estimator=ESTIMATOR_CANDIDATES):
+        """Adds `spp` samples per pixel of the converged-image estimator to the FP64 device sums
+        (grisConvergedAccumulate); depth_normal / albedo_matid: the G-buffer of `cam`."""
+        b = ConvergedBindings(width, height, depth_normal, albedo_matid, sum_ptr, sumsq_ptr)
+        self.ctx.check(load().grisConvergedAccumulate(self.ctx.h, self.h, ctypes.byref(b), ctypes.byref(cam),
+                                                      ctypes.byref(settings), int(spp_begin), int(spp), int(estimator)),
+                       "grisConvergedAccumulate")
 
     def trace_host(self, rays, any_hit=False):
         rays = np.ascontiguousarray(rays, dtype=np.float32).reshape(-1, 8)
