@@ -287,6 +287,43 @@ int grisConvergedAccumulate(GrisContext* ctx, const GrisScene* scene, const Gris
 int grisRelMSE(GrisContext* ctx, const float* image, const double* refSum, double refScale, uint64_t pixels,
                double eps, double out[2]);
 
+/* ---------------------------------------------------------------- guiding network */
+/* A directional proposal learned online: an MLP (80 -> 64 x4 -> 48, BF16 tensor-core matrix
+ * products with FP32 accumulation) predicts per path vertex an 8-lobe von Mises-Fisher mixture
+ * over world directions from the vertex position (12-frequency sin/cos encoding in the scene
+ * box), shading normal and direction towards the previous vertex. A guided batch draws the
+ * directions of the vertices after a path's reconnection vertex (which the hybrid shift never
+ * replays) from the mixture with probability `mix` and from the BSDF otherwise, with the
+ * one-sample MIS pdf of both, and trains the network on the radiance those paths carry
+ * (Adam on -sum w log p / sum w, w = luminance(f cos L) / pdf). No counterpart in the
+ * reference; guiding off reproduces the reference's sampling exactly. */
+typedef struct GrisGuide GrisGuide;
+typedef struct GrisGuideConfig {
+    uint64_t seed;              /* Glorot-uniform initialisation */
+    float learningRate;         /* Adam (1e-3) */
+    float mix;                  /* probability of drawing from the guide at a guided vertex (0.5) */
+    uint32_t samplesPerFrame;   /* training records gathered per frame (2^18) */
+    uint32_t stepsPerFrame;     /* Adam steps per frame, each on samplesPerFrame / stepsPerFrame records */
+    uint32_t train;             /* train while rendering */
+    uint32_t reserved[3];
+} GrisGuideConfig;
+int grisGuideCreate(GrisContext* ctx, const GrisGuideConfig* cfg, GrisGuide** out);
+int grisGuideDestroy(GrisGuide* guide);
+int grisGuideParamCount(void);                                   /* 20784 FP32 values: W0 b0 ... W4 b4 */
+int grisGuideSetParams(GrisGuide* guide, const float* params, size_t count);   /* host; resets Adam */
+int grisGuideGetParams(GrisGuide* guide, float* params, size_t count);         /* host */
+int grisGuideSetTraining(GrisGuide* guide, int enable);
+/* device pointers: feat 9 floats per sample (position in [0,1]^3, normal, wo), out 40 raw
+ * outputs per sample (lobe j: direction 5j..5j+2, log-concentration 5j+3, logit 5j+4) */
+int grisGuideForward(GrisContext* ctx, GrisGuide* guide, const float* feat, uint32_t n, float* out);
+/* gradient of -sum_i weight_i log p(dir_i) / sum_i weight_i with respect to the FP32 parameters
+ * (device; overwritten) at the current weights */
+int grisGuideGradient(GrisContext* ctx, GrisGuide* guide, const float* feat, const float* dir, const float* weight,
+                      uint32_t n, float* grad);
+/* one Adam step on that loss */
+int grisGuideTrainStep(GrisContext* ctx, GrisGuide* guide, const float* feat, const float* dir, const float* weight,
+                       uint32_t n);
+
 /* ---------------------------------------------------------------- scene */
 /* Copies the arrays to the device and builds the 8-wide BVH over lights (instance 0) and every
  * instance's world-space triangles. */

@@ -41,6 +41,10 @@ int ctx_path_form(GrisContext* ctx);
 KernelTimer* ctx_timer(GrisContext* ctx);
 int ctx_fail(GrisContext* ctx, int code, const std::string& msg);
 struct WaveLaunch;
+namespace guide { struct GuideDevice; }
+guide::GuideDevice guide_device(const GrisGuide* g);
+const GrisGuideConfig& guide_config(const GrisGuide* g);
+cudaError_t guide_train_frame(GrisGuide* g, cudaStream_t st);
 bool ctx_graphs(GrisContext* ctx);            /* graphs enabled and per-kernel profiling off */
 WaveLaunch ctx_wave_launch(GrisContext* ctx);
 void ctx_set_tuning(GrisContext* ctx, int pathForm, WaveLaunch wl);

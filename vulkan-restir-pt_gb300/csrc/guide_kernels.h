@@ -1,0 +1,53 @@
+/* Host-side declarations of the guiding network's kernels (guide.cu). */
+#pragma once
+#include <cuda_bf16.h>
+#include <cuda_runtime.h>
+#include <stddef.h>
+#include <stdint.h>
+
+namespace grisrt {
+namespace guide {
+
+/* features: per sample 9 floats (position in [0,1]^3, normal, wo); out: 40 raw values per sample */
+struct FwdArgs {
+    const __nv_bfloat16* wPacked;
+    const float* bias;
+    const float* feat;
+    const uint32_t* count;     /* optional device count (samples = min(*count, n)) */
+    uint32_t n;
+    float* out;
+};
+
+/* gradient of loss = -sum_i weight_i log p(dir_i | feat_i) / sum_i weight_i, added to grad */
+struct GradArgs {
+    const __nv_bfloat16* wPacked;
+    const float* bias;
+    const float* feat;
+    const float* dir;
+    const float* weight;
+    const uint32_t* count;
+    uint32_t n;
+    float* invWeightSum;       /* device scalar: written here from the weights, then read */
+    float* grad;
+};
+
+/* what the path tracer needs of a guide: the network and the training-record batch */
+struct GuideDevice {
+    const __nv_bfloat16* wPacked;
+    const float* bias;
+    float* tFeat;
+    float* tDir;
+    float* tWeight;
+    uint32_t* tCount;
+    uint32_t cap;
+    float mix;
+};
+
+cudaError_t launch_forward(const FwdArgs& a, cudaStream_t stream);
+cudaError_t launch_grad(const GradArgs& a, cudaStream_t stream);
+cudaError_t launch_pack(const float* params, __nv_bfloat16* wPacked, float* bias, cudaStream_t stream);
+cudaError_t launch_adam(float* params, float* grad, float* m, float* v, uint32_t* step, float lr, cudaStream_t stream);
+size_t grad_smem_bytes();
+
+}  // namespace guide
+}  // namespace grisrt

@@ -113,6 +113,16 @@ class ConvergedBindings(ctypes.Structure):
 ESTIMATOR_CANDIDATES, ESTIMATOR_INDIRECT = 0, 1
 
 
+class GuideConfig(ctypes.Structure):
+    _fields_ = [("seed", ctypes.c_uint64), ("learningRate", ctypes.c_float), ("mix", ctypes.c_float),
+                ("samplesPerFrame", ctypes.c_uint32), ("stepsPerFrame", ctypes.c_uint32), ("train", ctypes.c_uint32),
+                ("reserved", ctypes.c_uint32 * 3)]
+
+    @staticmethod
+    def make(seed=1, learningRate=1e-3, mix=0.5, samplesPerFrame=1 << 18, stepsPerFrame=4, train=True):
+        return GuideConfig(seed, learningRate, mix, samplesPerFrame, stepsPerFrame, int(train))
+
+
 class KernelProfile(ctypes.Structure):
     _fields_ = [("ms", ctypes.c_double), ("launches", ctypes.c_uint64), ("nodes", ctypes.c_uint64),
                 ("tris", ctypes.c_uint64), ("rays", ctypes.c_uint64)]
@@ -137,6 +147,8 @@ EXPORTS = [
     "grisFrameUpload", "grisSetPathForm", "grisBatchCreate", "grisBatchDestroy", "grisBatchRender", "grisBatchGetBuffer",
     "grisBatchDownload", "grisSetGraphs", "grisSetWaveLaunch", "grisBatchAutotune",
     "grisReadKernelProfile", "grisConvergedAccumulate", "grisRelMSE",
+    "grisGuideCreate", "grisGuideDestroy", "grisGuideParamCount", "grisGuideSetParams", "grisGuideGetParams",
+    "grisGuideSetTraining", "grisGuideForward", "grisGuideGradient", "grisGuideTrainStep",
 ]
 
 _lib = None
@@ -197,6 +209,15 @@ def load(path=None):
         "grisBatchGetBuffer": (i32, [vp, u32, i32, i32, ctypes.POINTER(vp), ctypes.POINTER(ctypes.c_size_t)]),
         "grisBatchDownload": (i32, [vp, vp, u32, i32, i32, vp, ctypes.c_size_t]),
         "grisSetGraphs": (i32, [vp, i32]),
+        "grisGuideCreate": (i32, [vp, ctypes.POINTER(GuideConfig), ctypes.POINTER(vp)]),
+        "grisGuideDestroy": (i32, [vp]),
+        "grisGuideParamCount": (i32, []),
+        "grisGuideSetParams": (i32, [vp, vp, ctypes.c_size_t]),
+        "grisGuideGetParams": (i32, [vp, vp, ctypes.c_size_t]),
+        "grisGuideSetTraining": (i32, [vp, i32]),
+        "grisGuideForward": (i32, [vp, vp, vp, u32, vp]),
+        "grisGuideGradient": (i32, [vp, vp, vp, vp, vp, u32, vp]),
+        "grisGuideTrainStep": (i32, [vp, vp, vp, vp, vp, u32]),
         "grisConvergedAccumulate": (i32, [vp, vp, ctypes.POINTER(ConvergedBindings), ctypes.POINTER(Camera),
                                           ctypes.POINTER(Settings), u32, u32, i32]),
         "grisRelMSE": (i32, [vp, vp, vp, ctypes.c_double, u64, ctypes.c_double, ctypes.POINTER(ctypes.c_double)]),
@@ -450,7 +471,8 @@ class Scene:
 
     def close(self):
         if self.h:
-            load().grisSceneDestroy(self.h)
+            if self.ctx.h:   # a context destroyed first (garbage collection order) took its objects' use with it
+                load().grisSceneDestroy(self.h)
             self.h = None
 
     def __del__(self):
@@ -498,11 +520,64 @@ class Frame:
 
     def close(self):
         if self.handle:
-            load().grisFrameDestroy(self.handle)
+            if self.ctx.h:   # a context destroyed first (garbage collection order) took its objects' use with it
+                load().grisFrameDestroy(self.handle)
             self.handle = None
 
     def __del__(self):
         # at interpreter exit the CUDA runtime may already be torn down: leave it to the driver
+        if sys.is_finalizing():
+            return
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class Guide:
+    """The guiding network (grisGuide*): parameters as one flat FP32 vector W0 b0 ... W4 b4
+    (W row-major out x in), device-pointer forward / gradient / Adam step."""
+
+    def __init__(self, ctx, config=None):
+        self.ctx = ctx
+        cfg = config or GuideConfig.make()
+        h = ctypes.c_void_p()
+        ctx.check(load().grisGuideCreate(ctx.h, ctypes.byref(cfg), ctypes.byref(h)), "grisGuideCreate")
+        self.h = h
+        self.n_params = load().grisGuideParamCount()
+
+    def get_params(self):
+        p = np.zeros(self.n_params, np.float32)
+        self.ctx.check(load().grisGuideGetParams(self.h, ctypes.c_void_p(p.ctypes.data), p.size), "grisGuideGetParams")
+        return p
+
+    def set_params(self, p):
+        p = np.ascontiguousarray(p, np.float32)
+        self.ctx.check(load().grisGuideSetParams(self.h, ctypes.c_void_p(p.ctypes.data), p.size), "grisGuideSetParams")
+
+    def set_training(self, enable):
+        self.ctx.check(load().grisGuideSetTraining(self.h, int(enable)), "grisGuideSetTraining")
+
+    def forward(self, feat_ptr, n, out_ptr):
+        self.ctx.check(load().grisGuideForward(self.ctx.h, self.h, ctypes.c_void_p(feat_ptr), n, ctypes.c_void_p(out_ptr)),
+                       "grisGuideForward")
+
+    def gradient(self, feat_ptr, dir_ptr, weight_ptr, n, grad_ptr):
+        self.ctx.check(load().grisGuideGradient(self.ctx.h, self.h, ctypes.c_void_p(feat_ptr), ctypes.c_void_p(dir_ptr),
+                                                ctypes.c_void_p(weight_ptr), n, ctypes.c_void_p(grad_ptr)),
+                       "grisGuideGradient")
+
+    def train_step(self, feat_ptr, dir_ptr, weight_ptr, n):
+        self.ctx.check(load().grisGuideTrainStep(self.ctx.h, self.h, ctypes.c_void_p(feat_ptr), ctypes.c_void_p(dir_ptr),
+                                                 ctypes.c_void_p(weight_ptr), n), "grisGuideTrainStep")
+
+    def close(self):
+        if self.h:
+            if self.ctx.h:   # a context destroyed first (garbage collection order) took its objects' use with it
+                load().grisGuideDestroy(self.h)
+            self.h = None
+
+    def __del__(self):
         if sys.is_finalizing():
             return
         try:
@@ -567,7 +642,8 @@ class Batch:
 
     def close(self):
         if self.handle:
-            load().grisBatchDestroy(self.handle)
+            if self.ctx.h:   # a context destroyed first (garbage collection order) took its objects' use with it
+                load().grisBatchDestroy(self.handle)
             self.handle = None
 
     def __del__(self):
