@@ -219,14 +219,16 @@ int grisSetLaunchMode(GrisContext* ctx, int mode);
 int grisReadWorkCounters(GrisContext* ctx, uint64_t nodes[4], uint64_t tris[4], uint64_t closestRays[4], int reset);
 /* Per-kernel profile with the wavefront stages on their own: slots 0-3 as grisReadProfile (slot 1
  * spans the whole path tracer), then the wavefront's begin, extension (closest hits), shading,
- * shadow and post stages. ms/launches while profiling is on; nodes/tris/rays while work counting
+ * shadow and post stages, then the guide's inference and training. ms/launches while profiling is on; nodes/tris/rays while work counting
  * is on, for the slots that traverse (rays: closest-hit rays, shadow rays for the shadow stage). */
-#define GRIS_PROFILE_SLOTS 9
+#define GRIS_PROFILE_SLOTS 11
 #define GRIS_SLOT_WAVE_BEGIN 4
 #define GRIS_SLOT_WAVE_EXTEND 5
 #define GRIS_SLOT_WAVE_SHADE 6
 #define GRIS_SLOT_WAVE_SHADOW 7
 #define GRIS_SLOT_WAVE_POST 8
+#define GRIS_SLOT_GUIDE_INFER 9     /* guided batches: the network's inference per level */
+#define GRIS_SLOT_GUIDE_TRAIN 10    /* guided batches: the frame's training steps */
 typedef struct GrisKernelProfile {
     double ms;
     uint64_t launches;
@@ -406,6 +408,10 @@ int grisBatchGetBuffer(const GrisBatch* batch, uint32_t view, int which, int slo
 /* Copies one view's buffer to host memory on the context stream and waits for it. */
 int grisBatchDownload(GrisContext* ctx, const GrisBatch* batch, uint32_t view, int which, int slot, void* host,
                       size_t bytes);
+/* Attaches a guide (NULL detaches it): the batch's path tracing then guides the vertices after
+ * each path's reconnection vertex and, when the guide trains, runs its Adam steps on the
+ * frame's records after each frame (wavefront path form only). */
+int grisBatchSetGuide(GrisBatch* batch, GrisGuide* guide);
 int grisBatchAutotune(GrisContext* ctx, GrisBatch* batch, const GrisCamera* cams, const GrisCamera* prevCams,
                       const GrisSettings* settings, int frames, GrisTuneResult* out);
 

@@ -13,6 +13,8 @@
 
 #include "../../include/grisrt.h"
 #include "gris_kernels.h"
+#include "guide.cuh"
+#include "guide_kernels.h"
 #include "grisrt_internal.h"
 
 struct GrisBatch {
@@ -43,7 +45,11 @@ struct GrisBatch {
         cudaGraphExec_t exec = nullptr;
         int pathForm = -1, maxDepth = -1, trace = 0, shade = 0, countWork = -1;
         uint32_t pixels = 0, tiles = 0;
+        const GrisGuide* guide = nullptr;
+        int train = -1;
     } graph[2];
+    GrisGuide* guide = nullptr;
+    void* guideBlock = nullptr;   /* the guided-wavefront buffers (allocated with the first guide) */
 };
 
 static void drop_graphs(GrisBatch* b) {
@@ -106,7 +112,7 @@ int grisBatchCreate(GrisContext* ctx, uint32_t n, const GrisScene* const* scenes
     alloc((void**)&b->wave.queue[0], P * 4, false);
     alloc((void**)&b->wave.queue[1], P * 4, false);
     alloc((void**)&b->wave.shadowQueue, P * 4, false);
-    alloc((void**)&b->wave.counts, 512 * 4, true);
+    alloc((void**)&b->wave.counts, 1024 * 4, true);
     b->wave.capacity = P;
     alloc(&b->dViews, view_entry_bytes() * n, false);
     for (int i = 0; i < 2 && e == cudaSuccess; i++) {
@@ -128,6 +134,7 @@ int grisBatchDestroy(GrisBatch* b) {
     cudaSetDevice(ctx_device(b->ctx));
     cudaStreamSynchronize(ctx_stream(b->ctx));
     drop_graphs(b);
+    if (b->guideBlock) cudaFree(b->guideBlock);
     for (void* p : b->allocations) cudaFree(p);
     for (int i = 0; i < 2; i++) {
         if (b->hViews[i]) cudaFreeHost(b->hViews[i]);
@@ -170,16 +177,25 @@ int grisBatchRender(GrisContext* ctx, GrisBatch* b, const GrisCamera* cams, cons
     BatchShape sh = fill_view_table(views.data(), (int)b->n, b->hViews[k], ctx_counters(ctx), ctx_count_work(ctx));
     int form = ctx_path_form(ctx);
     WaveLaunch wl = ctx_wave_launch(ctx);
+    guide::GuideDevice gd{};
+    int train = 0;
+    if (b->guide) {
+        if (form != GRIS_PATH_WAVEFRONT) return ctx_fail(ctx, GRIS_ERR_UNSUPPORTED, "guided batches need the wavefront path form");
+        gd = guide_device(b->guide);
+        train = guide_config(b->guide).train ? 1 : 0;
+    }
     if (ctx_graphs(ctx)) {
         GrisBatch::Graph& g = b->graph[k];
         if (!g.exec || g.pathForm != form || g.maxDepth != sh.maxDepth || g.pixels != sh.pixels || g.tiles != sh.tiles ||
-            g.trace != wl.traceBlocksPerSM || g.shade != wl.shadeBlocksPerSM || g.countWork != ctx_count_work(ctx)) {
+            g.trace != wl.traceBlocksPerSM || g.shade != wl.shadeBlocksPerSM || g.countWork != ctx_count_work(ctx) ||
+            g.guide != b->guide || g.train != train) {
             if (g.exec) { cudaGraphExecDestroy(g.exec); g.exec = nullptr; }
             cudaGraph_t graph = nullptr;
             e = cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal);
             if (e == cudaSuccess) {
                 cudaError_t ee = enqueue_batch(sh, b->dViews, b->hViews[k], b->wave, ctx_counters(ctx), ctx_count_work(ctx),
-                                               nullptr, st, form, 15, wl);
+                                               nullptr, st, form, 15, wl, b->guide ? &gd : nullptr);
+                if (ee == cudaSuccess && train) ee = guide_train_frame(b->guide, st);
                 e = cudaStreamEndCapture(st, &graph);
                 if (e == cudaSuccess) e = ee;
             }
@@ -188,11 +204,18 @@ int grisBatchRender(GrisContext* ctx, GrisBatch* b, const GrisCamera* cams, cons
             if (e != cudaSuccess) return ctx_fail(ctx, GRIS_ERR_CUDA, std::string("graph capture: ") + cudaGetErrorString(e));
             g.pathForm = form; g.maxDepth = sh.maxDepth; g.pixels = sh.pixels; g.tiles = sh.tiles;
             g.trace = wl.traceBlocksPerSM; g.shade = wl.shadeBlocksPerSM; g.countWork = ctx_count_work(ctx);
+            g.guide = b->guide; g.train = train;
         }
         e = cudaGraphLaunch(g.exec, st);
     } else {
         e = enqueue_batch(sh, b->dViews, b->hViews[k], b->wave, ctx_counters(ctx), ctx_count_work(ctx), ctx_timer(ctx), st,
-                          form, 15, wl);
+                          form, 15, wl, b->guide ? &gd : nullptr);
+        if (e == cudaSuccess && train) {
+            KernelTimer* tm = ctx_timer(ctx);
+            if (tm) tm->mark(10, true, st);
+            e = guide_train_frame(b->guide, st);
+            if (tm) tm->mark(10, false, st);
+        }
     }
     if (e == cudaSuccess) e = cudaEventRecord(b->staged[k], st);
     if (e != cudaSuccess) return ctx_fail(ctx, GRIS_ERR_CUDA, std::string("grisBatchRender: ") + cudaGetErrorString(e));
@@ -219,6 +242,30 @@ int grisBatchGetBuffer(const GrisBatch* b, uint32_t view, int which, int slot, v
     }
     *devPtr = p;
     if (bytes) *bytes = sz;
+    return GRIS_OK;
+}
+
+int grisBatchSetGuide(GrisBatch* b, GrisGuide* g) {
+    if (!b) return GRIS_ERR_INVALID_ARGUMENT;
+    GrisContext* ctx = b->ctx;
+    cudaSetDevice(ctx_device(ctx));
+    if (g && !b->guideBlock) {
+        size_t P = (size_t)b->pixels;
+        auto up = [](size_t n) { return (n + 255) & ~(size_t)255; };
+        size_t bytes = up(P * 4) + up(P * 9 * 4) + up(P * guide::kRaw * 4) + up(P * 18 * 4) + 256;
+        cudaError_t e = cudaMalloc(&b->guideBlock, bytes);
+        if (e != cudaSuccess) { b->guideBlock = nullptr; return ctx_fail(ctx, GRIS_ERR_OUT_OF_MEMORY, "guided batch buffers"); }
+        char* p = (char*)b->guideBlock;
+        b->wave.postQueue = (uint32_t*)p; p += up(P * 4);
+        b->wave.gFeat = (float*)p; p += up(P * 9 * 4);
+        b->wave.gOut = (float*)p; p += up(P * guide::kRaw * 4);
+        b->wave.gRec = (float*)p; p += up(P * 18 * 4);
+        b->wave.gFrame = (uint32_t*)p;
+        e = cudaMemsetAsync(b->wave.gFrame, 0, 256, ctx_stream(ctx));
+        if (e == cudaSuccess) e = cudaStreamSynchronize(ctx_stream(ctx));
+        if (e != cudaSuccess) return ctx_fail(ctx, GRIS_ERR_CUDA, std::string("guided batch buffers: ") + cudaGetErrorString(e));
+    }
+    b->guide = g;
     return GRIS_OK;
 }
 

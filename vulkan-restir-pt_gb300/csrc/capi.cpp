@@ -9,6 +9,7 @@
 #include <cuda_runtime.h>
 #include <string.h>
 
+#include <algorithm>
 #include <string>
 #include <vector>
 
@@ -369,6 +370,17 @@ int grisSceneCreate(GrisContext* ctx, const GrisSceneDesc* d, GrisScene** out) {
     s->ctx = ctx;
     std::string err;
     if (!grisrt::build_bvh(*d, s->bvh, err)) { delete s; return fail(ctx, GRIS_ERR_INVALID_ARGUMENT, err); }
+    {
+        float mn[3] = {3.0e38f, 3.0e38f, 3.0e38f}, mx[3] = {-3.0e38f, -3.0e38f, -3.0e38f};
+        const std::vector<float>& T = s->bvh.tris;
+        for (size_t t = 0; t + 12 <= T.size(); t += 12)   /* v0, instance, e1, triangle, e2, 0 */
+            for (int c = 0; c < 3; c++) {
+                float v0 = T[t + c], p1 = v0 + T[t + 4 + c], p2 = v0 + T[t + 8 + c];
+                mn[c] = std::min(mn[c], std::min(v0, std::min(p1, p2)));
+                mx[c] = std::max(mx[c], std::max(v0, std::max(p1, p2)));
+            }
+        for (int c = 0; c < 3; c++) { s->view.boxMin[c] = mn[c]; s->view.boxMax[c] = mx[c]; }
+    }
     int rc = GRIS_OK;
 #define UP(src, n, dst) if (rc == GRIS_OK) rc = upload(ctx, s, src, n, dst)
     UP(d->vertices, d->vertexCount, &s->view.vertices);
@@ -538,7 +550,7 @@ int grisPassRender(GrisContext* ctx, const GrisScene* s, const GrisPassBindings*
             alloc((void**)&w.wb.queue[0], P * 4);
             alloc((void**)&w.wb.queue[1], P * 4);
             alloc((void**)&w.wb.shadowQueue, P * 4);
-            alloc((void**)&w.wb.counts, 512 * 4);
+            alloc((void**)&w.wb.counts, 1024 * 4);
             alloc(&w.dViews, grisrt::view_entry_bytes());
             for (int i = 0; i < 2 && e == cudaSuccess; i++) {
                 e = cudaMallocHost(&w.hViews[i], grisrt::view_entry_bytes());

@@ -17,6 +17,8 @@
 
 #include "gris_device.cuh"
 #include "gris_kernels.h"
+#include "guide.cuh"
+#include "guide_kernels.h"
 
 namespace grisrt {
 
@@ -110,9 +112,15 @@ GD uint32_t nextRcVertexSampleState(uint32_t state, bool connectible) {         
  * epilogue that writes the canonical reservoir. Driving begin / step until false or maxDepth /
  * end performs exactly the reference's sequence of operations for the pixel.
  * kAcc (the converged-image estimators) also sums, per path, the candidate contributions given
- * to the reservoir stream (accCand) and every NEE / light-hit contribution (accAll). */
-template <bool kAcc>
+ * to the reservoir stream (accCand) and every NEE / light-hit contribution (accAll).
+ * kGuide (guided batches, implies kAcc): shade() leaves post() to the caller (kPost), and post()
+ * draws the direction from the guide mixture or the BSDF (one-sample MIS) where the caller
+ * passes the vertex's mixture; light hits then weigh the BSDF strategy by the BSDF's own pdf of
+ * the sampled direction (pdfHit), so the estimand stays the unguided one. */
+template <bool kAcc, bool kGuide = false>
 struct PathTracerT {
+    static constexpr bool kAccumulate = kAcc || kGuide;
+    static constexpr bool kGuided = kGuide;
     uint32_t ix, iy;
     int bounce;
     uint32_t rng;
@@ -134,10 +142,13 @@ struct PathTracerT {
     float lightDist, lightPdf, lightJacobian;
     uint32_t lightId;
     V3 accCand, accAll;
+    float pdfHit;        /* kGuide: the BSDF pdf of the last sampled direction */
+    V3 thrSampled;       /* kGuide: the throughput at the last sampling, before its BSDF factor */
+    uint32_t rec;        /* kGuide: this path holds a training record */
 
     GD void candidate() {
         addStream(stream, pathSample, luminance(pathSample.F), resvRandSample);
-        if constexpr (kAcc) accCand = accCand + pathSample.F;
+        if constexpr (kAccumulate) accCand = accCand + pathSample.F;
     }
 
     GD bool begin(const PassCtx& P, uint32_t px, uint32_t py) { return begin(P, px, py, P.cam.seed); }
@@ -153,7 +164,8 @@ struct PathTracerT {
         int matId = matMeshId >> 16;
         ray = pinholeCameraSampleRay(P.cam, v2(uv.x, 1.0f - uv.y));
         rng = makeSeed2(frameSeed, ix, iy);
-        if constexpr (kAcc) { accCand = v3s(0.0f); accAll = v3s(0.0f); }
+        if constexpr (kAccumulate) { accCand = v3s(0.0f); accAll = v3s(0.0f); }
+        if constexpr (kGuide) { pdfHit = 0.0f; thrSampled = v3s(0.0f); rec = 0u; }
         throughput = v3s(1.0f);
         rcThroughput = v3s(0.0f);
         wo = -ray.dir;
@@ -181,7 +193,7 @@ struct PathTracerT {
      * light sample: kShadow asks the caller for the shadow query (surf.pos along lightDir, up to
      * lightDist - MinRayDistance) and then post(shadowed); kNext / kEnd report a vertex without
      * NEE whose post() already ran (continue / the reference breaks). */
-    static constexpr int kEnd = 0, kShadow = 1, kNext = 2;
+    static constexpr int kEnd = 0, kShadow = 1, kNext = 2, kPost = 3;
     GD int shade(const PassCtx& P, const Isec& hit) {
         const DevScene& sc = P.sc;
         if (bounce > 0) {
@@ -212,9 +224,9 @@ struct PathTracerT {
                 float weight = 1.0f;
                 float sumPower = load_table(sc, 0).prob;
                 float lightPdf = luminance(surf.albedo) / sumPower / geometryJacobian;
-                if (!isSampleTypeDelta(s.type)) weight = MISWeight(s.pdf, lightPdf);
+                if (!isSampleTypeDelta(s.type)) weight = MISWeight(kGuide ? pdfHit : s.pdf, lightPdf);
                 V3 weightedLi = surf.albedo * weight;
-                if constexpr (kAcc) accAll = accAll + weightedLi * throughput;
+                if constexpr (kAccumulate) accAll = accAll + weightedLi * throughput;
                 if (sampleState == 2u && lastSampleState == 2u) {
                     pathSample.rcLi = pathSample.rcLi + weightedLi * rcThroughput;
                     pathSample.F = pathSample.F + weightedLi * throughput;
@@ -256,19 +268,20 @@ struct PathTracerT {
                                                lightId, lightRandSample);
             return kShadow;
         }
+        if constexpr (kGuide) return kPost;
         return post(P, false) ? kNext : kEnd;
     }
 
     /* second part: the NEE contribution (when shade() sampled a light), Russian roulette, BSDF
      * sampling; true = the path continues */
-    GD bool post(const PassCtx& P, bool shadowed) {
+    GD bool post(const PassCtx& P, bool shadowed, const guide::Lobes* L = nullptr, float mix = 0.0f) {
         if (nee) {
             if (!shadowed && lightPdf > 1e-6f) {
                 float bsdfPdf = absDot(surf.norm, lightDir) * kPiInv;
                 float weight = MISWeight(lightPdf, bsdfPdf);
                 V3 scatterTerm = evalBSDF(mat, surf.albedo, surf.norm, wo, lightDir) * satDot(surf.norm, lightDir);
                 V3 weightedLi = lightRadiance / lightPdf * weight;
-                if constexpr (kAcc) accAll = accAll + weightedLi * scatterTerm * throughput;
+                if constexpr (kAccumulate) accAll = accAll + weightedLi * scatterTerm * throughput;
                 if (sampleState == 2u && lastSampleState == 2u) {
                     pathSample.rcLi = pathSample.rcLi + weightedLi * scatterTerm * rcThroughput;
                     pathSample.F = pathSample.F + weightedLi * scatterTerm * throughput;
@@ -300,7 +313,33 @@ struct PathTracerT {
             rcThroughput = rcThroughput / (1.0f - pdfTerminate);
         }
 
-        if (!sampleBSDF(mat, surf.albedo, surf.norm, wo, sample3f(rng), s) || s.pdf < 1e-6f) return false;
+        if constexpr (kGuide) {
+            thrSampled = throughput;
+            if (L) {
+                /* one-sample MIS of the guide mixture (probability mix) and the BSDF sampler */
+                float u = sample1f(rng);
+                V3 r = sample3f(rng);
+                if (u < mix) {
+                    float d[3];
+                    guide::lobes_sample(*L, r.x, r.y, r.z, d);
+                    s.wi = v3(d[0], d[1], d[2]);
+                    if (dot3(surf.norm, s.wi) <= 0.0f) return false;   /* no reflection there: a zero sample */
+                    s.bsdf = evalBSDF(mat, surf.albedo, surf.norm, wo, s.wi);
+                    pdfHit = evalPdf(mat, surf.norm, wo, s.wi);
+                    s.type = kReflection | (mat.type == 1u ? kDiffuse : kGlossy);
+                } else {
+                    if (!sampleBSDF(mat, surf.albedo, surf.norm, wo, r, s)) return false;
+                    pdfHit = s.pdf;
+                }
+                s.pdf = mix * guide::lobes_pdf(*L, s.wi.x, s.wi.y, s.wi.z) + (1.0f - mix) * pdfHit;
+                if (!(s.pdf >= 1e-6f)) return false;
+            } else {
+                if (!sampleBSDF(mat, surf.albedo, surf.norm, wo, sample3f(rng), s) || s.pdf < 1e-6f) return false;
+                pdfHit = s.pdf;
+            }
+        } else {
+            if (!sampleBSDF(mat, surf.albedo, surf.norm, wo, sample3f(rng), s) || s.pdf < 1e-6f) return false;
+        }
 
         float cosTheta = isSampleTypeDelta(s.type) ? 1.0f : absDot(surf.norm, s.wi);
         V3 scatterTerm = s.bsdf * cosTheta / s.pdf;
@@ -1079,6 +1118,7 @@ struct ViewEntry {
     uint32_t tilesX;
     uint32_t pixelBase;  /* first path id of the view */
     uint32_t pad;
+    float boxMin[3], boxInv[3];   /* the scene box (guide inputs: position in [0,1]^3) */
 };
 
 size_t view_entry_bytes() { return sizeof(ViewEntry); }
@@ -1153,7 +1193,8 @@ GD void ps_from_words(PathSample& p, const uint4* w) {
     p.rcPrevSamplePdf = __uint_as_float(w[3].z); p.rcJacobian = __uint_as_float(w[3].w);
     p.F = v3(__uint_as_float(w[4].x), __uint_as_float(w[4].y), __uint_as_float(w[4].z)); p.primaryRng = w[4].w;
 }
-GD void save_wave(WaveRec* __restrict__ dst, const PathTracer& t) {
+template <class T>
+GD void save_wave(WaveRec* __restrict__ dst, const T& t) {
     uint4 w[17];
     w[0] = make_uint4(t.rng, t.sampleState | (t.lastSampleState << 8) | ((t.isLastVertexConnectible ? 1u : 0u) << 16),
                       t.surf.matIndex, t.s.type);
@@ -1161,15 +1202,27 @@ GD void save_wave(WaveRec* __restrict__ dst, const PathTracer& t) {
     w[2] = u4f(t.rcThroughput.x, t.rcThroughput.y, t.rcThroughput.z, t.stream.weight);
     w[3] = u4f(t.lastPos.x, t.lastPos.y, t.lastPos.z, t.stream.sumWeight);
     w[4] = make_uint4(__float_as_uint(t.ray.ori.x), __float_as_uint(t.ray.ori.y), __float_as_uint(t.ray.ori.z), t.stream.sampleCount);
-    w[5] = u4f(t.ray.dir.x, t.ray.dir.y, t.ray.dir.z, 0.0f);
+    float pdfHit = 0.0f;
+    if constexpr (T::kGuided) pdfHit = t.pdfHit;
+    w[5] = u4f(t.ray.dir.x, t.ray.dir.y, t.ray.dir.z, pdfHit);
     ps_to_words(t.pathSample, w + 6);
     ps_to_words(t.stream.ps, w + 11);
     w[16] = make_uint4(0u, 0u, 0u, 0u);
+    if constexpr (T::kAccumulate) w[16] = make_uint4(__float_as_uint(t.accAll.x), __float_as_uint(t.accAll.y),
+                                                     __float_as_uint(t.accAll.z), 0u);
+    if constexpr (T::kGuided) w[16].w = t.rec;
     for (int i = 0; i < 17; i++) dst->w[i] = w[i];
 }
-GD void load_wave(const WaveRec* __restrict__ src, PathTracer& t) {
+template <class T>
+GD void load_wave(const WaveRec* __restrict__ src, T& t) {
     uint4 w[17];
     for (int i = 0; i < 16; i++) w[i] = src->w[i];
+    if constexpr (T::kAccumulate) {
+        w[16] = src->w[16];
+        t.accAll = v3(__uint_as_float(w[16].x), __uint_as_float(w[16].y), __uint_as_float(w[16].z));
+        t.accCand = v3s(0.0f);
+    }
+    if constexpr (T::kGuided) { t.rec = w[16].w; t.pdfHit = __uint_as_float(w[5].w); t.thrSampled = v3s(0.0f); }
     t.rng = w[0].x;
     t.sampleState = w[0].y & 0xffu; t.lastSampleState = (w[0].y >> 8) & 0xffu; t.isLastVertexConnectible = (w[0].y >> 16) & 1u;
     t.surf.matIndex = w[0].z; t.s.type = w[0].w;
@@ -1184,26 +1237,29 @@ GD void load_wave(const WaveRec* __restrict__ src, PathTracer& t) {
     t.s.wi = v3s(0.0f); t.s.bsdf = v3s(0.0f);
     t.surf.isLight = false;
 }
-GD void save_nee(NeeRec* __restrict__ dst, const PathTracer& t) {
+template <class T>
+GD void save_nee(NeeRec* __restrict__ dst, const T& t) {
     dst->w[0] = make_uint4(__float_as_uint(t.surf.pos.x), __float_as_uint(t.surf.pos.y), __float_as_uint(t.surf.pos.z),
                            __float_as_uint(t.resvRandSample));
     dst->w[1] = make_uint4(__float_as_uint(t.surf.norm.x), __float_as_uint(t.surf.norm.y), __float_as_uint(t.surf.norm.z),
-                           t.isThisVertexConnectible ? 1u : 0u);
+                           (t.isThisVertexConnectible ? 1u : 0u) | (t.nee ? 2u : 0u));
     dst->w[2] = make_uint4(__float_as_uint(t.surf.albedo.x), __float_as_uint(t.surf.albedo.y), __float_as_uint(t.surf.albedo.z), t.lightId);
     dst->w[3] = u4f(t.lightRadiance.x, t.lightRadiance.y, t.lightRadiance.z, t.lightDist);
     dst->w[4] = u4f(t.lightDir.x, t.lightDir.y, t.lightDir.z, t.lightPdf);
     dst->w[5] = u4f(t.lightBary.x, t.lightBary.y, t.lightJacobian, 0.0f);
 }
-GD void load_nee(const NeeRec* __restrict__ src, PathTracer& t) {
+template <class T>
+GD void load_nee(const NeeRec* __restrict__ src, T& t) {
     uint4 w[6];
     for (int i = 0; i < 6; i++) w[i] = src->w[i];
     t.surf.pos = v3(__uint_as_float(w[0].x), __uint_as_float(w[0].y), __uint_as_float(w[0].z)); t.resvRandSample = __uint_as_float(w[0].w);
-    t.surf.norm = v3(__uint_as_float(w[1].x), __uint_as_float(w[1].y), __uint_as_float(w[1].z)); t.isThisVertexConnectible = w[1].w != 0u;
+    t.surf.norm = v3(__uint_as_float(w[1].x), __uint_as_float(w[1].y), __uint_as_float(w[1].z));
+    t.isThisVertexConnectible = (w[1].w & 1u) != 0u;
+    t.nee = (w[1].w & 2u) != 0u;
     t.surf.albedo = v3(__uint_as_float(w[2].x), __uint_as_float(w[2].y), __uint_as_float(w[2].z)); t.lightId = w[2].w;
     t.lightRadiance = v3(__uint_as_float(w[3].x), __uint_as_float(w[3].y), __uint_as_float(w[3].z)); t.lightDist = __uint_as_float(w[3].w);
     t.lightDir = v3(__uint_as_float(w[4].x), __uint_as_float(w[4].y), __uint_as_float(w[4].z)); t.lightPdf = __uint_as_float(w[4].w);
     t.lightBary = v2(__uint_as_float(w[5].x), __uint_as_float(w[5].y)); t.lightJacobian = __uint_as_float(w[5].z);
-    t.nee = true;
 }
 
 struct WaveCtx {
@@ -1216,9 +1272,18 @@ struct WaveCtx {
     unsigned char* blocked;
     uint32_t* queue[2];
     uint32_t* shadowQueue;
-    uint32_t* counts;   /* [level] path count of level, [256 + level] shadow-query count of level */
+    uint32_t* counts;   /* [level] paths, [256 + level] shadow queries, [512 + level] post() calls and
+                           [768 + level] guided vertices of the level (guided batches) */
     unsigned long long* counters;
     int countWork;
+    /* guided batches */
+    uint32_t* postQueue;
+    float* gFeat;        /* per guided vertex (queue order): position in [0,1]^3, normal, wo */
+    float* gOut;         /* per guided vertex: the network's 40 raw outputs */
+    float* gRec;         /* per path: its training record (features 9, direction 3, throughput 3, sum 3) */
+    uint32_t* gFrame;    /* [0] guided vertices this frame, [1] record probability (float bits) */
+    guide::GuideDevice guide;
+    uint32_t frameSeed;
 };
 
 /* Appends `id` (for lanes with `push`) to a queue with one atomic per warp. */
@@ -1240,8 +1305,35 @@ GD void path_coords(const WaveCtx& C, uint32_t id, int& v, uint32_t& x, uint32_t
     y = px / C.V[v].P.b.width;
 }
 
+/* At the end of a guided path holding a training record: the record's sample weight
+ * w = luminance((radiance gathered after the vertex) / (throughput at the vertex)) — the
+ * one-sample estimate of f cos L_in / pdf for the sampled direction — and, when positive, the
+ * record joins the frame's training batch. */
+template <class T>
+GD void guide_finish_record(const WaveCtx& C, const T& t, uint32_t id) {
+    if constexpr (T::kGuided) {
+        if (!t.rec) return;
+        const float* r = C.gRec + (size_t)id * 18;
+        const float acc[3] = {t.accAll.x, t.accAll.y, t.accAll.z};
+        float li[3];
+        for (int c = 0; c < 3; c++) {
+            float thr = r[12 + c];
+            li[c] = thr > 1e-20f ? (acc[c] - r[15 + c]) / thr : 0.0f;
+        }
+        float w = luminance(v3(li[0], li[1], li[2]));
+        if (!(w > 0.0f)) return;
+        w = fminf(w, 1e4f);
+        uint32_t slot = atomicAdd(C.guide.tCount, 1u);
+        if (slot >= C.guide.cap) return;
+        for (int i = 0; i < 9; i++) C.guide.tFeat[(size_t)slot * 9 + i] = r[i];
+        for (int i = 0; i < 3; i++) C.guide.tDir[(size_t)slot * 3 + i] = r[9 + i];
+        C.guide.tWeight[slot] = w;
+    }
+}
+
 /* After a bounce's post(): the next level or the end of the path. */
-GD void wave_continue(const WaveCtx& C, const PassCtx& P, PathTracer& t, uint32_t id, bool cont, int level, bool& push) {
+template <class T>
+GD void wave_continue(const WaveCtx& C, const PassCtx& P, T& t, uint32_t id, bool cont, int level, bool& push) {
     push = false;
     if (cont) {
         t.bounce++;
@@ -1252,6 +1344,7 @@ GD void wave_continue(const WaveCtx& C, const PassCtx& P, PathTracer& t, uint32_
         }
     }
     t.end(P);
+    guide_finish_record(C, t, id);
 }
 
 /* level 0: begin() + the primary vertex for every pixel of every view */
@@ -1367,6 +1460,155 @@ __global__ void __launch_bounds__(128) k_wave_post(WaveCtx C, int level) {
     }
 }
 
+/* ------------------------------------------------------------------ guided wavefront */
+using GuidedTracer = PathTracerT<true, true>;
+
+/* Vertices whose outgoing direction the guide may draw: after the path's reconnection vertex
+ * (a surface), which the hybrid shift never replays, on Lambert or rough metallic-workflow
+ * surfaces, when the direction will be traced. */
+GD bool guide_eligible(const GuidedTracer& t, const PassCtx& P) {
+    return t.sampleState == 2u && rcVertexType(t.pathSample.flags) == kRcSurface && !t.surf.isLight &&
+           (t.mat.type == 1u || (t.mat.type == 2u && t.mat.roughness >= 0.01f)) && t.bounce + 1 < (int)P.set.maxDepth;
+}
+
+/* A slot per lane with `take` from a counter, one atomic per warp. */
+GD uint32_t warp_alloc(uint32_t* count, bool take) {
+    unsigned m = __ballot_sync(0xffffffffu, take);
+    if (!m) return 0u;
+    uint32_t lane = threadIdx.x & 31u, leader = __ffs(m) - 1;
+    uint32_t base = 0;
+    if (lane == leader) base = atomicAdd(count, (uint32_t)__popc(m));
+    base = __shfl_sync(0xffffffffu, base, leader);
+    return base + __popc(m & ((1u << lane) - 1u));
+}
+
+/* frame start: the probability of keeping a guided vertex as a training record, from the
+ * previous frame's count of guided vertices, so that about `cap` records are gathered */
+__global__ void k_guide_frame_begin(uint32_t* frame, uint32_t* tCount, uint32_t cap) {
+    uint32_t e = frame[0];
+    float p = e > 0u ? fminf(1.0f, 1.25f * (float)cap / (float)e) : 1.0f;
+    frame[1] = __float_as_uint(p);
+    frame[0] = 0u;
+    frame[2] += 1u;
+    *tCount = 0u;
+}
+
+__global__ void __launch_bounds__(128) k_gwave_begin(WaveCtx C) {
+    uint32_t id = blockIdx.x * blockDim.x + threadIdx.x;
+    bool push = false;
+    if (id < C.totalPixels) {
+        int v; uint32_t x, y;
+        path_coords(C, id, v, x, y);
+        const PassCtx& P = C.V[v].P;
+        GuidedTracer t;
+        if (t.begin(P, x, y)) {
+            int r = t.shade(P, isec_zero());   /* no NEE at bounce 0; never guided */
+            bool cont = r == GuidedTracer::kPost ? t.post(P, false) : false;
+            wave_continue(C, P, t, id, cont, 0, push);
+        }
+    }
+    warp_push(C.queue[1], C.counts + 1, push, id);
+}
+
+/* shade() of the level's paths: the end, or a post() call (after a shadow query for NEE
+ * vertices), with the guide's inputs written for eligible vertices */
+__global__ void __launch_bounds__(128) k_gwave_shade(WaveCtx C, int level) {
+    const uint32_t n = C.counts[level];
+    const uint32_t* q = C.queue[level & 1];
+    for (uint32_t i0 = blockIdx.x * blockDim.x; i0 < n; i0 += gridDim.x * blockDim.x) {
+        uint32_t i = i0 + threadIdx.x;
+        bool pushPost = false, pushShadow = false, pushGuide = false;
+        uint32_t id = 0;
+        float feat[9];
+        if (i < n) {
+            id = q[i];
+            int v; uint32_t x, y;
+            path_coords(C, id, v, x, y);
+            const PassCtx& P = C.V[v].P;
+            GuidedTracer t;
+            load_wave(C.state + id, t);
+            t.ix = x; t.iy = y; t.bounce = level;
+            t.mat = load_material(P.sc, t.surf.matIndex);
+            int r = t.shade(P, C.hit[id]);
+            if (r == GuidedTracer::kShadow || r == GuidedTracer::kPost) {
+                pushGuide = guide_eligible(t, P);
+                if (pushGuide) {
+                    const ViewEntry& V = C.V[v];
+                    feat[0] = fminf(fmaxf((t.surf.pos.x - V.boxMin[0]) * V.boxInv[0], 0.0f), 1.0f);
+                    feat[1] = fminf(fmaxf((t.surf.pos.y - V.boxMin[1]) * V.boxInv[1], 0.0f), 1.0f);
+                    feat[2] = fminf(fmaxf((t.surf.pos.z - V.boxMin[2]) * V.boxInv[2], 0.0f), 1.0f);
+                    feat[3] = t.surf.norm.x; feat[4] = t.surf.norm.y; feat[5] = t.surf.norm.z;
+                    feat[6] = t.wo.x; feat[7] = t.wo.y; feat[8] = t.wo.z;
+                }
+                save_wave(C.state + id, t);
+                save_nee(C.nee + id, t);
+                pushPost = true;
+                pushShadow = r == GuidedTracer::kShadow;
+            } else {
+                bool unused;
+                wave_continue(C, P, t, id, false, level, unused);
+            }
+        }
+        uint32_t slot = warp_alloc(C.counts + 768 + level, pushGuide);
+        if (pushGuide) {
+            for (int k = 0; k < 9; k++) C.gFeat[(size_t)slot * 9 + k] = feat[k];
+        }
+        if (pushPost) reinterpret_cast<uint32_t*>(&C.nee[id].w[5])[3] = pushGuide ? slot + 1u : 0u;
+        warp_push(C.postQueue, C.counts + 512 + level, pushPost, id);
+        warp_push(C.shadowQueue, C.counts + 256 + level, pushShadow, id);
+    }
+}
+
+/* post() of the level's paths, with the guide mixture at guided vertices; a guided vertex is
+ * kept as its path's training record with the frame's record probability */
+__global__ void __launch_bounds__(128) k_gwave_post(WaveCtx C, int level) {
+    const uint32_t n = C.counts[512 + level];
+    const float pKeep = __uint_as_float(C.gFrame[1]);
+    const uint32_t frame = C.gFrame[2];
+    for (uint32_t i0 = blockIdx.x * blockDim.x; i0 < n; i0 += gridDim.x * blockDim.x) {
+        uint32_t i = i0 + threadIdx.x;
+        bool push = false, guided = false;
+        uint32_t id = 0;
+        if (i < n) {
+            id = C.postQueue[i];
+            int v; uint32_t x, y;
+            path_coords(C, id, v, x, y);
+            const PassCtx& P = C.V[v].P;
+            GuidedTracer t;
+            load_wave(C.state + id, t);
+            load_nee(C.nee + id, t);
+            t.ix = x; t.iy = y; t.bounce = level;
+            t.mat = load_material(P.sc, t.surf.matIndex);
+            const uint32_t slot1 = reinterpret_cast<const uint32_t*>(&C.nee[id].w[5])[3];
+            guide::Lobes L;
+            if (slot1) guide::make_lobes(C.gOut + (size_t)(slot1 - 1u) * guide::kRaw, L);
+            guided = slot1 != 0u;
+            bool blocked = t.nee ? C.blocked[id] != 0 : false;
+            bool cont = t.post(P, blocked, guided ? &L : nullptr, C.guide.mix);
+            if (cont && guided) {
+                uint32_t h = hash2(frame * 0x9e3779b9u ^ hash2(id * 0x85ebca6bu + (uint32_t)level));
+                if ((float)(h >> 8) * (1.0f / 16777216.0f) < pKeep) {
+                    float* r = C.gRec + (size_t)id * 18;
+                    const float* f = C.gFeat + (size_t)(slot1 - 1u) * 9;
+                    for (int k = 0; k < 9; k++) r[k] = f[k];
+                    r[9] = t.s.wi.x; r[10] = t.s.wi.y; r[11] = t.s.wi.z;
+                    r[12] = t.thrSampled.x; r[13] = t.thrSampled.y; r[14] = t.thrSampled.z;
+                    r[15] = t.accAll.x; r[16] = t.accAll.y; r[17] = t.accAll.z;
+                    t.rec = 1u;
+                }
+            }
+            wave_continue(C, P, t, id, cont, level, push);
+        }
+        unsigned m = __ballot_sync(0xffffffffu, guided);
+        if (m && (threadIdx.x & 31u) == (uint32_t)(__ffs(m) - 1)) atomicAdd(C.gFrame, (uint32_t)__popc(m));
+        warp_push(C.queue[(level + 1) & 1], C.counts + level + 1, push, id);
+    }
+}
+
+size_t guide_wave_bytes_per_path() {
+    return sizeof(uint32_t) + (9 + guide::kRaw + 18) * sizeof(float);
+}
+
 size_t wave_bytes_per_path() { return sizeof(WaveRec) + sizeof(NeeRec) + sizeof(Isec) + 1 + 3 * sizeof(uint32_t); }
 
 BatchShape fill_view_table(const BatchView* views, int n, void* hViews, unsigned long long* counters, int countWork) {
@@ -1390,6 +1632,11 @@ BatchShape fill_view_table(const BatchView* views, int n, void* hViews, unsigned
         e.G.b = bv.gb;
         e.G.counters = counters;
         e.G.countWork = countWork;
+        for (int c = 0; c < 3; c++) {
+            float ext = bv.scene.boxMax[c] - bv.scene.boxMin[c];
+            e.boxMin[c] = bv.scene.boxMin[c];
+            e.boxInv[c] = ext > 0.0f ? 1.0f / ext : 0.0f;
+        }
         e.tilesX = (bv.b.width + 15) / 16;
         e.tileBase = sh.tiles;
         e.pixelBase = sh.pixels;
@@ -1402,8 +1649,9 @@ BatchShape fill_view_table(const BatchView* views, int n, void* hViews, unsigned
 
 cudaError_t enqueue_batch(const BatchShape& sh, void* dViews, const void* hViews, const WaveBuffers& wb,
                           unsigned long long* counters, int countWork, KernelTimer* timer, cudaStream_t stream,
-                          int pathForm, int passes, const WaveLaunch& wl) {
+                          int pathForm, int passes, const WaveLaunch& wl, const guide::GuideDevice* guide) {
     const int n = sh.n;
+    if (guide && (pathForm != GRIS_PATH_WAVEFRONT || !wb.postQueue)) return cudaErrorInvalidValue;
     if (n <= 0 || n > 4096) return cudaErrorInvalidValue;
     if ((uint64_t)sh.pixels > wb.capacity && pathForm == GRIS_PATH_WAVEFRONT && (passes & 1)) return cudaErrorInvalidValue;
     cudaError_t e = cudaMemcpyAsync(dViews, hViews, sizeof(ViewEntry) * (size_t)n, cudaMemcpyHostToDevice, stream);
@@ -1430,7 +1678,11 @@ cudaError_t enqueue_batch(const BatchShape& sh, void* dViews, const void* hViews
             C.counts = wb.counts;
             C.counters = counters;
             C.countWork = countWork;
-            e = cudaMemsetAsync(wb.counts, 0, 512 * sizeof(uint32_t), stream);
+            C.postQueue = wb.postQueue;
+            C.gFeat = wb.gFeat; C.gOut = wb.gOut; C.gRec = wb.gRec; C.gFrame = wb.gFrame;
+            if (guide) C.guide = *guide; else memset(&C.guide, 0, sizeof(C.guide));
+            C.frameSeed = 0u;
+            e = cudaMemsetAsync(wb.counts, 0, 1024 * sizeof(uint32_t), stream);
             if (e != cudaSuccess) return e;
             static int sm = 0;
             if (sm == 0) { int dev = 0; cudaGetDevice(&dev); cudaDeviceGetAttribute(&sm, cudaDevAttrMultiProcessorCount, dev); }
@@ -1438,6 +1690,37 @@ cudaError_t enqueue_batch(const BatchShape& sh, void* dViews, const void* hViews
             const int gridTrace = sm * (wl.traceBlocksPerSM > 0 ? wl.traceBlocksPerSM : 16);
             /* timer slots 4..8: begin, extend, shade, shadow, post */
             auto mark = [&](int slot, bool begin) { if (timer) timer->mark(slot, begin, stream); };
+            if (guide) {
+                /* guided: every path continues through post(); guided vertices get the network's
+                 * mixture between the shading and post() (timer slot 9) */
+                k_guide_frame_begin<<<1, 1, 0, stream>>>(wb.gFrame, guide->tCount, guide->cap);
+                mark(4, true);
+                k_gwave_begin<<<(pixels + 127) / 128, 128, 0, stream>>>(C);
+                mark(4, false);
+                for (int level = 1; level < sh.maxDepth; level++) {
+                    mark(5, true);
+                    k_wave_extend<<<gridTrace, 128, 0, stream>>>(C, level);
+                    mark(5, false);
+                    mark(6, true);
+                    k_gwave_shade<<<gridShade, 128, 0, stream>>>(C, level);
+                    mark(6, false);
+                    mark(7, true);
+                    k_wave_shadow<<<gridTrace, 128, 0, stream>>>(C, level);
+                    mark(7, false);
+                    mark(9, true);
+                    guide::FwdArgs fa;
+                    fa.wPacked = guide->wPacked; fa.bias = guide->bias; fa.feat = wb.gFeat;
+                    fa.count = wb.counts + 768 + level; fa.n = (uint32_t)wb.capacity; fa.out = wb.gOut;
+                    e = guide::launch_forward(fa, stream);
+                    if (e != cudaSuccess) return e;
+                    mark(9, false);
+                    mark(8, true);
+                    k_gwave_post<<<gridShade, 128, 0, stream>>>(C, level);
+                    mark(8, false);
+                }
+                if (timer) timer->mark(1, false, stream);
+                goto reuse;
+            }
             mark(4, true);
             k_wave_begin<<<(pixels + 127) / 128, 128, 0, stream>>>(C);
             mark(4, false);
@@ -1460,6 +1743,7 @@ cudaError_t enqueue_batch(const BatchShape& sh, void* dViews, const void* hViews
         }
         if (timer) timer->mark(1, false, stream);
     }
+reuse:
     if (passes & 2) {
         if (timer) timer->mark(2, true, stream);
         k_batch_pass<TemporalTask, 2><<<tiles, blk, 0, stream>>>(V, n);
@@ -1478,7 +1762,7 @@ cudaError_t launch_batch(const BatchView* views, int n, void* dViews, void* hVie
                          int pathForm, int passes, const WaveLaunch& wl) {
     if (n <= 0 || n > 4096) return cudaErrorInvalidValue;
     BatchShape sh = fill_view_table(views, n, hViews, counters, countWork);
-    return enqueue_batch(sh, dViews, hViews, wb, counters, countWork, timer, stream, pathForm, passes, wl);
+    return enqueue_batch(sh, dViews, hViews, wb, counters, countWork, timer, stream, pathForm, passes, wl, nullptr);
 }
 
 }  // namespace grisrt

@@ -8,6 +8,7 @@
 #include <stdint.h>
 
 #include "../../include/grisrt.h"
+#include "guide_kernels.h"
 
 namespace grisrt {
 
@@ -22,6 +23,7 @@ struct DeviceSceneView {
     const GrisLightTableEntry* table; uint64_t nTable;
     const uint32_t* nodes;
     const float* tris;
+    float boxMin[3], boxMax[3];   /* bounds of the world-space triangles */
 };
 
 /* Receives a mark before (begin = true) and after each kernel launch, on the launch stream. */
@@ -61,9 +63,18 @@ struct WaveBuffers {
     unsigned char* blocked;
     uint32_t* queue[2];
     uint32_t* shadowQueue;
-    uint32_t* counts;   /* 512 words */
+    uint32_t* counts;   /* 1024 words */
     uint64_t capacity;
+    /* guided batches only (null otherwise): post queue, guide inputs / outputs per guided
+     * vertex, training record per path, frame state (4 words) */
+    uint32_t* postQueue;
+    float* gFeat;
+    float* gOut;
+    float* gRec;
+    uint32_t* gFrame;
 };
+/* bytes per path of the guided-batch buffers */
+size_t guide_wave_bytes_per_path();
 size_t wave_bytes_per_path();
 size_t view_entry_bytes();
 
@@ -86,7 +97,8 @@ BatchShape fill_view_table(const BatchView* views, int n, void* hViews, unsigned
  * GRIS_PATH_WAVEFRONT. Only stream operations: it can be captured into a CUDA graph. */
 cudaError_t enqueue_batch(const BatchShape& sh, void* dViews, const void* hViews, const WaveBuffers& wb,
                           unsigned long long* counters, int countWork, KernelTimer* timer, cudaStream_t stream,
-                          int pathForm, int passes, const WaveLaunch& wl);
+                          int pathForm, int passes, const WaveLaunch& wl,
+                          const guide::GuideDevice* guide = nullptr);
 cudaError_t launch_batch(const BatchView* views, int n, void* dViews, void* hViews, const WaveBuffers& wb,
                          unsigned long long* counters, int countWork, KernelTimer* timer, cudaStream_t stream,
                          int pathForm, int passes, const WaveLaunch& wl);

@@ -129,7 +129,7 @@ __global__ void __launch_bounds__(kGradWarps * 32, 1) k_guide_grad(GradArgs a) {
     __nv_bfloat16* hT = reinterpret_cast<__nv_bfloat16*>(warpBase + (size_t)warp * kWarpBytes);
     __nv_bfloat16* dzT = hT + kHtElems;
     float* ob = reinterpret_cast<float*>(dzT + kDzElems);
-    const uint32_t n = a.count ? min(*a.count, a.n) : a.n;
+    const uint32_t n = a.count ? min(max(*a.count, a.base) - a.base, a.n) : a.n;
     const float invSum = *a.invWeightSum;
     const uint32_t warps = gridDim.x * kGradWarps;
 
@@ -364,9 +364,10 @@ __global__ void k_guide_adam(float* __restrict__ params, float* __restrict__ gra
 __global__ void k_guide_step(uint32_t* step) { *step += 1u; }
 
 /* 1 / sum of the batch's sample weights (a fixed-order FP64 reduction in one block) */
-__global__ void __launch_bounds__(256) k_guide_weight_sum(const float* weight, const uint32_t* count, uint32_t n, float* invSum) {
+__global__ void __launch_bounds__(256) k_guide_weight_sum(const float* weight, const uint32_t* count, uint32_t base, uint32_t n,
+                                                          float* invSum) {
     __shared__ double part[256];
-    uint32_t m = count ? min(*count, n) : n;
+    uint32_t m = count ? min(max(*count, base) - base, n) : n;
     double s = 0.0;
     for (uint32_t i = threadIdx.x; i < m; i += 256) s += (double)weight[i];
     part[threadIdx.x] = s;
@@ -396,7 +397,7 @@ cudaError_t launch_grad(const GradArgs& a, cudaStream_t stream) {
         attr = true;
     }
     if (!a.invWeightSum) return cudaErrorInvalidValue;
-    k_guide_weight_sum<<<1, 256, 0, stream>>>(a.weight, a.count, a.n, a.invWeightSum);
+    k_guide_weight_sum<<<1, 256, 0, stream>>>(a.weight, a.count, a.base, a.n, a.invWeightSum);
     k_guide_grad<<<sm, kGradWarps * 32, kGradSmem, stream>>>(a);
     return cudaGetLastError();
 }

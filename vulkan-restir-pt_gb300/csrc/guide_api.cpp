@@ -62,7 +62,8 @@ cudaError_t guide_train_frame(GrisGuide* g, cudaStream_t st) {
         a.feat = g->tFeat + (size_t)s * per * 9;
         a.dir = g->tDir + (size_t)s * per * 3;
         a.weight = g->tWeight + (size_t)s * per;
-        a.count = nullptr;
+        a.count = g->tCount;
+        a.base = s * per;
         a.n = per;
         a.invWeightSum = g->invSum;
         a.grad = g->grad;
@@ -215,7 +216,7 @@ int grisGuideGradient(GrisContext* ctx, GrisGuide* g, const float* feat, const f
     if (n == 0) return GRIS_OK;
     guide::GradArgs a;
     a.wPacked = g->wPacked; a.bias = g->bias; a.feat = feat; a.dir = dir; a.weight = weight;
-    a.count = nullptr; a.n = n; a.invWeightSum = g->invSum; a.grad = gradOut;
+    a.count = nullptr; a.base = 0; a.n = n; a.invWeightSum = g->invSum; a.grad = gradOut;
     GUIDE_CK(ctx, guide::launch_grad(a, st));
     return GRIS_OK;
 }
@@ -227,7 +228,7 @@ int grisGuideTrainStep(GrisContext* ctx, GrisGuide* g, const float* feat, const 
     if (n) {
         guide::GradArgs a;
         a.wPacked = g->wPacked; a.bias = g->bias; a.feat = feat; a.dir = dir; a.weight = weight;
-        a.count = nullptr; a.n = n; a.invWeightSum = g->invSum; a.grad = g->grad;
+        a.count = nullptr; a.base = 0; a.n = n; a.invWeightSum = g->invSum; a.grad = g->grad;
         GUIDE_CK(ctx, guide::launch_grad(a, st));
     }
     GUIDE_CK(ctx, guide::launch_adam(g->params, g->grad, g->m, g->v, g->step, g->cfg.learningRate, st));

@@ -25,7 +25,8 @@ struct GradArgs {
     const float* feat;
     const float* dir;
     const float* weight;
-    const uint32_t* count;
+    const uint32_t* count;     /* optional device count of the whole record array: samples = */
+    uint32_t base;             /* min(max(*count, base) - base, n), from feat/dir/weight (already offset) */
     uint32_t n;
     float* invWeightSum;       /* device scalar: written here from the weights, then read */
     float* grad;

@@ -129,7 +129,7 @@ class KernelProfile(ctypes.Structure):
 
 
 PROFILE_SLOTS = ["gbuffer", "path_trace", "temporal", "spatial", "wave_begin", "wave_extend", "wave_shade",
-                 "wave_shadow", "wave_post"]
+                 "wave_shadow", "wave_post", "guide_infer", "guide_train"]
 
 
 class TuneResult(ctypes.Structure):
@@ -148,7 +148,7 @@ EXPORTS = [
     "grisBatchDownload", "grisSetGraphs", "grisSetWaveLaunch", "grisBatchAutotune",
     "grisReadKernelProfile", "grisConvergedAccumulate", "grisRelMSE",
     "grisGuideCreate", "grisGuideDestroy", "grisGuideParamCount", "grisGuideSetParams", "grisGuideGetParams",
-    "grisGuideSetTraining", "grisGuideForward", "grisGuideGradient", "grisGuideTrainStep",
+    "grisGuideSetTraining", "grisGuideForward", "grisGuideGradient", "grisGuideTrainStep", "grisBatchSetGuide",
 ]
 
 _lib = None
@@ -218,6 +218,7 @@ def load(path=None):
         "grisGuideForward": (i32, [vp, vp, vp, u32, vp]),
         "grisGuideGradient": (i32, [vp, vp, vp, vp, vp, u32, vp]),
         "grisGuideTrainStep": (i32, [vp, vp, vp, vp, vp, u32]),
+        "grisBatchSetGuide": (i32, [vp, vp]),
         "grisConvergedAccumulate": (i32, [vp, vp, ctypes.POINTER(ConvergedBindings), ctypes.POINTER(Camera),
                                           ctypes.POINTER(Settings), u32, u32, i32]),
         "grisRelMSE": (i32, [vp, vp, vp, ctypes.c_double, u64, ctypes.c_double, ctypes.POINTER(ctypes.c_double)]),
@@ -607,6 +608,11 @@ class Batch:
         p = (Camera * n)(*prev_cams)
         s = (Settings * n)(*settings)
         self.ctx.check(load().grisBatchRender(self.ctx.h, self.handle, c, p, s), "grisBatchRender")
+
+    def set_guide(self, guide):
+        """Attaches a Guide (None detaches): guided path sampling, and training if the guide trains."""
+        self.guide = guide
+        self.ctx.check(load().grisBatchSetGuide(self.handle, guide.h if guide is not None else None), "grisBatchSetGuide")
 
     def autotune(self, cams, prev_cams, settings, frames=3):
         """Times the candidate launch configurations on these views (rendering frames), keeps the
