@@ -49,6 +49,7 @@ for p in (PKG, REPO):
 METRICS = {
     "c2": "ReSTIR PT frames/s at 1080p (1.16M-tri synthetic scene, depth 8, temporal+spatial reuse)",
     "c3": "Batched ReSTIR PT frames/s (64 views of {64..512}^2, 10k-200k tris each, depth 2-10)",
+    "c4": "Guided / plain ReSTIR PT time to equal relMSE (1080p glossy scene, depth 8, accumulating frames)",
 }
 UNIT = "frames/s"
 NODE_BYTES, TRI_BYTES = 80, 48
@@ -93,7 +94,10 @@ def parse():
     ap.add_argument("--steps", type=int, default=30)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="grisrt", choices=["grisrt", "reference"])
-    ap.add_argument("--workload", default="c2", choices=["c2", "c3"])
+    ap.add_argument("--workload", default="c2", choices=["c2", "c3", "c4"])
+    ap.add_argument("--ref-spp", type=int, default=1024, help="c4: samples per pixel of the converged image")
+    ap.add_argument("--c4-reuse", default="on", choices=["on", "off"],
+                    help="c4: temporal + spatial reuse on (ReSTIR PT) or off (the canonical samples alone)")
     ap.add_argument("--width", type=int, default=1920)
     ap.add_argument("--height", type=int, default=1080)
     ap.add_argument("--grid", type=int, default=512)
@@ -188,8 +192,8 @@ def make_views(args, frames):
                                maxDepth=depth, spatialNeighbors=3, spatialRadius=20.0)
     common = {"spatial_neighbors": 3, "spatial_radius_px": 20.0, "cap": 20, "shift": "hybrid",
               "l2": "flushed between frames (256 MiB write outside the timed events)"}
-    if args.workload == "c2":
-        hs = G.HostScene(1, seed=args.seed, grid=args.grid, spheres=args.spheres)
+    if args.workload in ("c2", "c4"):
+        hs = G.HostScene(2 if args.workload == "c4" else 1, seed=args.seed, grid=args.grid, spheres=args.spheres)
         views = [View(hs, args.width, args.height, settings(args.depth), frames, args.seed)]
         config = {"workload": "C2: %dx%d, %d^2 fBm heightfield + %d icospheres (%d tris), depth %d, orbit" % (
             args.width, args.height, args.grid, args.spheres, hs.triangle_count(), args.depth),
@@ -263,6 +267,133 @@ def cpu_oracle_run(views, target_seconds, frames=2, ora=None, plan=None):
     return fps, threads, sample, rays / t_sample, plan, ora
 
 
+def run_guided(args):
+    """c4: plain and guided ReSTIR PT on the glossy scene, each accumulating frames (static camera)
+    from a cold start; the relMSE of the running mean against a converged image (FP64 sums of
+    independent paths, --ref-spp per pixel) after every frame, and each frame's device time. The
+    value is the guided run's time to reach the plain run's final relMSE over the plain run's
+    time (lower is better; the guide's training from scratch is inside the guided time)."""
+    import torch
+    import grisrt as G
+    W, H, F = args.width, args.height, args.steps
+    ctx = G.Context(0)
+    ctx.set_path_form(G.PATH_WAVEFRONT)
+    hs = G.HostScene(2, seed=args.seed, grid=args.grid, spheres=args.spheres)
+    scene = G.Scene(ctx, hs)
+    reuse = args.c4_reuse == "on"
+    st = G.Settings.make(shiftType=2, rrScale=1.0, temporalReuse=reuse, spatialReuse=reuse, cap=20,
+                         maxDepth=args.depth, spatialNeighbors=3, spatialRadius=20.0)
+    stream = torch.cuda.ExternalStream(ctx.stream(), device=torch.device("cuda", 0))
+    cam0 = hs.camera(0, 60, W, H)
+    cams, prevs = [], []
+    for f in range(F + 4):
+        c = cam0.copy()
+        c.seed = G.frame_seed(args.seed, f)
+        ctypes.memmove(c.lastProjView, cam0.projView, 64)
+        c.frameIndex = G.CLEAR_FLAG if f == 0 else f
+        cams.append(c)
+        prevs.append(cam0.copy())
+    # converged image
+    n = W * H
+    dn = torch.zeros((n, 4), dtype=torch.float32, device="cuda")
+    am = torch.zeros((n, 2), dtype=torch.int32, device="cuda")
+    mv = torch.zeros((n, 2), dtype=torch.int16, device="cuda")
+    gb = G.GBufferBindings(W, H, dn.data_ptr(), am.data_ptr(), mv.data_ptr())
+    lib = G.load()
+    ctx.check(lib.grisPassGBuffer(ctx.h, scene.h, ctypes.byref(gb), ctypes.byref(cam0)), "grisPassGBuffer")
+    ref = torch.zeros(n * 3, dtype=torch.float64, device="cuda")
+    t0 = time.perf_counter()
+    for k in range(0, args.ref_spp, 32):
+        scene.converged(cam0, st, W, H, dn.data_ptr(), am.data_ptr(), ref.data_ptr(), None, spp_begin=k,
+                        spp=min(32, args.ref_spp - k), estimator=G.ESTIMATOR_CANDIDATES)
+    ctx.sync()
+    ref_s = time.perf_counter() - t0
+    scale = 1.0 / args.ref_spp
+    import numpy as np
+    ref_host = ref.cpu().numpy().reshape(-1, 3) * scale
+    fg = ref_host.sum(axis=1) > 0
+
+    def run(guided):
+        batch = G.Batch(ctx, [scene], [(W, H)])
+        guide = None
+        if guided:
+            guide = G.Guide(ctx, G.GuideConfig.make(seed=args.seed, samplesPerFrame=1 << 18, stepsPerFrame=4,
+                                                    learningRate=1e-3, mix=0.5))
+            batch.set_guide(guide)
+        out_ptr, _ = batch.device_ptr(0, G.BUF_OUTPUT)
+        times, rel, med = [], [], []
+        with torch.cuda.stream(stream):
+            for f in range(F):
+                e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                e0.record(stream)
+                batch.render([cams[f]], [prevs[f]], [st])
+                e1.record(stream)
+                rel.append(ctx.relmse(out_ptr, ref.data_ptr(), scale, n)[0])
+                times.append(e0.elapsed_time(e1))
+                img = batch.download(0, G.BUF_OUTPUT)[:, :3].astype(np.float64)
+                e = np.mean((img - ref_host) ** 2 / (ref_host ** 2 + 1e-2), axis=1)
+                med.append(float(np.median(e[fg])))
+        # one profiled frame: the network's share of a frame
+        ctx.set_profiling(True)
+        ctx.kernel_profile(reset=True)
+        batch.render([cams[F]], [prevs[F]], [st])
+        ctx.sync()
+        prof = ctx.kernel_profile(reset=True)
+        ctx.set_profiling(False)
+        batch.close()
+        if guide is not None:
+            guide.close()
+        total = sum(prof[k]["ms"] for k in ("gbuffer", "path_trace", "temporal", "spatial")) + prof["guide_train"]["ms"]
+        mlp = prof["guide_infer"]["ms"] + prof["guide_train"]["ms"]
+        return np.array(times), np.array(rel), np.array(med), {"frame_ms": total, "mlp_ms": mlp,
+                                                               "mlp_share": mlp / total if total > 0 else 0.0}
+
+    tp, rp, mp, pp = run(False)
+    tg, rg, mg, pg = run(True)
+    Tp = tp.sum()
+    cg = np.cumsum(tg)
+
+    def time_to(curve_g, target):
+        """guided time (ms) to first reach `target` on its error curve (log-linear crossing)"""
+        hit = np.nonzero(curve_g <= target)[0]
+        if not len(hit):
+            return None
+        f = int(hit[0])
+        if f > 0 and curve_g[f - 1] > target:
+            a = (np.log(curve_g[f - 1]) - np.log(target)) / (np.log(curve_g[f - 1]) - np.log(curve_g[f]))
+            return float(cg[f - 1] + a * (cg[f] - cg[f - 1]))
+        return float(cg[f])
+
+    Tg = time_to(rg, rp[-1])
+    ratio = Tg / Tp if Tg is not None else None
+    Tg_med = time_to(mg, mp[-1])
+    ratio_med = Tg_med / Tp if Tg_med is not None else None
+    # guided error at the plain run's total time
+    k = min(int(np.searchsorted(cg, Tp)), F - 1)
+    rel_equal_time = float(rg[k])
+    line = {"metric": METRICS["c4"], "value": ratio, "unit": "x", "n_gpus": 1, "steps": F, "warmup": 0,
+            "ms_per_step": float(tg.mean()), "higher_is_better": False, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f32 paths, bf16 network", "data": "synthetic (seeded scene generator, no dataset)",
+            "config": {"workload": "C4: %dx%d glossy variant (%d tris), depth %d, temporal+spatial reuse, static camera, "
+                                   "frames accumulated" % (W, H, hs.triangle_count(), args.depth),
+                       "guide": "MLP 80-64x4-48 BF16 mma.sync, 8 vMF lobes, mix 0.5, Adam 1e-3, 2^18 records/frame, 4 steps"},
+            "reference": {"spp": args.ref_spp, "seconds": ref_s, "estimator": "candidates"},
+            "reuse": reuse,
+            "median_error_time_ratio": ratio_med,
+            "plain": {"fps": 1000.0 / float(tp.mean()), "total_ms": float(Tp), "relmse_final": float(rp[-1]),
+                      "median_final": float(mp[-1]), "relmse_curve": [float(x) for x in rp],
+                      "median_curve": [float(x) for x in mp], "profile": pp},
+            "guided": {"fps": 1000.0 / float(tg.mean()), "total_ms": float(cg[-1]), "relmse_final": float(rg[-1]),
+                       "median_final": float(mg[-1]), "relmse_at_plain_time": rel_equal_time,
+                       "median_at_plain_time": float(mg[k]), "relmse_curve": [float(x) for x in rg],
+                       "median_curve": [float(x) for x in mg], "profile": pg},
+            "gpu_launches": None}
+    print(json.dumps(line))
+    scene.close()
+    ctx.close()
+    return 0
+
+
 def main():
     args = parse()
     rank = int(os.environ.get("RANK", "0"))
@@ -271,6 +402,8 @@ def main():
     K, WU = args.steps, max(args.warmup, 0)
     if args.workload == "c3":
         args.api = "batch"
+    if args.workload == "c4" and args.impl != "reference":
+        return run_guided(args)
     import grisrt as G
     metric = METRICS[args.workload]
 
