@@ -47,6 +47,7 @@ for p in (PKG, REPO):
         sys.path.insert(0, p)
 
 METRICS = {
+    "c1": "ReSTIR PT frames/s at 256x256 (box scene, 24 triangles + light, depth 3, temporal+spatial reuse)",
     "c2": "ReSTIR PT frames/s at 1080p (1.16M-tri synthetic scene, depth 8, temporal+spatial reuse)",
     "c3": "Batched ReSTIR PT frames/s (64 views of {64..512}^2, 10k-200k tris each, depth 2-10)",
     "c4": "Guided / plain ReSTIR PT time to equal relMSE (1080p glossy scene, depth 8, accumulating frames)",
@@ -94,7 +95,7 @@ def parse():
     ap.add_argument("--steps", type=int, default=30)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="grisrt", choices=["grisrt", "reference"])
-    ap.add_argument("--workload", default="c2", choices=["c2", "c3", "c4"])
+    ap.add_argument("--workload", default="c2", choices=["c1", "c2", "c3", "c4"])
     ap.add_argument("--ref-spp", type=int, default=1024, help="c4: samples per pixel of the converged image")
     ap.add_argument("--c4-reuse", default="on", choices=["on", "off"],
                     help="c4: temporal + spatial reuse on (ReSTIR PT) or off (the canonical samples alone)")
@@ -192,6 +193,16 @@ def make_views(args, frames):
                                maxDepth=depth, spatialNeighbors=3, spatialRadius=20.0)
     common = {"spatial_neighbors": 3, "spatial_radius_px": 20.0, "cap": 20, "shift": "hybrid",
               "l2": "flushed between frames (256 MiB write outside the timed events)"}
+    if args.workload == "c1":
+        hs = G.HostScene(0, seed=args.seed)
+        st = G.Settings.make(shiftType=2, rrScale=1.0, temporalReuse=True, spatialReuse=True, cap=20, maxDepth=3,
+                             spatialNeighbors=3, spatialRadius=30.0)
+        views = [View(hs, 256, 256, st, frames, args.seed)]
+        config = {"workload": "C1: 256x256 box (%d tris), depth 3, static camera" % hs.triangle_count(),
+                  "width": 256, "height": 256, "triangles": hs.triangle_count(), "max_depth": 3}
+        config.update(common)
+        config["spatial_radius_px"] = 30.0
+        return views, config
     if args.workload in ("c2", "c4"):
         hs = G.HostScene(2 if args.workload == "c4" else 1, seed=args.seed, grid=args.grid, spheres=args.spheres)
         views = [View(hs, args.width, args.height, settings(args.depth), frames, args.seed)]
