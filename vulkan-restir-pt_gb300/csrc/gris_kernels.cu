@@ -57,9 +57,18 @@ GD bool traceShadow(const DevScene& sc, V3 o, float tmin, V3 d, float tmax, RayC
     GrisRayHit h;
     return gris_bvh_trace<true>(sc.nodes, sc.tris, o.x, o.y, o.z, d.x, d.y, d.z, tmin, tmax, false, &h, &err, &rc.work);
 }
+/* The same queries as out-of-line calls, for the reuse passes: there the traversal loop would be
+ * inlined at three call sites of one kernel, and the one shared copy runs faster (fewer
+ * instruction-fetch stalls); the path tracer keeps the inlined form. */
+__device__ __noinline__ Isec traceClosestHitCall(const DevScene& sc, V3 o, V3 d, float tmin, float tmax, RayCount& rc, int& err) {
+    return traceClosestHit(sc, o, d, tmin, tmax, rc, err);
+}
+__device__ __noinline__ bool traceShadowCall(const DevScene& sc, V3 o, float tmin, V3 d, float tmax, RayCount& rc, int& err) {
+    return traceShadow(sc, o, tmin, d, tmax, rc, err);
+}
 /* ray_query.glsl:29-39 */
 GD bool traceVisibility(const DevScene& sc, V3 from, V3 to, RayCount& rc, int& err) {
-    return !traceShadow(sc, from, kMinRayDistance, normalize3(to - from), distance3(to, from) - kMinRayDistance, rc, err);
+    return !traceShadowCall(sc, from, kMinRayDistance, normalize3(to - from), distance3(to, from) - kMinRayDistance, rc, err);
 }
 
 /* counters: [0] closest, [1] shadow, [2] primary, [3] error word,
@@ -422,7 +431,7 @@ GD void traceReplay(const PassCtx& P, Isec isec, Surf surf, Ray3 ray, uint32_t t
     const int maxDepth = (int)P.set.maxDepth;
     for (int bounce = 0; bounce < maxDepth; bounce++) {
         if (bounce > 0) {
-            isec = traceClosestHit(sc, ray.ori, ray.dir, kMinRayDistance, kMaxRayDistance, rc, err);
+            isec = traceClosestHitCall(sc, ray.ori, ray.dir, kMinRayDistance, kMaxRayDistance, rc, err);
             if (isec.inst == kInvalidHit) break;
             loadSurfaceInfo(sc, isec, surf);
             mat = load_material(sc, surf.matIndex);
