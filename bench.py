@@ -89,6 +89,22 @@ def alg_bytes(slot, w, px):
     return 0
 
 
+def max_over_ranks(x, device):
+    """The maximum of a per-rank scalar over the process group (x itself on one rank)."""
+    import torch
+    import torch.distributed as dist
+    if not dist.is_available() or not dist.is_initialized() or dist.get_world_size() == 1:
+        return float(x)
+    t = torch.tensor([float(x)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def aggregate_rate(units_per_rank, seconds_max, world):
+    """Whole-job rate of replicas: every rank processed `units_per_rank` in at most `seconds_max`."""
+    return world * units_per_rank / seconds_max
+
+
 def parse():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -520,12 +536,8 @@ def main():
     ms = sum(a.elapsed_time(b) for a, b in events)
     cnt = ctx.counters(reset=True)
     ctx.sync()
-    t_max = ms
-    if world > 1:
-        t = torch.tensor([ms], device="cuda")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        t_max = float(t.item())
-    value = world * K / (t_max / 1000.0)
+    t_max = max_over_ranks(ms, "cuda")
+    value = aggregate_rate(K, t_max / 1000.0, world)
     rays = cnt[0] + cnt[1] + cnt[2]
     mrays = world * rays / (t_max / 1000.0) / 1e6
 
@@ -575,12 +587,8 @@ def main():
                                                 v.w * v.h * 16), "grisFrameDownload")
         fi += 1
     barrier()
-    e2e_s = time.perf_counter() - t0
-    if world > 1:
-        t = torch.tensor([e2e_s], device="cuda")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        e2e_s = float(t.item())
-    e2e = {"value": world * K / e2e_s, "unit": UNIT, "h2d_bytes_per_step": n * (2 * 352 + 64),
+    e2e_s = max_over_ranks(time.perf_counter() - t0, "cuda")
+    e2e = {"value": aggregate_rate(K, e2e_s, world), "unit": UNIT, "h2d_bytes_per_step": n * (2 * 352 + 64),
            "d2h_bytes_per_step": px * 16}
 
     # ---------------- roofline of the kernel with the largest share
