@@ -260,6 +260,13 @@ int grisHostSceneDesc(const GrisHostScene* hs, GrisSceneDesc* out);
 int grisHostSceneCamera(const GrisHostScene* hs, uint32_t frame, uint32_t frames, uint32_t width,
                         uint32_t height, GrisCamera* out);
 int grisHostSceneDestroy(GrisHostScene* hs);
+/* A scene in the reference's XML scene format (src/Scene.cpp:131-303) with Wavefront OBJ meshes:
+ * integrator size, camera (position + angle or lookAt, fov), model instances with transforms,
+ * light radiance (power over the light's area) and material overrides. errBuf (optional)
+ * receives a message on failure. The camera comes from grisHostSceneCamera; the film size
+ * given by the file from grisHostSceneFilmSize (0 x 0 when absent). */
+int grisHostSceneLoad(const char* path, GrisHostScene** out, char* errBuf, size_t errLen);
+int grisHostSceneFilmSize(const GrisHostScene* hs, uint32_t* width, uint32_t* height);
 
 /* ---------------------------------------------------------------- converged image */
 /* The converged image the GRIS path converges to, for quality measurement (relMSE): per pixel,

@@ -6,11 +6,18 @@
  * deterministic transcendental functions of detmath.h, so a scene and a camera built on an
  * x86-64 host and on an aarch64 host are byte-identical.
  */
+#include <ctype.h>
 #include <math.h>
 #include <stdint.h>
+#include <stdio.h>
+#include <stdlib.h>
 #include <string.h>
 
 #include <algorithm>
+#include <map>
+#include <memory>
+#include <string>
+#include <tuple>
 #include <vector>
 
 #include "../../include/grisrt.h"
@@ -213,6 +220,10 @@ struct GrisHostScene {
     float center[3] = {0, 0, 0};
     float orbitRadius = 1.0f, orbitHeight = 0.0f, fov = 60.0f;
     float camPos[3] = {0, 0, 0}, camAngle[3] = {0, 0, 0};
+    /* scenes loaded from a scene file */
+    bool camLookAt = false;
+    float camTarget[3] = {0, 0, 0};
+    uint32_t filmW = 0, filmH = 0;
 };
 
 namespace {
@@ -558,6 +569,7 @@ extern "C" int grisHostSceneDesc(const GrisHostScene* s, GrisSceneDesc* d) {
 extern "C" int grisHostSceneCamera(const GrisHostScene* s, uint32_t frame, uint32_t frames, uint32_t width,
                                    uint32_t height, GrisCamera* out) {
     if (!s || !out) return GRIS_ERR_INVALID_ARGUMENT;
+    if (s->camLookAt) return grisCameraLookAt(out, s->camPos, s->camTarget, s->fov, width, height);
     if (s->orbitRadius <= 0.0f) return grisCameraSetup(out, s->camPos, s->camAngle, s->fov, width, height);
     float a = 0.7853982f + 1.5707964f * (float)frame / (float)(frames > 1 ? frames : 1);
     float sa, ca;
@@ -569,5 +581,445 @@ extern "C" int grisHostSceneCamera(const GrisHostScene* s, uint32_t frame, uint3
 
 extern "C" int grisHostSceneDestroy(GrisHostScene* s) {
     delete s;
+    return GRIS_OK;
+}
+
+/* ------------------------------------------------------------------ scene files */
+/* The reference's scene description (src/Scene.cpp:131-303, src/Material.cpp:5-70): an XML
+ * document <scene> with <integrator><size width height/></integrator>, <camera> (<position
+ * value="x y z"/>, <angle value="yaw pitch roll"/> or <lookAt value="x y z"/>, <fov value/>),
+ * and <modelInstances> whose children name a mesh file (path relative to the scene file), a
+ * <transform translate scale rotate/> (model matrix as src/Model.cpp:11-21: translate, rotate
+ * rot.x about z, rot.y + 90 degrees about x, rot.z about y, scale (s.x, s.z, s.y)), for
+ * type="light" a <radiance value/> (the light's power, spread over its world-space area) and an
+ * optional flip="true", and otherwise an optional <material type=...> overriding the mesh's
+ * materials (lambertian, metalWorkflow, metal, dielectric, thinDielectric, fake; "default"
+ * keeps the mesh file's) with <baseColor value/>, <metallic/>, <roughness/>, <ior/>.
+ * Meshes are Wavefront OBJ (+ MTL diffuse colours), read by a small loader standing in for the
+ * reference's assimp import: polygons fan-triangulated, a vertex per face corner, texture v
+ * flipped, missing normals generated (objects: the mean of the unit face normals at each
+ * position; lights: flat). Image textures are rejected (the GRIS kernels read base colours). */
+namespace {
+
+struct XmlNode {
+    std::string name;
+    std::vector<std::pair<std::string, std::string>> attrs;
+    std::vector<XmlNode> kids;
+    const char* attr(const char* k) const {
+        for (auto& a : attrs) if (a.first == k) return a.second.c_str();
+        return nullptr;
+    }
+    const XmlNode* child(const char* k) const {
+        for (auto& c : kids) if (c.name == k) return &c;
+        return nullptr;
+    }
+};
+
+struct XmlParser {
+    const std::string& t;
+    size_t i = 0;
+    std::string err;
+    explicit XmlParser(const std::string& text) : t(text) {}
+    void ws() { while (i < t.size() && isspace((unsigned char)t[i])) i++; }
+    bool starts(const char* p) const { return t.compare(i, strlen(p), p) == 0; }
+    bool skip_misc() {   /* comments, processing instructions, doctype, text */
+        for (;;) {
+            while (i < t.size() && t[i] != '<') i++;
+            if (i >= t.size()) return false;
+            if (starts("<!--")) { size_t e = t.find("-->", i); if (e == std::string::npos) return false; i = e + 3; continue; }
+            if (starts("<?") || starts("<!")) { size_t e = t.find('>', i); if (e == std::string::npos) return false; i = e + 1; continue; }
+            return true;
+        }
+    }
+    static std::string unescape(const std::string& v) {
+        std::string r;
+        for (size_t k = 0; k < v.size(); k++) {
+            if (v[k] == '&') {
+                static const char* ent[][2] = {{"&amp;", "&"}, {"&lt;", "<"}, {"&gt;", ">"}, {"&quot;", "\""}, {"&apos;", "'"}};
+                bool done = false;
+                for (auto& e : ent)
+                    if (v.compare(k, strlen(e[0]), e[0]) == 0) { r += e[1]; k += strlen(e[0]) - 1; done = true; break; }
+                if (!done) r += v[k];
+            } else {
+                r += v[k];
+            }
+        }
+        return r;
+    }
+    bool element(XmlNode& n, int depth) {
+        if (depth > 64) { err = "nesting too deep"; return false; }
+        if (!skip_misc() || t[i] != '<') { err = "expected an element"; return false; }
+        i++;
+        size_t b = i;
+        while (i < t.size() && !isspace((unsigned char)t[i]) && t[i] != '>' && t[i] != '/') i++;
+        n.name = t.substr(b, i - b);
+        for (;;) {
+            ws();
+            if (i >= t.size()) { err = "unterminated tag"; return false; }
+            if (t[i] == '/') { if (i + 1 < t.size() && t[i + 1] == '>') { i += 2; return true; } err = "bad tag end"; return false; }
+            if (t[i] == '>') { i++; break; }
+            size_t k = i;
+            while (i < t.size() && t[i] != '=' && !isspace((unsigned char)t[i])) i++;
+            std::string key = t.substr(k, i - k);
+            ws();
+            if (i >= t.size() || t[i] != '=') { err = "attribute without value"; return false; }
+            i++;
+            ws();
+            if (i >= t.size() || (t[i] != '"' && t[i] != '\'')) { err = "unquoted attribute"; return false; }
+            char q = t[i++];
+            size_t e = t.find(q, i);
+            if (e == std::string::npos) { err = "unterminated attribute"; return false; }
+            n.attrs.push_back({key, unescape(t.substr(i, e - i))});
+            i = e + 1;
+        }
+        for (;;) {
+            if (!skip_misc()) { err = "unterminated element " + n.name; return false; }
+            if (starts("</")) {
+                size_t e = t.find('>', i);
+                if (e == std::string::npos) { err = "bad closing tag"; return false; }
+                i = e + 1;
+                return true;
+            }
+            n.kids.emplace_back();
+            if (!element(n.kids.back(), depth + 1)) return false;
+        }
+    }
+};
+
+bool read_file(const std::string& path, std::string& out) {
+    FILE* f = fopen(path.c_str(), "rb");
+    if (!f) return false;
+    char buf[65536];
+    size_t n;
+    while ((n = fread(buf, 1, sizeof(buf), f)) > 0) out.append(buf, n);
+    fclose(f);
+    return true;
+}
+
+std::string dir_of(const std::string& p) {
+    size_t k = p.find_last_of('/');
+    return k == std::string::npos ? std::string(".") : p.substr(0, k);
+}
+
+bool parse_floats(const char* v, float* out, int n) {
+    if (!v) return false;
+    const char* p = v;
+    for (int k = 0; k < n; k++) {
+        char* e = nullptr;
+        double d = strtod(p, &e);
+        if (e == p) return false;
+        out[k] = (float)d;
+        p = e;
+    }
+    return true;
+}
+
+struct ObjMesh {            /* one material group of an OBJ file, a vertex per face corner */
+    std::vector<GrisMeshVertex> verts;
+    int material = -1;      /* index into ObjModel::materials, or -1 */
+};
+struct ObjModel {
+    std::vector<ObjMesh> meshes;
+    std::vector<H3> materials;   /* MTL diffuse colours */
+};
+
+bool load_mtl(const std::string& path, std::vector<std::string>& names, std::vector<H3>& kd) {
+    std::string text;
+    if (!read_file(path, text)) return false;
+    size_t pos = 0;
+    while (pos < text.size()) {
+        size_t e = text.find('\n', pos);
+        std::string line = text.substr(pos, e == std::string::npos ? std::string::npos : e - pos);
+        pos = e == std::string::npos ? text.size() : e + 1;
+        char word[64] = {0};
+        if (sscanf(line.c_str(), "%63s", word) != 1) continue;
+        if (!strcmp(word, "newmtl")) {
+            char name[256] = {0};
+            sscanf(line.c_str(), "%*s %255s", name);
+            names.push_back(name);
+            kd.push_back(h3(0.6f, 0.6f, 0.6f));
+        } else if (!strcmp(word, "Kd") && !kd.empty()) {
+            float c[3];
+            if (sscanf(line.c_str(), "%*s %f %f %f", &c[0], &c[1], &c[2]) == 3) kd.back() = h3(c[0], c[1], c[2]);
+        }
+    }
+    return true;
+}
+
+bool load_obj(const std::string& path, bool light, ObjModel& m, std::string& err) {
+    std::string text;
+    if (!read_file(path, text)) { err = "cannot read " + path; return false; }
+    std::vector<H3> P, N;
+    std::vector<float> UV;
+    std::vector<std::string> mtlNames;
+    std::vector<H3> mtlKd;
+    int current = -1;
+    m.meshes.emplace_back();
+    std::vector<std::vector<int>> hasN(1);
+    size_t pos = 0;
+    while (pos < text.size()) {
+        size_t e = text.find('\n', pos);
+        std::string line = text.substr(pos, e == std::string::npos ? std::string::npos : e - pos);
+        pos = e == std::string::npos ? text.size() : e + 1;
+        const char* c = line.c_str();
+        while (*c == ' ' || *c == '\t') c++;
+        if (c[0] == 'v' && (c[1] == ' ' || c[1] == '\t')) {
+            float v[3] = {0, 0, 0};
+            sscanf(c + 1, "%f %f %f", &v[0], &v[1], &v[2]);
+            P.push_back(h3(v[0], v[1], v[2]));
+        } else if (c[0] == 'v' && c[1] == 'n') {
+            float v[3] = {0, 0, 0};
+            sscanf(c + 2, "%f %f %f", &v[0], &v[1], &v[2]);
+            N.push_back(h3(v[0], v[1], v[2]));
+        } else if (c[0] == 'v' && c[1] == 't') {
+            float v[2] = {0, 0};
+            sscanf(c + 2, "%f %f", &v[0], &v[1]);
+            UV.push_back(v[0]); UV.push_back(v[1]);
+        } else if (!strncmp(c, "mtllib", 6)) {
+            char name[512] = {0};
+            if (sscanf(c + 6, "%511s", name) == 1) load_mtl(dir_of(path) + "/" + name, mtlNames, mtlKd);
+        } else if (!strncmp(c, "usemtl", 6)) {
+            char name[256] = {0};
+            sscanf(c + 6, "%255s", name);
+            int idx = -1;
+            for (size_t k = 0; k < mtlNames.size(); k++) if (mtlNames[k] == name) idx = (int)k;
+            if (idx != current) {
+                current = idx;
+                if (!m.meshes.back().verts.empty()) { m.meshes.emplace_back(); hasN.emplace_back(); }
+                m.meshes.back().material = idx;
+            }
+        } else if (c[0] == 'f' && (c[1] == ' ' || c[1] == '\t')) {
+            struct Corner { int p, t, n; };
+            std::vector<Corner> poly;
+            const char* q = c + 1;
+            for (;;) {
+                while (*q == ' ' || *q == '\t') q++;
+                if (!*q || *q == '\r') break;
+                Corner k = {0, 0, 0};
+                char* endp = nullptr;
+                k.p = (int)strtol(q, &endp, 10);
+                q = endp;
+                if (*q == '/') {
+                    q++;
+                    if (*q != '/') { k.t = (int)strtol(q, &endp, 10); q = endp; }
+                    if (*q == '/') { q++; k.n = (int)strtol(q, &endp, 10); q = endp; }
+                }
+                while (*q && *q != ' ' && *q != '\t') q++;
+                auto fix = [](int i, size_t n) { return i < 0 ? (int)n + i : i - 1; };   /* 1-based or negative */
+                k.p = fix(k.p, P.size());
+                k.t = k.t ? fix(k.t, UV.size() / 2) : -1;
+                k.n = k.n ? fix(k.n, N.size()) : -1;
+                if (k.p < 0 || k.p >= (int)P.size() || k.t >= (int)(UV.size() / 2) || k.n >= (int)N.size()) {
+                    err = path + ": face index out of range";
+                    return false;
+                }
+                poly.push_back(k);
+            }
+            for (size_t j = 1; j + 1 < poly.size(); j++) {
+                const Corner tri[3] = {poly[0], poly[j], poly[j + 1]};
+                H3 fn = hcross(P[tri[1].p] - P[tri[0].p], P[tri[2].p] - P[tri[0].p]);
+                float fl = hlen(fn);
+                fn = fl > 0.0f ? fn * (1.0f / fl) : h3(0, 0, 1);
+                for (const Corner& k : tri) {
+                    GrisMeshVertex v;
+                    v.pos[0] = P[k.p].x; v.pos[1] = P[k.p].y; v.pos[2] = P[k.p].z;
+                    H3 n = k.n >= 0 ? N[k.n] : fn;
+                    v.norm[0] = n.x; v.norm[1] = n.y; v.norm[2] = n.z;
+                    v.uvx = k.t >= 0 ? UV[2 * k.t] : 0.0f;
+                    v.uvy = k.t >= 0 ? 1.0f - UV[2 * k.t + 1] : 0.0f;
+                    m.meshes.back().verts.push_back(v);
+                    hasN.back().push_back(k.n >= 0 ? 1 : 0);
+                }
+            }
+        }
+    }
+    if (m.meshes.back().verts.empty() && m.meshes.size() > 1) { m.meshes.pop_back(); hasN.pop_back(); }
+    if (!light) {
+        /* smooth normals where the file has none: the mean of the unit face normals at each position */
+        for (size_t mi = 0; mi < m.meshes.size(); mi++) {
+            auto& V = m.meshes[mi].verts;
+            std::map<std::tuple<float, float, float>, H3> acc;
+            for (size_t k = 0; k < V.size(); k++) {
+                if (hasN[mi][k]) continue;
+                auto key = std::make_tuple(V[k].pos[0], V[k].pos[1], V[k].pos[2]);
+                H3 n = h3(V[k].norm[0], V[k].norm[1], V[k].norm[2]);
+                auto it = acc.find(key);
+                acc[key] = it == acc.end() ? n : it->second + n;
+            }
+            for (size_t k = 0; k < V.size(); k++) {
+                if (hasN[mi][k]) continue;
+                H3 n = acc[std::make_tuple(V[k].pos[0], V[k].pos[1], V[k].pos[2])];
+                float l = hlen(n);
+                if (l > 0.0f) { n = n * (1.0f / l); V[k].norm[0] = n.x; V[k].norm[1] = n.y; V[k].norm[2] = n.z; }
+            }
+        }
+    }
+    m.materials = mtlKd;
+    return true;
+}
+
+M4 m4_rot(float deg, int axis) {
+    float s, c;
+    gris_det_sincosf(deg * 0.017453292519943295f, &s, &c);
+    M4 r = m4_identity();
+    int a = (axis + 1) % 3, b = (axis + 2) % 3;   /* rotation in the (a, b) plane, counter-clockwise */
+    r.m[a * 4 + a] = c; r.m[b * 4 + a] = -s;
+    r.m[a * 4 + b] = s; r.m[b * 4 + b] = c;
+    return r;
+}
+
+}  // namespace
+
+namespace grisrt {
+/* reference: ModelInstance::modelMatrix (src/Model.cpp:11-21) */
+M4 model_matrix(const float pos[3], const float scale[3], const float rot[3]) {
+    M4 t = m4_identity();
+    t.m[12] = pos[0]; t.m[13] = pos[1]; t.m[14] = pos[2];
+    M4 m = m4_mul(t, m4_rot(rot[0], 2));
+    m = m4_mul(m, m4_rot(rot[1] + 90.0f, 0));
+    m = m4_mul(m, m4_rot(rot[2], 1));
+    M4 sc = m4_identity();
+    sc.m[0] = scale[0]; sc.m[5] = scale[2]; sc.m[10] = scale[1];
+    return m4_mul(m, sc);
+}
+}  // namespace grisrt
+
+static int xml_fail(char* errBuf, size_t errLen, const std::string& msg) {
+    if (errBuf && errLen) {
+        strncpy(errBuf, msg.c_str(), errLen - 1);
+        errBuf[errLen - 1] = 0;
+    }
+    return GRIS_ERR_INVALID_ARGUMENT;
+}
+
+extern "C" int grisHostSceneLoad(const char* path, GrisHostScene** out, char* errBuf, size_t errLen) {
+    if (!path || !out) return xml_fail(errBuf, errLen, "null argument");
+    *out = nullptr;
+    std::string text;
+    if (!read_file(path, text)) return xml_fail(errBuf, errLen, std::string("cannot read ") + path);
+    XmlParser xp(text);
+    XmlNode root;
+    if (!xp.element(root, 0)) return xml_fail(errBuf, errLen, std::string(path) + ": " + xp.err);
+    if (root.name != "scene") return xml_fail(errBuf, errLen, std::string(path) + ": the root element is not <scene>");
+    std::unique_ptr<GrisHostScene> s(new GrisHostScene());
+    s->kind = -1;
+    s->orbitRadius = 0.0f;
+    const std::string base = dir_of(path);
+    if (const XmlNode* integ = root.child("integrator"))
+        if (const XmlNode* size = integ->child("size")) {
+            const char* w = size->attr("width");
+            const char* h = size->attr("height");
+            s->filmW = w ? (uint32_t)atoi(w) : 0;
+            s->filmH = h ? (uint32_t)atoi(h) : 0;
+        }
+    if (const XmlNode* cam = root.child("camera")) {
+        const XmlNode* p = cam->child("position");
+        if (p) parse_floats(p->attr("value"), s->camPos, 3);
+        if (const XmlNode* a = cam->child("angle")) parse_floats(a->attr("value"), s->camAngle, 3);
+        else if (const XmlNode* l = cam->child("lookAt")) { s->camLookAt = parse_floats(l->attr("value"), s->camTarget, 3); }
+        if (const XmlNode* f = cam->child("fov")) parse_floats(f->attr("value"), &s->fov, 1);
+    }
+    /* materials[0]: the default (magenta) material of an empty resource (src/Resource.cpp:36-40) */
+    s->materials.push_back(make_material(1u, h3(1.0f, 0.0f, 1.0f), 0.0f, 1.0f));
+    std::vector<float> lightPower;
+    const XmlNode* models = root.child("modelInstances");
+    if (models) for (const XmlNode& mi : models->kids) {
+        const char* rel = mi.attr("path");
+        if (!rel) return xml_fail(errBuf, errLen, "a model instance without a path");
+        const bool isLight = mi.attr("type") && !strcmp(mi.attr("type"), "light");
+        ObjModel obj;
+        std::string err;
+        if (!load_obj(base + "/" + rel, isLight, obj, err)) return xml_fail(errBuf, errLen, err);
+        float pos[3] = {0, 0, 0}, scale[3] = {1, 1, 1}, rot[3] = {0, 0, 0};
+        if (const XmlNode* tr = mi.child("transform")) {
+            if (tr->attr("translate")) parse_floats(tr->attr("translate"), pos, 3);
+            if (tr->attr("scale")) parse_floats(tr->attr("scale"), scale, 3);
+            if (tr->attr("rotate")) parse_floats(tr->attr("rotate"), rot, 3);
+        }
+        M4 M = model_matrix(pos, scale, rot);
+        if (isLight) {
+            float power[3] = {0, 0, 0};
+            if (const XmlNode* r = mi.child("radiance")) parse_floats(r->attr("value"), power, 3);
+            const bool flip = mi.attr("flip") && !strcmp(mi.attr("flip"), "true");
+            size_t first = s->lights.size();
+            float area = 0.0f;   /* summed serially, in triangle order */
+            for (const ObjMesh& mesh : obj.meshes)
+                for (size_t k = 0; k + 2 < mesh.verts.size(); k += 3) {
+                    H3 w[3];
+                    for (int j = 0; j < 3; j++) {
+                        const float* p = mesh.verts[k + j].pos;
+                        w[j] = h3(((M.m[0] * p[0] + M.m[4] * p[1]) + M.m[8] * p[2]) + M.m[12],
+                                  ((M.m[1] * p[0] + M.m[5] * p[1]) + M.m[9] * p[2]) + M.m[13],
+                                  ((M.m[2] * p[0] + M.m[6] * p[1]) + M.m[10] * p[2]) + M.m[14]);
+                    }
+                    GrisTriangleLight L;
+                    memset(&L, 0, sizeof(L));
+                    H3 n = hcross(w[1] - w[0], w[2] - w[0]);
+                    L.area = 0.5f * hlen(n);
+                    n = hnorm(n);
+                    if (flip) n = n * -1.0f;
+                    L.v0[0] = w[0].x; L.v0[1] = w[0].y; L.v0[2] = w[0].z;
+                    L.v1[0] = w[1].x; L.v1[1] = w[1].y; L.v1[2] = w[1].z;
+                    L.v2[0] = w[2].x; L.v2[1] = w[2].y; L.v2[2] = w[2].z;
+                    L.nx = n.x; L.ny = n.y; L.nz = n.z;
+                    area += L.area;
+                    s->lights.push_back(L);
+                }
+            for (size_t k = first; k < s->lights.size(); k++)
+                for (int c = 0; c < 3; c++) s->lights[k].radiance[c] = power[c] / area;
+            continue;
+        }
+        /* materials of this model: the MTL colours (or the default), overridden by <material> */
+        std::vector<uint32_t> matOf(obj.meshes.size());
+        const XmlNode* mat = mi.child("material");
+        const char* mtype = mat ? mat->attr("type") : nullptr;
+        const bool override = mtype && strcmp(mtype, "default") != 0;
+        for (size_t k = 0; k < obj.meshes.size(); k++) {
+            GrisMaterial g = make_material(1u, h3(1.0f, 1.0f, 1.0f), 0.0f, 1.0f);
+            int src = obj.meshes[k].material;
+            if (src >= 0 && src < (int)obj.materials.size()) {
+                g.baseColor[0] = obj.materials[src].x; g.baseColor[1] = obj.materials[src].y; g.baseColor[2] = obj.materials[src].z;
+            }
+            if (override) {
+                static const char* names[] = {"principled", "lambertian", "metalWorkflow", "metal", "dielectric", "thinDielectric", "fake"};
+                int type = -1;
+                for (int t = 0; t < 7; t++) if (!strcmp(mtype, names[t])) type = t;
+                if (type < 1) return xml_fail(errBuf, errLen, std::string("unsupported material type ") + mtype);
+                g.type = (uint32_t)type;
+                g.metallic = 0.0f; g.roughness = 1.0f; g.ior = 1.5f;
+                if (const XmlNode* c = mat->child("metallic")) parse_floats(c->attr("value"), &g.metallic, 1);
+                if (const XmlNode* c = mat->child("roughness")) parse_floats(c->attr("value"), &g.roughness, 1);
+                if (const XmlNode* c = mat->child("ior")) parse_floats(c->attr("value"), &g.ior, 1);
+                if (const XmlNode* bc = mat->child("baseColor")) {
+                    if (bc->attr("image")) return xml_fail(errBuf, errLen, "image textures are not supported");
+                    if (bc->attr("value")) parse_floats(bc->attr("value"), g.baseColor, 3);
+                    else { g.baseColor[0] = g.baseColor[1] = g.baseColor[2] = 1.0f; }
+                }
+            }
+            matOf[k] = (uint32_t)s->materials.size();
+            s->materials.push_back(g);
+        }
+        uint32_t indexOffset = (uint32_t)s->indices.size();
+        for (size_t k = 0; k < obj.meshes.size(); k++) {
+            const ObjMesh& mesh = obj.meshes[k];
+            uint32_t vbase = (uint32_t)s->vertices.size();
+            for (const GrisMeshVertex& v : mesh.verts) s->vertices.push_back(v);
+            for (uint32_t j = 0; j < (uint32_t)mesh.verts.size(); j++) s->indices.push_back(vbase + j);
+            for (size_t f = 0; f < mesh.verts.size() / 3; f++) s->materialIndices.push_back((int32_t)matOf[k]);
+        }
+        uint32_t indexCount = (uint32_t)s->indices.size() - indexOffset;
+        s->instances.emplace_back();
+        set_instance(s->instances.back(), M, indexOffset, indexCount, obj.meshes.empty() ? 0u : matOf[0]);
+    }
+    if (s->lights.empty()) return xml_fail(errBuf, errLen, "the scene has no light");
+    build_light_table(*s);
+    *out = s.release();
+    return GRIS_OK;
+}
+
+extern "C" int grisHostSceneFilmSize(const GrisHostScene* s, uint32_t* width, uint32_t* height) {
+    if (!s || !width || !height) return GRIS_ERR_INVALID_ARGUMENT;
+    *width = s->filmW;
+    *height = s->filmH;
     return GRIS_OK;
 }

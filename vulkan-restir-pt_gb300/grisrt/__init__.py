@@ -149,6 +149,7 @@ EXPORTS = [
     "grisReadKernelProfile", "grisConvergedAccumulate", "grisRelMSE",
     "grisGuideCreate", "grisGuideDestroy", "grisGuideParamCount", "grisGuideSetParams", "grisGuideGetParams",
     "grisGuideSetTraining", "grisGuideForward", "grisGuideGradient", "grisGuideTrainStep", "grisBatchSetGuide",
+    "grisHostSceneLoad", "grisHostSceneFilmSize",
 ]
 
 _lib = None
@@ -219,6 +220,8 @@ def load(path=None):
         "grisGuideGradient": (i32, [vp, vp, vp, vp, vp, u32, vp]),
         "grisGuideTrainStep": (i32, [vp, vp, vp, vp, vp, u32]),
         "grisBatchSetGuide": (i32, [vp, vp]),
+        "grisHostSceneLoad": (i32, [ctypes.c_char_p, ctypes.POINTER(vp), ctypes.c_char_p, ctypes.c_size_t]),
+        "grisHostSceneFilmSize": (i32, [vp, ctypes.POINTER(u32), ctypes.POINTER(u32)]),
         "grisConvergedAccumulate": (i32, [vp, vp, ctypes.POINTER(ConvergedBindings), ctypes.POINTER(Camera),
                                           ctypes.POINTER(Settings), u32, u32, i32]),
         "grisRelMSE": (i32, [vp, vp, vp, ctypes.c_double, u64, ctypes.c_double, ctypes.POINTER(ctypes.c_double)]),
@@ -266,10 +269,13 @@ def camera_setup(pos, angle, fov, width, height):
 class HostScene:
     """Synthetic scene (kind 0 box, 1 terrain + spheres, 2 glossy terrain) as reference-layout arrays."""
 
-    def __init__(self, kind=0, seed=1, grid=512, spheres=2000):
+    def __init__(self, kind=0, seed=1, grid=512, spheres=2000, _handle=None):
         lib = load()
-        h = ctypes.c_void_p()
-        _check(lib.grisHostSceneCreate(kind, seed, grid, spheres, ctypes.byref(h)), what="grisHostSceneCreate")
+        if _handle is None:
+            h = ctypes.c_void_p()
+            _check(lib.grisHostSceneCreate(kind, seed, grid, spheres, ctypes.byref(h)), what="grisHostSceneCreate")
+        else:
+            h = _handle
         self._h = h
         d = SceneDesc()
         _check(lib.grisHostSceneDesc(h, ctypes.byref(d)), what="grisHostSceneDesc")
@@ -287,6 +293,21 @@ class HostScene:
         self.material_indices = arr(d.materialIndices, d.materialIndexCount, np.int32)
         self.lights = arr(d.lights, d.lightCount, LIGHT)
         self.light_table = arr(d.lightTable, d.lightTableCount, TABLE)
+
+    @classmethod
+    def load(cls, path):
+        """A scene file in the reference's XML format with OBJ meshes (grisHostSceneLoad)."""
+        h = ctypes.c_void_p()
+        err = ctypes.create_string_buffer(512)
+        rc = load().grisHostSceneLoad(os.fsencode(path), ctypes.byref(h), err, len(err))
+        if rc != 0:
+            raise GrisError("grisHostSceneLoad failed (%d): %s" % (rc, err.value.decode(errors="replace")))
+        return cls(_handle=h)
+
+    def film_size(self):
+        w, h = ctypes.c_uint32(), ctypes.c_uint32()
+        _check(load().grisHostSceneFilmSize(self._h, ctypes.byref(w), ctypes.byref(h)), what="grisHostSceneFilmSize")
+        return w.value, h.value
 
     def camera(self, frame, frames, width, height):
         c = Camera()
