@@ -499,9 +499,10 @@ def main():
         r = batch.autotune([v.cams[fi] for v in views], [v.prevs[fi] for v in views], [v.settings for v in views],
                            frames=3)
         fi += 1
-        names = ["megakernel"] + ["wavefront t%d s%d" % (t, s) for t in (8, 16, 32) for s in (4, 8, 16)]
+        names = (["megakernel"] + ["wavefront t%d s%d" % (t, s) for t in (8, 16, 32) for s in (4, 8, 16)] +
+                 ["wavefront refill t%d s16" % t for t in (4, 8, 16)])
         tune = {"chosen": "megakernel" if r.pathForm == G.PATH_MEGAKERNEL else
-                "wavefront t%d s%d" % (r.traceBlocksPerSM, r.shadeBlocksPerSM),
+                "wavefront%s t%d s%d" % (" refill" if r.refill else "", r.traceBlocksPerSM, r.shadeBlocksPerSM),
                 "ms": {names[i]: round(r.candidateMs[i], 3) for i in range(r.candidates)}}
         form = r.pathForm
     else:

@@ -393,16 +393,21 @@ int grisSetPathForm(GrisContext* ctx, int form);
 int grisSetGraphs(GrisContext* ctx, int enable);
 /* Grid sizes of the wavefront kernels, in 128-thread blocks per SM (defaults 16 and 8). */
 int grisSetWaveLaunch(GrisContext* ctx, int traceBlocksPerSM, int shadeBlocksPerSM);
-/* Times candidate configurations — the megakernel path tracer and the wavefront one with trace
- * grids of 8/16/32 and shading grids of 4/8/16 blocks per SM — over `frames` frames each on the
- * given views (those frames are rendered: reservoirs and output change), keeps the fastest in
- * the context and reports it. */
+/* 1: the wavefront's traversal kernels keep every lane busy (a lane whose ray is finished takes
+ * the next ray while the others of its warp still walk); same results. */
+int grisSetWaveRefill(GrisContext* ctx, int enable);
+/* Times candidate configurations — the megakernel path tracer, the wavefront one with trace
+ * grids of 8/16/32 and shading grids of 4/8/16 blocks per SM, and the wavefront one with the
+ * refilling traversal kernels at 4/8/16 blocks per SM — over `frames` frames each on the given
+ * views (those frames are rendered: reservoirs and output change), keeps the fastest in the
+ * context and reports it. */
 typedef struct GrisTuneResult {
     int pathForm;
     int traceBlocksPerSM, shadeBlocksPerSM;
     int candidates;
     double msPerFrame;            /* of the chosen configuration */
     double candidateMs[16];       /* per candidate, in the order above */
+    int refill;                   /* the chosen wavefront uses the refilling traversal kernels */
 } GrisTuneResult;
 int grisBatchCreate(GrisContext* ctx, uint32_t nViews, const GrisScene* const* scenes, const uint32_t* widths,
                     const uint32_t* heights, GrisBatch** out);

@@ -38,16 +38,19 @@ def setup():
     ctx.close()
 
 
-@pytest.mark.parametrize("form,graphs,wave", [
-    (G.PATH_WAVEFRONT, True, (16, 8)), (G.PATH_WAVEFRONT, False, (16, 8)), (G.PATH_WAVEFRONT, True, (8, 4)),
-    (G.PATH_WAVEFRONT, True, (32, 16)), (G.PATH_MEGAKERNEL, True, (16, 8)), (G.PATH_MEGAKERNEL, False, (16, 8))],
-    ids=["wavefront-graph", "wavefront-eager", "wavefront-small-grids", "wavefront-large-grids", "megakernel-graph",
-         "megakernel-eager"])
-def test_batch_views_match_oracle(setup, form, graphs, wave):
+@pytest.mark.parametrize("form,graphs,wave,refill", [
+    (G.PATH_WAVEFRONT, True, (16, 8), False), (G.PATH_WAVEFRONT, False, (16, 8), False),
+    (G.PATH_WAVEFRONT, True, (8, 4), False), (G.PATH_WAVEFRONT, True, (32, 16), False),
+    (G.PATH_WAVEFRONT, True, (8, 16), True), (G.PATH_WAVEFRONT, False, (2, 8), True),
+    (G.PATH_MEGAKERNEL, True, (16, 8), False), (G.PATH_MEGAKERNEL, False, (16, 8), False)],
+    ids=["wavefront-graph", "wavefront-eager", "wavefront-small-grids", "wavefront-large-grids", "wavefront-refill",
+         "wavefront-refill-eager-tiny-grid", "megakernel-graph", "megakernel-eager"])
+def test_batch_views_match_oracle(setup, form, graphs, wave, refill):
     ctx, hss, scenes, seqs, settings, want = setup
     ctx.set_path_form(form)
     ctx.set_graphs(graphs)
     ctx.set_wave_launch(*wave)
+    ctx.set_wave_refill(refill)
     batch = G.Batch(ctx, scenes, [(W, H) for (k, g, sp, W, H, kw) in VIEWS])
     ctx.counters(reset=True)
     keys = {"resv": G.BUF_RESERVOIR, "temp": G.BUF_TEMP, "out": G.BUF_OUTPUT, "dn": G.BUF_DEPTH_NORMAL,
@@ -65,6 +68,7 @@ def test_batch_views_match_oracle(setup, form, graphs, wave):
     ctx.set_path_form(G.PATH_WAVEFRONT)
     ctx.set_graphs(True)
     ctx.set_wave_launch(16, 8)
+    ctx.set_wave_refill(False)
 
 
 def test_autotune_picks_a_candidate_and_results_stay_exact(setup):
@@ -76,7 +80,7 @@ def test_autotune_picks_a_candidate_and_results_stay_exact(setup):
     tb = G.Batch(ctx, scenes, sizes)
     r = tb.autotune([seqs[v][0][1] for v in range(n)], [seqs[v][1][1] for v in range(n)], settings, frames=2)
     tb.close()
-    assert r.candidates == 10
+    assert r.candidates == 13
     ms = list(r.candidateMs)[:r.candidates]
     assert all(m > 0 for m in ms)
     assert r.msPerFrame == min(ms)
@@ -90,6 +94,7 @@ def test_autotune_picks_a_candidate_and_results_stay_exact(setup):
     batch.close()
     ctx.set_path_form(G.PATH_WAVEFRONT)
     ctx.set_wave_launch(16, 8)
+    ctx.set_wave_refill(False)
 
 
 def test_single_view_batch_equals_frame_api(setup):

@@ -43,7 +43,7 @@ struct GrisBatch {
     /* captured frames, one per staging slot, valid for one frame shape */
     struct Graph {
         cudaGraphExec_t exec = nullptr;
-        int pathForm = -1, maxDepth = -1, trace = 0, shade = 0, countWork = -1;
+        int pathForm = -1, maxDepth = -1, trace = 0, shade = 0, refill = -1, countWork = -1;
         uint32_t pixels = 0, tiles = 0;
         const GrisGuide* guide = nullptr;
         int train = -1;
@@ -112,7 +112,7 @@ int grisBatchCreate(GrisContext* ctx, uint32_t n, const GrisScene* const* scenes
     alloc((void**)&b->wave.queue[0], P * 4, false);
     alloc((void**)&b->wave.queue[1], P * 4, false);
     alloc((void**)&b->wave.shadowQueue, P * 4, false);
-    alloc((void**)&b->wave.counts, 1024 * 4, true);
+    alloc((void**)&b->wave.counts, 1536 * 4, true);
     b->wave.capacity = P;
     alloc(&b->dViews, view_entry_bytes() * n, false);
     for (int i = 0; i < 2 && e == cudaSuccess; i++) {
@@ -187,7 +187,8 @@ int grisBatchRender(GrisContext* ctx, GrisBatch* b, const GrisCamera* cams, cons
     if (ctx_graphs(ctx)) {
         GrisBatch::Graph& g = b->graph[k];
         if (!g.exec || g.pathForm != form || g.maxDepth != sh.maxDepth || g.pixels != sh.pixels || g.tiles != sh.tiles ||
-            g.trace != wl.traceBlocksPerSM || g.shade != wl.shadeBlocksPerSM || g.countWork != ctx_count_work(ctx) ||
+            g.trace != wl.traceBlocksPerSM || g.shade != wl.shadeBlocksPerSM || g.refill != wl.refill ||
+            g.countWork != ctx_count_work(ctx) ||
             g.guide != b->guide || g.train != train) {
             if (g.exec) { cudaGraphExecDestroy(g.exec); g.exec = nullptr; }
             cudaGraph_t graph = nullptr;
@@ -203,7 +204,7 @@ int grisBatchRender(GrisContext* ctx, GrisBatch* b, const GrisCamera* cams, cons
             if (graph) cudaGraphDestroy(graph);
             if (e != cudaSuccess) return ctx_fail(ctx, GRIS_ERR_CUDA, std::string("graph capture: ") + cudaGetErrorString(e));
             g.pathForm = form; g.maxDepth = sh.maxDepth; g.pixels = sh.pixels; g.tiles = sh.tiles;
-            g.trace = wl.traceBlocksPerSM; g.shade = wl.shadeBlocksPerSM; g.countWork = ctx_count_work(ctx);
+            g.trace = wl.traceBlocksPerSM; g.shade = wl.shadeBlocksPerSM; g.refill = wl.refill; g.countWork = ctx_count_work(ctx);
             g.guide = b->guide; g.train = train;
         }
         e = cudaGraphLaunch(g.exec, st);
@@ -273,10 +274,11 @@ int grisBatchAutotune(GrisContext* ctx, GrisBatch* b, const GrisCamera* cams, co
                       const GrisSettings* settings, int frames, GrisTuneResult* out) {
     if (!ctx || !b || !out || frames < 1) return ctx_fail(ctx, GRIS_ERR_INVALID_ARGUMENT, "bad autotune request");
     cudaSetDevice(ctx_device(ctx));
-    struct Cand { int form, trace, shade; };
-    std::vector<Cand> cands = {{GRIS_PATH_MEGAKERNEL, 16, 8}};
+    struct Cand { int form, trace, shade, refill; };
+    std::vector<Cand> cands = {{GRIS_PATH_MEGAKERNEL, 16, 8, 0}};
     for (int t : {8, 16, 32})
-        for (int sh : {4, 8, 16}) cands.push_back({GRIS_PATH_WAVEFRONT, t, sh});
+        for (int sh : {4, 8, 16}) cands.push_back({GRIS_PATH_WAVEFRONT, t, sh, 0});
+    for (int t : {4, 8, 16}) cands.push_back({GRIS_PATH_WAVEFRONT, t, 16, 1});
     memset(out, 0, sizeof(*out));
     cudaStream_t st = ctx_stream(ctx);
     cudaEvent_t e0, e1;
@@ -291,6 +293,7 @@ int grisBatchAutotune(GrisContext* ctx, GrisBatch* b, const GrisCamera* cams, co
         WaveLaunch wl;
         wl.traceBlocksPerSM = cands[i].trace;
         wl.shadeBlocksPerSM = cands[i].shade;
+        wl.refill = cands[i].refill;
         ctx_set_tuning(ctx, cands[i].form, wl);
         rc = grisBatchRender(ctx, b, cams, prevCams, settings);   /* warm-up (and graph capture) */
         cudaEventRecord(e0, st);
@@ -309,8 +312,10 @@ int grisBatchAutotune(GrisContext* ctx, GrisBatch* b, const GrisCamera* cams, co
     WaveLaunch wl;
     wl.traceBlocksPerSM = cands[bestI].trace;
     wl.shadeBlocksPerSM = cands[bestI].shade;
+    wl.refill = cands[bestI].refill;
     ctx_set_tuning(ctx, cands[bestI].form, wl);
     out->pathForm = cands[bestI].form;
+    out->refill = wl.refill;
     out->traceBlocksPerSM = wl.traceBlocksPerSM;
     out->shadeBlocksPerSM = wl.shadeBlocksPerSM;
     out->msPerFrame = best;

@@ -28,8 +28,10 @@
 
 #ifdef __CUDACC__
 #define GRIS_HD __host__ __device__ __forceinline__
+#define GRIS_HDM __host__ __device__ __forceinline__
 #else
 #define GRIS_HD static inline
+#define GRIS_HDM inline
 #endif
 
 #define GRIS_BVH_STACK 64
@@ -121,35 +123,48 @@ GRIS_HD bool gris_tri_test(const float* T, float ox, float oy, float oz, float d
 GRIS_HD uint32_t gris_byte(uint32_t w, int i) { return (w >> (i * 8)) & 0xffu; }
 
 /*
- * Walks the BVH. ANY: return at the first accepted hit (shadow rays). skipInst0: ignore the
- * light instance (the G-buffer is rasterised without lights). Returns true if a hit was
- * found; `hit` receives the closest one. *err is set to 1 if the stack limit was reached (the
- * builder guarantees it is not: tree depth <= GRIS_BVH_STACK).
+ * One ray's walk of the BVH as a resumable state machine: init() then step() until it returns
+ * false (each step visits one node or pops one group). ANY: stop at the first accepted hit
+ * (shadow rays). skipInst0: ignore the light instance (the G-buffer is rasterised without
+ * lights). *err is set to 1 if the stack limit was reached (the builder guarantees it is not:
+ * tree depth <= GRIS_BVH_STACK). Resumable so that a lane whose ray has finished can take the
+ * next ray while the other lanes of its warp are still walking.
  */
 template <bool ANY>
-GRIS_HD bool gris_bvh_trace(const uint32_t* __restrict__ nodes, const float* __restrict__ tris,
-                            float ox, float oy, float oz, float dx, float dy, float dz,
-                            float tmin, float tmax, bool skipInst0, GrisRayHit* hit, int* err,
-                            GrisWork* work) {
-    const float tiny = 1e-30f;
-    float idx = 1.0f / ((dx > tiny || dx < -tiny) ? dx : (dx < 0.0f ? -tiny : tiny));
-    float idy = 1.0f / ((dy > tiny || dy < -tiny) ? dy : (dy < 0.0f ? -tiny : tiny));
-    float idz = 1.0f / ((dz > tiny || dz < -tiny) ? dz : (dz < 0.0f ? -tiny : tiny));
-    uint32_t oct = (dx < 0.0f ? 1u : 0u) | (dy < 0.0f ? 2u : 0u) | (dz < 0.0f ? 4u : 0u);
-    float bestT = tmax;
-    uint32_t bestInst = GRIS_INVALID_HIT, bestTri = GRIS_INVALID_HIT;
-    float bestU = 0.0f, bestV = 0.0f;
-    bool found = false;
+struct GrisTraversal {
+    float ox, oy, oz, dx, dy, dz, idx, idy, idz, tmin;
+    uint32_t oct;
+    float bestT, bestU, bestV;
+    uint32_t bestInst, bestTri;
+    bool found;
+    int sp;
+    uint32_t grpBase, grpHits, grpImask, nodeIdx;
+    bool haveNode;
+    uint32_t visits, tests;
 
-    uint32_t stackBase[GRIS_BVH_STACK];
-    uint32_t stackBits[GRIS_BVH_STACK];
-    int sp = 0;
-    uint32_t grpBase = 0, grpHits = 0, grpImask = 0;
-    uint32_t nodeIdx = 0;
-    bool haveNode = true;
-    uint32_t visits = 0, tests = 0;
+    GRIS_HDM void init(float ox_, float oy_, float oz_, float dx_, float dy_, float dz_, float tmin_, float tmax_) {
+        const float tiny = 1e-30f;
+        ox = ox_; oy = oy_; oz = oz_; dx = dx_; dy = dy_; dz = dz_; tmin = tmin_;
+        idx = 1.0f / ((dx > tiny || dx < -tiny) ? dx : (dx < 0.0f ? -tiny : tiny));
+        idy = 1.0f / ((dy > tiny || dy < -tiny) ? dy : (dy < 0.0f ? -tiny : tiny));
+        idz = 1.0f / ((dz > tiny || dz < -tiny) ? dz : (dz < 0.0f ? -tiny : tiny));
+        oct = (dx < 0.0f ? 1u : 0u) | (dy < 0.0f ? 2u : 0u) | (dz < 0.0f ? 4u : 0u);
+        bestT = tmax_;
+        bestInst = GRIS_INVALID_HIT; bestTri = GRIS_INVALID_HIT;
+        bestU = 0.0f; bestV = 0.0f;
+        found = false;
+        sp = 0;
+        grpBase = 0; grpHits = 0; grpImask = 0;
+        nodeIdx = 0;
+        haveNode = true;
+        visits = 0; tests = 0;
+    }
 
-    while (true) {
+    /* false: the walk is over (found / best* hold the result). The stack arrays (GRIS_BVH_STACK
+     * entries each) are the caller's: kept outside the struct, the struct's scalars stay in
+     * registers. */
+    GRIS_HDM bool step(const uint32_t* __restrict__ nodes, const float* __restrict__ tris, bool skipInst0, int* err,
+                       uint32_t* stackBase, uint32_t* stackBits) {
         if (haveNode) {
             const uint32_t* N = nodes + (uint64_t)nodeIdx * GRIS_NODE_WORDS;
 #ifdef __CUDA_ARCH__
@@ -213,9 +228,8 @@ GRIS_HD bool gris_bvh_trace(const uint32_t* __restrict__ nodes, const float* __r
                 float t, u, v;
                 if (!gris_tri_test(TT, ox, oy, oz, dx, dy, dz, tmin, bestT, &t, &u, &v)) continue;
                 if (ANY) {
-                    hit->t = t; hit->u = u; hit->v = v; hit->inst = inst; hit->tri = tri;
-                    if (work) { work->nodes += visits; work->tris += tests; }
-                    return true;
+                    bestT = t; bestU = u; bestV = v; bestInst = inst; bestTri = tri; found = true;
+                    return false;
                 }
                 /* t <= bestT here (the test used bestT as tmax) */
                 bool keyLess = inst < bestInst || (inst == bestInst && tri < bestTri);
@@ -226,7 +240,7 @@ GRIS_HD bool gris_bvh_trace(const uint32_t* __restrict__ nodes, const float* __r
             }
             if (innerHits) {
                 if (grpHits) {
-                    if (sp >= GRIS_BVH_STACK) { *err = 1; break; }
+                    if (sp >= GRIS_BVH_STACK) { *err = 1; return false; }
                     stackBase[sp] = grpBase; stackBits[sp] = grpHits | (grpImask << 8); sp++;
                 }
                 grpBase = W[4]; grpHits = innerHits; grpImask = imask;
@@ -234,7 +248,7 @@ GRIS_HD bool gris_bvh_trace(const uint32_t* __restrict__ nodes, const float* __r
             haveNode = false;
         }
         if (grpHits == 0) {
-            if (sp == 0) break;
+            if (sp == 0) return false;
             sp--;
             grpBase = stackBase[sp]; grpHits = stackBits[sp] & 0xffu; grpImask = stackBits[sp] >> 8;
         }
@@ -243,10 +257,28 @@ GRIS_HD bool gris_bvh_trace(const uint32_t* __restrict__ nodes, const float* __r
         uint32_t slot = (uint32_t)pos ^ oct;
         nodeIdx = grpBase + (uint32_t)gris_popc(grpImask & ((1u << slot) - 1u));
         haveNode = true;
+        return true;
     }
-    if (work) { work->nodes += visits; work->tris += tests; }
-    if (found) { hit->t = bestT; hit->u = bestU; hit->v = bestV; hit->inst = bestInst; hit->tri = bestTri; }
-    return found;
+
+    GRIS_HDM void result(GrisRayHit* hit, GrisWork* work) const {
+        if (work) { work->nodes += visits; work->tris += tests; }
+        if (found) { hit->t = bestT; hit->u = bestU; hit->v = bestV; hit->inst = bestInst; hit->tri = bestTri; }
+    }
+};
+
+/* A whole walk in one call: returns true if a hit was found; `hit` receives the closest one
+ * (any one for ANY). */
+template <bool ANY>
+GRIS_HD bool gris_bvh_trace(const uint32_t* __restrict__ nodes, const float* __restrict__ tris,
+                            float ox, float oy, float oz, float dx, float dy, float dz,
+                            float tmin, float tmax, bool skipInst0, GrisRayHit* hit, int* err,
+                            GrisWork* work) {
+    GrisTraversal<ANY> w;
+    uint32_t stackBase[GRIS_BVH_STACK], stackBits[GRIS_BVH_STACK];
+    w.init(ox, oy, oz, dx, dy, dz, tmin, tmax);
+    while (w.step(nodes, tris, skipInst0, err, stackBase, stackBits)) {}
+    w.result(hit, work);
+    return w.found;
 }
 
 #endif

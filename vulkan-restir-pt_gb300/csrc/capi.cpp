@@ -313,6 +313,12 @@ int grisSetWaveLaunch(GrisContext* ctx, int traceBlocksPerSM, int shadeBlocksPer
     return GRIS_OK;
 }
 
+int grisSetWaveRefill(GrisContext* ctx, int enable) {
+    if (!ctx) return GRIS_ERR_INVALID_ARGUMENT;
+    ctx->waveLaunch.refill = enable != 0;
+    return GRIS_OK;
+}
+
 int grisSetPathForm(GrisContext* ctx, int form) {
     if (!ctx || (form != GRIS_PATH_MEGAKERNEL && form != GRIS_PATH_WAVEFRONT)) return GRIS_ERR_INVALID_ARGUMENT;
     ctx->pathForm = form;
@@ -550,7 +556,7 @@ int grisPassRender(GrisContext* ctx, const GrisScene* s, const GrisPassBindings*
             alloc((void**)&w.wb.queue[0], P * 4);
             alloc((void**)&w.wb.queue[1], P * 4);
             alloc((void**)&w.wb.shadowQueue, P * 4);
-            alloc((void**)&w.wb.counts, 1024 * 4);
+            alloc((void**)&w.wb.counts, 1536 * 4);
             alloc(&w.dViews, grisrt::view_entry_bytes());
             for (int i = 0; i < 2 && e == cudaSuccess; i++) {
                 e = cudaMallocHost(&w.hViews[i], grisrt::view_entry_bytes());

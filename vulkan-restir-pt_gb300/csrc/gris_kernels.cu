@@ -1394,6 +1394,78 @@ __global__ void __launch_bounds__(128) k_wave_extend(WaveCtx C, int level) {
     flush_counts(C.counters, rc, err, 1, C.countWork, 0);
 }
 
+/* The level's closest hits (ANY = false, the path queue) or shadow queries (ANY = true, the
+ * shadow queue), resident form: every lane walks its own ray step by step, and whenever a quarter
+ * of a warp's lanes are idle the warp takes that many rays from the queue (one atomic on the
+ * level's cursor), so lanes do not wait for the longest walk of their warp. Same walks, same
+ * results as k_wave_extend / k_wave_shadow. */
+template <bool ANY>
+__global__ void __launch_bounds__(128) k_wave_trace_refill(WaveCtx C, int level) {
+    const uint32_t n = ANY ? C.counts[256 + level] : C.counts[level];
+    const uint32_t* q = ANY ? C.shadowQueue : C.queue[level & 1];
+    uint32_t* cursor = C.counts + (ANY ? 1280 : 1024) + level;
+    const uint32_t lane = threadIdx.x & 31u;
+    RayCount rc = ray_count();
+    int err = 0;
+    GrisTraversal<ANY> tr;
+    uint32_t stackBase[GRIS_BVH_STACK], stackBits[GRIS_BVH_STACK];
+    const uint32_t* nodes = nullptr;
+    const float* tris = nullptr;
+    uint32_t id = 0;
+    bool active = false, more = true;
+    while (true) {
+        unsigned idle = __ballot_sync(0xffffffffu, !active);
+        if (more && __popc(idle) >= 8) {
+            uint32_t take = (uint32_t)__popc(idle), leader = __ffs(idle) - 1, base = 0;
+            if (lane == leader) base = atomicAdd(cursor, take);
+            base = __shfl_sync(0xffffffffu, base, leader);
+            if (!active) {
+                uint32_t i = base + (uint32_t)__popc(idle & ((1u << lane) - 1u));
+                if (i < n) {
+                    id = q[i];
+                    int v = find_view_by_pixel(C.V, C.nViews, id);
+                    nodes = C.V[v].P.sc.nodes;
+                    tris = C.V[v].P.sc.tris;
+                    if (ANY) {
+                        const uint4* w = C.nee[id].w;
+                        uint4 a = w[0], d4 = w[4], r3 = w[3];
+                        float dist = __uint_as_float(r3.w);
+                        tr.init(__uint_as_float(a.x), __uint_as_float(a.y), __uint_as_float(a.z), __uint_as_float(d4.x),
+                                __uint_as_float(d4.y), __uint_as_float(d4.z), kMinRayDistance, dist - kMinRayDistance);
+                    } else {
+                        const uint4* w = C.state[id].w;
+                        uint4 a = w[4], b = w[5];
+                        tr.init(__uint_as_float(a.x), __uint_as_float(a.y), __uint_as_float(a.z), __uint_as_float(b.x),
+                                __uint_as_float(b.y), __uint_as_float(b.z), kMinRayDistance, kMaxRayDistance);
+                    }
+                    active = true;
+                }
+            }
+            if (base + take >= n) more = false;
+        }
+        if (__ballot_sync(0xffffffffu, active) == 0u) {
+            if (!more) break;
+            continue;
+        }
+        if (active && !tr.step(nodes, tris, false, &err, stackBase, stackBits)) {
+            GrisRayHit h;
+            tr.result(&h, &rc.work);
+            if (ANY) {
+                rc.shadow++;
+                C.blocked[id] = tr.found ? 1 : 0;
+            } else {
+                rc.closest++;
+                Isec r;
+                if (tr.found) { r.bx = h.u; r.by = h.v; r.inst = h.inst; r.tri = h.tri; }
+                else { r.bx = 0.0f; r.by = 0.0f; r.inst = kInvalidHit; r.tri = 0u; }
+                C.hit[id] = r;
+            }
+            active = false;
+        }
+    }
+    flush_counts(C.counters, rc, err, 1, C.countWork, ANY ? 1 : 0);
+}
+
 /* shade() of the level's paths: the end, the next level, or a shadow query */
 __global__ void __launch_bounds__(128) k_wave_shade(WaveCtx C, int level) {
     const uint32_t n = C.counts[level];
@@ -1691,7 +1763,7 @@ cudaError_t enqueue_batch(const BatchShape& sh, void* dViews, const void* hViews
             C.gFeat = wb.gFeat; C.gOut = wb.gOut; C.gRec = wb.gRec; C.gFrame = wb.gFrame;
             if (guide) C.guide = *guide; else memset(&C.guide, 0, sizeof(C.guide));
             C.frameSeed = 0u;
-            e = cudaMemsetAsync(wb.counts, 0, 1024 * sizeof(uint32_t), stream);
+            e = cudaMemsetAsync(wb.counts, 0, 1536 * sizeof(uint32_t), stream);
             if (e != cudaSuccess) return e;
             static int sm = 0;
             if (sm == 0) { int dev = 0; cudaGetDevice(&dev); cudaDeviceGetAttribute(&sm, cudaDevAttrMultiProcessorCount, dev); }
@@ -1708,13 +1780,15 @@ cudaError_t enqueue_batch(const BatchShape& sh, void* dViews, const void* hViews
                 mark(4, false);
                 for (int level = 1; level < sh.maxDepth; level++) {
                     mark(5, true);
-                    k_wave_extend<<<gridTrace, 128, 0, stream>>>(C, level);
+                    if (wl.refill) k_wave_trace_refill<false><<<gridTrace, 128, 0, stream>>>(C, level);
+                    else k_wave_extend<<<gridTrace, 128, 0, stream>>>(C, level);
                     mark(5, false);
                     mark(6, true);
                     k_gwave_shade<<<gridShade, 128, 0, stream>>>(C, level);
                     mark(6, false);
                     mark(7, true);
-                    k_wave_shadow<<<gridTrace, 128, 0, stream>>>(C, level);
+                    if (wl.refill) k_wave_trace_refill<true><<<gridTrace, 128, 0, stream>>>(C, level);
+                    else k_wave_shadow<<<gridTrace, 128, 0, stream>>>(C, level);
                     mark(7, false);
                     mark(9, true);
                     guide::FwdArgs fa;
@@ -1735,13 +1809,15 @@ cudaError_t enqueue_batch(const BatchShape& sh, void* dViews, const void* hViews
             mark(4, false);
             for (int level = 1; level < sh.maxDepth; level++) {
                 mark(5, true);
-                k_wave_extend<<<gridTrace, 128, 0, stream>>>(C, level);
+                if (wl.refill) k_wave_trace_refill<false><<<gridTrace, 128, 0, stream>>>(C, level);
+                else k_wave_extend<<<gridTrace, 128, 0, stream>>>(C, level);
                 mark(5, false);
                 mark(6, true);
                 k_wave_shade<<<gridShade, 128, 0, stream>>>(C, level);
                 mark(6, false);
                 mark(7, true);
-                k_wave_shadow<<<gridTrace, 128, 0, stream>>>(C, level);
+                if (wl.refill) k_wave_trace_refill<true><<<gridTrace, 128, 0, stream>>>(C, level);
+                else k_wave_shadow<<<gridTrace, 128, 0, stream>>>(C, level);
                 mark(7, false);
                 mark(8, true);
                 k_wave_post<<<gridShade, 128, 0, stream>>>(C, level);

@@ -63,7 +63,7 @@ struct WaveBuffers {
     unsigned char* blocked;
     uint32_t* queue[2];
     uint32_t* shadowQueue;
-    uint32_t* counts;   /* 1024 words */
+    uint32_t* counts;   /* 1536 words */
     uint64_t capacity;
     /* guided batches only (null otherwise): post queue, guide inputs / outputs per guided
      * vertex, training record per path, frame state (4 words) */
@@ -82,6 +82,7 @@ size_t view_entry_bytes();
 struct WaveLaunch {
     int traceBlocksPerSM = 16;
     int shadeBlocksPerSM = 8;
+    int refill = 0;   /* 1: the resident traversal kernels (lanes take new rays while others walk) */
 };
 
 struct BatchShape {

@@ -134,7 +134,8 @@ PROFILE_SLOTS = ["gbuffer", "path_trace", "temporal", "spatial", "wave_begin", "
 
 class TuneResult(ctypes.Structure):
     _fields_ = [("pathForm", ctypes.c_int), ("traceBlocksPerSM", ctypes.c_int), ("shadeBlocksPerSM", ctypes.c_int),
-                ("candidates", ctypes.c_int), ("msPerFrame", ctypes.c_double), ("candidateMs", ctypes.c_double * 16)]
+                ("candidates", ctypes.c_int), ("msPerFrame", ctypes.c_double), ("candidateMs", ctypes.c_double * 16),
+                ("refill", ctypes.c_int)]
 
 
 EXPORTS = [
@@ -149,7 +150,7 @@ EXPORTS = [
     "grisReadKernelProfile", "grisConvergedAccumulate", "grisRelMSE",
     "grisGuideCreate", "grisGuideDestroy", "grisGuideParamCount", "grisGuideSetParams", "grisGuideGetParams",
     "grisGuideSetTraining", "grisGuideForward", "grisGuideGradient", "grisGuideTrainStep", "grisBatchSetGuide",
-    "grisHostSceneLoad", "grisHostSceneFilmSize",
+    "grisHostSceneLoad", "grisHostSceneFilmSize", "grisSetWaveRefill",
 ]
 
 _lib = None
@@ -227,6 +228,7 @@ def load(path=None):
         "grisRelMSE": (i32, [vp, vp, vp, ctypes.c_double, u64, ctypes.c_double, ctypes.POINTER(ctypes.c_double)]),
         "grisReadKernelProfile": (i32, [vp, ctypes.POINTER(KernelProfile), i32]),
         "grisSetWaveLaunch": (i32, [vp, i32, i32]),
+        "grisSetWaveRefill": (i32, [vp, i32]),
         "grisBatchAutotune": (i32, [vp, vp, ctypes.POINTER(Camera), ctypes.POINTER(Camera), ctypes.POINTER(Settings), i32,
                                     ctypes.POINTER(TuneResult)]),
     }
@@ -432,6 +434,9 @@ class Context:
     def set_wave_launch(self, trace_blocks_per_sm, shade_blocks_per_sm):
         self.check(load().grisSetWaveLaunch(self.h, int(trace_blocks_per_sm), int(shade_blocks_per_sm)),
                    "grisSetWaveLaunch")
+
+    def set_wave_refill(self, enable):
+        self.check(load().grisSetWaveRefill(self.h, int(enable)), "grisSetWaveRefill")
 
     def set_work_counting(self, enable):
         self.check(load().grisSetWorkCounting(self.h, int(enable)), "grisSetWorkCounting")
