@@ -348,7 +348,7 @@ def run_guided(args):
                                                     learningRate=1e-3, mix=0.5))
             batch.set_guide(guide)
         out_ptr, _ = batch.device_ptr(0, G.BUF_OUTPUT)
-        times, rel, med = [], [], []
+        times, rel, med, energy = [], [], [], []
         with torch.cuda.stream(stream):
             for f in range(F):
                 e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
@@ -360,6 +360,7 @@ def run_guided(args):
                 img = batch.download(0, G.BUF_OUTPUT)[:, :3].astype(np.float64)
                 e = np.mean((img - ref_host) ** 2 / (ref_host ** 2 + 1e-2), axis=1)
                 med.append(float(np.median(e[fg])))
+                energy.append(float(img.sum() / max(ref_host.sum(), 1e-30)))
         # one profiled frame: the network's share of a frame
         ctx.set_profiling(True)
         ctx.kernel_profile(reset=True)
@@ -373,10 +374,15 @@ def run_guided(args):
         total = sum(prof[k]["ms"] for k in ("gbuffer", "path_trace", "temporal", "spatial")) + prof["guide_train"]["ms"]
         mlp = prof["guide_infer"]["ms"] + prof["guide_train"]["ms"]
         return np.array(times), np.array(rel), np.array(med), {"frame_ms": total, "mlp_ms": mlp,
-                                                               "mlp_share": mlp / total if total > 0 else 0.0}
+                                                               "mlp_share": mlp / total if total > 0 else 0.0,
+                                                               "energy_curve": energy,
+                                                               "frame_ms_curve": [float(t) for t in times]}
 
+    sampler = ClockSampler(0)
+    sampler.start()
     tp, rp, mp, pp = run(False)
     tg, rg, mg, pg = run(True)
+    clocks = sampler.stop()
     Tp = tp.sum()
     cg = np.cumsum(tg)
 
@@ -405,7 +411,7 @@ def run_guided(args):
                                    "frames accumulated" % (W, H, hs.triangle_count(), args.depth),
                        "guide": "MLP 80-64x4-48 BF16 mma.sync, 8 vMF lobes, mix 0.5, Adam 1e-3, 2^18 records/frame, 4 steps"},
             "reference": {"spp": args.ref_spp, "seconds": ref_s, "estimator": "candidates"},
-            "reuse": reuse,
+            "reuse": reuse, "clocks": clocks,
             "median_error_time_ratio": ratio_med,
             "plain": {"fps": 1000.0 / float(tp.mean()), "total_ms": float(Tp), "relmse_final": float(rp[-1]),
                       "median_final": float(mp[-1]), "relmse_curve": [float(x) for x in rp],
