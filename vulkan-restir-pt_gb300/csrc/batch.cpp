@@ -174,7 +174,6 @@ int grisBatchRender(GrisContext* ctx, GrisBatch* b, const GrisCamera* cams, cons
     cudaStream_t st = ctx_stream(ctx);
     cudaError_t e = cudaEventSynchronize(b->staged[k]);   /* the staging slot's previous copy is done */
     if (e != cudaSuccess) return ctx_fail(ctx, GRIS_ERR_CUDA, std::string("grisBatchRender: ") + cudaGetErrorString(e));
-    BatchShape sh = fill_view_table(views.data(), (int)b->n, b->hViews[k], ctx_counters(ctx), ctx_count_work(ctx));
     int form = ctx_path_form(ctx);
     WaveLaunch wl = ctx_wave_launch(ctx);
     guide::GuideDevice gd{};
@@ -184,6 +183,8 @@ int grisBatchRender(GrisContext* ctx, GrisBatch* b, const GrisCamera* cams, cons
         gd = guide_device(b->guide);
         train = guide_config(b->guide).train ? 1 : 0;
     }
+    BatchShape sh = fill_view_table(views.data(), (int)b->n, b->hViews[k], ctx_counters(ctx), ctx_count_work(ctx),
+                                    b->guide ? b->wave.gPrimOut : nullptr, b->guide ? gd.mix : 0.0f);
     if (ctx_graphs(ctx)) {
         GrisBatch::Graph& g = b->graph[k];
         if (!g.exec || g.pathForm != form || g.maxDepth != sh.maxDepth || g.pixels != sh.pixels || g.tiles != sh.tiles ||
@@ -253,7 +254,8 @@ int grisBatchSetGuide(GrisBatch* b, GrisGuide* g) {
     if (g && !b->guideBlock) {
         size_t P = (size_t)b->pixels;
         auto up = [](size_t n) { return (n + 255) & ~(size_t)255; };
-        size_t bytes = up(P * 4) + up(P * 9 * 4) + up(P * guide::kRaw * 4) + up(P * 18 * 4) + 256;
+        size_t bytes = up(P * 4) + up(P * 9 * 4) + up(P * guide::kRaw * 4) + up(P * 18 * 4) + up(P * 9 * 4) +
+                       up(P * guide::kRaw * 4) + 256;
         cudaError_t e = cudaMalloc(&b->guideBlock, bytes);
         if (e != cudaSuccess) { b->guideBlock = nullptr; return ctx_fail(ctx, GRIS_ERR_OUT_OF_MEMORY, "guided batch buffers"); }
         char* p = (char*)b->guideBlock;
@@ -261,6 +263,8 @@ int grisBatchSetGuide(GrisBatch* b, GrisGuide* g) {
         b->wave.gFeat = (float*)p; p += up(P * 9 * 4);
         b->wave.gOut = (float*)p; p += up(P * guide::kRaw * 4);
         b->wave.gRec = (float*)p; p += up(P * 18 * 4);
+        b->wave.gPrimFeat = (float*)p; p += up(P * 9 * 4);
+        b->wave.gPrimOut = (float*)p; p += up(P * guide::kRaw * 4);
         b->wave.gFrame = (uint32_t*)p;
         e = cudaMemsetAsync(b->wave.gFrame, 0, 256, ctx_stream(ctx));
         if (e == cudaSuccess) e = cudaStreamSynchronize(ctx_stream(ctx));

@@ -29,6 +29,11 @@ struct PassCtx {
     GrisPassBindings b;
     unsigned long long* counters;
     int countWork;
+    /* guided batches: the network's raw outputs at every pixel's primary vertex (indexed by the
+     * batch's path id = pixelBase + pixel), and the probability of drawing from the guide */
+    const float* gPrim;
+    float gMix;
+    uint32_t pixelBase;
 };
 
 /* ------------------------------------------------------------------ ray queries */
@@ -114,6 +119,41 @@ GD uint32_t nextRcVertexSampleState(uint32_t state, bool connectible) {         
     if (state == 2u) return 2u;
     if (!connectible) return 0u;
     return state + (connectible ? 1u : 0u);
+}
+
+/* ------------------------------------------------------------------ guided sampling */
+/* Whether the guide may draw at a vertex of this material (Lambert, or metallic-workflow rough
+ * enough that the BSDF sampler never returns a specular-typed sample). */
+GD bool guide_material(const Mat& m) { return m.type == 1u || (m.type == 2u && m.roughness >= 0.01f); }
+
+/* One-sample MIS of the guide mixture (probability mix) and the BSDF sampler: s.pdf is the
+ * mixture pdf of the direction, pdfBsdf the BSDF's own pdf of it. Draws sample1f + sample3f. */
+GD bool guided_sample(const guide::Lobes& L, float mix, const Mat& mat, V3 albedo, V3 n, V3 wo, uint32_t& rng,
+                      BsdfSample& s, float& pdfBsdf) {
+    float u = sample1f(rng);
+    V3 r = sample3f(rng);
+    if (u < mix) {
+        float d[3];
+        guide::lobes_sample(L, r.x, r.y, r.z, d);
+        s.wi = v3(d[0], d[1], d[2]);
+        if (dot3(n, s.wi) <= 0.0f) return false;   /* no reflection there: a zero sample */
+        s.bsdf = evalBSDF(mat, albedo, n, wo, s.wi);
+        pdfBsdf = evalPdf(mat, n, wo, s.wi);
+        s.type = kReflection | (mat.type == 1u ? kDiffuse : kGlossy);
+    } else {
+        if (!sampleBSDF(mat, albedo, n, wo, r, s)) return false;
+        pdfBsdf = s.pdf;
+    }
+    s.pdf = mix * guide::lobes_pdf(L, s.wi.x, s.wi.y, s.wi.z) + (1.0f - mix) * pdfBsdf;
+    return s.pdf >= 1e-6f;
+}
+
+/* The mixture at the primary vertex of pixel `idx` of the view (guided batches): false where
+ * the primary vertex is not guided. */
+GD bool primary_lobes(const PassCtx& P, uint64_t idx, const Mat& mat, guide::Lobes& L) {
+    if (!P.gPrim || !guide_material(mat) || P.set.maxDepth < 2u) return false;
+    guide::make_lobes(P.gPrim + ((uint64_t)P.pixelBase + idx) * guide::kRaw, L);
+    return true;
 }
 
 /* tracePath (gris_path_trace.glsl:45-306) as a state machine: begin() is the prologue up to the
@@ -325,23 +365,7 @@ struct PathTracerT {
         if constexpr (kGuide) {
             thrSampled = throughput;
             if (L) {
-                /* one-sample MIS of the guide mixture (probability mix) and the BSDF sampler */
-                float u = sample1f(rng);
-                V3 r = sample3f(rng);
-                if (u < mix) {
-                    float d[3];
-                    guide::lobes_sample(*L, r.x, r.y, r.z, d);
-                    s.wi = v3(d[0], d[1], d[2]);
-                    if (dot3(surf.norm, s.wi) <= 0.0f) return false;   /* no reflection there: a zero sample */
-                    s.bsdf = evalBSDF(mat, surf.albedo, surf.norm, wo, s.wi);
-                    pdfHit = evalPdf(mat, surf.norm, wo, s.wi);
-                    s.type = kReflection | (mat.type == 1u ? kDiffuse : kGlossy);
-                } else {
-                    if (!sampleBSDF(mat, surf.albedo, surf.norm, wo, r, s)) return false;
-                    pdfHit = s.pdf;
-                }
-                s.pdf = mix * guide::lobes_pdf(*L, s.wi.x, s.wi.y, s.wi.z) + (1.0f - mix) * pdfHit;
-                if (!(s.pdf >= 1e-6f)) return false;
+                if (!guided_sample(*L, mix, mat, surf.albedo, surf.norm, wo, rng, s, pdfHit)) return false;
             } else {
                 if (!sampleBSDF(mat, surf.albedo, surf.norm, wo, sample3f(rng), s) || s.pdf < 1e-6f) return false;
                 pdfHit = s.pdf;
@@ -413,7 +437,7 @@ using PathTracer = PathTracerT<false>;
 /* ------------------------------------------------------------------ hybrid shift (gris_retrace.glsl) */
 /* traceReplayPathForHybridShift (:42-136) */
 GD void traceReplay(const PassCtx& P, Isec isec, Surf surf, Ray3 ray, uint32_t targetFlags, uint32_t rng, RcData& rcData,
-                    RayCount& rc, int& err) {
+                    RayCount& rc, int& err, const guide::Lobes* L = nullptr) {
     const DevScene& sc = P.sc;
     V3 throughput = v3s(1.0f);
     V3 wo = -ray.dir;
@@ -456,7 +480,13 @@ GD void traceReplay(const PassCtx& P, Isec isec, Surf surf, Ray3 ray, uint32_t t
             if (sample1f(rng) < pdfTerminate) break;
             throughput = throughput / (1.0f - pdfTerminate);
         }
-        if (!sampleBSDF(mat, surf.albedo, surf.norm, wo, sample3f(rng), s) || s.pdf < 1e-6f) break;
+        if (L && bounce == 0) {
+            /* a guided batch draws the primary vertex's direction from the destination pixel's mixture */
+            float pdfBsdf;
+            if (!guided_sample(*L, P.gMix, mat, surf.albedo, surf.norm, wo, rng, s, pdfBsdf)) break;
+        } else if (!sampleBSDF(mat, surf.albedo, surf.norm, wo, sample3f(rng), s) || s.pdf < 1e-6f) {
+            break;
+        }
         float cosTheta = isSampleTypeDelta(s.type) ? 1.0f : absDot(surf.norm, s.wi);
         V3 scatterTerm = s.bsdf * cosTheta / s.pdf;
         throughput = throughput * scatterTerm;
@@ -468,7 +498,8 @@ GD void traceReplay(const PassCtx& P, Isec isec, Surf surf, Ray3 ray, uint32_t t
 
 /* GRISReservoirReuseAndMerge (:138-236) */
 GD void reuseAndMerge(const PassCtx& P, Resv& dstResv, const Surf& dstPrimarySurf, const Isec& dstPrimaryIsec,
-                      const Ray3& primaryRay, Resv srcResv, uint32_t& rng, RayCount& rc, int& err) {
+                      const Ray3& primaryRay, Resv srcResv, uint32_t& rng, RayCount& rc, int& err,
+                      const guide::Lobes* L = nullptr) {
     const DevScene& sc = P.sc;
     PathSample srcSample = srcResv.s;
     RcData dstRcData;
@@ -481,7 +512,8 @@ GD void reuseAndMerge(const PassCtx& P, Resv& dstResv, const Surf& dstPrimarySur
     float dstJacobian = 0.0f, jacobian = 0.0f, dist = 0.0f, dstPHat = 0.0f, dstSamplePdf = 0.0f;
 
     if (srcSample.rcIsec.inst != kInvalidHit) {
-        traceReplay(P, dstPrimaryIsec, dstPrimarySurf, primaryRay, srcSample.flags, srcSample.primaryRng, dstRcData, rc, err);
+        traceReplay(P, dstPrimaryIsec, dstPrimarySurf, primaryRay, srcSample.flags, srcSample.primaryRng, dstRcData, rc, err,
+                    L);
         if (dstRcData.rcPrevIsec.inst != kInvalidHit) {
             if (dstRcData.rcPrevIsec.inst == kSpecialHit) rcPrevSurf = dstPrimarySurf;
             else loadSurfaceInfo(sc, dstRcData.rcPrevIsec, rcPrevSurf);
@@ -516,6 +548,8 @@ GD void reuseAndMerge(const PassCtx& P, Resv& dstResv, const Surf& dstPrimarySur
                 dstSamplePdf = luminance(rcSurf.albedo) / sumPower / dstJacobian;
             } else {
                 dstSamplePdf = evalPdf(rcPrevMat, rcPrevSurf.norm, dstRcData.rcPrevWo, wi);
+                if (L && dstRcData.rcPrevIsec.inst == kSpecialHit)   /* the destination's primary vertex is guided */
+                    dstSamplePdf = P.gMix * guide::lobes_pdf(*L, wi.x, wi.y, wi.z) + (1.0f - P.gMix) * dstSamplePdf;
             }
         }
         float srcPHat = luminance(srcSample.F);
@@ -536,7 +570,8 @@ GD void reuseAndMerge(const PassCtx& P, Resv& dstResv, const Surf& dstPrimarySur
 /* temporalReuse (gris_resample_temporal.glsl:36-83): begin() finds the previous reservoir
  * (findPreviousReservoir, :11-34) and finishes the pixel when there is nothing to merge;
  * step() shifts and merges it and writes the temporary reservoir. */
-struct TemporalTask {
+template <bool kGuide>
+struct TemporalTaskT {
     uint64_t idx;
     Resv resv, src;
     Surf dst;
@@ -597,18 +632,25 @@ struct TemporalTask {
     }
 
     GD bool step(const PassCtx& P, RayCount& rc, int& err) {
-        reuseAndMerge(P, resv, dst, dstIsec, ray, src, resvRng, rc, err);
+        const guide::Lobes* Lp = nullptr;
+        guide::Lobes L;
+        if constexpr (kGuide) {
+            if (primary_lobes(P, idx, load_material(P.sc, dst.matIndex), L)) Lp = &L;
+        }
+        reuseAndMerge(P, resv, dst, dstIsec, ray, src, resvRng, rc, err, Lp);
         finish(P);
         return false;
     }
 };
+using TemporalTask = TemporalTaskT<false>;
 
 /* ------------------------------------------------------------------ spatial reuse + final shading */
 /* spatialReuse (gris_resample_spatial.glsl:36-135) + the running mean of
  * gris_resample_spatial.comp:21-27. begin() reads the pixel (a background pixel only updates the
  * running mean); each step() handles one neighbour (findNeighborReservoir, :11-34, then the shift
  * and merge); the last step writes the reservoir, shades and accumulates. */
-struct SpatialTask {
+template <bool kGuide>
+struct SpatialTaskT {
     uint32_t ix, iy, i, rng;
     uint64_t idx;
     Resv resv;
@@ -670,7 +712,14 @@ struct SpatialTask {
             if (dot3(normalN, dst.norm) < 0.9f || distance3(dst.pos, posN) > 0.4f) return true;
             uint32_t nidx = (uint32_t)P.cam.w * (uint32_t)py + (uint32_t)px;
             Resv neighborResv = load_resv(P.b.reservoirTemp, nidx, n);
-            if (resvIsValid(neighborResv)) reuseAndMerge(P, resv, dst, dstIsec, ray, neighborResv, rng, rc, err);
+            if (resvIsValid(neighborResv)) {
+                const guide::Lobes* Lp = nullptr;
+                guide::Lobes L;
+                if constexpr (kGuide) {
+                    if (primary_lobes(P, idx, load_material(sc, dst.matIndex), L)) Lp = &L;
+                }
+                reuseAndMerge(P, resv, dst, dstIsec, ray, neighborResv, rng, rc, err, Lp);
+            }
             return true;
         }
         resvResetIfInvalid(resv);
@@ -681,7 +730,12 @@ struct SpatialTask {
             if (pathSample.rcIsec.inst != kInvalidHit) {
                 RcData rcData;
                 rcData.rcPrevIsec = isec_zero(); rcData.rcPrevWo = v3s(0.0f); rcData.rcPrevThroughput = v3s(0.0f);
-                traceReplay(P, dstIsec, dst, ray, pathSample.flags, pathSample.primaryRng, rcData, rc, err);
+                const guide::Lobes* Lp = nullptr;
+                guide::Lobes L;
+                if constexpr (kGuide) {
+                    if (primary_lobes(P, idx, load_material(sc, dst.matIndex), L)) Lp = &L;
+                }
+                traceReplay(P, dstIsec, dst, ray, pathSample.flags, pathSample.primaryRng, rcData, rc, err, Lp);
                 if (rcData.rcPrevIsec.inst != kInvalidHit) {
                     Surf rcPrevSurf = surf_zero(), rcSurf = surf_zero();
                     if (rcData.rcPrevIsec.inst == kSpecialHit) rcPrevSurf = dst;
@@ -705,6 +759,7 @@ struct SpatialTask {
         return false;
     }
 };
+using SpatialTask = SpatialTaskT<false>;
 
 struct PathTask {
     PathTracer t;
@@ -1290,6 +1345,7 @@ struct WaveCtx {
     float* gFeat;        /* per guided vertex (queue order): position in [0,1]^3, normal, wo */
     float* gOut;         /* per guided vertex: the network's 40 raw outputs */
     float* gRec;         /* per path: its training record (features 9, direction 3, throughput 3, sum 3) */
+    float* gPrimFeat;    /* per path: the guide's inputs at its primary vertex */
     uint32_t* gFrame;    /* [0] guided vertices this frame, [1] record probability (float bits) */
     guide::GuideDevice guide;
     uint32_t frameSeed;
@@ -1574,20 +1630,72 @@ __global__ void k_guide_frame_begin(uint32_t* frame, uint32_t* tCount, uint32_t 
     *tCount = 0u;
 }
 
+/* The guide's inputs at every pixel's primary vertex (zeros for the background), for one
+ * inference over the whole batch before the path tracer. */
+__global__ void __launch_bounds__(128) k_guide_primary_features(WaveCtx C, float* feat) {
+    uint32_t id = blockIdx.x * blockDim.x + threadIdx.x;
+    if (id >= C.totalPixels) return;
+    int v; uint32_t x, y;
+    path_coords(C, id, v, x, y);
+    const ViewEntry& V = C.V[v];
+    const PassCtx& P = V.P;
+    const int W = (int)P.b.width, H = (int)P.b.height;
+    V2 uv = v2(((float)x + 0.5f) / (float)W, ((float)y + 0.5f) / (float)H);
+    float depth = 0.0f; V3 norm = v3s(0.0f), albedo = v3s(0.0f); int matMeshId = 0;
+    float4 dn = texture_bilinear(reinterpret_cast<const float4*>(P.b.depthNormal), W, H, uv);
+    uint2 am = fetch_am(reinterpret_cast<const uint2*>(P.b.albedoMatId), W, H, (int)x, (int)y);
+    float f[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+    if (unpackGBuffer(dn, am, depth, norm, albedo, matMeshId)) {
+        Ray3 ray = pinholeCameraSampleRay(P.cam, v2(uv.x, 1.0f - uv.y));
+        V3 pos = ray.ori + ray.dir * (depth - 1e-4f);
+        f[0] = fminf(fmaxf((pos.x - V.boxMin[0]) * V.boxInv[0], 0.0f), 1.0f);
+        f[1] = fminf(fmaxf((pos.y - V.boxMin[1]) * V.boxInv[1], 0.0f), 1.0f);
+        f[2] = fminf(fmaxf((pos.z - V.boxMin[2]) * V.boxInv[2], 0.0f), 1.0f);
+        f[3] = norm.x; f[4] = norm.y; f[5] = norm.z;
+        f[6] = -ray.dir.x; f[7] = -ray.dir.y; f[8] = -ray.dir.z;
+    }
+    for (int k = 0; k < 9; k++) feat[(size_t)id * 9 + k] = f[k];
+}
+
+/* Keeps the guided vertex just sampled as the path's training record with the frame's record
+ * probability (a hash of the frame, the path and the level). */
+GD void guide_maybe_record(const WaveCtx& C, GuidedTracer& t, uint32_t id, int level, const float* feat, float pKeep,
+                           uint32_t frame) {
+    uint32_t h = hash2(frame * 0x9e3779b9u ^ hash2(id * 0x85ebca6bu + (uint32_t)level));
+    if ((float)(h >> 8) * (1.0f / 16777216.0f) >= pKeep) return;
+    float* r = C.gRec + (size_t)id * 18;
+    for (int k = 0; k < 9; k++) r[k] = feat[k];
+    r[9] = t.s.wi.x; r[10] = t.s.wi.y; r[11] = t.s.wi.z;
+    r[12] = t.thrSampled.x; r[13] = t.thrSampled.y; r[14] = t.thrSampled.z;
+    r[15] = t.accAll.x; r[16] = t.accAll.y; r[17] = t.accAll.z;
+    t.rec = 1u;
+}
+
+/* level 0 of a guided batch: the primary vertex's direction is drawn from the pixel's mixture
+ * (the hybrid shift replays that draw with the destination pixel's mixture) */
 __global__ void __launch_bounds__(128) k_gwave_begin(WaveCtx C) {
     uint32_t id = blockIdx.x * blockDim.x + threadIdx.x;
-    bool push = false;
+    bool push = false, guided = false;
     if (id < C.totalPixels) {
         int v; uint32_t x, y;
         path_coords(C, id, v, x, y);
         const PassCtx& P = C.V[v].P;
         GuidedTracer t;
         if (t.begin(P, x, y)) {
-            int r = t.shade(P, isec_zero());   /* no NEE at bounce 0; never guided */
-            bool cont = r == GuidedTracer::kPost ? t.post(P, false) : false;
+            int r = t.shade(P, isec_zero());   /* no NEE at bounce 0 */
+            bool cont = false;
+            if (r == GuidedTracer::kPost) {
+                guide::Lobes L;
+                guided = primary_lobes(P, (uint64_t)y * P.b.width + x, t.mat, L);
+                cont = t.post(P, false, guided ? &L : nullptr, P.gMix);
+                if (cont && guided)
+                    guide_maybe_record(C, t, id, 0, C.gPrimFeat + (size_t)id * 9, __uint_as_float(C.gFrame[1]), C.gFrame[2]);
+            }
             wave_continue(C, P, t, id, cont, 0, push);
         }
     }
+    unsigned m = __ballot_sync(0xffffffffu, guided);
+    if (m && (threadIdx.x & 31u) == (uint32_t)(__ffs(m) - 1)) atomicAdd(C.gFrame, (uint32_t)__popc(m));
     warp_push(C.queue[1], C.counts + 1, push, id);
 }
 
@@ -1666,18 +1774,7 @@ __global__ void __launch_bounds__(128) k_gwave_post(WaveCtx C, int level) {
             guided = slot1 != 0u;
             bool blocked = t.nee ? C.blocked[id] != 0 : false;
             bool cont = t.post(P, blocked, guided ? &L : nullptr, C.guide.mix);
-            if (cont && guided) {
-                uint32_t h = hash2(frame * 0x9e3779b9u ^ hash2(id * 0x85ebca6bu + (uint32_t)level));
-                if ((float)(h >> 8) * (1.0f / 16777216.0f) < pKeep) {
-                    float* r = C.gRec + (size_t)id * 18;
-                    const float* f = C.gFeat + (size_t)(slot1 - 1u) * 9;
-                    for (int k = 0; k < 9; k++) r[k] = f[k];
-                    r[9] = t.s.wi.x; r[10] = t.s.wi.y; r[11] = t.s.wi.z;
-                    r[12] = t.thrSampled.x; r[13] = t.thrSampled.y; r[14] = t.thrSampled.z;
-                    r[15] = t.accAll.x; r[16] = t.accAll.y; r[17] = t.accAll.z;
-                    t.rec = 1u;
-                }
-            }
+            if (cont && guided) guide_maybe_record(C, t, id, level, C.gFeat + (size_t)(slot1 - 1u) * 9, pKeep, frame);
             wave_continue(C, P, t, id, cont, level, push);
         }
         unsigned m = __ballot_sync(0xffffffffu, guided);
@@ -1687,12 +1784,13 @@ __global__ void __launch_bounds__(128) k_gwave_post(WaveCtx C, int level) {
 }
 
 size_t guide_wave_bytes_per_path() {
-    return sizeof(uint32_t) + (9 + guide::kRaw + 18) * sizeof(float);
+    return sizeof(uint32_t) + (9 + guide::kRaw + 18 + 9 + guide::kRaw) * sizeof(float);
 }
 
 size_t wave_bytes_per_path() { return sizeof(WaveRec) + sizeof(NeeRec) + sizeof(Isec) + 1 + 3 * sizeof(uint32_t); }
 
-BatchShape fill_view_table(const BatchView* views, int n, void* hViews, unsigned long long* counters, int countWork) {
+BatchShape fill_view_table(const BatchView* views, int n, void* hViews, unsigned long long* counters, int countWork,
+                           const float* gPrim, float gMix) {
     BatchShape sh;
     sh.n = n; sh.tiles = 0; sh.pixels = 0; sh.maxDepth = 0;
     ViewEntry* H = reinterpret_cast<ViewEntry*>(hViews);
@@ -1707,6 +1805,9 @@ BatchShape fill_view_table(const BatchView* views, int n, void* hViews, unsigned
         e.P.set = bv.set;
         e.P.b = bv.b;
         e.P.counters = counters;
+        e.P.gPrim = gPrim;
+        e.P.gMix = gMix;
+        e.P.pixelBase = sh.pixels;
         e.G.sc = e.P.sc;
         e.G.cam = e.P.cam;
         for (int k = 0; k < 16; k++) e.G.lastProjView[k] = bv.cam.lastProjView[k];
@@ -1760,7 +1861,7 @@ cudaError_t enqueue_batch(const BatchShape& sh, void* dViews, const void* hViews
             C.counters = counters;
             C.countWork = countWork;
             C.postQueue = wb.postQueue;
-            C.gFeat = wb.gFeat; C.gOut = wb.gOut; C.gRec = wb.gRec; C.gFrame = wb.gFrame;
+            C.gFeat = wb.gFeat; C.gOut = wb.gOut; C.gRec = wb.gRec; C.gFrame = wb.gFrame; C.gPrimFeat = wb.gPrimFeat;
             if (guide) C.guide = *guide; else memset(&C.guide, 0, sizeof(C.guide));
             C.frameSeed = 0u;
             e = cudaMemsetAsync(wb.counts, 0, 1536 * sizeof(uint32_t), stream);
@@ -1775,6 +1876,16 @@ cudaError_t enqueue_batch(const BatchShape& sh, void* dViews, const void* hViews
                 /* guided: every path continues through post(); guided vertices get the network's
                  * mixture between the shading and post() (timer slot 9) */
                 k_guide_frame_begin<<<1, 1, 0, stream>>>(wb.gFrame, guide->tCount, guide->cap);
+                mark(9, true);
+                k_guide_primary_features<<<(pixels + 127) / 128, 128, 0, stream>>>(C, wb.gPrimFeat);
+                {
+                    guide::FwdArgs fa;
+                    fa.wPacked = guide->wPacked; fa.bias = guide->bias; fa.feat = wb.gPrimFeat;
+                    fa.count = nullptr; fa.n = pixels; fa.out = wb.gPrimOut;
+                    e = guide::launch_forward(fa, stream);
+                    if (e != cudaSuccess) return e;
+                }
+                mark(9, false);
                 mark(4, true);
                 k_gwave_begin<<<(pixels + 127) / 128, 128, 0, stream>>>(C);
                 mark(4, false);
@@ -1831,12 +1942,14 @@ cudaError_t enqueue_batch(const BatchShape& sh, void* dViews, const void* hViews
 reuse:
     if (passes & 2) {
         if (timer) timer->mark(2, true, stream);
-        k_batch_pass<TemporalTask, 2><<<tiles, blk, 0, stream>>>(V, n);
+        if (guide) k_batch_pass<TemporalTaskT<true>, 2><<<tiles, blk, 0, stream>>>(V, n);
+        else k_batch_pass<TemporalTask, 2><<<tiles, blk, 0, stream>>>(V, n);
         if (timer) timer->mark(2, false, stream);
     }
     if (passes & 4) {
         if (timer) timer->mark(3, true, stream);
-        k_batch_pass<SpatialTask, 3><<<tiles, blk, 0, stream>>>(V, n);
+        if (guide) k_batch_pass<SpatialTaskT<true>, 3><<<tiles, blk, 0, stream>>>(V, n);
+        else k_batch_pass<SpatialTask, 3><<<tiles, blk, 0, stream>>>(V, n);
         if (timer) timer->mark(3, false, stream);
     }
     return cudaGetLastError();
@@ -1846,7 +1959,7 @@ cudaError_t launch_batch(const BatchView* views, int n, void* dViews, void* hVie
                          unsigned long long* counters, int countWork, KernelTimer* timer, cudaStream_t stream,
                          int pathForm, int passes, const WaveLaunch& wl) {
     if (n <= 0 || n > 4096) return cudaErrorInvalidValue;
-    BatchShape sh = fill_view_table(views, n, hViews, counters, countWork);
+    BatchShape sh = fill_view_table(views, n, hViews, counters, countWork, nullptr, 0.0f);
     return enqueue_batch(sh, dViews, hViews, wb, counters, countWork, timer, stream, pathForm, passes, wl, nullptr);
 }
 

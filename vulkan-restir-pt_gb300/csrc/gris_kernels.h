@@ -72,6 +72,8 @@ struct WaveBuffers {
     float* gOut;
     float* gRec;
     uint32_t* gFrame;
+    float* gPrimFeat;   /* the guide's inputs / raw outputs at every path's primary vertex */
+    float* gPrimOut;
 };
 /* bytes per path of the guided-batch buffers */
 size_t guide_wave_bytes_per_path();
@@ -92,7 +94,8 @@ struct BatchShape {
 };
 
 /* Writes the view table of a frame into hViews (pinned host memory). */
-BatchShape fill_view_table(const BatchView* views, int n, void* hViews, unsigned long long* counters, int countWork);
+BatchShape fill_view_table(const BatchView* views, int n, void* hViews, unsigned long long* counters, int countWork,
+                           const float* gPrim = nullptr, float gMix = 0.0f);
 /* Enqueues one batch frame: copy of the view table, then the kernels. passes: bit 3 G-buffer,
  * bit 0 path trace, bit 1 temporal, bit 2 spatial. pathForm: GRIS_PATH_MEGAKERNEL or
  * GRIS_PATH_WAVEFRONT. Only stream operations: it can be captured into a CUDA graph. */
