@@ -113,6 +113,8 @@ def parse():
     ap.add_argument("--impl", default="grisrt", choices=["grisrt", "reference"])
     ap.add_argument("--workload", default="c2", choices=["c1", "c2", "c3", "c4"])
     ap.add_argument("--ref-spp", type=int, default=1024, help="c4: samples per pixel of the converged image")
+    ap.add_argument("--mis", default="reference", choices=["reference", "pairwise"],
+                    help="c4: the reuse passes' MIS weights (the reference's merge, or the pairwise extension)")
     ap.add_argument("--c4-reuse", default="on", choices=["on", "off"],
                     help="c4: temporal + spatial reuse on (ReSTIR PT) or off (the canonical samples alone)")
     ap.add_argument("--width", type=int, default=1920)
@@ -309,7 +311,8 @@ def run_guided(args):
     scene = G.Scene(ctx, hs)
     reuse = args.c4_reuse == "on"
     st = G.Settings.make(shiftType=2, rrScale=1.0, temporalReuse=reuse, spatialReuse=reuse, cap=20,
-                         maxDepth=args.depth, spatialNeighbors=3, spatialRadius=20.0)
+                         maxDepth=args.depth, spatialNeighbors=3, spatialRadius=20.0,
+                         misWeights=1 if args.mis == "pairwise" else 0)
     stream = torch.cuda.ExternalStream(ctx.stream(), device=torch.device("cuda", 0))
     cam0 = hs.camera(0, 60, W, H)
     cams, prevs = [], []
@@ -424,7 +427,7 @@ def run_guided(args):
                                    "frames accumulated" % (W, H, hs.triangle_count(), args.depth),
                        "guide": "MLP 80-64x4-48 BF16 mma.sync, 8 vMF lobes, mix 0.5, Adam 1e-3, 2^18 records/frame, 4 steps"},
             "reference": {"spp": args.ref_spp, "seconds": ref_s, "estimator": "candidates"},
-            "reuse": reuse, "clocks": clocks,
+            "reuse": reuse, "mis": args.mis, "clocks": clocks,
             "median_error_time_ratio": ratio_med,
             "plain": {"fps": 1000.0 / float(tp.mean()), "total_ms": float(Tp), "relmse_final": float(rp[-1]),
                       "median_final": float(mp[-1]), "relmse_curve": [float(x) for x in rp],

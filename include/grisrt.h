@@ -137,7 +137,10 @@ typedef struct GrisSettings {
     uint32_t spatialNeighbors;  /* ResampleNum, gris_resample_spatial.glsl:65 (3) */
     float spatialRadius;        /* ResampleRadius in pixels, gris_resample_spatial.glsl:66 (20) */
     float envRadiance[3];       /* extension: constant environment (0 = the reference: a miss ends the path) */
-    uint32_t reserved[5];
+    uint32_t misWeights;        /* extension: 0 = the reference's merge (M-proportional weights); 1 = pairwise
+                                   generalised balance heuristic (each reused sample and the canonical one are
+                                   weighed against each other through shifts in both directions) */
+    uint32_t reserved[4];
 } GrisSettings;
 
 /* Host-side scene arrays (what DeviceScene uploads, src/Scene.cpp:368-446). */

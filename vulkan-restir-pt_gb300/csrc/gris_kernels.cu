@@ -32,6 +32,7 @@ struct PassCtx {
     /* guided batches: the network's raw outputs at every pixel's primary vertex (indexed by the
      * batch's path id = pixelBase + pixel), and the probability of drawing from the guide */
     const float* gPrim;
+    const float* gPrimPrev;   /* the previous frame's, for shifts into the previous frame's pixels */
     float gMix;
     uint32_t pixelBase;
 };
@@ -150,11 +151,13 @@ GD bool guided_sample(const guide::Lobes& L, float mix, const Mat& mat, V3 albed
 
 /* The mixture at the primary vertex of pixel `idx` of the view (guided batches): false where
  * the primary vertex is not guided. */
-GD bool primary_lobes(const PassCtx& P, uint64_t idx, const Mat& mat, guide::Lobes& L) {
-    if (!P.gPrim || !guide_material(mat) || P.set.maxDepth < 2u) return false;
-    guide::make_lobes(P.gPrim + ((uint64_t)P.pixelBase + idx) * guide::kRaw, L);
+GD bool primary_lobes(const PassCtx& P, uint64_t idx, const Mat& mat, guide::Lobes& L, bool previousFrame = false) {
+    const float* g = previousFrame ? P.gPrimPrev : P.gPrim;
+    if (!g || !guide_material(mat) || P.set.maxDepth < 2u) return false;
+    guide::make_lobes(g + ((uint64_t)P.pixelBase + idx) * guide::kRaw, L);
     return true;
 }
+
 
 /* tracePath (gris_path_trace.glsl:45-306) as a state machine: begin() is the prologue up to the
  * bounce loop, step() one iteration of the loop (false where the reference breaks), end() the
@@ -496,7 +499,86 @@ GD void traceReplay(const PassCtx& P, Isec isec, Surf surf, Ray3 ray, uint32_t t
     }
 }
 
-/* GRISReservoirReuseAndMerge (:138-236) */
+/* The shift of a path sample into a destination pixel's domain (gris_retrace.glsl:138-219):
+ * prefix replay from the destination's primary vertex, reconnection, visibility. On success
+ * `out` is the shifted sample (F, rcJacobian and rcPrevSamplePdf of the destination) and
+ * dstPHat = luminance(F * jacobian); srcPHat = luminance(src.F). */
+struct Shift {
+    bool valid;
+    float dstPHat, srcPHat;
+    PathSample out;
+};
+GD Shift shiftToDomain(const PassCtx& P, const Surf& dstPrimarySurf, const Isec& dstPrimaryIsec, const Ray3& primaryRay,
+                       const PathSample& srcIn, RayCount& rc, int& err, const guide::Lobes* L = nullptr) {
+    const DevScene& sc = P.sc;
+    PathSample srcSample = srcIn;
+    RcData dstRcData;
+    dstRcData.rcPrevIsec = isec_zero(); dstRcData.rcPrevWo = v3s(0.0f); dstRcData.rcPrevThroughput = v3s(0.0f);
+    Surf rcPrevSurf = surf_zero(), rcSurf = surf_zero();
+    Mat rcMat = load_material(sc, 0xffffffffu), rcPrevMat = rcMat;
+    V3 wi = v3s(0.0f);
+    V3 Li = v3s(0.0f);
+    bool srcSampleValid = false;
+    float dstJacobian = 0.0f, jacobian = 0.0f, dist = 0.0f, dstPHat = 0.0f, dstSamplePdf = 0.0f;
+
+    if (srcSample.rcIsec.inst != kInvalidHit) {
+        traceReplay(P, dstPrimaryIsec, dstPrimarySurf, primaryRay, srcSample.flags, srcSample.primaryRng, dstRcData, rc, err,
+                    L);
+        if (dstRcData.rcPrevIsec.inst != kInvalidHit) {
+            if (dstRcData.rcPrevIsec.inst == kSpecialHit) rcPrevSurf = dstPrimarySurf;
+            else loadSurfaceInfo(sc, dstRcData.rcPrevIsec, rcPrevSurf);
+            loadSurfaceInfo(sc, srcSample.rcIsec, rcSurf);
+            rcMat = load_material(sc, rcSurf.matIndex);
+            rcPrevMat = load_material(sc, rcPrevSurf.matIndex);
+            dist = distance3(rcPrevSurf.pos, rcSurf.pos);
+            wi = normalize3(rcSurf.pos - rcPrevSurf.pos);
+            float cosTheta = -dot3(rcSurf.norm, wi);
+            dstJacobian = fabsf(cosTheta) / square(dist);
+            jacobian = dstJacobian / srcSample.rcJacobian;
+            if (dist > kDistanceThreshold && cosTheta > 0.0f && !isnan(jacobian) && srcSample.rcJacobian > 0.0f &&
+                isBSDFConnectible(rcPrevMat)) {
+                if (traceVisibility(sc, rcPrevSurf.pos, rcSurf.pos, rc, err)) srcSampleValid = true;
+            }
+        }
+    }
+
+    Shift r;
+    r.valid = srcSampleValid;
+    r.dstPHat = 0.0f;
+    r.srcPHat = luminance(srcSample.F);
+    if (srcSampleValid) {
+        uint32_t rcType = rcVertexType(srcSample.flags);
+        if (!isnan(srcSample.rcPrevSamplePdf) && srcSample.rcPrevSamplePdf > 1e-6f) {
+            Li = srcSample.rcLi;
+            if (rcType == kRcSurface && length3(srcSample.rcWi) > 0.5f) {
+                Li = Li * (evalBSDF(rcMat, rcSurf.albedo, rcSurf.norm, -wi, srcSample.rcWi) * satDot(rcSurf.norm, srcSample.rcWi));
+            }
+            Li = Li * (evalBSDF(rcPrevMat, rcPrevSurf.albedo, rcPrevSurf.norm, dstRcData.rcPrevWo, wi) * satDot(rcPrevSurf.norm, wi));
+            Li = Li * dstRcData.rcPrevThroughput;
+            Li = Li / srcSample.rcPrevSamplePdf;
+            if (!isBlack(Li) && !isnan3(Li)) dstPHat = luminance(Li * jacobian);
+            if (rcType == kRcLightSampled) {
+                float sumPower = load_table(sc, 0).prob;
+                dstSamplePdf = luminance(rcSurf.albedo) / sumPower / dstJacobian;
+            } else {
+                dstSamplePdf = evalPdf(rcPrevMat, rcPrevSurf.norm, dstRcData.rcPrevWo, wi);
+                if (L && dstRcData.rcPrevIsec.inst == kSpecialHit)   /* the destination's primary vertex is guided */
+                    dstSamplePdf = P.gMix * guide::lobes_pdf(*L, wi.x, wi.y, wi.z) + (1.0f - P.gMix) * dstSamplePdf;
+            }
+        }
+        srcSample.rcJacobian = dstJacobian;
+        srcSample.rcPrevSamplePdf = dstSamplePdf;
+        srcSample.F = Li;
+        if (srcSample.rcPrevSamplePdf < 1e-6f || isnan(srcSample.rcPrevSamplePdf)) srcSample.rcPrevSamplePdf = 0.0f;
+        r.dstPHat = dstPHat;
+    }
+    r.out = srcSample;
+    return r;
+}
+
+/* GRISReservoirReuseAndMerge (:138-236): the shift (as shiftToDomain, written out here: this
+ * form keeps the reuse kernels' register footprint), the source weight scaled by the ratio of
+ * the targets, the merge (M adds up: the M-proportional weights of the reference), the M cap. */
 GD void reuseAndMerge(const PassCtx& P, Resv& dstResv, const Surf& dstPrimarySurf, const Isec& dstPrimaryIsec,
                       const Ray3& primaryRay, Resv srcResv, uint32_t& rng, RayCount& rc, int& err,
                       const guide::Lobes* L = nullptr) {
@@ -566,11 +648,67 @@ GD void reuseAndMerge(const PassCtx& P, Resv& dstResv, const Surf& dstPrimarySur
     resvCap(dstResv, (float)P.set.cap);
 }
 
+/* Pairwise generalised balance heuristic (GrisSettings.misWeights = 1). The canonical reservoir
+ * c (M_c, sample x_c) and k reused reservoirs i (M_i, x_i): pair i weighs technique i against
+ * a 1/k share of the canonical one, m_i(y) = M_i p_i(y) / (M_i p_i(y) + (M_c/k) p_c(y)), where
+ * p_i(y) is i's target at the shift of y into i's pixel times the shift's Jacobian. For a
+ * reused sample y_i = T(x_i) that is M_i pHat_i(x_i) / (M_i pHat_i(x_i) + (M_c/k) dstPHat) (the
+ * forward shift's numbers); the canonical sample gets (1/k) sum over the pairs of the
+ * complementary weight, which needs the shift of x_c into each reused pixel (backward shift).
+ * Resampling weights w = m * target * unbiased contribution weight (= resampleWeight / M of the
+ * source); the merged reservoir keeps the reference's representation (resampleWeight = sum w *
+ * M, M = sum of the Ms), so the final shading is unchanged. */
+struct PairwiseMerge {
+    float Mc, pc, Rc;      /* canonical: M, target of its own sample, resampleWeight */
+    float k, mcSum, wSum, M;
+    PathSample canon, sel;
+    GD void begin(const Resv& canonical, float kNeighbours) {
+        Mc = canonical.sampleCount;
+        pc = luminance(canonical.s.F);
+        Rc = canonical.resampleWeight;
+        k = kNeighbours;
+        mcSum = 0.0f; wSum = 0.0f; M = Mc;
+        canon = canonical.s;
+        sel = canonical.s;
+    }
+    /* a reused reservoir: its forward shift, and the target of the canonical sample shifted into
+     * its pixel times that shift's Jacobian (pBack, 0 if the shift failed) */
+    GD void add(const Resv& src, const Shift& fw, float pBack, float rnd) {
+        const float Mi = src.sampleCount;
+        if (pc > 0.0f) {
+            float a = (Mc / k) * pc, b = Mi * pBack;
+            mcSum += a / (a + b);
+        }
+        float w = 0.0f;
+        if (fw.valid && fw.dstPHat > 0.0f && fw.srcPHat > 0.0f && Mi > 0.0f)
+            w = (1.0f / k) * fw.dstPHat * src.resampleWeight / (Mi * fw.srcPHat + (Mc / k) * fw.dstPHat);
+        if (!(w >= 0.0f) || isinf(w)) w = 0.0f;
+        wSum += w;
+        if (rnd * wSum < w) sel = fw.out;
+        M += Mi;
+    }
+    /* a reused slot without a reservoir: its pair gives the canonical sample the full weight */
+    GD void skip() { if (pc > 0.0f) mcSum += 1.0f; }
+    /* the canonical candidate last, then the merged reservoir */
+    GD Resv finish(float rnd, float cap) {
+        float wc = (pc > 0.0f && Mc > 0.0f) ? (mcSum / k) * Rc / Mc : 0.0f;
+        if (!(wc >= 0.0f) || isinf(wc)) wc = 0.0f;
+        float total = wSum + wc;
+        Resv out = resv_zero();
+        resvReset(out);
+        out.s = (rnd * total < wc) ? canon : sel;
+        out.sampleCount = M;
+        out.resampleWeight = total * M;
+        resvCap(out, cap);
+        return out;
+    }
+};
+
 /* ------------------------------------------------------------------ temporal reuse */
 /* temporalReuse (gris_resample_temporal.glsl:36-83): begin() finds the previous reservoir
  * (findPreviousReservoir, :11-34) and finishes the pixel when there is nothing to merge;
  * step() shifts and merges it and writes the temporary reservoir. */
-template <bool kGuide>
+template <bool kGuide, bool kPair = false>
 struct TemporalTaskT {
     uint64_t idx;
     Resv resv, src;
@@ -578,6 +716,11 @@ struct TemporalTaskT {
     Isec dstIsec;
     Ray3 ray;
     uint32_t resvRng;
+    /* the previous frame's pixel (pairwise weights: the shift of the canonical sample into it) */
+    Surf prevSurf;
+    Isec prevIsec;
+    Ray3 prevRay;
+    uint32_t pidx;
 
     GD void finish(const PassCtx& P) {
         resvResetIfInvalid(resv);
@@ -618,9 +761,15 @@ struct TemporalTaskT {
                         Ray3 pray = pinholeCameraSampleRay(P.prev, v2(puv.x, 1.0f - puv.y));
                         V3 posPrev = pray.ori + pray.dir * (depthPrev - 1e-4f);
                         if (!(matMeshIdPrev != matMeshId || dot3(normalPrev, norm) < 0.95f || distance3(pos, posPrev) > 0.5f)) {
-                            uint32_t pidx = (uint32_t)P.cam.w * (uint32_t)py + (uint32_t)px;
+                            pidx = (uint32_t)P.cam.w * (uint32_t)py + (uint32_t)px;
                             src = load_resv(P.b.reservoirPrev, pidx, n);
                             found = true;
+                            if (kPair && P.set.misWeights) {
+                                prevSurf.pos = posPrev; prevSurf.norm = normalPrev; prevSurf.albedo = albedoPrev;
+                                prevSurf.matIndex = (uint32_t)(matMeshIdPrev >> 16); prevSurf.isLight = false;
+                                prevIsec.bx = puv.x; prevIsec.by = puv.y; prevIsec.inst = kSpecialHit; prevIsec.tri = 0u;
+                                prevRay = pray;
+                            }
                         }
                     }
                 }
@@ -637,7 +786,25 @@ struct TemporalTaskT {
         if constexpr (kGuide) {
             if (primary_lobes(P, idx, load_material(P.sc, dst.matIndex), L)) Lp = &L;
         }
-        reuseAndMerge(P, resv, dst, dstIsec, ray, src, resvRng, rc, err, Lp);
+        if (!(kPair && P.set.misWeights)) {
+            reuseAndMerge(P, resv, dst, dstIsec, ray, src, resvRng, rc, err, Lp);
+        } else {
+            PairwiseMerge pm;
+            pm.begin(resv, 1.0f);
+            Shift fw = shiftToDomain(P, dst, dstIsec, ray, src.s, rc, err, Lp);
+            float pBack = 0.0f;
+            if (pm.pc > 0.0f) {
+                const guide::Lobes* Lq = nullptr;
+                guide::Lobes Lprev;
+                if constexpr (kGuide) {
+                    if (primary_lobes(P, pidx, load_material(P.sc, prevSurf.matIndex), Lprev, true)) Lq = &Lprev;
+                }
+                Shift bw = shiftToDomain(P, prevSurf, prevIsec, prevRay, resv.s, rc, err, Lq);
+                if (bw.valid) pBack = bw.dstPHat;
+            }
+            pm.add(src, fw, pBack, sample1f(resvRng));
+            resv = pm.finish(sample1f(resvRng), (float)P.set.cap);
+        }
         finish(P);
         return false;
     }
@@ -649,8 +816,9 @@ using TemporalTask = TemporalTaskT<false>;
  * gris_resample_spatial.comp:21-27. begin() reads the pixel (a background pixel only updates the
  * running mean); each step() handles one neighbour (findNeighborReservoir, :11-34, then the shift
  * and merge); the last step writes the reservoir, shades and accumulates. */
-template <bool kGuide>
+template <bool kGuide, bool kPair = false>
 struct SpatialTaskT {
+    PairwiseMerge pm;   /* pairwise weights (misWeights = 1) */
     uint32_t ix, iy, i, rng;
     uint64_t idx;
     Resv resv;
@@ -687,6 +855,7 @@ struct SpatialTaskT {
         dstIsec.bx = uv.x; dstIsec.by = uv.y; dstIsec.inst = kSpecialHit; dstIsec.tri = 0u;
         dst.pos = pos; dst.norm = norm; dst.albedo = albedo; dst.matIndex = (uint32_t)matId; dst.isLight = false;
         i = 0;
+        if (kPair && P.set.misWeights && P.set.spatialReuse && P.set.spatialNeighbors > 0u) pm.begin(resv, (float)P.set.spatialNeighbors);
         return true;
     }
 
@@ -701,17 +870,41 @@ struct SpatialTaskT {
             V2 uv = v2(dstIsec.bx, dstIsec.by);
             V2 d = toConcentricDisk(sample2f(rng));
             V2 nb = v2(uv.x + d.x * resampleRadius * tx, uv.y + d.y * resampleRadius * ty);
-            if (nb.x < 0.0f || nb.y < 0.0f || nb.x > 1.0f || nb.y > 1.0f) return true;
+            const bool pairwise = kPair && P.set.misWeights != 0u;
+            if (nb.x < 0.0f || nb.y < 0.0f || nb.x > 1.0f || nb.y > 1.0f) { if (pairwise) pm.skip(); return true; }
             int px = (int)(nb.x * (float)P.cam.w), py = (int)(nb.y * (float)P.cam.h);
             float depthN = 0.0f; V3 normalN = v3s(0.0f), albedoN = v3s(0.0f); int matMeshIdN = 0;
             float4 ndn = texture_bilinear(reinterpret_cast<const float4*>(P.b.depthNormal), W, H, nb);
             uint2 nam = fetch_am(reinterpret_cast<const uint2*>(P.b.albedoMatId), W, H, px, py);
-            if (!unpackGBuffer(ndn, nam, depthN, normalN, albedoN, matMeshIdN)) return true;
+            if (!unpackGBuffer(ndn, nam, depthN, normalN, albedoN, matMeshIdN)) { if (pairwise) pm.skip(); return true; }
             Ray3 nray = pinholeCameraSampleRay(P.cam, v2(nb.x, 1.0f - nb.y));
             V3 posN = nray.ori + nray.dir * (depthN - 1e-4f);
-            if (dot3(normalN, dst.norm) < 0.9f || distance3(dst.pos, posN) > 0.4f) return true;
+            if (dot3(normalN, dst.norm) < 0.9f || distance3(dst.pos, posN) > 0.4f) { if (pairwise) pm.skip(); return true; }
             uint32_t nidx = (uint32_t)P.cam.w * (uint32_t)py + (uint32_t)px;
             Resv neighborResv = load_resv(P.b.reservoirTemp, nidx, n);
+            if (pairwise) {
+                if (!resvIsValid(neighborResv)) { pm.skip(); return true; }
+                const guide::Lobes* Lp = nullptr;
+                const guide::Lobes* Lq = nullptr;
+                guide::Lobes L, Ln;
+                Surf nbSurf;
+                nbSurf.pos = posN; nbSurf.norm = normalN; nbSurf.albedo = albedoN;
+                nbSurf.matIndex = (uint32_t)(matMeshIdN >> 16); nbSurf.isLight = false;
+                if constexpr (kGuide) {
+                    if (primary_lobes(P, idx, load_material(sc, dst.matIndex), L)) Lp = &L;
+                    if (primary_lobes(P, nidx, load_material(sc, nbSurf.matIndex), Ln)) Lq = &Ln;
+                }
+                Shift fw = shiftToDomain(P, dst, dstIsec, ray, neighborResv.s, rc, err, Lp);
+                float pBack = 0.0f;
+                if (pm.pc > 0.0f) {
+                    Isec nbIsec;
+                    nbIsec.bx = nb.x; nbIsec.by = nb.y; nbIsec.inst = kSpecialHit; nbIsec.tri = 0u;
+                    Shift bw = shiftToDomain(P, nbSurf, nbIsec, nray, pm.canon, rc, err, Lq);
+                    if (bw.valid) pBack = bw.dstPHat;
+                }
+                pm.add(neighborResv, fw, pBack, sample1f(rng));
+                return true;
+            }
             if (resvIsValid(neighborResv)) {
                 const guide::Lobes* Lp = nullptr;
                 guide::Lobes L;
@@ -722,6 +915,7 @@ struct SpatialTaskT {
             }
             return true;
         }
+        if (kPair && P.set.misWeights && P.set.spatialReuse && P.set.spatialNeighbors > 0u) resv = pm.finish(sample1f(rng), (float)P.set.cap);
         resvResetIfInvalid(resv);
         store_resv(P.b.reservoirThis, idx, resv);
         V3 radiance = v3s(0.0f);
@@ -1040,13 +1234,15 @@ cudaError_t launch_gris(const DeviceSceneView& scene, const GrisPassBindings& b,
     }
     if (passes & 2) {
         if (timer) timer->mark(2, true, stream);
-        if (persistent) k_pass_persistent<TemporalTask, 2><<<blocksT, 128, 0, stream>>>(P);
+        if (set.misWeights) k_pass_grid<TemporalTaskT<false, true>, 2><<<grid, block, 0, stream>>>(P);
+        else if (persistent) k_pass_persistent<TemporalTask, 2><<<blocksT, 128, 0, stream>>>(P);
         else k_pass_grid<TemporalTask, 2><<<grid, block, 0, stream>>>(P);
         if (timer) timer->mark(2, false, stream);
     }
     if (passes & 4) {
         if (timer) timer->mark(3, true, stream);
-        if (persistent) k_pass_persistent<SpatialTask, 3><<<blocksS, 128, 0, stream>>>(P);
+        if (set.misWeights) k_pass_grid<SpatialTaskT<false, true>, 3><<<grid, block, 0, stream>>>(P);
+        else if (persistent) k_pass_persistent<SpatialTask, 3><<<blocksS, 128, 0, stream>>>(P);
         else k_pass_grid<SpatialTask, 3><<<grid, block, 0, stream>>>(P);
         if (timer) timer->mark(3, false, stream);
     }
@@ -1825,6 +2021,7 @@ BatchShape fill_view_table(const BatchView* views, int n, void* hViews, unsigned
         sh.tiles += e.tilesX * ((bv.b.height + 7) / 8);
         sh.pixels += bv.b.width * bv.b.height;
         if ((int)bv.set.maxDepth > sh.maxDepth) sh.maxDepth = (int)bv.set.maxDepth;
+        if (bv.set.misWeights) sh.pairwise = true;
     }
     return sh;
 }
@@ -1942,13 +2139,17 @@ cudaError_t enqueue_batch(const BatchShape& sh, void* dViews, const void* hViews
 reuse:
     if (passes & 2) {
         if (timer) timer->mark(2, true, stream);
-        if (guide) k_batch_pass<TemporalTaskT<true>, 2><<<tiles, blk, 0, stream>>>(V, n);
+        if (guide && sh.pairwise) k_batch_pass<TemporalTaskT<true, true>, 2><<<tiles, blk, 0, stream>>>(V, n);
+        else if (guide) k_batch_pass<TemporalTaskT<true>, 2><<<tiles, blk, 0, stream>>>(V, n);
+        else if (sh.pairwise) k_batch_pass<TemporalTaskT<false, true>, 2><<<tiles, blk, 0, stream>>>(V, n);
         else k_batch_pass<TemporalTask, 2><<<tiles, blk, 0, stream>>>(V, n);
         if (timer) timer->mark(2, false, stream);
     }
     if (passes & 4) {
         if (timer) timer->mark(3, true, stream);
-        if (guide) k_batch_pass<SpatialTaskT<true>, 3><<<tiles, blk, 0, stream>>>(V, n);
+        if (guide && sh.pairwise) k_batch_pass<SpatialTaskT<true, true>, 3><<<tiles, blk, 0, stream>>>(V, n);
+        else if (guide) k_batch_pass<SpatialTaskT<true>, 3><<<tiles, blk, 0, stream>>>(V, n);
+        else if (sh.pairwise) k_batch_pass<SpatialTaskT<false, true>, 3><<<tiles, blk, 0, stream>>>(V, n);
         else k_batch_pass<SpatialTask, 3><<<tiles, blk, 0, stream>>>(V, n);
         if (timer) timer->mark(3, false, stream);
     }

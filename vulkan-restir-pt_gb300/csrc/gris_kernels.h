@@ -91,6 +91,7 @@ struct BatchShape {
     int n;
     uint32_t tiles, pixels;
     int maxDepth;
+    bool pairwise = false;   /* some view uses the pairwise MIS weights */
 };
 
 /* Writes the view table of a frame into hViews (pinned host memory). */

@@ -65,14 +65,15 @@ class Settings(ctypes.Structure):
     _fields_ = [("shiftType", ctypes.c_uint32), ("rrScale", ctypes.c_float), ("temporalReuse", ctypes.c_uint32),
                 ("spatialReuse", ctypes.c_uint32), ("cap", ctypes.c_uint32), ("maxDepth", ctypes.c_uint32),
                 ("spatialNeighbors", ctypes.c_uint32), ("spatialRadius", ctypes.c_float),
-                ("envRadiance", ctypes.c_float * 3), ("reserved", ctypes.c_uint32 * 5)]
+                ("envRadiance", ctypes.c_float * 3), ("misWeights", ctypes.c_uint32), ("reserved", ctypes.c_uint32 * 4)]
 
     @classmethod
     def make(cls, shiftType=2, rrScale=1.0, temporalReuse=True, spatialReuse=True, cap=20, maxDepth=15,
-             spatialNeighbors=3, spatialRadius=20.0):
+             spatialNeighbors=3, spatialRadius=20.0, misWeights=0):
         s = cls()
         s.shiftType, s.rrScale, s.temporalReuse, s.spatialReuse = shiftType, rrScale, int(temporalReuse), int(spatialReuse)
         s.cap, s.maxDepth, s.spatialNeighbors, s.spatialRadius = cap, maxDepth, spatialNeighbors, spatialRadius
+        s.misWeights = int(misWeights)
         return s
 
 
