@@ -156,7 +156,9 @@ struct GrisTraversal {
         sp = 0;
         grpBase = 0; grpHits = 0; grpImask = 0;
         nodeIdx = 0;
-        haveNode = true;
+        /* A ray with a NaN coordinate hits nothing (every triangle test compares a NaN), but the
+         * box test's maxNum/minNum would pass every node on it: skip the walk, same result. */
+        haveNode = !(ox != ox || oy != oy || oz != oz || dx != dx || dy != dy || dz != dz);
         visits = 0; tests = 0;
     }
 
