@@ -82,3 +82,23 @@ class _HostOnlyScene:
 
 def _host_scene(hs):
     return _HostOnlyScene(hs)
+
+
+
+def test_nan_rays_miss_like_brute_force(oracle_bf):
+    """A ray with a NaN coordinate misses every triangle; the walk stops at once instead of
+    visiting the whole tree (which the box test's maxNum/minNum would let it do)."""
+    hs = G.HostScene(1, seed=3, grid=48, spheres=60)
+    scene = _host_scene(hs)
+    oracle_bf.set_scene(hs)
+    oracle_bf.set_traversal(False)
+    rays = _rays(hs, 64, 11, "random")
+    rays[0:16, 0] = np.nan      # origin
+    rays[16:32, 5] = np.nan     # direction
+    for any_hit in (False, True):
+        t1, i1, r1 = scene.trace_host(rays, any_hit=any_hit)
+        t2, i2, r2 = oracle_bf.trace_rays(rays, any_hit=any_hit)
+        assert np.array_equal(i1, i2) and np.array_equal(r1, r2)
+        assert np.all(i1[:32] == 0xffffffff)
+        if not any_hit:
+            assert t1.tobytes() == t2.tobytes()
