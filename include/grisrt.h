@@ -222,9 +222,10 @@ int grisSetLaunchMode(GrisContext* ctx, int mode);
 int grisReadWorkCounters(GrisContext* ctx, uint64_t nodes[4], uint64_t tris[4], uint64_t closestRays[4], int reset);
 /* Per-kernel profile with the wavefront stages on their own: slots 0-3 as grisReadProfile (slot 1
  * spans the whole path tracer), then the wavefront's begin, extension (closest hits), shading,
- * shadow and post stages, then the guide's inference and training. ms/launches while profiling is on; nodes/tris/rays while work counting
+ * shadow and post stages, then the guide's inference and training, then the three ReSTIR DI
+ * kernels. ms/launches while profiling is on; nodes/tris/rays while work counting
  * is on, for the slots that traverse (rays: closest-hit rays, shadow rays for the shadow stage). */
-#define GRIS_PROFILE_SLOTS 11
+#define GRIS_PROFILE_SLOTS 14
 #define GRIS_SLOT_WAVE_BEGIN 4
 #define GRIS_SLOT_WAVE_EXTEND 5
 #define GRIS_SLOT_WAVE_SHADE 6
@@ -232,13 +233,17 @@ int grisReadWorkCounters(GrisContext* ctx, uint64_t nodes[4], uint64_t tris[4], 
 #define GRIS_SLOT_WAVE_POST 8
 #define GRIS_SLOT_GUIDE_INFER 9     /* guided batches: the network's inference per level */
 #define GRIS_SLOT_GUIDE_TRAIN 10    /* guided batches: the frame's training steps */
+#define GRIS_SLOT_DI_CANDIDATES 11  /* ReSTIR DI (rays: closest-hit and shadow rays together) */
+#define GRIS_SLOT_DI_TEMPORAL 12
+#define GRIS_SLOT_DI_SPATIAL 13
 typedef struct GrisKernelProfile {
     double ms;
     uint64_t launches;
     uint64_t nodes, tris, rays;
 } GrisKernelProfile;
 int grisReadKernelProfile(GrisContext* ctx, GrisKernelProfile out[GRIS_PROFILE_SLOTS], int reset);
-size_t grisSizeof(int which);   /* 0 camera, 1 reservoir, 2 material, 3 vertex, 4 instance, 5 light, 6 table entry, 7 settings */
+size_t grisSizeof(int which);   /* 0 camera, 1 reservoir, 2 material, 3 vertex, 4 instance, 5 light, 6 table entry,
+                                   7 settings, 8 DI reservoir, 9 DI settings */
 
 /* ---------------------------------------------------------------- host helpers (no GPU) */
 /* reference: DiscreteSampler1D::build, src/util/AliasTable.h:26-71 (table of n+1 entries). */
@@ -438,11 +443,77 @@ int grisFrameDestroy(GrisFrame* frame);
 /* G-buffer into the current slot, then GRISReSTIR::render on the current slot, then swap. */
 int grisFrameRender(GrisContext* ctx, const GrisScene* scene, GrisFrame* frame, const GrisCamera* cam,
                     const GrisCamera* prevCam, const GrisSettings* settings);
-/* which: 0 depthNormal, 1 albedoMatId, 2 motion, 3 reservoir, 4 temp reservoir, 5 output.
+/* which: 0 depthNormal, 1 albedoMatId, 2 motion, 3 reservoir, 4 temp reservoir, 5 output,
+ * 6 DI reservoir, 7 DI temp reservoir, 8 direct output (6-8 once grisFrameRenderDI ran).
  * slot: 0 = the slot the last grisFrameRender wrote (current), 1 = the other one. */
 int grisFrameGetBuffer(const GrisFrame* frame, int which, int slot, void** devPtr, size_t* bytes);
 int grisFrameDownload(GrisContext* ctx, const GrisFrame* frame, int which, int slot, void* host, size_t bytes);
 int grisFrameUpload(GrisContext* ctx, GrisFrame* frame, int which, int slot, const void* host, size_t bytes);
+
+/* ---------------------------------------------------------------- ReSTIR DI (direct lighting)
+ * The reference's ReSTIR DI pass (TestReSTIR::render, src/TestReSTIR.cpp:9-35), which the
+ * renderer runs for directMethod = ReSTIR DI before the indirect pass (src/Renderer.cpp:449-476):
+ *   candidates  di_path_gen.glsl:9-40 + sampleLi (di_reservoir.glsl:78-174): one light sample
+ *               (power-proportional, shadow-tested) and/or one BSDF sample that hits a light,
+ *               streamed into a reservoir at the primary vertex
+ *   temporal    di_temporal.glsl:9-90: the previous frame's reservoir at the reprojected pixel
+ *               (same mat/mesh id, normal >= 0.95, distance <= 0.5), shifted and merged, the
+ *               final sample's visibility tested, M capped at 40
+ *   spatial     di_spatial.glsl:9-121: 10 neighbours in a 20-pixel disk (normal >= 0.9,
+ *               distance <= 0.4), shifted and merged, visibility, cap 40, then the final
+ *               shading Li / lum(Li) * W / M into the running mean of the direct output
+ *               (di_spatial.comp:14-27)
+ * Shifts (di_reservoir.glsl:176-296): reconnection (the light vertex seen from the destination,
+ * one visibility ray) or random replay (the source's candidates drawn again at the destination
+ * from the source's seed); the reference merges nothing for its third value (hybrid). */
+#define GRIS_DI_SHIFT_RECONNECTION 0
+#define GRIS_DI_SHIFT_REPLAY 1
+#define GRIS_DI_SHIFT_HYBRID 2
+#define GRIS_DI_SAMPLE_LIGHT 0
+#define GRIS_DI_SAMPLE_BSDF 1
+#define GRIS_DI_SAMPLE_BOTH 2
+/* TestReSTIR::Settings (src/TestReSTIR.h:12-17), the pass's 16-byte push constant; the
+ * reference's defaults are {RECONNECTION, LIGHT, 0, 1} (TestReSTIR.h:29). */
+typedef struct GrisDISettings {
+    uint32_t shiftType;
+    uint32_t sampleType;
+    uint32_t temporalReuse;
+    uint32_t spatialReuse;
+} GrisDISettings;
+/* DIReservoir (layouts.glsl:96-115), 64 B std430 (DIReservoirData, src/Renderer.cpp:33). */
+typedef struct GrisDIReservoir {
+    float bary[2];
+    uint32_t instanceIdx, triangleIdx;   /* instance 0: a light triangle */
+    float Li[3];
+    float pad0;
+    float jacobian;                      /* |cos| / d^2 at the light vertex */
+    float samplePdf;
+    uint32_t rng;                        /* the candidates' seed (random replay) */
+    uint32_t isLightSample;              /* GLSL bool: 0 / 1 */
+    uint32_t sampleCount;
+    float resampleWeight, contribWeight, weight;
+} GrisDIReservoir;
+typedef struct GrisDIBindings {
+    uint32_t width, height;
+    const float* depthNormal;        /* the G-buffer of grisPassGBuffer, as for GrisPassBindings */
+    const float* depthNormalPrev;
+    const uint32_t* albedoMatId;
+    const uint32_t* albedoMatIdPrev;
+    const uint16_t* motion;
+    GrisDIReservoir* reservoirThis;
+    const GrisDIReservoir* reservoirPrev;
+    GrisDIReservoir* reservoirTemp;
+    float* directOutput;             /* float4 RGBA32F, running mean */
+} GrisDIBindings;
+/* passes: bit 0 candidates, bit 1 temporal, bit 2 spatial (7 = TestReSTIR::render). */
+int grisPassDI(GrisContext* ctx, const GrisScene* scene, const GrisDIBindings* b, const GrisCamera* cam,
+               const GrisCamera* prevCam, const GrisDISettings* settings, int passes);
+/* The renderer's frame with directMethod = ReSTIR DI: G-buffer into the current slot, the DI pass
+ * on the frame's DI buffers (allocated on first use, zeroed: two reservoirs per pixel
+ * ping-ponged with the frame's slots, a temporary one and the direct output), then
+ * GRISReSTIR::render unless `settings` is NULL (indirectMethod = None), then swap. */
+int grisFrameRenderDI(GrisContext* ctx, const GrisScene* scene, GrisFrame* frame, const GrisCamera* cam,
+                      const GrisCamera* prevCam, const GrisSettings* settings, const GrisDISettings* di);
 
 #ifdef __cplusplus
 }

@@ -910,6 +910,296 @@ static F3 spatialPixel(Pass& P, int x, int y) {
     return F3(fmn(fmx(color.x, 0.0f), 1e4f), fmn(fmx(color.y, 0.0f), 1e4f), fmn(fmx(color.z, 0.0f), 1e4f));
 }
 
+/* ================================================================== ReSTIR DI
+ * Direct lighting at the primary vertex (TestReSTIR::render, src/TestReSTIR.cpp:9-35):
+ * candidates (di_path_gen.glsl:9-62 with sampleLi, di_reservoir.glsl:78-174), temporal reuse
+ * (di_temporal.glsl:36-90) and spatial reuse + shading (di_spatial.glsl:36-121). */
+struct DISample { Hit isec; float Li[3]; float pad0; float jac, pdf; uint32_t rng, isLight; };   /* layouts.glsl:96-106 */
+struct DIResv { DISample s; uint32_t M; float W, contrib, weight; };                           /* :108-115 */
+struct DISettings { uint32_t shift, mode, temporal, spatial; };                                 /* TestReSTIR.h:12-17 */
+static_assert(sizeof(DIResv) == 64, "DIReservoir layout");
+enum : uint32_t { DI_LIGHT = 0, DI_BSDF = 1, DI_RECONNECT = 0, DI_REPLAY = 1 };
+static const uint32_t DI_CAP = 40, DI_NEIGHBOURS = 10;
+static const float DI_RADIUS = 20.0f;
+
+static inline bool diUsable(const DIResv& r) { return !std::isnan(r.W); }                   /* di_reservoir.glsl:40-42 */
+static inline void diClear(DIResv& r) { r.M = 0u; r.W = 0.0f; r.contrib = 0.0f; }          /* :34-38 */
+static inline void diAdd(DIResv& r, const DISample& s, float w, float u) {                  /* :50-58 */
+    r.W += w;
+    r.M++;
+    if (u * r.W < w) { r.s = s; r.weight = w; }
+}
+static inline void diMerge(DIResv& r, const DIResv& rhs, float u) {                         /* :60-68 */
+    r.W += rhs.W;
+    r.M += rhs.M;
+    if (u * r.W < rhs.W) { r.s = rhs.s; r.weight = rhs.weight; }
+}
+static inline void diCap(DIResv& r, uint32_t cap) {                                         /* :70-75 */
+    if (r.M > cap) { r.W *= (float)cap / (float)r.M; r.M = cap; }
+}
+
+/* sampleLi (di_reservoir.glsl:78-174): one light sample and/or one BSDF sample streamed into
+ * `resv` (draws from resvRng), then the chosen sample's Li scaled by W / w, M = 1. */
+static void diSampleLi(const Surface& surf, const Material& mat, const F3& wo, uint32_t rng, uint32_t& resvRng, DIResv& resv,
+                       uint32_t mode) {
+    DISample ps; memset(&ps, 0, sizeof(ps));
+    ps.rng = rng;
+    float lr[4], sr[3];
+    for (int k = 0; k < 4; k++) lr[k] = rnd(rng);
+    for (int k = 0; k < 3; k++) sr[k] = rnd(rng);
+    if (mode != DI_BSDF && !deltaBsdf(mat)) {
+        F3 wi; float dist, pdf, jac; F2 bary; uint32_t id;
+        F3 Le = sampleLight(surf.p, lr, wi, dist, pdf, jac, bary, id);
+        __atomic_fetch_add(&g_counts[1], 1ull, __ATOMIC_RELAXED);
+        bool shadowed = traceQuery(surf.p, wi, RAY_TMIN, dist - RAY_TMIN, true, false, nullptr, nullptr);
+        if (!shadowed && pdf > 1e-6f) {
+            float w = mis(pdf, bsdfPdf(mat, surf.n, wo, wi));
+            if (mode == DI_LIGHT) w = 1.0f;
+            F3 contrib = Le * bsdfEval(mat, surf.albedo, surf.n, wo, wi) * fmx(dot(surf.n, wi), 0.0f) / pdf * w;
+            float sw = lum(contrib);
+            if (std::isnan(sw) || sw < 0.0f) sw = 0.0f;
+            ps.isec.bx = bary.x; ps.isec.by = bary.y; ps.isec.inst = 0u; ps.isec.tri = id;
+            st3(ps.Li, Le * w);
+            ps.jac = jac; ps.pdf = pdf; ps.isLight = 1u;
+            diAdd(resv, ps, sw, rnd(resvRng));
+        }
+    }
+    ps.isLight = 0u;
+    Lobe s; memset(&s, 0, sizeof(s));
+    if (mode != DI_LIGHT && bsdfSample(mat, surf.albedo, surf.n, wo, F3(sr[0], sr[1], sr[2]), s) && s.pdf > 1e-6f) {
+        __atomic_fetch_add(&g_counts[0], 1ull, __ATOMIC_RELAXED);
+        Hit h;
+        if (traceQuery(surf.p, s.wi, RAY_TMIN, RAY_TMAX, false, false, &h, nullptr)) {
+            Surface hit; memset(&hit, 0, sizeof(hit));
+            fetchSurface(h, hit);
+            float cosT = -dot(s.wi, hit.n);
+            if (hit.light && cosT > 0.0f) {
+                float dist = len(hit.p - surf.p);
+                float lightPdf = lum(hit.albedo) / at(g.table, 0).prob * dist * dist / fabsf(cosT);
+                float w = mis(s.pdf, lightPdf);
+                bool delta = (s.type & SPECULAR) == SPECULAR;
+                if (mode == DI_BSDF || delta) w = 1.0f;
+                float cosTerm = delta ? 1.0f : fmx(dot(surf.n, s.wi), 0.0f);
+                F3 contrib = hit.albedo * s.f * cosTerm / s.pdf * w;
+                ps.isec = h;
+                st3(ps.Li, hit.albedo * w);
+                ps.jac = fabsf(cosT) / (dist * dist); ps.pdf = s.pdf; ps.isLight = 0u;
+                diAdd(resv, ps, lum(contrib), rnd(resvRng));   /* unclamped weight, as the reference */
+            }
+        }
+    }
+    if (!diUsable(resv)) diClear(resv);
+    if (resv.M > 0u && resv.s.isec.inst != NO_HIT && resv.weight > 0.0f) {
+        st3(resv.s.Li, ld3(resv.s.Li) * (resv.W / resv.weight));
+        resv.weight = resv.W;
+    } else {
+        resv.s.isec.inst = NO_HIT;
+        resv.weight = 0.0f;
+        resv.W = 0.0f;
+    }
+    resv.M = 1u;
+}
+
+struct DIPass {
+    Camera cam, prev;
+    DISettings set;
+    GBuf cur, old;
+    std::vector<float> motion;
+    DIResv *self, *previous, *temp;
+    uint64_t n;
+    int W, H;
+};
+
+static inline DIResv readDI(const DIResv* buf, uint64_t i, uint64_t n) {
+    if (i < n) return buf[i];
+    DIResv z; memset(&z, 0, sizeof(z)); return z;
+}
+
+/* randomReplay (di_reservoir.glsl:176-209): the source's candidates drawn again at the
+ * destination from the source's seed; the reservoir draws come from the merge stream. */
+static void diReplay(DIResv& dst, const Surface& ds, const DIResv& src, const F3& wo, uint32_t& rng, uint32_t mode) {
+    Material mat = at(g.materials, ds.mat);
+    DIResv rr; memset(&rr, 0, sizeof(rr));
+    diClear(rr);
+    diSampleLi(ds, mat, wo, src.s.rng, rng, rr, mode);
+    if (rr.s.isec.inst != NO_HIT) {
+        Surface rs; memset(&rs, 0, sizeof(rs));
+        fetchSurface(rr.s.isec, rs);
+        F3 wi = unit(rs.p - ds.p);
+        F3 Li = ld3(rr.s.Li) * bsdfEval(mat, ds.albedo, ds.n, wo, wi) * fmx(dot(ds.n, wi), 0.0f) / rr.s.pdf;
+        float pHat = lum(Li * 1.0f);
+        rr.W = src.W * pHat / src.weight;
+        rr.M = src.M;
+    } else {
+        rr.W = 0.0f;
+    }
+    if (diUsable(rr)) diMerge(dst, rr, rnd(rng));
+}
+
+/* reconnection (di_reservoir.glsl:211-287): the source's light vertex seen from the destination. */
+static void diReconnect(DIResv& dst, const Surface& ds, DIResv src, const F3& wo, uint32_t& rng) {
+    Material mat = at(g.materials, ds.mat);
+    DISample ss = src.s;
+    Surface rc; memset(&rc, 0, sizeof(rc));
+    fetchSurface(ss.isec, rc);
+    float dist = len(rc.p - ds.p);
+    F3 wi = unit(rc.p - ds.p);
+    float cosT = -dot(rc.n, wi);
+    float dstJac = fabsf(cosT) / (dist * dist);
+    float jac = dstJac / ss.jac;
+    bool ok = false;
+    float pHat = 0.0f, dstPdf = 0.0f;
+    if (ss.isec.inst != NO_HIT && dist > 1e-4f) {
+        if (cosT > 0.0f && !std::isnan(jac) && ss.jac > 0.0f) {
+            if (visible(ds.p, rc.p)) {
+                ok = true;
+                if (!std::isnan(ss.pdf) && ss.pdf > 1e-6f) {
+                    F3 Li = ld3(src.s.Li) * bsdfEval(mat, ds.albedo, ds.n, wo, wi) * fmx(dot(ds.n, wi), 0.0f) / ss.pdf;
+                    pHat = lum(Li * jac);
+                }
+                if (ss.isLight) dstPdf = lum(rc.albedo) / at(g.table, 0).prob / dstJac;
+                else dstPdf = bsdfPdf(mat, ds.n, wo, wi);
+            }
+        }
+    }
+    if (ok) {
+        ss.jac = dstJac;
+        ss.pdf = dstPdf;
+        if (ss.pdf < 1e-6f || std::isnan(ss.pdf)) ss.pdf = 0.0f;
+        src.s = ss;
+        src.W *= pHat / src.weight;
+        if (std::isnan(src.W)) src.W = 0.0f;
+    } else {
+        src.W = 0.0f;
+    }
+    if (diUsable(src)) diMerge(dst, src, rnd(rng));
+}
+
+static void diReuse(const DIPass& P, DIResv& dst, const Surface& ds, const DIResv& src, const F3& wo, uint32_t& rng) {
+    if (P.set.shift == DI_RECONNECT) diReconnect(dst, ds, src, wo, rng);           /* di_reservoir.glsl:289-296 */
+    else if (P.set.shift == DI_REPLAY) diReplay(dst, ds, src, wo, rng, P.set.mode);
+}
+
+/* generatePath (di_path_gen.glsl:9-40): candidates at the primary vertex; the returned colour
+ * is never stored (di_path_gen.comp:14-26). */
+static void diGenPixel(DIPass& P, int x, int y) {
+    F2 uv = pixelUV(x, y, P.W, P.H);
+    float dn[4]; uint32_t am[2];
+    sampleDN(P.cur, uv, dn);
+    fetchAM(P.cur, x, y, am);
+    float depth; F3 nrm, alb; int matMesh;
+    if (!decodeGBuffer(dn, am, depth, nrm, alb, matMesh)) return;
+    Ray ray = cameraRay(P.cam, F2{uv.x, 1.0f - uv.y});
+    uint32_t rng = pixelSeed(P.cam.seed, (uint32_t)x, (uint32_t)y);
+    uint32_t resvRng = ~rng;
+    Surface s; s.p = ray.o + ray.d * (depth - 1e-4f); s.n = nrm; s.albedo = alb; s.mat = (uint32_t)(matMesh >> 16); s.light = false;
+    DIResv r; memset(&r, 0, sizeof(r));
+    diClear(r);
+    diSampleLi(s, at(g.materials, s.mat), -ray.d, rng, resvRng, r, P.set.mode);
+    P.self[(size_t)y * P.W + x] = r;
+}
+
+/* The final-sample visibility test of both reuse passes (di_temporal.glsl:76-85, di_spatial.glsl:84-93). */
+static inline void diOcclude(DIResv& r, const F3& pos) {
+    if (diUsable(r) && r.s.isec.inst != NO_HIT) {
+        Surface s; memset(&s, 0, sizeof(s));
+        fetchSurface(r.s.isec, s);
+        if (!visible(pos, s.p)) r.W = 0.0f;
+    }
+}
+
+/* temporalReuse + findPreviousReservoir (di_temporal.glsl:9-90) */
+static void diTemporalPixel(DIPass& P, int x, int y) {
+    F2 uv = pixelUV(x, y, P.W, P.H);
+    float dn[4]; uint32_t am[2];
+    sampleDN(P.cur, uv, dn);
+    fetchAM(P.cur, x, y, am);
+    float depth; F3 nrm, alb; int matMesh;
+    if (!decodeGBuffer(dn, am, depth, nrm, alb, matMesh)) return;
+    size_t i = (size_t)y * P.W + x;
+    F2 mv{P.motion[i * 2], P.motion[i * 2 + 1]};
+    Ray ray = cameraRay(P.cam, F2{uv.x, 1.0f - uv.y});
+    uint32_t resvRng = ~(pixelSeed(P.cam.seed, (uint32_t)x, (uint32_t)y) ^ 1u);
+    F3 pos = ray.o + ray.d * (depth - 1e-4f);
+    DIResv r = P.self[i];
+    if (P.set.temporal) {
+        Surface ds; ds.p = pos; ds.n = nrm; ds.albedo = alb; ds.mat = (uint32_t)(matMesh >> 16); ds.light = false;
+        F2 puv{uv.x + mv.x, uv.y + mv.y};
+        if ((P.cam.frameIndex & 0x80000000u) == 0u && !(puv.x < 0.0f || puv.y < 0.0f || puv.x > 1.0f || puv.y > 1.0f)) {
+            int px = (int)(puv.x * (float)P.cam.film[0]), py = (int)(puv.y * (float)P.cam.film[1]);
+            float pdn[4]; uint32_t pam[2];
+            sampleDN(P.old, puv, pdn);
+            fetchAM(P.old, px, py, pam);
+            float pdepth; F3 pn, palb; int pmm;
+            if (decodeGBuffer(pdn, pam, pdepth, pn, palb, pmm)) {
+                Ray pr = cameraRay(P.prev, F2{puv.x, 1.0f - puv.y});
+                F3 ppos = pr.o + pr.d * (pdepth - 1e-4f);
+                if (!(pmm != matMesh || dot(pn, nrm) < 0.95f || len(pos - ppos) > 0.5f)) {
+                    DIResv src = readDI(P.previous, (uint64_t)(P.cam.film[0] * (uint32_t)py + (uint32_t)px), P.n);
+                    if (diUsable(src)) diReuse(P, r, ds, src, -ray.d, resvRng);
+                }
+            }
+        }
+        diOcclude(r, pos);
+    }
+    diCap(r, DI_CAP);
+    if (!diUsable(r)) diClear(r);
+    P.temp[i] = r;
+}
+
+/* spatialReuse + findNeighborReservoir (di_spatial.glsl:9-121); returns the pixel colour */
+static F3 diSpatialPixel(DIPass& P, int x, int y) {
+    F2 uv = pixelUV(x, y, P.W, P.H);
+    float dn[4]; uint32_t am[2];
+    sampleDN(P.cur, uv, dn);
+    fetchAM(P.cur, x, y, am);
+    float depth; F3 nrm, alb; int matMesh;
+    if (!decodeGBuffer(dn, am, depth, nrm, alb, matMesh)) return F3(0.0f);
+    uint32_t rng = pixelSeed(P.cam.seed, (uint32_t)x, (uint32_t)y) ^ 2u;
+    Ray ray = cameraRay(P.cam, F2{uv.x, 1.0f - uv.y});
+    F3 pos = ray.o + ray.d * (depth - 1e-4f), wo = -ray.d;
+    size_t i = (size_t)y * P.W + x;
+    DIResv r = P.temp[i];
+    Surface ds; ds.p = pos; ds.n = nrm; ds.albedo = alb; ds.mat = (uint32_t)(matMesh >> 16); ds.light = false;
+    if (P.set.spatial) {
+        float tx = 1.0f / (float)P.W, ty = 1.0f / (float)P.H;
+        for (uint32_t k = 0; k < DI_NEIGHBOURS; k++) {
+            float r0 = rnd(rng), r1 = rnd(rng);
+            F2 d = concentric(F2{r0, r1});
+            F2 nb{uv.x + d.x * DI_RADIUS * tx, uv.y + d.y * DI_RADIUS * ty};
+            if (nb.x < 0.0f || nb.y < 0.0f || nb.x > 1.0f || nb.y > 1.0f) continue;
+            int px = (int)(nb.x * (float)P.cam.film[0]), py = (int)(nb.y * (float)P.cam.film[1]);
+            float ndn[4]; uint32_t nam[2];
+            sampleDN(P.cur, nb, ndn);
+            fetchAM(P.cur, px, py, nam);
+            float ndepth; F3 nn, nalb; int nmm;
+            if (!decodeGBuffer(ndn, nam, ndepth, nn, nalb, nmm)) continue;
+            Ray nr = cameraRay(P.cam, F2{nb.x, 1.0f - nb.y});
+            F3 npos = nr.o + nr.d * (ndepth - 1e-4f);
+            if (dot(nn, nrm) < 0.9f || len(pos - npos) > 0.4f) continue;
+            DIResv src = readDI(P.temp, (uint64_t)(P.cam.film[0] * (uint32_t)py + (uint32_t)px), P.n);
+            if (diUsable(src)) diReuse(P, r, ds, src, wo, rng);
+        }
+        diOcclude(r, pos);
+    }
+    diCap(r, DI_CAP);
+    if (!diUsable(r)) diClear(r);
+    P.self[i] = r;
+    F3 color(0.0f);
+    if (diUsable(r) && r.s.isec.inst != NO_HIT) {
+        Surface ls; memset(&ls, 0, sizeof(ls));
+        fetchSurface(r.s.isec, ls);
+        F3 wi = unit(ls.p - pos);
+        if (r.M > 0u) {
+            Material mat = at(g.materials, ds.mat);
+            F3 Li = ld3(r.s.Li) * bsdfEval(mat, alb, nrm, wo, wi) * fmx(dot(nrm, wi), 0.0f) / r.s.pdf;
+            if (!(lum(Li) < 1e-5f)) color = Li / lum(Li) * r.W / (float)r.M;
+        }
+    }
+    if (anyNan(color)) return F3(0.0f);
+    return F3(fmn(fmx(color.x, 0.0f), 1e4f), fmn(fmx(color.y, 0.0f), 1e4f), fmn(fmx(color.z, 0.0f), 1e4f));
+}
+
 }  // namespace oracle
 
 using namespace oracle;
@@ -1084,6 +1374,44 @@ void oracle_gris_frame(const void* camera, const void* prevCamera, const void* s
         for (int y = y0; y < y1; y++)
             for (int x = 0; x < P.W; x++) {
                 F3 c = spatialPixel(P, x, y);
+                float* o = output + ((size_t)y * P.W + x) * 4;
+                F3 acc = (F3(o[0], o[1], o[2]) * n + c) / (n + 1.0f);
+                o[0] = acc.x; o[1] = acc.y; o[2] = acc.z; o[3] = 1.0f;
+            }
+    }
+}
+
+/* TestReSTIR::render (src/TestReSTIR.cpp:9-35): passes bit 0 candidates, 1 temporal, 2 spatial +
+ * running mean into the direct output (di_spatial.comp:14-27). */
+void oracle_di_frame(const void* camera, const void* prevCamera, const void* settings, const float* dnCur,
+                     const float* dnPrev, const uint32_t* amCur, const uint32_t* amPrev, const uint16_t* motion,
+                     void* resvThis, void* resvPrev, void* resvTemp, float* output, int passes) {
+    DIPass P;
+    memcpy(&P.cam, camera, sizeof(Camera));
+    memcpy(&P.prev, prevCamera, sizeof(Camera));
+    memcpy(&P.set, settings, sizeof(DISettings));
+    P.W = (int)P.cam.film[0]; P.H = (int)P.cam.film[1];
+    P.n = (uint64_t)P.W * P.H;
+    P.cur = GBuf{dnCur, amCur, P.W, P.H};
+    P.old = GBuf{dnPrev, amPrev, P.W, P.H};
+    P.motion.resize(P.n * 2);
+    for (uint64_t i = 0; i < P.n * 2; i++) P.motion[i] = fromHalf(motion[i]);
+    P.self = (DIResv*)resvThis; P.previous = (DIResv*)resvPrev; P.temp = (DIResv*)resvTemp;
+    int y0 = std::max(0, g_row0), y1 = std::min(P.H, g_row1);
+    if (passes & 1) {
+#pragma omp parallel for schedule(dynamic, 2)
+        for (int y = y0; y < y1; y++) for (int x = 0; x < P.W; x++) diGenPixel(P, x, y);
+    }
+    if (passes & 2) {
+#pragma omp parallel for schedule(dynamic, 2)
+        for (int y = y0; y < y1; y++) for (int x = 0; x < P.W; x++) diTemporalPixel(P, x, y);
+    }
+    if (passes & 4) {
+        float n = (float)(P.cam.frameIndex & 0x7fffffffu);
+#pragma omp parallel for schedule(dynamic, 2)
+        for (int y = y0; y < y1; y++)
+            for (int x = 0; x < P.W; x++) {
+                F3 c = diSpatialPixel(P, x, y);
                 float* o = output + ((size_t)y * P.W + x) * 4;
                 F3 acc = (F3(o[0], o[1], o[2]) * n + c) / (n + 1.0f);
                 o[0] = acc.x; o[1] = acc.y; o[2] = acc.z; o[3] = 1.0f;

@@ -1,5 +1,5 @@
 """Python driver of the CPU oracle (oracle/_build/liboracle.so) and of the compiled reference
-shaders (oracle/_ref/libgrisref.so).
+shaders (oracle/_ref/libgrisref.so for the GRIS pass, oracle/_ref/libdiref.so for ReSTIR DI).
 
 TEST INFRASTRUCTURE: only tests/, __graft_entry__.smoke() and bench.py's CPU legs import it.
 
@@ -16,6 +16,7 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 ORACLE_LIB = os.path.join(HERE, "_build", "liboracle.so")
 REF_LIB = os.path.join(HERE, "_ref", "libgrisref.so")
+DI_REF_LIB = os.path.join(HERE, "_ref", "libdiref.so")
 
 
 class CpuImpl:
@@ -31,10 +32,14 @@ class CpuImpl:
         self._fn("counters", None, [vp, ctypes.c_int])
         self._fn("trace", None, [vp, u64, ctypes.c_int, vp, vp, vp])
         self._fn("sizeof", ctypes.c_int, [ctypes.c_int])
+        self._fn("di_frame", None, [vp] * 12 + [ctypes.c_int], optional=True)
         self._arrays = None
 
-    def _fn(self, name, res, args):
-        f = getattr(self.lib, self.prefix + name)
+    def _fn(self, name, res, args, optional=False):
+        f = getattr(self.lib, self.prefix + name, None)
+        if f is None and optional:
+            setattr(self, name, None)
+            return
         f.restype, f.argtypes = res, args
         setattr(self, name, f)
 
@@ -90,6 +95,41 @@ def reference():
     return CpuImpl(REF_LIB, "gref_")
 
 
+class DiReference:
+    """The reference's ReSTIR DI shaders compiled as C++ (oracle/_ref/libdiref.so): scene binding,
+    ray counters and one TestReSTIR::render (dref_di_frame). No G-buffer of its own: the frames
+    take the G-buffer of the GRIS harness or of the oracle (identical)."""
+
+    def __init__(self, path=DI_REF_LIB):
+        if not os.path.exists(path):
+            raise FileNotFoundError(path)
+        self.lib = ctypes.CDLL(path)
+        vp, u64 = ctypes.c_void_p, ctypes.c_ulonglong
+        self.lib.dref_scene_set.argtypes, self.lib.dref_scene_set.restype = [vp, u64] * 7, ctypes.c_int
+        self.lib.dref_di_frame.argtypes, self.lib.dref_di_frame.restype = [vp] * 12 + [ctypes.c_int], None
+        self.lib.dref_counters.argtypes, self.lib.dref_counters.restype = [vp, ctypes.c_int], None
+        self.lib.dref_sizeof.restype = ctypes.c_int
+        self.di_frame = self.lib.dref_di_frame
+        self._arrays = None
+
+    def set_scene(self, host_scene):
+        arrs = [np.ascontiguousarray(a) for a in host_scene.arrays()]
+        self._arrays = arrs
+        args = []
+        for a in arrs:
+            args += [a.ctypes.data, len(a)]
+        return self.lib.dref_scene_set(*args)
+
+    def read_counters(self, reset=True):
+        out = (ctypes.c_ulonglong * 4)()
+        self.lib.dref_counters(out, int(reset))
+        return list(out)
+
+
+def reference_di():
+    return DiReference()
+
+
 def _p(a):
     return ctypes.c_void_p(a.ctypes.data)
 
@@ -127,6 +167,39 @@ def run_sequence(impl, cams, prevs, settings, width, height, frames=None, record
             rec["am"] = am[j].copy()
         if "mv" in record:
             rec["mv"] = mv.copy()
+        results.append(rec)
+        j ^= 1
+    return results
+
+
+def run_di_sequence(gbuffer_impl, di_impl, cams, prevs, di_settings, width, height, record=("resv", "temp", "out")):
+    """Frames of TestReSTIR::render with the renderer's ping-pong (src/Renderer.cpp:339-341): the
+    G-buffer (gbuffer_impl) into slot j, the DI pass with This = R[j], Prev = R[j^1], j ^= 1.
+    di_settings: grisrt.DISettings. Returns per-frame copies of the recorded buffers."""
+    from grisrt import DI_RESERVOIR
+    n = width * height
+    dn = [np.zeros((n, 4), np.float32) for _ in range(2)]
+    am = [np.zeros((n, 2), np.uint32) for _ in range(2)]
+    mv = np.zeros((n, 2), np.uint16)
+    resv = [np.zeros(n, DI_RESERVOIR) for _ in range(2)]
+    temp = np.zeros(n, DI_RESERVOIR)
+    out = np.zeros((n, 4), np.float32)
+    sbuf = np.frombuffer(bytes(memoryview(di_settings)), dtype=np.uint8).copy()
+    results = []
+    j = 0
+    for f in range(len(cams)):
+        cb = np.frombuffer(cams[f].tobytes(), np.uint8).copy()
+        pb = np.frombuffer(prevs[f].tobytes(), np.uint8).copy()
+        gbuffer_impl.gbuffer(_p(cb), width, height, _p(dn[j]), _p(am[j]), _p(mv))
+        di_impl.di_frame(_p(cb), _p(pb), _p(sbuf), _p(dn[j]), _p(dn[j ^ 1]), _p(am[j]), _p(am[j ^ 1]), _p(mv),
+                         _p(resv[j]), _p(resv[j ^ 1]), _p(temp), _p(out), 7)
+        rec = {}
+        if "resv" in record:
+            rec["resv"] = resv[j].copy()
+        if "temp" in record:
+            rec["temp"] = temp.copy()
+        if "out" in record:
+            rec["out"] = out.copy()
         results.append(rec)
         j ^= 1
     return results

@@ -1,5 +1,6 @@
 #!/usr/bin/env python3
-"""Build oracle/_ref/libgrisref.so: the reference's own GRIS shader code, compiled as C++.
+"""Build oracle/_ref/libgrisref.so and libdiref.so: the reference's own GRIS and ReSTIR DI
+shader code, compiled as C++.
 
 TEST INFRASTRUCTURE (oracle). The output is the pinning reference for the oracle
 restatement; it is never part of the product and never travels as source.
@@ -24,9 +25,10 @@ Recipe
      parameters whose defaults are the reference's values.
 3. Compile oracle/ref/alias_ref.cpp against the reference's src/util/AliasTable.h (plain
    C++, used as is) into oracle/_ref/libaliasref.so.
-4. Compile oracle/ref/ref_harness.cpp (which includes the rewritten shaders after
-   glsl_compat.h) with g++ -std=c++20 -fsingle-precision-constant -ffp-contract=off
-   -ftrivial-auto-var-init=zero -fopenmp.
+4. Compile oracle/ref/ref_harness.cpp (the GRIS pass) and oracle/ref/ref_harness_di.cpp
+   (the ReSTIR DI pass), each including the rewritten shaders after glsl_compat.h and
+   ref_common.h, with g++ -std=c++20 -fsingle-precision-constant -ffp-contract=off
+   -ftrivial-auto-var-init=zero -fopenmp, into oracle/_ref/libgrisref.so and libdiref.so.
 
 Usage: python oracle/ref/make_ref.py [--reference DIR] [--out DIR]
 """
@@ -45,6 +47,7 @@ SHADERS = [
     "camera.glsl", "gbuffer_util.glsl", "ray_gbuffer_util.glsl", "light_sampling.glsl",
     "gris_reservoir.glsl", "gris_path_trace.glsl", "gris_retrace.glsl",
     "gris_resample_temporal.glsl", "gris_resample_spatial.glsl", "gi_naive.glsl",
+    "di_reservoir.glsl", "di_path_gen.glsl", "di_temporal.glsl", "di_spatial.glsl",
 ]
 
 
@@ -158,11 +161,12 @@ def main():
     for name in SHADERS:
         with open(os.path.join(shader_dir, name), "rb") as f:
             h.update(f.read())
-    for name in ("ref_harness.cpp", "glsl_compat.h", "alias_ref.cpp", "make_ref.py", "../detmath.h"):
+    for name in ("ref_harness.cpp", "ref_harness_di.cpp", "ref_common.h", "glsl_compat.h", "alias_ref.cpp",
+                 "make_ref.py", "../detmath.h"):
         with open(os.path.join(HERE, name), "rb") as f:
             h.update(f.read())
     stamp = os.path.join(args.out, "stamp")
-    outputs = [os.path.join(args.out, "libgrisref.so"), os.path.join(args.out, "libaliasref.so")]
+    outputs = [os.path.join(args.out, n) for n in ("libgrisref.so", "libdiref.so", "libaliasref.so")]
     if "--force" not in sys.argv and all(os.path.exists(o) for o in outputs) and os.path.exists(stamp):
         with open(stamp) as f:
             if f.read() == h.hexdigest():
@@ -173,13 +177,14 @@ def main():
         with open(os.path.join(gdir, name), "w") as f:
             f.write(rewrite(name, src))
     so = os.path.join(args.out, "libgrisref.so")
-    cmd = [args.cxx, "-std=c++20", "-O2", "-fPIC", "-shared", "-fopenmp",
-           "-fsingle-precision-constant", "-ffp-contract=off", "-ftrivial-auto-var-init=zero",
-           "-fno-strict-aliasing", "-Wno-unknown-pragmas", "-Wno-div-by-zero",
-           "-I", gdir, "-I", HERE, os.path.join(HERE, "ref_harness.cpp"), "-o", so]
-    r = subprocess.run(cmd)
-    if r.returncode != 0:
-        return r.returncode
+    di = os.path.join(args.out, "libdiref.so")
+    flags = [args.cxx, "-std=c++20", "-O2", "-fPIC", "-shared", "-fopenmp", "-Wl,-Bsymbolic",
+             "-fsingle-precision-constant", "-ffp-contract=off", "-ftrivial-auto-var-init=zero",
+             "-fno-strict-aliasing", "-Wno-unknown-pragmas", "-Wno-div-by-zero", "-I", gdir, "-I", HERE]
+    for src, out in (("ref_harness.cpp", so), ("ref_harness_di.cpp", di)):
+        r = subprocess.run(flags + [os.path.join(HERE, src), "-o", out])
+        if r.returncode != 0:
+            return r.returncode
     alias = os.path.join(args.out, "libaliasref.so")
     r = subprocess.run([args.cxx, "-std=c++20", "-O2", "-fPIC", "-shared", "-ffp-contract=off",
                         "-I", os.path.join(args.reference, "src"), os.path.join(HERE, "alias_ref.cpp"), "-o", alias])
@@ -188,6 +193,7 @@ def main():
     with open(stamp, "w") as f:
         f.write(h.hexdigest())
     print(so)
+    print(di)
     print(alias)
     return 0
 

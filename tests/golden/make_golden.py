@@ -1,6 +1,8 @@
 #!/usr/bin/env python3
 """Generates the golden vectors in tests/golden/ from the reference's own shader code compiled
-as C++ (oracle/_ref, built by oracle/ref/make_ref.py where the reference sources are present).
+as C++ (oracle/_ref, built by oracle/ref/make_ref.py where the reference sources are present):
+the GRIS pass (libgrisref.so) and, in the di_*.npz files, the ReSTIR DI pass (libdiref.so, on the
+G-buffer of libgrisref.so).
 
 For each case the file stores the scene-array hash, the cameras and settings used, the ray
 counts, and per frame the SHA-256 digest of every buffer (G-buffer, motion, reservoirs,
@@ -29,6 +31,13 @@ CASES = {
     "terrain_24x20_d8": (1, 24, 12, 24, 20, 2, dict(maxDepth=8, spatialRadius=30.0), True),
     "glossy_24x20_d8": (2, 24, 12, 24, 20, 2, dict(maxDepth=8), True),
     "box_256x256_c1_8frames": (0, 0, 0, 256, 256, 8, dict(maxDepth=3, spatialRadius=30.0), False),
+}
+DI_BUFFERS = ("resv", "temp", "out")
+# name: (kind, grid, spheres, W, H, frames, DI settings)
+DI_CASES = {
+    "di_box_32x32_temporal": (0, 0, 0, 32, 32, 3, dict(temporalReuse=True)),
+    "di_box_32x24_replay_both": (0, 0, 0, 32, 24, 2, dict(shiftType=1, sampleType=2, temporalReuse=True)),
+    "di_terrain_24x20_both": (1, 24, 12, 24, 20, 2, dict(sampleType=2, temporalReuse=True)),
 }
 
 
@@ -68,8 +77,33 @@ def make(name):
     return path
 
 
+def make_di(name):
+    kind, grid, spheres, W, H, frames, kw = DI_CASES[name]
+    G.load()
+    hs = G.HostScene(kind, seed=3, grid=grid, spheres=spheres)
+    cams, prevs = G.sequence_cameras(hs, frames, W, H, seed=23)
+    di = G.DISettings.make(**kw)
+    gref, dref = O.reference(), O.reference_di()
+    gref.set_scene(hs)
+    dref.set_scene(hs)
+    dref.read_counters(reset=True)
+    res = O.run_di_sequence(gref, dref, cams, prevs, di, W, H)
+    cnt = dref.read_counters(reset=True)
+    out = {"scene_sha256": np.array(scene_hash(hs)), "di_settings": np.frombuffer(bytes(memoryview(di)), np.uint8),
+           "cams": np.stack([np.frombuffer(c.tobytes(), np.uint8) for c in cams]),
+           "prevs": np.stack([np.frombuffer(c.tobytes(), np.uint8) for c in prevs]),
+           "counters": np.array(cnt[:2], np.uint64), "meta": np.array([kind, grid, spheres, W, H, frames], np.int64)}
+    for f in range(frames):
+        for k in DI_BUFFERS:
+            out["%s_%d" % (k, f)] = res[f][k]
+            out["%s_%d_sha256" % (k, f)] = np.array(digest(res[f][k]))
+    path = os.path.join(HERE, name + ".npz")
+    np.savez_compressed(path, **out)
+    return path
+
+
 if __name__ == "__main__":
-    if not os.path.exists(O.REF_LIB):
-        sys.exit("oracle/_ref/libgrisref.so missing: run oracle/ref/make_ref.py (needs the reference sources)")
-    for n in (sys.argv[1:] or CASES):
-        print(make(n), os.path.getsize(os.path.join(HERE, n + ".npz")))
+    if not os.path.exists(O.REF_LIB) or not os.path.exists(O.DI_REF_LIB):
+        sys.exit("oracle/_ref libraries missing: run oracle/ref/make_ref.py (needs the reference sources)")
+    for n in (sys.argv[1:] or list(CASES) + list(DI_CASES)):
+        print(make_di(n) if n in DI_CASES else make(n), os.path.getsize(os.path.join(HERE, n + ".npz")))

@@ -26,6 +26,8 @@ static_assert(sizeof(GrisLightTableEntry) == 8, "LightSampleTableElement is 8 B"
 static_assert(sizeof(GrisCamera) == 352, "Camera is 352 B");
 static_assert(sizeof(GrisReservoir) == 96, "GRISReservoir is 96 B");
 static_assert(sizeof(GrisSettings) == 64, "GrisSettings is 64 B");
+static_assert(sizeof(GrisDIReservoir) == 64, "DIReservoir is 64 B");
+static_assert(sizeof(GrisDISettings) == 16, "TestReSTIR::Settings is 16 B");
 
 /* Per-kernel CUDA-event timing of every launch while enabled (events recorded on the
  * launch stream around each kernel; read back and summed on request). */
@@ -75,7 +77,7 @@ struct Profiler : grisrt::KernelTimer {
     }
 };
 
-#define GRIS_NUM_COUNTERS 32
+#define GRIS_NUM_COUNTERS 48
 
 /* Scratch of the wavefront path tracer for the single-view entry points, grown on demand. */
 struct WaveScratch {
@@ -131,6 +133,10 @@ struct GrisFrame {
     GrisReservoir* resv[2] = {nullptr, nullptr};
     GrisReservoir* temp = nullptr;
     float* output = nullptr;
+    /* ReSTIR DI buffers (grisFrameRenderDI allocates them on first use) */
+    GrisDIReservoir* diResv[2] = {nullptr, nullptr};
+    GrisDIReservoir* diTemp = nullptr;
+    float* directOutput = nullptr;
     int next = 0;   /* slot the next render writes */
 };
 
@@ -197,6 +203,8 @@ size_t grisSizeof(int which) {
     case 5: return sizeof(GrisTriangleLight);
     case 6: return sizeof(GrisLightTableEntry);
     case 7: return sizeof(GrisSettings);
+    case 8: return sizeof(GrisDIReservoir);
+    case 9: return sizeof(GrisDISettings);
     }
     return 0;
 }
@@ -270,11 +278,11 @@ int grisReadKernelProfile(GrisContext* ctx, GrisKernelProfile out[GRIS_PROFILE_S
     if (!ctx || !out) return GRIS_ERR_INVALID_ARGUMENT;
     cudaSetDevice(ctx->device);
     ctx->prof.collect();
-    GRIS_CK(ctx, cudaMemcpyAsync(ctx->hCounters + 8, ctx->dCounters + 8, 24 * sizeof(unsigned long long),
+    GRIS_CK(ctx, cudaMemcpyAsync(ctx->hCounters + 8, ctx->dCounters + 8, 35 * sizeof(unsigned long long),
                                  cudaMemcpyDeviceToHost, ctx->stream));
     if (reset) {
         GRIS_CK(ctx, cudaMemsetAsync(ctx->dCounters + 8, 0, 16 * sizeof(unsigned long long), ctx->stream));
-        GRIS_CK(ctx, cudaMemsetAsync(ctx->dCounters + 26, 0, 6 * sizeof(unsigned long long), ctx->stream));
+        GRIS_CK(ctx, cudaMemsetAsync(ctx->dCounters + 26, 0, 17 * sizeof(unsigned long long), ctx->stream));
     }
     GRIS_CK(ctx, cudaStreamSynchronize(ctx->stream));
     const unsigned long long* c = ctx->hCounters;
@@ -287,6 +295,10 @@ int grisReadKernelProfile(GrisContext* ctx, GrisKernelProfile out[GRIS_PROFILE_S
         if (k == GRIS_SLOT_WAVE_EXTEND || k == GRIS_SLOT_WAVE_SHADOW) {
             int s = k == GRIS_SLOT_WAVE_EXTEND ? 0 : 1;
             o.nodes = c[26 + 3 * s]; o.tris = c[27 + 3 * s]; o.rays = c[28 + 3 * s];
+        }
+        if (k >= GRIS_SLOT_DI_CANDIDATES && k <= GRIS_SLOT_DI_SPATIAL) {
+            int d = k - GRIS_SLOT_DI_CANDIDATES;
+            o.nodes = c[32 + 3 * d]; o.tris = c[33 + 3 * d]; o.rays = c[34 + 3 * d];
         }
     }
     if (reset) ctx->prof.reset();
@@ -338,7 +350,7 @@ int grisReadWorkCounters(GrisContext* ctx, uint64_t nodes[4], uint64_t tris[4], 
                                  cudaMemcpyDeviceToHost, ctx->stream));
     if (reset) {
         GRIS_CK(ctx, cudaMemsetAsync(ctx->dCounters + 8, 0, 16 * sizeof(unsigned long long), ctx->stream));
-        GRIS_CK(ctx, cudaMemsetAsync(ctx->dCounters + 26, 0, 6 * sizeof(unsigned long long), ctx->stream));
+        GRIS_CK(ctx, cudaMemsetAsync(ctx->dCounters + 26, 0, 17 * sizeof(unsigned long long), ctx->stream));
     }
     GRIS_CK(ctx, cudaStreamSynchronize(ctx->stream));
     for (int k = 0; k < 4; k++) {
@@ -614,8 +626,10 @@ int grisFrameDestroy(GrisFrame* f) {
     if (!f) return GRIS_ERR_INVALID_ARGUMENT;
     cudaSetDevice(f->ctx->device);
     cudaStreamSynchronize(f->ctx->stream);
-    for (int i = 0; i < 2; i++) { cudaFree(f->depthNormal[i]); cudaFree(f->albedoMatId[i]); cudaFree(f->resv[i]); }
-    cudaFree(f->motion); cudaFree(f->temp); cudaFree(f->output);
+    for (int i = 0; i < 2; i++) {
+        cudaFree(f->depthNormal[i]); cudaFree(f->albedoMatId[i]); cudaFree(f->resv[i]); cudaFree(f->diResv[i]);
+    }
+    cudaFree(f->motion); cudaFree(f->temp); cudaFree(f->output); cudaFree(f->diTemp); cudaFree(f->directOutput);
     delete f;
     return GRIS_OK;
 }
@@ -642,6 +656,81 @@ int grisFrameRender(GrisContext* ctx, const GrisScene* s, GrisFrame* f, const Gr
     return GRIS_OK;
 }
 
+/* ------------------------------------------------------------------ ReSTIR DI */
+int grisPassDI(GrisContext* ctx, const GrisScene* s, const GrisDIBindings* b, const GrisCamera* cam,
+               const GrisCamera* prevCam, const GrisDISettings* set, int passes) {
+    if (!ctx || !s || !b || !cam || !prevCam || !set) return fail(ctx, GRIS_ERR_INVALID_ARGUMENT, "null argument");
+    if (b->width == 0 || b->height == 0 || !b->depthNormal || !b->albedoMatId || !b->reservoirThis ||
+        ((passes & 6) && !b->reservoirTemp) ||
+        ((passes & 2) && (!b->depthNormalPrev || !b->albedoMatIdPrev || !b->motion || !b->reservoirPrev)) ||
+        ((passes & 4) && !b->directOutput))
+        return fail(ctx, GRIS_ERR_INVALID_ARGUMENT, "DI pass bindings incomplete");
+    if (cam->filmSize[0] != b->width || cam->filmSize[1] != b->height)
+        return fail(ctx, GRIS_ERR_INVALID_ARGUMENT, "camera filmSize differs from the bound extent");
+    if (set->shiftType > GRIS_DI_SHIFT_HYBRID || set->sampleType > GRIS_DI_SAMPLE_BOTH)
+        return fail(ctx, GRIS_ERR_INVALID_ARGUMENT, "DI shiftType must be 0..2 and sampleType 0..2");
+    grisrt::DeviceSceneView view;
+    int dev = -1;
+    if (!grisrt::scene_device(s, &view, &dev)) return fail(ctx, GRIS_ERR_INVALID_ARGUMENT, "scene has no device copy");
+    if (dev != ctx->device) return fail(ctx, GRIS_ERR_INVALID_ARGUMENT, "scene lives on another device");
+    cudaSetDevice(ctx->device);
+    GRIS_CK(ctx, grisrt::launch_di(view, *b, *cam, *prevCam, *set, passes & 7, ctx->dCounters, ctx->countWork,
+                                   &ctx->prof, ctx->stream));
+    return GRIS_OK;
+}
+
+int grisFrameRenderDI(GrisContext* ctx, const GrisScene* s, GrisFrame* f, const GrisCamera* cam,
+                      const GrisCamera* prevCam, const GrisSettings* set, const GrisDISettings* di) {
+    if (!ctx || !s || !f || !cam || !prevCam || !di) return fail(ctx, GRIS_ERR_INVALID_ARGUMENT, "null argument");
+    cudaSetDevice(ctx->device);
+    size_t n = (size_t)f->w * f->h;
+    if (!f->directOutput) {
+        cudaError_t e = cudaSuccess;
+        auto alloc = [&](void** p, size_t bytes) {
+            if (e == cudaSuccess) e = cudaMalloc(p, bytes);
+            if (e == cudaSuccess) e = cudaMemsetAsync(*p, 0, bytes, ctx->stream);
+        };
+        alloc((void**)&f->diResv[0], n * sizeof(GrisDIReservoir));
+        alloc((void**)&f->diResv[1], n * sizeof(GrisDIReservoir));
+        alloc((void**)&f->diTemp, n * sizeof(GrisDIReservoir));
+        alloc((void**)&f->directOutput, n * 16);
+        if (e != cudaSuccess) {
+            for (int i = 0; i < 2; i++) { cudaFree(f->diResv[i]); f->diResv[i] = nullptr; }
+            cudaFree(f->diTemp); cudaFree(f->directOutput);
+            f->diTemp = nullptr; f->directOutput = nullptr;
+            return cuda_fail(ctx, e, "DI buffers");
+        }
+    }
+    int j = f->next;
+    GrisGBufferBindings gb;
+    gb.width = f->w; gb.height = f->h;
+    gb.depthNormal = f->depthNormal[j]; gb.albedoMatId = f->albedoMatId[j]; gb.motion = f->motion;
+    int rc = grisPassGBuffer(ctx, s, &gb, cam);
+    if (rc != GRIS_OK) return rc;
+    GrisDIBindings d;
+    d.width = f->w; d.height = f->h;
+    d.depthNormal = f->depthNormal[j]; d.depthNormalPrev = f->depthNormal[j ^ 1];
+    d.albedoMatId = f->albedoMatId[j]; d.albedoMatIdPrev = f->albedoMatId[j ^ 1];
+    d.motion = f->motion;
+    d.reservoirThis = f->diResv[j]; d.reservoirPrev = f->diResv[j ^ 1]; d.reservoirTemp = f->diTemp;
+    d.directOutput = f->directOutput;
+    rc = grisPassDI(ctx, s, &d, cam, prevCam, di, 7);
+    if (rc != GRIS_OK) return rc;
+    if (set) {
+        GrisPassBindings b;
+        b.width = f->w; b.height = f->h;
+        b.depthNormal = f->depthNormal[j]; b.depthNormalPrev = f->depthNormal[j ^ 1];
+        b.albedoMatId = f->albedoMatId[j]; b.albedoMatIdPrev = f->albedoMatId[j ^ 1];
+        b.motion = f->motion;
+        b.reservoirThis = f->resv[j]; b.reservoirPrev = f->resv[j ^ 1]; b.reservoirTemp = f->temp;
+        b.output = f->output;
+        rc = grisPassRender(ctx, s, &b, cam, prevCam, set, 7);
+        if (rc != GRIS_OK) return rc;
+    }
+    f->next = j ^ 1;
+    return GRIS_OK;
+}
+
 int grisFrameGetBuffer(const GrisFrame* f, int which, int slot, void** devPtr, size_t* bytes) {
     if (!f || !devPtr || slot < 0 || slot > 1) return GRIS_ERR_INVALID_ARGUMENT;
     int j = (f->next ^ 1) ^ slot;   /* slot 0: written by the last render */
@@ -655,8 +744,12 @@ int grisFrameGetBuffer(const GrisFrame* f, int which, int slot, void** devPtr, s
     case 3: p = f->resv[j]; sz = n * sizeof(GrisReservoir); break;
     case 4: p = f->temp; sz = n * sizeof(GrisReservoir); break;
     case 5: p = f->output; sz = n * 16; break;
+    case 6: p = f->diResv[j]; sz = n * sizeof(GrisDIReservoir); break;
+    case 7: p = f->diTemp; sz = n * sizeof(GrisDIReservoir); break;
+    case 8: p = f->directOutput; sz = n * 16; break;
     default: return GRIS_ERR_INVALID_ARGUMENT;
     }
+    if (!p) return GRIS_ERR_INVALID_ARGUMENT;
     *devPtr = p;
     if (bytes) *bytes = sz;
     return GRIS_OK;

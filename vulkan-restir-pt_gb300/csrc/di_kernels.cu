@@ -1,0 +1,388 @@
+/*
+ * di_kernels.cu — the ReSTIR DI pass (direct lighting at the primary vertex) on sm_103a.
+ *
+ *   k_di_candidates  di_path_gen.comp / generatePath (di_path_gen.glsl:9-40) with sampleLi
+ *                    (di_reservoir.glsl:78-174)
+ *   k_di_temporal    di_temporal.comp / temporalReuse (di_temporal.glsl:9-90)
+ *   k_di_spatial     di_spatial.comp / spatialReuse + final shading + running mean
+ *                    (di_spatial.glsl:9-121, di_spatial.comp:14-27)
+ * with the two shifts of DIReservoirReuseAndMerge (reconnection, random replay;
+ * di_reservoir.glsl:176-296) shared by the reuse kernels, in the order of TestReSTIR::render
+ * (src/TestReSTIR.cpp:9-35).
+ *
+ * One thread per pixel of a 16 x 8 tile, as the GRIS kernels; reservoirs are 64 B (four 16-byte
+ * words per pixel, read and written as uint4). Traversal is the 8-wide BVH walk shared with the
+ * GRIS kernels (ray_query.cuh), called out of line from the several query sites of a kernel.
+ */
+#include <cuda_fp16.h>
+#include <cuda_runtime.h>
+
+#include "gris_device.cuh"
+#include "gris_kernels.h"
+#include "ray_query.cuh"
+
+namespace grisrt {
+
+static_assert(sizeof(GrisDIReservoir) == 64, "DIReservoir is 64 B");
+
+struct DISample { Isec isec; V3 Li; float pad0; float jac, pdf; uint32_t rng, isLight; };   /* layouts.glsl:96-106 */
+struct DIResv { DISample s; uint32_t M; float W, contrib, weight; };                        /* :108-115 */
+
+struct DICtx {
+    DevScene sc;
+    CamD cam, prev;
+    GrisDISettings set;
+    GrisDIBindings b;
+    unsigned long long* counters;
+    int countWork;
+};
+
+constexpr uint32_t kDICap = 40;              /* DIReservoirCapSample(resv, 40), di_temporal.glsl:87 / di_spatial.glsl:95 */
+constexpr uint32_t kDINeighbours = 10;       /* ResampleNum, di_spatial.glsl:62 */
+constexpr float kDIRadius = 20.0f;           /* ResampleRadius, di_spatial.glsl:63 */
+
+GD DIResv di_zero() {
+    DIResv r;
+    r.s.isec = isec_zero(); r.s.Li = v3s(0.0f); r.s.pad0 = 0.0f; r.s.jac = 0.0f; r.s.pdf = 0.0f;
+    r.s.rng = 0u; r.s.isLight = 0u;
+    r.M = 0u; r.W = 0.0f; r.contrib = 0.0f; r.weight = 0.0f;
+    return r;
+}
+GD bool di_usable(const DIResv& r) { return !isnan(r.W); }                                    /* di_reservoir.glsl:40-42 */
+GD void di_clear(DIResv& r) { r.M = 0u; r.W = 0.0f; r.contrib = 0.0f; }                       /* :34-38 */
+GD void di_add(DIResv& r, const DISample& s, float w, float u) {                              /* :50-58 */
+    r.W += w;
+    r.M++;
+    if (u * r.W < w) { r.s = s; r.weight = w; }
+}
+GD void di_merge(DIResv& r, const DIResv& rhs, float u) {                                     /* :60-68 */
+    r.W += rhs.W;
+    r.M += rhs.M;
+    if (u * r.W < rhs.W) { r.s = rhs.s; r.weight = rhs.weight; }
+}
+GD void di_cap(DIResv& r, uint32_t cap) {                                                      /* :70-75 */
+    if (r.M > cap) { r.W *= (float)cap / (float)r.M; r.M = cap; }
+}
+
+GD DIResv load_di(const GrisDIReservoir* buf, uint64_t i, uint64_t n) {
+    if (i >= n) return di_zero();
+    const uint4* p = reinterpret_cast<const uint4*>(buf + i);
+    uint4 a = p[0], b = p[1], c = p[2], d = p[3];
+    DIResv r;
+    r.s.isec.bx = __uint_as_float(a.x); r.s.isec.by = __uint_as_float(a.y); r.s.isec.inst = a.z; r.s.isec.tri = a.w;
+    r.s.Li = v3(__uint_as_float(b.x), __uint_as_float(b.y), __uint_as_float(b.z)); r.s.pad0 = __uint_as_float(b.w);
+    r.s.jac = __uint_as_float(c.x); r.s.pdf = __uint_as_float(c.y); r.s.rng = c.z; r.s.isLight = c.w;
+    r.M = d.x; r.W = __uint_as_float(d.y); r.contrib = __uint_as_float(d.z); r.weight = __uint_as_float(d.w);
+    return r;
+}
+GD void store_di(GrisDIReservoir* buf, uint64_t i, const DIResv& r) {
+    uint4* p = reinterpret_cast<uint4*>(buf + i);
+    p[0] = make_uint4(__float_as_uint(r.s.isec.bx), __float_as_uint(r.s.isec.by), r.s.isec.inst, r.s.isec.tri);
+    p[1] = make_uint4(__float_as_uint(r.s.Li.x), __float_as_uint(r.s.Li.y), __float_as_uint(r.s.Li.z), __float_as_uint(r.s.pad0));
+    p[2] = make_uint4(__float_as_uint(r.s.jac), __float_as_uint(r.s.pdf), r.s.rng, r.s.isLight);
+    p[3] = make_uint4(r.M, __float_as_uint(r.W), __float_as_uint(r.contrib), __float_as_uint(r.weight));
+}
+
+/* sampleLi (di_reservoir.glsl:78-174): the light and / or BSDF candidate streamed into `resv`
+ * (one draw of resvRng per candidate), then the chosen sample's Li scaled by W / w and M = 1.
+ * The candidates' own colour sum is never used by the pass and is not formed. */
+GD void di_sample_li(const DICtx& P, const Surf& surf, const Mat& mat, V3 wo, uint32_t rng, uint32_t& resvRng,
+                     DIResv& resv, RayCount& rc, int& err) {
+    DISample ps = di_zero().s;
+    ps.rng = rng;
+    V4 lr = sample4f(rng);
+    V3 sr = sample3f(rng);
+    if (P.set.sampleType != GRIS_DI_SAMPLE_BSDF && !isBSDFDelta(mat)) {
+        V3 wi = v3s(0.0f); float dist = 0.0f, pdf = 0.0f, jac = 0.0f; V2 bary = v2(0.0f, 0.0f); uint32_t id = 0u;
+        V3 Le = sampleLightByPower(P.sc, surf.pos, wi, dist, pdf, jac, bary, id, lr);
+        bool shadowed = traceShadowCall(P.sc, surf.pos, kMinRayDistance, wi, dist - kMinRayDistance, rc, err);
+        if (!shadowed && pdf > 1e-6f) {
+            float w = MISWeight(pdf, evalPdf(mat, surf.norm, wo, wi));
+            if (P.set.sampleType == GRIS_DI_SAMPLE_LIGHT) w = 1.0f;
+            V3 contrib = Le * evalBSDF(mat, surf.albedo, surf.norm, wo, wi) * satDot(surf.norm, wi) / pdf * w;
+            float sw = luminance(contrib);
+            if (isnan(sw) || sw < 0.0f) sw = 0.0f;
+            ps.isec.bx = bary.x; ps.isec.by = bary.y; ps.isec.inst = 0u; ps.isec.tri = id;
+            ps.Li = Le * w;
+            ps.jac = jac; ps.pdf = pdf; ps.isLight = 1u;
+            di_add(resv, ps, sw, sample1f(resvRng));
+        }
+    }
+    ps.isLight = 0u;
+    BsdfSample s = bs_zero();
+    if (P.set.sampleType != GRIS_DI_SAMPLE_LIGHT && sampleBSDF(mat, surf.albedo, surf.norm, wo, sr, s) && s.pdf > 1e-6f) {
+        Isec isec = traceClosestHitCall(P.sc, surf.pos, s.wi, kMinRayDistance, kMaxRayDistance, rc, err);
+        if (isec.inst != kInvalidHit) {
+            Surf hit = surf_zero();
+            loadSurfaceInfo(P.sc, isec, hit);
+            float cosT = -dot3(s.wi, hit.norm);
+            if (hit.isLight && cosT > 0.0f) {
+                float dist = length3(hit.pos - surf.pos);
+                float lightPdf = luminance(hit.albedo) / load_table(P.sc, 0).prob * dist * dist / fabsf(cosT);
+                float w = MISWeight(s.pdf, lightPdf);
+                bool delta = isSampleTypeDelta(s.type);
+                if (P.set.sampleType == GRIS_DI_SAMPLE_BSDF || delta) w = 1.0f;
+                float cosTerm = delta ? 1.0f : satDot(surf.norm, s.wi);
+                V3 contrib = hit.albedo * s.bsdf * cosTerm / s.pdf * w;
+                ps.isec = isec;
+                ps.Li = hit.albedo * w;
+                ps.jac = fabsf(cosT) / square(dist); ps.pdf = s.pdf; ps.isLight = 0u;
+                di_add(resv, ps, luminance(contrib), sample1f(resvRng));   /* unclamped, as the reference */
+            }
+        }
+    }
+    if (!di_usable(resv)) di_clear(resv);
+    if (resv.M > 0u && resv.s.isec.inst != kInvalidHit && resv.weight > 0.0f) {
+        resv.s.Li = resv.s.Li * (resv.W / resv.weight);
+        resv.weight = resv.W;
+    } else {
+        resv.s.isec.inst = kInvalidHit;
+        resv.weight = 0.0f;
+        resv.W = 0.0f;
+    }
+    resv.M = 1u;
+}
+
+/* randomReplay (di_reservoir.glsl:176-209): the source's candidates drawn again at the
+ * destination from the source's seed; their reservoir draws come from the merge stream. */
+GD void di_replay(const DICtx& P, DIResv& dst, const Surf& ds, const DIResv& src, V3 wo, uint32_t& rng, RayCount& rc,
+                  int& err) {
+    Mat mat = load_material(P.sc, ds.matIndex);
+    DIResv rr = di_zero();
+    di_clear(rr);
+    di_sample_li(P, ds, mat, wo, src.s.rng, rng, rr, rc, err);
+    if (rr.s.isec.inst != kInvalidHit) {
+        Surf rs = surf_zero();
+        loadSurfaceInfo(P.sc, rr.s.isec, rs);
+        V3 wi = normalize3(rs.pos - ds.pos);
+        V3 Li = rr.s.Li * evalBSDF(mat, ds.albedo, ds.norm, wo, wi) * satDot(ds.norm, wi) / rr.s.pdf;
+        float pHat = luminance(Li * 1.0f);
+        rr.W = src.W * pHat / src.weight;
+        rr.M = src.M;
+    } else {
+        rr.W = 0.0f;
+    }
+    if (di_usable(rr)) di_merge(dst, rr, sample1f(rng));
+}
+
+/* reconnection (di_reservoir.glsl:211-287): the source's light vertex seen from the destination
+ * (one visibility ray), Jacobian (|cos| / d^2)_dst / jacobian_src. */
+GD void di_reconnect(const DICtx& P, DIResv& dst, const Surf& ds, DIResv src, V3 wo, uint32_t& rng, RayCount& rc,
+                     int& err) {
+    Mat mat = load_material(P.sc, ds.matIndex);
+    DISample ss = src.s;
+    Surf lv = surf_zero();
+    loadSurfaceInfo(P.sc, ss.isec, lv);
+    float dist = distance3(lv.pos, ds.pos);
+    V3 wi = normalize3(lv.pos - ds.pos);
+    float cosT = -dot3(lv.norm, wi);
+    float dstJac = fabsf(cosT) / square(dist);
+    float jac = dstJac / ss.jac;
+    bool ok = false;
+    float pHat = 0.0f, dstPdf = 0.0f;
+    if (ss.isec.inst != kInvalidHit && dist > 1e-4f) {
+        if (cosT > 0.0f && !isnan(jac) && ss.jac > 0.0f) {
+            if (traceVisibility(P.sc, ds.pos, lv.pos, rc, err)) {
+                ok = true;
+                if (!isnan(ss.pdf) && ss.pdf > 1e-6f) {
+                    V3 Li = src.s.Li * evalBSDF(mat, ds.albedo, ds.norm, wo, wi) * satDot(ds.norm, wi) / ss.pdf;
+                    pHat = luminance(Li * jac);
+                }
+                if (ss.isLight) dstPdf = luminance(lv.albedo) / load_table(P.sc, 0).prob / dstJac;
+                else dstPdf = evalPdf(mat, ds.norm, wo, wi);
+            }
+        }
+    }
+    if (ok) {
+        ss.jac = dstJac;
+        ss.pdf = dstPdf;
+        if (ss.pdf < 1e-6f || isnan(ss.pdf)) ss.pdf = 0.0f;
+        src.s = ss;
+        src.W *= pHat / src.weight;
+        if (isnan(src.W)) src.W = 0.0f;
+    } else {
+        src.W = 0.0f;
+    }
+    if (di_usable(src)) di_merge(dst, src, sample1f(rng));
+}
+
+/* DIReservoirReuseAndMerge (di_reservoir.glsl:289-296) */
+GD void di_reuse(const DICtx& P, DIResv& dst, const Surf& ds, const DIResv& src, V3 wo, uint32_t& rng, RayCount& rc,
+                 int& err) {
+    if (P.set.shiftType == GRIS_DI_SHIFT_RECONNECTION) di_reconnect(P, dst, ds, src, wo, rng, rc, err);
+    else if (P.set.shiftType == GRIS_DI_SHIFT_REPLAY) di_replay(P, dst, ds, src, wo, rng, rc, err);
+}
+
+/* The final sample's visibility in both reuse passes (di_temporal.glsl:76-85, di_spatial.glsl:84-93). */
+GD void di_occlude(const DICtx& P, DIResv& r, V3 pos, RayCount& rc, int& err) {
+    if (di_usable(r) && r.s.isec.inst != kInvalidHit) {
+        Surf s = surf_zero();
+        loadSurfaceInfo(P.sc, r.s.isec, s);
+        if (!traceVisibility(P.sc, pos, s.pos, rc, err)) r.W = 0.0f;
+    }
+}
+
+/* The pixel's primary vertex from the G-buffer (unpackGBuffer + camera ray, as every DI shader). */
+struct DIPixel {
+    V2 uv;
+    Ray3 ray;
+    Surf surf;
+    int matMeshId;
+};
+GD bool di_pixel(const DICtx& P, uint32_t ix, uint32_t iy, DIPixel& px) {
+    const int W = (int)P.b.width, H = (int)P.b.height;
+    px.uv = v2(((float)ix + 0.5f) / (float)W, ((float)iy + 0.5f) / (float)H);
+    float depth = 0.0f; V3 norm = v3s(0.0f), albedo = v3s(0.0f); int mm = 0;
+    float4 dn = texture_bilinear(reinterpret_cast<const float4*>(P.b.depthNormal), W, H, px.uv);
+    uint2 am = fetch_am(reinterpret_cast<const uint2*>(P.b.albedoMatId), W, H, (int)ix, (int)iy);
+    if (!unpackGBuffer(dn, am, depth, norm, albedo, mm)) return false;
+    px.ray = pinholeCameraSampleRay(P.cam, v2(px.uv.x, 1.0f - px.uv.y));
+    px.surf.pos = px.ray.ori + px.ray.dir * (depth - 1e-4f);
+    px.surf.norm = norm; px.surf.albedo = albedo; px.surf.matIndex = (uint32_t)(mm >> 16); px.surf.isLight = false;
+    px.matMeshId = mm;
+    return true;
+}
+
+/* ------------------------------------------------------------------ kernels */
+__global__ void __launch_bounds__(128) k_di_candidates(DICtx P) {
+    RayCount rc = ray_count();
+    int err = 0;
+    uint32_t x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y * blockDim.y + threadIdx.y;
+    DIPixel px;
+    if (x < P.b.width && y < P.b.height && di_pixel(P, x, y, px)) {
+        uint32_t rng = makeSeed2(P.cam.seed, x, y);
+        uint32_t resvRng = ~rng;
+        DIResv r = di_zero();
+        di_clear(r);
+        di_sample_li(P, px.surf, load_material(P.sc, px.surf.matIndex), -px.ray.dir, rng, resvRng, r, rc, err);
+        store_di(P.b.reservoirThis, (uint64_t)y * P.b.width + x, r);
+    }
+    flush_counts(P.counters, rc, err, 4, P.countWork);
+}
+
+/* findPreviousReservoir (di_temporal.glsl:9-34) + temporalReuse (:36-90) */
+__global__ void __launch_bounds__(128) k_di_temporal(DICtx P) {
+    RayCount rc = ray_count();
+    int err = 0;
+    uint32_t x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y * blockDim.y + threadIdx.y;
+    DIPixel px;
+    if (x < P.b.width && y < P.b.height && di_pixel(P, x, y, px)) {
+        const int W = (int)P.b.width, H = (int)P.b.height;
+        const uint64_t n = (uint64_t)W * (uint64_t)H, idx = (uint64_t)y * W + x;
+        float2 motion = __half22float2(reinterpret_cast<const __half2*>(P.b.motion)[idx]);
+        uint32_t resvRng = ~(makeSeed2(P.cam.seed, x, y) ^ 1u);
+        DIResv r = load_di(P.b.reservoirThis, idx, n);
+        if (P.set.temporalReuse) {
+            V2 puv = v2(px.uv.x + motion.x, px.uv.y + motion.y);
+            if ((P.cam.frameIndex & kCameraClearFlag) == 0u && !(puv.x < 0.0f || puv.y < 0.0f || puv.x > 1.0f || puv.y > 1.0f)) {
+                int qx = (int)(puv.x * (float)P.cam.w), qy = (int)(puv.y * (float)P.cam.h);
+                float pdepth = 0.0f; V3 pn = v3s(0.0f), palb = v3s(0.0f); int pmm = 0;
+                float4 pdn = texture_bilinear(reinterpret_cast<const float4*>(P.b.depthNormalPrev), W, H, puv);
+                uint2 pam = fetch_am(reinterpret_cast<const uint2*>(P.b.albedoMatIdPrev), W, H, qx, qy);
+                if (unpackGBuffer(pdn, pam, pdepth, pn, palb, pmm)) {
+                    Ray3 pray = pinholeCameraSampleRay(P.prev, v2(puv.x, 1.0f - puv.y));
+                    V3 ppos = pray.ori + pray.dir * (pdepth - 1e-4f);
+                    if (!(pmm != px.matMeshId || dot3(pn, px.surf.norm) < 0.95f || distance3(px.surf.pos, ppos) > 0.5f)) {
+                        DIResv src = load_di(P.b.reservoirPrev, (uint64_t)((uint32_t)P.cam.w * (uint32_t)qy + (uint32_t)qx), n);
+                        if (di_usable(src)) di_reuse(P, r, px.surf, src, -px.ray.dir, resvRng, rc, err);
+                    }
+                }
+            }
+            di_occlude(P, r, px.surf.pos, rc, err);
+        }
+        di_cap(r, kDICap);
+        if (!di_usable(r)) di_clear(r);
+        store_di(P.b.reservoirTemp, idx, r);
+    }
+    flush_counts(P.counters, rc, err, 5, P.countWork);
+}
+
+/* findNeighborReservoir (di_spatial.glsl:9-34) + spatialReuse (:36-121) + the running mean of
+ * di_spatial.comp:21-26 (a background pixel accumulates black). */
+__global__ void __launch_bounds__(128) k_di_spatial(DICtx P) {
+    RayCount rc = ray_count();
+    int err = 0;
+    uint32_t x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y * blockDim.y + threadIdx.y;
+    if (x < P.b.width && y < P.b.height) {
+        const int W = (int)P.b.width, H = (int)P.b.height;
+        const uint64_t n = (uint64_t)W * (uint64_t)H, idx = (uint64_t)y * W + x;
+        V3 color = v3s(0.0f);
+        DIPixel px;
+        if (di_pixel(P, x, y, px)) {
+            uint32_t rng = makeSeed2(P.cam.seed, x, y) ^ 2u;
+            V3 wo = -px.ray.dir;
+            DIResv r = load_di(P.b.reservoirTemp, idx, n);
+            if (P.set.spatialReuse) {
+                float tx = 1.0f / (float)W, ty = 1.0f / (float)H;
+                for (uint32_t k = 0; k < kDINeighbours; k++) {
+                    V2 d = toConcentricDisk(sample2f(rng));
+                    V2 nb = v2(px.uv.x + d.x * kDIRadius * tx, px.uv.y + d.y * kDIRadius * ty);
+                    if (nb.x < 0.0f || nb.y < 0.0f || nb.x > 1.0f || nb.y > 1.0f) continue;
+                    int qx = (int)(nb.x * (float)P.cam.w), qy = (int)(nb.y * (float)P.cam.h);
+                    float ndepth = 0.0f; V3 nn = v3s(0.0f), nalb = v3s(0.0f); int nmm = 0;
+                    float4 ndn = texture_bilinear(reinterpret_cast<const float4*>(P.b.depthNormal), W, H, nb);
+                    uint2 nam = fetch_am(reinterpret_cast<const uint2*>(P.b.albedoMatId), W, H, qx, qy);
+                    if (!unpackGBuffer(ndn, nam, ndepth, nn, nalb, nmm)) continue;
+                    Ray3 nr = pinholeCameraSampleRay(P.cam, v2(nb.x, 1.0f - nb.y));
+                    V3 npos = nr.ori + nr.dir * (ndepth - 1e-4f);
+                    if (dot3(nn, px.surf.norm) < 0.9f || distance3(px.surf.pos, npos) > 0.4f) continue;
+                    DIResv src = load_di(P.b.reservoirTemp, (uint64_t)((uint32_t)P.cam.w * (uint32_t)qy + (uint32_t)qx), n);
+                    if (di_usable(src)) di_reuse(P, r, px.surf, src, wo, rng, rc, err);
+                }
+                di_occlude(P, r, px.surf.pos, rc, err);
+            }
+            di_cap(r, kDICap);
+            if (!di_usable(r)) di_clear(r);
+            store_di(P.b.reservoirThis, idx, r);
+            if (di_usable(r) && r.s.isec.inst != kInvalidHit) {
+                Surf ls = surf_zero();
+                loadSurfaceInfo(P.sc, r.s.isec, ls);
+                V3 wi = normalize3(ls.pos - px.surf.pos);
+                if (r.M > 0u) {
+                    Mat mat = load_material(P.sc, px.surf.matIndex);
+                    V3 Li = r.s.Li * evalBSDF(mat, px.surf.albedo, px.surf.norm, wo, wi) * satDot(px.surf.norm, wi) / r.s.pdf;
+                    if (!isBlack(Li)) color = Li / luminance(Li) * r.W / (float)r.M;
+                }
+            }
+            color = clampColor(color);
+        }
+        float frameCount = (float)(P.cam.frameIndex & kCameraFrameIndexMask);
+        float4* out = reinterpret_cast<float4*>(P.b.directOutput) + idx;
+        float4 o = *out;
+        V3 acc = (v3(o.x, o.y, o.z) * frameCount + color) / (frameCount + 1.0f);
+        *out = make_float4(acc.x, acc.y, acc.z, 1.0f);
+    }
+    flush_counts(P.counters, rc, err, 6, P.countWork);
+}
+
+cudaError_t launch_di(const DeviceSceneView& scene, const GrisDIBindings& b, const GrisCamera& cam,
+                      const GrisCamera& prevCam, const GrisDISettings& set, int passes, unsigned long long* counters,
+                      int countWork, KernelTimer* timer, cudaStream_t stream) {
+    DICtx P;
+    P.sc = to_dev(scene);
+    P.cam = make_cam(cam);
+    P.prev = make_cam(prevCam);
+    P.set = set;
+    P.b = b;
+    P.counters = counters;
+    P.countWork = countWork;
+    dim3 block(16, 8), grid((b.width + 15) / 16, (b.height + 7) / 8);
+    if (passes & 1) {
+        if (timer) timer->mark(GRIS_SLOT_DI_CANDIDATES, true, stream);
+        k_di_candidates<<<grid, block, 0, stream>>>(P);
+        if (timer) timer->mark(GRIS_SLOT_DI_CANDIDATES, false, stream);
+    }
+    if (passes & 2) {
+        if (timer) timer->mark(GRIS_SLOT_DI_TEMPORAL, true, stream);
+        k_di_temporal<<<grid, block, 0, stream>>>(P);
+        if (timer) timer->mark(GRIS_SLOT_DI_TEMPORAL, false, stream);
+    }
+    if (passes & 4) {
+        if (timer) timer->mark(GRIS_SLOT_DI_SPATIAL, true, stream);
+        k_di_spatial<<<grid, block, 0, stream>>>(P);
+        if (timer) timer->mark(GRIS_SLOT_DI_SPATIAL, false, stream);
+    }
+    return cudaGetLastError();
+}
+
+}  // namespace grisrt

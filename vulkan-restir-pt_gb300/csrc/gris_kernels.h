@@ -38,6 +38,10 @@ cudaError_t launch_gbuffer(const DeviceSceneView& scene, const GrisGBufferBindin
 cudaError_t launch_gris(const DeviceSceneView& scene, const GrisPassBindings& b, const GrisCamera& cam,
                         const GrisCamera& prevCam, const GrisSettings& set, int passes, unsigned long long* counters,
                         int countWork, KernelTimer* timer, cudaStream_t stream, int launchMode = GRIS_LAUNCH_PERSISTENT);
+/* ReSTIR DI (TestReSTIR::render): passes bit 0 candidates, bit 1 temporal, bit 2 spatial */
+cudaError_t launch_di(const DeviceSceneView& scene, const GrisDIBindings& b, const GrisCamera& cam,
+                      const GrisCamera& prevCam, const GrisDISettings& set, int passes, unsigned long long* counters,
+                      int countWork, KernelTimer* timer, cudaStream_t stream);
 /* converged image: FP64 sums of independent paths per pixel; relMSE / MSE reduction */
 cudaError_t launch_converged(const DeviceSceneView& scene, const GrisConvergedBindings& b, const GrisCamera& cam,
                              const GrisSettings& set, uint32_t sppBegin, uint32_t sppCount, int estimator,

@@ -32,6 +32,12 @@ RESERVOIR = np.dtype([("bary", "<f4", 2), ("instanceIdx", "<u4"), ("triangleIdx"
                       ("pad", "<f4", 2), ("rcPrevSamplePdf", "<f4"), ("rcJacobian", "<f4"),
                       ("F", "<f4", 3), ("primaryRng", "<u4"),
                       ("sampleCount", "<f4"), ("resampleWeight", "<f4"), ("contribWeight", "<f4"), ("pad0", "<f4")])
+# DIReservoir (layouts.glsl:96-115), 64 B; isLightSample is the GLSL bool as a 32-bit 0 / 1
+DI_RESERVOIR = np.dtype([("bary", "<f4", 2), ("instanceIdx", "<u4"), ("triangleIdx", "<u4"),
+                         ("Li", "<f4", 3), ("pad0", "<f4"), ("jacobian", "<f4"), ("samplePdf", "<f4"),
+                         ("rng", "<u4"), ("isLightSample", "<u4"), ("sampleCount", "<u4"),
+                         ("resampleWeight", "<f4"), ("contribWeight", "<f4"), ("weight", "<f4")])
+assert DI_RESERVOIR.itemsize == 64
 assert MATERIAL.itemsize == 32 and VERTEX.itemsize == 32 and INSTANCE.itemsize == 224
 assert LIGHT.itemsize == 64 and TABLE.itemsize == 8 and RESERVOIR.itemsize == 96
 
@@ -40,6 +46,8 @@ LAUNCH_GRID, LAUNCH_PERSISTENT = 0, 1
 PATH_MEGAKERNEL, PATH_WAVEFRONT = 0, 1
 NOALLOC_MAX_PIXELS = 65536
 CLEAR_FLAG = 0x80000000
+DI_SHIFT_RECONNECTION, DI_SHIFT_REPLAY, DI_SHIFT_HYBRID = 0, 1, 2
+DI_SAMPLE_LIGHT, DI_SAMPLE_BSDF, DI_SAMPLE_BOTH = 0, 1, 2
 
 
 class Camera(ctypes.Structure):
@@ -75,6 +83,27 @@ class Settings(ctypes.Structure):
         s.cap, s.maxDepth, s.spatialNeighbors, s.spatialRadius = cap, maxDepth, spatialNeighbors, spatialRadius
         s.misWeights = int(misWeights)
         return s
+
+
+class DISettings(ctypes.Structure):
+    """TestReSTIR::Settings (src/TestReSTIR.h:12-17); defaults as TestReSTIR.h:29."""
+    _fields_ = [("shiftType", ctypes.c_uint32), ("sampleType", ctypes.c_uint32), ("temporalReuse", ctypes.c_uint32),
+                ("spatialReuse", ctypes.c_uint32)]
+
+    @classmethod
+    def make(cls, shiftType=DI_SHIFT_RECONNECTION, sampleType=DI_SAMPLE_LIGHT, temporalReuse=False, spatialReuse=True):
+        s = cls()
+        s.shiftType, s.sampleType = shiftType, sampleType
+        s.temporalReuse, s.spatialReuse = int(temporalReuse), int(spatialReuse)
+        return s
+
+
+class DIBindings(ctypes.Structure):
+    _fields_ = [("width", ctypes.c_uint32), ("height", ctypes.c_uint32),
+                ("depthNormal", ctypes.c_void_p), ("depthNormalPrev", ctypes.c_void_p),
+                ("albedoMatId", ctypes.c_void_p), ("albedoMatIdPrev", ctypes.c_void_p),
+                ("motion", ctypes.c_void_p), ("reservoirThis", ctypes.c_void_p), ("reservoirPrev", ctypes.c_void_p),
+                ("reservoirTemp", ctypes.c_void_p), ("directOutput", ctypes.c_void_p)]
 
 
 class SceneDesc(ctypes.Structure):
@@ -130,7 +159,8 @@ class KernelProfile(ctypes.Structure):
 
 
 PROFILE_SLOTS = ["gbuffer", "path_trace", "temporal", "spatial", "wave_begin", "wave_extend", "wave_shade",
-                 "wave_shadow", "wave_post", "guide_infer", "guide_train"]
+                 "wave_shadow", "wave_post", "guide_infer", "guide_train", "di_candidates", "di_temporal",
+                 "di_spatial"]
 
 
 class TuneResult(ctypes.Structure):
@@ -151,7 +181,7 @@ EXPORTS = [
     "grisReadKernelProfile", "grisConvergedAccumulate", "grisRelMSE",
     "grisGuideCreate", "grisGuideDestroy", "grisGuideParamCount", "grisGuideSetParams", "grisGuideGetParams",
     "grisGuideSetTraining", "grisGuideForward", "grisGuideGradient", "grisGuideTrainStep", "grisBatchSetGuide",
-    "grisHostSceneLoad", "grisHostSceneFilmSize", "grisSetWaveRefill",
+    "grisHostSceneLoad", "grisHostSceneFilmSize", "grisSetWaveRefill", "grisPassDI", "grisFrameRenderDI",
 ]
 
 _lib = None
@@ -230,6 +260,10 @@ def load(path=None):
         "grisReadKernelProfile": (i32, [vp, ctypes.POINTER(KernelProfile), i32]),
         "grisSetWaveLaunch": (i32, [vp, i32, i32]),
         "grisSetWaveRefill": (i32, [vp, i32]),
+        "grisPassDI": (i32, [vp, vp, ctypes.POINTER(DIBindings), ctypes.POINTER(Camera), ctypes.POINTER(Camera),
+                             ctypes.POINTER(DISettings), i32]),
+        "grisFrameRenderDI": (i32, [vp, vp, vp, ctypes.POINTER(Camera), ctypes.POINTER(Camera), ctypes.POINTER(Settings),
+                                    ctypes.POINTER(DISettings)]),
         "grisBatchAutotune": (i32, [vp, vp, ctypes.POINTER(Camera), ctypes.POINTER(Camera), ctypes.POINTER(Settings), i32,
                                     ctypes.POINTER(TuneResult)]),
     }
@@ -406,6 +440,11 @@ class Context:
         self.check(load().grisReadProfile(self.h, ms, n, int(reset)), "grisReadProfile")
         return list(ms), list(n)
 
+    def pass_di(self, scene, bindings, cam, prev_cam, di_settings, passes=7):
+        """grisPassDI on caller buffers (DIBindings of device pointers)."""
+        self.check(load().grisPassDI(self.h, scene.h, ctypes.byref(bindings), ctypes.byref(cam), ctypes.byref(prev_cam),
+                                     ctypes.byref(di_settings), int(passes)), "grisPassDI")
+
     def kernel_profile(self, reset=False):
         """{slot name: dict(ms, launches, nodes, tris, rays)} over PROFILE_SLOTS."""
         out = (KernelProfile * len(PROFILE_SLOTS))()
@@ -514,8 +553,10 @@ class Scene:
 
 
 BUF_DEPTH_NORMAL, BUF_ALBEDO_MATID, BUF_MOTION, BUF_RESERVOIR, BUF_TEMP, BUF_OUTPUT = range(6)
+BUF_DI_RESERVOIR, BUF_DI_TEMP, BUF_DIRECT_OUTPUT = 6, 7, 8
 _BUF_DTYPE = {0: (np.float32, 4), 1: (np.uint32, 2), 2: (np.uint16, 2), 3: (RESERVOIR, None),
-              4: (RESERVOIR, None), 5: (np.float32, 4)}
+              4: (RESERVOIR, None), 5: (np.float32, 4), 6: (DI_RESERVOIR, None), 7: (DI_RESERVOIR, None),
+              8: (np.float32, 4)}
 
 
 class Frame:
@@ -530,6 +571,14 @@ class Frame:
     def render(self, scene, cam, prev_cam, settings):
         self.ctx.check(load().grisFrameRender(self.ctx.h, scene.h, self.handle, ctypes.byref(cam), ctypes.byref(prev_cam),
                                               ctypes.byref(settings)), "grisFrameRender")
+
+    def render_di(self, scene, cam, prev_cam, di_settings, settings=None):
+        """The renderer's frame with the ReSTIR DI pass (grisFrameRenderDI); settings=None skips the
+        GRIS pass (indirect method None)."""
+        self.ctx.check(load().grisFrameRenderDI(self.ctx.h, scene.h, self.handle, ctypes.byref(cam),
+                                                ctypes.byref(prev_cam),
+                                                ctypes.byref(settings) if settings is not None else None,
+                                                ctypes.byref(di_settings)), "grisFrameRenderDI")
 
     def device_ptr(self, which, slot=0):
         p = ctypes.c_void_p()
