@@ -6,7 +6,10 @@ Workloads (--workload):
       instanced icospheres, GGX materials, 4 quad lights), max depth 8, temporal + spatial
       reuse (hybrid shift), camera orbit (60 frames per quarter turn);
   c3  64 independent views in one batch: resolutions from {64,128,256,512}^2, each with its own
-      box-or-terrain scene of 10k-200k triangles, max depth uniform in [2, 10].
+      box-or-terrain scene of 10k-200k triangles, max depth uniform in [2, 10];
+  c4  guided vs plain ReSTIR PT on the glossy variant (run_guided);
+  di  the ReSTIR DI pass (TestReSTIR::render) on the c2 scene at 1920x1080: G-buffer, candidates,
+      temporal and spatial reuse, direct output (run_di).
 
 One step = one frame of every view: G-buffer + path trace + temporal reuse + spatial reuse /
 final shading, rendered through grisBatchRender (a captured CUDA graph replayed per frame; the
@@ -51,6 +54,7 @@ METRICS = {
     "c2": "ReSTIR PT frames/s at 1080p (1.16M-tri synthetic scene, depth 8, temporal+spatial reuse)",
     "c3": "Batched ReSTIR PT frames/s (64 views of {64..512}^2, 10k-200k tris each, depth 2-10)",
     "c4": "Guided / plain ReSTIR PT time to equal relMSE (1080p glossy scene, depth 8, accumulating frames)",
+    "di": "ReSTIR DI frames/s at 1080p (1.16M-tri synthetic scene, candidates + temporal + spatial reuse)",
 }
 UNIT = "frames/s"
 NODE_BYTES, TRI_BYTES = 80, 48
@@ -111,7 +115,11 @@ def parse():
     ap.add_argument("--steps", type=int, default=30)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="grisrt", choices=["grisrt", "reference"])
-    ap.add_argument("--workload", default="c2", choices=["c1", "c2", "c3", "c4"])
+    ap.add_argument("--workload", default="c2", choices=["c1", "c2", "c3", "c4", "di"])
+    ap.add_argument("--di-shift", default="reconnection", choices=["reconnection", "replay", "hybrid"],
+                    help="di: the DI pass's shift")
+    ap.add_argument("--di-sample", default="both", choices=["light", "bsdf", "both"], help="di: candidate types")
+    ap.add_argument("--di-temporal", default="on", choices=["on", "off"], help="di: temporal reuse")
     ap.add_argument("--ref-spp", type=int, default=1024, help="c4: samples per pixel of the converged image")
     ap.add_argument("--mis", default="reference", choices=["reference", "pairwise"],
                     help="c4: the reuse passes' MIS weights (the reference's merge, or the pairwise extension)")
@@ -443,6 +451,221 @@ def run_guided(args):
     return 0
 
 
+def di_alg_bytes(slot, w, px):
+    """Algorithmic bytes of one frame of a DI kernel (work `w`, `px` pixels): traversal (nodes x 80 B
+    + triangles x 48 B) plus
+      di_candidates  24 B G-buffer read + 64 B reservoir write per pixel, a surface fetch per ray
+      di_temporal    24+4 B G-buffer + motion, 24 B previous G-buffer, 2 x 64 B reservoir reads,
+                     64 B write per pixel, a surface fetch per ray
+      di_spatial     11 x 24 B G-buffer + 11 x 64 B reservoir reads, 64 B write, 32 B output r/w per
+                     pixel, a surface fetch per ray."""
+    trav = w["nodes"] * NODE_BYTES + w["tris"] * TRI_BYTES
+    per_px = {"gbuffer": 28, "di_candidates": 88, "di_temporal": 244, "di_spatial": 11 * 24 + 11 * 64 + 64 + 32}
+    return trav + per_px[slot] * px + (SURFACE_BYTES * w["rays"] if slot != "gbuffer" else SURFACE_BYTES * px)
+
+
+def cpu_di_run(hs, cams, prevs, di, W, H, target_seconds, ora=None, plan=None):
+    """The oracle's DI pass (G-buffer + TestReSTIR::render) on a band of rows, calibrated to about
+    `target_seconds`; returns (frames/s, threads, sample text, plan, oracle)."""
+    from oracle import pyoracle as O
+    if ora is None:
+        ora = O.oracle()
+        ora.set_traversal(True)
+        ora.set_scene(hs)
+
+    def run(frac, nf):
+        rows = max(1, min(H, int(round(H * frac))))
+        ora.set_rows(0, rows)
+        t0 = time.perf_counter()
+        O.run_di_sequence(ora, ora, cams[:nf], prevs[:nf], di, W, H, record=())
+        dt = time.perf_counter() - t0
+        ora.set_rows(0, 1 << 30)
+        return dt, dt * H / rows
+
+    if plan is None:
+        frac, nf = 1.0 / 16.0, 2
+        for _ in range(6):
+            t_sample, t_full = run(frac, nf)
+            if t_sample >= 0.5 * target_seconds:
+                break
+            grow = max(2.0, min(16.0, target_seconds / max(t_sample, 1e-3)))
+            if frac < 1.0:
+                frac = min(1.0, frac * grow)
+            elif nf < len(cams):
+                nf = min(len(cams), int(math.ceil(nf * grow)))
+            else:
+                break
+        plan = (frac, nf)
+    else:
+        t_sample, t_full = run(*plan)
+    frac, nf = plan
+    sample = "%d frame(s) x the first %.1f%% of the rows, %.2f s of CPU time" % (nf, 100.0 * min(1.0, frac), t_sample)
+    return nf / t_full, ora.threads(), sample, plan, ora
+
+
+def run_di(args, rank, world, local):
+    """di: the ReSTIR DI pass through grisFrameRenderDI (G-buffer + candidates + temporal + spatial,
+    no indirect pass) on the c2 scene, camera orbit. Timed like c2: CUDA events on the library's
+    stream around every frame, L2 flushed between frames outside the events; e2e adds the direct
+    output's read-back into pinned host memory each frame; roofline from a profiled pass and a
+    work-counting pass of the same frames; the CPU baseline and the reference arm run the oracle's
+    DI pass (bit-identical to the reference's DI shaders run as C++)."""
+    import grisrt as G
+    K, WU = args.steps, max(args.warmup, 0)
+    shift = {"reconnection": G.DI_SHIFT_RECONNECTION, "replay": G.DI_SHIFT_REPLAY, "hybrid": G.DI_SHIFT_HYBRID}
+    sample = {"light": G.DI_SAMPLE_LIGHT, "bsdf": G.DI_SAMPLE_BSDF, "both": G.DI_SAMPLE_BOTH}
+    di = G.DISettings.make(shiftType=shift[args.di_shift], sampleType=sample[args.di_sample],
+                           temporalReuse=args.di_temporal == "on", spatialReuse=True)
+    hs = G.HostScene(1, seed=args.seed, grid=args.grid, spheres=args.spheres)
+    W, H = args.width, args.height
+    total = WU + 3 * K + 4
+    cams, prevs = G.sequence_cameras(hs, total, W, H, seed=args.seed, orbit_frames=60)
+    config = {"workload": "DI: %dx%d, %d^2 fBm heightfield + %d icospheres (%d tris), ReSTIR DI (%s shift, %s "
+                          "candidates, temporal %s, spatial 10 neighbours / 20 px, cap 40), orbit" % (
+                              W, H, args.grid, args.spheres, hs.triangle_count(), args.di_shift, args.di_sample,
+                              args.di_temporal),
+              "width": W, "height": H, "triangles": hs.triangle_count(), "di_shift": args.di_shift,
+              "di_sample": args.di_sample, "di_temporal": args.di_temporal,
+              "l2": "flushed between frames (256 MiB write outside the timed events)"}
+    metric = METRICS["di"]
+    if args.impl == "reference":
+        if rank != 0:
+            return 0
+        config["parallelism"] = "host cores (OpenMP)"
+        budget = max(5.0, min(60.0, 150.0 / max(1, K + WU)))
+        vals, plan, ora, threads, text = [], None, None, 0, ""
+        for step in range(WU + K):
+            fps, threads, text, plan, ora = cpu_di_run(hs, cams, prevs, di, W, H, budget, ora=ora, plan=plan)
+            if step >= WU:
+                vals.append(fps)
+        value = statistics.median(vals) if vals else 0.0
+        print(json.dumps({"metric": metric, "value": value, "unit": UNIT, "n_gpus": args.gpus, "steps": K,
+                          "warmup": WU, "ms_per_step": 1000.0 / value if value else None, "higher_is_better": True,
+                          "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+                          "data": "synthetic (seeded scene generator)", "config": config, "impl": "reference",
+                          "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
+                                           "sample": text},
+                          "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}))
+        return 0
+    import torch
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    config["parallelism"] = "replicas" if world > 1 else "1 GPU"
+    ctx = G.Context(local)
+    scene = G.Scene(ctx, hs)
+    frame = G.Frame(ctx, W, H)
+    stream = torch.cuda.ExternalStream(ctx.stream(), device=torch.device("cuda", local))
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
+    fi = 0
+
+    def barrier():
+        torch.cuda.synchronize()
+        if world > 1:
+            torch.distributed.barrier()
+
+    for _ in range(WU):
+        frame.render_di(scene, cams[fi], prevs[fi], di)
+        fi += 1
+    ctx.sync()
+    ctx.counters(reset=True)
+    sampler = ClockSampler(local)
+    sampler.start()
+    time.sleep(0.3)
+    barrier()
+    events = []
+    with torch.cuda.stream(stream):
+        for _ in range(K):
+            flush.zero_()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            frame.render_di(scene, cams[fi], prevs[fi], di)
+            e1.record(stream)
+            events.append((e0, e1))
+            fi += 1
+    barrier()
+    clocks = sampler.stop()
+    ms = sum(a.elapsed_time(b) for a, b in events)
+    cnt = ctx.counters(reset=True)
+    t_max = max_over_ranks(ms, "cuda")
+    value = aggregate_rate(K, t_max / 1000.0, world)
+    rays = cnt[0] + cnt[1] + cnt[2]
+    # per-kernel profile and work counts of the same frames
+    fi_p = fi - K
+    ctx.set_profiling(True)
+    ctx.kernel_profile(reset=True)
+    with torch.cuda.stream(stream):
+        for i in range(K):
+            flush.zero_()
+            frame.render_di(scene, cams[fi_p + i], prevs[fi_p + i], di)
+    ctx.sync()
+    prof = ctx.kernel_profile(reset=True)
+    ctx.set_profiling(False)
+    ctx.set_work_counting(True)
+    ctx.kernel_profile(reset=True)
+    for i in range(K):
+        frame.render_di(scene, cams[fi_p + i], prevs[fi_p + i], di)
+    ctx.sync()
+    work = ctx.kernel_profile(reset=True)
+    ctx.set_work_counting(False)
+    slots = ["gbuffer", "di_candidates", "di_temporal", "di_spatial"]
+    launches = sum(prof[s]["launches"] for s in slots)
+    # end to end: the direct output into pinned host memory every frame
+    lib = G.load()
+    out_host = torch.empty((W * H * 4,), dtype=torch.float32, pin_memory=True)
+    barrier()
+    t0 = time.perf_counter()
+    for _ in range(K):
+        frame.render_di(scene, cams[fi], prevs[fi], di)
+        ctx.check(lib.grisFrameDownload(ctx.h, frame.handle, G.BUF_DIRECT_OUTPUT, 0,
+                                        ctypes.c_void_p(out_host.data_ptr()), W * H * 16), "grisFrameDownload")
+        fi += 1
+    barrier()
+    e2e_s = max_over_ranks(time.perf_counter() - t0, "cuda")
+    e2e = {"value": aggregate_rate(K, e2e_s, world), "unit": UNIT, "h2d_bytes_per_step": 2 * 352 + 16,
+           "d2h_bytes_per_step": W * H * 16}
+    peak, peak_kind = load_peaks()
+    per_kernel = {}
+    for s_ in slots:
+        L = max(1, prof[s_]["launches"])
+        w = {k: work[s_][k] / K for k in ("nodes", "tris", "rays")}
+        alg = di_alg_bytes(s_, w, W * H)
+        avg_ms = prof[s_]["ms"] / L
+        per_kernel[s_] = {"ms_per_frame": prof[s_]["ms"] / K, "avg_launch_ms": avg_ms,
+                          "alg_bytes_per_launch": alg * K / L,
+                          "gbs": (alg * K / L) / (avg_ms / 1000.0) / 1e9 if avg_ms > 0 else None,
+                          "nodes_per_frame": w["nodes"], "tris_per_frame": w["tris"], "rays_per_frame": w["rays"]}
+    top = max(slots, key=lambda s_: prof[s_]["ms"])
+    pk = per_kernel[top]
+    achieved = pk["gbs"] or 0.0
+    roofline = {"bound": "hbm", "kernel": top, "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
+                "frac": round(achieved / peak, 4), "peak_source": peak_kind, "traffic": None,
+                "algorithmic_bytes_per_launch": pk["alg_bytes_per_launch"], "avg_launch_ms": pk["avg_launch_ms"],
+                "share_of_frame": round(prof[top]["ms"] / max(1e-9, sum(prof[s_]["ms"] for s_ in slots)), 3),
+                "kernels": per_kernel}
+    cpu = None
+    if rank == 0 and not args.no_cpu_baseline:
+        try:
+            fps, threads, text, _, _ = cpu_di_run(hs, cams, prevs, di, W, H, args.cpu_seconds)
+            cpu = {"value": fps, "unit": UNIT, "cores": threads, "kind": "port", "sample": text}
+        except Exception as ex:
+            cpu = {"value": None, "unit": UNIT, "cores": 0, "kind": "port", "sample": "failed: %s" % ex}
+    if rank == 0:
+        print(json.dumps({"metric": metric, "value": value, "unit": UNIT, "n_gpus": world, "steps": K, "warmup": WU,
+                          "ms_per_step": t_max / K, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+                          "dtype": "f32", "data": "synthetic (seeded scene generator, no dataset)", "config": config,
+                          "mrays_per_s": world * rays / (t_max / 1000.0) / 1e6, "rays_per_frame": rays / K,
+                          "clocks": clocks, "e2e": e2e, "gpu_launches": int(launches), "roofline": roofline,
+                          "cpu_baseline": cpu}))
+    frame.close()
+    scene.close()
+    ctx.close()
+    if world > 1:
+        torch.distributed.destroy_process_group()
+    return 0
+
+
 def main():
     args = parse()
     rank = int(os.environ.get("RANK", "0"))
@@ -453,6 +676,8 @@ def main():
         args.api = "batch"
     if args.workload == "c4" and args.impl != "reference":
         return run_guided(args)
+    if args.workload == "di":
+        return run_di(args, rank, world, local)
     import grisrt as G
     metric = METRICS[args.workload]
 
