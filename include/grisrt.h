@@ -515,6 +515,35 @@ int grisPassDI(GrisContext* ctx, const GrisScene* scene, const GrisDIBindings* b
 int grisFrameRenderDI(GrisContext* ctx, const GrisScene* scene, GrisFrame* frame, const GrisCamera* cam,
                       const GrisCamera* prevCam, const GrisSettings* settings, const GrisDISettings* di);
 
+/* ---------------------------------------------------------------- post-processing (headless)
+ * The reference's presentation pass (PostProcessFrag, src/shader/post_proc.frag:30-44, push
+ * constant src/PostProcessFrag.h:7-12) as a kernel: direct + indirect output (each unless its
+ * flag is set), tone mapping (0 none, 1 filmic, 2 ACES), gamma 1/2.2, then the B8G8R8A8_UNORM
+ * swapchain conversion (NaN -> 0, clamp to [0, 1], round(255 c)). The full-screen quad samples
+ * texel ivec2((size - 1) * uv) at uv = pixel centre / size, as the fragment shader does. The
+ * renderer's defaults are filmic + gamma (src/Renderer.h:32-33). pow is the library's
+ * deterministic x^y = 2^(y log2 x). */
+#define GRIS_TONEMAP_NONE 0
+#define GRIS_TONEMAP_FILMIC 1
+#define GRIS_TONEMAP_ACES 2
+typedef struct GrisPostSettings {   /* PostProcessFrag::PushConstant, 16 B */
+    uint32_t toneMapping;
+    uint32_t correctGamma;
+    uint32_t noDirect;
+    uint32_t noIndirect;
+} GrisPostSettings;
+typedef struct GrisPostBindings {
+    uint32_t width, height;
+    const float* directOutput;       /* float4 RGBA32F (may be NULL when noDirect) */
+    const float* indirectOutput;     /* float4 RGBA32F (may be NULL when noIndirect) */
+    float* color;                    /* float4: the fragment shader's output (may be NULL) */
+    uint8_t* rgba8;                  /* 4 bytes per pixel, R G B A, row 0 at the top (may be NULL) */
+} GrisPostBindings;
+int grisPostProcess(GrisContext* ctx, const GrisPostBindings* b, const GrisPostSettings* settings);
+/* Host: writes 8-bit RGBA pixels (row 0 at the top) as a PNG file (zlib stored blocks, no
+ * compression). Returns GRIS_OK or GRIS_ERR_INVALID_ARGUMENT with a message in errBuf. */
+int grisWritePNG(const char* path, const uint8_t* rgba, uint32_t width, uint32_t height, char* errBuf, size_t errLen);
+
 #ifdef __cplusplus
 }
 #endif

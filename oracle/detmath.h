@@ -55,4 +55,45 @@ static inline float oracle_det_sinf(float x) { float s, c; oracle_det_sincosf(x,
 static inline float oracle_det_cosf(float x) { float s, c; oracle_det_sincosf(x, &s, &c); return c; }
 static inline float oracle_det_tanf(float x) { float s, c; oracle_det_sincosf(x, &s, &c); return s / c; }
 
+/* x^y as the library's gris_det_powf (vulkan-restir-pt_gb300/csrc/detmath.h): 2^(y log2 x) with
+ * log2 from the atanh series of the mantissa in [sqrt(1/2), sqrt(2)) and 2^f from the Taylor
+ * series of e^(f ln 2); restated here so the oracle stays independent of the product's headers. */
+static inline unsigned oracle_dm_bits(float x) { unsigned u; __builtin_memcpy(&u, &x, 4); return u; }
+static inline float oracle_dm_float(unsigned u) { float x; __builtin_memcpy(&x, &u, 4); return x; }
+static inline float oracle_dm_pow2i(int n) { return oracle_dm_float((unsigned)(n + 127) << 23); }
+static inline float oracle_det_powf(float x, float y) {
+    if (!(x >= 0.0f)) return oracle_dm_float(0x7fc00000u);
+    if (x == 0.0f) return y > 0.0f ? 0.0f : (y == 0.0f ? 1.0f : oracle_dm_float(0x7f800000u));
+    if (x > 3.4028235e38f) return y > 0.0f ? x : (y == 0.0f ? 1.0f : 0.0f);
+    int e = 0;
+    if (x < 1.17549435e-38f) { x = x * 16777216.0f; e = -24; }
+    unsigned b = oracle_dm_bits(x);
+    e += (int)((b >> 23) & 0xffu) - 126;
+    float m = oracle_dm_float((b & 0x007fffffu) | 0x3f000000u);
+    if (m < 0.707106769f) { m = m * 2.0f; e -= 1; }
+    float t = (m - 1.0f) / (m + 1.0f), t2 = t * t;
+    float p = 0.111111112f;
+    p = p * t2 + 0.142857149f;
+    p = p * t2 + 0.200000003f;
+    p = p * t2 + 0.333333343f;
+    p = p * t2 + 1.0f;
+    float z = y * ((float)e + ((2.0f * t) * p) * 1.44269502f);
+    if (z > 128.0f) return oracle_dm_float(0x7f800000u);
+    if (z < -150.0f) return 0.0f;
+    float n = __builtin_rintf(z);
+    float r = (z - n) * 0.693147182f;
+    float q = 1.98412701e-4f;
+    q = q * r + 1.38888892e-3f;
+    q = q * r + 8.33333377e-3f;
+    q = q * r + 4.16666679e-2f;
+    q = q * r + 0.166666672f;
+    q = q * r + 0.5f;
+    q = q * r + 1.0f;
+    q = q * r + 1.0f;
+    int k = (int)n;
+    if (k > 127) return q * oracle_dm_pow2i(127) * oracle_dm_pow2i(k - 127);
+    if (k < -126) return q * oracle_dm_pow2i(-126) * oracle_dm_pow2i(k + 126);
+    return q * oracle_dm_pow2i(k);
+}
+
 #endif

@@ -1419,6 +1419,44 @@ void oracle_di_frame(const void* camera, const void* prevCamera, const void* set
     }
 }
 
+/* The presentation pass (post_proc.frag:16-44, push constant PostProcessFrag.h:7-12) at pixel
+ * centres of a full-screen quad; settings: {toneMapping, correctGamma, noDirect, noIndirect}.
+ * Writes the fragment colour (float4) and its B8G8R8A8_UNORM conversion (R, G, B, A bytes). */
+static inline float oraFilmicCurve(float c) {
+    return (c * (c * 0.22f + 0.03f) + 0.002f) / (c * (c * 0.22f + 0.3f) + 0.06f) - 1.0f / 30.0f;
+}
+static inline float oraTonemap(float c, uint32_t mode) {
+    if (mode == 0u) return c;
+    if (mode == 1u) return oraFilmicCurve(c * 1.6f) / oraFilmicCurve(11.2f);
+    return (c * (c * 2.51f + 0.03f)) / (c * (c * 2.43f + 0.59f) + 0.14f);
+}
+static inline uint8_t oraUnorm8(float c) {
+    if (!(c > 0.0f)) return 0;
+    if (c >= 1.0f) return 255;
+    return (uint8_t)floorf(c * 255.0f + 0.5f);
+}
+void oracle_post(uint32_t W, uint32_t H, const float* direct, const float* indirect, const uint32_t* settings,
+                 float* color, uint8_t* rgba8) {
+    for (uint32_t y = 0; y < H; y++)
+        for (uint32_t x = 0; x < W; x++) {
+            float u = ((float)x + 0.5f) / (float)W, v = ((float)y + 0.5f) / (float)H;
+            uint32_t cx = (uint32_t)((float)(W - 1u) * u), cy = (uint32_t)((float)(H - 1u) * v);
+            size_t src = (size_t)cy * W + cx, dst = (size_t)y * W + x;
+            float c[3] = {0.0f, 0.0f, 0.0f};
+            for (int k = 0; k < 3; k++) {
+                if (settings[2] == 0u) c[k] = c[k] + direct[src * 4 + k];
+                if (settings[3] == 0u) c[k] = c[k] + indirect[src * 4 + k];
+                c[k] = oraTonemap(c[k], settings[0]);
+                if (settings[1] != 0u) c[k] = oracle_det_powf(c[k], 1.0f / 2.2f);
+            }
+            if (color) { color[dst * 4] = c[0]; color[dst * 4 + 1] = c[1]; color[dst * 4 + 2] = c[2]; color[dst * 4 + 3] = 1.0f; }
+            if (rgba8) {
+                rgba8[dst * 4] = oraUnorm8(c[0]); rgba8[dst * 4 + 1] = oraUnorm8(c[1]);
+                rgba8[dst * 4 + 2] = oraUnorm8(c[2]); rgba8[dst * 4 + 3] = 255;
+            }
+        }
+}
+
 uint16_t oracle_f16(float f) { return toHalf(f); }
 
 }  /* extern "C" */

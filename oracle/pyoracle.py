@@ -172,6 +172,24 @@ def run_sequence(impl, cams, prevs, settings, width, height, frames=None, record
     return results
 
 
+def post_process(W, H, direct, indirect, post_settings):
+    """The oracle's presentation pass: returns (float32 [H*W, 4] colour, uint8 [H*W, 4] RGBA)."""
+    from . import build_oracle
+    lib = ctypes.CDLL(build_oracle.build())
+    vp = ctypes.c_void_p
+    lib.oracle_post.argtypes = [ctypes.c_uint32, ctypes.c_uint32, vp, vp, vp, vp, vp]
+    lib.oracle_post.restype = None
+    n = W * H
+    z = np.zeros((n, 4), np.float32)
+    d = np.ascontiguousarray(direct if direct is not None else z, np.float32)
+    i = np.ascontiguousarray(indirect if indirect is not None else z, np.float32)
+    sb = np.frombuffer(bytes(memoryview(post_settings)), np.uint32).copy()
+    color = np.zeros((n, 4), np.float32)
+    rgba = np.zeros((n, 4), np.uint8)
+    lib.oracle_post(W, H, _p(d), _p(i), _p(sb), _p(color), _p(rgba))
+    return color, rgba
+
+
 def run_di_sequence(gbuffer_impl, di_impl, cams, prevs, di_settings, width, height, record=("resv", "temp", "out")):
     """Frames of TestReSTIR::render with the renderer's ping-pong (src/Renderer.cpp:339-341): the
     G-buffer (gbuffer_impl) into slot j, the DI pass with This = R[j], Prev = R[j^1], j ^= 1.

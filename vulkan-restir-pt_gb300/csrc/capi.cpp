@@ -28,6 +28,7 @@ static_assert(sizeof(GrisReservoir) == 96, "GRISReservoir is 96 B");
 static_assert(sizeof(GrisSettings) == 64, "GrisSettings is 64 B");
 static_assert(sizeof(GrisDIReservoir) == 64, "DIReservoir is 64 B");
 static_assert(sizeof(GrisDISettings) == 16, "TestReSTIR::Settings is 16 B");
+static_assert(sizeof(GrisPostSettings) == 16, "PostProcessFrag::PushConstant is 16 B");
 
 /* Per-kernel CUDA-event timing of every launch while enabled (events recorded on the
  * launch stream around each kernel; read back and summed on request). */
@@ -728,6 +729,19 @@ int grisFrameRenderDI(GrisContext* ctx, const GrisScene* s, GrisFrame* f, const 
         if (rc != GRIS_OK) return rc;
     }
     f->next = j ^ 1;
+    return GRIS_OK;
+}
+
+/* ------------------------------------------------------------------ post-processing */
+int grisPostProcess(GrisContext* ctx, const GrisPostBindings* b, const GrisPostSettings* set) {
+    if (!ctx || !b || !set) return fail(ctx, GRIS_ERR_INVALID_ARGUMENT, "null argument");
+    if (b->width == 0 || b->height == 0 || (!b->color && !b->rgba8) || (!set->noDirect && !b->directOutput) ||
+        (!set->noIndirect && !b->indirectOutput))
+        return fail(ctx, GRIS_ERR_INVALID_ARGUMENT, "post-processing bindings incomplete");
+    if (set->toneMapping > GRIS_TONEMAP_ACES) return fail(ctx, GRIS_ERR_INVALID_ARGUMENT, "toneMapping must be 0..2");
+    if (b->height > 65535u) return fail(ctx, GRIS_ERR_INVALID_ARGUMENT, "height must be <= 65535");
+    cudaSetDevice(ctx->device);
+    GRIS_CK(ctx, grisrt::launch_post(*b, *set, ctx->stream));
     return GRIS_OK;
 }
 

@@ -42,6 +42,8 @@ cudaError_t launch_gris(const DeviceSceneView& scene, const GrisPassBindings& b,
 cudaError_t launch_di(const DeviceSceneView& scene, const GrisDIBindings& b, const GrisCamera& cam,
                       const GrisCamera& prevCam, const GrisDISettings& set, int passes, unsigned long long* counters,
                       int countWork, KernelTimer* timer, cudaStream_t stream);
+/* presentation pass (post_proc.frag): composition, tone mapping, gamma, UNORM8 */
+cudaError_t launch_post(const GrisPostBindings& b, const GrisPostSettings& set, cudaStream_t stream);
 /* converged image: FP64 sums of independent paths per pixel; relMSE / MSE reduction */
 cudaError_t launch_converged(const DeviceSceneView& scene, const GrisConvergedBindings& b, const GrisCamera& cam,
                              const GrisSettings& set, uint32_t sppBegin, uint32_t sppCount, int estimator,

@@ -106,6 +106,38 @@ class DIBindings(ctypes.Structure):
                 ("reservoirTemp", ctypes.c_void_p), ("directOutput", ctypes.c_void_p)]
 
 
+TONEMAP_NONE, TONEMAP_FILMIC, TONEMAP_ACES = 0, 1, 2
+
+
+class PostSettings(ctypes.Structure):
+    """PostProcessFrag::PushConstant (src/PostProcessFrag.h:7-12); defaults as src/Renderer.h:32-33."""
+    _fields_ = [("toneMapping", ctypes.c_uint32), ("correctGamma", ctypes.c_uint32), ("noDirect", ctypes.c_uint32),
+                ("noIndirect", ctypes.c_uint32)]
+
+    @classmethod
+    def make(cls, toneMapping=TONEMAP_FILMIC, correctGamma=True, noDirect=False, noIndirect=False):
+        s = cls()
+        s.toneMapping, s.correctGamma = toneMapping, int(correctGamma)
+        s.noDirect, s.noIndirect = int(noDirect), int(noIndirect)
+        return s
+
+
+class PostBindings(ctypes.Structure):
+    _fields_ = [("width", ctypes.c_uint32), ("height", ctypes.c_uint32), ("directOutput", ctypes.c_void_p),
+                ("indirectOutput", ctypes.c_void_p), ("color", ctypes.c_void_p), ("rgba8", ctypes.c_void_p)]
+
+
+def write_png(path, rgba, width, height):
+    """8-bit RGBA pixels (uint8 [height*width, 4], row 0 at the top) into a PNG file (grisWritePNG)."""
+    a = np.ascontiguousarray(rgba, dtype=np.uint8)
+    if a.size != width * height * 4:
+        raise ValueError("pixel array does not match %dx%d" % (width, height))
+    err = ctypes.create_string_buffer(256)
+    rc = load().grisWritePNG(os.fsencode(path), a.ctypes.data, width, height, err, 256)
+    if rc != 0:
+        raise GrisError("grisWritePNG failed (%d): %s" % (rc, err.value.decode(errors="replace")))
+
+
 class SceneDesc(ctypes.Structure):
     _fields_ = [("vertices", ctypes.c_void_p), ("vertexCount", ctypes.c_uint64),
                 ("indices", ctypes.c_void_p), ("indexCount", ctypes.c_uint64),
@@ -182,6 +214,7 @@ EXPORTS = [
     "grisGuideCreate", "grisGuideDestroy", "grisGuideParamCount", "grisGuideSetParams", "grisGuideGetParams",
     "grisGuideSetTraining", "grisGuideForward", "grisGuideGradient", "grisGuideTrainStep", "grisBatchSetGuide",
     "grisHostSceneLoad", "grisHostSceneFilmSize", "grisSetWaveRefill", "grisPassDI", "grisFrameRenderDI",
+    "grisPostProcess", "grisWritePNG",
 ]
 
 _lib = None
@@ -264,6 +297,8 @@ def load(path=None):
                              ctypes.POINTER(DISettings), i32]),
         "grisFrameRenderDI": (i32, [vp, vp, vp, ctypes.POINTER(Camera), ctypes.POINTER(Camera), ctypes.POINTER(Settings),
                                     ctypes.POINTER(DISettings)]),
+        "grisPostProcess": (i32, [vp, ctypes.POINTER(PostBindings), ctypes.POINTER(PostSettings)]),
+        "grisWritePNG": (i32, [ctypes.c_char_p, vp, u32, u32, ctypes.c_char_p, ctypes.c_size_t]),
         "grisBatchAutotune": (i32, [vp, vp, ctypes.POINTER(Camera), ctypes.POINTER(Camera), ctypes.POINTER(Settings), i32,
                                     ctypes.POINTER(TuneResult)]),
     }
@@ -439,6 +474,11 @@ class Context:
         n = (ctypes.c_uint64 * 4)()
         self.check(load().grisReadProfile(self.h, ms, n, int(reset)), "grisReadProfile")
         return list(ms), list(n)
+
+    def post_process(self, bindings, post_settings):
+        """grisPostProcess on device buffers (PostBindings of device pointers)."""
+        self.check(load().grisPostProcess(self.h, ctypes.byref(bindings), ctypes.byref(post_settings)),
+                   "grisPostProcess")
 
     def pass_di(self, scene, bindings, cam, prev_cam, di_settings, passes=7):
         """grisPassDI on caller buffers (DIBindings of device pointers)."""
