@@ -404,6 +404,11 @@ int grisSetWaveLaunch(GrisContext* ctx, int traceBlocksPerSM, int shadeBlocksPer
 /* 1: the wavefront's traversal kernels keep every lane busy (a lane whose ray is finished takes
  * the next ray while the others of its warp still walk); same results. */
 int grisSetWaveRefill(GrisContext* ctx, int enable);
+/* 1 (default): the batch spatial pass (reference merge, at most 4 neighbours) and the ReSTIR DI
+ * spatial pass (reconnection shift) walk each warp's reconnection visibility queries as one pool
+ * before their merges (a lane whose queries finish early walks the others'); 0: each lane traces
+ * its own queries inside its neighbour loop. Same results and ray counts. */
+int grisSetPooledVisibility(GrisContext* ctx, int enable);
 /* Times candidate configurations — the megakernel path tracer, the wavefront one with trace
  * grids of 8/16/32 and shading grids of 4/8/16 blocks per SM, and the wavefront one with the
  * refilling traversal kernels at 4/8/16 blocks per SM — over `frames` frames each on the given
