@@ -141,8 +141,6 @@ def parse():
     ap.add_argument("--path-form", default="wavefront", choices=["wavefront", "megakernel"],
                     help="starting form (the autotuner may switch)")
     ap.add_argument("--cpu-seconds", type=float, default=20.0, help="target CPU work of the baseline sample")
-    ap.add_argument("--pooled-visibility", default="on", choices=["on", "off"],
-                    help="spatial passes: walk each warp's visibility queries as one pool (grisSetPooledVisibility)")
     return ap.parse_args()
 
 
@@ -556,8 +554,6 @@ def run_di(args, rank, world, local):
         dist.init_process_group("nccl", device_id=torch.device("cuda", local))
     config["parallelism"] = "replicas" if world > 1 else "1 GPU"
     ctx = G.Context(local)
-    ctx.set_pooled_visibility(args.pooled_visibility == "on")
-    config["pooled_visibility"] = args.pooled_visibility == "on"
     scene = G.Scene(ctx, hs)
     frame = G.Frame(ctx, W, H)
     stream = torch.cuda.ExternalStream(ctx.stream(), device=torch.device("cuda", local))
@@ -725,8 +721,6 @@ def main():
     ctx.set_launch_mode(G.LAUNCH_PERSISTENT if args.launch_mode == "persistent" else G.LAUNCH_GRID)
     ctx.set_path_form(G.PATH_WAVEFRONT if args.path_form == "wavefront" else G.PATH_MEGAKERNEL)
     ctx.set_graphs(not args.no_graphs)
-    ctx.set_pooled_visibility(args.pooled_visibility == "on")
-    config["pooled_visibility"] = args.pooled_visibility == "on"
     scenes = [G.Scene(ctx, v.hs) for v in views]
     stats = [sc.stats() for sc in scenes]
     batch = G.Batch(ctx, scenes, [(v.w, v.h) for v in views]) if args.api == "batch" else None

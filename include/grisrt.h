@@ -404,11 +404,6 @@ int grisSetWaveLaunch(GrisContext* ctx, int traceBlocksPerSM, int shadeBlocksPer
 /* 1: the wavefront's traversal kernels keep every lane busy (a lane whose ray is finished takes
  * the next ray while the others of its warp still walk); same results. */
 int grisSetWaveRefill(GrisContext* ctx, int enable);
-/* 1 (default): the batch spatial pass (reference merge, at most 4 neighbours) and the ReSTIR DI
- * spatial pass (reconnection shift) walk each warp's reconnection visibility queries as one pool
- * before their merges (a lane whose queries finish early walks the others'); 0: each lane traces
- * its own queries inside its neighbour loop. Same results and ray counts. */
-int grisSetPooledVisibility(GrisContext* ctx, int enable);
 /* Times candidate configurations — the megakernel path tracer, the wavefront one with trace
  * grids of 8/16/32 and shading grids of 4/8/16 blocks per SM, and the wavefront one with the
  * refilling traversal kernels at 4/8/16 blocks per SM — over `frames` frames each on the given
@@ -541,7 +536,7 @@ typedef struct GrisPostBindings {
     uint32_t width, height;
     const float* directOutput;       /* float4 RGBA32F (may be NULL when noDirect) */
     const float* indirectOutput;     /* float4 RGBA32F (may be NULL when noIndirect) */
-    float* color;                    /* float4: the fragment shader's output (may be NULL) */
+    float* color;                    /* float4: the fragment shader's output, NaN as 0x7fc00000 (may be NULL) */
     uint8_t* rgba8;                  /* 4 bytes per pixel, R G B A, row 0 at the top (may be NULL) */
 } GrisPostBindings;
 int grisPostProcess(GrisContext* ctx, const GrisPostBindings* b, const GrisPostSettings* settings);

@@ -1449,7 +1449,10 @@ void oracle_post(uint32_t W, uint32_t H, const float* direct, const float* indir
                 c[k] = oraTonemap(c[k], settings[0]);
                 if (settings[1] != 0u) c[k] = oracle_det_powf(c[k], 1.0f / 2.2f);
             }
-            if (color) { color[dst * 4] = c[0]; color[dst * 4 + 1] = c[1]; color[dst * 4 + 2] = c[2]; color[dst * 4 + 3] = 1.0f; }
+            if (color) {   /* NaN channels as the canonical quiet NaN */
+                for (int k = 0; k < 3; k++) color[dst * 4 + k] = std::isnan(c[k]) ? oracle_dm_float(0x7fc00000u) : c[k];
+                color[dst * 4 + 3] = 1.0f;
+            }
             if (rgba8) {
                 rgba8[dst * 4] = oraUnorm8(c[0]); rgba8[dst * 4 + 1] = oraUnorm8(c[1]);
                 rgba8[dst * 4 + 2] = oraUnorm8(c[2]); rgba8[dst * 4 + 3] = 255;

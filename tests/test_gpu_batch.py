@@ -138,35 +138,3 @@ def test_batched_workload_views_match_oracle():
     for sc in scenes:
         sc.close()
     ctx.close()
-
-
-@pytest.mark.parametrize("pooled", [True, False], ids=["pooled", "per-lane"])
-def test_pooled_visibility_matches_oracle(setup, pooled):
-    """The spatial pass with the warp-pooled visibility queries (grisSetPooledVisibility; used when
-    every view has at most 4 neighbours) and without: every buffer equals the oracle's and the ray
-    counts are the same either way."""
-    ctx, hss, scenes, seqs, settings, want = setup
-    idx = [0, 1, 2, 3, 5]   # the views with at most 4 spatial neighbours
-    ctx.set_pooled_visibility(pooled)
-    batch = G.Batch(ctx, [scenes[v] for v in idx], [VIEWS[v][3:5] for v in idx])
-    ctx.counters(reset=True)
-    for f in range(FRAMES):
-        batch.render([seqs[v][0][f] for v in idx], [seqs[v][1][f] for v in idx], [settings[v] for v in idx])
-        for j, v in enumerate(idx):
-            for k, which in (("resv", G.BUF_RESERVOIR), ("temp", G.BUF_TEMP), ("out", G.BUF_OUTPUT)):
-                assert batch.download(j, which).tobytes() == want[v][f][k].tobytes(), \
-                    "pooled %s frame %d view %d buffer %s differs" % (pooled, f, v, k)
-    ctx.sync()
-    c = ctx.counters(reset=True)
-    assert c[3] == 0
-    ora = O.oracle()
-    total = [0, 0, 0]
-    for v in idx:
-        ora.set_scene(hss[v])
-        ora.read_counters(reset=True)
-        O.run_sequence(ora, seqs[v][0], seqs[v][1], settings[v], VIEWS[v][3], VIEWS[v][4], record=())
-        cv = ora.read_counters(reset=True)
-        total = [a + b for a, b in zip(total, cv[:3])]
-    assert list(c[:3]) == total
-    batch.close()
-    ctx.set_pooled_visibility(True)

@@ -55,13 +55,9 @@ def gpu_di(ctx, hs, cams, prevs, di, W, H_, settings=None):
     return out, counters
 
 
-@pytest.mark.parametrize("pooled", [True, False], ids=["pooled", "per-lane"])
 @pytest.mark.parametrize("case", CASES, ids=[c[0] for c in CASES])
-def test_gpu_di_matches_oracle(ctx, case, pooled):
-    """Both forms of the spatial kernel (warp-pooled visibility queries or per-lane ones) give the
-    oracle's buffers and ray counts."""
+def test_gpu_di_matches_oracle(ctx, case):
     name, kind, grid, spheres, W, H_, frames, kw = case
-    ctx.set_pooled_visibility(pooled)
     hs = G.HostScene(kind, seed=4, grid=grid, spheres=spheres)
     cams, prevs = G.sequence_cameras(hs, frames, W, H_, seed=17)
     di = G.DISettings.make(**kw)
@@ -75,7 +71,6 @@ def test_gpu_di_matches_oracle(ctx, case, pooled):
         for k in ("resv", "temp", "out"):
             assert got[f][k].tobytes() == want[f][k].tobytes(), "frame %d %s differs" % (f, k)
     assert list(cg[:3]) == list(cw[:3]) and cg[3] == 0
-    ctx.set_pooled_visibility(True)
 
 
 def test_gpu_di_pass_on_caller_buffers(ctx):

@@ -43,9 +43,8 @@ struct GrisBatch {
     /* captured frames, one per staging slot, valid for one frame shape */
     struct Graph {
         cudaGraphExec_t exec = nullptr;
-        int pathForm = -1, maxDepth = -1, trace = 0, shade = 0, refill = -1, countWork = -1, pooled = -1;
+        int pathForm = -1, maxDepth = -1, trace = 0, shade = 0, refill = -1, countWork = -1;
         bool pairwise = false;
-        uint32_t poolNeighbors = 0;
         uint32_t pixels = 0, tiles = 0;
         const GrisGuide* guide = nullptr;
         int train = -1;
@@ -191,8 +190,8 @@ int grisBatchRender(GrisContext* ctx, GrisBatch* b, const GrisCamera* cams, cons
         GrisBatch::Graph& g = b->graph[k];
         if (!g.exec || g.pathForm != form || g.maxDepth != sh.maxDepth || g.pixels != sh.pixels || g.tiles != sh.tiles ||
             g.trace != wl.traceBlocksPerSM || g.shade != wl.shadeBlocksPerSM || g.refill != wl.refill ||
-            g.countWork != ctx_count_work(ctx) || g.pooled != wl.pooledVisibility || g.pairwise != sh.pairwise ||
-            g.poolNeighbors != sh.poolNeighbors || g.guide != b->guide || g.train != train) {
+            g.countWork != ctx_count_work(ctx) || g.pairwise != sh.pairwise ||
+            g.guide != b->guide || g.train != train) {
             if (g.exec) { cudaGraphExecDestroy(g.exec); g.exec = nullptr; }
             cudaGraph_t graph = nullptr;
             e = cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal);
@@ -208,8 +207,7 @@ int grisBatchRender(GrisContext* ctx, GrisBatch* b, const GrisCamera* cams, cons
             if (e != cudaSuccess) return ctx_fail(ctx, GRIS_ERR_CUDA, std::string("graph capture: ") + cudaGetErrorString(e));
             g.pathForm = form; g.maxDepth = sh.maxDepth; g.pixels = sh.pixels; g.tiles = sh.tiles;
             g.trace = wl.traceBlocksPerSM; g.shade = wl.shadeBlocksPerSM; g.refill = wl.refill; g.countWork = ctx_count_work(ctx);
-            g.guide = b->guide; g.train = train;
-            g.pooled = wl.pooledVisibility; g.pairwise = sh.pairwise; g.poolNeighbors = sh.poolNeighbors;
+            g.guide = b->guide; g.train = train; g.pairwise = sh.pairwise;
         }
         e = cudaGraphLaunch(g.exec, st);
     } else {
@@ -297,7 +295,7 @@ int grisBatchAutotune(GrisContext* ctx, GrisBatch* b, const GrisCamera* cams, co
     int bestI = 0;
     int rc = GRIS_OK;
     for (size_t i = 0; i < cands.size() && i < 16 && rc == GRIS_OK; i++) {
-        WaveLaunch wl = savedWl;
+        WaveLaunch wl;
         wl.traceBlocksPerSM = cands[i].trace;
         wl.shadeBlocksPerSM = cands[i].shade;
         wl.refill = cands[i].refill;
@@ -316,7 +314,7 @@ int grisBatchAutotune(GrisContext* ctx, GrisBatch* b, const GrisCamera* cams, co
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
     if (rc != GRIS_OK) { ctx_set_tuning(ctx, savedForm, savedWl); return rc; }
-    WaveLaunch wl = savedWl;
+    WaveLaunch wl;
     wl.traceBlocksPerSM = cands[bestI].trace;
     wl.shadeBlocksPerSM = cands[bestI].shade;
     wl.refill = cands[bestI].refill;

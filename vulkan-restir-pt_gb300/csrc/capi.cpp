@@ -332,12 +332,6 @@ int grisSetWaveRefill(GrisContext* ctx, int enable) {
     return GRIS_OK;
 }
 
-int grisSetPooledVisibility(GrisContext* ctx, int enable) {
-    if (!ctx) return GRIS_ERR_INVALID_ARGUMENT;
-    ctx->waveLaunch.pooledVisibility = enable != 0;
-    return GRIS_OK;
-}
-
 int grisSetPathForm(GrisContext* ctx, int form) {
     if (!ctx || (form != GRIS_PATH_MEGAKERNEL && form != GRIS_PATH_WAVEFRONT)) return GRIS_ERR_INVALID_ARGUMENT;
     ctx->pathForm = form;
@@ -682,7 +676,7 @@ int grisPassDI(GrisContext* ctx, const GrisScene* s, const GrisDIBindings* b, co
     if (dev != ctx->device) return fail(ctx, GRIS_ERR_INVALID_ARGUMENT, "scene lives on another device");
     cudaSetDevice(ctx->device);
     GRIS_CK(ctx, grisrt::launch_di(view, *b, *cam, *prevCam, *set, passes & 7, ctx->dCounters, ctx->countWork,
-                                   &ctx->prof, ctx->stream, ctx->waveLaunch.pooledVisibility != 0));
+                                   &ctx->prof, ctx->stream));
     return GRIS_OK;
 }
 

@@ -166,11 +166,9 @@ GD void di_replay(const DICtx& P, DIResv& dst, const Surf& ds, const DIResv& src
 }
 
 /* reconnection (di_reservoir.glsl:211-287): the source's light vertex seen from the destination
- * (one visibility ray), Jacobian (|cos| / d^2)_dst / jacobian_src. pooled: -1 traces the
- * visibility ray here; 0 / 1 is its verdict walked ahead (warp_visibility), counted here.
- * Returns true when the merge drew its random number. */
-GD bool di_reconnect(const DICtx& P, DIResv& dst, const Surf& ds, DIResv src, V3 wo, uint32_t& rng, RayCount& rc,
-                     int& err, int pooled = -1) {
+ * (one visibility ray), Jacobian (|cos| / d^2)_dst / jacobian_src. */
+GD void di_reconnect(const DICtx& P, DIResv& dst, const Surf& ds, DIResv src, V3 wo, uint32_t& rng, RayCount& rc,
+                     int& err) {
     Mat mat = load_material(P.sc, ds.matIndex);
     DISample ss = src.s;
     Surf lv = surf_zero();
@@ -184,10 +182,7 @@ GD bool di_reconnect(const DICtx& P, DIResv& dst, const Surf& ds, DIResv src, V3
     float pHat = 0.0f, dstPdf = 0.0f;
     if (ss.isec.inst != kInvalidHit && dist > 1e-4f) {
         if (cosT > 0.0f && !isnan(jac) && ss.jac > 0.0f) {
-            bool visible;
-            if (pooled >= 0) { rc.shadow++; visible = pooled != 0; }
-            else visible = traceVisibility(P.sc, ds.pos, lv.pos, rc, err);
-            if (visible) {
+            if (traceVisibility(P.sc, ds.pos, lv.pos, rc, err)) {
                 ok = true;
                 if (!isnan(ss.pdf) && ss.pdf > 1e-6f) {
                     V3 Li = src.s.Li * evalBSDF(mat, ds.albedo, ds.norm, wo, wi) * satDot(ds.norm, wi) / ss.pdf;
@@ -208,9 +203,7 @@ GD bool di_reconnect(const DICtx& P, DIResv& dst, const Surf& ds, DIResv src, V3
     } else {
         src.W = 0.0f;
     }
-    bool drew = di_usable(src);
-    if (drew) di_merge(dst, src, sample1f(rng));
-    return drew;
+    if (di_usable(src)) di_merge(dst, src, sample1f(rng));
 }
 
 /* DIReservoirReuseAndMerge (di_reservoir.glsl:289-296) */
@@ -304,133 +297,67 @@ __global__ void __launch_bounds__(128) k_di_temporal(DICtx P) {
     flush_counts(P.counters, rc, err, 5, P.countWork);
 }
 
-/* findNeighborReservoir (di_spatial.glsl:9-34): the neighbour's reservoir when it passes the
- * gates (false: skipped, no merge). Draws the neighbour's position from rng. */
-GD bool di_neighbour(const DICtx& P, const DIPixel& px, uint32_t& rng, DIResv& src) {
-    const int W = (int)P.b.width, H = (int)P.b.height;
-    const float tx = 1.0f / (float)W, ty = 1.0f / (float)H;
-    V2 d = toConcentricDisk(sample2f(rng));
-    V2 nb = v2(px.uv.x + d.x * kDIRadius * tx, px.uv.y + d.y * kDIRadius * ty);
-    if (nb.x < 0.0f || nb.y < 0.0f || nb.x > 1.0f || nb.y > 1.0f) return false;
-    int qx = (int)(nb.x * (float)P.cam.w), qy = (int)(nb.y * (float)P.cam.h);
-    float ndepth = 0.0f; V3 nn = v3s(0.0f), nalb = v3s(0.0f); int nmm = 0;
-    float4 ndn = texture_bilinear(reinterpret_cast<const float4*>(P.b.depthNormal), W, H, nb);
-    uint2 nam = fetch_am(reinterpret_cast<const uint2*>(P.b.albedoMatId), W, H, qx, qy);
-    if (!unpackGBuffer(ndn, nam, ndepth, nn, nalb, nmm)) return false;
-    Ray3 nr = pinholeCameraSampleRay(P.cam, v2(nb.x, 1.0f - nb.y));
-    V3 npos = nr.ori + nr.dir * (ndepth - 1e-4f);
-    if (dot3(nn, px.surf.norm) < 0.9f || distance3(px.surf.pos, npos) > 0.4f) return false;
-    src = load_di(P.b.reservoirTemp, (uint64_t)((uint32_t)P.cam.w * (uint32_t)qy + (uint32_t)qx),
-                  (uint64_t)W * (uint64_t)H);
-    return true;
-}
-
-/* The spatial neighbour loop ahead of time on a copy of the random stream (reconnection shift):
- * every reconnection's visibility query goes into this lane's pool slot k. Every usable
- * neighbour's merge draws one number (a reconnection never leaves its weight NaN); the loop that
- * consumes the verdicts stops using them if that ever fails. Returns the posted mask. */
-GD uint32_t di_pool_prepare(const DICtx& P, const DIPixel& px, uint32_t rng, float (*seg)[6]) {
-    uint32_t posted = 0u;
-    for (uint32_t k = 0; k < kDINeighbours; k++) {
-        DIResv src = di_zero();
-        if (!di_neighbour(P, px, rng, src) || !di_usable(src)) continue;
-        if (src.s.isec.inst != kInvalidHit) {
-            Surf lv = surf_zero();
-            loadSurfaceInfo(P.sc, src.s.isec, lv);
-            float dist = distance3(lv.pos, px.surf.pos);
-            V3 wi = normalize3(lv.pos - px.surf.pos);
-            float cosT = -dot3(lv.norm, wi);
-            float jac = (fabsf(cosT) / square(dist)) / src.s.jac;
-            if (dist > 1e-4f && cosT > 0.0f && !isnan(jac) && src.s.jac > 0.0f) {
-                pool_post(seg[k], px.surf.pos, lv.pos);
-                posted |= 1u << k;
-            }
-        }
-        (void)sample1f(rng);   /* the merge's draw */
-    }
-    return posted;
-}
-
-/* spatialReuse (di_spatial.glsl:36-121) + the running mean of di_spatial.comp:21-26 (a background
- * pixel accumulates black). kPool: the warp's reconnection queries were walked ahead (posted /
- * vis masks over the neighbours). */
-template <bool kPool>
-GD void di_spatial_pixel(const DICtx& P, uint32_t x, uint32_t y, bool live, const DIPixel& px, uint32_t posted,
-                         uint32_t vis, RayCount& rc, int& err) {
-    if (x >= P.b.width || y >= P.b.height) return;
-    const int W = (int)P.b.width, H = (int)P.b.height;
-    const uint64_t n = (uint64_t)W * (uint64_t)H, idx = (uint64_t)y * W + x;
-    V3 color = v3s(0.0f);
-    if (live) {
-        uint32_t rng = makeSeed2(P.cam.seed, x, y) ^ 2u;
-        V3 wo = -px.ray.dir;
-        DIResv r = load_di(P.b.reservoirTemp, idx, n);
-        if (P.set.spatialReuse) {
-            bool poolLive = kPool;
-            for (uint32_t k = 0; k < kDINeighbours; k++) {
-                DIResv src = di_zero();
-                if (!di_neighbour(P, px, rng, src) || !di_usable(src)) continue;
-                if (kPool && P.set.shiftType == GRIS_DI_SHIFT_RECONNECTION) {
-                    int pooled = poolLive && ((posted >> k) & 1u) ? (int)((vis >> k) & 1u) : -1;
-                    if (!di_reconnect(P, r, px.surf, src, wo, rng, rc, err, pooled)) poolLive = false;
-                } else {
-                    di_reuse(P, r, px.surf, src, wo, rng, rc, err);
-                }
-            }
-            di_occlude(P, r, px.surf.pos, rc, err);
-        }
-        di_cap(r, kDICap);
-        if (!di_usable(r)) di_clear(r);
-        store_di(P.b.reservoirThis, idx, r);
-        if (di_usable(r) && r.s.isec.inst != kInvalidHit) {
-            Surf ls = surf_zero();
-            loadSurfaceInfo(P.sc, r.s.isec, ls);
-            V3 wi = normalize3(ls.pos - px.surf.pos);
-            if (r.M > 0u) {
-                Mat mat = load_material(P.sc, px.surf.matIndex);
-                V3 Li = r.s.Li * evalBSDF(mat, px.surf.albedo, px.surf.norm, wo, wi) * satDot(px.surf.norm, wi) / r.s.pdf;
-                if (!isBlack(Li)) color = Li / luminance(Li) * r.W / (float)r.M;
-            }
-        }
-        color = clampColor(color);
-    }
-    float frameCount = (float)(P.cam.frameIndex & kCameraFrameIndexMask);
-    float4* out = reinterpret_cast<float4*>(P.b.directOutput) + idx;
-    float4 o = *out;
-    V3 acc = (v3(o.x, o.y, o.z) * frameCount + color) / (frameCount + 1.0f);
-    *out = make_float4(acc.x, acc.y, acc.z, 1.0f);
-}
-
+/* findNeighborReservoir (di_spatial.glsl:9-34) + spatialReuse (:36-121) + the running mean of
+ * di_spatial.comp:21-26 (a background pixel accumulates black). */
 __global__ void __launch_bounds__(128) k_di_spatial(DICtx P) {
     RayCount rc = ray_count();
     int err = 0;
     uint32_t x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y * blockDim.y + threadIdx.y;
-    DIPixel px;
-    bool live = x < P.b.width && y < P.b.height && di_pixel(P, x, y, px);
-    di_spatial_pixel<false>(P, x, y, live, px, 0u, 0u, rc, err);
-    flush_counts(P.counters, rc, err, 6, P.countWork);
-}
-
-/* The spatial pass with the warp's reconnection queries walked as one pool first (reconnection
- * shift); same results and ray counts as k_di_spatial. */
-__global__ void __launch_bounds__(128) k_di_spatial_pool(DICtx P) {
-    __shared__ VisPool<kDINeighbours> pools[4];
-    RayCount rc = ray_count();
-    int err = 0;
-    uint32_t x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y * blockDim.y + threadIdx.y;
-    const uint32_t tid = threadIdx.y * blockDim.x + threadIdx.x, lane = tid & 31u;
-    VisPool<kDINeighbours>& pool = pools[tid >> 5];
-    DIPixel px;
-    bool live = x < P.b.width && y < P.b.height && di_pixel(P, x, y, px);
-    uint32_t posted = live ? di_pool_prepare(P, px, makeSeed2(P.cam.seed, x, y) ^ 2u, pool.seg + lane * kDINeighbours) : 0u;
-    uint32_t vis = warp_visibility<kDINeighbours>(pool, posted, P.sc.nodes, P.sc.tris, rc, err);
-    di_spatial_pixel<true>(P, x, y, live, px, posted, vis, rc, err);
+    if (x < P.b.width && y < P.b.height) {
+        const int W = (int)P.b.width, H = (int)P.b.height;
+        const uint64_t n = (uint64_t)W * (uint64_t)H, idx = (uint64_t)y * W + x;
+        V3 color = v3s(0.0f);
+        DIPixel px;
+        if (di_pixel(P, x, y, px)) {
+            uint32_t rng = makeSeed2(P.cam.seed, x, y) ^ 2u;
+            V3 wo = -px.ray.dir;
+            DIResv r = load_di(P.b.reservoirTemp, idx, n);
+            if (P.set.spatialReuse) {
+                float tx = 1.0f / (float)W, ty = 1.0f / (float)H;
+                for (uint32_t k = 0; k < kDINeighbours; k++) {
+                    V2 d = toConcentricDisk(sample2f(rng));
+                    V2 nb = v2(px.uv.x + d.x * kDIRadius * tx, px.uv.y + d.y * kDIRadius * ty);
+                    if (nb.x < 0.0f || nb.y < 0.0f || nb.x > 1.0f || nb.y > 1.0f) continue;
+                    int qx = (int)(nb.x * (float)P.cam.w), qy = (int)(nb.y * (float)P.cam.h);
+                    float ndepth = 0.0f; V3 nn = v3s(0.0f), nalb = v3s(0.0f); int nmm = 0;
+                    float4 ndn = texture_bilinear(reinterpret_cast<const float4*>(P.b.depthNormal), W, H, nb);
+                    uint2 nam = fetch_am(reinterpret_cast<const uint2*>(P.b.albedoMatId), W, H, qx, qy);
+                    if (!unpackGBuffer(ndn, nam, ndepth, nn, nalb, nmm)) continue;
+                    Ray3 nr = pinholeCameraSampleRay(P.cam, v2(nb.x, 1.0f - nb.y));
+                    V3 npos = nr.ori + nr.dir * (ndepth - 1e-4f);
+                    if (dot3(nn, px.surf.norm) < 0.9f || distance3(px.surf.pos, npos) > 0.4f) continue;
+                    DIResv src = load_di(P.b.reservoirTemp, (uint64_t)((uint32_t)P.cam.w * (uint32_t)qy + (uint32_t)qx), n);
+                    if (di_usable(src)) di_reuse(P, r, px.surf, src, wo, rng, rc, err);
+                }
+                di_occlude(P, r, px.surf.pos, rc, err);
+            }
+            di_cap(r, kDICap);
+            if (!di_usable(r)) di_clear(r);
+            store_di(P.b.reservoirThis, idx, r);
+            if (di_usable(r) && r.s.isec.inst != kInvalidHit) {
+                Surf ls = surf_zero();
+                loadSurfaceInfo(P.sc, r.s.isec, ls);
+                V3 wi = normalize3(ls.pos - px.surf.pos);
+                if (r.M > 0u) {
+                    Mat mat = load_material(P.sc, px.surf.matIndex);
+                    V3 Li = r.s.Li * evalBSDF(mat, px.surf.albedo, px.surf.norm, wo, wi) * satDot(px.surf.norm, wi) / r.s.pdf;
+                    if (!isBlack(Li)) color = Li / luminance(Li) * r.W / (float)r.M;
+                }
+            }
+            color = clampColor(color);
+        }
+        float frameCount = (float)(P.cam.frameIndex & kCameraFrameIndexMask);
+        float4* out = reinterpret_cast<float4*>(P.b.directOutput) + idx;
+        float4 o = *out;
+        V3 acc = (v3(o.x, o.y, o.z) * frameCount + color) / (frameCount + 1.0f);
+        *out = make_float4(acc.x, acc.y, acc.z, 1.0f);
+    }
     flush_counts(P.counters, rc, err, 6, P.countWork);
 }
 
 cudaError_t launch_di(const DeviceSceneView& scene, const GrisDIBindings& b, const GrisCamera& cam,
                       const GrisCamera& prevCam, const GrisDISettings& set, int passes, unsigned long long* counters,
-                      int countWork, KernelTimer* timer, cudaStream_t stream, bool pooled) {
+                      int countWork, KernelTimer* timer, cudaStream_t stream) {
     DICtx P;
     P.sc = to_dev(scene);
     P.cam = make_cam(cam);
@@ -452,8 +379,7 @@ cudaError_t launch_di(const DeviceSceneView& scene, const GrisDIBindings& b, con
     }
     if (passes & 4) {
         if (timer) timer->mark(GRIS_SLOT_DI_SPATIAL, true, stream);
-        if (pooled && set.spatialReuse && set.shiftType == GRIS_DI_SHIFT_RECONNECTION) k_di_spatial_pool<<<grid, block, 0, stream>>>(P);
-        else k_di_spatial<<<grid, block, 0, stream>>>(P);
+        k_di_spatial<<<grid, block, 0, stream>>>(P);
         if (timer) timer->mark(GRIS_SLOT_DI_SPATIAL, false, stream);
     }
     return cudaGetLastError();

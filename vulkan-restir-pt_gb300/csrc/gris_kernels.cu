@@ -507,12 +507,9 @@ GD Shift shiftToDomain(const PassCtx& P, const Surf& dstPrimarySurf, const Isec&
 /* GRISReservoirReuseAndMerge (:138-236): the shift (as shiftToDomain, written out here: this
  * form keeps the reuse kernels' register footprint), the source weight scaled by the ratio of
  * the targets, the merge (M adds up: the M-proportional weights of the reference), the M cap. */
-/* pooled: -1 traces the visibility ray here; 0 / 1 is its verdict, already walked (by
- * warp_visibility) and counted here. Returns true when the merge drew its random number (the
- * shifted reservoir was valid). */
-GD bool reuseAndMerge(const PassCtx& P, Resv& dstResv, const Surf& dstPrimarySurf, const Isec& dstPrimaryIsec,
+GD void reuseAndMerge(const PassCtx& P, Resv& dstResv, const Surf& dstPrimarySurf, const Isec& dstPrimaryIsec,
                       const Ray3& primaryRay, Resv srcResv, uint32_t& rng, RayCount& rc, int& err,
-                      const guide::Lobes* L = nullptr, int pooled = -1) {
+                      const guide::Lobes* L = nullptr) {
     const DevScene& sc = P.sc;
     PathSample srcSample = srcResv.s;
     RcData dstRcData;
@@ -540,10 +537,7 @@ GD bool reuseAndMerge(const PassCtx& P, Resv& dstResv, const Surf& dstPrimarySur
             jacobian = dstJacobian / srcSample.rcJacobian;
             if (dist > kDistanceThreshold && cosTheta > 0.0f && !isnan(jacobian) && srcSample.rcJacobian > 0.0f &&
                 isBSDFConnectible(rcPrevMat)) {
-                bool visible;
-                if (pooled >= 0) { rc.shadow++; visible = pooled != 0; }
-                else visible = traceVisibility(sc, rcPrevSurf.pos, rcSurf.pos, rc, err);
-                if (visible) srcSampleValid = true;
+                if (traceVisibility(sc, rcPrevSurf.pos, rcSurf.pos, rc, err)) srcSampleValid = true;
             }
         }
     }
@@ -578,10 +572,8 @@ GD bool reuseAndMerge(const PassCtx& P, Resv& dstResv, const Surf& dstPrimarySur
     } else {
         srcResv.resampleWeight = 0.0f;
     }
-    bool drew = resvIsValid(srcResv);
-    if (drew) resvMerge(dstResv, srcResv, sample1f(rng));
+    if (resvIsValid(srcResv)) resvMerge(dstResv, srcResv, sample1f(rng));
     resvCap(dstResv, (float)P.set.cap);
-    return drew;
 }
 
 /* Pairwise generalised balance heuristic (GrisSettings.misWeights = 1). The canonical reservoir
@@ -761,57 +753,6 @@ struct SpatialTaskT {
     Surf dst;
     Isec dstIsec;
     Ray3 ray;
-    /* warp-pooled visibility (k_batch_spatial_pool): the neighbours whose queries were walked
-     * ahead (bit k), their verdicts, and whether the pooled pass's random numbers still match */
-    uint32_t poolPosted = 0u, poolVis = 0u;
-    bool poolLive = false;
-
-    /* The neighbour loop of step() ahead of time, on a copy of the random stream: the
-     * visibility query of every shift that reconnects at the destination's primary vertex
-     * (rcVertexId 1: no replay) goes into this lane's pool slot k for neighbour k. It assumes
-     * that every shift of a valid neighbour ends in a merge that draws a number; step() stops
-     * using the pooled verdicts at the first shift where that does not hold. Reference merge,
-     * unguided. Returns the posted mask. */
-    template <int kMax>
-    GD uint32_t pool_prepare(const PassCtx& P, float (*seg)[6]) {
-        const DevScene& sc = P.sc;
-        const int W = (int)P.b.width, H = (int)P.b.height;
-        const uint64_t n = (uint64_t)W * (uint64_t)H;
-        uint32_t r = rng, posted = 0u;
-        const float tx = 1.0f / (float)W, ty = 1.0f / (float)H;
-        const V2 uv = v2(dstIsec.bx, dstIsec.by);
-        const bool dstConn = isBSDFConnectible(load_material(sc, dst.matIndex));
-        for (uint32_t k = 0; k < P.set.spatialNeighbors && k < (uint32_t)kMax; k++) {
-            V2 d = toConcentricDisk(sample2f(r));
-            V2 nb = v2(uv.x + d.x * P.set.spatialRadius * tx, uv.y + d.y * P.set.spatialRadius * ty);
-            if (nb.x < 0.0f || nb.y < 0.0f || nb.x > 1.0f || nb.y > 1.0f) continue;
-            int px = (int)(nb.x * (float)P.cam.w), py = (int)(nb.y * (float)P.cam.h);
-            float depthN = 0.0f; V3 normalN = v3s(0.0f), albedoN = v3s(0.0f); int matMeshIdN = 0;
-            float4 ndn = texture_bilinear(reinterpret_cast<const float4*>(P.b.depthNormal), W, H, nb);
-            uint2 nam = fetch_am(reinterpret_cast<const uint2*>(P.b.albedoMatId), W, H, px, py);
-            if (!unpackGBuffer(ndn, nam, depthN, normalN, albedoN, matMeshIdN)) continue;
-            Ray3 nray = pinholeCameraSampleRay(P.cam, v2(nb.x, 1.0f - nb.y));
-            V3 posN = nray.ori + nray.dir * (depthN - 1e-4f);
-            if (dot3(normalN, dst.norm) < 0.9f || distance3(dst.pos, posN) > 0.4f) continue;
-            Resv src = load_resv(P.b.reservoirTemp, (uint32_t)P.cam.w * (uint32_t)py + (uint32_t)px, n);
-            if (!resvIsValid(src)) continue;
-            const PathSample& ps = src.s;
-            if (dstConn && ps.rcIsec.inst != kInvalidHit && rcVertexId(ps.flags) == 1u) {
-                Surf rcSurf = surf_zero();
-                loadSurfaceInfo(sc, ps.rcIsec, rcSurf);
-                float dist = distance3(dst.pos, rcSurf.pos);
-                V3 wi = normalize3(rcSurf.pos - dst.pos);
-                float cosTheta = -dot3(rcSurf.norm, wi);
-                float jacobian = (fabsf(cosTheta) / square(dist)) / ps.rcJacobian;
-                if (dist > kDistanceThreshold && cosTheta > 0.0f && !isnan(jacobian) && ps.rcJacobian > 0.0f) {
-                    pool_post(seg[k], dst.pos, rcSurf.pos);
-                    posted |= 1u << k;
-                }
-            }
-            (void)sample1f(r);   /* the merge's draw */
-        }
-        return posted;
-    }
 
     GD static void accumulate(const PassCtx& P, uint32_t x, uint32_t y, V3 color) {
         float frameCount = (float)(P.cam.frameIndex & kCameraFrameIndexMask);
@@ -898,9 +839,7 @@ struct SpatialTaskT {
                 if constexpr (kGuide) {
                     if (primary_lobes(P, idx, load_material(sc, dst.matIndex), L)) Lp = &L;
                 }
-                const uint32_t k = i - 1u;
-                int pooled = poolLive && ((poolPosted >> k) & 1u) ? (int)((poolVis >> k) & 1u) : -1;
-                if (!reuseAndMerge(P, resv, dst, dstIsec, ray, neighborResv, rng, rc, err, Lp, pooled)) poolLive = false;
+                reuseAndMerge(P, resv, dst, dstIsec, ray, neighborResv, rng, rc, err, Lp);
             }
             return true;
         }
@@ -1391,34 +1330,6 @@ __global__ void __launch_bounds__(128, GridMinBlocks<KERNEL>::value) k_batch_pas
             while (task.step(P, rc, err)) {}
     }
     flush_counts(P.counters, rc, err, KERNEL, P.countWork);
-}
-
-/* The spatial pass with warp-pooled visibility (reference merge, unguided, at most kMax
- * neighbours): each lane prepares its neighbours' reconnection queries, the warp walks them all
- * (warp_visibility), then each lane runs the ordinary neighbour loop with the verdicts. Results
- * and ray counts are those of k_batch_pass<SpatialTask, 3>. */
-template <int kMax>
-__global__ void __launch_bounds__(128, GridMinBlocks<3>::value) k_batch_spatial_pool(const ViewEntry* __restrict__ V, int n) {
-    __shared__ VisPool<kMax> pools[4];
-    int v = find_view_by_tile(V, n, blockIdx.x);
-    const PassCtx& P = V[v].P;
-    uint32_t t = blockIdx.x - V[v].tileBase;
-    uint32_t x = (t % V[v].tilesX) * 16u + threadIdx.x, y = (t / V[v].tilesX) * 8u + threadIdx.y;
-    VisPool<kMax>& pool = pools[(threadIdx.y * 16u + threadIdx.x) >> 5];
-    const uint32_t lane = (threadIdx.y * 16u + threadIdx.x) & 31u;
-    RayCount rc = ray_count();
-    int err = 0;
-    SpatialTask task;
-    bool live = x < P.b.width && y < P.b.height && task.begin(P, x, y, rc, err);
-    uint32_t posted = live ? task.template pool_prepare<kMax>(P, pool.seg + lane * kMax) : 0u;
-    uint32_t vis = warp_visibility<kMax>(pool, posted, P.sc.nodes, P.sc.tris, rc, err);
-    if (live) {
-        task.poolPosted = posted;
-        task.poolVis = vis;
-        task.poolLive = true;
-        while (task.step(P, rc, err)) {}
-    }
-    flush_counts(P.counters, rc, err, 3, P.countWork);
 }
 
 /* ------------------------------------------------------------------ wavefront path tracer */
@@ -2014,7 +1925,6 @@ BatchShape fill_view_table(const BatchView* views, int n, void* hViews, unsigned
         sh.pixels += bv.b.width * bv.b.height;
         if ((int)bv.set.maxDepth > sh.maxDepth) sh.maxDepth = (int)bv.set.maxDepth;
         if (bv.set.misWeights) sh.pairwise = true;
-        if (bv.set.spatialReuse && bv.set.spatialNeighbors > sh.poolNeighbors) sh.poolNeighbors = bv.set.spatialNeighbors;
     }
     return sh;
 }
@@ -2143,7 +2053,6 @@ reuse:
         if (guide && sh.pairwise) k_batch_pass<SpatialTaskT<true, true>, 3><<<tiles, blk, 0, stream>>>(V, n);
         else if (guide) k_batch_pass<SpatialTaskT<true>, 3><<<tiles, blk, 0, stream>>>(V, n);
         else if (sh.pairwise) k_batch_pass<SpatialTaskT<false, true>, 3><<<tiles, blk, 0, stream>>>(V, n);
-        else if (wl.pooledVisibility && sh.poolNeighbors <= 4) k_batch_spatial_pool<4><<<tiles, blk, 0, stream>>>(V, n);
         else k_batch_pass<SpatialTask, 3><<<tiles, blk, 0, stream>>>(V, n);
         if (timer) timer->mark(3, false, stream);
     }

@@ -41,7 +41,7 @@ cudaError_t launch_gris(const DeviceSceneView& scene, const GrisPassBindings& b,
 /* ReSTIR DI (TestReSTIR::render): passes bit 0 candidates, bit 1 temporal, bit 2 spatial */
 cudaError_t launch_di(const DeviceSceneView& scene, const GrisDIBindings& b, const GrisCamera& cam,
                       const GrisCamera& prevCam, const GrisDISettings& set, int passes, unsigned long long* counters,
-                      int countWork, KernelTimer* timer, cudaStream_t stream, bool pooled = true);
+                      int countWork, KernelTimer* timer, cudaStream_t stream);
 /* presentation pass (post_proc.frag): composition, tone mapping, gamma, UNORM8 */
 cudaError_t launch_post(const GrisPostBindings& b, const GrisPostSettings& set, cudaStream_t stream);
 /* converged image: FP64 sums of independent paths per pixel; relMSE / MSE reduction */
@@ -91,7 +91,6 @@ struct WaveLaunch {
     int traceBlocksPerSM = 16;
     int shadeBlocksPerSM = 8;
     int refill = 0;   /* 1: the resident traversal kernels (lanes take new rays while others walk) */
-    int pooledVisibility = 1;   /* 1: the spatial pass walks its warps' visibility queries as one pool */
 };
 
 struct BatchShape {
@@ -99,7 +98,6 @@ struct BatchShape {
     uint32_t tiles, pixels;
     int maxDepth;
     bool pairwise = false;   /* some view uses the pairwise MIS weights */
-    uint32_t poolNeighbors = 0;   /* the largest spatial neighbour count of a view with spatial reuse */
 };
 
 /* Writes the view table of a frame into hViews (pinned host memory). */

@@ -54,7 +54,11 @@ __global__ void __launch_bounds__(256) k_post(PostCtx P) {
         const float e = 1.0f / 2.2f;
         r = gris_det_powf(r, e); g = gris_det_powf(g, e); bl = gris_det_powf(bl, e);
     }
-    if (P.b.color) reinterpret_cast<float4*>(P.b.color)[dst] = make_float4(r, g, bl, 1.0f);
+    if (P.b.color) {   /* a NaN channel is written as the canonical quiet NaN 0x7fc00000 */
+        const float qnan = __uint_as_float(0x7fc00000u);
+        reinterpret_cast<float4*>(P.b.color)[dst] = make_float4(isnan(r) ? qnan : r, isnan(g) ? qnan : g,
+                                                                isnan(bl) ? qnan : bl, 1.0f);
+    }
     if (P.b.rgba8)
         reinterpret_cast<uint32_t*>(P.b.rgba8)[dst] = unorm8(r) | (unorm8(g) << 8) | (unorm8(bl) << 16) | (255u << 24);
 }

@@ -90,75 +90,6 @@ GD void flush_counts(unsigned long long* counters, const RayCount& rc, int err, 
     }
 }
 
-/* ------------------------------------------------------------------ warp-pooled visibility */
-/* Visibility queries (traceVisibility semantics) posted by the lanes of one warp and walked by
- * the whole warp: lane l posts its query for neighbour k in slot l * kMax + k; the warp walks
- * every posted slot with the resumable walker, a lane taking the next unwalked slot as soon as
- * its current walk is over, so a lane whose queries are short works on the others' while they
- * are still walking. The verdict of a query does not depend on which lane walks it. */
-template <int kMax>
-struct VisPool {
-    float seg[32 * kMax][6];          /* from xyz, to xyz */
-    uint16_t order[32 * kMax];        /* the posted slots, lane by lane */
-    unsigned char vis[32 * kMax];     /* 1: unoccluded */
-};
-
-GD void pool_post(float* seg, V3 from, V3 to) {
-    seg[0] = from.x; seg[1] = from.y; seg[2] = from.z; seg[3] = to.x; seg[4] = to.y; seg[5] = to.z;
-}
-
-/* Called by all 32 lanes of a converged warp. posted: this lane's bit mask over k of the slots it
- * filled. Returns this lane's verdicts as a bit mask over k. Adds the walks' traversal work to the
- * walking lane's counts; the queries themselves are counted where their verdicts are used. */
-template <int kMax>
-GD uint32_t warp_visibility(VisPool<kMax>& pool, uint32_t posted, const uint32_t* __restrict__ nodes,
-                            const float* __restrict__ tris, RayCount& rc, int& err) {
-    const uint32_t lane = (threadIdx.x + threadIdx.y * blockDim.x) & 31u;
-    uint32_t cnt = (uint32_t)__popc(posted), off = cnt;
-    for (int d = 1; d < 32; d <<= 1) {
-        uint32_t v = __shfl_up_sync(0xffffffffu, off, d);
-        if (lane >= (uint32_t)d) off += v;
-    }
-    const uint32_t total = __shfl_sync(0xffffffffu, off, 31);
-    off -= cnt;   /* exclusive prefix */
-    for (uint32_t m = posted, j = off; m; m &= m - 1u, j++)
-        pool.order[j] = (uint16_t)(lane * kMax + (uint32_t)(__ffs(m) - 1));
-    __syncwarp();
-    GrisTraversal<true> tr;
-    uint32_t stackBase[GRIS_BVH_STACK], stackBits[GRIS_BVH_STACK];
-    uint32_t next = 0, slot = 0;
-    bool active = false;
-    while (true) {
-        unsigned idle = __ballot_sync(0xffffffffu, !active);
-        if (idle && next < total) {
-            uint32_t rank = (uint32_t)__popc(idle & ((1u << lane) - 1u));
-            if (!active && next + rank < total) {
-                slot = pool.order[next + rank];
-                const float* s = pool.seg[slot];
-                V3 from = v3(s[0], s[1], s[2]), to = v3(s[3], s[4], s[5]);
-                V3 d = normalize3(to - from);
-                tr.init(from.x, from.y, from.z, d.x, d.y, d.z, kMinRayDistance, distance3(to, from) - kMinRayDistance);
-                active = true;
-            }
-            next += (uint32_t)__popc(idle);
-        }
-        if (__ballot_sync(0xffffffffu, active) == 0u) break;
-        if (active && !tr.step(nodes, tris, false, &err, stackBase, stackBits)) {
-            GrisRayHit h;
-            tr.result(&h, &rc.work);
-            pool.vis[slot] = tr.found ? 0 : 1;
-            active = false;
-        }
-    }
-    __syncwarp();
-    uint32_t vis = 0;
-    for (uint32_t m = posted; m; m &= m - 1u) {
-        uint32_t k = (uint32_t)(__ffs(m) - 1);
-        if (pool.vis[lane * kMax + k]) vis |= 1u << k;
-    }
-    return vis;
-}
-
 /* ------------------------------------------------------------------ kernel arguments */
 inline CamD make_cam(const GrisCamera& c) {
     CamD d;

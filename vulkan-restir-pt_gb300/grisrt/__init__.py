@@ -214,7 +214,7 @@ EXPORTS = [
     "grisGuideCreate", "grisGuideDestroy", "grisGuideParamCount", "grisGuideSetParams", "grisGuideGetParams",
     "grisGuideSetTraining", "grisGuideForward", "grisGuideGradient", "grisGuideTrainStep", "grisBatchSetGuide",
     "grisHostSceneLoad", "grisHostSceneFilmSize", "grisSetWaveRefill", "grisPassDI", "grisFrameRenderDI",
-    "grisPostProcess", "grisWritePNG", "grisSetPooledVisibility",
+    "grisPostProcess", "grisWritePNG",
 ]
 
 _lib = None
@@ -293,7 +293,6 @@ def load(path=None):
         "grisReadKernelProfile": (i32, [vp, ctypes.POINTER(KernelProfile), i32]),
         "grisSetWaveLaunch": (i32, [vp, i32, i32]),
         "grisSetWaveRefill": (i32, [vp, i32]),
-        "grisSetPooledVisibility": (i32, [vp, i32]),
         "grisPassDI": (i32, [vp, vp, ctypes.POINTER(DIBindings), ctypes.POINTER(Camera), ctypes.POINTER(Camera),
                              ctypes.POINTER(DISettings), i32]),
         "grisFrameRenderDI": (i32, [vp, vp, vp, ctypes.POINTER(Camera), ctypes.POINTER(Camera), ctypes.POINTER(Settings),
@@ -518,9 +517,6 @@ class Context:
 
     def set_wave_refill(self, enable):
         self.check(load().grisSetWaveRefill(self.h, int(enable)), "grisSetWaveRefill")
-
-    def set_pooled_visibility(self, enable):
-        self.check(load().grisSetPooledVisibility(self.h, int(enable)), "grisSetPooledVisibility")
 
     def set_work_counting(self, enable):
         self.check(load().grisSetWorkCounting(self.h, int(enable)), "grisSetWorkCounting")
