@@ -136,7 +136,7 @@ typedef struct GrisSettings {
     uint32_t maxDepth;          /* MaxTracingDepth, gris_path_trace.glsl:46 (15) */
     uint32_t spatialNeighbors;  /* ResampleNum, gris_resample_spatial.glsl:65 (3) */
     float spatialRadius;        /* ResampleRadius in pixels, gris_resample_spatial.glsl:66 (20) */
-    float envRadiance[3];       /* extension: constant environment (0 = the reference: a miss ends the path) */
+    float envRadiance[3];       /* reserved, must be 0 (a miss ends the path, as in the reference) */
     uint32_t misWeights;        /* extension: 0 = the reference's merge (M-proportional weights); 1 = pairwise
                                    generalised balance heuristic (each reused sample and the canonical one are
                                    weighed against each other through shifts in both directions) */

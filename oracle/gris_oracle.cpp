@@ -78,7 +78,11 @@ struct PathSample {
     float pad[2]; float rcPrevSamplePdf, rcJacobian; float F[3]; uint32_t primaryRng;
 };
 struct Reservoir { PathSample s; float M, W, contribWeight, pad0; };
-struct Settings { uint32_t shift; float rrScale; uint32_t temporal, spatial, cap, maxDepth, neighbours; float radius; };
+struct Settings {
+    uint32_t shift; float rrScale; uint32_t temporal, spatial, cap, maxDepth, neighbours; float radius;
+    float envReserved[3];   /* must be 0 */
+    uint32_t misWeights;    /* extension: 1 = pairwise generalised balance heuristic in the reuse passes */
+};
 static_assert(sizeof(Camera) == 352 && sizeof(Reservoir) == 96 && sizeof(Instance) == 224, "layouts");
 
 static inline F3 ld3(const float* p) { return F3(p[0], p[1], p[2]); }
@@ -611,10 +615,11 @@ static inline bool visible(const F3& a, const F3& b) {         /* traceVisibilit
     return !traceQuery(a, unit(b - a), RAY_TMIN, len(b - a) - RAY_TMIN, true, false, nullptr, nullptr);
 }
 
-/* GRISReservoirReuseAndMerge (gris_retrace.glsl:138-236) */
-static void shiftAndMerge(const Pass& P, Reservoir& dst, const Surface& dstSurf, const Hit& dstHit, const Ray& primary,
-                          Reservoir src, uint32_t& rng) {
-    PathSample ps = src.s;
+/* The shift of the hybrid mapping (gris_retrace.glsl:138-224): replay of the source's prefix from
+ * the destination's primary vertex, reconnection with one visibility ray, and the shifted sample
+ * (its F, Jacobian and pdf at the destination). srcPHat: the target of the unshifted sample. */
+struct Shifted { bool valid; float dstPHat, srcPHat; PathSample out; };
+static Shifted shiftSample(const Pass& P, const Surface& dstSurf, const Hit& dstHit, const Ray& primary, PathSample ps) {
     Replay rd; memset(&rd, 0, sizeof(rd));
     Surface prevS; memset(&prevS, 0, sizeof(prevS));
     Surface rcS; memset(&rcS, 0, sizeof(rcS));
@@ -638,6 +643,10 @@ static void shiftAndMerge(const Pass& P, Reservoir& dst, const Surface& dstSurf,
                 ok = visible(prevS.p, rcS.p);
         }
     }
+    Shifted r;
+    r.valid = ok;
+    r.dstPHat = 0.0f;
+    r.srcPHat = lum(ld3(ps.F));
     if (ok) {
         uint32_t type = rcType(ps.flags);
         if (!std::isnan(ps.rcPrevSamplePdf) && ps.rcPrevSamplePdf > 1e-6f) {
@@ -650,13 +659,26 @@ static void shiftAndMerge(const Pass& P, Reservoir& dst, const Surface& dstSurf,
             if (!(lum(Li) < 1e-5f) && !anyNan(Li)) pHat = lum(Li * jac);
             if (type == 0u) dstPdf = lum(rcS.albedo) / at(g.table, 0).prob / dstJac;
             else dstPdf = bsdfPdf(prevMat, prevS.n, rd.prevWo, wi);
+        } else {
+            Li = F3(0.0f);
         }
-        float srcPHat = lum(ld3(ps.F));
         ps.rcJacobian = dstJac;
         ps.rcPrevSamplePdf = (dstPdf < 1e-6f || std::isnan(dstPdf)) ? 0.0f : dstPdf;
         st3(ps.F, Li);
-        src.s = ps;
-        src.W *= pHat / srcPHat;
+        r.dstPHat = pHat;
+    }
+    r.out = ps;
+    return r;
+}
+
+/* GRISReservoirReuseAndMerge (gris_retrace.glsl:138-236): the shift, the source weight scaled by
+ * the ratio of the targets, the merge (M adds up), the M cap. */
+static void shiftAndMerge(const Pass& P, Reservoir& dst, const Surface& dstSurf, const Hit& dstHit, const Ray& primary,
+                          Reservoir src, uint32_t& rng) {
+    Shifted sh = shiftSample(P, dstSurf, dstHit, primary, src.s);
+    if (sh.valid) {
+        src.s = sh.out;
+        src.W *= sh.dstPHat / sh.srcPHat;
     } else {
         src.W = 0.0f;
     }
@@ -669,6 +691,50 @@ static void shiftAndMerge(const Pass& P, Reservoir& dst, const Surface& dstSurf,
     float cap = (float)P.set.cap;
     if (dst.M > cap) { dst.W *= cap / dst.M; dst.M = cap; }
 }
+
+/* Pairwise generalised balance heuristic (GrisSettings.misWeights = 1, an extension of the
+ * reference): the canonical reservoir c and k reused reservoirs i; pair i weighs technique i
+ * against a 1/k share of the canonical one, m_i(y) = M_i p_i(y) / (M_i p_i(y) + (M_c / k) p_c(y)),
+ * with p_i the target of y shifted into i's pixel times that shift's Jacobian. A reused sample's
+ * weight comes from its forward shift; the canonical sample's from the backward shift of it into
+ * every reused pixel (pBack). The merged reservoir keeps the reference's representation
+ * (resampleWeight = sum w * M, M = sum of the Ms). */
+struct Pairwise {
+    float Mc, pc, Rc, k, mcSum, wSum, M;
+    PathSample canon, sel;
+    void begin(const Reservoir& c, float kk) {
+        Mc = c.M; pc = lum(ld3(c.s.F)); Rc = c.W; k = kk;
+        mcSum = 0.0f; wSum = 0.0f; M = Mc;
+        canon = c.s; sel = c.s;
+    }
+    void add(const Reservoir& src, const Shifted& fw, float pBack, float u) {
+        const float Mi = src.M;
+        if (pc > 0.0f) {
+            float a = (Mc / k) * pc, b = Mi * pBack;
+            mcSum += a / (a + b);
+        }
+        float w = 0.0f;
+        if (fw.valid && fw.dstPHat > 0.0f && fw.srcPHat > 0.0f && Mi > 0.0f)
+            w = (1.0f / k) * fw.dstPHat * src.W / (Mi * fw.srcPHat + (Mc / k) * fw.dstPHat);
+        if (!(w >= 0.0f) || std::isinf(w)) w = 0.0f;
+        wSum += w;
+        if (u * wSum < w) sel = fw.out;
+        M += Mi;
+    }
+    void skip() { if (pc > 0.0f) mcSum += 1.0f; }
+    Reservoir finish(float u, float cap) {
+        float wc = (pc > 0.0f && Mc > 0.0f) ? (mcSum / k) * Rc / Mc : 0.0f;
+        if (!(wc >= 0.0f) || std::isinf(wc)) wc = 0.0f;
+        float total = wSum + wc;
+        Reservoir out; memset(&out, 0, sizeof(out));
+        clearResv(out);
+        out.s = (u * total < wc) ? canon : sel;
+        out.M = M;
+        out.W = total * M;
+        if (out.M > cap) { out.W *= cap / out.M; out.M = cap; }
+        return out;
+    }
+};
 
 /* ------------------------------------------------------------------ passes */
 static inline F2 pixelUV(int x, int y, int W, int H) { return F2{((float)x + 0.5f) / (float)W, ((float)y + 0.5f) / (float)H}; }
@@ -841,7 +907,25 @@ static void temporalPixel(Pass& P, int x, int y) {
                 F3 ppos = pr.o + pr.d * (pdepth - 1e-4f);
                 if (!(pmm != matMesh || dot(pn, nrm) < 0.95f || len(pos - ppos) > 0.5f)) {
                     Reservoir src = readResv(P.previous, (uint64_t)(P.cam.film[0] * (uint32_t)py + (uint32_t)px), P.n);
-                    if (usable(src)) shiftAndMerge(P, r, ds, primary, ray, src, resvRng);
+                    if (usable(src) && P.set.misWeights) {
+                        /* pairwise: the backward shift of the canonical sample into the previous pixel */
+                        Surface ps; ps.p = ppos; ps.n = pn; ps.albedo = palb; ps.mat = (uint32_t)(pmm >> 16); ps.light = false;
+                        Hit ph; ph.bx = puv.x; ph.by = puv.y; ph.inst = PRIMARY_HIT; ph.tri = 0;
+                        Pairwise pw;
+                        pw.begin(r, 1.0f);
+                        Shifted fw = shiftSample(P, ds, primary, ray, src.s);
+                        float pBack = 0.0f;
+                        if (pw.pc > 0.0f) {
+                            Shifted bw = shiftSample(P, ps, ph, pr, r.s);
+                            if (bw.valid) pBack = bw.dstPHat;
+                        }
+                        float u0 = rnd(resvRng);
+                        pw.add(src, fw, pBack, u0);
+                        float u1 = rnd(resvRng);
+                        r = pw.finish(u1, (float)P.set.cap);
+                    } else if (usable(src)) {
+                        shiftAndMerge(P, r, ds, primary, ray, src, resvRng);
+                    }
                 }
             }
         }
@@ -866,24 +950,41 @@ static F3 spatialPixel(Pass& P, int x, int y) {
     Hit primary; primary.bx = uv.x; primary.by = uv.y; primary.inst = PRIMARY_HIT; primary.tri = 0;
     Surface ds; ds.p = pos; ds.n = nrm; ds.albedo = alb; ds.mat = (uint32_t)(matMesh >> 16); ds.light = false;
     if (P.set.spatial) {
+        const bool pairwise = P.set.misWeights != 0u && P.set.neighbours > 0u;
+        Pairwise pw;
+        if (pairwise) pw.begin(r, (float)P.set.neighbours);
         float tx = 1.0f / (float)P.W, ty = 1.0f / (float)P.H;
         for (uint32_t k = 0; k < P.set.neighbours; k++) {
             float r0 = rnd(rng), r1 = rnd(rng);
             F2 d = concentric(F2{r0, r1});
             F2 nb{uv.x + d.x * P.set.radius * tx, uv.y + d.y * P.set.radius * ty};
-            if (nb.x < 0.0f || nb.y < 0.0f || nb.x > 1.0f || nb.y > 1.0f) continue;
+            if (nb.x < 0.0f || nb.y < 0.0f || nb.x > 1.0f || nb.y > 1.0f) { if (pairwise) pw.skip(); continue; }
             int px = (int)(nb.x * (float)P.cam.film[0]), py = (int)(nb.y * (float)P.cam.film[1]);
             float ndn[4]; uint32_t nam[2];
             sampleDN(P.cur, nb, ndn);
             fetchAM(P.cur, px, py, nam);
             float ndepth; F3 nn, nalb; int nmm;
-            if (!decodeGBuffer(ndn, nam, ndepth, nn, nalb, nmm)) continue;
+            if (!decodeGBuffer(ndn, nam, ndepth, nn, nalb, nmm)) { if (pairwise) pw.skip(); continue; }
             Ray nr = cameraRay(P.cam, F2{nb.x, 1.0f - nb.y});
             F3 npos = nr.o + nr.d * (ndepth - 1e-4f);
-            if (dot(nn, nrm) < 0.9f || len(pos - npos) > 0.4f) continue;
+            if (dot(nn, nrm) < 0.9f || len(pos - npos) > 0.4f) { if (pairwise) pw.skip(); continue; }
             Reservoir src = readResv(P.temp, (uint64_t)(P.cam.film[0] * (uint32_t)py + (uint32_t)px), P.n);
+            if (pairwise) {
+                if (!usable(src)) { pw.skip(); continue; }
+                Surface ns; ns.p = npos; ns.n = nn; ns.albedo = nalb; ns.mat = (uint32_t)(nmm >> 16); ns.light = false;
+                Hit nh; nh.bx = nb.x; nh.by = nb.y; nh.inst = PRIMARY_HIT; nh.tri = 0;
+                Shifted fw = shiftSample(P, ds, primary, ray, src.s);
+                float pBack = 0.0f;
+                if (pw.pc > 0.0f) {
+                    Shifted bw = shiftSample(P, ns, nh, nr, pw.canon);
+                    if (bw.valid) pBack = bw.dstPHat;
+                }
+                pw.add(src, fw, pBack, rnd(rng));
+                continue;
+            }
             if (usable(src)) shiftAndMerge(P, r, ds, primary, ray, src, rng);
         }
+        if (pairwise) r = pw.finish(rnd(rng), (float)P.set.cap);
     }
     if (!usable(r)) clearResv(r);
     P.self[i] = r;

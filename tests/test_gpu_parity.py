@@ -84,6 +84,23 @@ def test_gpu_matches_oracle_bit_exact(case, mode, ctx, ora):
     assert gc[3] == 0
 
 
+PAIRWISE_CASES = [
+    ("box_pairwise", 0, 0, 0, 48, 40, 5, dict(maxDepth=4, spatialRadius=30.0, misWeights=1)),
+    ("terrain_pairwise", 1, 48, 60, 48, 40, 4, dict(maxDepth=8, misWeights=1)),
+    ("glossy_pairwise_5nb", 2, 48, 60, 40, 32, 3, dict(maxDepth=8, spatialNeighbors=5, misWeights=1)),
+    ("terrain_pairwise_no_temporal", 1, 32, 20, 37, 23, 3, dict(maxDepth=6, temporalReuse=False, misWeights=1)),
+    ("box_pairwise_no_spatial", 0, 0, 0, 32, 24, 4, dict(maxDepth=4, spatialReuse=False, misWeights=1)),
+]
+
+
+@pytest.mark.parametrize("mode", MODES, ids=["wavefront", "megakernel-grid", "megakernel-persistent"])
+@pytest.mark.parametrize("case", PAIRWISE_CASES, ids=[c[0] for c in PAIRWISE_CASES])
+def test_gpu_pairwise_weights_match_oracle(case, mode, ctx, ora):
+    """The pairwise MIS weights (GrisSettings.misWeights = 1, an extension with no counterpart in
+    the reference): the CUDA reuse passes against the oracle's restatement, bit for bit."""
+    test_gpu_matches_oracle_bit_exact(case, mode, ctx, ora)
+
+
 def test_device_traversal_matches_host(ctx):
     hs = G.HostScene(1, seed=4, grid=64, spheres=100)
     scene = G.Scene(ctx, hs)

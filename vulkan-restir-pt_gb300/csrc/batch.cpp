@@ -155,7 +155,8 @@ int grisBatchRender(GrisContext* ctx, GrisBatch* b, const GrisCamera* cams, cons
     for (uint32_t i = 0; i < b->n; i++) {
         if (cams[i].filmSize[0] != b->w[i] || cams[i].filmSize[1] != b->h[i])
             return ctx_fail(ctx, GRIS_ERR_INVALID_ARGUMENT, "view " + std::to_string(i) + ": camera filmSize differs from the view size");
-        if (settings[i].maxDepth == 0 || settings[i].maxDepth > 255 || settings[i].spatialNeighbors > 64)
+        if (settings[i].maxDepth == 0 || settings[i].maxDepth > 255 || settings[i].spatialNeighbors > 64 ||
+            settings[i].envRadiance[0] != 0.0f || settings[i].envRadiance[1] != 0.0f || settings[i].envRadiance[2] != 0.0f)
             return ctx_fail(ctx, GRIS_ERR_INVALID_ARGUMENT, "view " + std::to_string(i) + ": bad settings");
         BatchView& v = views[i];
         int dummy = 0;

@@ -548,6 +548,8 @@ int grisPassRender(GrisContext* ctx, const GrisScene* s, const GrisPassBindings*
         return fail(ctx, GRIS_ERR_INVALID_ARGUMENT, "camera filmSize differs from the bound extent");
     if (set->maxDepth == 0 || set->maxDepth > 255) return fail(ctx, GRIS_ERR_INVALID_ARGUMENT, "maxDepth must be 1..255");
     if (set->spatialNeighbors > 64) return fail(ctx, GRIS_ERR_INVALID_ARGUMENT, "spatialNeighbors must be <= 64");
+    if (set->envRadiance[0] != 0.0f || set->envRadiance[1] != 0.0f || set->envRadiance[2] != 0.0f)
+        return fail(ctx, GRIS_ERR_INVALID_ARGUMENT, "envRadiance is reserved and must be 0");
     cudaSetDevice(ctx->device);
     if (ctx->pathForm == GRIS_PATH_WAVEFRONT && (passes & 1)) {
         /* the wavefront path tracer through the batch launcher, as a one-view batch */

@@ -53,7 +53,8 @@ extern "C" int grisPassRenderNoAlloc(const GrisScene* scene, const GrisPassBindi
         b->reservoirTemp != nullptr)
         return GRIS_ERR_INVALID_ARGUMENT;
     if (cam->filmSize[0] != b->width || cam->filmSize[1] != b->height) return GRIS_ERR_INVALID_ARGUMENT;
-    if (settings->maxDepth == 0 || settings->maxDepth > 255 || settings->spatialNeighbors > 64)
+    if (settings->maxDepth == 0 || settings->maxDepth > 255 || settings->spatialNeighbors > 64 ||
+        settings->envRadiance[0] != 0.0f || settings->envRadiance[1] != 0.0f || settings->envRadiance[2] != 0.0f)
         return GRIS_ERR_INVALID_ARGUMENT;
     uint64_t pixels = (uint64_t)b->width * (uint64_t)b->height;
     if (pixels > (uint64_t)GRIS_NOALLOC_MAX_PIXELS) return GRIS_ERR_TOO_LARGE;
