@@ -123,6 +123,8 @@ def parse():
     ap.add_argument("--ref-spp", type=int, default=1024, help="c4: samples per pixel of the converged image")
     ap.add_argument("--mis", default="reference", choices=["reference", "pairwise"],
                     help="c4: the reuse passes' MIS weights (the reference's merge, or the pairwise extension)")
+    ap.add_argument("--guide-tc", default="off", choices=["on", "off"],
+                    help="c4: the guide's inference on tcgen05 (tensor memory) or mma.sync")
     ap.add_argument("--c4-reuse", default="on", choices=["on", "off"],
                     help="c4: temporal + spatial reuse on (ReSTIR PT) or off (the canonical samples alone)")
     ap.add_argument("--width", type=int, default=1920)
@@ -356,7 +358,7 @@ def run_guided(args):
         guide = None
         if guided:
             guide = G.Guide(ctx, G.GuideConfig.make(seed=args.seed, samplesPerFrame=1 << 18, stepsPerFrame=4,
-                                                    learningRate=1e-3, mix=0.5))
+                                                    learningRate=1e-3, mix=0.5, tensorCores=args.guide_tc == "on"))
             batch.set_guide(guide)
         out_ptr, _ = batch.device_ptr(0, G.BUF_OUTPUT)
         times, rel, med, energy = [], [], [], []
@@ -394,7 +396,8 @@ def run_guided(args):
         wb = G.Batch(ctx, [scene], [(W, H)])
         wg = None
         if guided:
-            wg = G.Guide(ctx, G.GuideConfig.make(seed=args.seed + 1, samplesPerFrame=1 << 16, stepsPerFrame=1))
+            wg = G.Guide(ctx, G.GuideConfig.make(seed=args.seed + 1, samplesPerFrame=1 << 16, stepsPerFrame=1,
+                                                 tensorCores=args.guide_tc == "on"))
             wb.set_guide(wg)
         for f in range(2):
             wb.render([cams[f]], [prevs[f]], [st])
@@ -433,7 +436,8 @@ def run_guided(args):
             "dtype": "f32 paths, bf16 network", "data": "synthetic (seeded scene generator, no dataset)",
             "config": {"workload": "C4: %dx%d glossy variant (%d tris), depth %d, temporal+spatial reuse, static camera, "
                                    "frames accumulated" % (W, H, hs.triangle_count(), args.depth),
-                       "guide": "MLP 80-64x4-48 BF16 mma.sync, 8 vMF lobes, mix 0.5, Adam 1e-3, 2^18 records/frame, 4 steps"},
+                       "guide": "MLP 80-64x4-48 BF16 (inference: %s; training: mma.sync), 8 vMF lobes, mix 0.5, Adam 1e-3, "
+                                "2^18 records/frame, 4 steps" % ("tcgen05" if args.guide_tc == "on" else "mma.sync")},
             "reference": {"spp": args.ref_spp, "seconds": ref_s, "estimator": "candidates"},
             "reuse": reuse, "mis": args.mis, "clocks": clocks,
             "median_error_time_ratio": ratio_med,

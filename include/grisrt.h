@@ -322,7 +322,9 @@ typedef struct GrisGuideConfig {
     uint32_t samplesPerFrame;   /* training records gathered per frame (2^18) */
     uint32_t stepsPerFrame;     /* Adam steps per frame, each on samplesPerFrame / stepsPerFrame records */
     uint32_t train;             /* train while rendering */
-    uint32_t reserved[3];
+    uint32_t tensorCores;       /* inference on the 5th-generation tensor cores (tcgen05, tensor-memory
+                                   accumulators) when 1; warp-level mma.sync when 0 */
+    uint32_t reserved[2];
 } GrisGuideConfig;
 int grisGuideCreate(GrisContext* ctx, const GrisGuideConfig* cfg, GrisGuide** out);
 int grisGuideDestroy(GrisGuide* guide);

@@ -60,7 +60,8 @@ def _render(ctx, scene, W, H, cams, prevs, st, guide=None):
     return np.stack(frames)
 
 
-def test_guided_estimator_is_unbiased_and_trains_to_lower_error():
+@pytest.mark.parametrize("tensor_cores", [False, True], ids=["mma_sync", "tcgen05"])
+def test_guided_estimator_is_unbiased_and_trains_to_lower_error(tensor_cores):
     W, H, F = 48, 48, 384
     ctx = G.Context(0)
     ctx.set_path_form(G.PATH_WAVEFRONT)
@@ -71,7 +72,8 @@ def test_guided_estimator_is_unbiased_and_trains_to_lower_error():
     ref, ref_var = _converged(ctx, scene, cams[0], st, W, H, 1 << 14)
 
     plain = _render(ctx, scene, W, H, cams, prevs, st)
-    guide = G.Guide(ctx, G.GuideConfig.make(seed=5, samplesPerFrame=1 << 14, stepsPerFrame=2, learningRate=2e-3))
+    guide = G.Guide(ctx, G.GuideConfig.make(seed=5, samplesPerFrame=1 << 14, stepsPerFrame=2, learningRate=2e-3,
+                                            tensorCores=tensor_cores))
     guided = _render(ctx, scene, W, H, cams, prevs, st, guide)
     trained = guide.get_params()
     assert np.all(np.isfinite(trained))

@@ -79,15 +79,19 @@ def test_oracle_mixture_sampler_matches_its_density():
 
 
 @pytest.mark.gpu
-def test_gpu_forward_matches_oracle():
+@pytest.mark.parametrize("n", [1000, 100003])
+@pytest.mark.parametrize("tensor_cores", [False, True], ids=["mma_sync", "tcgen05"])
+def test_gpu_forward_matches_oracle(tensor_cores, n):
+    """Inference by the warp-level mma.sync kernel and by the tcgen05 kernel (128-vertex tiles,
+    tensor-memory accumulators): both within the BF16 tolerance of the oracle; n covers partial
+    tiles and several tiles per CTA."""
     import torch
     ctx = G.Context(0)
-    g = G.Guide(ctx, G.GuideConfig.make(samplesPerFrame=1024, stepsPerFrame=1))
+    g = G.Guide(ctx, G.GuideConfig.make(samplesPerFrame=1024, stepsPerFrame=1, tensorCores=tensor_cores))
     W, b = _params(7)
     p = _join(W, b)
     g.set_params(p)
     assert np.array_equal(g.get_params(), p)
-    n = 1000
     feat, _, _ = _inputs(n, 9)
     tf = torch.from_numpy(feat).cuda()
     to = torch.zeros((n, 40), dtype=torch.float32, device="cuda")
@@ -101,6 +105,7 @@ def test_gpu_forward_matches_oracle():
     # the same BF16 roundings on both sides; FP32 against FP64 sums flip a rounding here and there
     assert np.median(err) < 1e-4 * scale
     assert err.max() < 2e-2 * scale
+    assert ctx.counters()[3] == 0   # no tensor-core wait gave up
     g.close()
     ctx.close()
 

@@ -1982,6 +1982,7 @@ cudaError_t enqueue_batch(const BatchShape& sh, void* dViews, const void* hViews
                     guide::FwdArgs fa;
                     fa.wPacked = guide->wPacked; fa.bias = guide->bias; fa.feat = wb.gPrimFeat;
                     fa.count = nullptr; fa.n = pixels; fa.out = wb.gPrimOut;
+                    fa.tensorCores = guide->tensorCores; fa.err = counters + GRIS_COUNTER_ERROR;
                     e = guide::launch_forward(fa, stream);
                     if (e != cudaSuccess) return e;
                 }
@@ -2005,6 +2006,7 @@ cudaError_t enqueue_batch(const BatchShape& sh, void* dViews, const void* hViews
                     guide::FwdArgs fa;
                     fa.wPacked = guide->wPacked; fa.bias = guide->bias; fa.feat = wb.gFeat;
                     fa.count = wb.counts + 768 + level; fa.n = (uint32_t)wb.capacity; fa.out = wb.gOut;
+                    fa.tensorCores = guide->tensorCores; fa.err = counters + GRIS_COUNTER_ERROR;
                     e = guide::launch_forward(fa, stream);
                     if (e != cudaSuccess) return e;
                     mark(9, false);

@@ -381,6 +381,7 @@ __global__ void __launch_bounds__(256) k_guide_weight_sum(const float* weight, c
 
 /* ---------------------------------------------------------------- launchers */
 cudaError_t launch_forward(const FwdArgs& a, cudaStream_t stream) {
+    if (a.tensorCores) return launch_forward_tc(a, stream);
     static int sm = 0;
     if (!sm) { int dev = 0; cudaGetDevice(&dev); cudaDeviceGetAttribute(&sm, cudaDevAttrMultiProcessorCount, dev); }
     k_guide_forward<<<sm * 4, 128, 0, stream>>>(a);

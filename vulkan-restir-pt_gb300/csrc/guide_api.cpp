@@ -47,6 +47,7 @@ guide::GuideDevice guide_device(const GrisGuide* g) {
     guide::GuideDevice d;
     d.wPacked = g->wPacked; d.bias = g->bias;
     d.tFeat = g->tFeat; d.tDir = g->tDir; d.tWeight = g->tWeight; d.tCount = g->tCount; d.cap = g->cap;
+    d.tensorCores = g->cfg.tensorCores != 0;
     d.mix = g->cfg.mix;
     return d;
 }
@@ -202,6 +203,7 @@ int grisGuideForward(GrisContext* ctx, GrisGuide* g, const float* feat, uint32_t
     cudaSetDevice(ctx_device(ctx));
     guide::FwdArgs a;
     a.wPacked = g->wPacked; a.bias = g->bias; a.feat = feat; a.count = nullptr; a.n = n; a.out = out;
+    a.tensorCores = g->cfg.tensorCores != 0; a.err = ctx_counters(ctx) + GRIS_COUNTER_ERROR;
     GUIDE_CK(ctx, guide::launch_forward(a, ctx_stream(ctx)));
     return GRIS_OK;
 }

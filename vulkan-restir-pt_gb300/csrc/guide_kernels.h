@@ -16,6 +16,8 @@ struct FwdArgs {
     const uint32_t* count;     /* optional device count (samples = min(*count, n)) */
     uint32_t n;
     float* out;
+    int tensorCores = 0;                /* 1: the tcgen05 kernel (guide_tc.cu), 0: mma.sync */
+    unsigned long long* err = nullptr;  /* error word (bit 1: a tensor-core wait gave up) */
 };
 
 /* gradient of loss = -sum_i weight_i log p(dir_i | feat_i) / sum_i weight_i, added to grad */
@@ -42,9 +44,12 @@ struct GuideDevice {
     uint32_t* tCount;
     uint32_t cap;
     float mix;
+    int tensorCores;   /* inference kernel: 1 tcgen05, 0 mma.sync */
 };
 
 cudaError_t launch_forward(const FwdArgs& a, cudaStream_t stream);
+cudaError_t launch_forward_tc(const FwdArgs& a, cudaStream_t stream);
+size_t tc_smem_bytes();
 cudaError_t launch_grad(const GradArgs& a, cudaStream_t stream);
 cudaError_t launch_pack(const float* params, __nv_bfloat16* wPacked, float* bias, cudaStream_t stream);
 cudaError_t launch_adam(float* params, float* grad, float* m, float* v, uint32_t* step, float lr, cudaStream_t stream);

@@ -1,0 +1,258 @@
+/* guide_tc.cu — the guiding network's inference on the 5th-generation tensor cores (tcgen05).
+ *
+ * A CTA of 128 threads carries 128 vertices (one per thread, one accumulator row each) through
+ * the five layers: the layer input sits in shared memory as a 128 x K BF16 tile, one elected
+ * thread issues the layer's K/16 `tcgen05.mma.cta_group::1.kind::f16` (M = 128, N = 64 or 48,
+ * K = 16 each, FP32 accumulation in tensor memory), a `tcgen05.commit` arrives on an mbarrier
+ * when they are done, and each warp reads its 32 accumulator rows back with `tcgen05.ld`
+ * (32x32b shape), adds the bias, applies ReLU and writes the next layer's input tile as BF16.
+ * The weights of all layers stay in shared memory for the CTA's life.
+ *
+ * Shared-memory operand layout (no swizzle, K-major): 8 x 8 BF16 core matrices of 128
+ * contiguous bytes (8 rows of 16 B); for a tile of R rows and K columns, core matrix
+ * (r / 8, k / 8) starts at ((r / 8) * (K / 8) + k / 8) * 128 B, so the descriptor's leading byte
+ * offset (between the two core matrices of a 16-wide K slice) is 128 B and its stride byte
+ * offset (between 8-row groups) is K / 8 * 128 B. An MMA's K slice s starts 2 s core matrices in.
+ *
+ * Every wait on the mbarrier is bounded: on timeout the kernel sets the error word, waits
+ * (bounded) for its MMAs once more, frees its tensor memory and returns.
+ */
+#include <cuda_bf16.h>
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "guide.cuh"
+#include "guide_kernels.h"
+
+namespace grisrt {
+namespace guide {
+
+#if defined(__CUDA_ARCH__) && (__CUDA_ARCH__ >= 1000)
+#define GRIS_TC_DEVICE 1
+#endif
+
+constexpr int kTcRows = 128;                 /* vertices per CTA tile = MMA M */
+constexpr uint32_t kTmemCols = 64;           /* accumulator columns (N <= 64) */
+constexpr uint32_t kWaitLimit = 1u << 22;    /* mbarrier polls before the kernel gives up */
+
+/* byte offset of core matrix (row, k) inside a tile of K columns */
+__host__ __device__ constexpr uint32_t core_off(uint32_t row, uint32_t k, uint32_t K) {
+    return ((row >> 3) * (K >> 3) + (k >> 3)) * 128u + (row & 7u) * 16u;
+}
+/* shared memory: weights of the five layers (tile of layer_out x layer_in), the layer-input
+ * tile (128 x 80 at most), biases, mbarrier, tensor-memory address slot */
+__host__ __device__ constexpr uint32_t tc_w_off(int l) {
+    return l == 0 ? 0u : tc_w_off(l - 1) + (uint32_t)(layer_out(l - 1) * layer_in(l - 1)) * 2u;
+}
+constexpr uint32_t kTcA = tc_w_off(5);                                  /* 40960 */
+constexpr uint32_t kTcBias = kTcA + (uint32_t)(kTcRows * kIn) * 2u;     /* + 20480 */
+constexpr uint32_t kTcBar = kTcBias + (uint32_t)kBiases * 4u;
+constexpr uint32_t kTcSlot = kTcBar + 8u;
+constexpr uint32_t kTcSmem = kTcSlot + 8u + 1024u;                      /* + alignment slack */
+static_assert(kTcA % 1024u == 0u && kTcBar % 8u == 0u, "operand tiles 1024-B aligned, mbarrier 8-B aligned");
+
+size_t tc_smem_bytes() { return kTcSmem; }
+
+/* instruction descriptor of kind::f16: D FP32, A and B BF16, both K-major, M = 128, N = n */
+__host__ __device__ constexpr uint32_t tc_idesc(uint32_t n) {
+    return (1u << 4) | (1u << 7) | (1u << 10) | ((n >> 3) << 17) | ((uint32_t)(kTcRows >> 4) << 24);
+}
+
+#ifdef GRIS_TC_DEVICE
+__device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+/* shared-memory matrix descriptor: start address, leading / stride byte offsets (16-B units),
+ * descriptor version 1, no swizzle */
+__device__ __forceinline__ uint64_t tc_sdesc(uint32_t addr, uint32_t lbo, uint32_t sbo) {
+    return (uint64_t)((addr & 0x3ffffu) >> 4) | ((uint64_t)((lbo >> 4) & 0x3fffu) << 16) |
+           ((uint64_t)((sbo >> 4) & 0x3fffu) << 32) | (1ull << 46);
+}
+
+__device__ __forceinline__ void tc_mma(uint32_t tmem, uint64_t a, uint64_t b, uint32_t idesc, uint32_t acc) {
+    asm volatile(
+        "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+        " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n"
+        :: "r"(tmem), "l"(a), "l"(b), "r"(idesc), "r"(acc) : "memory");
+}
+__device__ __forceinline__ void tc_commit(uint32_t bar) {
+    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" :: "r"(bar) : "memory");
+}
+__device__ __forceinline__ bool bar_try(uint32_t bar, uint32_t parity) {
+    uint32_t ok;
+    asm volatile("{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+                 : "=r"(ok) : "r"(bar), "r"(parity) : "memory");
+    return ok != 0u;
+}
+/* bounded wait for the phase `parity` of the mbarrier; false: gave up */
+__device__ __forceinline__ bool bar_wait(uint32_t bar, uint32_t parity) {
+    for (uint32_t i = 0; i < kWaitLimit; i++)
+        if (bar_try(bar, parity)) return true;
+    return false;
+}
+__device__ __forceinline__ void tc_ld16(uint32_t taddr, uint32_t r[16]) {
+    asm volatile("tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
+                 : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+                   "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+                 : "r"(taddr));
+}
+__device__ __forceinline__ void tc_wait_ld() { asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory"); }
+__device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void fence_async_smem() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
+
+/* ReLU(acc + bias) of 16 columns [c, c + 16) of this thread's row, as BF16 into the next tile */
+__device__ __forceinline__ void store_hidden16(unsigned char* tile, uint32_t row, uint32_t c, const uint32_t r[16],
+                                               const float* bias) {
+    uint32_t w[8];
+#pragma unroll
+    for (int i = 0; i < 8; i++) {
+        float a = fmaxf(__uint_as_float(r[2 * i]) + bias[c + 2 * i], 0.0f);
+        float b = fmaxf(__uint_as_float(r[2 * i + 1]) + bias[c + 2 * i + 1], 0.0f);
+        w[i] = pack_bf16(a, b);
+    }
+    *reinterpret_cast<uint4*>(tile + core_off(row, c, kHid)) = make_uint4(w[0], w[1], w[2], w[3]);
+    *reinterpret_cast<uint4*>(tile + core_off(row, c + 8, kHid)) = make_uint4(w[4], w[5], w[6], w[7]);
+}
+#endif
+
+__global__ void __launch_bounds__(kTcRows, 1) k_guide_forward_tc(FwdArgs a) {
+#ifdef GRIS_TC_DEVICE
+    extern __shared__ unsigned char smemRaw[];
+    unsigned char* smem = reinterpret_cast<unsigned char*>((reinterpret_cast<uintptr_t>(smemRaw) + 1023u) & ~(uintptr_t)1023u);
+    unsigned char* sA = smem + kTcA;
+    float* sBias = reinterpret_cast<float*>(smem + kTcBias);
+    const uint32_t bar = smem_u32(smem + kTcBar);
+    uint32_t* slot = reinterpret_cast<uint32_t*>(smem + kTcSlot);
+    __shared__ uint32_t sFail;
+    const uint32_t tid = threadIdx.x, warp = tid >> 5;
+
+    /* weights into the core-matrix layout (16-B chunks: row n, columns 8kg..8kg+7) and biases */
+    for (int l = 0; l < 5; l++) {
+        const int K = layer_in(l), N = layer_out(l), chunks = N * (K / 8);
+        for (int i = (int)tid; i < chunks; i += kTcRows) {
+            int n = i / (K / 8), kg = i % (K / 8);
+            uint4 v = *reinterpret_cast<const uint4*>(a.wPacked + packed_w(l) + n * stride_w(l) + 8 * kg);
+            *reinterpret_cast<uint4*>(smem + tc_w_off(l) + core_off((uint32_t)n, (uint32_t)(8 * kg), (uint32_t)K)) = v;
+        }
+    }
+    for (int i = (int)tid; i < kBiases; i += kTcRows) sBias[i] = a.bias[i];
+    if (tid == 0) {
+        sFail = 0u;
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" :: "r"(bar) : "memory");
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" :: "r"(smem_u32(slot)), "r"(kTmemCols)
+                     : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+    }
+    fence_async_smem();
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    const uint32_t tmem = *slot;
+    const uint32_t myLanes = tmem + ((warp * 32u) << 16);
+    uint32_t phase = 0u;
+    const uint32_t n = a.count ? min(*a.count, a.n) : a.n;
+
+    for (uint32_t tile = blockIdx.x; tile * (uint32_t)kTcRows < n; tile += gridDim.x) {
+        const uint32_t row = tid, v = tile * (uint32_t)kTcRows + tid;
+        /* layer-0 input: the encoding of this thread's vertex (zeros past the end) */
+        float f[9];
+#pragma unroll
+        for (int i = 0; i < 9; i++) f[i] = v < n ? a.feat[(size_t)v * 9 + i] : 0.0f;
+        float e[kIn];
+#pragma unroll
+        for (int c = 0; c < 3; c++)
+#pragma unroll
+            for (int j = 0; j < 12; j++) {
+                float s, co;
+                sincospif(f[c] * (float)(1 << j), &s, &co);
+                e[c * 24 + j] = s;
+                e[c * 24 + 12 + j] = co;
+            }
+#pragma unroll
+        for (int i = 72; i < 78; i++) e[i] = f[i - 69];
+        e[78] = 0.0f; e[79] = 0.0f;
+#pragma unroll
+        for (int kg = 0; kg < kIn / 8; kg++)
+            *reinterpret_cast<uint4*>(sA + core_off(row, (uint32_t)(8 * kg), kIn)) =
+                make_uint4(pack_bf16(e[8 * kg], e[8 * kg + 1]), pack_bf16(e[8 * kg + 2], e[8 * kg + 3]),
+                           pack_bf16(e[8 * kg + 4], e[8 * kg + 5]), pack_bf16(e[8 * kg + 6], e[8 * kg + 7]));
+        fence_async_smem();
+        tc_fence_before();
+        __syncthreads();
+        bool ok = sFail == 0u;
+        for (int l = 0; l < 5 && ok; l++) {
+            const uint32_t K = (uint32_t)layer_in(l), N = (uint32_t)layer_out(l);
+            if (tid == 0) {
+                tc_fence_after();
+                const uint32_t aBase = smem_u32(sA), bBase = smem_u32(smem + tc_w_off(l));
+                for (uint32_t s = 0; s < K / 16u; s++)
+                    tc_mma(tmem, tc_sdesc(aBase + s * 256u, 128u, (K / 8u) * 128u),
+                           tc_sdesc(bBase + s * 256u, 128u, (K / 8u) * 128u), tc_idesc(N), s > 0u ? 1u : 0u);
+                tc_commit(bar);
+            }
+            if (!bar_wait(bar, phase)) {
+                sFail = 1u;
+                if (a.err) atomicOr(a.err, 2ull);
+            }
+            phase ^= 1u;
+            tc_fence_after();
+            __syncthreads();
+            ok = sFail == 0u;
+            if (!ok) break;
+            const float* bias = sBias + bias_off(l);
+            if (l < 4) {
+#pragma unroll
+                for (uint32_t c = 0; c < (uint32_t)kHid; c += 16u) {
+                    uint32_t r[16];
+                    tc_ld16(myLanes + c, r);
+                    tc_wait_ld();
+                    store_hidden16(sA, row, c, r, bias);
+                }
+                fence_async_smem();
+                tc_fence_before();
+                __syncthreads();
+            } else {
+#pragma unroll
+                for (uint32_t c = 0; c < 48u; c += 16u) {
+                    uint32_t r[16];
+                    tc_ld16(myLanes + c, r);
+                    tc_wait_ld();
+                    if (v < n) {
+#pragma unroll
+                        for (uint32_t i = 0; i < 16u; i++)
+                            if (c + i < (uint32_t)kRaw) a.out[(size_t)v * kRaw + c + i] = __uint_as_float(r[i]) + bias[c + i];
+                    }
+                }
+                tc_fence_before();
+                __syncthreads();
+            }
+        }
+        if (!ok) break;
+    }
+    /* after a timeout: one more bounded wait for the MMAs in flight before the memory is freed */
+    if (sFail && tid == 0) (void)bar_wait(bar, phase);
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" :: "r"(tmem), "r"(kTmemCols) : "memory");
+#endif
+}
+
+cudaError_t launch_forward_tc(const FwdArgs& a, cudaStream_t stream) {
+    static int sm = 0;
+    static bool attr = false;
+    if (!sm) { int dev = 0; cudaGetDevice(&dev); cudaDeviceGetAttribute(&sm, cudaDevAttrMultiProcessorCount, dev); }
+    if (!attr) {
+        cudaError_t e = cudaFuncSetAttribute(k_guide_forward_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kTcSmem);
+        if (e != cudaSuccess) return e;
+        attr = true;
+    }
+    k_guide_forward_tc<<<sm * 2, kTcRows, kTcSmem, stream>>>(a);
+    return cudaGetLastError();
+}
+
+}  // namespace guide
+}  // namespace grisrt
