@@ -29,7 +29,9 @@ def test_library_exports_every_declared_symbol():
 
 def test_layout_sizes_match_reference_std430():
     lib = G.load()
-    assert [lib.grisSizeof(i) for i in range(8)] == [352, 96, 32, 32, 224, 64, 8, 64]
+    assert [lib.grisSizeof(i) for i in range(10)] == [352, 96, 32, 32, 224, 64, 8, 64, 64, 16]
+    assert G.DI_RESERVOIR.itemsize == 64 and ctypes.sizeof(G.DISettings) == 16
+    assert ctypes.sizeof(G.PostSettings) == 16 and ctypes.sizeof(G.GuideConfig) == 40
     from oracle import pyoracle
     ora = pyoracle.oracle()
     assert [ora.sizeof(i) for i in range(7)] == [352, 96, 32, 32, 224, 64, 8]
