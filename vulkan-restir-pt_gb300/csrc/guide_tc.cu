@@ -1,12 +1,14 @@
 /* guide_tc.cu — the guiding network's inference on the 5th-generation tensor cores (tcgen05).
  *
- * A CTA of 128 threads carries 128 vertices (one per thread, one accumulator row each) through
- * the five layers: the layer input sits in shared memory as a 128 x K BF16 tile, one elected
- * thread issues the layer's K/16 `tcgen05.mma.cta_group::1.kind::f16` (M = 128, N = 64 or 48,
- * K = 16 each, FP32 accumulation in tensor memory), a `tcgen05.commit` arrives on an mbarrier
- * when they are done, and each warp reads its 32 accumulator rows back with `tcgen05.ld`
- * (32x32b shape), adds the bias, applies ReLU and writes the next layer's input tile as BF16.
- * The weights of all layers stay in shared memory for the CTA's life.
+ * A CTA holds the weights of all layers in shared memory and runs two independent groups of 128
+ * threads; a group carries 128 vertices (one per thread, one accumulator row each) through the
+ * five layers: the layer input sits in shared memory as a 128 x K BF16 tile, one elected thread
+ * of the group issues the layer's K/16 `tcgen05.mma.cta_group::1.kind::f16` (M = 128, N = 64 or
+ * 48, K = 16 each, FP32 accumulation in the group's 64 tensor-memory columns), a
+ * `tcgen05.commit` arrives on the group's mbarrier when they are done, and each warp reads its 32
+ * accumulator rows back with `tcgen05.ld` (32x32b shape), adds the bias, applies ReLU and writes
+ * the next layer's input tile as BF16. The groups synchronise on their own named barriers, so
+ * one group's epilogue overlaps the other's matrix products.
  *
  * Shared-memory operand layout (no swizzle, K-major): 8 x 8 BF16 core matrices of 128
  * contiguous bytes (8 rows of 16 B); for a tile of R rows and K columns, core matrix
@@ -31,8 +33,9 @@ namespace guide {
 #define GRIS_TC_DEVICE 1
 #endif
 
-constexpr int kTcRows = 128;                 /* vertices per CTA tile = MMA M */
-constexpr uint32_t kTmemCols = 64;           /* accumulator columns (N <= 64) */
+constexpr int kTcRows = 128;                 /* vertices per group tile = MMA M */
+constexpr int kTcGroups = 2;                 /* independent groups (tiles in flight) per CTA */
+constexpr uint32_t kTmemCols = 64 * kTcGroups;   /* accumulator columns: 64 per group (N <= 64) */
 constexpr uint32_t kWaitLimit = 1u << 22;    /* mbarrier polls before the kernel gives up */
 
 /* byte offset of core matrix (row, k) inside a tile of K columns */
@@ -45,9 +48,10 @@ __host__ __device__ constexpr uint32_t tc_w_off(int l) {
     return l == 0 ? 0u : tc_w_off(l - 1) + (uint32_t)(layer_out(l - 1) * layer_in(l - 1)) * 2u;
 }
 constexpr uint32_t kTcA = tc_w_off(5);                                  /* 40960 */
-constexpr uint32_t kTcBias = kTcA + (uint32_t)(kTcRows * kIn) * 2u;     /* + 20480 */
-constexpr uint32_t kTcBar = kTcBias + (uint32_t)kBiases * 4u;
-constexpr uint32_t kTcSlot = kTcBar + 8u;
+constexpr uint32_t kTcATile = (uint32_t)(kTcRows * kIn) * 2u;           /* 20480 per group */
+constexpr uint32_t kTcBias = kTcA + kTcATile * (uint32_t)kTcGroups;
+constexpr uint32_t kTcBar = kTcBias + (uint32_t)kBiases * 4u;           /* one mbarrier per group */
+constexpr uint32_t kTcSlot = kTcBar + 8u * (uint32_t)kTcGroups;
 constexpr uint32_t kTcSmem = kTcSlot + 8u + 1024u;                      /* + alignment slack */
 static_assert(kTcA % 1024u == 0u && kTcBar % 8u == 0u, "operand tiles 1024-B aligned, mbarrier 8-B aligned");
 
@@ -99,6 +103,8 @@ __device__ __forceinline__ void tc_wait_ld() { asm volatile("tcgen05.wait::ld.sy
 __device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
 __device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
 __device__ __forceinline__ void fence_async_smem() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
+/* barrier of one group's 128 threads (named barrier 1 + group) */
+__device__ __forceinline__ void group_sync(uint32_t g) { asm volatile("bar.sync %0, %1;" :: "r"(1u + g), "r"(kTcRows) : "memory"); }
 
 /* ReLU(acc + bias) of 16 columns [c, c + 16) of this thread's row, as BF16 into the next tile */
 __device__ __forceinline__ void store_hidden16(unsigned char* tile, uint32_t row, uint32_t c, const uint32_t r[16],
@@ -115,33 +121,36 @@ __device__ __forceinline__ void store_hidden16(unsigned char* tile, uint32_t row
 }
 #endif
 
-__global__ void __launch_bounds__(kTcRows, 1) k_guide_forward_tc(FwdArgs a) {
+__global__ void __launch_bounds__(kTcRows * kTcGroups, 2) k_guide_forward_tc(FwdArgs a) {
 #ifdef GRIS_TC_DEVICE
     extern __shared__ unsigned char smemRaw[];
     unsigned char* smem = reinterpret_cast<unsigned char*>((reinterpret_cast<uintptr_t>(smemRaw) + 1023u) & ~(uintptr_t)1023u);
-    unsigned char* sA = smem + kTcA;
+    const uint32_t ctaThreads = (uint32_t)(kTcRows * kTcGroups);
+    const uint32_t grp = threadIdx.x / (uint32_t)kTcRows;     /* this thread's group */
+    const uint32_t tid = threadIdx.x % (uint32_t)kTcRows;     /* = its row in the group's tile */
+    const uint32_t warp = tid >> 5;                           /* warp within the group: TMEM lanes 32 warp.. */
+    unsigned char* sA = smem + kTcA + grp * kTcATile;
     float* sBias = reinterpret_cast<float*>(smem + kTcBias);
-    const uint32_t bar = smem_u32(smem + kTcBar);
+    const uint32_t bar = smem_u32(smem + kTcBar + 8u * grp);
     uint32_t* slot = reinterpret_cast<uint32_t*>(smem + kTcSlot);
-    __shared__ uint32_t sFail;
-    const uint32_t tid = threadIdx.x, warp = tid >> 5;
+    __shared__ uint32_t sFail[kTcGroups];
 
     /* weights into the core-matrix layout (16-B chunks: row n, columns 8kg..8kg+7) and biases */
     for (int l = 0; l < 5; l++) {
         const int K = layer_in(l), N = layer_out(l), chunks = N * (K / 8);
-        for (int i = (int)tid; i < chunks; i += kTcRows) {
+        for (int i = (int)threadIdx.x; i < chunks; i += (int)ctaThreads) {
             int n = i / (K / 8), kg = i % (K / 8);
             uint4 v = *reinterpret_cast<const uint4*>(a.wPacked + packed_w(l) + n * stride_w(l) + 8 * kg);
             *reinterpret_cast<uint4*>(smem + tc_w_off(l) + core_off((uint32_t)n, (uint32_t)(8 * kg), (uint32_t)K)) = v;
         }
     }
-    for (int i = (int)tid; i < kBiases; i += kTcRows) sBias[i] = a.bias[i];
+    for (int i = (int)threadIdx.x; i < kBiases; i += (int)ctaThreads) sBias[i] = a.bias[i];
     if (tid == 0) {
-        sFail = 0u;
+        sFail[grp] = 0u;
         asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" :: "r"(bar) : "memory");
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
-    if (warp == 0) {
+    if (threadIdx.x < 32u) {
         asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" :: "r"(smem_u32(slot)), "r"(kTmemCols)
                      : "memory");
         asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
@@ -150,39 +159,39 @@ __global__ void __launch_bounds__(kTcRows, 1) k_guide_forward_tc(FwdArgs a) {
     tc_fence_before();
     __syncthreads();
     tc_fence_after();
-    const uint32_t tmem = *slot;
+    const uint32_t tmemBase = *slot;
+    const uint32_t tmem = tmemBase + 64u * grp;                 /* the group's accumulator columns */
     const uint32_t myLanes = tmem + ((warp * 32u) << 16);
     uint32_t phase = 0u;
     const uint32_t n = a.count ? min(*a.count, a.n) : a.n;
 
-    for (uint32_t tile = blockIdx.x; tile * (uint32_t)kTcRows < n; tile += gridDim.x) {
+    for (uint32_t tile = blockIdx.x * kTcGroups + grp; tile * (uint32_t)kTcRows < n; tile += gridDim.x * kTcGroups) {
         const uint32_t row = tid, v = tile * (uint32_t)kTcRows + tid;
         /* layer-0 input: the encoding of this thread's vertex (zeros past the end) */
         float f[9];
 #pragma unroll
         for (int i = 0; i < 9; i++) f[i] = v < n ? a.feat[(size_t)v * 9 + i] : 0.0f;
-        float e[kIn];
+        /* position encoding per coordinate: 12 sines then 12 cosines = three 8-column chunks */
 #pragma unroll
-        for (int c = 0; c < 3; c++)
+        for (int c = 0; c < 3; c++) {
+            float sv[12], cv[12];
 #pragma unroll
-            for (int j = 0; j < 12; j++) {
-                float s, co;
-                sincospif(f[c] * (float)(1 << j), &s, &co);
-                e[c * 24 + j] = s;
-                e[c * 24 + 12 + j] = co;
-            }
-#pragma unroll
-        for (int i = 72; i < 78; i++) e[i] = f[i - 69];
-        e[78] = 0.0f; e[79] = 0.0f;
-#pragma unroll
-        for (int kg = 0; kg < kIn / 8; kg++)
-            *reinterpret_cast<uint4*>(sA + core_off(row, (uint32_t)(8 * kg), kIn)) =
-                make_uint4(pack_bf16(e[8 * kg], e[8 * kg + 1]), pack_bf16(e[8 * kg + 2], e[8 * kg + 3]),
-                           pack_bf16(e[8 * kg + 4], e[8 * kg + 5]), pack_bf16(e[8 * kg + 6], e[8 * kg + 7]));
+            for (int j = 0; j < 12; j++) sincospif(f[c] * (float)(1 << j), &sv[j], &cv[j]);
+            unsigned char* base = sA + core_off(row, (uint32_t)(24 * c), kIn);
+            *reinterpret_cast<uint4*>(base) =
+                make_uint4(pack_bf16(sv[0], sv[1]), pack_bf16(sv[2], sv[3]), pack_bf16(sv[4], sv[5]), pack_bf16(sv[6], sv[7]));
+            *reinterpret_cast<uint4*>(base + 128) =
+                make_uint4(pack_bf16(sv[8], sv[9]), pack_bf16(sv[10], sv[11]), pack_bf16(cv[0], cv[1]), pack_bf16(cv[2], cv[3]));
+            *reinterpret_cast<uint4*>(base + 256) =
+                make_uint4(pack_bf16(cv[4], cv[5]), pack_bf16(cv[6], cv[7]), pack_bf16(cv[8], cv[9]), pack_bf16(cv[10], cv[11]));
+        }
+        /* normal, direction towards the previous vertex, two zeros */
+        *reinterpret_cast<uint4*>(sA + core_off(row, 72u, kIn)) =
+            make_uint4(pack_bf16(f[3], f[4]), pack_bf16(f[5], f[6]), pack_bf16(f[7], f[8]), pack_bf16(0.0f, 0.0f));
         fence_async_smem();
         tc_fence_before();
-        __syncthreads();
-        bool ok = sFail == 0u;
+        group_sync(grp);
+        bool ok = sFail[grp] == 0u;
         for (int l = 0; l < 5 && ok; l++) {
             const uint32_t K = (uint32_t)layer_in(l), N = (uint32_t)layer_out(l);
             if (tid == 0) {
@@ -194,13 +203,13 @@ __global__ void __launch_bounds__(kTcRows, 1) k_guide_forward_tc(FwdArgs a) {
                 tc_commit(bar);
             }
             if (!bar_wait(bar, phase)) {
-                sFail = 1u;
+                sFail[grp] = 1u;
                 if (a.err) atomicOr(a.err, 2ull);
             }
             phase ^= 1u;
             tc_fence_after();
-            __syncthreads();
-            ok = sFail == 0u;
+            group_sync(grp);
+            ok = sFail[grp] == 0u;
             if (!ok) break;
             const float* bias = sBias + bias_off(l);
             if (l < 4) {
@@ -213,7 +222,7 @@ __global__ void __launch_bounds__(kTcRows, 1) k_guide_forward_tc(FwdArgs a) {
                 }
                 fence_async_smem();
                 tc_fence_before();
-                __syncthreads();
+                group_sync(grp);
             } else {
 #pragma unroll
                 for (uint32_t c = 0; c < 48u; c += 16u) {
@@ -227,17 +236,18 @@ __global__ void __launch_bounds__(kTcRows, 1) k_guide_forward_tc(FwdArgs a) {
                     }
                 }
                 tc_fence_before();
-                __syncthreads();
+                group_sync(grp);
             }
         }
         if (!ok) break;
     }
     /* after a timeout: one more bounded wait for the MMAs in flight before the memory is freed */
-    if (sFail && tid == 0) (void)bar_wait(bar, phase);
+    if (sFail[grp] && tid == 0) (void)bar_wait(bar, phase);
     tc_fence_before();
     __syncthreads();
     tc_fence_after();
-    if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" :: "r"(tmem), "r"(kTmemCols) : "memory");
+    if (threadIdx.x < 32u)
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" :: "r"(tmemBase), "r"(kTmemCols) : "memory");
 #endif
 }
 
@@ -250,7 +260,7 @@ cudaError_t launch_forward_tc(const FwdArgs& a, cudaStream_t stream) {
         if (e != cudaSuccess) return e;
         attr = true;
     }
-    k_guide_forward_tc<<<sm * 2, kTcRows, kTcSmem, stream>>>(a);
+    k_guide_forward_tc<<<sm * 2, kTcRows * kTcGroups, kTcSmem, stream>>>(a);
     return cudaGetLastError();
 }
 
