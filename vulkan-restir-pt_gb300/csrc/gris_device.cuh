@@ -464,17 +464,19 @@ GD void loadSurfaceInfo(const DevScene& sc, const Isec& isec, Surf& info) {
 }
 
 /* ---------------------------------------------------------------- camera.glsl:28-42 */
+/* aspect = w / h and tanHalfFov = tan(FOV / 2) are the per-frame constants of the ray
+ * (computed on the host by make_cam with the same binary32 operations as the shader's). */
 struct CamD {
     V3 pos, front, right, up;
     float FOV;
     uint32_t w, h, frameIndex, seed;
+    float aspect, tanHalfFov;
 };
+/* The shader adds (1 / size) * 0 to uv before mapping to [-1, 1]; that term is +0 and changes no
+ * result (x + 0 = x, and -0 maps to -1 as +0 does), so it is left out. */
 GD Ray3 pinholeCameraSampleRay(const CamD& cam, V2 uv) {
-    float tx = 1.0f / (float)cam.w, ty = 1.0f / (float)cam.h;
-    V2 biased = v2(uv.x + tx * 0.0f, uv.y + ty * 0.0f);
-    V2 ndc = v2(biased.x * 2.0f - 1.0f, biased.y * 2.0f - 1.0f);
-    float aspect = (float)cam.w / (float)cam.h;
-    float tanFOV = gris_det_tanf(cam.FOV * 0.5f * 0.01745329251994329577f);
+    V2 ndc = v2(uv.x * 2.0f - 1.0f, uv.y * 2.0f - 1.0f);
+    const float aspect = cam.aspect, tanFOV = cam.tanHalfFov;
     V3 pFocus = v3(ndc.x * aspect * tanFOV, ndc.y * 1.0f * tanFOV, 1.0f);
     V3 dir = normalize3(pFocus);
     dir = normalize3(cam.right * dir.x + cam.up * dir.y + cam.front * dir.z);

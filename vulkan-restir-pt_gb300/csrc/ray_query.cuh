@@ -100,6 +100,8 @@ inline CamD make_cam(const GrisCamera& c) {
     d.FOV = c.FOV;
     d.w = c.filmSize[0]; d.h = c.filmSize[1];
     d.frameIndex = c.frameIndex; d.seed = c.seed;
+    d.aspect = (float)d.w / (float)d.h;
+    d.tanHalfFov = gris_det_tanf(c.FOV * 0.5f * 0.01745329251994329577f);
     return d;
 }
 
