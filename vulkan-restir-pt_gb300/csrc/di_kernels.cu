@@ -13,9 +13,10 @@
  * One thread per pixel of a 16 x 8 tile, as the GRIS kernels; reservoirs are 64 B (four 16-byte
  * words per pixel, read and written as uint4). Traversal is the 8-wide BVH walk shared with the
  * GRIS kernels (ray_query.cuh), called out of line from the several query sites of a kernel.
- * The kernels ask for 5 resident blocks of 128 threads per SM (at most 96 registers): measured at
- * 1080p, the spatial pass runs in 4.81 ms that way against 5.91 ms at its natural 160 registers
- * (3 blocks), despite a few hundred bytes of spills.
+ * The kernels ask for 8 resident blocks of 128 threads per SM (at most 64 registers): measured at
+ * 1080p, the spatial pass runs in 4.53 ms that way, 4.81 ms at 5 blocks, 4.60 at 10 and 5.91 ms
+ * at its natural 160 registers (3 blocks); the latency of the walks is hidden by more warps
+ * rather than by registers, despite the spills.
  */
 #include <cuda_fp16.h>
 #include <cuda_runtime.h>
@@ -247,7 +248,7 @@ GD bool di_pixel(const DICtx& P, uint32_t ix, uint32_t iy, DIPixel& px) {
 }
 
 /* ------------------------------------------------------------------ kernels */
-__global__ void __launch_bounds__(128, 5) k_di_candidates(DICtx P) {
+__global__ void __launch_bounds__(128, 8) k_di_candidates(DICtx P) {
     RayCount rc = ray_count();
     int err = 0;
     uint32_t x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y * blockDim.y + threadIdx.y;
@@ -264,7 +265,7 @@ __global__ void __launch_bounds__(128, 5) k_di_candidates(DICtx P) {
 }
 
 /* findPreviousReservoir (di_temporal.glsl:9-34) + temporalReuse (:36-90) */
-__global__ void __launch_bounds__(128, 5) k_di_temporal(DICtx P) {
+__global__ void __launch_bounds__(128, 8) k_di_temporal(DICtx P) {
     RayCount rc = ray_count();
     int err = 0;
     uint32_t x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y * blockDim.y + threadIdx.y;
@@ -302,7 +303,7 @@ __global__ void __launch_bounds__(128, 5) k_di_temporal(DICtx P) {
 
 /* findNeighborReservoir (di_spatial.glsl:9-34) + spatialReuse (:36-121) + the running mean of
  * di_spatial.comp:21-26 (a background pixel accumulates black). */
-__global__ void __launch_bounds__(128, 5) k_di_spatial(DICtx P) {
+__global__ void __launch_bounds__(128, 8) k_di_spatial(DICtx P) {
     RayCount rc = ray_count();
     int err = 0;
     uint32_t x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y * blockDim.y + threadIdx.y;

@@ -951,8 +951,9 @@ GD void run_persistent(const PassCtx& P, unsigned int* cursor, RayCount& rc, int
 
 /* ------------------------------------------------------------------ kernels */
 /* Resident blocks per SM requested from the compiler for the grid form: the reuse passes run
- * faster at 5 blocks (96 registers) despite a few spills; the path tracer at its natural 3. */
-template <int KERNEL> struct GridMinBlocks { static constexpr int value = KERNEL == 1 ? 1 : 5; };
+ * faster at 8 blocks (64 registers) despite their spills (1080p C2: temporal + spatial 3.65 ms at
+ * 8 blocks, 3.79 at 6, 4.04 at 5); the path tracer at its natural occupancy. */
+template <int KERNEL> struct GridMinBlocks { static constexpr int value = KERNEL == 1 ? 1 : 8; };
 
 template <typename Task, int KERNEL>
 __global__ void __launch_bounds__(128, GridMinBlocks<KERNEL>::value) k_pass_grid(PassCtx P) {
