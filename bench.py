@@ -643,8 +643,17 @@ def run_di(args, rank, world, local):
     top = max(slots, key=lambda s_: prof[s_]["ms"])
     pk = per_kernel[top]
     achieved = pk["gbs"] or 0.0
+    traffic = None
+    tfile = os.path.join(REPO, "profiles", "ncu_dram_traffic.json")
+    if os.path.exists(tfile):
+        try:
+            e = json.load(open(tfile)).get("di", {}).get(top)
+            if e:
+                traffic = float(e["bytes_per_launch"]) * (W * H / float(e.get("pixels", W * H)))
+        except Exception:
+            traffic = None
     roofline = {"bound": "hbm", "kernel": top, "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
-                "frac": round(achieved / peak, 4), "peak_source": peak_kind, "traffic": None,
+                "frac": round(achieved / peak, 4), "peak_source": peak_kind, "traffic": traffic,
                 "algorithmic_bytes_per_launch": pk["alg_bytes_per_launch"], "avg_launch_ms": pk["avg_launch_ms"],
                 "share_of_frame": round(prof[top]["ms"] / max(1e-9, sum(prof[s_]["ms"] for s_ in slots)), 3),
                 "kernels": per_kernel}
