@@ -138,3 +138,28 @@ def test_batched_workload_views_match_oracle():
     for sc in scenes:
         sc.close()
     ctx.close()
+
+
+def test_batch_graph_follows_the_mis_weights_setting():
+    """One batch (graphs on) renders a sequence with the reference merge and then one with the
+    pairwise weights: the second must not replay the first's captured graph. Closed box: every
+    pixel has geometry, so no buffer keeps data from the first sequence."""
+    ctx = G.Context(0)
+    ctx.set_graphs(True)
+    hs = G.HostScene(0, seed=7)
+    scene = G.Scene(ctx, hs)
+    W, H = 32, 24
+    batch = G.Batch(ctx, [scene], [(W, H)])
+    ora = O.oracle()
+    ora.set_scene(hs)
+    for seed, mis in ((3, 0), (4, 1), (5, 0)):
+        cams, prevs = G.sequence_cameras(hs, 3, W, H, seed=seed)
+        st = G.Settings.make(maxDepth=4, misWeights=mis)
+        want = O.run_sequence(ora, cams, prevs, st, W, H, record=("resv", "out"))
+        for f in range(3):
+            batch.render([cams[f]], [prevs[f]], [st])
+            assert batch.download(0, G.BUF_RESERVOIR).tobytes() == want[f]["resv"].tobytes(), (mis, f)
+            assert batch.download(0, G.BUF_OUTPUT).tobytes() == want[f]["out"].tobytes(), (mis, f)
+    batch.close()
+    scene.close()
+    ctx.close()
