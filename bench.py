@@ -136,6 +136,9 @@ def parse():
     ap.add_argument("--seed", type=int, default=1)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-autotune", action="store_true")
+    ap.add_argument("--wave", default=None,
+                    help="with --no-autotune: the wavefront launch as TRACE,SHADE[,refill] blocks per SM (e.g. 16,16,refill), "
+                         "the form the autotuner picks, so that a profiler run can skip the tuning frames")
     ap.add_argument("--no-graphs", action="store_true")
     ap.add_argument("--launch-mode", default="grid", choices=["persistent", "grid"])
     ap.add_argument("--api", default="batch", choices=["batch", "frame"],
@@ -733,6 +736,10 @@ def main():
     ctx = G.Context(local)
     ctx.set_launch_mode(G.LAUNCH_PERSISTENT if args.launch_mode == "persistent" else G.LAUNCH_GRID)
     ctx.set_path_form(G.PATH_WAVEFRONT if args.path_form == "wavefront" else G.PATH_MEGAKERNEL)
+    if args.wave:
+        parts = args.wave.split(",")
+        ctx.set_wave_launch(int(parts[0]), int(parts[1]))
+        ctx.set_wave_refill(len(parts) > 2 and parts[2] == "refill")
     ctx.set_graphs(not args.no_graphs)
     scenes = [G.Scene(ctx, v.hs) for v in views]
     stats = [sc.stats() for sc in scenes]
@@ -770,6 +777,8 @@ def main():
     config["path_form"] = ("wavefront" if form == G.PATH_WAVEFRONT else "megakernel") if batch is not None else "megakernel"
     config["graphs"] = batch is not None and not args.no_graphs
     config["autotune"] = tune
+    if args.wave and tune is None:
+        config["wave"] = args.wave
 
     def barrier():
         torch.cuda.synchronize()
