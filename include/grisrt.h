@@ -37,7 +37,8 @@ extern "C" {
 #define GRIS_ERR_CUDA (-2)
 #define GRIS_ERR_OUT_OF_MEMORY (-3)
 #define GRIS_ERR_UNSUPPORTED (-4)
-#define GRIS_ERR_DEVICE_FAULT (-5)   /* a kernel raised its error word (e.g. a bounded wait ran out) */
+#define GRIS_ERR_DEVICE_FAULT (-5)   /* a kernel raised its error word: bit 0 the traversal stack limit,
+                                        bit 1 a bounded tensor-core wait ran out */
 #define GRIS_ERR_TOO_LARGE (-6)
 
 /* ---------------------------------------------------------------- layouts */

@@ -367,7 +367,13 @@ int grisSync(GrisContext* ctx) {
     cudaSetDevice(ctx->device);
     GRIS_CK(ctx, cudaStreamSynchronize(ctx->stream));
     GRIS_CK(ctx, cudaMemcpy(ctx->hCounters + 3, ctx->dCounters + 3, sizeof(unsigned long long), cudaMemcpyDeviceToHost));
-    if (ctx->hCounters[3]) return fail(ctx, GRIS_ERR_DEVICE_FAULT, "a kernel raised the error word (traversal stack limit)");
+    if (ctx->hCounters[3]) {
+        const unsigned long long w = ctx->hCounters[3];
+        std::string what;
+        if (w & 1ull) what += " traversal stack limit";
+        if (w & 2ull) what += " tensor-core wait gave up";
+        return fail(ctx, GRIS_ERR_DEVICE_FAULT, "a kernel raised the error word (bits " + std::to_string(w) + ":" + what + ")");
+    }
     return GRIS_OK;
 }
 
