@@ -336,6 +336,11 @@ int grisGuideSetTraining(GrisGuide* guide, int enable);
 /* device pointers: feat 9 floats per sample (position in [0,1]^3, normal, wo), out 40 raw
  * outputs per sample (lobe j: direction 5j..5j+2, log-concentration 5j+3, logit 5j+4) */
 int grisGuideForward(GrisContext* ctx, GrisGuide* guide, const float* feat, uint32_t n, float* out);
+/* Test of the tcgen05 kernel's bounded waits: the inference with the completion of its matrix
+ * products never signalled. Every wait gives up after its poll limit (well under a second), the
+ * kernel raises bit 1 of the error word (grisSync then returns GRIS_ERR_DEVICE_FAULT), frees its
+ * tensor memory and returns; the context stays usable (reset the word with grisReadCounters). */
+int grisDebugGuideForwardStall(GrisContext* ctx, GrisGuide* guide, const float* feat, uint32_t n, float* out);
 /* gradient of -sum_i weight_i log p(dir_i) / sum_i weight_i with respect to the FP32 parameters
  * (device; overwritten) at the current weights */
 int grisGuideGradient(GrisContext* ctx, GrisGuide* guide, const float* feat, const float* dir, const float* weight,

@@ -214,3 +214,37 @@ def test_gpu_training_fits_a_target_distribution():
     assert after > before + 2.0
     g.close()
     ctx.close()
+
+
+@pytest.mark.gpu
+def test_tcgen05_wait_gives_up_and_reports():
+    """The tcgen05 inference with the completion of its matrix products never signalled
+    (grisDebugGuideForwardStall): its bounded waits run out, it raises bit 1 of the error word,
+    frees its tensor memory and returns; the context then runs an ordinary forward correctly."""
+    import time
+    import torch
+    ctx = G.Context(0)
+    g = G.Guide(ctx, G.GuideConfig.make(samplesPerFrame=1024, stepsPerFrame=1, tensorCores=True))
+    p = _join(*_params(3))
+    g.set_params(p)
+    n = 300
+    feat, _, _ = _inputs(n, 4)
+    tf = torch.from_numpy(feat).cuda()
+    to = torch.zeros((n, 40), dtype=torch.float32, device="cuda")
+    lib = G.load()
+    t0 = time.time()
+    ctx.check(lib.grisDebugGuideForwardStall(ctx.h, g.h, tf.data_ptr(), n, to.data_ptr()), "stall")
+    rc = lib.grisSync(ctx.h)
+    assert rc == -5, rc                              # GRIS_ERR_DEVICE_FAULT
+    assert time.time() - t0 < 10.0
+    c = ctx.counters(reset=True)
+    assert c[3] & 2
+    g.forward(tf.data_ptr(), n, to.data_ptr())       # the context is still usable
+    ctx.sync()
+    x = M.encode(feat[:, :3].astype(np.float64), feat[:, 3:6].astype(np.float64), feat[:, 6:9].astype(np.float64))
+    want = M.forward(*_split(p), x, quantize=True)[0][:, :40]
+    got = to.cpu().numpy().astype(np.float64)
+    assert np.median(np.abs(got - want)) < 1e-4 * np.abs(want).max()
+    assert ctx.counters()[3] == 0
+    g.close()
+    ctx.close()

@@ -208,6 +208,16 @@ int grisGuideForward(GrisContext* ctx, GrisGuide* g, const float* feat, uint32_t
     return GRIS_OK;
 }
 
+int grisDebugGuideForwardStall(GrisContext* ctx, GrisGuide* g, const float* feat, uint32_t n, float* out) {
+    if (!ctx || !g || !n || !feat || !out) return ctx_fail(ctx, GRIS_ERR_INVALID_ARGUMENT, "bad guide forward");
+    cudaSetDevice(ctx_device(ctx));
+    guide::FwdArgs a;
+    a.wPacked = g->wPacked; a.bias = g->bias; a.feat = feat; a.count = nullptr; a.n = n; a.out = out;
+    a.tensorCores = 1; a.err = ctx_counters(ctx) + GRIS_COUNTER_ERROR; a.withholdCommit = 1;
+    GUIDE_CK(ctx, guide::launch_forward(a, ctx_stream(ctx)));
+    return GRIS_OK;
+}
+
 int grisGuideGradient(GrisContext* ctx, GrisGuide* g, const float* feat, const float* dir, const float* weight, uint32_t n,
                       float* gradOut) {
     if (!ctx || !g || !gradOut || (n && (!feat || !dir || !weight)))

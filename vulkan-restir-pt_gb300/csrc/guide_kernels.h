@@ -18,6 +18,7 @@ struct FwdArgs {
     float* out;
     int tensorCores = 0;                /* 1: the tcgen05 kernel (guide_tc.cu), 0: mma.sync */
     unsigned long long* err = nullptr;  /* error word (bit 1: a tensor-core wait gave up) */
+    int withholdCommit = 0;             /* test of the bounded waits: the MMAs' completion is never signalled */
 };
 
 /* gradient of loss = -sum_i weight_i log p(dir_i | feat_i) / sum_i weight_i, added to grad */

@@ -36,7 +36,8 @@ namespace guide {
 constexpr int kTcRows = 128;                 /* vertices per group tile = MMA M */
 constexpr int kTcGroups = 2;                 /* independent groups (tiles in flight) per CTA */
 constexpr uint32_t kTmemCols = 64 * kTcGroups;   /* accumulator columns: 64 per group (N <= 64) */
-constexpr uint32_t kWaitLimit = 1u << 22;    /* mbarrier polls before the kernel gives up */
+constexpr uint64_t kWaitNs = 200000000ull;   /* a wait on the mbarrier gives up after 0.2 s */
+constexpr uint32_t kWaitPolls = 1u << 26;    /* and after this many polls in any case */
 
 /* byte offset of core matrix (row, k) inside a tile of K columns */
 __host__ __device__ constexpr uint32_t core_off(uint32_t row, uint32_t k, uint32_t K) {
@@ -87,10 +88,20 @@ __device__ __forceinline__ bool bar_try(uint32_t bar, uint32_t parity) {
                  : "=r"(ok) : "r"(bar), "r"(parity) : "memory");
     return ok != 0u;
 }
-/* bounded wait for the phase `parity` of the mbarrier; false: gave up */
+__device__ __forceinline__ uint64_t global_ns() {
+    uint64_t t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+/* bounded wait for the phase `parity` of the mbarrier (0.2 s of the global timer, or the poll
+ * limit); false: gave up */
 __device__ __forceinline__ bool bar_wait(uint32_t bar, uint32_t parity) {
-    for (uint32_t i = 0; i < kWaitLimit; i++)
+    if (bar_try(bar, parity)) return true;
+    const uint64_t t0 = global_ns();
+    for (uint32_t i = 1; i < kWaitPolls; i++) {
         if (bar_try(bar, parity)) return true;
+        if ((i & 255u) == 0u && global_ns() - t0 > kWaitNs) return false;
+    }
     return false;
 }
 __device__ __forceinline__ void tc_ld16(uint32_t taddr, uint32_t r[16]) {
@@ -200,7 +211,7 @@ __global__ void __launch_bounds__(kTcRows * kTcGroups, 2) k_guide_forward_tc(Fwd
                 for (uint32_t s = 0; s < K / 16u; s++)
                     tc_mma(tmem, tc_sdesc(aBase + s * 256u, 128u, (K / 8u) * 128u),
                            tc_sdesc(bBase + s * 256u, 128u, (K / 8u) * 128u), tc_idesc(N), s > 0u ? 1u : 0u);
-                tc_commit(bar);
+                if (!a.withholdCommit) tc_commit(bar);
             }
             if (!bar_wait(bar, phase)) {
                 sFail[grp] = 1u;

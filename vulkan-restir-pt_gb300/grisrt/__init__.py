@@ -214,7 +214,7 @@ EXPORTS = [
     "grisGuideCreate", "grisGuideDestroy", "grisGuideParamCount", "grisGuideSetParams", "grisGuideGetParams",
     "grisGuideSetTraining", "grisGuideForward", "grisGuideGradient", "grisGuideTrainStep", "grisBatchSetGuide",
     "grisHostSceneLoad", "grisHostSceneFilmSize", "grisSetWaveRefill", "grisPassDI", "grisFrameRenderDI",
-    "grisPostProcess", "grisWritePNG",
+    "grisPostProcess", "grisWritePNG", "grisDebugGuideForwardStall",
 ]
 
 _lib = None
@@ -282,6 +282,7 @@ def load(path=None):
         "grisGuideGetParams": (i32, [vp, vp, ctypes.c_size_t]),
         "grisGuideSetTraining": (i32, [vp, i32]),
         "grisGuideForward": (i32, [vp, vp, vp, u32, vp]),
+        "grisDebugGuideForwardStall": (i32, [vp, vp, vp, u32, vp]),
         "grisGuideGradient": (i32, [vp, vp, vp, vp, vp, u32, vp]),
         "grisGuideTrainStep": (i32, [vp, vp, vp, vp, vp, u32]),
         "grisBatchSetGuide": (i32, [vp, vp]),
