@@ -102,8 +102,43 @@ def make_di(name):
     return path
 
 
+# visual regression: name -> (kind, grid, spheres, W, H, frames, GRIS settings, DI settings)
+PNG_CASES = {
+    "post_box_48x32": (0, 0, 0, 48, 32, 4, dict(maxDepth=4), dict(sampleType=2, temporalReuse=True)),
+}
+
+
+def make_png(name):
+    """The renderer's frame with both passes (GRIS and ReSTIR DI from the reference's shaders run
+    as C++), presented by the oracle's post_proc.frag restatement (filmic, gamma, UNORM8) and
+    written with the library's PNG writer; the inputs go into <name>.npz beside the image."""
+    kind, grid, spheres, W, H, frames, kw, dkw = PNG_CASES[name]
+    G.load()
+    hs = G.HostScene(kind, seed=3, grid=grid, spheres=spheres)
+    cams, prevs = G.sequence_cameras(hs, frames, W, H, seed=29)
+    st, di, post = G.Settings.make(**kw), G.DISettings.make(**dkw), G.PostSettings.make()
+    gref, dref = O.reference(), O.reference_di()
+    gref.set_scene(hs)
+    dref.set_scene(hs)
+    ind = O.run_sequence(gref, cams, prevs, st, W, H, record=("out",))[-1]["out"]
+    dirr = O.run_di_sequence(gref, dref, cams, prevs, di, W, H, record=("out",))[-1]["out"]
+    _, rgba = O.post_process(W, H, dirr, ind, post)
+    G.write_png(os.path.join(HERE, name + ".png"), rgba, W, H)
+    np.savez_compressed(os.path.join(HERE, name + ".npz"), scene_sha256=np.array(scene_hash(hs)),
+                        settings=np.frombuffer(bytes(memoryview(st)), np.uint8),
+                        di_settings=np.frombuffer(bytes(memoryview(di)), np.uint8),
+                        post_settings=np.frombuffer(bytes(memoryview(post)), np.uint8),
+                        cams=np.stack([np.frombuffer(c.tobytes(), np.uint8) for c in cams]),
+                        prevs=np.stack([np.frombuffer(c.tobytes(), np.uint8) for c in prevs]),
+                        meta=np.array([kind, grid, spheres, W, H, frames], np.int64))
+    return os.path.join(HERE, name + ".png")
+
+
 if __name__ == "__main__":
     if not os.path.exists(O.REF_LIB) or not os.path.exists(O.DI_REF_LIB):
         sys.exit("oracle/_ref libraries missing: run oracle/ref/make_ref.py (needs the reference sources)")
-    for n in (sys.argv[1:] or list(CASES) + list(DI_CASES)):
+    for n in (sys.argv[1:] or list(CASES) + list(DI_CASES) + list(PNG_CASES)):
+        if n in PNG_CASES:
+            print(make_png(n), os.path.getsize(os.path.join(HERE, n + ".png")))
+            continue
         print(make_di(n) if n in DI_CASES else make(n), os.path.getsize(os.path.join(HERE, n + ".npz")))

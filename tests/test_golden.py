@@ -14,7 +14,8 @@ from oracle import pyoracle as O
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 ALL = sorted(glob.glob(os.path.join(HERE, "golden", "*.npz")))
-FILES = [p for p in ALL if not os.path.basename(p).startswith("di_")]
+FILES = [p for p in ALL if not os.path.basename(p).startswith(("di_", "post_"))]
+PNG_FILES = [p for p in ALL if os.path.basename(p).startswith("post_")]
 DI_FILES = [p for p in ALL if os.path.basename(p).startswith("di_")]
 BUFFERS = ("dn", "am", "mv", "resv", "temp", "out")
 DI_BUFFERS = ("resv", "temp", "out")
@@ -122,4 +123,71 @@ def test_gpu_reproduces_di_golden_vectors(path):
                     "out": fr.download(G.BUF_DIRECT_OUTPUT)})
     ctx.sync()
     check_di(z, res, ctx.counters(reset=True), frames)
+    fr.close(); scene.close(); ctx.close()
+
+
+def _png_pixels(path):
+    """RGBA bytes of a PNG written by grisWritePNG (stored deflate blocks, filter 0 rows)."""
+    import struct
+    import zlib
+    data = open(path, "rb").read()
+    pos, idat, W, H = 8, b"", 0, 0
+    while pos < len(data):
+        n, typ = struct.unpack(">I4s", data[pos:pos + 8])
+        body = data[pos + 8:pos + 8 + n]
+        if typ == b"IHDR":
+            W, H = struct.unpack(">II", body[:8])
+        elif typ == b"IDAT":
+            idat += body
+        pos += 12 + n
+    rows = np.frombuffer(zlib.decompress(idat), np.uint8).reshape(H, W * 4 + 1)
+    return rows[:, 1:].reshape(-1, 4), W, H
+
+
+def _png_case(path):
+    z = np.load(path)
+    kind, grid, spheres, W, H, frames = [int(x) for x in z["meta"]]
+    hs = G.HostScene(kind, seed=3, grid=grid, spheres=spheres)
+    h = hashlib.sha256()
+    for a in hs.arrays():
+        h.update(np.ascontiguousarray(a).tobytes())
+    assert h.hexdigest() == str(z["scene_sha256"])
+    cams = [G.Camera.from_buffer_copy(bytes(c)) for c in z["cams"]]
+    prevs = [G.Camera.from_buffer_copy(bytes(c)) for c in z["prevs"]]
+    return (hs, cams, prevs, G.Settings.from_buffer_copy(bytes(z["settings"])),
+            G.DISettings.from_buffer_copy(bytes(z["di_settings"])),
+            G.PostSettings.from_buffer_copy(bytes(z["post_settings"])), W, H)
+
+
+@pytest.mark.parametrize("path", PNG_FILES, ids=[os.path.basename(p)[:-4] for p in PNG_FILES])
+def test_oracle_reproduces_golden_image(path):
+    """Visual regression: the frame with both passes, presented, equals the committed image."""
+    want, W0, H0 = _png_pixels(path[:-4] + ".png")
+    hs, cams, prevs, st, di, post, W, H = _png_case(path)
+    assert (W, H) == (W0, H0)
+    ora = O.oracle()
+    ora.set_scene(hs)
+    ind = O.run_sequence(ora, cams, prevs, st, W, H, record=("out",))[-1]["out"]
+    dirr = O.run_di_sequence(ora, ora, cams, prevs, di, W, H, record=("out",))[-1]["out"]
+    _, rgba = O.post_process(W, H, dirr, ind, post)
+    assert rgba.tobytes() == want.tobytes()
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("path", PNG_FILES, ids=[os.path.basename(p)[:-4] for p in PNG_FILES])
+def test_gpu_reproduces_golden_image(path):
+    import torch
+    want, _, _ = _png_pixels(path[:-4] + ".png")
+    hs, cams, prevs, st, di, post, W, H = _png_case(path)
+    ctx = G.Context(0)
+    scene = G.Scene(ctx, hs)
+    fr = G.Frame(ctx, W, H)
+    for f in range(len(cams)):
+        fr.render_di(scene, cams[f], prevs[f], di, st)
+    dptr, _ = fr.device_ptr(G.BUF_DIRECT_OUTPUT)
+    iptr, _ = fr.device_ptr(G.BUF_OUTPUT)
+    dev = torch.zeros((W * H, 4), dtype=torch.uint8, device="cuda")
+    ctx.post_process(G.PostBindings(W, H, dptr, iptr, 0, dev.data_ptr()), post)
+    ctx.sync()
+    assert dev.cpu().numpy().tobytes() == want.tobytes()
     fr.close(); scene.close(); ctx.close()
