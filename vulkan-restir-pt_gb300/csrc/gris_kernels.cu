@@ -367,6 +367,11 @@ using PathTracer = PathTracerT<false>;
 
 /* ------------------------------------------------------------------ hybrid shift (gris_retrace.glsl) */
 /* traceReplayPathForHybridShift (:42-136) */
+/* evalBSDF as one out-of-line copy (arguments by value) for the reuse passes, which evaluate the
+ * BSDF at four sites: inlined there, the kernels' code outgrew the instruction cache (1080p C2:
+ * spatial 2.67 -> 2.41 ms, temporal 0.98 -> 0.96 ms out of line). */
+__device__ __noinline__ V3 evalBSDFCall(Mat mat, V3 albedo, V3 n, V3 wo, V3 wi) { return evalBSDF(mat, albedo, n, wo, wi); }
+
 GD void traceReplay(const PassCtx& P, Isec isec, Surf surf, Ray3 ray, uint32_t targetFlags, uint32_t rng, RcData& rcData,
                     RayCount& rc, int& err, const guide::Lobes* L = nullptr) {
     const DevScene& sc = P.sc;
@@ -479,9 +484,9 @@ GD Shift shiftToDomain(const PassCtx& P, const Surf& dstPrimarySurf, const Isec&
         if (!isnan(srcSample.rcPrevSamplePdf) && srcSample.rcPrevSamplePdf > 1e-6f) {
             Li = srcSample.rcLi;
             if (rcType == kRcSurface && length3(srcSample.rcWi) > 0.5f) {
-                Li = Li * (evalBSDF(rcMat, rcSurf.albedo, rcSurf.norm, -wi, srcSample.rcWi) * satDot(rcSurf.norm, srcSample.rcWi));
+                Li = Li * (evalBSDFCall(rcMat, rcSurf.albedo, rcSurf.norm, -wi, srcSample.rcWi) * satDot(rcSurf.norm, srcSample.rcWi));
             }
-            Li = Li * (evalBSDF(rcPrevMat, rcPrevSurf.albedo, rcPrevSurf.norm, dstRcData.rcPrevWo, wi) * satDot(rcPrevSurf.norm, wi));
+            Li = Li * (evalBSDFCall(rcPrevMat, rcPrevSurf.albedo, rcPrevSurf.norm, dstRcData.rcPrevWo, wi) * satDot(rcPrevSurf.norm, wi));
             Li = Li * dstRcData.rcPrevThroughput;
             Li = Li / srcSample.rcPrevSamplePdf;
             if (!isBlack(Li) && !isnan3(Li)) dstPHat = luminance(Li * jacobian);
@@ -547,9 +552,9 @@ GD void reuseAndMerge(const PassCtx& P, Resv& dstResv, const Surf& dstPrimarySur
         if (!isnan(srcSample.rcPrevSamplePdf) && srcSample.rcPrevSamplePdf > 1e-6f) {
             Li = srcSample.rcLi;
             if (rcType == kRcSurface && length3(srcSample.rcWi) > 0.5f) {
-                Li = Li * (evalBSDF(rcMat, rcSurf.albedo, rcSurf.norm, -wi, srcSample.rcWi) * satDot(rcSurf.norm, srcSample.rcWi));
+                Li = Li * (evalBSDFCall(rcMat, rcSurf.albedo, rcSurf.norm, -wi, srcSample.rcWi) * satDot(rcSurf.norm, srcSample.rcWi));
             }
-            Li = Li * (evalBSDF(rcPrevMat, rcPrevSurf.albedo, rcPrevSurf.norm, dstRcData.rcPrevWo, wi) * satDot(rcPrevSurf.norm, wi));
+            Li = Li * (evalBSDFCall(rcPrevMat, rcPrevSurf.albedo, rcPrevSurf.norm, dstRcData.rcPrevWo, wi) * satDot(rcPrevSurf.norm, wi));
             Li = Li * dstRcData.rcPrevThroughput;
             Li = Li / srcSample.rcPrevSamplePdf;
             if (!isBlack(Li) && !isnan3(Li)) dstPHat = luminance(Li * jacobian);
@@ -869,8 +874,8 @@ struct SpatialTaskT {
                     uint32_t rcType = rcVertexType(pathSample.flags);
                     V3 wi = normalize3(rcSurf.pos - rcPrevSurf.pos);
                     if (rcType == kRcSurface && length3(pathSample.rcWi) > 0.5f)
-                        Li = Li * (evalBSDF(rcMat, rcSurf.albedo, rcSurf.norm, -wi, pathSample.rcWi) * satDot(rcSurf.norm, pathSample.rcWi));
-                    Li = Li * (evalBSDF(rcPrevMat, rcPrevSurf.albedo, rcPrevSurf.norm, rcData.rcPrevWo, wi) * satDot(rcPrevSurf.norm, wi));
+                        Li = Li * (evalBSDFCall(rcMat, rcSurf.albedo, rcSurf.norm, -wi, pathSample.rcWi) * satDot(rcSurf.norm, pathSample.rcWi));
+                    Li = Li * (evalBSDFCall(rcPrevMat, rcPrevSurf.albedo, rcPrevSurf.norm, rcData.rcPrevWo, wi) * satDot(rcPrevSurf.norm, wi));
                     Li = Li * rcData.rcPrevThroughput;
                     Li = Li / pathSample.rcPrevSamplePdf;
                     if (!isBlack(Li) && !isnan3(Li)) radiance = Li / luminance(Li) * resv.resampleWeight / resv.sampleCount;
