@@ -370,7 +370,7 @@ using PathTracer = PathTracerT<false>;
 /* evalBSDF as one out-of-line copy (arguments by value) for the reuse passes, which evaluate the
  * BSDF at four sites: inlined there, the kernels' code outgrew the instruction cache (1080p C2:
  * spatial 2.67 -> 2.41 ms, temporal 0.98 -> 0.96 ms out of line). */
-__device__ __noinline__ V3 evalBSDFCall(Mat mat, V3 albedo, V3 n, V3 wo, V3 wi) { return evalBSDF(mat, albedo, n, wo, wi); }
+static __device__ __noinline__ V3 evalBSDFCall(Mat mat, V3 albedo, V3 n, V3 wo, V3 wi) { return evalBSDF(mat, albedo, n, wo, wi); }
 
 GD void traceReplay(const PassCtx& P, Isec isec, Surf surf, Ray3 ray, uint32_t targetFlags, uint32_t rng, RcData& rcData,
                     RayCount& rc, int& err, const guide::Lobes* L = nullptr) {
