@@ -87,8 +87,10 @@ GD void store_di(GrisDIReservoir* buf, uint64_t i, const DIResv& r) {
     p[3] = make_uint4(r.M, __float_as_uint(r.W), __float_as_uint(r.contrib), __float_as_uint(r.weight));
 }
 
-static __device__ __noinline__ V3 evalBSDFCall(Mat mat, V3 albedo, V3 n, V3 wo, V3 wi) { return evalBSDFCall(mat, albedo, n, wo, wi); }
-static __device__ __noinline__ float evalPdfCall(Mat mat, V3 n, V3 wo, V3 wi) { return evalPdfCall(mat, n, wo, wi); }
+/* The material functions as single out-of-line copies (arguments by value) for the DI passes,
+ * which call them at several sites per kernel. */
+static __device__ __noinline__ V3 evalBSDFCall(Mat mat, V3 albedo, V3 n, V3 wo, V3 wi) { return evalBSDF(mat, albedo, n, wo, wi); }
+static __device__ __noinline__ float evalPdfCall(Mat mat, V3 n, V3 wo, V3 wi) { return evalPdf(mat, n, wo, wi); }
 static __device__ __noinline__ bool sampleBSDFCall(Mat mat, V3 albedo, V3 n, V3 wo, V3 r, BsdfSample* s) { return sampleBSDF(mat, albedo, n, wo, r, *s); }
 
 /* sampleLi (di_reservoir.glsl:78-174): the light and / or BSDF candidate streamed into `resv`
