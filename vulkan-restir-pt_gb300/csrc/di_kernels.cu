@@ -87,12 +87,6 @@ GD void store_di(GrisDIReservoir* buf, uint64_t i, const DIResv& r) {
     p[3] = make_uint4(r.M, __float_as_uint(r.W), __float_as_uint(r.contrib), __float_as_uint(r.weight));
 }
 
-/* The material functions as single out-of-line copies (arguments by value) for the DI passes,
- * which call them at several sites per kernel. */
-static __device__ __noinline__ V3 evalBSDFCall(Mat mat, V3 albedo, V3 n, V3 wo, V3 wi) { return evalBSDF(mat, albedo, n, wo, wi); }
-static __device__ __noinline__ float evalPdfCall(Mat mat, V3 n, V3 wo, V3 wi) { return evalPdf(mat, n, wo, wi); }
-static __device__ __noinline__ bool sampleBSDFCall(Mat mat, V3 albedo, V3 n, V3 wo, V3 r, BsdfSample* s) { return sampleBSDF(mat, albedo, n, wo, r, *s); }
-
 /* sampleLi (di_reservoir.glsl:78-174): the light and / or BSDF candidate streamed into `resv`
  * (one draw of resvRng per candidate), then the chosen sample's Li scaled by W / w and M = 1.
  * The candidates' own colour sum is never used by the pass and is not formed. */
@@ -107,9 +101,9 @@ GD void di_sample_li(const DICtx& P, const Surf& surf, const Mat& mat, V3 wo, ui
         V3 Le = sampleLightByPower(P.sc, surf.pos, wi, dist, pdf, jac, bary, id, lr);
         bool shadowed = traceShadowCall(P.sc, surf.pos, kMinRayDistance, wi, dist - kMinRayDistance, rc, err);
         if (!shadowed && pdf > 1e-6f) {
-            float w = MISWeight(pdf, evalPdfCall(mat, surf.norm, wo, wi));
+            float w = MISWeight(pdf, evalPdf(mat, surf.norm, wo, wi));
             if (P.set.sampleType == GRIS_DI_SAMPLE_LIGHT) w = 1.0f;
-            V3 contrib = Le * evalBSDFCall(mat, surf.albedo, surf.norm, wo, wi) * satDot(surf.norm, wi) / pdf * w;
+            V3 contrib = Le * evalBSDF(mat, surf.albedo, surf.norm, wo, wi) * satDot(surf.norm, wi) / pdf * w;
             float sw = luminance(contrib);
             if (isnan(sw) || sw < 0.0f) sw = 0.0f;
             ps.isec.bx = bary.x; ps.isec.by = bary.y; ps.isec.inst = 0u; ps.isec.tri = id;
@@ -120,7 +114,7 @@ GD void di_sample_li(const DICtx& P, const Surf& surf, const Mat& mat, V3 wo, ui
     }
     ps.isLight = 0u;
     BsdfSample s = bs_zero();
-    if (P.set.sampleType != GRIS_DI_SAMPLE_LIGHT && sampleBSDFCall(mat, surf.albedo, surf.norm, wo, sr, &s) && s.pdf > 1e-6f) {
+    if (P.set.sampleType != GRIS_DI_SAMPLE_LIGHT && sampleBSDF(mat, surf.albedo, surf.norm, wo, sr, s) && s.pdf > 1e-6f) {
         Isec isec = traceClosestHitCall(P.sc, surf.pos, s.wi, kMinRayDistance, kMaxRayDistance, rc, err);
         if (isec.inst != kInvalidHit) {
             Surf hit = surf_zero();
@@ -165,7 +159,7 @@ GD void di_replay(const DICtx& P, DIResv& dst, const Surf& ds, const DIResv& src
         Surf rs = surf_zero();
         loadSurfaceInfo(P.sc, rr.s.isec, rs);
         V3 wi = normalize3(rs.pos - ds.pos);
-        V3 Li = rr.s.Li * evalBSDFCall(mat, ds.albedo, ds.norm, wo, wi) * satDot(ds.norm, wi) / rr.s.pdf;
+        V3 Li = rr.s.Li * evalBSDF(mat, ds.albedo, ds.norm, wo, wi) * satDot(ds.norm, wi) / rr.s.pdf;
         float pHat = luminance(Li * 1.0f);
         rr.W = src.W * pHat / src.weight;
         rr.M = src.M;
@@ -195,11 +189,11 @@ GD void di_reconnect(const DICtx& P, DIResv& dst, const Surf& ds, DIResv src, V3
             if (traceVisibility(P.sc, ds.pos, lv.pos, rc, err)) {
                 ok = true;
                 if (!isnan(ss.pdf) && ss.pdf > 1e-6f) {
-                    V3 Li = src.s.Li * evalBSDFCall(mat, ds.albedo, ds.norm, wo, wi) * satDot(ds.norm, wi) / ss.pdf;
+                    V3 Li = src.s.Li * evalBSDF(mat, ds.albedo, ds.norm, wo, wi) * satDot(ds.norm, wi) / ss.pdf;
                     pHat = luminance(Li * jac);
                 }
                 if (ss.isLight) dstPdf = luminance(lv.albedo) / load_table(P.sc, 0).prob / dstJac;
-                else dstPdf = evalPdfCall(mat, ds.norm, wo, wi);
+                else dstPdf = evalPdf(mat, ds.norm, wo, wi);
             }
         }
     }
@@ -350,7 +344,7 @@ __global__ void __launch_bounds__(128, 8) k_di_spatial(DICtx P) {
                 V3 wi = normalize3(ls.pos - px.surf.pos);
                 if (r.M > 0u) {
                     Mat mat = load_material(P.sc, px.surf.matIndex);
-                    V3 Li = r.s.Li * evalBSDFCall(mat, px.surf.albedo, px.surf.norm, wo, wi) * satDot(px.surf.norm, wi) / r.s.pdf;
+                    V3 Li = r.s.Li * evalBSDF(mat, px.surf.albedo, px.surf.norm, wo, wi) * satDot(px.surf.norm, wi) / r.s.pdf;
                     if (!isBlack(Li)) color = Li / luminance(Li) * r.W / (float)r.M;
                 }
             }
