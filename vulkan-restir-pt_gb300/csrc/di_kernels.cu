@@ -301,6 +301,89 @@ __global__ void __launch_bounds__(128, 8) k_di_temporal(DICtx P) {
     flush_counts(P.counters, rc, err, 5, P.countWork);
 }
 
+/* The spatial pass's neighbour loop under the reconnection shift (di_spatial.glsl:60-82 with
+ * di_reservoir.glsl:211-287), in three phases with the reference's results and draw order:
+ *   1. every neighbour's gather, gates and shift up to its visibility query, with the merge's
+ *      draw taken where the reference takes it (one per neighbour reaching the shift: a shifted
+ *      reservoir is always usable, its W being 0 when the shift fails);
+ *   2. the lane's visibility queries back to back (a warp walks max-over-lanes of the query
+ *      counts, not one walk per neighbour index with the lanes whose neighbour needs none idle);
+ *   3. the merges in neighbour order with the verdicts, and the chosen neighbour's reservoir
+ *      read again for its sample. */
+struct DINeighbour {
+    float Wv, u, jac, pdf;   /* W if visible; merge draw; Jacobian and pdf at the destination */
+    uint32_t M, q;           /* source M; source pixel */
+    V3 to;                   /* the light vertex the query looks at */
+};
+GD void di_spatial_reconnect(const DICtx& P, const DIPixel& px, V3 wo, uint32_t& rng, DIResv& r, RayCount& rc,
+                             int& err) {
+    const int W = (int)P.b.width, H = (int)P.b.height;
+    const uint64_t n = (uint64_t)W * (uint64_t)H;
+    const Surf& ds = px.surf;
+    const Mat mat = load_material(P.sc, ds.matIndex);
+    const float tx = 1.0f / (float)W, ty = 1.0f / (float)H;
+    DINeighbour nb[kDINeighbours];
+    uint32_t m = 0, queries = 0;
+    for (uint32_t k = 0; k < kDINeighbours; k++) {
+        V2 d = toConcentricDisk(sample2f(rng));
+        V2 uv = v2(px.uv.x + d.x * kDIRadius * tx, px.uv.y + d.y * kDIRadius * ty);
+        if (uv.x < 0.0f || uv.y < 0.0f || uv.x > 1.0f || uv.y > 1.0f) continue;
+        int qx = (int)(uv.x * (float)P.cam.w), qy = (int)(uv.y * (float)P.cam.h);
+        float ndepth = 0.0f; V3 nn = v3s(0.0f), nalb = v3s(0.0f); int nmm = 0;
+        float4 ndn = texture_bilinear(reinterpret_cast<const float4*>(P.b.depthNormal), W, H, uv);
+        uint2 nam = fetch_am(reinterpret_cast<const uint2*>(P.b.albedoMatId), W, H, qx, qy);
+        if (!unpackGBuffer(ndn, nam, ndepth, nn, nalb, nmm)) continue;
+        Ray3 nr = pinholeCameraSampleRay(P.cam, v2(uv.x, 1.0f - uv.y));
+        V3 npos = nr.ori + nr.dir * (ndepth - 1e-4f);
+        if (dot3(nn, ds.norm) < 0.9f || distance3(ds.pos, npos) > 0.4f) continue;
+        const uint32_t q = (uint32_t)P.cam.w * (uint32_t)qy + (uint32_t)qx;
+        DIResv src = load_di(P.b.reservoirTemp, (uint64_t)q, n);
+        if (!di_usable(src)) continue;
+        Surf lv = surf_zero();
+        loadSurfaceInfo(P.sc, src.s.isec, lv);
+        float dist = distance3(lv.pos, ds.pos);
+        V3 wi = normalize3(lv.pos - ds.pos);
+        float cosT = -dot3(lv.norm, wi);
+        float dstJac = fabsf(cosT) / square(dist);
+        float jac = dstJac / src.s.jac;
+        bool query = src.s.isec.inst != kInvalidHit && dist > 1e-4f && cosT > 0.0f && !isnan(jac) && src.s.jac > 0.0f;
+        float pHat = 0.0f, dstPdf = 0.0f, Wv = 0.0f;
+        if (query) {
+            if (!isnan(src.s.pdf) && src.s.pdf > 1e-6f) {
+                V3 Li = src.s.Li * evalBSDF(mat, ds.albedo, ds.norm, wo, wi) * satDot(ds.norm, wi) / src.s.pdf;
+                pHat = luminance(Li * jac);
+            }
+            if (src.s.isLight) dstPdf = luminance(lv.albedo) / load_table(P.sc, 0).prob / dstJac;
+            else dstPdf = evalPdf(mat, ds.norm, wo, wi);
+            if (dstPdf < 1e-6f || isnan(dstPdf)) dstPdf = 0.0f;
+            Wv = src.W * (pHat / src.weight);
+            if (isnan(Wv)) Wv = 0.0f;
+            queries |= 1u << m;
+        }
+        nb[m].Wv = Wv; nb[m].u = sample1f(rng); nb[m].jac = dstJac; nb[m].pdf = dstPdf;
+        nb[m].M = src.M; nb[m].q = q; nb[m].to = lv.pos;
+        m++;
+    }
+    uint32_t visible = 0u;
+    for (uint32_t pending = queries; pending; pending &= pending - 1u) {
+        const uint32_t i = (uint32_t)__ffs(pending) - 1u;
+        if (traceVisibility(P.sc, ds.pos, nb[i].to, rc, err)) visible |= 1u << i;
+    }
+    int sel = -1;
+    for (uint32_t i = 0; i < m; i++) {
+        const float w = (visible >> i) & 1u ? nb[i].Wv : 0.0f;
+        r.W += w;
+        r.M += nb[i].M;
+        if (nb[i].u * r.W < w) sel = (int)i;
+    }
+    if (sel >= 0) {
+        DIResv src = load_di(P.b.reservoirTemp, (uint64_t)nb[sel].q, n);
+        r.s = src.s;
+        r.weight = src.weight;
+        if ((visible >> sel) & 1u) { r.s.jac = nb[sel].jac; r.s.pdf = nb[sel].pdf; }
+    }
+}
+
 /* findNeighborReservoir (di_spatial.glsl:9-34) + spatialReuse (:36-121) + the running mean of
  * di_spatial.comp:21-26 (a background pixel accumulates black). */
 __global__ void __launch_bounds__(128, 8) k_di_spatial(DICtx P) {
@@ -316,7 +399,10 @@ __global__ void __launch_bounds__(128, 8) k_di_spatial(DICtx P) {
             uint32_t rng = makeSeed2(P.cam.seed, x, y) ^ 2u;
             V3 wo = -px.ray.dir;
             DIResv r = load_di(P.b.reservoirTemp, idx, n);
-            if (P.set.spatialReuse) {
+            if (P.set.spatialReuse && P.set.shiftType == GRIS_DI_SHIFT_RECONNECTION) {
+                di_spatial_reconnect(P, px, wo, rng, r, rc, err);
+                di_occlude(P, r, px.surf.pos, rc, err);
+            } else if (P.set.spatialReuse) {
                 float tx = 1.0f / (float)W, ty = 1.0f / (float)H;
                 for (uint32_t k = 0; k < kDINeighbours; k++) {
                     V2 d = toConcentricDisk(sample2f(rng));
