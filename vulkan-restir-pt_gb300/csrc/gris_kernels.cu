@@ -792,10 +792,158 @@ struct SpatialTaskT {
         return true;
     }
 
+    /* The neighbours under the reference's weights (misWeights = 0) in chunks of kChunk, each in
+     * three phases with the results and draw order of one step() per neighbour:
+     *   1. per neighbour: the gather and gates, the source reservoir, the replay and the shift up
+     *      to its visibility query (target, pdf, Jacobian, weight if visible), and the merge's
+     *      draw where reuseAndMerge takes it — always, unless the weight if visible is not a
+     *      valid weight, in which case the query is answered on the spot, as it decides the draw;
+     *   2. the lane's pending queries back to back (a warp walks max-over-lanes of the query
+     *      counts rather than one walk per neighbour index, most lanes having no query);
+     *   3. the merges and M caps in neighbour order with the verdicts. */
+    static constexpr uint32_t kChunk = 4;
+    struct Pending {
+        float rw, rnd, jac, pdf;   /* weight if visible; merge draw; the shifted sample's Jacobian and pdf */
+        float M;                   /* the source's sample count */
+        V3 F, from, to;            /* the shifted sample's F; the query's endpoints */
+        uint32_t nidx, state;      /* source pixel; kMerge | kQuery | kVisible */
+    };
+    static constexpr uint32_t kMerge = 1u, kQuery = 2u, kVisible = 4u;
+
+    GD void reuse_phased(const PassCtx& P, RayCount& rc, int& err) {
+        const DevScene& sc = P.sc;
+        const int W = (int)P.b.width, H = (int)P.b.height;
+        const uint64_t n = (uint64_t)W * (uint64_t)H;
+        const float tx = 1.0f / (float)W, ty = 1.0f / (float)H;
+        const V2 uv = v2(dstIsec.bx, dstIsec.by);
+        const guide::Lobes* Lp = nullptr;
+        guide::Lobes L;
+        if constexpr (kGuide) {
+            if (primary_lobes(P, idx, load_material(sc, dst.matIndex), L)) Lp = &L;
+        }
+        for (uint32_t base = 0; base < P.set.spatialNeighbors; base += kChunk) {
+            const uint32_t end = min(P.set.spatialNeighbors, base + kChunk);
+            Pending e[kChunk];
+            uint32_t m = 0, queries = 0;
+            for (uint32_t k = base; k < end; k++) {
+                V2 d = toConcentricDisk(sample2f(rng));
+                V2 nb = v2(uv.x + d.x * P.set.spatialRadius * tx, uv.y + d.y * P.set.spatialRadius * ty);
+                if (nb.x < 0.0f || nb.y < 0.0f || nb.x > 1.0f || nb.y > 1.0f) continue;
+                int px = (int)(nb.x * (float)P.cam.w), py = (int)(nb.y * (float)P.cam.h);
+                float depthN = 0.0f; V3 normalN = v3s(0.0f), albedoN = v3s(0.0f); int matMeshIdN = 0;
+                float4 ndn = texture_bilinear(reinterpret_cast<const float4*>(P.b.depthNormal), W, H, nb);
+                uint2 nam = fetch_am(reinterpret_cast<const uint2*>(P.b.albedoMatId), W, H, px, py);
+                if (!unpackGBuffer(ndn, nam, depthN, normalN, albedoN, matMeshIdN)) continue;
+                Ray3 nray = pinholeCameraSampleRay(P.cam, v2(nb.x, 1.0f - nb.y));
+                V3 posN = nray.ori + nray.dir * (depthN - 1e-4f);
+                if (dot3(normalN, dst.norm) < 0.9f || distance3(dst.pos, posN) > 0.4f) continue;
+                const uint32_t nidx = (uint32_t)P.cam.w * (uint32_t)py + (uint32_t)px;
+                const Resv src = load_resv(P.b.reservoirTemp, nidx, n);
+                if (!resvIsValid(src)) continue;
+                /* reuseAndMerge up to the visibility query */
+                const PathSample& s = src.s;
+                RcData rd;
+                rd.rcPrevIsec = isec_zero(); rd.rcPrevWo = v3s(0.0f); rd.rcPrevThroughput = v3s(0.0f);
+                Surf rcPrevSurf = surf_zero(), rcSurf = surf_zero();
+                Pending& q = e[m];
+                q.rw = 0.0f; q.jac = 0.0f; q.pdf = 0.0f; q.F = v3s(0.0f); q.nidx = nidx; q.state = 0u;
+                q.M = src.sampleCount;
+                bool query = false;
+                float dstJacobian = 0.0f, jacobian = 0.0f;
+                V3 wi = v3s(0.0f);
+                Mat rcMat = load_material(sc, 0xffffffffu), rcPrevMat = rcMat;
+                if (s.rcIsec.inst != kInvalidHit) {
+                    traceReplay(P, dstIsec, dst, ray, s.flags, s.primaryRng, rd, rc, err, Lp);
+                    if (rd.rcPrevIsec.inst != kInvalidHit) {
+                        if (rd.rcPrevIsec.inst == kSpecialHit) rcPrevSurf = dst;
+                        else loadSurfaceInfo(sc, rd.rcPrevIsec, rcPrevSurf);
+                        loadSurfaceInfo(sc, s.rcIsec, rcSurf);
+                        rcMat = load_material(sc, rcSurf.matIndex);
+                        rcPrevMat = load_material(sc, rcPrevSurf.matIndex);
+                        float dist = distance3(rcPrevSurf.pos, rcSurf.pos);
+                        wi = normalize3(rcSurf.pos - rcPrevSurf.pos);
+                        float cosTheta = -dot3(rcSurf.norm, wi);
+                        dstJacobian = fabsf(cosTheta) / square(dist);
+                        jacobian = dstJacobian / s.rcJacobian;
+                        query = dist > kDistanceThreshold && cosTheta > 0.0f && !isnan(jacobian) && s.rcJacobian > 0.0f &&
+                                isBSDFConnectible(rcPrevMat);
+                    }
+                }
+                bool merge = true;
+                if (query) {
+                    V3 Li = v3s(0.0f);
+                    float dstPHat = 0.0f, dstSamplePdf = 0.0f;
+                    uint32_t rcType = rcVertexType(s.flags);
+                    if (!isnan(s.rcPrevSamplePdf) && s.rcPrevSamplePdf > 1e-6f) {
+                        Li = s.rcLi;
+                        if (rcType == kRcSurface && length3(s.rcWi) > 0.5f) {
+                            Li = Li * (evalBSDFCall(rcMat, rcSurf.albedo, rcSurf.norm, -wi, s.rcWi) * satDot(rcSurf.norm, s.rcWi));
+                        }
+                        Li = Li * (evalBSDFCall(rcPrevMat, rcPrevSurf.albedo, rcPrevSurf.norm, rd.rcPrevWo, wi) * satDot(rcPrevSurf.norm, wi));
+                        Li = Li * rd.rcPrevThroughput;
+                        Li = Li / s.rcPrevSamplePdf;
+                        if (!isBlack(Li) && !isnan3(Li)) dstPHat = luminance(Li * jacobian);
+                        if (rcType == kRcLightSampled) {
+                            float sumPower = load_table(sc, 0).prob;
+                            dstSamplePdf = luminance(rcSurf.albedo) / sumPower / dstJacobian;
+                        } else {
+                            dstSamplePdf = evalPdf(rcPrevMat, rcPrevSurf.norm, rd.rcPrevWo, wi);
+                            if (Lp && rd.rcPrevIsec.inst == kSpecialHit)
+                                dstSamplePdf = P.gMix * guide::lobes_pdf(*Lp, wi.x, wi.y, wi.z) + (1.0f - P.gMix) * dstSamplePdf;
+                        }
+                    }
+                    float srcPHat = luminance(s.F);
+                    q.rw = src.resampleWeight * (dstPHat / srcPHat);
+                    q.jac = dstJacobian;
+                    q.pdf = (dstSamplePdf < 1e-6f || isnan(dstSamplePdf)) ? 0.0f : dstSamplePdf;
+                    q.F = Li;
+                    q.from = rcPrevSurf.pos; q.to = rcSurf.pos;
+                    if (!isnan(q.rw) && q.rw >= 0.0f) {
+                        q.state = kQuery;
+                        queries |= 1u << m;
+                    } else {   /* visible: an invalid weight, no merge and no draw; occluded: weight 0, merged */
+                        bool vis = traceVisibility(sc, q.from, q.to, rc, err);
+                        merge = !vis;
+                    }
+                }
+                if (merge) { q.state |= kMerge; q.rnd = sample1f(rng); }
+                m++;
+            }
+            for (uint32_t pending = queries; pending; pending &= pending - 1u) {
+                const uint32_t j = (uint32_t)__ffs(pending) - 1u;
+                if (traceVisibility(sc, e[j].from, e[j].to, rc, err)) e[j].state |= kVisible;
+            }
+            int sel = -1;
+            for (uint32_t j = 0; j < m; j++) {
+                if (e[j].state & kMerge) {
+                    const float w = (e[j].state & kVisible) ? e[j].rw : 0.0f;
+                    resv.sampleCount += e[j].M;
+                    resv.resampleWeight += w;
+                    if (e[j].rnd * resv.resampleWeight < w) sel = (int)j;
+                }
+                resvCap(resv, (float)P.set.cap);
+            }
+            if (sel >= 0) {
+                Resv src = load_resv(P.b.reservoirTemp, e[sel].nidx, n);
+                resv.s = src.s;
+                if (e[sel].state & kVisible) {
+                    resv.s.rcJacobian = e[sel].jac;
+                    resv.s.rcPrevSamplePdf = e[sel].pdf;
+                    resv.s.F = e[sel].F;
+                }
+            }
+        }
+    }
+
     GD bool step(const PassCtx& P, RayCount& rc, int& err) {
         const DevScene& sc = P.sc;
         const int W = (int)P.b.width, H = (int)P.b.height;
         const uint64_t n = (uint64_t)W * (uint64_t)H;
+        if (P.set.spatialReuse && i < P.set.spatialNeighbors && !(kPair && P.set.misWeights != 0u)) {
+            reuse_phased(P, rc, err);
+            i = P.set.spatialNeighbors;
+            return true;
+        }
         if (P.set.spatialReuse && i < P.set.spatialNeighbors) {
             i++;
             const float resampleRadius = P.set.spatialRadius;
