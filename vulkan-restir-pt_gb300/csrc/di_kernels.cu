@@ -303,27 +303,27 @@ __global__ void __launch_bounds__(128, 8) k_di_temporal(DICtx P) {
 
 /* The spatial pass's neighbour loop under the reconnection shift (di_spatial.glsl:60-82 with
  * di_reservoir.glsl:211-287), in three phases with the reference's results and draw order:
- *   1. every neighbour's gather, gates and shift up to its visibility query, with the merge's
- *      draw taken where the reference takes it (one per neighbour reaching the shift: a shifted
- *      reservoir is always usable, its W being 0 when the shift fails);
- *   2. the lane's visibility queries back to back (a warp walks max-over-lanes of the query
- *      counts, not one walk per neighbour index with the lanes whose neighbour needs none idle);
- *   3. the merges in neighbour order with the verdicts, and the chosen neighbour's reservoir
- *      read again for its sample. */
+ *   1. di_spatial_shift: every neighbour's gather, gates and shift up to its visibility query,
+ *      with the merge's draw taken where the reference takes it (one per neighbour reaching the
+ *      shift: a shifted reservoir is always usable, its W being 0 when the shift fails);
+ *   2. di_pooled_visibility: the warp's queries pooled and walked 32 at a time, one per lane
+ *      whichever pixel posted it (a warp walks ceil(queries / 32) times instead of once per
+ *      neighbour index with the lanes whose neighbour needs no query idle);
+ *   3. di_spatial_merge: the merges in neighbour order with the verdicts, and the chosen
+ *      neighbour's reservoir read again for its sample. */
 struct DINeighbour {
     float Wv, u, jac, pdf;   /* W if visible; merge draw; Jacobian and pdf at the destination */
     uint32_t M, q;           /* source M; source pixel */
     V3 to;                   /* the light vertex the query looks at */
 };
-GD void di_spatial_reconnect(const DICtx& P, const DIPixel& px, V3 wo, uint32_t& rng, DIResv& r, RayCount& rc,
-                             int& err) {
+GD void di_spatial_shift(const DICtx& P, const DIPixel& px, V3 wo, uint32_t& rng, DINeighbour* nb, uint32_t& m,
+                         uint32_t& queries) {
     const int W = (int)P.b.width, H = (int)P.b.height;
     const uint64_t n = (uint64_t)W * (uint64_t)H;
     const Surf& ds = px.surf;
     const Mat mat = load_material(P.sc, ds.matIndex);
     const float tx = 1.0f / (float)W, ty = 1.0f / (float)H;
-    DINeighbour nb[kDINeighbours];
-    uint32_t m = 0, queries = 0;
+    m = 0; queries = 0;
     for (uint32_t k = 0; k < kDINeighbours; k++) {
         V2 d = toConcentricDisk(sample2f(rng));
         V2 uv = v2(px.uv.x + d.x * kDIRadius * tx, px.uv.y + d.y * kDIRadius * ty);
@@ -364,11 +364,53 @@ GD void di_spatial_reconnect(const DICtx& P, const DIPixel& px, V3 wo, uint32_t&
         nb[m].M = src.M; nb[m].q = q; nb[m].to = lv.pos;
         m++;
     }
-    uint32_t visible = 0u;
-    for (uint32_t pending = queries; pending; pending &= pending - 1u) {
-        const uint32_t i = (uint32_t)__ffs(pending) - 1u;
-        if (traceVisibility(P.sc, ds.pos, nb[i].to, rc, err)) visible |= 1u << i;
+}
+
+/* Called by every lane of the warp (lanes without a pixel post no query): each lane posts its
+ * queries (from its pixel's position to a light vertex) in a per-warp list in shared memory, at
+ * the exclusive prefix of the lanes' query counts; the warp walks the list 32 entries per round
+ * and sets the verdict bits in the posting lane's word. Returns the lane's verdicts by query bit. */
+constexpr uint32_t kDIWarps = 4;   /* 128 threads per block */
+GD uint32_t di_pooled_visibility(const DICtx& P, V3 from, const DINeighbour* nb, uint32_t queries, RayCount& rc,
+                                 int& err) {
+    __shared__ float4 sFrom[kDIWarps][32];
+    __shared__ float4 sTo[kDIWarps][32];
+    __shared__ uint32_t sVerdict[kDIWarps][32];
+    const uint32_t t = threadIdx.y * blockDim.x + threadIdx.x, w = t >> 5, lane = t & 31u;
+    const uint32_t c = (uint32_t)__popc(queries);
+    uint32_t incl = c;
+    for (uint32_t d = 1; d < 32; d <<= 1) {
+        uint32_t v = __shfl_up_sync(0xffffffffu, incl, d);
+        if (lane >= d) incl += v;
     }
+    const uint32_t first = incl - c, total = __shfl_sync(0xffffffffu, incl, 31);
+    sFrom[w][lane] = make_float4(from.x, from.y, from.z, 0.0f);
+    sVerdict[w][lane] = 0u;
+    for (uint32_t base = 0; base < total; base += 32) {
+        __syncwarp();
+        if (first < base + 32 && first + c > base) {
+            uint32_t g = first;
+            for (uint32_t pending = queries; pending; pending &= pending - 1u, g++) {
+                if (g < base || g >= base + 32) continue;
+                const uint32_t i = (uint32_t)__ffs(pending) - 1u;
+                sTo[w][g - base] = make_float4(nb[i].to.x, nb[i].to.y, nb[i].to.z, __uint_as_float((lane << 4) | i));
+            }
+        }
+        __syncwarp();
+        if (base + lane < total) {
+            const float4 q = sTo[w][lane];
+            const uint32_t tag = __float_as_uint(q.w), owner = tag >> 4;
+            const float4 f = sFrom[w][owner];
+            if (traceVisibility(P.sc, v3(f.x, f.y, f.z), v3(q.x, q.y, q.z), rc, err))
+                atomicOr(&sVerdict[w][owner], 1u << (tag & 15u));
+        }
+    }
+    __syncwarp();
+    return sVerdict[w][lane];
+}
+
+GD void di_spatial_merge(const DICtx& P, const DINeighbour* nb, uint32_t m, uint32_t visible, DIResv& r) {
+    const uint64_t n = (uint64_t)P.b.width * (uint64_t)P.b.height;
     int sel = -1;
     for (uint32_t i = 0; i < m; i++) {
         const float w = (visible >> i) & 1u ? nb[i].Wv : 0.0f;
@@ -385,57 +427,71 @@ GD void di_spatial_reconnect(const DICtx& P, const DIPixel& px, V3 wo, uint32_t&
 }
 
 /* findNeighborReservoir (di_spatial.glsl:9-34) + spatialReuse (:36-121) + the running mean of
- * di_spatial.comp:21-26 (a background pixel accumulates black). */
+ * di_spatial.comp:21-26 (a background pixel accumulates black). Every lane of a warp reaches the
+ * pooled visibility phase (the block is 16 x 8, whole warps, lanes outside the image included). */
 __global__ void __launch_bounds__(128, 8) k_di_spatial(DICtx P) {
     RayCount rc = ray_count();
     int err = 0;
-    uint32_t x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y * blockDim.y + threadIdx.y;
-    if (x < P.b.width && y < P.b.height) {
-        const int W = (int)P.b.width, H = (int)P.b.height;
-        const uint64_t n = (uint64_t)W * (uint64_t)H, idx = (uint64_t)y * W + x;
-        V3 color = v3s(0.0f);
-        DIPixel px;
-        if (di_pixel(P, x, y, px)) {
-            uint32_t rng = makeSeed2(P.cam.seed, x, y) ^ 2u;
-            V3 wo = -px.ray.dir;
-            DIResv r = load_di(P.b.reservoirTemp, idx, n);
-            if (P.set.spatialReuse && P.set.shiftType == GRIS_DI_SHIFT_RECONNECTION) {
-                di_spatial_reconnect(P, px, wo, rng, r, rc, err);
-                di_occlude(P, r, px.surf.pos, rc, err);
-            } else if (P.set.spatialReuse) {
-                float tx = 1.0f / (float)W, ty = 1.0f / (float)H;
-                for (uint32_t k = 0; k < kDINeighbours; k++) {
-                    V2 d = toConcentricDisk(sample2f(rng));
-                    V2 nb = v2(px.uv.x + d.x * kDIRadius * tx, px.uv.y + d.y * kDIRadius * ty);
-                    if (nb.x < 0.0f || nb.y < 0.0f || nb.x > 1.0f || nb.y > 1.0f) continue;
-                    int qx = (int)(nb.x * (float)P.cam.w), qy = (int)(nb.y * (float)P.cam.h);
-                    float ndepth = 0.0f; V3 nn = v3s(0.0f), nalb = v3s(0.0f); int nmm = 0;
-                    float4 ndn = texture_bilinear(reinterpret_cast<const float4*>(P.b.depthNormal), W, H, nb);
-                    uint2 nam = fetch_am(reinterpret_cast<const uint2*>(P.b.albedoMatId), W, H, qx, qy);
-                    if (!unpackGBuffer(ndn, nam, ndepth, nn, nalb, nmm)) continue;
-                    Ray3 nr = pinholeCameraSampleRay(P.cam, v2(nb.x, 1.0f - nb.y));
-                    V3 npos = nr.ori + nr.dir * (ndepth - 1e-4f);
-                    if (dot3(nn, px.surf.norm) < 0.9f || distance3(px.surf.pos, npos) > 0.4f) continue;
-                    DIResv src = load_di(P.b.reservoirTemp, (uint64_t)((uint32_t)P.cam.w * (uint32_t)qy + (uint32_t)qx), n);
-                    if (di_usable(src)) di_reuse(P, r, px.surf, src, wo, rng, rc, err);
-                }
-                di_occlude(P, r, px.surf.pos, rc, err);
+    const uint32_t x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y * blockDim.y + threadIdx.y;
+    const int W = (int)P.b.width, H = (int)P.b.height;
+    const uint64_t n = (uint64_t)W * (uint64_t)H, idx = (uint64_t)y * W + x;
+    const bool inside = x < P.b.width && y < P.b.height;
+    const bool phased = P.set.spatialReuse && P.set.shiftType == GRIS_DI_SHIFT_RECONNECTION;
+    DIPixel px;
+    const bool fg = inside && di_pixel(P, x, y, px);
+    uint32_t rng = 0u;
+    V3 wo = v3s(0.0f), from = v3s(0.0f);
+    DIResv r = di_zero();
+    DINeighbour nb[kDINeighbours];
+    uint32_t m = 0, queries = 0, visible = 0;
+    if (fg) {
+        rng = makeSeed2(P.cam.seed, x, y) ^ 2u;
+        wo = -px.ray.dir;
+        from = px.surf.pos;
+        r = load_di(P.b.reservoirTemp, idx, n);
+        if (phased) di_spatial_shift(P, px, wo, rng, nb, m, queries);
+    }
+    if (phased) visible = di_pooled_visibility(P, from, nb, queries, rc, err);
+    V3 color = v3s(0.0f);
+    if (fg) {
+        if (phased) {
+            di_spatial_merge(P, nb, m, visible, r);
+            di_occlude(P, r, px.surf.pos, rc, err);
+        } else if (P.set.spatialReuse) {
+            float tx = 1.0f / (float)W, ty = 1.0f / (float)H;
+            for (uint32_t k = 0; k < kDINeighbours; k++) {
+                V2 d = toConcentricDisk(sample2f(rng));
+                V2 nuv = v2(px.uv.x + d.x * kDIRadius * tx, px.uv.y + d.y * kDIRadius * ty);
+                if (nuv.x < 0.0f || nuv.y < 0.0f || nuv.x > 1.0f || nuv.y > 1.0f) continue;
+                int qx = (int)(nuv.x * (float)P.cam.w), qy = (int)(nuv.y * (float)P.cam.h);
+                float ndepth = 0.0f; V3 nn = v3s(0.0f), nalb = v3s(0.0f); int nmm = 0;
+                float4 ndn = texture_bilinear(reinterpret_cast<const float4*>(P.b.depthNormal), W, H, nuv);
+                uint2 nam = fetch_am(reinterpret_cast<const uint2*>(P.b.albedoMatId), W, H, qx, qy);
+                if (!unpackGBuffer(ndn, nam, ndepth, nn, nalb, nmm)) continue;
+                Ray3 nr = pinholeCameraSampleRay(P.cam, v2(nuv.x, 1.0f - nuv.y));
+                V3 npos = nr.ori + nr.dir * (ndepth - 1e-4f);
+                if (dot3(nn, px.surf.norm) < 0.9f || distance3(px.surf.pos, npos) > 0.4f) continue;
+                DIResv src = load_di(P.b.reservoirTemp, (uint64_t)((uint32_t)P.cam.w * (uint32_t)qy + (uint32_t)qx), n);
+                if (di_usable(src)) di_reuse(P, r, px.surf, src, wo, rng, rc, err);
             }
-            di_cap(r, kDICap);
-            if (!di_usable(r)) di_clear(r);
-            store_di(P.b.reservoirThis, idx, r);
-            if (di_usable(r) && r.s.isec.inst != kInvalidHit) {
-                Surf ls = surf_zero();
-                loadSurfaceInfo(P.sc, r.s.isec, ls);
-                V3 wi = normalize3(ls.pos - px.surf.pos);
-                if (r.M > 0u) {
-                    Mat mat = load_material(P.sc, px.surf.matIndex);
-                    V3 Li = r.s.Li * evalBSDF(mat, px.surf.albedo, px.surf.norm, wo, wi) * satDot(px.surf.norm, wi) / r.s.pdf;
-                    if (!isBlack(Li)) color = Li / luminance(Li) * r.W / (float)r.M;
-                }
-            }
-            color = clampColor(color);
+            di_occlude(P, r, px.surf.pos, rc, err);
         }
+        di_cap(r, kDICap);
+        if (!di_usable(r)) di_clear(r);
+        store_di(P.b.reservoirThis, idx, r);
+        if (di_usable(r) && r.s.isec.inst != kInvalidHit) {
+            Surf ls = surf_zero();
+            loadSurfaceInfo(P.sc, r.s.isec, ls);
+            V3 wi = normalize3(ls.pos - px.surf.pos);
+            if (r.M > 0u) {
+                Mat mat = load_material(P.sc, px.surf.matIndex);
+                V3 Li = r.s.Li * evalBSDF(mat, px.surf.albedo, px.surf.norm, wo, wi) * satDot(px.surf.norm, wi) / r.s.pdf;
+                if (!isBlack(Li)) color = Li / luminance(Li) * r.W / (float)r.M;
+            }
+        }
+        color = clampColor(color);
+    }
+    if (inside) {
         float frameCount = (float)(P.cam.frameIndex & kCameraFrameIndexMask);
         float4* out = reinterpret_cast<float4*>(P.b.directOutput) + idx;
         float4 o = *out;
