@@ -835,6 +835,12 @@ def main():
     slots = (["gbuffer", "temporal", "spatial", "wave_begin", "wave_extend", "wave_shade", "wave_shadow", "wave_post"]
              if wave else ["gbuffer", "path_trace", "temporal", "spatial"])
     launches_per_frame = sum(prof[s]["launches"] for s in slots) / K
+    refill = (tune is not None and " refill" in tune["chosen"]) or (tune is None and bool(args.wave) and
+                                                                    args.wave.endswith("refill"))
+    if wave and refill:
+        # each timed extension / shadow level launches two kernels: the refilling walk of a full
+        # level and the one-ray-per-warp walk of a sparse level (one of them returns at once)
+        launches_per_frame += (prof["wave_extend"]["launches"] + prof["wave_shadow"]["launches"]) / K
 
     # ---------------- end to end through the C ABI with host buffers
     out_host = torch.empty((px * 4,), dtype=torch.float32, pin_memory=True)

@@ -20,6 +20,8 @@ CASES = [
     ("glossy_depth8", 2, 48, 60, 48, 40, 4, dict(maxDepth=8, spatialRadius=30.0)),
     ("glossy_rr", 2, 24, 30, 32, 24, 3, dict(maxDepth=12, rrScale=0.5, spatialNeighbors=5)),
     ("odd_size", 1, 32, 20, 37, 23, 3, dict(maxDepth=5)),
+    ("terrain_9nb_cap3", 1, 32, 40, 40, 30, 3, dict(maxDepth=6, spatialNeighbors=9, cap=3)),   # three chunks of neighbours
+    ("box_1nb", 0, 0, 0, 24, 16, 3, dict(maxDepth=4, spatialNeighbors=1)),
 ]
 
 
@@ -38,6 +40,7 @@ def ora():
 def gpu_sequence(ctx, hs, cams, prevs, st, W, H, mode=(G.PATH_WAVEFRONT, G.LAUNCH_GRID)):
     ctx.set_path_form(mode[0])
     ctx.set_launch_mode(mode[1])
+    ctx.set_wave_refill(len(mode) > 2 and mode[2])
     scene = G.Scene(ctx, hs)
     fr = G.Frame(ctx, W, H)
     ctx.counters(reset=True)
@@ -54,10 +57,12 @@ def gpu_sequence(ctx, hs, cams, prevs, st, W, H, mode=(G.PATH_WAVEFRONT, G.LAUNC
     return out, counters
 
 
-MODES = [(G.PATH_WAVEFRONT, G.LAUNCH_GRID), (G.PATH_MEGAKERNEL, G.LAUNCH_GRID), (G.PATH_MEGAKERNEL, G.LAUNCH_PERSISTENT)]
+MODES = [(G.PATH_WAVEFRONT, G.LAUNCH_GRID), (G.PATH_MEGAKERNEL, G.LAUNCH_GRID), (G.PATH_MEGAKERNEL, G.LAUNCH_PERSISTENT),
+         (G.PATH_WAVEFRONT, G.LAUNCH_GRID, True)]   # refilling wavefront: sparse levels walked one ray per warp
+MODE_IDS = ["wavefront", "megakernel-grid", "megakernel-persistent", "wavefront-refill"]
 
 
-@pytest.mark.parametrize("mode", MODES, ids=["wavefront", "megakernel-grid", "megakernel-persistent"])
+@pytest.mark.parametrize("mode", MODES, ids=MODE_IDS)
 @pytest.mark.parametrize("case", CASES, ids=[c[0] for c in CASES])
 def test_gpu_matches_oracle_bit_exact(case, mode, ctx, ora):
     name, kind, grid, spheres, W, H, frames, kw = case
@@ -67,6 +72,7 @@ def test_gpu_matches_oracle_bit_exact(case, mode, ctx, ora):
     got, gc = gpu_sequence(ctx, hs, cams, prevs, st, W, H, mode)
     ctx.set_path_form(G.PATH_WAVEFRONT)
     ctx.set_launch_mode(G.LAUNCH_GRID)
+    ctx.set_wave_refill(False)
     ora.set_scene(hs)
     ora.read_counters(reset=True)
     want = O.run_sequence(ora, cams, prevs, st, W, H)
@@ -93,7 +99,7 @@ PAIRWISE_CASES = [
 ]
 
 
-@pytest.mark.parametrize("mode", MODES, ids=["wavefront", "megakernel-grid", "megakernel-persistent"])
+@pytest.mark.parametrize("mode", MODES, ids=MODE_IDS)
 @pytest.mark.parametrize("case", PAIRWISE_CASES, ids=[c[0] for c in PAIRWISE_CASES])
 def test_gpu_pairwise_weights_match_oracle(case, mode, ctx, ora):
     """The pairwise MIS weights (GrisSettings.misWeights = 1, an extension with no counterpart in

@@ -1703,6 +1703,179 @@ __global__ void __launch_bounds__(128) k_wave_extend(WaveCtx C, int level) {
     flush_counts(C.counters, rc, err, 1, C.countWork, 0);
 }
 
+/* ---------------------------------------------------------------- sparse levels: one ray per warp */
+/* A level with fewer rays than kCoopMaxRays lasts as long as its longest walk (a lane per ray, one
+ * dependent node or triangle fetch after another). There the warp walks one ray at a time:
+ * each round takes up to 4 nodes off the warp's stack, 8 lanes per node test one child box each
+ * (the walker's own box test), the hit inner children are pushed, and the hit leaves' triangles
+ * are tested 32 at a time (the walker's triangle test, tmax = the best t so far) and reduced over
+ * the warp. The closest hit is the lexicographic minimum of (t, instanceIdx, triangleIdx) over
+ * the accepted triangles, and an any-hit query asks only whether one exists, so the order of the
+ * visits does not change a result: k_wave_trace_refill's results, bit for bit. */
+constexpr uint32_t kCoopMaxRays = 8192;
+constexpr uint32_t kCoopStack = 1024;      /* node indices per warp (pushes are at most 32 per round) */
+constexpr uint32_t kCoopTris = 96;         /* triangles per round: 4 nodes x 8 slots x 3 */
+constexpr uint32_t kCoopMaxRounds = 1u << 20;
+
+struct CoopHit { bool found; float t, u, v; uint32_t inst, tri; };
+
+template <bool ANY>
+GD CoopHit coop_walk(const uint32_t* __restrict__ nodes, const float* __restrict__ tris, float ox, float oy, float oz,
+                     float dx, float dy, float dz, float tmin, float tmax, uint32_t* stack, uint32_t* triList,
+                     RayCount& rc, int& err) {
+    const uint32_t lane = threadIdx.x & 31u;
+    const float tiny = 1e-30f;
+    const float idx = 1.0f / ((dx > tiny || dx < -tiny) ? dx : (dx < 0.0f ? -tiny : tiny));
+    const float idy = 1.0f / ((dy > tiny || dy < -tiny) ? dy : (dy < 0.0f ? -tiny : tiny));
+    const float idz = 1.0f / ((dz > tiny || dz < -tiny) ? dz : (dz < 0.0f ? -tiny : tiny));
+    CoopHit best;
+    best.found = false; best.t = tmax; best.u = 0.0f; best.v = 0.0f; best.inst = kInvalidHit; best.tri = kInvalidHit;
+    if (ox != ox || oy != oy || oz != oz || dx != dx || dy != dy || dz != dz) return best;   /* as GrisTraversal::init */
+    uint32_t sp = 1u;
+    if (lane == 0u) stack[0] = 0u;
+    __syncwarp();
+    for (uint32_t round = 0; sp > 0u; round++) {
+        if (round >= kCoopMaxRounds) { err = 1; break; }
+        const uint32_t p = min(sp, 4u), j = lane >> 3, s = lane & 7u;
+        bool inner = false;
+        uint32_t child = 0u, triCnt = 0u, triFirst = 0u;
+        if (j < p) {
+            const uint4* N = reinterpret_cast<const uint4*>(nodes + (uint64_t)stack[sp - 1u - j] * GRIS_NODE_WORDS);
+            const uint4 w0 = __ldg(N + 0), w1 = __ldg(N + 1), w2 = __ldg(N + 2), w3 = __ldg(N + 3), w4 = __ldg(N + 4);
+            const uint32_t W[20] = {w0.x, w0.y, w0.z, w0.w, w1.x, w1.y, w1.z, w1.w, w2.x, w2.y,
+                                    w2.z, w2.w, w3.x, w3.y, w3.z, w3.w, w4.x, w4.y, w4.z, w4.w};
+            const uint32_t meta = gris_byte(W[6 + (s >> 2)], (int)(s & 3u));
+            if (meta != 0u) {
+                const float px = gris_u2f(W[0]), py = gris_u2f(W[1]), pz = gris_u2f(W[2]);
+                const uint32_t e = W[3], imask = e >> 24;
+                const float sx = gris_u2f((e & 0xffu) << 23), sy = gris_u2f(((e >> 8) & 0xffu) << 23),
+                            sz = gris_u2f(((e >> 16) & 0xffu) << 23);
+                const float ax = sx * idx, ay = sy * idy, az = sz * idz;
+                const float bx = (px - ox) * idx, by = (py - oy) * idy, bz = (pz - oz) * idz;
+                const int wi = (int)(s >> 2), bi = (int)(s & 3u);
+                const float lx = gris_fma((float)gris_byte(W[8 + wi], bi), ax, bx);
+                const float ly = gris_fma((float)gris_byte(W[10 + wi], bi), ay, by);
+                const float lz = gris_fma((float)gris_byte(W[12 + wi], bi), az, bz);
+                const float hx = gris_fma((float)gris_byte(W[14 + wi], bi), ax, bx);
+                const float hy = gris_fma((float)gris_byte(W[16 + wi], bi), ay, by);
+                const float hz = gris_fma((float)gris_byte(W[18 + wi], bi), az, bz);
+                const float tn = gris_fmax(gris_fmax(gris_fmin(lx, hx), gris_fmin(ly, hy)), gris_fmax(gris_fmin(lz, hz), tmin));
+                const float tf = gris_fmin(gris_fmin(gris_fmax(lx, hx), gris_fmax(ly, hy)), gris_fmin(gris_fmax(lz, hz), best.t));
+                if (tn <= tf) {
+                    if (imask & (1u << s)) { inner = true; child = W[4] + (uint32_t)__popc(imask & ((1u << s) - 1u)); }
+                    else { triCnt = (meta >> 5) & 3u; triFirst = W[5] + (meta & 31u); }
+                }
+            }
+        }
+        if (lane == 0u) rc.work.nodes += p;
+        __syncwarp();                                     /* the popped entries are read before pushes */
+        sp -= p;
+        const unsigned im = __ballot_sync(0xffffffffu, inner);
+        const uint32_t nIn = (uint32_t)__popc(im);
+        if (sp + nIn > kCoopStack) {
+            err = 1;                                      /* not reached for trees the builder accepts */
+        } else {
+            if (inner) stack[sp + (uint32_t)__popc(im & ((1u << lane) - 1u))] = child;
+            sp += nIn;
+        }
+        uint32_t incl = triCnt;
+        for (uint32_t d = 1; d < 32; d <<= 1) {
+            const uint32_t v = __shfl_up_sync(0xffffffffu, incl, d);
+            if (lane >= d) incl += v;
+        }
+        const uint32_t total = __shfl_sync(0xffffffffu, incl, 31);
+        for (uint32_t k = 0; k < triCnt; k++) triList[incl - triCnt + k] = triFirst + k;
+        __syncwarp();
+        for (uint32_t base = 0; base < total; base += 32u) {
+            bool ok = false;
+            float t = 0.0f, u = 0.0f, v = 0.0f;
+            uint32_t inst = kInvalidHit, tri = kInvalidHit;
+            if (base + lane < total) {
+                const float4* T4 = reinterpret_cast<const float4*>(tris + (uint64_t)triList[base + lane] * GRIS_TRI_FLOATS);
+                const float4 t0 = __ldg(T4 + 0), t1 = __ldg(T4 + 1), t2 = __ldg(T4 + 2);
+                const float TT[12] = {t0.x, t0.y, t0.z, t0.w, t1.x, t1.y, t1.z, t1.w, t2.x, t2.y, t2.z, t2.w};
+                inst = gris_f2u(TT[3]); tri = gris_f2u(TT[7]);
+                rc.work.tris++;
+                ok = gris_tri_test(TT, ox, oy, oz, dx, dy, dz, tmin, best.t, &t, &u, &v);
+            }
+            if constexpr (ANY) {
+                if (__any_sync(0xffffffffu, ok)) { best.found = true; break; }
+                continue;
+            } else {
+            /* the warp's best accepted triangle by (t, instanceIdx, triangleIdx), in every lane */
+            for (uint32_t off = 16; off > 0; off >>= 1) {
+                const bool ok2 = __shfl_xor_sync(0xffffffffu, ok, off);
+                const float t2_ = __shfl_xor_sync(0xffffffffu, t, off), u2 = __shfl_xor_sync(0xffffffffu, u, off),
+                            v2 = __shfl_xor_sync(0xffffffffu, v, off);
+                const uint32_t i2 = __shfl_xor_sync(0xffffffffu, inst, off), r2 = __shfl_xor_sync(0xffffffffu, tri, off);
+                const bool take = ok2 && (!ok || t2_ < t || (t2_ == t && (i2 < inst || (i2 == inst && r2 < tri))));
+                if (take) { ok = true; t = t2_; u = u2; v = v2; inst = i2; tri = r2; }
+            }
+            if (ok) {
+                const bool keyLess = inst < best.inst || (inst == best.inst && tri < best.tri);
+                if (t < best.t || (t == best.t && keyLess)) {
+                    best.found = true; best.t = t; best.u = u; best.v = v; best.inst = inst; best.tri = tri;
+                }
+            }
+            }
+        }
+        if (ANY && best.found) break;
+        __syncwarp();                                     /* triList and the stack are rewritten next round */
+    }
+    return best;
+}
+
+template <bool ANY>
+__global__ void __launch_bounds__(128) k_wave_trace_coop(WaveCtx C, int level) {
+    const uint32_t n = ANY ? C.counts[256 + level] : C.counts[level];
+    if (n >= kCoopMaxRays) return;                        /* k_wave_trace_refill takes the level */
+    __shared__ uint32_t sStack[4][kCoopStack];
+    __shared__ uint32_t sTris[4][kCoopTris];
+    const uint32_t w = threadIdx.x >> 5, lane = threadIdx.x & 31u;
+    const uint32_t* q = ANY ? C.shadowQueue : C.queue[level & 1];
+    uint32_t* cursor = C.counts + (ANY ? 1280 : 1024) + level;
+    RayCount rc = ray_count();
+    int err = 0;
+    while (true) {
+        uint32_t i = 0u;
+        if (lane == 0u) i = atomicAdd(cursor, 1u);
+        i = __shfl_sync(0xffffffffu, i, 0);
+        if (i >= n) break;
+        const uint32_t id = q[i];
+        const int v = find_view_by_pixel(C.V, C.nViews, id);
+        float o[3], d[3], tmax;
+        if (ANY) {
+            const uint4* wv = C.nee[id].w;
+            const uint4 a = wv[0], d4 = wv[4], r3 = wv[3];
+            o[0] = __uint_as_float(a.x); o[1] = __uint_as_float(a.y); o[2] = __uint_as_float(a.z);
+            d[0] = __uint_as_float(d4.x); d[1] = __uint_as_float(d4.y); d[2] = __uint_as_float(d4.z);
+            tmax = __uint_as_float(r3.w) - kMinRayDistance;
+        } else {
+            const uint4* wv = C.state[id].w;
+            const uint4 a = wv[4], b = wv[5];
+            o[0] = __uint_as_float(a.x); o[1] = __uint_as_float(a.y); o[2] = __uint_as_float(a.z);
+            d[0] = __uint_as_float(b.x); d[1] = __uint_as_float(b.y); d[2] = __uint_as_float(b.z);
+            tmax = kMaxRayDistance;
+        }
+        const CoopHit h = coop_walk<ANY>(C.V[v].P.sc.nodes, C.V[v].P.sc.tris, o[0], o[1], o[2], d[0], d[1], d[2],
+                                         kMinRayDistance, tmax, sStack[w], sTris[w], rc, err);
+        if (lane == 0u) {
+            if (ANY) {
+                rc.shadow++;
+                C.blocked[id] = h.found ? 1 : 0;
+            } else {
+                rc.closest++;
+                Isec r;
+                if (h.found) { r.bx = h.u; r.by = h.v; r.inst = h.inst; r.tri = h.tri; }
+                else { r.bx = 0.0f; r.by = 0.0f; r.inst = kInvalidHit; r.tri = 0u; }
+                C.hit[id] = r;
+            }
+        }
+        __syncwarp();
+    }
+    flush_counts(C.counters, rc, err, 1, C.countWork, ANY ? 1 : 0);
+}
+
 /* The level's closest hits (ANY = false, the path queue) or shadow queries (ANY = true, the
  * shadow queue), resident form: every lane walks its own ray step by step, and whenever a quarter
  * of a warp's lanes are idle the warp takes that many rays from the queue (one atomic on the
@@ -1711,6 +1884,7 @@ __global__ void __launch_bounds__(128) k_wave_extend(WaveCtx C, int level) {
 template <bool ANY>
 __global__ void __launch_bounds__(128) k_wave_trace_refill(WaveCtx C, int level) {
     const uint32_t n = ANY ? C.counts[256 + level] : C.counts[level];
+    if (n < kCoopMaxRays) return;                         /* k_wave_trace_coop takes a sparse level */
     const uint32_t* q = ANY ? C.shadowQueue : C.queue[level & 1];
     uint32_t* cursor = C.counts + (ANY ? 1280 : 1024) + level;
     const uint32_t lane = threadIdx.x & 31u;
@@ -2124,6 +2298,7 @@ cudaError_t enqueue_batch(const BatchShape& sh, void* dViews, const void* hViews
             if (sm == 0) { int dev = 0; cudaGetDevice(&dev); cudaDeviceGetAttribute(&sm, cudaDevAttrMultiProcessorCount, dev); }
             const int gridShade = sm * (wl.shadeBlocksPerSM > 0 ? wl.shadeBlocksPerSM : 8);
             const int gridTrace = sm * (wl.traceBlocksPerSM > 0 ? wl.traceBlocksPerSM : 16);
+            const int gridCoop = sm * 4;   /* sparse levels: 4 blocks of 4 warps per SM, 17.9 KB shared each */
             /* timer slots 4..8: begin, extend, shade, shadow, post */
             auto mark = [&](int slot, bool begin) { if (timer) timer->mark(slot, begin, stream); };
             if (guide) {
@@ -2146,14 +2321,14 @@ cudaError_t enqueue_batch(const BatchShape& sh, void* dViews, const void* hViews
                 mark(4, false);
                 for (int level = 1; level < sh.maxDepth; level++) {
                     mark(5, true);
-                    if (wl.refill) k_wave_trace_refill<false><<<gridTrace, 128, 0, stream>>>(C, level);
+                    if (wl.refill) { k_wave_trace_refill<false><<<gridTrace, 128, 0, stream>>>(C, level); k_wave_trace_coop<false><<<gridCoop, 128, 0, stream>>>(C, level); }
                     else k_wave_extend<<<gridTrace, 128, 0, stream>>>(C, level);
                     mark(5, false);
                     mark(6, true);
                     k_gwave_shade<<<gridShade, 128, 0, stream>>>(C, level);
                     mark(6, false);
                     mark(7, true);
-                    if (wl.refill) k_wave_trace_refill<true><<<gridTrace, 128, 0, stream>>>(C, level);
+                    if (wl.refill) { k_wave_trace_refill<true><<<gridTrace, 128, 0, stream>>>(C, level); k_wave_trace_coop<true><<<gridCoop, 128, 0, stream>>>(C, level); }
                     else k_wave_shadow<<<gridTrace, 128, 0, stream>>>(C, level);
                     mark(7, false);
                     mark(9, true);
@@ -2176,14 +2351,14 @@ cudaError_t enqueue_batch(const BatchShape& sh, void* dViews, const void* hViews
             mark(4, false);
             for (int level = 1; level < sh.maxDepth; level++) {
                 mark(5, true);
-                if (wl.refill) k_wave_trace_refill<false><<<gridTrace, 128, 0, stream>>>(C, level);
+                if (wl.refill) { k_wave_trace_refill<false><<<gridTrace, 128, 0, stream>>>(C, level); k_wave_trace_coop<false><<<gridCoop, 128, 0, stream>>>(C, level); }
                 else k_wave_extend<<<gridTrace, 128, 0, stream>>>(C, level);
                 mark(5, false);
                 mark(6, true);
                 k_wave_shade<<<gridShade, 128, 0, stream>>>(C, level);
                 mark(6, false);
                 mark(7, true);
-                if (wl.refill) k_wave_trace_refill<true><<<gridTrace, 128, 0, stream>>>(C, level);
+                if (wl.refill) { k_wave_trace_refill<true><<<gridTrace, 128, 0, stream>>>(C, level); k_wave_trace_coop<true><<<gridCoop, 128, 0, stream>>>(C, level); }
                 else k_wave_shadow<<<gridTrace, 128, 0, stream>>>(C, level);
                 mark(7, false);
                 mark(8, true);
