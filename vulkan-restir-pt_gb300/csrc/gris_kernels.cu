@@ -11,6 +11,13 @@
  *
  * One thread per pixel, 16 x 8 pixel tiles; traversal is the 8-wide BVH walk of
  * bvh_traverse.h. Ray counts are accumulated per thread and added once per warp.
+ *
+ * Batches (k_batch_gbuffer, k_batch_pass) run the same tasks for many views per launch. Their
+ * path tracer can also run as a wavefront, one launch per stage and bounce level over compacted
+ * queues: k_wave_begin, then per level the closest hits (k_wave_extend, or k_wave_trace_refill
+ * for full levels + k_wave_trace_coop, one ray per warp, for levels under 8,192 rays),
+ * k_wave_shade, the shadow queries (k_wave_shadow, or the same refilling / one-ray-per-warp
+ * pair) and k_wave_post; k_gwave_* are the guided stages.
  */
 #include <cuda_fp16.h>
 #include <cuda_runtime.h>
