@@ -93,6 +93,17 @@ def alg_bytes(slot, w, px):
     return 0
 
 
+def kernel_launches_per_frame(prof, slots, frames, wavefront, refill):
+    """The library's kernel launches per frame from the per-slot launch counts of the profiled
+    pass. With the refilling wavefront each timed extension / shadow level launches two kernels
+    (the refilling walk of a full level and the one-ray-per-warp walk of a sparse level; one of
+    them returns at once) inside one timed slot."""
+    n = sum(prof[s]["launches"] for s in slots) / frames
+    if wavefront and refill:
+        n += (prof["wave_extend"]["launches"] + prof["wave_shadow"]["launches"]) / frames
+    return n
+
+
 def max_over_ranks(x, device):
     """The maximum of a per-rank scalar over the process group (x itself on one rank)."""
     import torch
@@ -840,13 +851,9 @@ def main():
     wave = config["path_form"] == "wavefront"
     slots = (["gbuffer", "temporal", "spatial", "wave_begin", "wave_extend", "wave_shade", "wave_shadow", "wave_post"]
              if wave else ["gbuffer", "path_trace", "temporal", "spatial"])
-    launches_per_frame = sum(prof[s]["launches"] for s in slots) / K
     refill = (tune is not None and " refill" in tune["chosen"]) or (tune is None and bool(args.wave) and
                                                                     args.wave.endswith("refill"))
-    if wave and refill:
-        # each timed extension / shadow level launches two kernels: the refilling walk of a full
-        # level and the one-ray-per-warp walk of a sparse level (one of them returns at once)
-        launches_per_frame += (prof["wave_extend"]["launches"] + prof["wave_shadow"]["launches"]) / K
+    launches_per_frame = kernel_launches_per_frame(prof, slots, K, wave, refill)
 
     # ---------------- end to end through the C ABI with host buffers
     out_host = torch.empty((px * 4,), dtype=torch.float32, pin_memory=True)
