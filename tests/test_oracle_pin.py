@@ -17,6 +17,8 @@ CASES = [
     ("terrain_depth8", 1, 40, 40, 40, 32, 3, dict(maxDepth=8, spatialRadius=30.0)),
     ("glossy_depth8", 2, 40, 40, 40, 32, 3, dict(maxDepth=8, spatialRadius=30.0)),
     ("glossy_rr", 2, 24, 30, 32, 24, 3, dict(maxDepth=12, rrScale=0.5, spatialNeighbors=5)),
+    ("terrain_9nb_cap3", 1, 32, 40, 40, 30, 3, dict(maxDepth=6, spatialNeighbors=9, cap=3)),
+    ("box_1nb", 0, 0, 0, 24, 16, 3, dict(maxDepth=4, spatialNeighbors=1)),
 ]
 
 
