@@ -31,6 +31,7 @@ CASES = {
     "terrain_24x20_d8": (1, 24, 12, 24, 20, 2, dict(maxDepth=8, spatialRadius=30.0), True),
     "glossy_24x20_d8": (2, 24, 12, 24, 20, 2, dict(maxDepth=8), True),
     "box_256x256_c1_8frames": (0, 0, 0, 256, 256, 8, dict(maxDepth=3, spatialRadius=30.0), False),
+    "terrain_32x24_9nb_cap3": (1, 32, 40, 32, 24, 3, dict(maxDepth=6, spatialNeighbors=9, cap=3), False),
 }
 DI_BUFFERS = ("resv", "temp", "out")
 # name: (kind, grid, spheres, W, H, frames, DI settings)
