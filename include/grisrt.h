@@ -410,7 +410,8 @@ int grisSetGraphs(GrisContext* ctx, int enable);
 /* Grid sizes of the wavefront kernels, in 128-thread blocks per SM (defaults 16 and 8). */
 int grisSetWaveLaunch(GrisContext* ctx, int traceBlocksPerSM, int shadeBlocksPerSM);
 /* 1: the wavefront's traversal kernels keep every lane busy (a lane whose ray is finished takes
- * the next ray while the others of its warp still walk); same results. */
+ * the next ray while the others of its warp still walk), and a bounce level with fewer than 8,192
+ * rays is walked one ray per warp (each round 4 nodes and up to 32 triangles); same results. */
 int grisSetWaveRefill(GrisContext* ctx, int enable);
 /* Times candidate configurations — the megakernel path tracer, the wavefront one with trace
  * grids of 8/16/32 and shading grids of 4/8/16 blocks per SM, and the wavefront one with the
