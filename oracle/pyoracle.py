@@ -17,6 +17,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 ORACLE_LIB = os.path.join(HERE, "_build", "liboracle.so")
 REF_LIB = os.path.join(HERE, "_ref", "libgrisref.so")
 DI_REF_LIB = os.path.join(HERE, "_ref", "libdiref.so")
+POST_REF_LIB = os.path.join(HERE, "_ref", "libpostref.so")
 
 
 class CpuImpl:
@@ -172,13 +173,22 @@ def run_sequence(impl, cams, prevs, settings, width, height, frames=None, record
     return results
 
 
-def post_process(W, H, direct, indirect, post_settings):
-    """The oracle's presentation pass: returns (float32 [H*W, 4] colour, uint8 [H*W, 4] RGBA)."""
-    from . import build_oracle
-    lib = ctypes.CDLL(build_oracle.build())
+def post_process(W, H, direct, indirect, post_settings, reference=False):
+    """The oracle's presentation pass: returns (float32 [H*W, 4] colour, uint8 [H*W, 4] RGBA).
+    reference=True: the reference's own post_proc.frag compiled as C++ (oracle/_ref/libpostref.so)
+    in its place, for the pin."""
     vp = ctypes.c_void_p
-    lib.oracle_post.argtypes = [ctypes.c_uint32, ctypes.c_uint32, vp, vp, vp, vp, vp]
-    lib.oracle_post.restype = None
+    if reference:
+        if not os.path.exists(POST_REF_LIB):
+            raise FileNotFoundError(POST_REF_LIB)
+        lib = ctypes.CDLL(POST_REF_LIB)
+        fn = lib.pref_post
+    else:
+        from . import build_oracle
+        lib = ctypes.CDLL(build_oracle.build())
+        fn = lib.oracle_post
+    fn.argtypes = [ctypes.c_uint32, ctypes.c_uint32, vp, vp, vp, vp, vp]
+    fn.restype = None
     n = W * H
     z = np.zeros((n, 4), np.float32)
     d = np.ascontiguousarray(direct if direct is not None else z, np.float32)
@@ -186,7 +196,7 @@ def post_process(W, H, direct, indirect, post_settings):
     sb = np.frombuffer(bytes(memoryview(post_settings)), np.uint32).copy()
     color = np.zeros((n, 4), np.float32)
     rgba = np.zeros((n, 4), np.uint8)
-    lib.oracle_post(W, H, _p(d), _p(i), _p(sb), _p(color), _p(rgba))
+    fn(W, H, _p(d), _p(i), _p(sb), _p(color), _p(rgba))
     return color, rgba
 
 

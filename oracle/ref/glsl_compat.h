@@ -18,12 +18,12 @@
  *   - dot(a,b) = (a.x*b.x + a.y*b.y) + a.z*b.z; normalize(v) = v * (1 / sqrt(dot(v,v)));
  *     mat*vec sums columns left to right; mix(x,y,a) = x*(1-a) + y*a (the GLSL spec form).
  *   - max/min follow IEEE maxNum/minNum (a NaN operand yields the other operand).
- *   - sin/cos/tan are the deterministic functions of oracle/detmath.h.
+ *   - sin/cos/tan/pow are the deterministic functions of oracle/detmath.h.
  *   - inverse(mat3) is the adjugate divided by the determinant.
  *   - texture(sampler2D, uv) is bilinear with REPEAT addressing and 8-bit sub-texel
  *     weights (the fixed-point weights hardware samplers use; this also makes a lookup
  *     at a texel centre return that texel exactly).
- *   - texelFetch outside the image and buffer reads past the end return zeros, writes
+ *   - texelFetch and imageLoad outside the image and buffer reads past the end return zeros, writes
  *     past the end are dropped (Vulkan robust access).
  */
 #ifndef GRIS_GLSL_COMPAT_H
@@ -135,6 +135,7 @@ inline vec3::vec3(const vec4& v) : x(v.x), y(v.y), z(v.z) {}
 GLSL_VEC2_OP(+) GLSL_VEC2_OP(-) GLSL_VEC2_OP(*) GLSL_VEC2_OP(/)
 GLSL_VEC3_OP(+) GLSL_VEC3_OP(-) GLSL_VEC3_OP(*) GLSL_VEC3_OP(/)
 GLSL_VEC4_OP(+) GLSL_VEC4_OP(-) GLSL_VEC4_OP(*) GLSL_VEC4_OP(/)
+inline ivec2 operator-(const ivec2& a, int b) { return ivec2(a.x - b, a.y - b); }
 inline vec2 operator-(const vec2& a) { return vec2(-a.x, -a.y); }
 inline vec3 operator-(const vec3& a) { return vec3(-a.x, -a.y, -a.z); }
 inline vec4 operator-(const vec4& a) { return vec4(-a.x, -a.y, -a.z, -a.w); }
@@ -175,6 +176,9 @@ inline float tan(float x) { return oracle_det_tanf(x); }
 inline float asin(float x) { return __builtin_asinf(x); }
 inline float atan(float y, float x) { return __builtin_atan2f(y, x); }
 inline float radians(float deg) { return deg * 0.01745329251994329577f; }
+/* pow is implementation-defined in GLSL: here the deterministic oracle_det_powf of detmath.h */
+inline float pow(float x, float y) { return oracle_det_powf(x, y); }
+inline vec3 pow(const vec3& x, const vec3& y) { return vec3(pow(x.x, y.x), pow(x.y, y.y), pow(x.z, y.z)); }
 inline bool isnan(float x) { return __builtin_isnan(x); }
 inline bool isinf(float x) { return __builtin_isinf(x); }
 inline float mix(float x, float y, float a) { return x * (1.0f - a) + y * a; }
@@ -246,7 +250,7 @@ struct usampler2D {            /* RG32UI */
     const uint* data = nullptr;
     int w = 0, h = 0;
 };
-struct image2D { float* data = nullptr; int w = 0, h = 0; };
+struct image2D { float* data = nullptr; int w = 0, h = 0; };   /* RGBA32F */
 struct accelerationStructureEXT { int unused = 0; };
 
 inline vec4 glsl_texel(const sampler2D& s, int x, int y) {
@@ -259,6 +263,12 @@ inline uvec4 texelFetch(const usampler2D& s, const ivec2& p, int) {
     if (p.x < 0 || p.y < 0 || p.x >= s.w || p.y >= s.h || !s.data) return uvec4(0, 0, 0, 0);
     const uint* q = s.data + ((size_t)p.y * s.w + p.x) * 2;
     return uvec4(q[0], q[1], 0, 1);
+}
+inline ivec2 textureSize(const sampler2D& s, int) { return ivec2(s.w, s.h); }
+inline vec4 imageLoad(const image2D& im, const ivec2& p) {
+    if (p.x < 0 || p.y < 0 || p.x >= im.w || p.y >= im.h || !im.data) return vec4(0.0f);
+    const float* q = im.data + ((size_t)p.y * im.w + p.x) * 4;
+    return vec4(q[0], q[1], q[2], q[3]);
 }
 inline int glsl_wrap(int i, int n) { int r = i % n; return r < 0 ? r + n : r; }
 inline vec4 texture(const sampler2D& s, const vec2& uv) {

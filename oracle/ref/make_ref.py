@@ -1,6 +1,6 @@
 #!/usr/bin/env python3
-"""Build oracle/_ref/libgrisref.so and libdiref.so: the reference's own GRIS and ReSTIR DI
-shader code, compiled as C++.
+"""Build oracle/_ref/libgrisref.so, libdiref.so and libpostref.so: the reference's own GRIS,
+ReSTIR DI and presentation (post_proc.frag) shader code, compiled as C++.
 
 TEST INFRASTRUCTURE (oracle). The output is the pinning reference for the oracle
 restatement; it is never part of the product and never travels as source.
@@ -14,7 +14,8 @@ Recipe
    - HostDevice.h: take the shader-side branch of its `#ifdef __cplusplus`.
    - `layout(...) uniform|buffer _Block { members };` -> the members as globals, an
      unsized array `T a[];` becoming `GBuf<T> a;` (a bounds-checked buffer view);
-     `layout(...) uniform sampler2D x;` -> `sampler2D x;`.
+     `layout(...) uniform sampler2D x;` -> `sampler2D x;`; a fragment shader's
+     `layout(location = n) in|out T x;` -> the global `T x;`.
    - `out T x` / `inout T x` parameters -> `T& x`.
    - swizzles .xy .zw .yz .xyz .yzw .rgb -> accessor calls returning references.
    - vector constructors whose arguments draw random numbers (`sampleNf(...)`) use
@@ -25,12 +26,15 @@ Recipe
      parameters whose defaults are the reference's values.
 3. Compile oracle/ref/alias_ref.cpp against the reference's src/util/AliasTable.h (plain
    C++, used as is) into oracle/_ref/libaliasref.so.
-4. Compile oracle/ref/ref_harness.cpp (the GRIS pass) and oracle/ref/ref_harness_di.cpp
-   (the ReSTIR DI pass), each including the rewritten shaders after glsl_compat.h and
-   ref_common.h, with g++ -std=c++20 -fsingle-precision-constant -ffp-contract=off
-   -ftrivial-auto-var-init=zero -fopenmp, into oracle/_ref/libgrisref.so and libdiref.so.
+4. Compile oracle/ref/ref_harness.cpp (the GRIS pass), oracle/ref/ref_harness_di.cpp
+   (the ReSTIR DI pass) and oracle/ref/ref_harness_post.cpp (the presentation pass), each
+   including the rewritten shaders after glsl_compat.h and ref_common.h, with g++ -std=c++20
+   -fsingle-precision-constant -ffp-contract=off -ftrivial-auto-var-init=zero -fopenmp, into
+   oracle/_ref/libgrisref.so, libdiref.so and libpostref.so.
 
 Usage: python oracle/ref/make_ref.py [--reference DIR] [--out DIR]
+The reference sources are looked up in --reference, else $GRIS_REFERENCE, else the checkout
+location below; where none holds them the recipe builds nothing and exits with status 2.
 """
 import argparse
 import os
@@ -48,6 +52,7 @@ SHADERS = [
     "gris_reservoir.glsl", "gris_path_trace.glsl", "gris_retrace.glsl",
     "gris_resample_temporal.glsl", "gris_resample_spatial.glsl", "gi_naive.glsl",
     "di_reservoir.glsl", "di_path_gen.glsl", "di_temporal.glsl", "di_spatial.glsl",
+    "post_proc.frag",
 ]
 
 
@@ -77,6 +82,7 @@ def _rewrite_decl(decl):
             am = re.match(r"^(\w+)\s+(\w+)\s*\[\s*\]$", m)
             out.append("GBuf<%s> %s;" % (am.group(1), am.group(2)) if am else m + ";")
         return "\n".join(out)
+    decl = re.sub(r"^(in|out)\s+", "", decl)   # a fragment shader's interface variable -> a global
     am = re.match(r"^(\w+)\s+(\w+)\s*\[\s*\]\s*;$", decl)
     if am:
         return "GBuf<%s> %s;" % (am.group(1), am.group(2))
@@ -161,12 +167,12 @@ def main():
     for name in SHADERS:
         with open(os.path.join(shader_dir, name), "rb") as f:
             h.update(f.read())
-    for name in ("ref_harness.cpp", "ref_harness_di.cpp", "ref_common.h", "glsl_compat.h", "alias_ref.cpp",
-                 "make_ref.py", "../detmath.h"):
+    for name in ("ref_harness.cpp", "ref_harness_di.cpp", "ref_harness_post.cpp", "ref_common.h", "glsl_compat.h",
+                 "alias_ref.cpp", "make_ref.py", "../detmath.h"):
         with open(os.path.join(HERE, name), "rb") as f:
             h.update(f.read())
     stamp = os.path.join(args.out, "stamp")
-    outputs = [os.path.join(args.out, n) for n in ("libgrisref.so", "libdiref.so", "libaliasref.so")]
+    outputs = [os.path.join(args.out, n) for n in ("libgrisref.so", "libdiref.so", "libpostref.so", "libaliasref.so")]
     if "--force" not in sys.argv and all(os.path.exists(o) for o in outputs) and os.path.exists(stamp):
         with open(stamp) as f:
             if f.read() == h.hexdigest():
@@ -178,10 +184,11 @@ def main():
             f.write(rewrite(name, src))
     so = os.path.join(args.out, "libgrisref.so")
     di = os.path.join(args.out, "libdiref.so")
+    post = os.path.join(args.out, "libpostref.so")
     flags = [args.cxx, "-std=c++20", "-O2", "-fPIC", "-shared", "-fopenmp", "-Wl,-Bsymbolic",
              "-fsingle-precision-constant", "-ffp-contract=off", "-ftrivial-auto-var-init=zero",
              "-fno-strict-aliasing", "-Wno-unknown-pragmas", "-Wno-div-by-zero", "-I", gdir, "-I", HERE]
-    for src, out in (("ref_harness.cpp", so), ("ref_harness_di.cpp", di)):
+    for src, out in (("ref_harness.cpp", so), ("ref_harness_di.cpp", di), ("ref_harness_post.cpp", post)):
         r = subprocess.run(flags + [os.path.join(HERE, src), "-o", out])
         if r.returncode != 0:
             return r.returncode
@@ -194,6 +201,7 @@ def main():
         f.write(h.hexdigest())
     print(so)
     print(di)
+    print(post)
     print(alias)
     return 0
 

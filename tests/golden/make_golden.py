@@ -111,7 +111,7 @@ PNG_CASES = {
 
 def make_png(name):
     """The renderer's frame with both passes (GRIS and ReSTIR DI from the reference's shaders run
-    as C++), presented by the oracle's post_proc.frag restatement (filmic, gamma, UNORM8) and
+    as C++), presented by the reference's post_proc.frag run as C++ (filmic, gamma, UNORM8) and
     written with the library's PNG writer; the inputs go into <name>.npz beside the image."""
     kind, grid, spheres, W, H, frames, kw, dkw = PNG_CASES[name]
     G.load()
@@ -123,7 +123,7 @@ def make_png(name):
     dref.set_scene(hs)
     ind = O.run_sequence(gref, cams, prevs, st, W, H, record=("out",))[-1]["out"]
     dirr = O.run_di_sequence(gref, dref, cams, prevs, di, W, H, record=("out",))[-1]["out"]
-    _, rgba = O.post_process(W, H, dirr, ind, post)
+    _, rgba = O.post_process(W, H, dirr, ind, post, reference=True)
     G.write_png(os.path.join(HERE, name + ".png"), rgba, W, H)
     np.savez_compressed(os.path.join(HERE, name + ".npz"), scene_sha256=np.array(scene_hash(hs)),
                         settings=np.frombuffer(bytes(memoryview(st)), np.uint8),
@@ -136,7 +136,7 @@ def make_png(name):
 
 
 if __name__ == "__main__":
-    if not os.path.exists(O.REF_LIB) or not os.path.exists(O.DI_REF_LIB):
+    if not all(os.path.exists(p) for p in (O.REF_LIB, O.DI_REF_LIB, O.POST_REF_LIB)):
         sys.exit("oracle/_ref libraries missing: run oracle/ref/make_ref.py (needs the reference sources)")
     for n in (sys.argv[1:] or list(CASES) + list(DI_CASES) + list(PNG_CASES)):
         if n in PNG_CASES:

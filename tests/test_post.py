@@ -1,7 +1,9 @@
 """The presentation pass (post_proc.frag:16-44 as grisPostProcess) and the headless PNG writer:
-the oracle's pass against a float64 numpy restatement of the shader (tone curves, gamma,
+the oracle's pass against the reference's own post_proc.frag compiled as C++ (oracle/_ref,
+byte for byte) and against a float64 numpy restatement of the shader (tone curves, gamma,
 composition flags, the fragment shader's texel mapping), the library's PNG files decoded with
 zlib, and on the GPU the kernel against the oracle bit for bit (colour and bytes)."""
+import os
 import struct
 import zlib
 
@@ -64,6 +66,24 @@ def test_oracle_post_matches_numpy(kw):
     wb = np.where(ok, np.clip(np.nan_to_num(want, nan=0.0), 0, 1) * 255.0, 0.0)
     assert np.abs(rgba[:, :3].astype(np.float64) - wb).max() <= 0.5 + 1e-3
     assert np.all(rgba[5, :3] == 0) or kw.get("noDirect")
+
+
+@pytest.mark.parametrize("kw", SETTINGS, ids=["defaults", "none", "aces", "no_gamma", "no_direct", "aces_no_indirect"])
+@pytest.mark.parametrize("size", [(37, 23), (64, 1), (1, 9), (130, 77)], ids=["37x23", "64x1", "1x9", "130x77"])
+def test_oracle_post_matches_compiled_reference(kw, size):
+    """The oracle's presentation pass against post_proc.frag itself (compiled as C++ by
+    oracle/ref/make_ref.py, run per fragment of the full-screen quad): the fragment colours
+    (NaN channels as the canonical quiet NaN) and their UNORM8 bytes, byte for byte, over images
+    with zeros, very bright texels, NaN radiance and odd sizes (texel mapping ivec2((size-1) uv))."""
+    if not os.path.exists(O.POST_REF_LIB):
+        pytest.skip("oracle/_ref not built (reference sources absent)")
+    W, H = size
+    d, i = _images(W, H, 7 + W)
+    st = G.PostSettings.make(**kw)
+    color, rgba = O.post_process(W, H, d, i, st)
+    ref_color, ref_rgba = O.post_process(W, H, d, i, st, reference=True)
+    assert color.tobytes() == ref_color.tobytes()
+    assert rgba.tobytes() == ref_rgba.tobytes()
 
 
 def test_png_writer_roundtrip(tmp_path):
