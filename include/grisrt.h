@@ -353,6 +353,9 @@ int grisGuideTrainStep(GrisContext* ctx, GrisGuide* guide, const float* feat, co
 /* Copies the arrays to the device and builds the 8-wide BVH over lights (instance 0) and every
  * instance's world-space triangles. */
 int grisSceneCreate(GrisContext* ctx, const GrisSceneDesc* desc, GrisScene** out);
+/* Synchronizes the context's stream, then frees the scene's device buffers. Work that reads the
+ * scene on other streams (grisPassRenderNoAlloc on a caller's stream) must be synchronized by the
+ * caller first. */
 int grisSceneDestroy(GrisScene* scene);
 int grisSceneGetStats(const GrisScene* scene, GrisSceneStats* out);
 /* Builder check: closest-hit / any-hit of n rays (float[8] each: org.xyz, tmin, dir.xyz, tmax)
@@ -387,10 +390,19 @@ int grisPassRender(GrisContext* ctx, const GrisScene* scene, const GrisPassBindi
  * grisPassRender's with a zero-filled reservoirTemp), then launches. The first call on a device
  * looks up the array's device address (cudaGetSymbolAddress, with that device current); make
  * that first call before any stream capture. Every call shares the one array: calls that overlap
- * on the GPU (other streams, other threads) race on it. */
+ * on the GPU (other streams, other threads) race on it. The call makes the scene's device current
+ * for its launches and gives the caller's current device back before it returns. Errors the
+ * kernels raise on the device (bit 0: the traversal stack limit) accumulate in the array's error
+ * word across calls; grisNoAllocReadError reads and clears it. The scene must outlive the work:
+ * synchronize `stream` before grisSceneDestroy. */
 #define GRIS_NOALLOC_MAX_PIXELS 65536
 int grisPassRenderNoAlloc(const GrisScene* scene, const GrisPassBindings* b, const GrisCamera* cam,
                           const GrisCamera* prevCam, const GrisSettings* settings, void* stream);
+/* No counterpart in the reference. The device error word of grisPassRenderNoAlloc on `device`,
+ * read after the work queued on `stream` (the call synchronizes `stream`) and then cleared.
+ * Returns GRIS_OK with *errorWord = 0, or GRIS_ERR_DEVICE_FAULT with the bits in *errorWord.
+ * Allocates nothing; restores the caller's current device. */
+int grisNoAllocReadError(int device, void* stream, uint64_t* errorWord);
 
 /* ---------------------------------------------------------------- batches of views */
 /* A batch renders many independent views per frame — each with its own scene, resolution,

@@ -188,3 +188,40 @@ def test_invalid_arguments_are_rejected(ctx):
     d = bad.desc()
     assert lib.grisSceneCreate(ctx.h, ctypes.byref(d), ctypes.byref(h)) == -4
     scene.close()
+
+
+def test_persistent_launches_from_two_threads(ora):
+    """The persistent launch form looks up the SM count and each kernel's resident blocks per SM
+    once per device, under a lock shared by every host thread: two threads with their own
+    contexts, rendering at the same time from a cold start, both get the oracle's frames."""
+    import threading
+    W, H, frames = 32, 24, 3
+    hs = G.HostScene(1, seed=2, grid=32, spheres=20)
+    cams, prevs = G.sequence_cameras(hs, frames, W, H, seed=7)
+    st = G.Settings.make(maxDepth=5)
+    ora.set_scene(hs)
+    want = O.run_sequence(ora, cams, prevs, st, W, H, record=("resv", "out"))
+    results, errors = [None, None], []
+    start = threading.Barrier(2)
+
+    def run(k):
+        try:
+            c = G.Context(0)
+            start.wait()
+            got, counters = gpu_sequence(c, hs, cams, prevs, st, W, H, (G.PATH_MEGAKERNEL, G.LAUNCH_PERSISTENT))
+            results[k] = (got, counters)
+            c.close()
+        except Exception as e:   # reported by the main thread
+            errors.append(e)
+
+    threads = [threading.Thread(target=run, args=(k,)) for k in range(2)]
+    for t in threads:
+        t.start()
+    for t in threads:
+        t.join()
+    assert not errors, errors
+    for got, counters in results:
+        assert counters[3] == 0
+        for f in range(frames):
+            assert got[f]["resv"].tobytes() == want[f]["resv"].tobytes()
+            assert got[f]["out"].tobytes() == want[f]["out"].tobytes()

@@ -220,7 +220,9 @@ def test_gpu_training_fits_a_target_distribution():
 def test_tcgen05_wait_gives_up_and_reports():
     """The tcgen05 inference with the completion of its matrix products never signalled
     (grisDebugGuideForwardStall): its bounded waits run out, it raises bit 1 of the error word,
-    frees its tensor memory and returns; the context then runs an ordinary forward correctly."""
+    commits once more so that its last bounded wait drains the products in flight (bit 2 stays
+    clear: that drain finished), frees its tensor memory and returns; the context then runs an
+    ordinary forward correctly."""
     import time
     import torch
     ctx = G.Context(0)
@@ -239,6 +241,7 @@ def test_tcgen05_wait_gives_up_and_reports():
     assert time.time() - t0 < 10.0
     c = ctx.counters(reset=True)
     assert c[3] & 2
+    assert not (c[3] & 4)                            # the drain after the timeout completed
     g.forward(tf.data_ptr(), n, to.data_ptr())       # the context is still usable
     ctx.sync()
     x = M.encode(feat[:, :3].astype(np.float64), feat[:, 3:6].astype(np.float64), feat[:, 6:9].astype(np.float64))

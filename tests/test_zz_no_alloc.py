@@ -54,10 +54,16 @@ def test_no_alloc_pass_matches_allocating_pass_on_consecutive_calls():
         # the allocation-free pass on the same inputs, same stream
         bb = G.PassBindings(W, H, dn[j].data_ptr(), dn[j ^ 1].data_ptr(), am[j].data_ptr(), am[j ^ 1].data_ptr(),
                             mv.data_ptr(), b_resv[j].data_ptr(), b_resv[j ^ 1].data_ptr(), None, b_out.data_ptr())
+        dev_before = torch.cuda.current_device()
         rc = lib.grisPassRenderNoAlloc(scene.h, ctypes.byref(bb), ctypes.byref(cams[f]), ctypes.byref(prevs[f]),
                                        ctypes.byref(st), ctx.stream())
         assert rc == 0, rc
+        assert torch.cuda.current_device() == dev_before   # the caller's current device is given back
         ctx.sync()
+        # no device-side error (traversal stack limit) was raised; reading clears the word
+        word = ctypes.c_uint64(123)
+        assert lib.grisNoAllocReadError(0, ctx.stream(), ctypes.byref(word)) == 0
+        assert word.value == 0
         ra, rb = a_resv[j].cpu().numpy(), b_resv[j].cpu().numpy()
         assert ra.tobytes() == rb.tobytes(), "call %d: reservoirs differ" % f
         assert a_out.cpu().numpy().tobytes() == b_out.cpu().numpy().tobytes(), "call %d: radiance differs" % f

@@ -10,6 +10,7 @@
 #include <string.h>
 
 #include <algorithm>
+#include <mutex>
 #include <string>
 #include <vector>
 
@@ -173,6 +174,34 @@ grisrt::DeviceSceneView scene_view(const GrisScene* s) { return s->view; }
 }  // namespace
 
 int grisrt::ctx_device(GrisContext* ctx) { return ctx->device; }
+
+namespace {
+constexpr int kCacheDevices = 64;
+std::mutex g_deviceCacheLock;
+int g_deviceCache[kCacheDevices][grisrt::kDeviceKeys];
+bool g_deviceCached[kCacheDevices][grisrt::kDeviceKeys];
+}  // namespace
+
+int grisrt::once_per_device(int key, int (*f)()) {
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kCacheDevices || key < 0 || key >= kDeviceKeys)
+        return f();
+    std::lock_guard<std::mutex> lock(g_deviceCacheLock);
+    if (g_deviceCached[dev][key]) return g_deviceCache[dev][key];
+    int v = f();
+    if (v >= 0) { g_deviceCache[dev][key] = v; g_deviceCached[dev][key] = true; }
+    return v;
+}
+
+int grisrt::current_sm_count() {
+    int v = once_per_device(kDeviceKeySMs, []() {
+        int dev = 0, sm = 0;
+        if (cudaGetDevice(&dev) != cudaSuccess || cudaDeviceGetAttribute(&sm, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
+            return -1;
+        return sm;
+    });
+    return v > 0 ? v : 1;
+}
 cudaStream_t grisrt::ctx_stream(GrisContext* ctx) { return ctx->stream; }
 unsigned long long* grisrt::ctx_counters(GrisContext* ctx) { return ctx->dCounters; }
 int grisrt::ctx_count_work(GrisContext* ctx) { return ctx->countWork; }

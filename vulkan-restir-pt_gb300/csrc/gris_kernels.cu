@@ -27,6 +27,7 @@
 #include "ray_query.cuh"
 #include "guide.cuh"
 #include "guide_kernels.h"
+#include "grisrt_internal.h"
 
 namespace grisrt {
 
@@ -1275,15 +1276,21 @@ cudaError_t launch_gris(const DeviceSceneView& scene, const GrisPassBindings& b,
     bool persistent = launchMode == GRIS_LAUNCH_PERSISTENT;
     int blocksPT = 0, blocksT = 0, blocksS = 0;
     if (persistent) {
-        static int smCount = 0, occ[3] = {0, 0, 0};
-        if (smCount == 0) {
-            int dev = 0;
-            cudaGetDevice(&dev);
-            cudaDeviceGetAttribute(&smCount, cudaDevAttrMultiProcessorCount, dev);
-            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ[0], k_pass_persistent<PathTask, 1>, 128, 0);
-            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ[1], k_pass_persistent<TemporalTask, 2>, 128, 0);
-            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ[2], k_pass_persistent<SpatialTask, 3>, 128, 0);
-        }
+        /* SM count and resident blocks per SM of each persistent kernel, per device */
+        const int smCount = current_sm_count();
+        int occ[3];
+        occ[0] = once_per_device(kDeviceKeyOccPath, []() {
+            int o = 0;
+            return cudaOccupancyMaxActiveBlocksPerMultiprocessor(&o, k_pass_persistent<PathTask, 1>, 128, 0) == cudaSuccess ? o : -1;
+        });
+        occ[1] = once_per_device(kDeviceKeyOccTemporal, []() {
+            int o = 0;
+            return cudaOccupancyMaxActiveBlocksPerMultiprocessor(&o, k_pass_persistent<TemporalTask, 2>, 128, 0) == cudaSuccess ? o : -1;
+        });
+        occ[2] = once_per_device(kDeviceKeyOccSpatial, []() {
+            int o = 0;
+            return cudaOccupancyMaxActiveBlocksPerMultiprocessor(&o, k_pass_persistent<SpatialTask, 3>, 128, 0) == cudaSuccess ? o : -1;
+        });
         blocksPT = smCount * (occ[0] > 0 ? occ[0] : 1);
         blocksT = smCount * (occ[1] > 0 ? occ[1] : 1);
         blocksS = smCount * (occ[2] > 0 ? occ[2] : 1);
@@ -2301,8 +2308,7 @@ cudaError_t enqueue_batch(const BatchShape& sh, void* dViews, const void* hViews
             C.frameSeed = 0u;
             e = cudaMemsetAsync(wb.counts, 0, 1536 * sizeof(uint32_t), stream);
             if (e != cudaSuccess) return e;
-            static int sm = 0;
-            if (sm == 0) { int dev = 0; cudaGetDevice(&dev); cudaDeviceGetAttribute(&sm, cudaDevAttrMultiProcessorCount, dev); }
+            const int sm = current_sm_count();
             const int gridShade = sm * (wl.shadeBlocksPerSM > 0 ? wl.shadeBlocksPerSM : 8);
             const int gridTrace = sm * (wl.traceBlocksPerSM > 0 ? wl.traceBlocksPerSM : 16);
             const int gridCoop = sm * 4;   /* sparse levels: 4 blocks of 4 warps per SM, 17.9 KB shared each */

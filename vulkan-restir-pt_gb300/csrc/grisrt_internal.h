@@ -51,6 +51,25 @@ void ctx_set_tuning(GrisContext* ctx, int pathForm, WaveLaunch wl);
 /* Device view and device ordinal of an uploaded scene; false for a host-only scene. */
 bool scene_device(const GrisScene* s, DeviceSceneView* view, int* device);
 
+/* Values looked up once per device and cached for every later launch on that device: SM counts,
+ * occupancies, kernel attributes. once_per_device(key, f) runs f() with the calling thread's
+ * current device, under a lock shared by all threads, the first time `key` is asked for on that
+ * device, and returns its result then and afterwards; a negative result (an error) is returned
+ * but not cached, so the next call tries again. Keys are the kDeviceKey* values below. */
+constexpr int kDeviceKeys = 16;
+enum {
+    kDeviceKeySMs = 0,              /* multiprocessor count */
+    kDeviceKeyOccPath = 1,          /* resident blocks per SM of the persistent pass kernels */
+    kDeviceKeyOccTemporal = 2,
+    kDeviceKeyOccSpatial = 3,
+    kDeviceKeyGuideTcAttr = 4,      /* dynamic shared memory attribute of the tcgen05 inference kernel */
+    kDeviceKeyGuideGradAttr = 5,    /* ... of the gradient kernel */
+    kDeviceKeyGuideGradTcAttr = 6,  /* ... of the tcgen05 gradient kernel */
+};
+int once_per_device(int key, int (*f)());
+/* SM count of the current device (cached; 1 if it cannot be read). */
+int current_sm_count();
+
 }  // namespace grisrt
 
 #endif

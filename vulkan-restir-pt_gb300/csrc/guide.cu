@@ -10,6 +10,7 @@
 
 #include "guide.cuh"
 #include "guide_kernels.h"
+#include "grisrt_internal.h"
 
 namespace grisrt {
 namespace guide {
@@ -382,21 +383,19 @@ __global__ void __launch_bounds__(256) k_guide_weight_sum(const float* weight, c
 /* ---------------------------------------------------------------- launchers */
 cudaError_t launch_forward(const FwdArgs& a, cudaStream_t stream) {
     if (a.tensorCores) return launch_forward_tc(a, stream);
-    static int sm = 0;
-    if (!sm) { int dev = 0; cudaGetDevice(&dev); cudaDeviceGetAttribute(&sm, cudaDevAttrMultiProcessorCount, dev); }
+    const int sm = current_sm_count();
     k_guide_forward<<<sm * 4, 128, 0, stream>>>(a);
     return cudaGetLastError();
 }
 
 cudaError_t launch_grad(const GradArgs& a, cudaStream_t stream) {
-    static int sm = 0;
-    static bool attr = false;
-    if (!sm) { int dev = 0; cudaGetDevice(&dev); cudaDeviceGetAttribute(&sm, cudaDevAttrMultiProcessorCount, dev); }
-    if (!attr) {
+    const int sm = current_sm_count();
+    /* the shared-memory attribute is a per-device property of the kernel: set once per device */
+    const int attr = once_per_device(kDeviceKeyGuideGradAttr, []() {
         cudaError_t e = cudaFuncSetAttribute(k_guide_grad, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kGradSmem);
-        if (e != cudaSuccess) return e;
-        attr = true;
-    }
+        return e == cudaSuccess ? 1 : -(int)e;
+    });
+    if (attr < 0) return (cudaError_t)(-attr);
     if (!a.invWeightSum) return cudaErrorInvalidValue;
     k_guide_weight_sum<<<1, 256, 0, stream>>>(a.weight, a.count, a.base, a.n, a.invWeightSum);
     k_guide_grad<<<sm, kGradWarps * 32, kGradSmem, stream>>>(a);

@@ -16,8 +16,9 @@
  * offset (between the two core matrices of a 16-wide K slice) is 128 B and its stride byte
  * offset (between 8-row groups) is K / 8 * 128 B. An MMA's K slice s starts 2 s core matrices in.
  *
- * Every wait on the mbarrier is bounded: on timeout the kernel sets the error word, waits
- * (bounded) for its MMAs once more, frees its tensor memory and returns.
+ * Every wait on the mbarrier is bounded: on timeout the kernel sets the error word, commits once
+ * more and waits (bounded) on that commit, so that no MMA it issued is still running, then frees
+ * its tensor memory and returns.
  */
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
@@ -25,6 +26,7 @@
 
 #include "guide.cuh"
 #include "guide_kernels.h"
+#include "grisrt_internal.h"
 
 namespace grisrt {
 namespace guide {
@@ -252,8 +254,14 @@ __global__ void __launch_bounds__(kTcRows * kTcGroups, 2) k_guide_forward_tc(Fwd
         }
         if (!ok) break;
     }
-    /* after a timeout: one more bounded wait for the MMAs in flight before the memory is freed */
-    if (sFail[grp] && tid == 0) (void)bar_wait(bar, phase);
+    /* After a timeout the phase waited on (parity phase ^ 1, `phase` having been flipped since) is
+     * still open: a commit now arrives on it once every matrix product this thread issued has
+     * completed, and one more bounded wait on that phase drains them before the tensor memory is
+     * freed. Bit 2 of the error word records a drain that did not finish either. */
+    if (sFail[grp] && tid == 0) {
+        tc_commit(bar);
+        if (!bar_wait(bar, phase ^ 1u) && a.err) atomicOr(a.err, 4ull);
+    }
     tc_fence_before();
     __syncthreads();
     tc_fence_after();
@@ -263,14 +271,13 @@ __global__ void __launch_bounds__(kTcRows * kTcGroups, 2) k_guide_forward_tc(Fwd
 }
 
 cudaError_t launch_forward_tc(const FwdArgs& a, cudaStream_t stream) {
-    static int sm = 0;
-    static bool attr = false;
-    if (!sm) { int dev = 0; cudaGetDevice(&dev); cudaDeviceGetAttribute(&sm, cudaDevAttrMultiProcessorCount, dev); }
-    if (!attr) {
+    const int sm = current_sm_count();
+    /* the shared-memory attribute is a per-device property of the kernel: set once per device */
+    const int attr = once_per_device(kDeviceKeyGuideTcAttr, []() {
         cudaError_t e = cudaFuncSetAttribute(k_guide_forward_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kTcSmem);
-        if (e != cudaSuccess) return e;
-        attr = true;
-    }
+        return e == cudaSuccess ? 1 : -(int)e;
+    });
+    if (attr < 0) return (cudaError_t)(-attr);
     k_guide_forward_tc<<<sm * 2, kTcRows * kTcGroups, kTcSmem, stream>>>(a);
     return cudaGetLastError();
 }

@@ -45,6 +45,26 @@ cudaError_t scratch_address(int device, void** out) {
 
 }  // namespace
 
+namespace {
+
+/* Makes `device` current for the lifetime of the guard and gives the caller's current device back
+ * on every return path: the callers of these entry points run inside other frameworks' threads. */
+struct DeviceGuard {
+    int saved = -1;
+    bool ok = false;
+    explicit DeviceGuard(int device) {
+        if (cudaGetDevice(&saved) != cudaSuccess) saved = -1;
+        ok = cudaSetDevice(device) == cudaSuccess;
+    }
+    ~DeviceGuard() {
+        if (saved >= 0) cudaSetDevice(saved);
+    }
+};
+
+constexpr uint64_t kErrorWord = GRIS_COUNTER_ERROR;   /* the counter word the kernels OR errors into */
+
+}  // namespace
+
 extern "C" int grisPassRenderNoAlloc(const GrisScene* scene, const GrisPassBindings* b, const GrisCamera* cam,
                                      const GrisCamera* prevCam, const GrisSettings* settings, void* stream) {
     if (!scene || !b || !cam || !prevCam || !settings) return GRIS_ERR_INVALID_ARGUMENT;
@@ -62,17 +82,41 @@ extern "C" int grisPassRenderNoAlloc(const GrisScene* scene, const GrisPassBindi
     int device = 0;
     if (!grisrt::scene_device(scene, &view, &device) || device < 0 || device >= kMaxDevices)
         return GRIS_ERR_INVALID_ARGUMENT;
-    if (cudaSetDevice(device) != cudaSuccess) return GRIS_ERR_CUDA;
+    DeviceGuard guard(device);
+    if (!guard.ok) return GRIS_ERR_CUDA;
     void* base = nullptr;
     if (scratch_address(device, &base) != cudaSuccess) return GRIS_ERR_CUDA;
     cudaStream_t s = (cudaStream_t)stream;
     unsigned char* temp = (unsigned char*)base;
     unsigned long long* counters = (unsigned long long*)(temp + kTempBytes);
-    /* what must start at zero: the reservoirs of this frame's size and the counter words */
+    /* what must start at zero: the reservoirs of this frame's size and the ray-counter words; the
+     * error word (counter 3) is left alone, so that errors of earlier calls stay readable until
+     * grisNoAllocReadError takes them */
     if (cudaMemsetAsync(temp, 0, pixels * sizeof(GrisReservoir), s) != cudaSuccess) return GRIS_ERR_CUDA;
-    if (cudaMemsetAsync(counters, 0, kCounterBytes, s) != cudaSuccess) return GRIS_ERR_CUDA;
+    if (cudaMemsetAsync(counters, 0, kErrorWord * sizeof(unsigned long long), s) != cudaSuccess) return GRIS_ERR_CUDA;
+    if (cudaMemsetAsync(counters + kErrorWord + 1, 0, kCounterBytes - (kErrorWord + 1) * sizeof(unsigned long long), s) !=
+        cudaSuccess)
+        return GRIS_ERR_CUDA;
     GrisPassBindings pb = *b;
     pb.reservoirTemp = (GrisReservoir*)temp;
     cudaError_t e = grisrt::launch_gris(view, pb, *cam, *prevCam, *settings, 7, counters, 0, nullptr, s);
     return e == cudaSuccess ? GRIS_OK : GRIS_ERR_CUDA;
+}
+
+extern "C" int grisNoAllocReadError(int device, void* stream, uint64_t* errorWord) {
+    if (!errorWord || device < 0 || device >= kMaxDevices) return GRIS_ERR_INVALID_ARGUMENT;
+    *errorWord = 0;
+    DeviceGuard guard(device);
+    if (!guard.ok) return GRIS_ERR_CUDA;
+    void* base = nullptr;
+    if (scratch_address(device, &base) != cudaSuccess) return GRIS_ERR_CUDA;
+    cudaStream_t s = (cudaStream_t)stream;
+    unsigned long long* word = (unsigned long long*)((unsigned char*)base + kTempBytes) + kErrorWord;
+    unsigned long long v = 0;
+    /* after the caller's work on `stream`: read the word into this host variable, then clear it */
+    if (cudaMemcpyAsync(&v, word, sizeof(v), cudaMemcpyDeviceToHost, s) != cudaSuccess) return GRIS_ERR_CUDA;
+    if (cudaMemsetAsync(word, 0, sizeof(v), s) != cudaSuccess) return GRIS_ERR_CUDA;
+    if (cudaStreamSynchronize(s) != cudaSuccess) return GRIS_ERR_CUDA;
+    *errorWord = (uint64_t)v;
+    return v ? GRIS_ERR_DEVICE_FAULT : GRIS_OK;
 }

@@ -207,6 +207,7 @@ EXPORTS = [
     "grisSizeof", "grisBuildLightTable", "grisCameraSetup", "grisCameraLookAt", "grisHostSceneCreate",
     "grisHostSceneDesc", "grisHostSceneCamera", "grisHostSceneDestroy", "grisSceneCreate", "grisSceneDestroy",
     "grisSceneGetStats", "grisDebugHostSceneCreate", "grisDebugTraceHost", "grisDebugTraceDevice", "grisPassGBuffer", "grisPassRender", "grisPassRenderNoAlloc",
+    "grisNoAllocReadError",
     "grisFrameCreate", "grisFrameDestroy", "grisFrameRender", "grisFrameGetBuffer", "grisFrameDownload",
     "grisFrameUpload", "grisSetPathForm", "grisBatchCreate", "grisBatchDestroy", "grisBatchRender", "grisBatchGetBuffer",
     "grisBatchDownload", "grisSetGraphs", "grisSetWaveLaunch", "grisBatchAutotune",
@@ -262,6 +263,7 @@ def load(path=None):
                                  ctypes.POINTER(Settings), i32]),
         "grisPassRenderNoAlloc": (i32, [vp, ctypes.POINTER(PassBindings), ctypes.POINTER(Camera), ctypes.POINTER(Camera),
                                         ctypes.POINTER(Settings), vp]),
+        "grisNoAllocReadError": (i32, [i32, vp, ctypes.POINTER(u64)]),
         "grisFrameCreate": (i32, [vp, u32, u32, ctypes.POINTER(vp)]),
         "grisFrameDestroy": (i32, [vp]),
         "grisFrameRender": (i32, [vp, vp, vp, ctypes.POINTER(Camera), ctypes.POINTER(Camera), ctypes.POINTER(Settings)]),
