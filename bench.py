@@ -225,8 +225,10 @@ class View:
         self.cams, self.prevs = G.sequence_cameras(hs, frames, width, height, seed=seed, orbit_frames=60)
 
 
-def make_views(args, frames):
-    """The workload's views with `frames` cameras each, and its config dict."""
+def make_views(args, frames, scene_lib=None):
+    """The workload's views with `frames` cameras each, and its config dict (the workload alone:
+    both arms print the same one). scene_lib: the generator library (grisrt.scene_library) —
+    the reference arm's, which loads no part of libgrisrt; default libgrisrt's own."""
     import grisrt as G
     from grisrt import workloads
 
@@ -236,7 +238,7 @@ def make_views(args, frames):
     common = {"spatial_neighbors": 3, "spatial_radius_px": 20.0, "cap": 20, "shift": "hybrid",
               "l2": "flushed between frames (256 MiB write outside the timed events)"}
     if args.workload == "c1":
-        hs = G.HostScene(0, seed=args.seed)
+        hs = G.HostScene(0, seed=args.seed, lib=scene_lib)
         st = G.Settings.make(shiftType=2, rrScale=1.0, temporalReuse=True, spatialReuse=True, cap=20, maxDepth=3,
                              spatialNeighbors=3, spatialRadius=30.0)
         views = [View(hs, 256, 256, st, frames, args.seed)]
@@ -246,7 +248,8 @@ def make_views(args, frames):
         config["spatial_radius_px"] = 30.0
         return views, config
     if args.workload in ("c2", "c4"):
-        hs = G.HostScene(2 if args.workload == "c4" else 1, seed=args.seed, grid=args.grid, spheres=args.spheres)
+        hs = G.HostScene(2 if args.workload == "c4" else 1, seed=args.seed, grid=args.grid, spheres=args.spheres,
+                         lib=scene_lib)
         views = [View(hs, args.width, args.height, settings(args.depth), frames, args.seed)]
         config = {"workload": "C2: %dx%d, %d^2 fBm heightfield + %d icospheres (%d tris), depth %d, orbit" % (
             args.width, args.height, args.grid, args.spheres, hs.triangle_count(), args.depth),
@@ -255,7 +258,7 @@ def make_views(args, frames):
         specs = workloads.batched_views(args.views, seed=args.seed + 6)
         views = []
         for i, s in enumerate(specs):
-            hs = G.HostScene(s["kind"], seed=s["seed"], grid=s["grid"], spheres=s["spheres"])
+            hs = G.HostScene(s["kind"], seed=s["seed"], grid=s["grid"], spheres=s["spheres"], lib=scene_lib)
             views.append(View(hs, s["width"], s["height"], settings(s["maxDepth"]), frames, args.seed + i))
         tris = [v.hs.triangle_count() for v in views]
         px = sum(v.w * v.h for v in views)
@@ -534,7 +537,11 @@ def run_di(args, rank, world, local):
     sample = {"light": G.DI_SAMPLE_LIGHT, "bsdf": G.DI_SAMPLE_BSDF, "both": G.DI_SAMPLE_BOTH}
     di = G.DISettings.make(shiftType=shift[args.di_shift], sampleType=sample[args.di_sample],
                            temporalReuse=args.di_temporal == "on", spatialReuse=True)
-    hs = G.HostScene(1, seed=args.seed, grid=args.grid, spheres=args.spheres)
+    scene_lib = None
+    if args.impl == "reference":   # the reference arm builds its inputs without libgrisrt
+        from oracle import build_oracle
+        scene_lib = G.scene_library(build_oracle.build_scenegen())
+    hs = G.HostScene(1, seed=args.seed, grid=args.grid, spheres=args.spheres, lib=scene_lib)
     W, H = args.width, args.height
     total = WU + 3 * K + 4
     cams, prevs = G.sequence_cameras(hs, total, W, H, seed=args.seed, orbit_frames=60)
@@ -549,7 +556,6 @@ def run_di(args, rank, world, local):
     if args.impl == "reference":
         if rank != 0:
             return 0
-        config["parallelism"] = "host cores (OpenMP)"
         budget = max(5.0, min(60.0, 150.0 / max(1, K + WU)))
         vals, plan, ora, threads, text = [], None, None, 0, ""
         for step in range(WU + K):
@@ -560,7 +566,8 @@ def run_di(args, rank, world, local):
         print(json.dumps({"metric": metric, "value": value, "unit": UNIT, "n_gpus": args.gpus, "steps": K,
                           "warmup": WU, "ms_per_step": 1000.0 / value if value else None, "higher_is_better": True,
                           "scaling": "weak", "vs_baseline": None, "dtype": "f32",
-                          "data": "synthetic (seeded scene generator)", "config": config, "impl": "reference",
+                          "data": "synthetic (seeded scene generator)", "config": config,
+                          "run": {"parallelism": "host cores (OpenMP)"}, "impl": "reference",
                           "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
                                            "sample": text},
                           "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}))
@@ -570,7 +577,7 @@ def run_di(args, rank, world, local):
     if world > 1:
         import torch.distributed as dist
         dist.init_process_group("nccl", device_id=torch.device("cuda", local))
-    config["parallelism"] = "replicas" if world > 1 else "1 GPU"
+    run = {"parallelism": "replicas" if world > 1 else "1 GPU"}
     ctx = G.Context(local)
     scene = G.Scene(ctx, hs)
     frame = G.Frame(ctx, W, H)
@@ -685,7 +692,7 @@ def run_di(args, rank, world, local):
         print(json.dumps({"metric": metric, "value": value, "unit": UNIT, "n_gpus": world, "steps": K, "warmup": WU,
                           "ms_per_step": t_max / K, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
                           "dtype": "f32", "data": "synthetic (seeded scene generator, no dataset)", "config": config,
-                          "mrays_per_s": world * rays / (t_max / 1000.0) / 1e6, "rays_per_frame": rays / K,
+                          "run": run, "mrays_per_s": world * rays / (t_max / 1000.0) / 1e6, "rays_per_frame": rays / K,
                           "clocks": clocks, "e2e": e2e, "gpu_launches": int(launches), "roofline": roofline,
                           "cpu_baseline": cpu}))
     frame.close()
@@ -714,8 +721,9 @@ def main():
     if args.impl == "reference":
         if rank != 0:
             return 0
-        views, config = make_views(args, 16)
-        config["parallelism"] = "host cores (OpenMP)"
+        from oracle import build_oracle
+        views, config = make_views(args, 16, scene_lib=G.scene_library(build_oracle.build_scenegen()))
+        run = {"parallelism": "host cores (OpenMP)", "api": "oracle restatement (C++)"}
         budget = max(5.0, min(60.0, 150.0 / max(1, K + WU)))
         vals = []
         plan, ora = None, None
@@ -728,7 +736,7 @@ def main():
         line = {"metric": metric, "value": value, "unit": UNIT, "n_gpus": args.gpus, "steps": K, "warmup": WU,
                 "ms_per_step": 1000.0 / value if value else None, "higher_is_better": True, "scaling": "weak",
                 "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded scene generator)", "config": config,
-                "impl": "reference",
+                "run": run, "impl": "reference",
                 "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port", "sample": sample},
                 "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
                 "note": "the reference's GLSL/Vulkan path is unavailable on this box (no graphics stack); this arm "
@@ -744,7 +752,7 @@ def main():
         dist.init_process_group("nccl", device_id=torch.device("cuda", local))
     total = WU + 3 * K + 8
     views, config = make_views(args, total)
-    config["parallelism"] = "replicas" if world > 1 else "1 GPU"
+    run = {"parallelism": "replicas" if world > 1 else "1 GPU"}   # how this arm ran the workload
     n = len(views)
     px = sum(v.w * v.h for v in views)
     ctx = G.Context(local)
@@ -759,7 +767,7 @@ def main():
     stats = [sc.stats() for sc in scenes]
     batch = G.Batch(ctx, scenes, [(v.w, v.h) for v in views]) if args.api == "batch" else None
     frame = G.Frame(ctx, views[0].w, views[0].h) if args.api == "frame" else None
-    config["api"] = args.api
+    run["api"] = args.api
     stream = torch.cuda.ExternalStream(ctx.stream(), device=torch.device("cuda", local))
     flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
     fi = 0
@@ -788,11 +796,11 @@ def main():
         form = r.pathForm
     else:
         form = G.PATH_WAVEFRONT if args.path_form == "wavefront" else G.PATH_MEGAKERNEL
-    config["path_form"] = ("wavefront" if form == G.PATH_WAVEFRONT else "megakernel") if batch is not None else "megakernel"
-    config["graphs"] = batch is not None and not args.no_graphs
-    config["autotune"] = tune
+    run["path_form"] = ("wavefront" if form == G.PATH_WAVEFRONT else "megakernel") if batch is not None else "megakernel"
+    run["graphs"] = batch is not None and not args.no_graphs
+    run["autotune"] = tune
     if args.wave and tune is None:
-        config["wave"] = args.wave
+        run["wave"] = args.wave
 
     def barrier():
         torch.cuda.synchronize()
@@ -848,7 +856,7 @@ def main():
     work = ctx.kernel_profile(reset=True)
     ctx.set_work_counting(False)
 
-    wave = config["path_form"] == "wavefront"
+    wave = run["path_form"] == "wavefront"
     slots = (["gbuffer", "temporal", "spatial", "wave_begin", "wave_extend", "wave_shade", "wave_shadow", "wave_post"]
              if wave else ["gbuffer", "path_trace", "temporal", "spatial"])
     refill = (tune is not None and " refill" in tune["chosen"]) or (tune is None and bool(args.wave) and
@@ -927,7 +935,7 @@ def main():
         line = {"metric": metric, "value": value, "unit": UNIT, "n_gpus": world, "steps": K, "warmup": WU,
                 "ms_per_step": t_max / K, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
                 "dtype": "f32", "data": "synthetic (seeded scene generator, no dataset)", "config": config,
-                "mrays_per_s": mrays, "rays_per_frame": rays / K,
+                "run": run, "mrays_per_s": mrays, "rays_per_frame": rays / K,
                 "bvh": {"nodes": sum(s.nodeCount for s in stats), "node_mb": sum(s.nodeBytes for s in stats) / 1e6,
                         "tri_mb": sum(s.triangleBytes for s in stats) / 1e6, "depth": max(s.maxDepth for s in stats),
                         "build_s": sum(s.buildSeconds for s in stats)},

@@ -1,5 +1,6 @@
 """Seeded workload definitions (batched views) and the oracle's resident scene slots."""
 import numpy as np
+import pytest
 
 import grisrt as G
 from grisrt import workloads
@@ -60,3 +61,20 @@ def test_oracle_scene_slots_keep_scenes_resident():
     ref = O.run_sequence(ora, runs[1][0], runs[1][1], st, W, H, record=("resv",))[0]
     assert ref["resv"].tobytes() == got[1]["resv"].tobytes()
     ora.select_scene(0)
+
+
+@pytest.mark.parametrize("kind,grid,spheres", [(0, 0, 0), (1, 48, 30), (2, 40, 20)])
+def test_oracle_side_generator_builds_the_same_inputs(kind, grid, spheres):
+    """The benchmark's CPU reference arm builds its inputs with oracle/_build/libscenegen.so (the
+    same generator compiled on the oracle side, so that arm loads no part of libgrisrt): every scene
+    array and every camera of a sequence are byte-identical to libgrisrt's."""
+    from oracle import build_oracle
+    lib = G.scene_library(build_oracle.build_scenegen())
+    a = G.HostScene(kind, seed=5, grid=grid, spheres=spheres)
+    b = G.HostScene(kind, seed=5, grid=grid, spheres=spheres, lib=lib)
+    for x, y in zip(a.arrays(), b.arrays()):
+        assert x.tobytes() == y.tobytes()
+    ca, pa = G.sequence_cameras(a, 5, 64, 48, seed=3, orbit_frames=60)
+    cb, pb = G.sequence_cameras(b, 5, 64, 48, seed=3, orbit_frames=60)
+    for u, v in zip(ca + pa, cb + pb):
+        assert bytes(memoryview(u)) == bytes(memoryview(v))

@@ -341,11 +341,29 @@ def camera_setup(pos, angle, fov, width, height):
     return c
 
 
-class HostScene:
-    """Synthetic scene (kind 0 box, 1 terrain + spheres, 2 glossy terrain) as reference-layout arrays."""
+def scene_library(path):
+    """Another build of the synthetic-scene generator (grisHostScene* and the camera helpers of
+    csrc/host_scene.cpp) as a library of its own, for HostScene(lib=...): the CPU reference arm of
+    the benchmark builds its inputs with it and loads no part of libgrisrt."""
+    lib = ctypes.CDLL(path)
+    vp, u32, u64, i32 = ctypes.c_void_p, ctypes.c_uint32, ctypes.c_uint64, ctypes.c_int
+    for name, (res, args) in {
+            "grisHostSceneCreate": (i32, [i32, u64, u32, u32, ctypes.POINTER(vp)]),
+            "grisHostSceneDesc": (i32, [vp, ctypes.POINTER(SceneDesc)]),
+            "grisHostSceneCamera": (i32, [vp, u32, u32, u32, u32, ctypes.POINTER(Camera)]),
+            "grisHostSceneDestroy": (i32, [vp])}.items():
+        f = getattr(lib, name)
+        f.restype, f.argtypes = res, args
+    return lib
 
-    def __init__(self, kind=0, seed=1, grid=512, spheres=2000, _handle=None):
-        lib = load()
+
+class HostScene:
+    """Synthetic scene (kind 0 box, 1 terrain + spheres, 2 glossy terrain) as reference-layout arrays.
+    lib: the library that generates it (default libgrisrt; see scene_library)."""
+
+    def __init__(self, kind=0, seed=1, grid=512, spheres=2000, _handle=None, lib=None):
+        lib = lib if lib is not None else load()
+        self._lib = lib
         if _handle is None:
             h = ctypes.c_void_p()
             _check(lib.grisHostSceneCreate(kind, seed, grid, spheres, ctypes.byref(h)), what="grisHostSceneCreate")
@@ -386,7 +404,8 @@ class HostScene:
 
     def camera(self, frame, frames, width, height):
         c = Camera()
-        _check(load().grisHostSceneCamera(self._h, frame, frames, width, height, ctypes.byref(c)), what="grisHostSceneCamera")
+        _check(self._lib.grisHostSceneCamera(self._h, frame, frames, width, height, ctypes.byref(c)),
+               what="grisHostSceneCamera")
         return c
 
     def desc(self):
@@ -408,8 +427,9 @@ class HostScene:
         return len(self.lights) + int(sum(int(i["indexCount"]) // 3 for i in self.instances))
 
     def __del__(self):
-        if getattr(self, "_h", None) and _lib is not None and not sys.is_finalizing():
-            _lib.grisHostSceneDestroy(self._h)
+        lib = getattr(self, "_lib", None)
+        if getattr(self, "_h", None) and lib is not None and not sys.is_finalizing():
+            lib.grisHostSceneDestroy(self._h)
             self._h = None
 
 
