@@ -74,12 +74,24 @@ def alg_bytes(slot, w, px):
       wave_extend  per ray: 32 B ray + 16 B hit + 4 B queue entry, plus traversal
       wave_shade   per path: record read and write + 16 B hit + a surface fetch + 4 B queue entry
       wave_shadow  per shadow ray: 48 B query + 1 B verdict + 4 B queue entry, plus traversal
-      wave_post    per shadow query: record read and write + query read + verdict + queue entry"""
+      wave_post    per shadow query: record read and write + query read + verdict + queue entry
+    The reuse passes in three launches (prepare, visibility walk, finish; w["split"] true):
+      temporal     (prepare + finish) the per-pixel figure + a 37 B merge record written and read
+                   + the 96 B reservoir read again by the finish + a 32 B queue entry per query
+      spatial      (prepare + finish) the per-pixel figure + 37 B written and read per neighbour
+                   slot + the pixel's G-buffer and reservoir read again by the finish (120 B)
+                   + a 32 B queue entry per query
+      reuse_vis_*  per query: 32 B queue entry + 1 B verdict read and written, plus traversal"""
     trav = w["nodes"] * NODE_BYTES + w["tris"] * TRI_BYTES
     r = w["rays"]
     per_px = {"gbuffer": 28, "path_trace": 120, "temporal": 340, "spatial": 608, "wave_begin": 24 + WAVE_STATE + 4}
+    if slot in ("temporal", "spatial") and w.get("split"):
+        extra = 2 * 37 + 96 if slot == "temporal" else 2 * 37 * w["neighbours"] + 120
+        return trav + (per_px[slot] + extra) * px + SURFACE_BYTES * r + 32 * w["queries"]
     if slot in ("gbuffer", "path_trace", "temporal", "spatial"):
         return trav + per_px[slot] * px + SURFACE_BYTES * r
+    if slot in ("reuse_vis_temporal", "reuse_vis_spatial"):
+        return trav + 34 * r
     if slot == "wave_begin":
         return per_px[slot] * px
     if slot == "wave_extend":
@@ -654,6 +666,7 @@ def run_di(args, rank, world, local):
     e2e = {"value": aggregate_rate(K, e2e_s, world), "unit": UNIT, "h2d_bytes_per_step": 2 * 352 + 16,
            "d2h_bytes_per_step": W * H * 16}
     peak, peak_kind = load_peaks()
+    l2_gbs = ctx.l2_bandwidth()
     per_kernel = {}
     for s_ in slots:
         L = max(1, prof[s_]["launches"])
@@ -678,6 +691,9 @@ def run_di(args, rank, world, local):
             traffic = None
     roofline = {"bound": "hbm", "kernel": top, "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
                 "frac": round(achieved / peak, 4), "peak_source": peak_kind, "traffic": traffic,
+                "l2_peak": round(l2_gbs, 1), "l2_frac": round(achieved / l2_gbs, 4) if l2_gbs else None,
+                "l2_peak_source": "measured in this run (grisMeasureL2Bandwidth: 48 MiB read 20 times per launch, "
+                                  "best of 5)",
                 "algorithmic_bytes_per_launch": pk["alg_bytes_per_launch"], "avg_launch_ms": pk["avg_launch_ms"],
                 "share_of_frame": round(prof[top]["ms"] / max(1e-9, sum(prof[s_]["ms"] for s_ in slots)), 3),
                 "kernels": per_kernel}
@@ -859,6 +875,18 @@ def main():
     wave = run["path_form"] == "wavefront"
     slots = (["gbuffer", "temporal", "spatial", "wave_begin", "wave_extend", "wave_shade", "wave_shadow", "wave_post"]
              if wave else ["gbuffer", "path_trace", "temporal", "spatial"])
+    # batches run each reuse pass as prepare -> visibility walk -> finish: the pass's span (slot
+    # "temporal" / "spatial") then holds its walk (slot "reuse_vis_*"), counted on its own here
+    split = prof["reuse_vis_spatial"]["launches"] > 0 or prof["reuse_vis_temporal"]["launches"] > 0
+    if split:
+        for pas, vis in (("temporal", "reuse_vis_temporal"), ("spatial", "reuse_vis_spatial")):
+            prof[pas] = dict(prof[pas])
+            prof[pas]["ms"] = max(0.0, prof[pas]["ms"] - prof[vis]["ms"])
+            prof[pas]["launches"] = 2 * prof[pas]["launches"]     # prepare + finish
+            work[pas] = dict(work[pas])
+            for k in ("nodes", "tris"):
+                work[pas][k] = max(0, work[pas][k] - work[vis][k])
+        slots += ["reuse_vis_temporal", "reuse_vis_spatial"]
     refill = (tune is not None and " refill" in tune["chosen"]) or (tune is None and bool(args.wave) and
                                                                     args.wave.endswith("refill"))
     launches_per_frame = kernel_launches_per_frame(prof, slots, K, wave, refill)
@@ -890,18 +918,27 @@ def main():
 
     # ---------------- roofline of the kernel with the largest share
     peak, peak_kind = load_peaks()
+    # the second denominator: the BVH (tens of MB) and the queues stay in the 129-MB L2, so the
+    # traversal and reuse kernels read most of their algorithmic bytes from L2
+    l2_gbs = ctx.l2_bandwidth()
     per_kernel = {}
     for s in slots:
         L = max(1, prof[s]["launches"])
         w = {k: work[s][k] / K for k in ("nodes", "tris", "rays")}
         w["paths"] = work["wave_extend"]["rays"] / K
         w["shadow_paths"] = work["wave_shadow"]["rays"] / K
+        w["split"] = split
+        w["neighbours"] = max(v.settings.spatialNeighbors for v in views)
+        w["queries"] = work["reuse_vis_" + s]["rays"] / K if s in ("temporal", "spatial") else 0
         alg_frame = alg_bytes(s, w, px)
         avg_ms = prof[s]["ms"] / L
         per_kernel[s] = {"ms_per_frame": prof[s]["ms"] / K, "launches_per_frame": prof[s]["launches"] / K,
                          "avg_launch_ms": avg_ms, "alg_bytes_per_launch": alg_frame * K / L,
                          "gbs": (alg_frame * K / L) / (avg_ms / 1000.0) / 1e9 if avg_ms > 0 else None,
                          "nodes_per_frame": w["nodes"], "tris_per_frame": w["tris"], "rays_per_frame": w["rays"]}
+        g = per_kernel[s]["gbs"]
+        per_kernel[s]["hbm_frac"] = round(g / peak, 4) if g else None
+        per_kernel[s]["l2_frac"] = round(g / l2_gbs, 4) if g and l2_gbs else None
     top = max(slots, key=lambda s: prof[s]["ms"])
     pk = per_kernel[top]
     achieved = pk["gbs"] or 0.0
@@ -917,6 +954,9 @@ def main():
             traffic = None
     roofline = {"bound": "hbm", "kernel": top, "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
                 "frac": round(achieved / peak, 4), "peak_source": peak_kind, "traffic": traffic,
+                "l2_peak": round(l2_gbs, 1), "l2_frac": round(achieved / l2_gbs, 4) if l2_gbs else None,
+                "l2_peak_source": "measured in this run (grisMeasureL2Bandwidth: 48 MiB read 20 times per launch, "
+                                  "best of 5)",
                 "algorithmic_bytes_per_launch": pk["alg_bytes_per_launch"], "avg_launch_ms": pk["avg_launch_ms"],
                 "share_of_frame": round(prof[top]["ms"] / max(1e-9, sum(prof[s]["ms"] for s in slots)), 3),
                 "kernels": per_kernel}

@@ -224,9 +224,11 @@ int grisReadWorkCounters(GrisContext* ctx, uint64_t nodes[4], uint64_t tris[4], 
 /* Per-kernel profile with the wavefront stages on their own: slots 0-3 as grisReadProfile (slot 1
  * spans the whole path tracer), then the wavefront's begin, extension (closest hits), shading,
  * shadow and post stages, then the guide's inference and training, then the three ReSTIR DI
- * kernels. ms/launches while profiling is on; nodes/tris/rays while work counting
- * is on, for the slots that traverse (rays: closest-hit rays, shadow rays for the shadow stage). */
-#define GRIS_PROFILE_SLOTS 14
+ * kernels, then the visibility walks of the temporal and the spatial pass (batches, where a pass
+ * runs as prepare -> walk -> finish; slots 2 and 3 span the whole pass, walk included).
+ * ms/launches while profiling is on; nodes/tris/rays while work counting is on, for the slots
+ * that traverse (rays: closest-hit rays, shadow rays for the shadow stage and the walks). */
+#define GRIS_PROFILE_SLOTS 16
 #define GRIS_SLOT_WAVE_BEGIN 4
 #define GRIS_SLOT_WAVE_EXTEND 5
 #define GRIS_SLOT_WAVE_SHADE 6
@@ -237,12 +239,20 @@ int grisReadWorkCounters(GrisContext* ctx, uint64_t nodes[4], uint64_t tris[4], 
 #define GRIS_SLOT_DI_CANDIDATES 11  /* ReSTIR DI (rays: closest-hit and shadow rays together) */
 #define GRIS_SLOT_DI_TEMPORAL 12
 #define GRIS_SLOT_DI_SPATIAL 13
+#define GRIS_SLOT_REUSE_VIS_TEMPORAL 14
+#define GRIS_SLOT_REUSE_VIS_SPATIAL 15
 typedef struct GrisKernelProfile {
     double ms;
     uint64_t launches;
     uint64_t nodes, tris, rays;
 } GrisKernelProfile;
 int grisReadKernelProfile(GrisContext* ctx, GrisKernelProfile out[GRIS_PROFILE_SLOTS], int reset);
+/* No counterpart in the reference. The GPU's L2 read bandwidth in GB/s: a plain read kernel
+ * (16-B loads that bypass L1) over a buffer of `bytes` (1 to 256 MiB; choose one that fits in L2)
+ * read `reps` times per launch, best of five launches timed with CUDA events on the context's
+ * stream. Allocates and frees its buffer. The roofline denominator of the kernels whose working
+ * set (the BVH, the queues) stays in L2. */
+int grisMeasureL2Bandwidth(GrisContext* ctx, uint64_t bytes, int reps, double* gbs);
 size_t grisSizeof(int which);   /* 0 camera, 1 reservoir, 2 material, 3 vertex, 4 instance, 5 light, 6 table entry,
                                    7 settings, 8 DI reservoir, 9 DI settings */
 

@@ -108,6 +108,9 @@ def test_gpu_pairwise_weights_match_oracle(case, mode, ctx, ora):
 
 
 def test_device_traversal_matches_host(ctx):
+    """50,000 random rays, closest hit and any hit: the device walk with the resident traversal
+    kernels' short stack (two register entries, here one shared-memory entry, then the local-memory
+    overflow, so deep walks use all three) against the host walk's array stack, bit for bit."""
     hs = G.HostScene(1, seed=4, grid=64, spheres=100)
     scene = G.Scene(ctx, hs)
     rng = np.random.default_rng(5)

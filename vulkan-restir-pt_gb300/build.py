@@ -19,7 +19,7 @@ OUT_DIR = os.path.join(HERE, "grisrt")
 LIB = os.path.join(OUT_DIR, "libgrisrt.so")
 BUILD = os.path.join(HERE, "_build")
 
-CUDA_SOURCES = ["gris_kernels.cu", "di_kernels.cu", "post.cu", "noalloc.cu", "guide.cu", "guide_tc.cu"]
+CUDA_SOURCES = ["gris_kernels.cu", "di_kernels.cu", "post.cu", "noalloc.cu", "guide.cu", "guide_tc.cu", "measure.cu"]
 HOST_SOURCES = ["capi.cpp", "batch.cpp", "host_scene.cpp", "bvh_build.cpp", "guide_api.cpp", "image_io.cpp"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 

@@ -62,6 +62,23 @@ static void drop_graphs(GrisBatch* b) {
 
 using namespace grisrt;
 
+/* The reuse passes' three-launch form keeps per-slot records for every pixel and neighbour: sized
+ * for the largest neighbour count seen so far (growing drops the captured frames, whose launches
+ * hold the old buffers). */
+static cudaError_t ensure_reuse(GrisBatch* b, uint32_t slots, cudaStream_t st) {
+    if (b->wave.reuse.slots >= slots && b->wave.reuse.capacity >= b->pixels) return cudaSuccess;
+    cudaError_t e = cudaStreamSynchronize(st);
+    if (e != cudaSuccess) return e;
+    drop_graphs(b);
+    if (b->wave.reuse.block) cudaFree(b->wave.reuse.block);
+    b->wave.reuse = ReuseBuffers{};
+    void* p = nullptr;
+    e = cudaMalloc(&p, reuse_bytes(b->pixels, slots));
+    if (e != cudaSuccess) return e;
+    reuse_carve(b->wave.reuse, p, b->pixels, slots);
+    return cudaSuccess;
+}
+
 extern "C" {
 
 int grisBatchCreate(GrisContext* ctx, uint32_t n, const GrisScene* const* scenes, const uint32_t* widths,
@@ -136,6 +153,7 @@ int grisBatchDestroy(GrisBatch* b) {
     cudaStreamSynchronize(ctx_stream(b->ctx));
     drop_graphs(b);
     if (b->guideBlock) cudaFree(b->guideBlock);
+    if (b->wave.reuse.block) cudaFree(b->wave.reuse.block);
     for (void* p : b->allocations) cudaFree(p);
     for (int i = 0; i < 2; i++) {
         if (b->hViews[i]) cudaFreeHost(b->hViews[i]);
@@ -176,6 +194,20 @@ int grisBatchRender(GrisContext* ctx, GrisBatch* b, const GrisCamera* cams, cons
     cudaStream_t st = ctx_stream(ctx);
     cudaError_t e = cudaEventSynchronize(b->staged[k]);   /* the staging slot's previous copy is done */
     if (e != cudaSuccess) return ctx_fail(ctx, GRIS_ERR_CUDA, std::string("grisBatchRender: ") + cudaGetErrorString(e));
+    {
+        uint32_t slots = 1;
+        bool pairwise = false;
+        for (uint32_t i = 0; i < b->n; i++) {
+            if (settings[i].spatialNeighbors > slots) slots = settings[i].spatialNeighbors;
+            if (settings[i].misWeights) pairwise = true;
+        }
+        if (!pairwise && slots <= kReuseMaxSlots) {
+            e = ensure_reuse(b, slots, st);
+            if (e != cudaSuccess)
+                return ctx_fail(ctx, e == cudaErrorMemoryAllocation ? GRIS_ERR_OUT_OF_MEMORY : GRIS_ERR_CUDA,
+                                std::string("reuse pass buffers: ") + cudaGetErrorString(e));
+        }
+    }
     int form = ctx_path_form(ctx);
     WaveLaunch wl = ctx_wave_launch(ctx);
     guide::GuideDevice gd{};

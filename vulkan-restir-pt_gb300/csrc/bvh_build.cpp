@@ -8,15 +8,18 @@
  * (instanceIdx, triangleIdx) pair, with instance 0 = the light triangles.
  *
  * Steps: (1) world-space triangles; (2) top-down binary BVH by binned SAH (16 bins, leaves of
- * at most 3 triangles, OpenMP tasks for large subtrees); (3) collapse to 8-wide nodes by
- * repeatedly opening the largest-area internal child (Ylitie et al. 2017); (4) order each
- * node's children over 8 slots by a greedy octant assignment; (5) quantise the child boxes
- * to 8 bits per plane, padded and rounded outward, each bound verified in float.
+ * at most 3 triangles, OpenMP tasks for large subtrees); (3) SAH-optimal collapse to 8-wide
+ * nodes by dynamic programming over the binary tree (Ylitie et al. 2017, section 3.1): every
+ * subtree's best use of 1..8 slots, a slot holding a leaf of at most 3 triangles or a wide
+ * internal node; (4) order each node's children over 8 slots by a greedy octant assignment;
+ * (5) quantise the child boxes to 8 bits per plane, padded and rounded outward, each bound
+ * verified in float.
  */
 #include <math.h>
 #include <string.h>
 
 #include <algorithm>
+#include <array>
 #include <atomic>
 #include <chrono>
 #include <vector>
@@ -235,31 +238,96 @@ bool build_bvh(const GrisSceneDesc& d, BvhHost& out, std::string& err) {
 #pragma omp single
     B.build(0, 0, (uint32_t)n);
 
+    /* Every binary subtree's triangle range (contiguous: the builder partitions in place), then
+     * the SAH-optimal collapse to 8-wide nodes (the dynamic programme of Ylitie, Karras & Laine
+     * 2017, section 3.1, written from the paper): cost[n][j-1] = the least SAH cost of covering
+     * subtree n with at most j slots of a wide node, where one slot holds either a leaf (a subtree
+     * of at most 3 triangles: area x kTriCost x triangles) or a wide internal node (area x
+     * kNodeCost + its own 8 slots distributed over the subtree); split[n][j-1] = how many of the j
+     * slots the left child takes when the subtree is split (0: not split). Children have larger
+     * indices than their parents, so a reverse sweep is bottom-up. */
+    const uint32_t nb = B.used.load();
+    std::vector<uint32_t> subFirst(nb), subCount(nb);
+    for (int64_t id = (int64_t)nb - 1; id >= 0; id--) {
+        const BNode& bn = B.nodes[id];
+        if (bn.count > 0) { subFirst[id] = bn.first; subCount[id] = bn.count; }
+        else { subFirst[id] = subFirst[bn.left]; subCount[id] = subCount[bn.left] + subCount[bn.right]; }
+    }
+    constexpr float kNodeCost = 1.0f, kTriCost = 0.5f;   /* a triangle test against a node visit */
+    std::vector<std::array<float, 8>> cost(nb);
+    std::vector<std::array<uint8_t, 8>> split(nb);
+    std::vector<uint8_t> asLeaf(nb);   /* with one slot: a leaf (1) or a wide internal node (0) */
+    for (int64_t id = (int64_t)nb - 1; id >= 0; id--) {
+        const BNode& bn = B.nodes[id];
+        const float area = bn.box.area();
+        const float leafCost = subCount[id] <= 3u ? area * kTriCost * (float)subCount[id] : INFINITY;
+        float dist[9];
+        uint8_t arg[9];
+        for (int j = 0; j <= 8; j++) { dist[j] = INFINITY; arg[j] = 0; }
+        if (bn.count == 0) {
+            for (int j = 2; j <= 8; j++)
+                for (int k = 1; k < j; k++) {
+                    const float c = cost[bn.left][k - 1] + cost[bn.right][j - k - 1];
+                    if (c < dist[j]) { dist[j] = c; arg[j] = (uint8_t)k; }
+                }
+        }
+        const float internalCost = area * kNodeCost + dist[8];
+        asLeaf[id] = leafCost <= internalCost ? 1 : 0;
+        cost[id][0] = std::min(leafCost, internalCost);
+        split[id][0] = 0;
+        for (int j = 2; j <= 8; j++) {
+            if (dist[j] < cost[id][j - 2]) { cost[id][j - 1] = dist[j]; split[id][j - 1] = arg[j]; }
+            else { cost[id][j - 1] = cost[id][j - 2]; split[id][j - 1] = 0; }
+        }
+    }
+    /* the slots of the wide node rooted at binary node r: subtree c with j slots either splits
+     * into its children (split[c][j-1] of them to the left) or, with one slot or none to gain,
+     * takes one slot */
+    struct Slot { int32_t bnode; bool leaf; };
+    auto slots_of = [&](int32_t r, std::vector<Slot>& out) {
+        out.clear();
+        struct Item { int32_t c; int j; };
+        Item st[16];
+        int sp = 0;
+        const BNode& rn = B.nodes[r];
+        if (rn.count > 0) { out.push_back({r, true}); return; }
+        /* the root's own 8 slots: the best distribution between its two children */
+        float best = INFINITY;
+        int bk = 1;
+        for (int k = 1; k < 8; k++) {
+            const float c = cost[rn.left][k - 1] + cost[rn.right][8 - k - 1];
+            if (c < best) { best = c; bk = k; }
+        }
+        st[sp++] = {rn.right, 8 - bk};
+        st[sp++] = {rn.left, bk};
+        while (sp > 0) {
+            Item it = st[--sp];
+            int j = it.j;
+            while (j > 1 && split[it.c][j - 1] == 0) j--;
+            if (j == 1) { out.push_back({it.c, asLeaf[it.c] != 0}); continue; }
+            const int k = split[it.c][j - 1];
+            const BNode& cn = B.nodes[it.c];
+            st[sp++] = {cn.right, j - k};
+            st[sp++] = {cn.left, k};
+        }
+    };
+
     struct Task { uint32_t wide; int32_t bnode; uint32_t depth; };
     std::vector<Task> queue;
     queue.push_back({0, 0, 1});
+    std::vector<Slot> slotList;
     for (size_t qi = 0; qi < queue.size(); qi++) {
         Task task = queue[qi];
         const BNode& bn = B.nodes[task.bnode];
+        slots_of(task.bnode, slotList);
         std::vector<int32_t> ch;
-        if (bn.count > 0) ch.push_back(task.bnode);
-        else { ch.push_back(bn.left); ch.push_back(bn.right); }
-        while (ch.size() < 8) {
-            int best = -1;
-            float bestA = -1.0f;
-            for (size_t i = 0; i < ch.size(); i++) {
-                const BNode& c = B.nodes[ch[i]];
-                if (c.count == 0 && c.box.area() > bestA) { bestA = c.box.area(); best = (int)i; }
-            }
-            if (best < 0) break;
-            int32_t c = ch[best];
-            ch[best] = B.nodes[c].left;
-            ch.push_back(B.nodes[c].right);
-        }
+        std::vector<bool> chLeaf;
+        for (const Slot& sl : slotList) { ch.push_back(sl.bnode); chLeaf.push_back(sl.leaf); }
         /* slot order: slot s holds the child nearest along the diagonal of octant s */
         float pc[3];
         for (int a = 0; a < 3; a++) pc[a] = 0.5f * (bn.box.lo[a] + bn.box.hi[a]);
         int childAt[8];
+        bool leafAt[8] = {false};
         bool slotUsed[8] = {false}, childUsed[8] = {false};
         for (int s = 0; s < 8; s++) childAt[s] = -1;
         for (size_t round = 0; round < ch.size(); round++) {
@@ -278,12 +346,12 @@ bool build_bvh(const GrisSceneDesc& d, BvhHost& out, std::string& err) {
                     if (c < bestC) { bestC = c; bs = s; bi = (int)i; }
                 }
             }
-            slotUsed[bs] = true; childUsed[bi] = true; childAt[bs] = ch[bi];
+            slotUsed[bs] = true; childUsed[bi] = true; childAt[bs] = ch[bi]; leafAt[bs] = chLeaf[bi];
         }
         uint32_t* W = nullptr;
         uint32_t internalCount = 0, imask = 0;
         for (int s = 0; s < 8; s++)
-            if (childAt[s] >= 0 && B.nodes[childAt[s]].count == 0) { imask |= 1u << s; internalCount++; }
+            if (childAt[s] >= 0 && !leafAt[s]) { imask |= 1u << s; internalCount++; }
         uint32_t childBase = (uint32_t)(out.nodes.size() / GRIS_NODE_WORDS);
         uint8_t meta[8] = {0};
         uint32_t rank = 0;
@@ -299,10 +367,10 @@ bool build_bvh(const GrisSceneDesc& d, BvhHost& out, std::string& err) {
         uint32_t triOff = 0;
         for (int s = 0; s < 8; s++) {
             if (childAt[s] < 0 || (imask & (1u << s))) continue;
-            const BNode& leaf = B.nodes[childAt[s]];
-            meta[s] = (uint8_t)(0x80u | (leaf.count << 5) | triOff);
-            for (uint32_t i = 0; i < leaf.count; i++) {
-                uint32_t t = B.idx[leaf.first + i];
+            const uint32_t lfirst = subFirst[childAt[s]], lcount = subCount[childAt[s]];
+            meta[s] = (uint8_t)(0x80u | (lcount << 5) | triOff);
+            for (uint32_t i = 0; i < lcount; i++) {
+                uint32_t t = B.idx[lfirst + i];
                 const float* p = &v[(size_t)t * 9];
                 float rec[12] = {p[0], p[1], p[2], 0.0f, p[3] - p[0], p[4] - p[1], p[5] - p[2], 0.0f,
                                  p[6] - p[0], p[7] - p[1], p[8] - p[2], 0.0f};
@@ -311,7 +379,7 @@ bool build_bvh(const GrisSceneDesc& d, BvhHost& out, std::string& err) {
                 memcpy(&rec[7], &tri, 4);
                 out.tris.insert(out.tris.end(), rec, rec + 12);
             }
-            triOff += leaf.count;
+            triOff += lcount;
         }
         /* quantised child boxes */
         double clo[3][8], chi[3][8];

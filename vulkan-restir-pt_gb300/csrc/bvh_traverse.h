@@ -123,12 +123,82 @@ GRIS_HD bool gris_tri_test(const float* T, float ox, float oy, float oz, float d
 GRIS_HD uint32_t gris_byte(uint32_t w, int i) { return (w >> (i * 8)) & 0xffu; }
 
 /*
+ * The walk's stack of pending node groups. An entry is (first child node of a group, the group's
+ * hit slots | the node's internal-child mask << 8). push() returns false when GRIS_BVH_STACK
+ * entries are held, pop() when none is.
+ *
+ * GrisArrayStack holds every entry in one array: the host walk, and the device walks that run
+ * outside the traversal kernels (per-thread local memory there).
+ */
+struct GrisArrayStack {
+    uint32_t base[GRIS_BVH_STACK], bits[GRIS_BVH_STACK];
+    int n;
+    GRIS_HDM void reset() { n = 0; }
+    GRIS_HDM bool push(uint32_t b, uint32_t m) {
+        if (n >= GRIS_BVH_STACK) return false;
+        base[n] = b; bits[n] = m; n++;
+        return true;
+    }
+    GRIS_HDM bool pop(uint32_t& b, uint32_t& m) {
+        if (n == 0) return false;
+        n--; b = base[n]; m = bits[n];
+        return true;
+    }
+};
+
+#ifdef __CUDACC__
+/*
+ * GrisShortStack (device): the top two entries in registers, the next kShared in the calling
+ * thread's column of a shared-memory slab (entry i at sh[2 i stride] and sh[(2 i + 1) stride],
+ * stride = the block's thread count, so a warp's same-depth accesses hit distinct banks), and
+ * only deeper entries — rare: a wide BVH's walk seldom holds more than a few groups — in a
+ * local-memory overflow array. A pop hands out the register top at once; the refill of the
+ * second register from the slab is off the walk's critical path.
+ */
+template <int kShared>
+struct GrisShortStack {
+    uint32_t b0, m0, b1, m1;
+    uint32_t* sh;
+    uint32_t stride;
+    int n;
+    uint32_t lb[GRIS_BVH_STACK - 2 - kShared], lm[GRIS_BVH_STACK - 2 - kShared];
+    __device__ __forceinline__ void bind(uint32_t* slab, uint32_t tid, uint32_t threads) {
+        sh = slab + tid; stride = threads; n = 0;
+    }
+    __device__ __forceinline__ void reset() { n = 0; }
+    __device__ __forceinline__ void store(int i, uint32_t b, uint32_t m) {
+        if (i < kShared) { sh[(uint32_t)(2 * i) * stride] = b; sh[(uint32_t)(2 * i + 1) * stride] = m; }
+        else { lb[i - kShared] = b; lm[i - kShared] = m; }
+    }
+    __device__ __forceinline__ void load(int i, uint32_t& b, uint32_t& m) const {
+        if (i < kShared) { b = sh[(uint32_t)(2 * i) * stride]; m = sh[(uint32_t)(2 * i + 1) * stride]; }
+        else { b = lb[i - kShared]; m = lm[i - kShared]; }
+    }
+    __device__ __forceinline__ bool push(uint32_t b, uint32_t m) {
+        if (n >= GRIS_BVH_STACK) return false;
+        if (n >= 2) store(n - 2, b1, m1);
+        b1 = b0; m1 = m0; b0 = b; m0 = m; n++;
+        return true;
+    }
+    __device__ __forceinline__ bool pop(uint32_t& b, uint32_t& m) {
+        if (n == 0) return false;
+        b = b0; m = m0; b0 = b1; m0 = m1;
+        if (n >= 3) load(n - 3, b1, m1);
+        n--;
+        return true;
+    }
+};
+#endif
+
+/*
  * One ray's walk of the BVH as a resumable state machine: init() then step() until it returns
  * false (each step visits one node or pops one group). ANY: stop at the first accepted hit
  * (shadow rays). skipInst0: ignore the light instance (the G-buffer is rasterised without
  * lights). *err is set to 1 if the stack limit was reached (the builder guarantees it is not:
  * tree depth <= GRIS_BVH_STACK). Resumable so that a lane whose ray has finished can take the
- * next ray while the other lanes of its warp are still walking.
+ * next ray while the other lanes of its warp are still walking. The stack (GrisArrayStack or
+ * GrisShortStack) is the caller's, reset by it before init(): kept outside the struct, the
+ * struct's scalars stay in registers.
  */
 template <bool ANY>
 struct GrisTraversal {
@@ -137,7 +207,6 @@ struct GrisTraversal {
     float bestT, bestU, bestV;
     uint32_t bestInst, bestTri;
     bool found;
-    int sp;
     uint32_t grpBase, grpHits, grpImask, nodeIdx;
     bool haveNode;
     uint32_t visits, tests;
@@ -153,7 +222,6 @@ struct GrisTraversal {
         bestInst = GRIS_INVALID_HIT; bestTri = GRIS_INVALID_HIT;
         bestU = 0.0f; bestV = 0.0f;
         found = false;
-        sp = 0;
         grpBase = 0; grpHits = 0; grpImask = 0;
         nodeIdx = 0;
         /* A ray with a NaN coordinate hits nothing (every triangle test compares a NaN), but the
@@ -162,11 +230,10 @@ struct GrisTraversal {
         visits = 0; tests = 0;
     }
 
-    /* false: the walk is over (found / best* hold the result). The stack arrays (GRIS_BVH_STACK
-     * entries each) are the caller's: kept outside the struct, the struct's scalars stay in
-     * registers. */
+    /* false: the walk is over (found / best* hold the result) */
+    template <class Stack>
     GRIS_HDM bool step(const uint32_t* __restrict__ nodes, const float* __restrict__ tris, bool skipInst0, int* err,
-                       uint32_t* stackBase, uint32_t* stackBits) {
+                       Stack& stack) {
         if (haveNode) {
             const uint32_t* N = nodes + (uint64_t)nodeIdx * GRIS_NODE_WORDS;
 #ifdef __CUDA_ARCH__
@@ -241,18 +308,15 @@ struct GrisTraversal {
                 }
             }
             if (innerHits) {
-                if (grpHits) {
-                    if (sp >= GRIS_BVH_STACK) { *err = 1; return false; }
-                    stackBase[sp] = grpBase; stackBits[sp] = grpHits | (grpImask << 8); sp++;
-                }
+                if (grpHits && !stack.push(grpBase, grpHits | (grpImask << 8))) { *err = 1; return false; }
                 grpBase = W[4]; grpHits = innerHits; grpImask = imask;
             }
             haveNode = false;
         }
         if (grpHits == 0) {
-            if (sp == 0) return false;
-            sp--;
-            grpBase = stackBase[sp]; grpHits = stackBits[sp] & 0xffu; grpImask = stackBits[sp] >> 8;
+            uint32_t b, m;
+            if (!stack.pop(b, m)) return false;
+            grpBase = b; grpHits = m & 0xffu; grpImask = m >> 8;
         }
         int pos = gris_ffs(grpHits);
         grpHits &= grpHits - 1u;
@@ -276,9 +340,10 @@ GRIS_HD bool gris_bvh_trace(const uint32_t* __restrict__ nodes, const float* __r
                             float tmin, float tmax, bool skipInst0, GrisRayHit* hit, int* err,
                             GrisWork* work) {
     GrisTraversal<ANY> w;
-    uint32_t stackBase[GRIS_BVH_STACK], stackBits[GRIS_BVH_STACK];
+    GrisArrayStack stack;
+    stack.reset();
     w.init(ox, oy, oz, dx, dy, dz, tmin, tmax);
-    while (w.step(nodes, tris, skipInst0, err, stackBase, stackBits)) {}
+    while (w.step(nodes, tris, skipInst0, err, stack)) {}
     w.result(hit, work);
     return w.found;
 }

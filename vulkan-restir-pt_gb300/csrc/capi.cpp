@@ -92,6 +92,7 @@ struct WaveScratch {
     void release() {
         for (void* p : allocations) cudaFree(p);
         allocations.clear();
+        if (wb.reuse.block) cudaFree(wb.reuse.block);
         for (int i = 0; i < 2; i++) {
             if (hViews[i]) cudaFreeHost(hViews[i]);
             if (staged[i]) cudaEventDestroy(staged[i]);
@@ -308,11 +309,11 @@ int grisReadKernelProfile(GrisContext* ctx, GrisKernelProfile out[GRIS_PROFILE_S
     if (!ctx || !out) return GRIS_ERR_INVALID_ARGUMENT;
     cudaSetDevice(ctx->device);
     ctx->prof.collect();
-    GRIS_CK(ctx, cudaMemcpyAsync(ctx->hCounters + 8, ctx->dCounters + 8, 35 * sizeof(unsigned long long),
+    GRIS_CK(ctx, cudaMemcpyAsync(ctx->hCounters + 8, ctx->dCounters + 8, 39 * sizeof(unsigned long long),
                                  cudaMemcpyDeviceToHost, ctx->stream));
     if (reset) {
         GRIS_CK(ctx, cudaMemsetAsync(ctx->dCounters + 8, 0, 16 * sizeof(unsigned long long), ctx->stream));
-        GRIS_CK(ctx, cudaMemsetAsync(ctx->dCounters + 26, 0, 17 * sizeof(unsigned long long), ctx->stream));
+        GRIS_CK(ctx, cudaMemsetAsync(ctx->dCounters + 26, 0, 21 * sizeof(unsigned long long), ctx->stream));
     }
     GRIS_CK(ctx, cudaStreamSynchronize(ctx->stream));
     const unsigned long long* c = ctx->hCounters;
@@ -325,6 +326,10 @@ int grisReadKernelProfile(GrisContext* ctx, GrisKernelProfile out[GRIS_PROFILE_S
         if (k == GRIS_SLOT_WAVE_EXTEND || k == GRIS_SLOT_WAVE_SHADOW) {
             int s = k == GRIS_SLOT_WAVE_EXTEND ? 0 : 1;
             o.nodes = c[26 + 3 * s]; o.tris = c[27 + 3 * s]; o.rays = c[28 + 3 * s];
+        }
+        if (k == GRIS_SLOT_REUSE_VIS_TEMPORAL || k == GRIS_SLOT_REUSE_VIS_SPATIAL) {
+            int r = k - GRIS_SLOT_REUSE_VIS_TEMPORAL;
+            o.nodes = c[41 + 3 * r]; o.tris = c[42 + 3 * r]; o.rays = c[43 + 3 * r];
         }
         if (k >= GRIS_SLOT_DI_CANDIDATES && k <= GRIS_SLOT_DI_SPATIAL) {
             int d = k - GRIS_SLOT_DI_CANDIDATES;
@@ -614,6 +619,18 @@ int grisPassRender(GrisContext* ctx, const GrisScene* s, const GrisPassBindings*
             }
             if (e != cudaSuccess) { w.release(); return cuda_fail(ctx, e, "wavefront scratch"); }
             w.wb.capacity = pixels;
+        }
+        /* the reuse passes' three-launch form: per-slot records for every pixel and neighbour */
+        const uint32_t slots = set->spatialNeighbors > 1u ? set->spatialNeighbors : 1u;
+        if (!set->misWeights && slots <= grisrt::kReuseMaxSlots &&
+            (w.wb.reuse.slots < slots || w.wb.reuse.capacity < pixels)) {
+            cudaStreamSynchronize(ctx->stream);
+            if (w.wb.reuse.block) cudaFree(w.wb.reuse.block);
+            w.wb.reuse = grisrt::ReuseBuffers{};
+            void* p = nullptr;
+            cudaError_t e = cudaMalloc(&p, grisrt::reuse_bytes(pixels, slots));
+            if (e != cudaSuccess) return cuda_fail(ctx, e, "reuse pass buffers");
+            grisrt::reuse_carve(w.wb.reuse, p, pixels, slots);
         }
         grisrt::BatchView v;
         memset(&v, 0, sizeof(v));

@@ -20,6 +20,7 @@
  * pair) and k_wave_post; k_gwave_* are the guided stages.
  */
 #include <cuda_fp16.h>
+#include <cooperative_groups.h>
 #include <cuda_runtime.h>
 
 #include "gris_device.cuh"
@@ -589,6 +590,80 @@ GD void reuseAndMerge(const PassCtx& P, Resv& dstResv, const Surf& dstPrimarySur
     resvCap(dstResv, (float)P.set.cap);
 }
 
+/* The shift of reservoir `src` into the destination pixel up to its reconnection's visibility
+ * query (reuseAndMerge, gris_retrace.glsl:138-219, without the query): the prefix replay, the
+ * reconnection's Jacobian and gates, and what the sample becomes if the query finds the segment
+ * visible — its resampling weight (src.resampleWeight * dstPHat / srcPHat), Jacobian, pdf and F —
+ * with the query's endpoints. Returns kShiftNoQuery when the shift fails before the query (the
+ * source then merges with weight 0), kShiftQuery when the query decides between that weight and
+ * 0, kShiftQueryBadWeight when the weight if visible is not a valid weight (NaN or negative: a
+ * visible segment then merges nothing, an occluded one merges with weight 0). */
+constexpr int kShiftNoQuery = 0, kShiftQuery = 1, kShiftQueryBadWeight = 2;
+struct ShiftPending {
+    float rw, jac, pdf;
+    V3 F, from, to;
+};
+GD int shift_until_query(const PassCtx& P, const Surf& dst, const Isec& dstIsec, const Ray3& ray, const Resv& src,
+                         const guide::Lobes* Lp, ShiftPending& q, RayCount& rc, int& err) {
+    const DevScene& sc = P.sc;
+    const PathSample& s = src.s;
+    RcData rd;
+    rd.rcPrevIsec = isec_zero(); rd.rcPrevWo = v3s(0.0f); rd.rcPrevThroughput = v3s(0.0f);
+    Surf rcPrevSurf = surf_zero(), rcSurf = surf_zero();
+    q.rw = 0.0f; q.jac = 0.0f; q.pdf = 0.0f; q.F = v3s(0.0f);
+    bool query = false;
+    float dstJacobian = 0.0f, jacobian = 0.0f;
+    V3 wi = v3s(0.0f);
+    Mat rcMat = load_material(sc, 0xffffffffu), rcPrevMat = rcMat;
+    if (s.rcIsec.inst != kInvalidHit) {
+        traceReplay(P, dstIsec, dst, ray, s.flags, s.primaryRng, rd, rc, err, Lp);
+        if (rd.rcPrevIsec.inst != kInvalidHit) {
+            if (rd.rcPrevIsec.inst == kSpecialHit) rcPrevSurf = dst;
+            else loadSurfaceInfo(sc, rd.rcPrevIsec, rcPrevSurf);
+            loadSurfaceInfo(sc, s.rcIsec, rcSurf);
+            rcMat = load_material(sc, rcSurf.matIndex);
+            rcPrevMat = load_material(sc, rcPrevSurf.matIndex);
+            float dist = distance3(rcPrevSurf.pos, rcSurf.pos);
+            wi = normalize3(rcSurf.pos - rcPrevSurf.pos);
+            float cosTheta = -dot3(rcSurf.norm, wi);
+            dstJacobian = fabsf(cosTheta) / square(dist);
+            jacobian = dstJacobian / s.rcJacobian;
+            query = dist > kDistanceThreshold && cosTheta > 0.0f && !isnan(jacobian) && s.rcJacobian > 0.0f &&
+                    isBSDFConnectible(rcPrevMat);
+        }
+    }
+    if (!query) return kShiftNoQuery;
+    V3 Li = v3s(0.0f);
+    float dstPHat = 0.0f, dstSamplePdf = 0.0f;
+    uint32_t rcType = rcVertexType(s.flags);
+    if (!isnan(s.rcPrevSamplePdf) && s.rcPrevSamplePdf > 1e-6f) {
+        Li = s.rcLi;
+        if (rcType == kRcSurface && length3(s.rcWi) > 0.5f) {
+            Li = Li * (evalBSDFCall(rcMat, rcSurf.albedo, rcSurf.norm, -wi, s.rcWi) * satDot(rcSurf.norm, s.rcWi));
+        }
+        Li = Li * (evalBSDFCall(rcPrevMat, rcPrevSurf.albedo, rcPrevSurf.norm, rd.rcPrevWo, wi) * satDot(rcPrevSurf.norm, wi));
+        Li = Li * rd.rcPrevThroughput;
+        Li = Li / s.rcPrevSamplePdf;
+        if (!isBlack(Li) && !isnan3(Li)) dstPHat = luminance(Li * jacobian);
+        if (rcType == kRcLightSampled) {
+            float sumPower = load_table(sc, 0).prob;
+            dstSamplePdf = luminance(rcSurf.albedo) / sumPower / dstJacobian;
+        } else {
+            dstSamplePdf = evalPdf(rcPrevMat, rcPrevSurf.norm, rd.rcPrevWo, wi);
+            if (Lp && rd.rcPrevIsec.inst == kSpecialHit)
+                dstSamplePdf = P.gMix * guide::lobes_pdf(*Lp, wi.x, wi.y, wi.z) + (1.0f - P.gMix) * dstSamplePdf;
+        }
+    }
+    float srcPHat = luminance(s.F);
+    q.rw = src.resampleWeight * (dstPHat / srcPHat);
+    q.jac = dstJacobian;
+    q.pdf = (dstSamplePdf < 1e-6f || isnan(dstSamplePdf)) ? 0.0f : dstSamplePdf;
+    q.F = Li;
+    q.from = rcPrevSurf.pos;
+    q.to = rcSurf.pos;
+    return (!isnan(q.rw) && q.rw >= 0.0f) ? kShiftQuery : kShiftQueryBadWeight;
+}
+
 /* Pairwise generalised balance heuristic (GrisSettings.misWeights = 1). The canonical reservoir
  * c (M_c, sample x_c) and k reused reservoirs i (M_i, x_i): pair i weighs technique i against
  * a 1/k share of the canonical one, m_i(y) = M_i p_i(y) / (M_i p_i(y) + (M_c/k) p_c(y)), where
@@ -1005,6 +1080,14 @@ struct SpatialTaskT {
             return true;
         }
         if (kPair && P.set.misWeights && P.set.spatialReuse && P.set.spatialNeighbors > 0u) resv = pm.finish(sample1f(rng), (float)P.set.cap);
+        shade_final(P, rc, err);
+        return false;
+    }
+
+    /* After the neighbours: the pixel's reservoir is stored, its sample replayed and shaded
+     * (gris_resample_spatial.glsl:88-133) and the result added to the running mean. */
+    GD void shade_final(const PassCtx& P, RayCount& rc, int& err) {
+        const DevScene& sc = P.sc;
         resvResetIfInvalid(resv);
         store_resv(P.b.reservoirThis, idx, resv);
         V3 radiance = v3s(0.0f);
@@ -1039,7 +1122,6 @@ struct SpatialTaskT {
             }
         }
         accumulate(P, ix, iy, clampColor(radiance));
-        return false;
     }
 };
 using SpatialTask = SpatialTaskT<false>;
@@ -1229,16 +1311,34 @@ __global__ void __launch_bounds__(128) k_gbuffer(GBufCtx G) {
     flush_gbuffer_counts(G.counters, primary, err, work, G.countWork);
 }
 
-/* Builder check: one ray per thread. */
-__global__ void k_debug_trace(const uint32_t* nodes, const float* tris, const float* rays, uint64_t n, int anyHit,
-                              float* hitTUV, uint32_t* hitInst, uint32_t* hitTri, unsigned long long* counters) {
+/* One whole walk with the resident kernels' stack, here with a single shared-memory entry, so that
+ * walks of depth 4 and more already use all three of its tiers (registers, shared memory, the
+ * local-memory overflow). */
+template <bool ANY>
+GD bool debug_walk_short_stack(const uint32_t* nodes, const float* tris, const float* r, uint32_t* slab, GrisRayHit* h,
+                               int* err) {
+    GrisTraversal<ANY> w;
+    GrisShortStack<1> stack;
+    stack.bind(slab, threadIdx.x, blockDim.x);
+    w.init(r[0], r[1], r[2], r[4], r[5], r[6], r[3], r[7]);
+    while (w.step(nodes, tris, false, err, stack)) {}
+    w.result(h, nullptr);
+    return w.found;
+}
+
+/* Builder check: one ray per thread, walked with the short stack of the resident traversal
+ * kernels (k_wave_trace_refill, k_reuse_visibility) in a small configuration. */
+__global__ void __launch_bounds__(128) k_debug_trace(const uint32_t* nodes, const float* tris, const float* rays, uint64_t n,
+                                                     int anyHit, float* hitTUV, uint32_t* hitInst, uint32_t* hitTri,
+                                                     unsigned long long* counters) {
+    __shared__ uint32_t slab[2 * 1 * 128];
     uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     const float* r = rays + i * 8;
     GrisRayHit h;
     int err = 0;
-    bool hit = anyHit ? gris_bvh_trace<true>(nodes, tris, r[0], r[1], r[2], r[4], r[5], r[6], r[3], r[7], false, &h, &err, nullptr)
-                      : gris_bvh_trace<false>(nodes, tris, r[0], r[1], r[2], r[4], r[5], r[6], r[3], r[7], false, &h, &err, nullptr);
+    bool hit = anyHit ? debug_walk_short_stack<true>(nodes, tris, r, slab, &h, &err)
+                      : debug_walk_short_stack<false>(nodes, tris, r, slab, &h, &err);
     if (hit) { hitTUV[i * 4] = h.t; hitTUV[i * 4 + 1] = h.u; hitTUV[i * 4 + 2] = h.v; hitTUV[i * 4 + 3] = 0.0f; hitInst[i] = h.inst; hitTri[i] = h.tri; }
     else { hitTUV[i * 4] = -1.0f; hitTUV[i * 4 + 1] = 0.0f; hitTUV[i * 4 + 2] = 0.0f; hitTUV[i * 4 + 3] = 0.0f; hitInst[i] = GRIS_INVALID_HIT; hitTri[i] = GRIS_INVALID_HIT; }
     if (err) atomicOr(counters + GRIS_COUNTER_ERROR, 1ull);
@@ -1726,6 +1826,17 @@ __global__ void __launch_bounds__(128) k_wave_extend(WaveCtx C, int level) {
  * the warp. The closest hit is the lexicographic minimum of (t, instanceIdx, triangleIdx) over
  * the accepted triangles, and an any-hit query asks only whether one exists, so the order of the
  * visits does not change a result: k_wave_trace_refill's results, bit for bit. */
+/* entries of a resident walk's stack held in shared memory (after two in registers) */
+#ifndef GRIS_WALK_SHARED_ENTRIES
+#define GRIS_WALK_SHARED_ENTRIES 8
+#endif
+constexpr int kWalkSharedEntries = GRIS_WALK_SHARED_ENTRIES;
+/* resident blocks of 128 threads per SM asked of the compiler for the resident traversal kernels
+ * (0: no request) */
+#ifndef GRIS_WALK_MIN_BLOCKS
+#define GRIS_WALK_MIN_BLOCKS 0
+#endif
+constexpr int kWalkMinBlocks = GRIS_WALK_MIN_BLOCKS;
 constexpr uint32_t kCoopMaxRays = 8192;
 constexpr uint32_t kCoopStack = 1024;      /* node indices per warp (pushes are at most 32 per round) */
 constexpr uint32_t kCoopTris = 96;         /* triangles per round: 4 nodes x 8 slots x 3 */
@@ -1896,7 +2007,7 @@ __global__ void __launch_bounds__(128) k_wave_trace_coop(WaveCtx C, int level) {
  * level's cursor), so lanes do not wait for the longest walk of their warp. Same walks, same
  * results as k_wave_extend / k_wave_shadow. */
 template <bool ANY>
-__global__ void __launch_bounds__(128) k_wave_trace_refill(WaveCtx C, int level) {
+__global__ void __launch_bounds__(128, kWalkMinBlocks) k_wave_trace_refill(WaveCtx C, int level) {
     const uint32_t n = ANY ? C.counts[256 + level] : C.counts[level];
     if (n < kCoopMaxRays) return;                         /* k_wave_trace_coop takes a sparse level */
     const uint32_t* q = ANY ? C.shadowQueue : C.queue[level & 1];
@@ -1905,7 +2016,9 @@ __global__ void __launch_bounds__(128) k_wave_trace_refill(WaveCtx C, int level)
     RayCount rc = ray_count();
     int err = 0;
     GrisTraversal<ANY> tr;
-    uint32_t stackBase[GRIS_BVH_STACK], stackBits[GRIS_BVH_STACK];
+    __shared__ uint32_t sStack[2 * (kWalkSharedEntries > 0 ? kWalkSharedEntries : 1) * 128];
+    GrisShortStack<kWalkSharedEntries> stack;
+    stack.bind(sStack, threadIdx.x, 128u);
     const uint32_t* nodes = nullptr;
     const float* tris = nullptr;
     uint32_t id = 0;
@@ -1923,6 +2036,7 @@ __global__ void __launch_bounds__(128) k_wave_trace_refill(WaveCtx C, int level)
                     int v = find_view_by_pixel(C.V, C.nViews, id);
                     nodes = C.V[v].P.sc.nodes;
                     tris = C.V[v].P.sc.tris;
+                    stack.reset();
                     if (ANY) {
                         const uint4* w = C.nee[id].w;
                         uint4 a = w[0], d4 = w[4], r3 = w[3];
@@ -1944,7 +2058,7 @@ __global__ void __launch_bounds__(128) k_wave_trace_refill(WaveCtx C, int level)
             if (!more) break;
             continue;
         }
-        if (active && !tr.step(nodes, tris, false, &err, stackBase, stackBits)) {
+        if (active && !tr.step(nodes, tris, false, &err, stack)) {
             GrisRayHit h;
             tr.result(&h, &rc.work);
             if (ANY) {
@@ -2036,6 +2150,313 @@ __global__ void __launch_bounds__(128) k_wave_post(WaveCtx C, int level) {
         }
         warp_push(C.queue[(level + 1) & 1], C.counts + level + 1, push, id);
     }
+}
+
+/* ------------------------------------------------------------------ reuse passes in three launches */
+/* The temporal and spatial passes of a batch as prepare -> visibility walk -> finish (views
+ * without pairwise weights; the per-pixel kernels k_batch_pass<TemporalTask / SpatialTask> stay
+ * for the other forms). A reconnection's visibility query is the bulk of a reuse pass's time, and
+ * inside a per-pixel kernel the few lanes that issue one leave the rest of their warp waiting:
+ *   prepare  per pixel (and neighbour): the gathers, the gates, the prefix replay and the shift up
+ *            to the visibility query (shift_until_query), the merge's random draw where the
+ *            reference takes it; the query goes into a compacted queue, what the merge needs
+ *            into per-slot records;
+ *   walk     the queue by the refilling any-hit traversal (every lane busy until it is empty);
+ *            a visible segment sets its slot's kRsVisible bit;
+ *   finish   per pixel: the merges and M caps in neighbour order with the verdicts, the selected
+ *            source sample (with the shifted Jacobian, pdf and F when visible), then the temporal
+ *            reservoir, or the spatial reservoir, final shading and running mean.
+ * Same operations on the same values in the same order as the per-pixel kernels: results bit for
+ * bit identical, ray counts equal. Slot k of pixel p (batch pixel id) lives at k * R.P + p. */
+constexpr uint8_t kRsEntry = 1u, kRsMerge = 2u, kRsQuery = 4u, kRsVisible = 8u, kRsBadWeight = 16u, kRsActive = 128u;
+
+struct ReuseCtx {
+    float4* pa;          /* weight if visible, source M, shifted Jacobian, shifted pdf */
+    float4* pb;          /* shifted F, merge draw */
+    uint32_t* pn;        /* source pixel (in the view) */
+    uint8_t* ps;         /* kRs* bits; slot 0 also carries kRsActive for a non-background pixel */
+    float4* q;           /* per query: origin + tmax, direction + slot */
+    uint32_t* counts;    /* [0] temporal queries, [1] their cursor, [2] spatial queries, [3] their cursor */
+    uint32_t P;          /* slot stride = pixels of the batch */
+    uint64_t qCap;       /* queries the queue holds */
+};
+
+/* Appends the visibility query of `q` (traceVisibility's ray: from -> to, tmin = MinRayDistance,
+ * tmax = distance - MinRayDistance) for `slot`, one atomic per group of converged lanes. */
+GD void reuse_push_query(const ReuseCtx& R, uint32_t* count, const ShiftPending& q, uint32_t slot, int& err) {
+    namespace cg = cooperative_groups;
+    cg::coalesced_group g = cg::coalesced_threads();
+    uint32_t base = 0;
+    if (g.thread_rank() == 0) base = atomicAdd(count, g.size());
+    base = g.shfl(base, 0) + g.thread_rank();
+    if ((uint64_t)base >= R.qCap) { err = 1; return; }   /* not reached: the queue holds a query per slot */
+    const V3 d = normalize3(q.to - q.from);
+    const float tmax = distance3(q.to, q.from) - kMinRayDistance;
+    R.q[2 * (uint64_t)base] = make_float4(q.from.x, q.from.y, q.from.z, tmax);
+    R.q[2 * (uint64_t)base + 1] = make_float4(d.x, d.y, d.z, __uint_as_float(slot));
+}
+
+/* resident blocks of 128 threads per SM asked of the compiler for the prepare / finish kernels */
+#ifndef GRIS_REUSE_PREPARE_BLOCKS
+#define GRIS_REUSE_PREPARE_BLOCKS 8
+#endif
+#ifndef GRIS_REUSE_FINISH_BLOCKS
+#define GRIS_REUSE_FINISH_BLOCKS 8
+#endif
+constexpr int kReusePrepareBlocks = GRIS_REUSE_PREPARE_BLOCKS, kReuseFinishBlocks = GRIS_REUSE_FINISH_BLOCKS;
+
+template <bool kGuide>
+__global__ void __launch_bounds__(128, kReusePrepareBlocks) k_reuse_temporal_prepare(const ViewEntry* __restrict__ V, int n,
+                                                                                     ReuseCtx R) {
+    const int v = find_view_by_tile(V, n, blockIdx.x);
+    const PassCtx& P = V[v].P;
+    const uint32_t t = blockIdx.x - V[v].tileBase;
+    const uint32_t x = (t % V[v].tilesX) * 16u + threadIdx.x, y = (t / V[v].tilesX) * 8u + threadIdx.y;
+    RayCount rc = ray_count();
+    int err = 0;
+    if (x < P.b.width && y < P.b.height) {
+        const uint32_t pix = V[v].pixelBase + y * P.b.width + x;
+        TemporalTaskT<kGuide> task;
+        uint8_t state = 0;
+        if (task.begin(P, x, y, rc, err)) {   /* false: nothing to merge, the temporary reservoir is written */
+            const guide::Lobes* Lp = nullptr;
+            guide::Lobes L;
+            if constexpr (kGuide) {
+                if (primary_lobes(P, task.idx, load_material(P.sc, task.dst.matIndex), L)) Lp = &L;
+            }
+            ShiftPending q;
+            const int kind = shift_until_query(P, task.dst, task.dstIsec, task.ray, task.src, Lp, q, rc, err);
+            state = kRsEntry;
+            if (kind != kShiftNoQuery) {
+                state |= kRsQuery | (kind == kShiftQueryBadWeight ? kRsBadWeight : 0u);
+                reuse_push_query(R, R.counts + 0, q, pix, err);
+            }
+            R.pa[pix] = make_float4(q.rw, task.src.sampleCount, q.jac, q.pdf);
+            R.pb[pix] = make_float4(q.F.x, q.F.y, q.F.z, 0.0f);
+            R.pn[pix] = task.pidx;
+        }
+        R.ps[pix] = state;
+    }
+    flush_counts(P.counters, rc, err, 2, P.countWork);
+}
+
+/* reuseAndMerge's merge and cap with the verdict, then TemporalTaskT::finish */
+__global__ void __launch_bounds__(128, kReuseFinishBlocks) k_reuse_temporal_finish(const ViewEntry* __restrict__ V, int n,
+                                                                                    ReuseCtx R) {
+    const int v = find_view_by_tile(V, n, blockIdx.x);
+    const PassCtx& P = V[v].P;
+    const uint32_t t = blockIdx.x - V[v].tileBase;
+    const uint32_t x = (t % V[v].tilesX) * 16u + threadIdx.x, y = (t / V[v].tilesX) * 8u + threadIdx.y;
+    if (x >= P.b.width || y >= P.b.height) return;
+    const uint32_t pix = V[v].pixelBase + y * P.b.width + x;
+    const uint8_t state = R.ps[pix];
+    if (!(state & kRsEntry)) return;
+    const uint64_t idx = (uint64_t)y * P.b.width + x, npx = (uint64_t)P.b.width * P.b.height;
+    Resv resv = load_resv(P.b.reservoirThis, idx, npx);
+    const float4 a = R.pa[pix];
+    const bool visible = (state & kRsVisible) != 0u;
+    const float w = visible ? a.x : 0.0f;   /* the source's weight: 0 unless the segment is visible */
+    if (!isnan(w) && w >= 0.0f) {           /* resvIsValid(srcResv): merge */
+        uint32_t resvRng = ~(makeSeed2(P.cam.seed, x, y) ^ 1u);
+        const float rnd = sample1f(resvRng);
+        resv.sampleCount += a.y;
+        resv.resampleWeight += w;
+        if (rnd * resv.resampleWeight < w) {
+            resv.s = load_resv(P.b.reservoirPrev, R.pn[pix], npx).s;
+            if (visible) {
+                const float4 b = R.pb[pix];
+                resv.s.rcJacobian = a.z;
+                resv.s.rcPrevSamplePdf = a.w;
+                resv.s.F = v3(b.x, b.y, b.z);
+            }
+        }
+    }
+    resvCap(resv, (float)P.set.cap);
+    resvResetIfInvalid(resv);
+    store_resv(P.b.reservoirTemp, idx, resv);
+}
+
+template <bool kGuide>
+__global__ void __launch_bounds__(128, kReusePrepareBlocks) k_reuse_spatial_prepare(const ViewEntry* __restrict__ V, int n,
+                                                                                    ReuseCtx R) {
+    const int v = find_view_by_tile(V, n, blockIdx.x);
+    const PassCtx& P = V[v].P;
+    const uint32_t t = blockIdx.x - V[v].tileBase;
+    const uint32_t x = (t % V[v].tilesX) * 16u + threadIdx.x, y = (t / V[v].tilesX) * 8u + threadIdx.y;
+    RayCount rc = ray_count();
+    int err = 0;
+    if (x < P.b.width && y < P.b.height) {
+        const uint32_t pix = V[v].pixelBase + y * P.b.width + x;
+        SpatialTaskT<kGuide> task;
+        const bool active = task.begin(P, x, y, rc, err);   /* false: background, its running mean is updated */
+        R.ps[pix] = active ? kRsActive : 0u;
+        if (active && P.set.spatialReuse) {
+            const DevScene& sc = P.sc;
+            const int W = (int)P.b.width, H = (int)P.b.height;
+            const uint64_t npx = (uint64_t)W * (uint64_t)H;
+            const float tx = 1.0f / (float)W, ty = 1.0f / (float)H;
+            const V2 uv = v2(task.dstIsec.bx, task.dstIsec.by);
+            const guide::Lobes* Lp = nullptr;
+            guide::Lobes L;
+            if constexpr (kGuide) {
+                if (primary_lobes(P, task.idx, load_material(sc, task.dst.matIndex), L)) Lp = &L;
+            }
+            for (uint32_t k = 0; k < P.set.spatialNeighbors; k++) {
+                const uint32_t slot = k * R.P + pix;
+                uint8_t st = 0;
+                /* findNeighborReservoir (gris_resample_spatial.glsl:11-34) */
+                const V2 d = toConcentricDisk(sample2f(task.rng));
+                const V2 nb = v2(uv.x + d.x * P.set.spatialRadius * tx, uv.y + d.y * P.set.spatialRadius * ty);
+                bool found = !(nb.x < 0.0f || nb.y < 0.0f || nb.x > 1.0f || nb.y > 1.0f);
+                uint32_t nidx = 0;
+                Resv src;
+                if (found) {
+                    const int px = (int)(nb.x * (float)P.cam.w), py = (int)(nb.y * (float)P.cam.h);
+                    float depthN = 0.0f; V3 normalN = v3s(0.0f), albedoN = v3s(0.0f); int matMeshIdN = 0;
+                    const float4 ndn = texture_bilinear(reinterpret_cast<const float4*>(P.b.depthNormal), W, H, nb);
+                    const uint2 nam = fetch_am(reinterpret_cast<const uint2*>(P.b.albedoMatId), W, H, px, py);
+                    found = unpackGBuffer(ndn, nam, depthN, normalN, albedoN, matMeshIdN);
+                    if (found) {
+                        const Ray3 nray = pinholeCameraSampleRay(P.cam, v2(nb.x, 1.0f - nb.y));
+                        const V3 posN = nray.ori + nray.dir * (depthN - 1e-4f);
+                        found = !(dot3(normalN, task.dst.norm) < 0.9f || distance3(task.dst.pos, posN) > 0.4f);
+                        nidx = (uint32_t)P.cam.w * (uint32_t)py + (uint32_t)px;
+                    }
+                }
+                if (found) {
+                    src = load_resv(P.b.reservoirTemp, nidx, npx);
+                    found = resvIsValid(src);
+                }
+                if (found) {
+                    ShiftPending q;
+                    const int kind = shift_until_query(P, task.dst, task.dstIsec, task.ray, src, Lp, q, rc, err);
+                    bool merge = true;
+                    st = kRsEntry;
+                    if (kind == kShiftQuery) {
+                        st |= kRsQuery;
+                        reuse_push_query(R, R.counts + 2, q, slot, err);
+                    } else if (kind == kShiftQueryBadWeight) {
+                        /* the verdict decides whether the merge (and its draw) happens: answered here */
+                        merge = !traceVisibility(sc, q.from, q.to, rc, err);
+                    }
+                    float rnd = 0.0f;
+                    if (merge) { st |= kRsMerge; rnd = sample1f(task.rng); }
+                    R.pa[slot] = make_float4(q.rw, src.sampleCount, q.jac, q.pdf);
+                    R.pb[slot] = make_float4(q.F.x, q.F.y, q.F.z, rnd);
+                    R.pn[slot] = nidx;
+                }
+                R.ps[slot] = k == 0u ? (uint8_t)(st | kRsActive) : st;
+            }
+        }
+    }
+    flush_counts(P.counters, rc, err, 3, P.countWork);
+}
+
+/* the merges and caps in neighbour order with the verdicts (SpatialTaskT::reuse_phased's last
+ * phase), then SpatialTaskT::shade_final */
+template <bool kGuide>
+__global__ void __launch_bounds__(128, kReuseFinishBlocks) k_reuse_spatial_finish(const ViewEntry* __restrict__ V, int n,
+                                                                                   ReuseCtx R) {
+    const int v = find_view_by_tile(V, n, blockIdx.x);
+    const PassCtx& P = V[v].P;
+    const uint32_t t = blockIdx.x - V[v].tileBase;
+    const uint32_t x = (t % V[v].tilesX) * 16u + threadIdx.x, y = (t / V[v].tilesX) * 8u + threadIdx.y;
+    RayCount rc = ray_count();
+    int err = 0;
+    if (x < P.b.width && y < P.b.height) {
+        const uint32_t pix = V[v].pixelBase + y * P.b.width + x;
+        if (R.ps[pix] & kRsActive) {
+            SpatialTaskT<kGuide> task;
+            task.begin(P, x, y, rc, err);   /* the pixel's surface, ray and temporary reservoir */
+            if (P.set.spatialReuse) {
+                int sel = -1;
+                float4 sa = make_float4(0.0f, 0.0f, 0.0f, 0.0f), sb = sa;
+                bool svis = false;
+                for (uint32_t k = 0; k < P.set.spatialNeighbors; k++) {
+                    const uint32_t slot = k * R.P + pix;
+                    const uint8_t st = R.ps[slot];
+                    if (!(st & kRsEntry)) continue;
+                    if (st & kRsMerge) {
+                        const float4 a = R.pa[slot], b = R.pb[slot];
+                        const bool vis = (st & kRsVisible) != 0u;
+                        const float w = vis ? a.x : 0.0f;
+                        task.resv.sampleCount += a.y;
+                        task.resv.resampleWeight += w;
+                        if (b.w * task.resv.resampleWeight < w) { sel = (int)k; sa = a; sb = b; svis = vis; }
+                    }
+                    resvCap(task.resv, (float)P.set.cap);
+                }
+                if (sel >= 0) {
+                    const uint64_t npx = (uint64_t)P.b.width * P.b.height;
+                    task.resv.s = load_resv(P.b.reservoirTemp, R.pn[(uint32_t)sel * R.P + pix], npx).s;
+                    if (svis) {
+                        task.resv.s.rcJacobian = sa.z;
+                        task.resv.s.rcPrevSamplePdf = sa.w;
+                        task.resv.s.F = v3(sb.x, sb.y, sb.z);
+                    }
+                }
+            }
+            task.shade_final(P, rc, err);
+        }
+    }
+    flush_counts(P.counters, rc, err, 3, P.countWork);
+}
+
+/* The pass's visibility queries, resident form of k_wave_trace_refill<true>: every lane walks its
+ * own query step by step, and whenever a quarter of a warp's lanes are idle the warp takes that
+ * many queries from the queue. KERNEL: the pass whose counters the walks add to (2 temporal,
+ * 3 spatial); which = 0 temporal queue, 1 spatial queue. */
+template <int KERNEL>
+__global__ void __launch_bounds__(128, kWalkMinBlocks) k_reuse_visibility(const ViewEntry* __restrict__ V, int nViews, ReuseCtx R,
+                                                                          int which) {
+    const uint32_t n = R.counts[2 * which];
+    uint32_t* cursor = R.counts + 2 * which + 1;
+    const uint32_t lane = threadIdx.x & 31u;
+    RayCount rc = ray_count();
+    int err = 0;
+    GrisTraversal<true> tr;
+    __shared__ uint32_t sStack[2 * (kWalkSharedEntries > 0 ? kWalkSharedEntries : 1) * 128];
+    GrisShortStack<kWalkSharedEntries> stack;
+    stack.bind(sStack, threadIdx.x, 128u);
+    const uint32_t* nodes = nullptr;
+    const float* tris = nullptr;
+    uint32_t slot = 0;
+    bool active = false, more = n > 0u;
+    while (true) {
+        unsigned idle = __ballot_sync(0xffffffffu, !active);
+        if (more && __popc(idle) >= 8) {
+            const uint32_t take = (uint32_t)__popc(idle), leader = __ffs(idle) - 1;
+            uint32_t base = 0;
+            if (lane == leader) base = atomicAdd(cursor, take);
+            base = __shfl_sync(0xffffffffu, base, leader);
+            if (!active) {
+                const uint32_t i = base + (uint32_t)__popc(idle & ((1u << lane) - 1u));
+                if (i < n) {
+                    const float4 a = R.q[2 * (uint64_t)i], b = R.q[2 * (uint64_t)i + 1];
+                    slot = __float_as_uint(b.w);
+                    const int v = find_view_by_pixel(V, nViews, slot % R.P);
+                    nodes = V[v].P.sc.nodes;
+                    tris = V[v].P.sc.tris;
+                    stack.reset();
+                    tr.init(a.x, a.y, a.z, b.x, b.y, b.z, kMinRayDistance, a.w);
+                    active = true;
+                }
+            }
+            if (base + take >= n) more = false;
+        }
+        if (__ballot_sync(0xffffffffu, active) == 0u) {
+            if (!more) break;
+            continue;
+        }
+        if (active && !tr.step(nodes, tris, false, &err, stack)) {
+            GrisRayHit h;
+            tr.result(&h, &rc.work);
+            rc.shadow++;
+            if (!tr.found) R.ps[slot] |= kRsVisible;
+            active = false;
+        }
+    }
+    flush_counts(V[0].P.counters, rc, err, KERNEL, V[0].P.countWork, KERNEL);
 }
 
 /* ------------------------------------------------------------------ guided wavefront */
@@ -2230,6 +2651,25 @@ size_t guide_wave_bytes_per_path() {
 
 size_t wave_bytes_per_path() { return sizeof(WaveRec) + sizeof(NeeRec) + sizeof(Isec) + 1 + 3 * sizeof(uint32_t); }
 
+static size_t reuse_up(size_t n) { return (n + 255) & ~(size_t)255; }
+size_t reuse_bytes(uint64_t pixels, uint32_t slots) {
+    const size_t s = (size_t)pixels * slots;
+    return 2 * reuse_up(s * 16) + reuse_up(s * 4) + reuse_up(s) + reuse_up(s * 32) + 256;
+}
+void reuse_carve(ReuseBuffers& r, void* block, uint64_t pixels, uint32_t slots) {
+    const size_t s = (size_t)pixels * slots;
+    char* p = (char*)block;
+    r.block = block;
+    r.pa = p; p += reuse_up(s * 16);
+    r.pb = p; p += reuse_up(s * 16);
+    r.pn = (uint32_t*)p; p += reuse_up(s * 4);
+    r.ps = (unsigned char*)p; p += reuse_up(s);
+    r.q = p; p += reuse_up(s * 32);
+    r.counts = (uint32_t*)p;
+    r.slots = slots;
+    r.capacity = pixels;
+}
+
 BatchShape fill_view_table(const BatchView* views, int n, void* hViews, unsigned long long* counters, int countWork,
                            const float* gPrim, float gMix) {
     BatchShape sh;
@@ -2267,6 +2707,7 @@ BatchShape fill_view_table(const BatchView* views, int n, void* hViews, unsigned
         sh.pixels += bv.b.width * bv.b.height;
         if ((int)bv.set.maxDepth > sh.maxDepth) sh.maxDepth = (int)bv.set.maxDepth;
         if (bv.set.misWeights) sh.pairwise = true;
+        if (bv.set.spatialNeighbors > sh.maxNeighbours) sh.maxNeighbours = bv.set.spatialNeighbors;
     }
     return sh;
 }
@@ -2384,6 +2825,46 @@ cudaError_t enqueue_batch(const BatchShape& sh, void* dViews, const void* hViews
         if (timer) timer->mark(1, false, stream);
     }
 reuse:
+    /* the three-launch form of the reuse passes where its buffers fit the frame */
+    const bool split = wb.reuse.slots > 0u && !sh.pairwise && sh.maxNeighbours <= wb.reuse.slots &&
+                       (uint64_t)sh.pixels <= wb.reuse.capacity && (passes & 6);
+    ReuseCtx R;
+    memset(&R, 0, sizeof(R));
+    if (split) {
+        R.pa = reinterpret_cast<float4*>(wb.reuse.pa);
+        R.pb = reinterpret_cast<float4*>(wb.reuse.pb);
+        R.pn = wb.reuse.pn;
+        R.ps = wb.reuse.ps;
+        R.q = reinterpret_cast<float4*>(wb.reuse.q);
+        R.counts = wb.reuse.counts;
+        R.P = pixels;
+        R.qCap = (uint64_t)pixels * wb.reuse.slots;
+        e = cudaMemsetAsync(wb.reuse.counts, 0, 4 * sizeof(uint32_t), stream);
+        if (e != cudaSuccess) return e;
+    }
+    const int gridVis = current_sm_count() * (wl.traceBlocksPerSM > 0 ? wl.traceBlocksPerSM : 16);
+    if (split && (passes & 2)) {
+        if (timer) timer->mark(2, true, stream);
+        if (guide) k_reuse_temporal_prepare<true><<<tiles, blk, 0, stream>>>(V, n, R);
+        else k_reuse_temporal_prepare<false><<<tiles, blk, 0, stream>>>(V, n, R);
+        if (timer) timer->mark(GRIS_SLOT_REUSE_VIS_TEMPORAL, true, stream);
+        k_reuse_visibility<2><<<gridVis, 128, 0, stream>>>(V, n, R, 0);
+        if (timer) timer->mark(GRIS_SLOT_REUSE_VIS_TEMPORAL, false, stream);
+        k_reuse_temporal_finish<<<tiles, blk, 0, stream>>>(V, n, R);
+        if (timer) timer->mark(2, false, stream);
+    }
+    if (split && (passes & 4)) {
+        if (timer) timer->mark(3, true, stream);
+        if (guide) k_reuse_spatial_prepare<true><<<tiles, blk, 0, stream>>>(V, n, R);
+        else k_reuse_spatial_prepare<false><<<tiles, blk, 0, stream>>>(V, n, R);
+        if (timer) timer->mark(GRIS_SLOT_REUSE_VIS_SPATIAL, true, stream);
+        k_reuse_visibility<3><<<gridVis, 128, 0, stream>>>(V, n, R, 1);
+        if (timer) timer->mark(GRIS_SLOT_REUSE_VIS_SPATIAL, false, stream);
+        if (guide) k_reuse_spatial_finish<true><<<tiles, blk, 0, stream>>>(V, n, R);
+        else k_reuse_spatial_finish<false><<<tiles, blk, 0, stream>>>(V, n, R);
+        if (timer) timer->mark(3, false, stream);
+    }
+    if (split) return cudaGetLastError();
     if (passes & 2) {
         if (timer) timer->mark(2, true, stream);
         if (guide && sh.pairwise) k_batch_pass<TemporalTaskT<true, true>, 2><<<tiles, blk, 0, stream>>>(V, n);

@@ -61,6 +61,25 @@ struct BatchView {
     GrisSettings set;
 };
 
+/* Device buffers of the reuse passes' three-launch form (prepare, visibility walk, finish) for up
+ * to `capacity` pixels with `slots` neighbour slots each; slots = 0: not allocated, the reuse
+ * passes then run as one per-pixel kernel each. One allocation (`block`, reuse_bytes bytes) carved
+ * by reuse_carve. */
+struct ReuseBuffers {
+    void* block;
+    void* pa;            /* float4 per slot */
+    void* pb;            /* float4 per slot */
+    uint32_t* pn;        /* per slot */
+    unsigned char* ps;   /* per slot */
+    void* q;             /* 32 B per query, a query per slot at most */
+    uint32_t* counts;    /* 4 words */
+    uint32_t slots;
+    uint64_t capacity;
+};
+constexpr uint32_t kReuseMaxSlots = 16;   /* views with more spatial neighbours use the per-pixel kernels */
+size_t reuse_bytes(uint64_t pixels, uint32_t slots);
+void reuse_carve(ReuseBuffers& r, void* block, uint64_t pixels, uint32_t slots);
+
 /* Device buffers of the wavefront path tracer, for up to `capacity` paths (pixels of a batch). */
 struct WaveBuffers {
     void* state;
@@ -80,6 +99,7 @@ struct WaveBuffers {
     uint32_t* gFrame;
     float* gPrimFeat;   /* the guide's inputs / raw outputs at every path's primary vertex */
     float* gPrimOut;
+    ReuseBuffers reuse;  /* the reuse passes' three-launch form (slots = 0: not used) */
 };
 /* bytes per path of the guided-batch buffers */
 size_t guide_wave_bytes_per_path();
@@ -98,6 +118,7 @@ struct BatchShape {
     uint32_t tiles, pixels;
     int maxDepth;
     bool pairwise = false;   /* some view uses the pairwise MIS weights */
+    uint32_t maxNeighbours = 0;   /* largest spatialNeighbors of the views */
 };
 
 /* Writes the view table of a frame into hViews (pinned host memory). */

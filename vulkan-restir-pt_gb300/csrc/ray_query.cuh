@@ -56,7 +56,9 @@ GD bool traceVisibility(const DevScene& sc, V3 from, V3 to, RayCount& rc, int& e
  * [8+2k] nodes and [9+2k] triangles of kernel k, [16+k] closest-hit rays of kernel k
  * (k: 0 G-buffer, 1 path trace, 2 temporal, 3 spatial); the wavefront's traversal stages also
  * count on their own: [26+3s] nodes, [27+3s] triangles, [28+3s] rays (closest for s = 0, the
- * extension stage; shadow for s = 1, the shadow stage); words 24-25 hold the persistent form's
+ * extension stage; shadow for s = 1, the shadow stage), and so do the visibility walks of the
+ * reuse passes' three-launch form: [41+3r] nodes, [42+3r] triangles, [43+3r] rays (stage s = 2 + r,
+ * r = 0 temporal, 1 spatial); words 24-25 hold the persistent form's
  * tile cursors; the ReSTIR DI kernels (k = 4, 5, 6: candidates, temporal, spatial) count their
  * work in [32+3d] nodes, [33+3d] triangles, [34+3d] rays of both kinds (d = k - 4). */
 GD void flush_counts(unsigned long long* counters, const RayCount& rc, int err, int kernel, int countWork,
@@ -82,9 +84,10 @@ GD void flush_counts(unsigned long long* counters, const RayCount& rc, int err, 
             atomicAdd(counters + 9 + 2 * kernel, tris);
             atomicAdd(counters + 16 + kernel, (unsigned long long)c);
             if (stage >= 0) {
-                atomicAdd(counters + 26 + 3 * stage, nodes);
-                atomicAdd(counters + 27 + 3 * stage, tris);
-                atomicAdd(counters + 28 + 3 * stage, (unsigned long long)(stage == 0 ? c : s));
+                const int w = stage < 2 ? 26 + 3 * stage : 41 + 3 * (stage - 2);
+                atomicAdd(counters + w, nodes);
+                atomicAdd(counters + w + 1, tris);
+                atomicAdd(counters + w + 2, (unsigned long long)(stage == 0 ? c : s));
             }
         }
     }

@@ -192,7 +192,7 @@ class KernelProfile(ctypes.Structure):
 
 PROFILE_SLOTS = ["gbuffer", "path_trace", "temporal", "spatial", "wave_begin", "wave_extend", "wave_shade",
                  "wave_shadow", "wave_post", "guide_infer", "guide_train", "di_candidates", "di_temporal",
-                 "di_spatial"]
+                 "di_spatial", "reuse_vis_temporal", "reuse_vis_spatial"]
 
 
 class TuneResult(ctypes.Structure):
@@ -207,7 +207,7 @@ EXPORTS = [
     "grisSizeof", "grisBuildLightTable", "grisCameraSetup", "grisCameraLookAt", "grisHostSceneCreate",
     "grisHostSceneDesc", "grisHostSceneCamera", "grisHostSceneDestroy", "grisSceneCreate", "grisSceneDestroy",
     "grisSceneGetStats", "grisDebugHostSceneCreate", "grisDebugTraceHost", "grisDebugTraceDevice", "grisPassGBuffer", "grisPassRender", "grisPassRenderNoAlloc",
-    "grisNoAllocReadError",
+    "grisNoAllocReadError", "grisMeasureL2Bandwidth",
     "grisFrameCreate", "grisFrameDestroy", "grisFrameRender", "grisFrameGetBuffer", "grisFrameDownload",
     "grisFrameUpload", "grisSetPathForm", "grisBatchCreate", "grisBatchDestroy", "grisBatchRender", "grisBatchGetBuffer",
     "grisBatchDownload", "grisSetGraphs", "grisSetWaveLaunch", "grisBatchAutotune",
@@ -264,6 +264,7 @@ def load(path=None):
         "grisPassRenderNoAlloc": (i32, [vp, ctypes.POINTER(PassBindings), ctypes.POINTER(Camera), ctypes.POINTER(Camera),
                                         ctypes.POINTER(Settings), vp]),
         "grisNoAllocReadError": (i32, [i32, vp, ctypes.POINTER(u64)]),
+        "grisMeasureL2Bandwidth": (i32, [vp, u64, i32, ctypes.POINTER(ctypes.c_double)]),
         "grisFrameCreate": (i32, [vp, u32, u32, ctypes.POINTER(vp)]),
         "grisFrameDestroy": (i32, [vp]),
         "grisFrameRender": (i32, [vp, vp, vp, ctypes.POINTER(Camera), ctypes.POINTER(Camera), ctypes.POINTER(Settings)]),
@@ -482,6 +483,12 @@ class Context:
 
     def stream(self):
         return load().grisGetStream(self.h)
+
+    def l2_bandwidth(self, nbytes=48 << 20, reps=20):
+        """L2 read bandwidth in GB/s (grisMeasureL2Bandwidth)."""
+        g = ctypes.c_double()
+        self.check(load().grisMeasureL2Bandwidth(self.h, int(nbytes), int(reps), ctypes.byref(g)), "grisMeasureL2Bandwidth")
+        return g.value
 
     def counters(self, reset=False):
         out = (ctypes.c_uint64 * 4)()
