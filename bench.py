@@ -148,6 +148,12 @@ def parse():
                     help="c4: the reuse passes' MIS weights (the reference's merge, or the pairwise extension)")
     ap.add_argument("--guide-tc", default="off", choices=["on", "off"],
                     help="c4: the guide's inference on tcgen05 (tensor memory) or mma.sync")
+    ap.add_argument("--guide-train", default="tcgen05", choices=["tcgen05", "mma.sync"],
+                    help="c4: the kernel of the guide's loss gradient")
+    ap.add_argument("--guide-mix", type=float, default=0.5, help="c4: probability of drawing from the guide")
+    ap.add_argument("--guide-lr", type=float, default=1e-3, help="c4: Adam learning rate")
+    ap.add_argument("--guide-records", type=int, default=1 << 18, help="c4: training records per frame")
+    ap.add_argument("--guide-steps", type=int, default=4, help="c4: Adam steps per frame")
     ap.add_argument("--c4-reuse", default="on", choices=["on", "off"],
                     help="c4: temporal + spatial reuse on (ReSTIR PT) or off (the canonical samples alone)")
     ap.add_argument("--width", type=int, default=1920)
@@ -370,24 +376,36 @@ def run_guided(args):
     gb = G.GBufferBindings(W, H, dn.data_ptr(), am.data_ptr(), mv.data_ptr())
     lib = G.load()
     ctx.check(lib.grisPassGBuffer(ctx.h, scene.h, ctypes.byref(gb), ctypes.byref(cam0)), "grisPassGBuffer")
-    ref = torch.zeros(n * 3, dtype=torch.float64, device="cuda")
+    # the converged image as two independent halves (even / odd chunks of 32 samples): their
+    # disagreement measures the converged image's own noise, stated beside every error it judges
+    halves = [torch.zeros(n * 3, dtype=torch.float64, device="cuda") for _ in range(2)]
     t0 = time.perf_counter()
-    for k in range(0, args.ref_spp, 32):
-        scene.converged(cam0, st, W, H, dn.data_ptr(), am.data_ptr(), ref.data_ptr(), None, spp_begin=k,
+    for i, k in enumerate(range(0, args.ref_spp, 32)):
+        scene.converged(cam0, st, W, H, dn.data_ptr(), am.data_ptr(), halves[i & 1].data_ptr(), None, spp_begin=k,
                         spp=min(32, args.ref_spp - k), estimator=G.ESTIMATOR_CANDIDATES)
     ctx.sync()
     ref_s = time.perf_counter() - t0
+    ref = halves[0] + halves[1]
     scale = 1.0 / args.ref_spp
     import numpy as np
     ref_host = ref.cpu().numpy().reshape(-1, 3) * scale
     fg = ref_host.sum(axis=1) > 0
+    nh = [sum(min(32, args.ref_spp - k) for i, k in enumerate(range(0, args.ref_spp, 32)) if (i & 1) == j) for j in (0, 1)]
+    ha, hb = (halves[j].cpu().numpy().reshape(-1, 3) / max(1, nh[j]) for j in (0, 1))
+    # relMSE of one half against the other = (var_a + var_b) / (ref^2 + eps), each half's variance
+    # twice the full image's: a quarter of it estimates the converged image's own relMSE
+    e_halves = (ha - hb) ** 2 / (ref_host ** 2 + 1e-2)
+    ref_noise = {"relmse": float(np.mean(e_halves) / 4.0), "median": float(np.median(e_halves.mean(axis=1)[fg]) / 4.0),
+                 "how": "relMSE / median per-pixel error between the two halves of the converged image's samples, / 4"}
 
     def run(guided):
         batch = G.Batch(ctx, [scene], [(W, H)])
         guide = None
         if guided:
-            guide = G.Guide(ctx, G.GuideConfig.make(seed=args.seed, samplesPerFrame=1 << 18, stepsPerFrame=4,
-                                                    learningRate=1e-3, mix=0.5, tensorCores=args.guide_tc == "on"))
+            guide = G.Guide(ctx, G.GuideConfig.make(seed=args.seed, samplesPerFrame=args.guide_records,
+                                                    stepsPerFrame=args.guide_steps, learningRate=args.guide_lr,
+                                                    mix=args.guide_mix, tensorCores=args.guide_tc == "on",
+                                                    trainKernel=1 if args.guide_train == "mma.sync" else 0))
             batch.set_guide(guide)
         out_ptr, _ = batch.device_ptr(0, G.BUF_OUTPUT)
         times, rel, med, energy = [], [], [], []
@@ -426,7 +444,8 @@ def run_guided(args):
         wg = None
         if guided:
             wg = G.Guide(ctx, G.GuideConfig.make(seed=args.seed + 1, samplesPerFrame=1 << 16, stepsPerFrame=1,
-                                                 tensorCores=args.guide_tc == "on"))
+                                                 tensorCores=args.guide_tc == "on",
+                                                 trainKernel=1 if args.guide_train == "mma.sync" else 0))
             wb.set_guide(wg)
         for f in range(2):
             wb.render([cams[f]], [prevs[f]], [st])
@@ -465,9 +484,12 @@ def run_guided(args):
             "dtype": "f32 paths, bf16 network", "data": "synthetic (seeded scene generator, no dataset)",
             "config": {"workload": "C4: %dx%d glossy variant (%d tris), depth %d, temporal+spatial reuse, static camera, "
                                    "frames accumulated" % (W, H, hs.triangle_count(), args.depth),
-                       "guide": "MLP 80-64x4-48 BF16 (inference: %s; training: mma.sync), 8 vMF lobes, mix 0.5, Adam 1e-3, "
-                                "2^18 records/frame, 4 steps" % ("tcgen05" if args.guide_tc == "on" else "mma.sync")},
-            "reference": {"spp": args.ref_spp, "seconds": ref_s, "estimator": "candidates"},
+                       "guide": "MLP 80-64x4-48 BF16 (inference: %s; training: %s), 8 vMF lobes, mix %g, Adam %g, "
+                                "%d records/frame, %d steps" % ("tcgen05" if args.guide_tc == "on" else "mma.sync",
+                                                                "mma.sync" if args.guide_train == "mma.sync" else "tcgen05",
+                                                                args.guide_mix, args.guide_lr, args.guide_records,
+                                                                args.guide_steps)},
+            "reference": {"spp": args.ref_spp, "seconds": ref_s, "estimator": "candidates", "noise_floor": ref_noise},
             "reuse": reuse, "mis": args.mis, "clocks": clocks,
             "median_error_time_ratio": ratio_med,
             "plain": {"fps": 1000.0 / float(tp.mean()), "total_ms": float(Tp), "relmse_final": float(rp[-1]),

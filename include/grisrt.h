@@ -335,7 +335,10 @@ typedef struct GrisGuideConfig {
     uint32_t train;             /* train while rendering */
     uint32_t tensorCores;       /* inference on the 5th-generation tensor cores (tcgen05, tensor-memory
                                    accumulators) when 1; warp-level mma.sync when 0 */
-    uint32_t reserved[2];
+    uint32_t trainKernel;       /* the loss gradient (training): 0 tcgen05 — 128-record tiles, the weight
+                                   gradients accumulated in tensor memory across the tiles — 1 warp-level
+                                   mma.sync */
+    uint32_t reserved;
 } GrisGuideConfig;
 int grisGuideCreate(GrisContext* ctx, const GrisGuideConfig* cfg, GrisGuide** out);
 int grisGuideDestroy(GrisGuide* guide);

@@ -110,15 +110,25 @@ def test_gpu_forward_matches_oracle(tensor_cores, n):
     ctx.close()
 
 
+TRAIN_KERNELS = [G.GuideConfig.TRAIN_MMA_SYNC, G.GuideConfig.TRAIN_TCGEN05]
+TRAIN_IDS = ["mma_sync", "tcgen05"]
+
+
 @pytest.mark.gpu
-def test_gpu_gradient_matches_oracle():
+@pytest.mark.parametrize("n", [3000, 100003, 77])
+@pytest.mark.parametrize("kernel", TRAIN_KERNELS, ids=TRAIN_IDS)
+def test_gpu_gradient_matches_oracle(kernel, n):
+    """The loss gradient by the warp-level mma.sync kernel and by the tcgen05 kernel (128-record
+    tiles; dW^T = H^T dZ and dH = dZ W as tensor-core products, the weight gradients accumulated in
+    tensor memory across a CTA's tiles, the bias gradients as the ones row of H^T): per layer within
+    2e-2 relative L2 of the oracle's float64 gradient with the same BF16 roundings; n covers one
+    partial tile, partial tiles at the end and several tiles per CTA."""
     import torch
     ctx = G.Context(0)
-    g = G.Guide(ctx, G.GuideConfig.make(samplesPerFrame=1024, stepsPerFrame=1))
+    g = G.Guide(ctx, G.GuideConfig.make(samplesPerFrame=1024, stepsPerFrame=1, trainKernel=kernel))
     W, b = _params(11)
     p = _join(W, b)
     g.set_params(p)
-    n = 3000
     feat, d, w = _inputs(n, 13)
     tf, td, tw = (torch.from_numpy(a).cuda() for a in (feat, d, w))
     grad = torch.zeros(g.n_params, dtype=torch.float32, device="cuda")
@@ -136,16 +146,18 @@ def test_gpu_gradient_matches_oracle():
             rel = np.linalg.norm(a - bb) / max(np.linalg.norm(bb), 1e-30)
             assert rel < 2e-2, (l, part, rel)
             off += size
+    assert ctx.counters()[3] == 0   # no tensor-core wait gave up
     g.close()
     ctx.close()
 
 
 @pytest.mark.gpu
-def test_gpu_adam_step_matches_oracle():
+@pytest.mark.parametrize("kernel", TRAIN_KERNELS, ids=TRAIN_IDS)
+def test_gpu_adam_step_matches_oracle(kernel):
     import torch
     ctx = G.Context(0)
     lr = 1e-3
-    g = G.Guide(ctx, G.GuideConfig.make(samplesPerFrame=1024, stepsPerFrame=1, learningRate=lr))
+    g = G.Guide(ctx, G.GuideConfig.make(samplesPerFrame=1024, stepsPerFrame=1, learningRate=lr, trainKernel=kernel))
     W, b = _params(17)
     p = _join(W, b)
     g.set_params(p)
@@ -168,12 +180,14 @@ def test_gpu_adam_step_matches_oracle():
 
 
 @pytest.mark.gpu
-def test_gpu_training_fits_a_target_distribution():
+@pytest.mark.parametrize("kernel", TRAIN_KERNELS, ids=TRAIN_IDS)
+def test_gpu_training_fits_a_target_distribution(kernel):
     """Directions drawn from a position-dependent target (a vMF about a direction that turns with
     x), weight 1: Adam on the loss raises the learned density at the target directions."""
     import torch
     ctx = G.Context(0)
-    g = G.Guide(ctx, G.GuideConfig.make(seed=3, samplesPerFrame=1024, stepsPerFrame=1, learningRate=5e-3))
+    g = G.Guide(ctx, G.GuideConfig.make(seed=3, samplesPerFrame=1024, stepsPerFrame=1, learningRate=5e-3,
+                                        trainKernel=kernel))
     rng = np.random.default_rng(23)
     n = 1 << 14
 

@@ -398,6 +398,7 @@ cudaError_t launch_grad(const GradArgs& a, cudaStream_t stream) {
     if (attr < 0) return (cudaError_t)(-attr);
     if (!a.invWeightSum) return cudaErrorInvalidValue;
     k_guide_weight_sum<<<1, 256, 0, stream>>>(a.weight, a.count, a.base, a.n, a.invWeightSum);
+    if (a.tensorCores) return launch_grad_tc(a, stream);
     k_guide_grad<<<sm, kGradWarps * 32, kGradSmem, stream>>>(a);
     return cudaGetLastError();
 }

@@ -68,6 +68,8 @@ cudaError_t guide_train_frame(GrisGuide* g, cudaStream_t st) {
         a.n = per;
         a.invWeightSum = g->invSum;
         a.grad = g->grad;
+        a.tensorCores = g->cfg.trainKernel == 0u;
+        a.err = ctx_counters(g->ctx) + GRIS_COUNTER_ERROR;
         cudaError_t e = guide::launch_grad(a, st);
         if (e != cudaSuccess) return e;
         e = guide::launch_adam(g->params, g->grad, g->m, g->v, g->step, g->cfg.learningRate, st);
@@ -229,6 +231,7 @@ int grisGuideGradient(GrisContext* ctx, GrisGuide* g, const float* feat, const f
     guide::GradArgs a;
     a.wPacked = g->wPacked; a.bias = g->bias; a.feat = feat; a.dir = dir; a.weight = weight;
     a.count = nullptr; a.base = 0; a.n = n; a.invWeightSum = g->invSum; a.grad = gradOut;
+    a.tensorCores = g->cfg.trainKernel == 0u; a.err = ctx_counters(ctx) + GRIS_COUNTER_ERROR;
     GUIDE_CK(ctx, guide::launch_grad(a, st));
     return GRIS_OK;
 }
@@ -241,6 +244,7 @@ int grisGuideTrainStep(GrisContext* ctx, GrisGuide* g, const float* feat, const 
         guide::GradArgs a;
         a.wPacked = g->wPacked; a.bias = g->bias; a.feat = feat; a.dir = dir; a.weight = weight;
         a.count = nullptr; a.base = 0; a.n = n; a.invWeightSum = g->invSum; a.grad = g->grad;
+        a.tensorCores = g->cfg.trainKernel == 0u; a.err = ctx_counters(ctx) + GRIS_COUNTER_ERROR;
         GUIDE_CK(ctx, guide::launch_grad(a, st));
     }
     GUIDE_CK(ctx, guide::launch_adam(g->params, g->grad, g->m, g->v, g->step, g->cfg.learningRate, st));

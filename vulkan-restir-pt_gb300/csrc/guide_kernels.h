@@ -33,6 +33,9 @@ struct GradArgs {
     uint32_t n;
     float* invWeightSum;       /* device scalar: written here from the weights, then read */
     float* grad;
+    int tensorCores = 0;                /* 1: the tcgen05 kernel (guide_tc.cu), 0: mma.sync */
+    unsigned long long* err = nullptr;  /* error word (bit 1: a tensor-core wait gave up) */
+    int withholdCommit = 0;             /* test of the bounded waits: a forward layer's completion is never signalled */
 };
 
 /* what the path tracer needs of a guide: the network and the training-record batch */
@@ -52,6 +55,8 @@ cudaError_t launch_forward(const FwdArgs& a, cudaStream_t stream);
 cudaError_t launch_forward_tc(const FwdArgs& a, cudaStream_t stream);
 size_t tc_smem_bytes();
 cudaError_t launch_grad(const GradArgs& a, cudaStream_t stream);
+cudaError_t launch_grad_tc(const GradArgs& a, cudaStream_t stream);
+size_t tc_grad_smem_bytes();
 cudaError_t launch_pack(const float* params, __nv_bfloat16* wPacked, float* bias, cudaStream_t stream);
 cudaError_t launch_adam(float* params, float* grad, float* m, float* v, uint32_t* step, float lr, cudaStream_t stream);
 size_t grad_smem_bytes();

@@ -270,6 +270,328 @@ __global__ void __launch_bounds__(kTcRows * kTcGroups, 2) k_guide_forward_tc(Fwd
 #endif
 }
 
+/* ================================================================ loss gradient on tcgen05 */
+/* One CTA of 128 threads per SM walks 128-record tiles (one thread per record = one accumulator
+ * row). Per tile:
+ *   forward   five layers as in k_guide_forward_tc, every layer's input tile kept in shared
+ *             memory (the backward pass needs them);
+ *   loss      each thread turns its record's 40 outputs into d loss / d outputs (lobes_loss_grad);
+ *   backward  per layer l = 4..0 one elected thread issues
+ *               dW_l^T += H_l^T dZ_l   (M = 128 input rows, N = out_l, K = the tile's 128 records)
+ *             into the layer's own tensor-memory accumulator, which stays resident across all
+ *             the CTA's tiles (this replaces the per-warp shared-memory atomic fold), and for l > 0
+ *               dH_l = dZ_l W_l        (M = 128 records, N = in_l = 64, K = out_l),
+ *             whose rows the threads read back to form dZ_{l-1} = dH_l * [H_l > 0].
+ * H_l^T and dZ_l^T (K = records) are written transposed into two scratch tiles; row in_l of H_l^T
+ * holds ones, so that row of the accumulator is the bias gradient sum_r dZ_l[r]. At the end each
+ * thread reads its accumulator rows and adds them to the gradient (one atomic per parameter and
+ * CTA). Operands: K-major, no swizzle, the core-matrix layout of k_guide_forward_tc; all MMAs are
+ * cta_group::1 kind::f16 with M = 128. Every mbarrier wait is bounded as in the inference kernel.
+ *
+ * Shared memory (from a 1024-B aligned base; every tile 1024-B aligned):
+ *   [0, 40960)        W_l, forward B operands (N = out_l rows, K = in_l)          tc_w_off(l)
+ *   [40960, 71680)    W_l^T, l = 1..4, dH B operands (N = in_l rows, K = out_l)   kGtWT + gt_wt_off(l)
+ *   [71680, 92160)    H_0: layer-0 inputs, 128 records x 80
+ *   [92160, 157696)   H_1..H_4: inputs of layers 1..4, 128 records x 64 each
+ *   [157696, 174080)  dZ_l, 128 records x out_l (A of dH)
+ *   [174080, 206848)  H_l^T: 128 rows (inputs; row in_l = ones) x 128 records (A of dW^T)
+ *   [206848, 223232)  dZ_l^T: out_l rows x 128 records (B of dW^T)
+ *   then biases (304 floats), the mbarrier and the tensor-memory address slot.
+ * Tensor memory: 512 columns; [0, 64) the forward / dH accumulator, 64 + 64 l the dW_l^T
+ * accumulator (N = out_l columns). */
+__host__ __device__ constexpr uint32_t gt_wt_off(int l) { return l <= 1 ? 0u : gt_wt_off(l - 1) + (uint32_t)(layer_in(l - 1) * layer_out(l - 1)) * 2u; }
+constexpr uint32_t kGtWT = tc_w_off(5);                                 /* 40960 */
+constexpr uint32_t kGtH0 = kGtWT + gt_wt_off(5);                        /* 71680 */
+constexpr uint32_t kGtH = kGtH0 + (uint32_t)(kTcRows * kIn) * 2u;       /* 92160 */
+constexpr uint32_t kGtHTile = (uint32_t)(kTcRows * kHid) * 2u;          /* 16384 */
+constexpr uint32_t kGtDZ = kGtH + 4u * kGtHTile;                        /* 157696 */
+constexpr uint32_t kGtHT = kGtDZ + kGtHTile;                            /* 174080 */
+constexpr uint32_t kGtDZT = kGtHT + 128u * 128u * 2u;                   /* 206848 */
+constexpr uint32_t kGtBias = kGtDZT + 64u * 128u * 2u;                  /* 223232 */
+constexpr uint32_t kGtBar = kGtBias + (uint32_t)kBiases * 4u;
+constexpr uint32_t kGtSlot = kGtBar + 8u;
+constexpr uint32_t kGtSmem = kGtSlot + 8u + 1024u;
+constexpr uint32_t kGtTmemCols = 512u;
+static_assert(kGtWT == 40960u && kGtH0 == 71680u && kGtDZT == 206848u, "gradient kernel layout");
+static_assert(kGtH0 % 1024u == 0u && kGtH % 1024u == 0u && kGtDZ % 1024u == 0u && kGtHT % 1024u == 0u &&
+              kGtDZT % 1024u == 0u && kGtBar % 8u == 0u, "operand tiles 1024-B aligned, mbarrier 8-B aligned");
+static_assert(kGtSmem <= 232448u, "fits the 227 KB a CTA may opt in to");
+
+size_t tc_grad_smem_bytes() { return kGtSmem; }
+
+#ifdef GRIS_TC_DEVICE
+/* one BF16 element (row, k) of a K-major no-swizzle tile of K columns */
+__device__ __forceinline__ void st_bf16(unsigned char* tile, uint32_t row, uint32_t k, uint32_t K, float v) {
+    *reinterpret_cast<__nv_bfloat16*>(tile + core_off(row, k, K) + (k & 7u) * 2u) = __float2bfloat16_rn(v);
+}
+__device__ __forceinline__ float ld_bf16(const unsigned char* tile, uint32_t row, uint32_t k, uint32_t K) {
+    return __bfloat162float(*reinterpret_cast<const __nv_bfloat16*>(tile + core_off(row, k, K) + (k & 7u) * 2u));
+}
+/* 8 BF16 values (columns c..c+7, c a multiple of 8) of one row as one 16-B store */
+__device__ __forceinline__ void st_row8(unsigned char* tile, uint32_t row, uint32_t c, uint32_t K, const float* v) {
+    *reinterpret_cast<uint4*>(tile + core_off(row, c, K)) =
+        make_uint4(pack_bf16(v[0], v[1]), pack_bf16(v[2], v[3]), pack_bf16(v[4], v[5]), pack_bf16(v[6], v[7]));
+}
+#endif
+
+__global__ void __launch_bounds__(kTcRows, 1) k_guide_grad_tc(GradArgs a) {
+#ifdef GRIS_TC_DEVICE
+    extern __shared__ unsigned char smemRaw[];
+    unsigned char* smem = reinterpret_cast<unsigned char*>((reinterpret_cast<uintptr_t>(smemRaw) + 1023u) & ~(uintptr_t)1023u);
+    const uint32_t tid = threadIdx.x, warp = tid >> 5;
+    float* sBias = reinterpret_cast<float*>(smem + kGtBias);
+    const uint32_t bar = smem_u32(smem + kGtBar);
+    uint32_t* slot = reinterpret_cast<uint32_t*>(smem + kGtSlot);
+    unsigned char* sH0 = smem + kGtH0;
+    unsigned char* sDZ = smem + kGtDZ;
+    unsigned char* sHT = smem + kGtHT;
+    unsigned char* sDZT = smem + kGtDZT;
+    __shared__ uint32_t sFail;
+
+    /* forward weights (as the inference kernel), transposed weights, biases; H^T's rows past the
+     * inputs start at zero */
+    for (int l = 0; l < 5; l++) {
+        const int K = layer_in(l), N = layer_out(l), chunks = N * (K / 8);
+        for (int i = (int)tid; i < chunks; i += kTcRows) {
+            int nn = i / (K / 8), kg = i % (K / 8);
+            uint4 v = *reinterpret_cast<const uint4*>(a.wPacked + packed_w(l) + nn * stride_w(l) + 8 * kg);
+            *reinterpret_cast<uint4*>(smem + tc_w_off(l) + core_off((uint32_t)nn, (uint32_t)(8 * kg), (uint32_t)K)) = v;
+        }
+    }
+    for (int l = 1; l < 5; l++) {
+        const int I = layer_in(l), O = layer_out(l);
+        unsigned char* wt = smem + kGtWT + gt_wt_off(l);
+        for (int i = (int)tid; i < I * O; i += kTcRows) {
+            const int in = i / O, o = i % O;   /* element (row in, column o) = W_l[o][in] */
+            *reinterpret_cast<__nv_bfloat16*>(wt + core_off((uint32_t)in, (uint32_t)o, (uint32_t)O) + (uint32_t)(o & 7) * 2u) =
+                a.wPacked[packed_w(l) + o * stride_w(l) + in];
+        }
+    }
+    for (int i = (int)tid; i < kBiases; i += kTcRows) sBias[i] = a.bias[i];
+    for (uint32_t i = tid; i < 128u * 128u * 2u / 16u; i += (uint32_t)kTcRows)
+        reinterpret_cast<uint4*>(sHT)[i] = make_uint4(0u, 0u, 0u, 0u);
+    if (tid == 0) {
+        sFail = 0u;
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" :: "r"(bar) : "memory");
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" :: "r"(smem_u32(slot)), "r"(kGtTmemCols)
+                     : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+    }
+    fence_async_smem();
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    const uint32_t tmem = *slot;
+    const uint32_t myLanes = tmem + ((warp * 32u) << 16);
+    uint32_t phase = 0u;
+    bool ok = true, any = false;
+    const uint32_t n = a.count ? min(max(*a.count, a.base) - a.base, a.n) : a.n;
+    const float invSum = *a.invWeightSum;
+
+    /* the elected thread issues, commits; every thread waits (bounded) for the phase */
+    auto wait_all = [&]() -> bool {
+        if (!bar_wait(bar, phase)) {
+            sFail = 1u;
+            if (a.err) atomicOr(a.err, 2ull);
+        }
+        phase ^= 1u;
+        tc_fence_after();
+        __syncthreads();
+        return sFail == 0u;
+    };
+
+    for (uint32_t tile = blockIdx.x; ok && tile * (uint32_t)kTcRows < n; tile += gridDim.x) {
+        const uint32_t r = tile * (uint32_t)kTcRows + tid;
+        const bool valid = r < n;
+        /* layer-0 input: the encoding of this thread's record (zeros past the end) */
+        float f[9];
+#pragma unroll
+        for (int i = 0; i < 9; i++) f[i] = valid ? a.feat[(size_t)r * 9 + i] : 0.0f;
+#pragma unroll
+        for (int c = 0; c < 3; c++) {
+            float sv[12], cv[12];
+#pragma unroll
+            for (int j = 0; j < 12; j++) sincospif(f[c] * (float)(1 << j), &sv[j], &cv[j]);
+            unsigned char* base = sH0 + core_off(tid, (uint32_t)(24 * c), kIn);
+            *reinterpret_cast<uint4*>(base) =
+                make_uint4(pack_bf16(sv[0], sv[1]), pack_bf16(sv[2], sv[3]), pack_bf16(sv[4], sv[5]), pack_bf16(sv[6], sv[7]));
+            *reinterpret_cast<uint4*>(base + 128) =
+                make_uint4(pack_bf16(sv[8], sv[9]), pack_bf16(sv[10], sv[11]), pack_bf16(cv[0], cv[1]), pack_bf16(cv[2], cv[3]));
+            *reinterpret_cast<uint4*>(base + 256) =
+                make_uint4(pack_bf16(cv[4], cv[5]), pack_bf16(cv[6], cv[7]), pack_bf16(cv[8], cv[9]), pack_bf16(cv[10], cv[11]));
+        }
+        *reinterpret_cast<uint4*>(sH0 + core_off(tid, 72u, kIn)) =
+            make_uint4(pack_bf16(f[3], f[4]), pack_bf16(f[5], f[6]), pack_bf16(f[7], f[8]), pack_bf16(0.0f, 0.0f));
+        fence_async_smem();
+        tc_fence_before();
+        __syncthreads();
+
+        /* ---- forward; raw: this record's 48 outputs */
+        float raw[kOut];
+        for (int l = 0; l < 5 && ok; l++) {
+            const uint32_t K = (uint32_t)layer_in(l), N = (uint32_t)layer_out(l);
+            if (tid == 0) {
+                tc_fence_after();
+                const uint32_t aBase = smem_u32(l == 0 ? sH0 : smem + kGtH + (uint32_t)(l - 1) * kGtHTile);
+                const uint32_t bBase = smem_u32(smem + tc_w_off(l));
+                for (uint32_t s = 0; s < K / 16u; s++)
+                    tc_mma(tmem, tc_sdesc(aBase + s * 256u, 128u, (K / 8u) * 128u),
+                           tc_sdesc(bBase + s * 256u, 128u, (K / 8u) * 128u), tc_idesc(N), s > 0u ? 1u : 0u);
+                if (!a.withholdCommit) tc_commit(bar);
+            }
+            ok = wait_all();
+            if (!ok) break;
+            const float* bias = sBias + bias_off(l);
+            if (l < 4) {
+                unsigned char* next = smem + kGtH + (uint32_t)l * kGtHTile;
+#pragma unroll
+                for (uint32_t c = 0; c < (uint32_t)kHid; c += 16u) {
+                    uint32_t q[16];
+                    tc_ld16(myLanes + c, q);
+                    tc_wait_ld();
+                    store_hidden16(next, tid, c, q, bias);
+                }
+            } else {
+#pragma unroll
+                for (uint32_t c = 0; c < (uint32_t)kOut; c += 16u) {
+                    uint32_t q[16];
+                    tc_ld16(myLanes + c, q);
+                    tc_wait_ld();
+#pragma unroll
+                    for (uint32_t i = 0; i < 16u; i++) raw[c + i] = __uint_as_float(q[i]) + bias[c + i];
+                }
+            }
+            fence_async_smem();
+            tc_fence_before();
+            __syncthreads();
+        }
+        if (!ok) break;
+
+        /* ---- d loss / d outputs of this record: dZ_4 (40 used of 48), with H_4^T */
+        {
+            float g[kRaw];
+            if (valid) {
+                const float d[3] = {a.dir[(size_t)r * 3], a.dir[(size_t)r * 3 + 1], a.dir[(size_t)r * 3 + 2]};
+                lobes_loss_grad(raw, d, a.weight[r] * invSum, g);
+            } else {
+#pragma unroll
+                for (int i = 0; i < kRaw; i++) g[i] = 0.0f;
+            }
+            float z8[8] = {0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f};
+#pragma unroll
+            for (uint32_t c = 0; c < (uint32_t)kRaw; c += 8u) st_row8(sDZ, tid, c, (uint32_t)kOut, g + c);
+            st_row8(sDZ, tid, (uint32_t)kRaw, (uint32_t)kOut, z8);
+            for (uint32_t o = 0; o < (uint32_t)kOut; o++) st_bf16(sDZT, o, tid, 128u, o < (uint32_t)kRaw ? g[o] : 0.0f);
+            const unsigned char* h4 = smem + kGtH + 3u * kGtHTile;
+            for (uint32_t m = 0; m < (uint32_t)kHid; m++) st_bf16(sHT, m, tid, 128u, ld_bf16(h4, tid, m, (uint32_t)kHid));
+            st_bf16(sHT, (uint32_t)kHid, tid, 128u, 1.0f);
+        }
+        fence_async_smem();
+        tc_fence_before();
+        __syncthreads();
+
+        /* ---- backward */
+        for (int l = 4; l >= 0 && ok; l--) {
+            const uint32_t I = (uint32_t)layer_in(l), O = (uint32_t)layer_out(l);
+            if (tid == 0) {
+                tc_fence_after();
+                const uint32_t aT = smem_u32(sHT), bT = smem_u32(sDZT);
+                const uint32_t acc = tmem + 64u + 64u * (uint32_t)l;
+                for (uint32_t s = 0; s < 8u; s++)   /* K = 128 records */
+                    tc_mma(acc, tc_sdesc(aT + s * 256u, 128u, 16u * 128u), tc_sdesc(bT + s * 256u, 128u, 16u * 128u),
+                           tc_idesc(O), (any || s > 0u) ? 1u : 0u);
+                if (l > 0) {
+                    const uint32_t aD = smem_u32(sDZ), bW = smem_u32(smem + kGtWT + gt_wt_off(l));
+                    for (uint32_t s = 0; s < O / 16u; s++)
+                        tc_mma(tmem, tc_sdesc(aD + s * 256u, 128u, (O / 8u) * 128u),
+                               tc_sdesc(bW + s * 256u, 128u, (O / 8u) * 128u), tc_idesc(I), s > 0u ? 1u : 0u);
+                }
+                tc_commit(bar);
+            }
+            ok = wait_all();
+            if (!ok || l == 0) break;
+            /* dZ_{l-1} = dH_l * [H_l > 0]; H_l = the input of layer l; then H_{l-1}^T */
+            const unsigned char* hl = smem + kGtH + (uint32_t)(l - 1) * kGtHTile;
+#pragma unroll
+            for (uint32_t c = 0; c < (uint32_t)kHid; c += 16u) {
+                uint32_t q[16];
+                tc_ld16(myLanes + c, q);
+                tc_wait_ld();
+                float dz[16];
+#pragma unroll
+                for (uint32_t i = 0; i < 16u; i++) dz[i] = ld_bf16(hl, tid, c + i, (uint32_t)kHid) > 0.0f ? __uint_as_float(q[i]) : 0.0f;
+                st_row8(sDZ, tid, c, (uint32_t)kHid, dz);
+                st_row8(sDZ, tid, c + 8u, (uint32_t)kHid, dz + 8);
+#pragma unroll
+                for (uint32_t i = 0; i < 16u; i++) st_bf16(sDZT, c + i, tid, 128u, dz[i]);
+            }
+            const uint32_t In = (uint32_t)layer_in(l - 1);
+            const unsigned char* hin = l - 1 == 0 ? sH0 : smem + kGtH + (uint32_t)(l - 2) * kGtHTile;
+            for (uint32_t m = 0; m < In; m++) st_bf16(sHT, m, tid, 128u, ld_bf16(hin, tid, m, In));
+            st_bf16(sHT, In, tid, 128u, 1.0f);
+            fence_async_smem();
+            tc_fence_before();
+            __syncthreads();
+        }
+        any = true;
+    }
+
+    /* ---- the CTA's weight and bias gradients: row m of dW_l^T is input m (m = in_l: the bias) */
+    if (ok && any) {
+        const uint32_t m = tid;
+        for (int l = 0; l < 5; l++) {
+            const uint32_t I = (uint32_t)layer_in(l), O = (uint32_t)layer_out(l);
+            for (uint32_t c = 0; c < O; c += 16u) {
+                uint32_t q[16];
+                tc_ld16(myLanes + 64u + 64u * (uint32_t)l + c, q);
+                tc_wait_ld();
+                if (m < I) {
+                    float* gw = a.grad + param_w(l);
+#pragma unroll
+                    for (uint32_t i = 0; i < 16u; i++) {
+                        const float v = __uint_as_float(q[i]);
+                        if (v != 0.0f) atomicAdd(gw + (c + i) * I + m, v);
+                    }
+                } else if (m == I) {
+                    float* gb = a.grad + param_b(l);
+#pragma unroll
+                    for (uint32_t i = 0; i < 16u; i++) {
+                        const float v = __uint_as_float(q[i]);
+                        if (v != 0.0f) atomicAdd(gb + c + i, v);
+                    }
+                }
+            }
+        }
+    }
+    /* after a timeout: a commit drains the products in flight (see k_guide_forward_tc) */
+    if (sFail && tid == 0) {
+        tc_commit(bar);
+        if (!bar_wait(bar, phase ^ 1u) && a.err) atomicOr(a.err, 4ull);
+    }
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    if (warp == 0)
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" :: "r"(tmem), "r"(kGtTmemCols) : "memory");
+#endif
+}
+
+cudaError_t launch_grad_tc(const GradArgs& a, cudaStream_t stream) {
+    const int sm = current_sm_count();
+    const int attr = once_per_device(kDeviceKeyGuideGradTcAttr, []() {
+        cudaError_t e = cudaFuncSetAttribute(k_guide_grad_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kGtSmem);
+        return e == cudaSuccess ? 1 : -(int)e;
+    });
+    if (attr < 0) return (cudaError_t)(-attr);
+    const uint32_t tiles = (a.n + (uint32_t)kTcRows - 1u) / (uint32_t)kTcRows;
+    const int grid = (int)(tiles < (uint32_t)sm ? (tiles > 0u ? tiles : 1u) : (uint32_t)sm);
+    k_guide_grad_tc<<<grid, kTcRows, kGtSmem, stream>>>(a);
+    return cudaGetLastError();
+}
+
 cudaError_t launch_forward_tc(const FwdArgs& a, cudaStream_t stream) {
     const int sm = current_sm_count();
     /* the shared-memory attribute is a per-device property of the kernel: set once per device */

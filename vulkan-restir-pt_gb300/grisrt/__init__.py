@@ -178,11 +178,15 @@ ESTIMATOR_CANDIDATES, ESTIMATOR_INDIRECT = 0, 1
 class GuideConfig(ctypes.Structure):
     _fields_ = [("seed", ctypes.c_uint64), ("learningRate", ctypes.c_float), ("mix", ctypes.c_float),
                 ("samplesPerFrame", ctypes.c_uint32), ("stepsPerFrame", ctypes.c_uint32), ("train", ctypes.c_uint32),
-                ("tensorCores", ctypes.c_uint32), ("reserved", ctypes.c_uint32 * 2)]
+                ("tensorCores", ctypes.c_uint32), ("trainKernel", ctypes.c_uint32), ("reserved", ctypes.c_uint32)]
+
+    TRAIN_TCGEN05, TRAIN_MMA_SYNC = 0, 1
 
     @staticmethod
-    def make(seed=1, learningRate=1e-3, mix=0.5, samplesPerFrame=1 << 18, stepsPerFrame=4, train=True, tensorCores=False):
-        return GuideConfig(seed, learningRate, mix, samplesPerFrame, stepsPerFrame, int(train), int(tensorCores))
+    def make(seed=1, learningRate=1e-3, mix=0.5, samplesPerFrame=1 << 18, stepsPerFrame=4, train=True, tensorCores=False,
+             trainKernel=0):
+        return GuideConfig(seed, learningRate, mix, samplesPerFrame, stepsPerFrame, int(train), int(tensorCores),
+                           int(trainKernel))
 
 
 class KernelProfile(ctypes.Structure):
