@@ -208,6 +208,7 @@ struct GrisTraversal {
     uint32_t bestInst, bestTri;
     bool found;
     uint32_t grpBase, grpHits, grpImask, nodeIdx;
+    uint32_t triBase, triHits;   /* the leaf triangles of the last node visited still to be tested */
     bool haveNode;
     uint32_t visits, tests;
 
@@ -223,6 +224,7 @@ struct GrisTraversal {
         bestU = 0.0f; bestV = 0.0f;
         found = false;
         grpBase = 0; grpHits = 0; grpImask = 0;
+        triBase = 0; triHits = 0;
         nodeIdx = 0;
         /* A ray with a NaN coordinate hits nothing (every triangle test compares a NaN), but the
          * box test's maxNum/minNum would pass every node on it: skip the walk, same result. */
@@ -230,8 +232,46 @@ struct GrisTraversal {
         visits = 0; tests = 0;
     }
 
-    /* false: the walk is over (found / best* hold the result) */
-    template <class Stack>
+    /* One leaf triangle of the last node visited (the lowest bit of triHits): the closest-hit
+     * update, or for ANY the end of the walk on an accepted hit (true: the walk is over). */
+    GRIS_HDM bool test_next_triangle(const float* __restrict__ tris, bool skipInst0) {
+        const int b = gris_ffs(triHits);
+        triHits &= triHits - 1u;
+        const float* T = tris + (uint64_t)(triBase + (uint32_t)b) * GRIS_TRI_FLOATS;
+#ifdef __CUDA_ARCH__
+        float4 t0 = __ldg(reinterpret_cast<const float4*>(T) + 0);
+        float4 t1 = __ldg(reinterpret_cast<const float4*>(T) + 1);
+        float4 t2 = __ldg(reinterpret_cast<const float4*>(T) + 2);
+        float TT[12] = {t0.x, t0.y, t0.z, t0.w, t1.x, t1.y, t1.z, t1.w, t2.x, t2.y, t2.z, t2.w};
+#else
+        float TT[12];
+        for (int i = 0; i < 12; i++) TT[i] = T[i];
+#endif
+        uint32_t inst = gris_f2u(TT[3]), tri = gris_f2u(TT[7]);
+        if (skipInst0 && inst == 0u) return false;
+        tests++;
+        float t, u, v;
+        if (!gris_tri_test(TT, ox, oy, oz, dx, dy, dz, tmin, bestT, &t, &u, &v)) return false;
+        if (ANY) {
+            bestT = t; bestU = u; bestV = v; bestInst = inst; bestTri = tri; found = true;
+            return true;
+        }
+        /* t <= bestT here (the test used bestT as tmax) */
+        bool keyLess = inst < bestInst || (inst == bestInst && tri < bestTri);
+        bool better = t < bestT || (t == bestT && keyLess);
+        if (better) {
+            bestT = t; bestU = u; bestV = v; bestInst = inst; bestTri = tri; found = true;
+        }
+        return false;
+    }
+
+    /* false: the walk is over (found / best* hold the result). A step visits the node chosen by
+     * the previous step (its child boxes; the hit leaves' triangles become pending), tests up to
+     * kTris pending triangles (0: all of them), and once none is pending chooses the next node.
+     * The order of the box and triangle tests, and so every result and count, is the same for
+     * every kTris; a small kTris only spreads a node's triangles over several steps, so that the
+     * lanes of a warp whose nodes hit few triangles do not wait for the lane whose node hit many. */
+    template <int kTris = 0, class Stack>
     GRIS_HDM bool step(const uint32_t* __restrict__ nodes, const float* __restrict__ tris, bool skipInst0, int* err,
                        Stack& stack) {
         if (haveNode) {
@@ -256,7 +296,7 @@ struct GrisTraversal {
             uint32_t imask = e >> 24;
             float ax = sx * idx, ay = sy * idy, az = sz * idz;
             float bx = (px - ox) * idx, by = (py - oy) * idy, bz = (pz - oz) * idz;
-            uint32_t innerHits = 0, triHits = 0;
+            uint32_t innerHits = 0, leafHits = 0;
 #pragma unroll
             for (int s = 0; s < 8; s++) {
                 uint32_t meta = gris_byte(W[6 + (s >> 2)], s & 3);
@@ -274,44 +314,24 @@ struct GrisTraversal {
                 if (imask & (1u << s)) innerHits |= 1u << (s ^ oct);
                 else {
                     uint32_t cnt = (meta >> 5) & 3u, off = meta & 31u;
-                    triHits |= ((1u << cnt) - 1u) << off;
+                    leafHits |= ((1u << cnt) - 1u) << off;
                 }
             }
-            uint32_t triBase = W[5];
-            while (triHits) {
-                int b = gris_ffs(triHits);
-                triHits &= triHits - 1u;
-                const float* T = tris + (uint64_t)(triBase + (uint32_t)b) * GRIS_TRI_FLOATS;
-#ifdef __CUDA_ARCH__
-                float4 t0 = __ldg(reinterpret_cast<const float4*>(T) + 0);
-                float4 t1 = __ldg(reinterpret_cast<const float4*>(T) + 1);
-                float4 t2 = __ldg(reinterpret_cast<const float4*>(T) + 2);
-                float TT[12] = {t0.x, t0.y, t0.z, t0.w, t1.x, t1.y, t1.z, t1.w, t2.x, t2.y, t2.z, t2.w};
-#else
-                float TT[12];
-                for (int i = 0; i < 12; i++) TT[i] = T[i];
-#endif
-                uint32_t inst = gris_f2u(TT[3]), tri = gris_f2u(TT[7]);
-                if (skipInst0 && inst == 0u) continue;
-                tests++;
-                float t, u, v;
-                if (!gris_tri_test(TT, ox, oy, oz, dx, dy, dz, tmin, bestT, &t, &u, &v)) continue;
-                if (ANY) {
-                    bestT = t; bestU = u; bestV = v; bestInst = inst; bestTri = tri; found = true;
-                    return false;
-                }
-                /* t <= bestT here (the test used bestT as tmax) */
-                bool keyLess = inst < bestInst || (inst == bestInst && tri < bestTri);
-                bool better = t < bestT || (t == bestT && keyLess);
-                if (better) {
-                    bestT = t; bestU = u; bestV = v; bestInst = inst; bestTri = tri; found = true;
-                }
-            }
+            triBase = W[5];
+            triHits = leafHits;
             if (innerHits) {
                 if (grpHits && !stack.push(grpBase, grpHits | (grpImask << 8))) { *err = 1; return false; }
                 grpBase = W[4]; grpHits = innerHits; grpImask = imask;
             }
             haveNode = false;
+        }
+        if (kTris == 0) {
+            while (triHits)
+                if (test_next_triangle(tris, skipInst0)) return false;
+        } else {
+            for (int k = 0; k < kTris && triHits; k++)
+                if (test_next_triangle(tris, skipInst0)) return false;
+            if (triHits) return true;
         }
         if (grpHits == 0) {
             uint32_t b, m;

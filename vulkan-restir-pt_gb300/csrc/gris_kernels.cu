@@ -1837,6 +1837,11 @@ constexpr int kWalkSharedEntries = GRIS_WALK_SHARED_ENTRIES;
 #define GRIS_WALK_MIN_BLOCKS 0
 #endif
 constexpr int kWalkMinBlocks = GRIS_WALK_MIN_BLOCKS;
+/* leaf triangles a resident walk tests per step (0: all of a node's at once) */
+#ifndef GRIS_WALK_TRIS_PER_STEP
+#define GRIS_WALK_TRIS_PER_STEP 1
+#endif
+constexpr int kWalkTrisPerStep = GRIS_WALK_TRIS_PER_STEP;
 constexpr uint32_t kCoopMaxRays = 8192;
 constexpr uint32_t kCoopStack = 1024;      /* node indices per warp (pushes are at most 32 per round) */
 constexpr uint32_t kCoopTris = 96;         /* triangles per round: 4 nodes x 8 slots x 3 */
@@ -2058,7 +2063,7 @@ __global__ void __launch_bounds__(128, kWalkMinBlocks) k_wave_trace_refill(WaveC
             if (!more) break;
             continue;
         }
-        if (active && !tr.step(nodes, tris, false, &err, stack)) {
+        if (active && !tr.template step<kWalkTrisPerStep>(nodes, tris, false, &err, stack)) {
             GrisRayHit h;
             tr.result(&h, &rc.work);
             if (ANY) {
@@ -2448,7 +2453,7 @@ __global__ void __launch_bounds__(128, kWalkMinBlocks) k_reuse_visibility(const 
             if (!more) break;
             continue;
         }
-        if (active && !tr.step(nodes, tris, false, &err, stack)) {
+        if (active && !tr.template step<kWalkTrisPerStep>(nodes, tris, false, &err, stack)) {
             GrisRayHit h;
             tr.result(&h, &rc.work);
             rc.shadow++;
