@@ -150,6 +150,7 @@ def parse():
                     help="c4: the guide's inference on tcgen05 (tensor memory) or mma.sync")
     ap.add_argument("--guide-train", default="tcgen05", choices=["tcgen05", "mma.sync"],
                     help="c4: the kernel of the guide's loss gradient")
+    ap.add_argument("--ref-cache", default=None, help="c4: path prefix of a saved converged image to reuse")
     ap.add_argument("--guide-mix", type=float, default=0.5, help="c4: probability of drawing from the guide")
     ap.add_argument("--guide-lr", type=float, default=1e-3, help="c4: Adam learning rate")
     ap.add_argument("--guide-records", type=int, default=1 << 18, help="c4: training records per frame")
@@ -380,10 +381,24 @@ def run_guided(args):
     # disagreement measures the converged image's own noise, stated beside every error it judges
     halves = [torch.zeros(n * 3, dtype=torch.float64, device="cuda") for _ in range(2)]
     t0 = time.perf_counter()
-    for i, k in enumerate(range(0, args.ref_spp, 32)):
-        scene.converged(cam0, st, W, H, dn.data_ptr(), am.data_ptr(), halves[i & 1].data_ptr(), None, spp_begin=k,
-                        spp=min(32, args.ref_spp - k), estimator=G.ESTIMATOR_CANDIDATES)
-    ctx.sync()
+    cache = None
+    if args.ref_cache:   # the same converged image for several runs (it depends on the scene, camera and depth only)
+        cache = "%s_%dx%d_d%d_s%d_g%d_n%d_spp%d.npy" % (args.ref_cache, W, H, args.depth, args.seed, args.grid, args.spheres,
+                                                          args.ref_spp)
+    cached = bool(cache and os.path.exists(cache))
+    if cached:
+        import numpy as np
+        both = np.load(cache)
+        for j in (0, 1):
+            halves[j].copy_(torch.from_numpy(both[j]))
+    else:
+        for i, k in enumerate(range(0, args.ref_spp, 32)):
+            scene.converged(cam0, st, W, H, dn.data_ptr(), am.data_ptr(), halves[i & 1].data_ptr(), None, spp_begin=k,
+                            spp=min(32, args.ref_spp - k), estimator=G.ESTIMATOR_CANDIDATES)
+        ctx.sync()
+        if cache:
+            import numpy as np
+            np.save(cache, np.stack([halves[0].cpu().numpy(), halves[1].cpu().numpy()]))
     ref_s = time.perf_counter() - t0
     ref = halves[0] + halves[1]
     scale = 1.0 / args.ref_spp
@@ -489,7 +504,8 @@ def run_guided(args):
                                                                 "mma.sync" if args.guide_train == "mma.sync" else "tcgen05",
                                                                 args.guide_mix, args.guide_lr, args.guide_records,
                                                                 args.guide_steps)},
-            "reference": {"spp": args.ref_spp, "seconds": ref_s, "estimator": "candidates", "noise_floor": ref_noise},
+            "reference": {"spp": args.ref_spp, "seconds": ref_s, "estimator": "candidates", "noise_floor": ref_noise,
+                          "loaded_from_cache": cached},
             "reuse": reuse, "mis": args.mis, "clocks": clocks,
             "median_error_time_ratio": ratio_med,
             "plain": {"fps": 1000.0 / float(tp.mean()), "total_ms": float(Tp), "relmse_final": float(rp[-1]),

@@ -144,6 +144,11 @@ struct GrisArrayStack {
         n--; b = base[n]; m = bits[n];
         return true;
     }
+    GRIS_HDM bool peek(uint32_t& b, uint32_t& m) const {
+        if (n == 0) return false;
+        b = base[n - 1]; m = bits[n - 1];
+        return true;
+    }
 };
 
 #ifdef __CUDACC__
@@ -185,6 +190,11 @@ struct GrisShortStack {
         b = b0; m = m0; b0 = b1; m0 = m1;
         if (n >= 3) load(n - 3, b1, m1);
         n--;
+        return true;
+    }
+    __device__ __forceinline__ bool peek(uint32_t& b, uint32_t& m) const {
+        if (n == 0) return false;
+        b = b0; m = m0;
         return true;
     }
 };
@@ -271,7 +281,7 @@ struct GrisTraversal {
      * The order of the box and triangle tests, and so every result and count, is the same for
      * every kTris; a small kTris only spreads a node's triangles over several steps, so that the
      * lanes of a warp whose nodes hit few triangles do not wait for the lane whose node hit many. */
-    template <int kTris = 0, class Stack>
+    template <int kTris = 0, bool kPrefetch = false, class Stack>
     GRIS_HDM bool step(const uint32_t* __restrict__ nodes, const float* __restrict__ tris, bool skipInst0, int* err,
                        Stack& stack) {
         if (haveNode) {
@@ -324,6 +334,21 @@ struct GrisTraversal {
                 grpBase = W[4]; grpHits = innerHits; grpImask = imask;
             }
             haveNode = false;
+#ifdef __CUDA_ARCH__
+            if (kPrefetch && kTris > 0 && triHits) {
+                /* the node visited after this one's triangles is known already (the group's first
+                 * remaining slot, or the top group of the stack): fetch it towards L1 while the
+                 * triangles are tested */
+                uint32_t nb = grpBase, nm = grpHits | (grpImask << 8);
+                if (grpHits || stack.peek(nb, nm)) {
+                    const uint32_t sl = (uint32_t)gris_ffs(nm & 0xffu) ^ oct;
+                    const uint32_t nxt = nb + (uint32_t)gris_popc((nm >> 8) & ((1u << sl) - 1u));
+                    const char* p = reinterpret_cast<const char*>(nodes + (uint64_t)nxt * GRIS_NODE_WORDS);
+                    asm volatile("prefetch.global.L1 [%0];" :: "l"(p));
+                    asm volatile("prefetch.global.L1 [%0];" :: "l"(p + 4 * GRIS_NODE_WORDS - 1));
+                }
+            }
+#endif
         }
         if (kTris == 0) {
             while (triHits)
