@@ -40,7 +40,7 @@ def ora():
 def gpu_sequence(ctx, hs, cams, prevs, st, W, H, mode=(G.PATH_WAVEFRONT, G.LAUNCH_GRID)):
     ctx.set_path_form(mode[0])
     ctx.set_launch_mode(mode[1])
-    ctx.set_wave_refill(len(mode) > 2 and mode[2])
+    ctx.set_wave_refill(mode[2] if len(mode) > 2 else 0)
     scene = G.Scene(ctx, hs)
     fr = G.Frame(ctx, W, H)
     ctx.counters(reset=True)
@@ -58,8 +58,9 @@ def gpu_sequence(ctx, hs, cams, prevs, st, W, H, mode=(G.PATH_WAVEFRONT, G.LAUNC
 
 
 MODES = [(G.PATH_WAVEFRONT, G.LAUNCH_GRID), (G.PATH_MEGAKERNEL, G.LAUNCH_GRID), (G.PATH_MEGAKERNEL, G.LAUNCH_PERSISTENT),
-         (G.PATH_WAVEFRONT, G.LAUNCH_GRID, True)]   # refilling wavefront: sparse levels walked one ray per warp
-MODE_IDS = ["wavefront", "megakernel-grid", "megakernel-persistent", "wavefront-refill"]
+         (G.PATH_WAVEFRONT, G.LAUNCH_GRID, 1),   # refilling wavefront: sparse levels walked one ray per warp
+         (G.PATH_WAVEFRONT, G.LAUNCH_GRID, 2)]   # eight lanes per ray (here the reuse passes' visibility queries)
+MODE_IDS = ["wavefront", "megakernel-grid", "megakernel-persistent", "wavefront-refill", "wavefront-group"]
 
 
 @pytest.mark.parametrize("mode", MODES, ids=MODE_IDS)
