@@ -436,12 +436,12 @@ int grisSetGraphs(GrisContext* ctx, int enable);
 int grisSetWaveLaunch(GrisContext* ctx, int traceBlocksPerSM, int shadeBlocksPerSM);
 /* The wavefront's traversal kernels: 0 one lane per ray over the level's queue; 1 one lane per ray,
  * every lane kept busy (a lane whose ray is finished takes the next ray while the others of its
- * warp still walk); 2 eight lanes per ray (each round a group tests the eight child boxes of one
- * node side by side, or up to eight of the triangles its last node hit), groups taking new rays
- * while the others walk, also for the reuse passes' visibility queries, where every view's BVH is
- * at most 27 levels deep (else mode 1). In modes 1 and 2 a bounce level with fewer than 8,192 rays
- * is walked one ray per warp (each round 4 nodes and up to 32 triangles). Same results in every
- * mode. */
+ * warp still walk); 2 / 3 eight / four lanes per ray (each round a group tests the eight child
+ * boxes of one node side by side, or up to eight of the triangles its last node hit), groups
+ * taking new rays while the others walk, also for the reuse passes' visibility queries, where
+ * every view's BVH is at most 27 levels deep (else mode 1). In modes 1-3 a bounce level with fewer
+ * than 8,192 rays is walked one ray per warp (each round 4 nodes and up to 32 triangles). Same
+ * results in every mode. */
 int grisSetWaveRefill(GrisContext* ctx, int mode);
 /* Times candidate configurations — the megakernel path tracer, the wavefront one with trace
  * grids of 8/16/32 and shading grids of 4/8/16 blocks per SM, the wavefront one with the
@@ -454,7 +454,7 @@ typedef struct GrisTuneResult {
     int candidates;
     double msPerFrame;            /* of the chosen configuration */
     double candidateMs[16];       /* per candidate, in the order above */
-    int refill;                   /* the chosen wavefront's traversal: 1 refilling, 2 eight lanes per ray */
+    int refill;                   /* the chosen wavefront's traversal (grisSetWaveRefill's mode) */
 } GrisTuneResult;
 int grisBatchCreate(GrisContext* ctx, uint32_t nViews, const GrisScene* const* scenes, const uint32_t* widths,
                     const uint32_t* heights, GrisBatch** out);

@@ -361,7 +361,7 @@ int grisSetWaveLaunch(GrisContext* ctx, int traceBlocksPerSM, int shadeBlocksPer
 }
 
 int grisSetWaveRefill(GrisContext* ctx, int mode) {
-    if (!ctx || mode < 0 || mode > 2) return GRIS_ERR_INVALID_ARGUMENT;
+    if (!ctx || mode < 0 || mode > 3) return GRIS_ERR_INVALID_ARGUMENT;
     ctx->waveLaunch.refill = mode;
     return GRIS_OK;
 }

@@ -2092,17 +2092,18 @@ __global__ void __launch_bounds__(128, kWalkMinBlocks) k_wave_trace_refill(WaveC
     flush_counts(C.counters, rc, err, 1, C.countWork, ANY ? 1 : 0);
 }
 
-/* ---------------------------------------------------------------- eight lanes per ray */
-/* The walk of full queues with a group of eight lanes per ray (four rays per warp): each round a
- * group either tests up to eight of the triangles its last node hit (one per lane, tmax = the best
- * t so far, the best reduced over the group) or visits the node on top of its stack — lane s
- * tests child slot s with the walker's box test, the hit inner children are pushed nearest on
- * top and the hit leaves' triangles listed. The node's 80 bytes are read by the eight lanes at the
- * same addresses (one transaction per 16 bytes for the group), the eight box tests run side by side,
- * and a warp's four rays take new rays from a pool the warp refills eight at a time. The closest
- * hit is the lexicographic minimum of (t, instanceIdx, triangleIdx) over the accepted triangles
- * whatever the visiting order, and an any-hit query asks only whether one exists, so the results
- * are the per-lane walk's, bit for bit (the node and triangle counts depend on the order). */
+/* ------------------------------------------------------- several lanes per ray (4 or 8) */
+/* The walk of full queues with a group of GW lanes per ray (GW = 8: four rays per warp; GW = 4:
+ * eight). Each round a group either tests up to eight of the triangles its last node hit (8 / GW
+ * per lane, tmax = the best t so far, the best reduced over the group) or visits the node on top
+ * of its stack — lane l tests child slots l, l + GW, ... with the walker's box test, the hit inner
+ * children are pushed nearest on top and the hit leaves' triangles listed. The node's 80 bytes are
+ * read by the group's lanes at the same addresses (one transaction per 16 bytes for the group),
+ * the box tests run side by side, and a warp's rays take new rays from a pool the warp refills by
+ * one atomic. The closest hit is the lexicographic minimum of (t, instanceIdx, triangleIdx) over
+ * the accepted triangles whatever the visiting order, and an any-hit query asks only whether one
+ * exists, so the results are the per-lane walk's, bit for bit (the node and triangle counts depend
+ * on the order). */
 constexpr uint32_t kGroupStack = 192;   /* node indices per group: 7 per level of a tree up to 27 deep */
 constexpr uint32_t kGroupTris = 24;     /* a node's leaf triangles: 8 slots x 3 */
 constexpr uint32_t kGroupMaxDepth = (kGroupStack - 1u) / 7u;
@@ -2134,11 +2135,18 @@ GD void group_ray_init(GroupRay& r, float ox, float oy, float oz, float dx, floa
     r.active = true;
 }
 
-/* One round of every group of the warp (all 32 lanes call it; lanes of a group hold the same ray
- * state). Returns true in the lanes of a group whose walk ended this round. */
-template <bool ANY>
+/* (t, inst, tri) lexicographically below the held best, or the held best empty */
+GD bool group_better(bool okB, float tB, uint32_t iB, uint32_t rB, bool okA, float tA, uint32_t iA, uint32_t rA) {
+    return okB && (!okA || tB < tA || (tB == tA && (iB < iA || (iB == iA && rB < rA))));
+}
+
+/* One round of every group of the warp (all 32 lanes call it; the lanes of a group hold the same
+ * ray state). Returns true in the lanes of a group whose walk ended this round. */
+template <bool ANY, int GW>
 GD bool group_round(GroupRay& r, const uint32_t* __restrict__ nodes, const float* __restrict__ tris, uint32_t* stack,
                     uint32_t* triList, uint32_t gl, uint32_t groupShift, RayCount& rc, int& err) {
+    constexpr uint32_t kPer = 8u / GW;                    /* child slots and batch triangles per lane */
+    constexpr uint32_t kMask = (1u << GW) - 1u;
     const bool doTri = r.active && r.triLeft > 0u;
     const bool doNode = r.active && !doTri && r.sp > 0u;
     bool ended = r.active && !doTri && r.sp == 0u;
@@ -2146,25 +2154,34 @@ GD bool group_round(GroupRay& r, const uint32_t* __restrict__ nodes, const float
     bool ok = false;
     float t = 0.0f, u = 0.0f, v = 0.0f;
     uint32_t inst = kInvalidHit, tri = kInvalidHit;
-    if (doTri && gl < r.triLeft) {
-        const float4* T4 = reinterpret_cast<const float4*>(tris + (uint64_t)triList[r.triPos + gl] * GRIS_TRI_FLOATS);
-        const float4 t0 = __ldg(T4 + 0), t1 = __ldg(T4 + 1), t2 = __ldg(T4 + 2);
-        const float TT[12] = {t0.x, t0.y, t0.z, t0.w, t1.x, t1.y, t1.z, t1.w, t2.x, t2.y, t2.z, t2.w};
-        inst = gris_f2u(TT[3]); tri = gris_f2u(TT[7]);
-        rc.work.tris++;
-        ok = gris_tri_test(TT, r.ox, r.oy, r.oz, r.dx, r.dy, r.dz, r.tmin, r.t, &t, &u, &v);
+    if (doTri) {
+#pragma unroll
+        for (uint32_t j = 0; j < kPer; j++) {
+            const uint32_t k = gl + GW * j;
+            if (k < r.triLeft) {
+                const float4* T4 =
+                    reinterpret_cast<const float4*>(tris + (uint64_t)triList[r.triPos + k] * GRIS_TRI_FLOATS);
+                const float4 t0 = __ldg(T4 + 0), t1 = __ldg(T4 + 1), t2 = __ldg(T4 + 2);
+                const float TT[12] = {t0.x, t0.y, t0.z, t0.w, t1.x, t1.y, t1.z, t1.w, t2.x, t2.y, t2.z, t2.w};
+                const uint32_t ik = gris_f2u(TT[3]), rk = gris_f2u(TT[7]);
+                rc.work.tris++;
+                float tk, uk, vk;
+                const bool okk = gris_tri_test(TT, r.ox, r.oy, r.oz, r.dx, r.dy, r.dz, r.tmin, r.t, &tk, &uk, &vk);
+                if (group_better(okk, tk, ik, rk, ok, t, inst, tri)) { ok = true; t = tk; u = uk; v = vk; inst = ik; tri = rk; }
+            }
+        }
     }
     if constexpr (ANY) {
         const unsigned b = __ballot_sync(0xffffffffu, ok);
-        if (doTri && ((b >> groupShift) & 0xffu)) { r.found = true; ended = true; }
+        if (doTri && ((b >> groupShift) & kMask)) { r.found = true; ended = true; }
     } else {
-        for (uint32_t off = 4u; off > 0u; off >>= 1) {   /* the group's best accepted triangle, in all its lanes */
+#pragma unroll
+        for (uint32_t off = GW / 2; off > 0u; off >>= 1) {   /* the group's best accepted triangle, in all its lanes */
             const bool ok2 = __shfl_xor_sync(0xffffffffu, ok, off);
             const float t2_ = __shfl_xor_sync(0xffffffffu, t, off), u2 = __shfl_xor_sync(0xffffffffu, u, off),
                         v2 = __shfl_xor_sync(0xffffffffu, v, off);
             const uint32_t i2 = __shfl_xor_sync(0xffffffffu, inst, off), r2 = __shfl_xor_sync(0xffffffffu, tri, off);
-            const bool take = ok2 && (!ok || t2_ < t || (t2_ == t && (i2 < inst || (i2 == inst && r2 < tri))));
-            if (take) { ok = true; t = t2_; u = u2; v = v2; inst = i2; tri = r2; }
+            if (group_better(ok2, t2_, i2, r2, ok, t, inst, tri)) { ok = true; t = t2_; u = u2; v = v2; inst = i2; tri = r2; }
         }
         if (doTri && ok) {
             const bool keyLess = inst < r.inst || (inst == r.inst && tri < r.tri);
@@ -2172,49 +2189,61 @@ GD bool group_round(GroupRay& r, const uint32_t* __restrict__ nodes, const float
         }
     }
     if (doTri) { r.triPos += 8u; r.triLeft = r.triLeft > 8u ? r.triLeft - 8u : 0u; }
-    /* ---- the node on top of the stack: lane gl tests child slot gl */
-    bool inner = false;
-    uint32_t child = 0u, triCnt = 0u, triFirst = 0u;
+    /* ---- the node on top of the stack: lane l tests child slots l + GW j */
+    bool inner[kPer];
+    uint32_t child[kPer], triCnt[kPer], triFirst[kPer];
+#pragma unroll
+    for (uint32_t j = 0; j < kPer; j++) { inner[j] = false; child[j] = 0u; triCnt[j] = 0u; triFirst[j] = 0u; }
     if (doNode) {
         const uint4* N = reinterpret_cast<const uint4*>(nodes + (uint64_t)stack[r.sp - 1u] * GRIS_NODE_WORDS);
         const uint4 w0 = __ldg(N + 0), w1 = __ldg(N + 1), w2 = __ldg(N + 2), w3 = __ldg(N + 3), w4 = __ldg(N + 4);
         const uint32_t W[20] = {w0.x, w0.y, w0.z, w0.w, w1.x, w1.y, w1.z, w1.w, w2.x, w2.y,
                                 w2.z, w2.w, w3.x, w3.y, w3.z, w3.w, w4.x, w4.y, w4.z, w4.w};
-        const uint32_t s = gl;
-        const uint32_t meta = gris_byte(W[6 + (s >> 2)], (int)(s & 3u));
-        if (meta != 0u) {
-            const float px = gris_u2f(W[0]), py = gris_u2f(W[1]), pz = gris_u2f(W[2]);
-            const uint32_t e = W[3], imask = e >> 24;
-            const float sx = gris_u2f((e & 0xffu) << 23), sy = gris_u2f(((e >> 8) & 0xffu) << 23),
-                        sz = gris_u2f(((e >> 16) & 0xffu) << 23);
-            const float ax = sx * r.idx, ay = sy * r.idy, az = sz * r.idz;
-            const float bx = (px - r.ox) * r.idx, by = (py - r.oy) * r.idy, bz = (pz - r.oz) * r.idz;
-            const int wi = (int)(s >> 2), bi = (int)(s & 3u);
-            const float lx = gris_fma((float)gris_byte(W[8 + wi], bi), ax, bx);
-            const float ly = gris_fma((float)gris_byte(W[10 + wi], bi), ay, by);
-            const float lz = gris_fma((float)gris_byte(W[12 + wi], bi), az, bz);
-            const float hx = gris_fma((float)gris_byte(W[14 + wi], bi), ax, bx);
-            const float hy = gris_fma((float)gris_byte(W[16 + wi], bi), ay, by);
-            const float hz = gris_fma((float)gris_byte(W[18 + wi], bi), az, bz);
+        const float px = gris_u2f(W[0]), py = gris_u2f(W[1]), pz = gris_u2f(W[2]);
+        const uint32_t e = W[3], imask = e >> 24;
+        const float sx = gris_u2f((e & 0xffu) << 23), sy = gris_u2f(((e >> 8) & 0xffu) << 23),
+                    sz = gris_u2f(((e >> 16) & 0xffu) << 23);
+        const float ax = sx * r.idx, ay = sy * r.idy, az = sz * r.idz;
+        const float bx = (px - r.ox) * r.idx, by = (py - r.oy) * r.idy, bz = (pz - r.oz) * r.idz;
+#pragma unroll
+        for (uint32_t j = 0; j < kPer; j++) {
+            const uint32_t s = gl + GW * j;
+            const bool hi = (s >> 2) != 0u;                 /* the slot's word of each byte array, chosen */
+            const int bi = (int)(s & 3u);                   /* without a run-time index into W */
+            const uint32_t meta = gris_byte(hi ? W[7] : W[6], bi);
+            if (meta == 0u) continue;
+            const float lx = gris_fma((float)gris_byte(hi ? W[9] : W[8], bi), ax, bx);
+            const float ly = gris_fma((float)gris_byte(hi ? W[11] : W[10], bi), ay, by);
+            const float lz = gris_fma((float)gris_byte(hi ? W[13] : W[12], bi), az, bz);
+            const float hx = gris_fma((float)gris_byte(hi ? W[15] : W[14], bi), ax, bx);
+            const float hy = gris_fma((float)gris_byte(hi ? W[17] : W[16], bi), ay, by);
+            const float hz = gris_fma((float)gris_byte(hi ? W[19] : W[18], bi), az, bz);
             const float tn = gris_fmax(gris_fmax(gris_fmin(lx, hx), gris_fmin(ly, hy)), gris_fmax(gris_fmin(lz, hz), r.tmin));
             const float tf = gris_fmin(gris_fmin(gris_fmax(lx, hx), gris_fmax(ly, hy)), gris_fmin(gris_fmax(lz, hz), r.t));
             if (tn <= tf) {
-                if (imask & (1u << s)) { inner = true; child = W[4] + (uint32_t)__popc(imask & ((1u << s) - 1u)); }
-                else { triCnt = (meta >> 5) & 3u; triFirst = W[5] + (meta & 31u); }
+                if (imask & (1u << s)) { inner[j] = true; child[j] = W[4] + (uint32_t)__popc(imask & ((1u << s) - 1u)); }
+                else { triCnt[j] = (meta >> 5) & 3u; triFirst[j] = W[5] + (meta & 31u); }
             }
         }
     }
-    const uint32_t gin = (__ballot_sync(0xffffffffu, inner) >> groupShift) & 0xffu;
-    uint32_t incl = triCnt;
-    for (uint32_t d = 1u; d < 8u; d <<= 1) {
-        const uint32_t x = __shfl_up_sync(0xffffffffu, incl, d, 8);
+    uint32_t gin = 0u, mine = 0u;
+#pragma unroll
+    for (uint32_t j = 0; j < kPer; j++) {
+        gin |= ((__ballot_sync(0xffffffffu, inner[j]) >> groupShift) & kMask) << (GW * j);
+        mine += triCnt[j];
+    }
+    uint32_t incl = mine;
+#pragma unroll
+    for (uint32_t d = 1u; d < (uint32_t)GW; d <<= 1) {
+        const uint32_t x = __shfl_up_sync(0xffffffffu, incl, d, GW);
         if (gl >= d) incl += x;
     }
-    const uint32_t total = __shfl_sync(0xffffffffu, incl, 7, 8);
+    const uint32_t total = __shfl_sync(0xffffffffu, incl, GW - 1, GW);
     if (doNode) {
         r.sp -= 1u;
         /* positions along the ray's octant order: the nearest child ends on top */
         uint32_t pm = 0u;
+#pragma unroll
         for (uint32_t q = 0; q < 8u; q++)
             if ((gin >> q) & 1u) pm |= 1u << (q ^ r.oct);
         const uint32_t nIn = (uint32_t)__popc(gin);
@@ -2222,10 +2251,15 @@ GD bool group_round(GroupRay& r, const uint32_t* __restrict__ nodes, const float
             err = 1;                                      /* not reached: the host checks the tree depth */
             ended = true;
         } else {
-            if (inner) stack[r.sp + (uint32_t)__popc(pm >> ((gl ^ r.oct) + 1u))] = child;
+#pragma unroll
+            for (uint32_t j = 0; j < kPer; j++)
+                if (inner[j]) stack[r.sp + (uint32_t)__popc(pm >> (((gl + GW * j) ^ r.oct) + 1u))] = child[j];
             r.sp += nIn;
         }
-        for (uint32_t k = 0; k < triCnt; k++) triList[incl - triCnt + k] = triFirst + k;
+        uint32_t at = incl - mine;
+#pragma unroll
+        for (uint32_t j = 0; j < kPer; j++)
+            for (uint32_t k = 0; k < triCnt[j]; k++) triList[at++] = triFirst[j] + k;
         r.triLeft = total;
         r.triPos = 0u;
         if (gl == 0u) rc.work.nodes++;
@@ -2235,24 +2269,27 @@ GD bool group_round(GroupRay& r, const uint32_t* __restrict__ nodes, const float
 }
 
 /* The warp's pool of ray indices: groups whose walk ended take the next indices; when the pool
- * runs short one atomic takes eight more from the queue's cursor. Returns the index given to
- * this lane's group (or n: none). All lanes call it. */
+ * runs short one atomic takes 32 / GW * 2 more from the queue's cursor. Returns the index given
+ * to this lane's group (or n: none). All lanes call it. */
+template <int GW>
 GD uint32_t group_take(bool idle, uint32_t gl, uint32_t gw, uint32_t lane, uint32_t n, uint32_t* cursor,
                        uint32_t& poolBase, uint32_t& poolLeft, bool& more) {
-    const unsigned need = __ballot_sync(0xffffffffu, idle && gl == 0u) & 0x01010101u;
+    constexpr uint32_t kLeaders = GW == 8 ? 0x01010101u : 0x11111111u;
+    constexpr uint32_t kFetch = 64u / GW;                 /* two rounds of the warp's groups */
+    const unsigned need = __ballot_sync(0xffffffffu, idle && gl == 0u) & kLeaders;
     if (!need || (!more && poolLeft == 0u)) return n;
     const uint32_t nNeed = (uint32_t)__popc(need);
     uint32_t newBase = n, newValid = 0u;
     if (poolLeft < nNeed && more) {
         uint32_t b = 0u;
-        if (lane == 0u) b = atomicAdd(cursor, 8u);
+        if (lane == 0u) b = atomicAdd(cursor, kFetch);
         newBase = __shfl_sync(0xffffffffu, b, 0);
-        newValid = newBase < n ? min(8u, n - newBase) : 0u;
-        if (newBase + 8u >= n) more = false;
+        newValid = newBase < n ? min(kFetch, n - newBase) : 0u;
+        if (newBase + kFetch >= n) more = false;
     }
-    const uint32_t k = (uint32_t)__popc(need & ((1u << (gw * 8u)) - 1u));
+    const uint32_t k = (uint32_t)__popc(need & ((1u << (gw * GW)) - 1u));
     uint32_t i = n;
-    if (idle && ((need >> (gw * 8u)) & 1u)) {
+    if (idle && ((need >> (gw * GW)) & 1u)) {
         if (k < poolLeft) i = poolBase + k;
         else if (k - poolLeft < newValid) i = newBase + (k - poolLeft);
     }
@@ -2265,14 +2302,15 @@ GD uint32_t group_take(bool idle, uint32_t gl, uint32_t gw, uint32_t lane, uint3
     return i;
 }
 
-/* the level's closest hits (ANY = false) or shadow queries (ANY = true), eight lanes per ray */
-template <bool ANY>
+/* the level's closest hits (ANY = false) or shadow queries (ANY = true), GW lanes per ray */
+template <bool ANY, int GW>
 __global__ void __launch_bounds__(128) k_wave_trace_group(WaveCtx C, int level) {
+    constexpr uint32_t kGroups = 128u / GW;
     const uint32_t n = ANY ? C.counts[256 + level] : C.counts[level];
     if (n < kCoopMaxRays) return;                         /* k_wave_trace_coop takes a sparse level */
-    __shared__ uint32_t sStack[16][kGroupStack];
-    __shared__ uint32_t sTris[16][kGroupTris];
-    const uint32_t lane = threadIdx.x & 31u, gl = lane & 7u, gw = lane >> 3, g = threadIdx.x >> 3;
+    __shared__ uint32_t sStack[kGroups][kGroupStack];
+    __shared__ uint32_t sTris[kGroups][kGroupTris];
+    const uint32_t lane = threadIdx.x & 31u, gl = lane % GW, gw = lane / GW, g = threadIdx.x / GW;
     uint32_t* stack = sStack[g];
     uint32_t* triList = sTris[g];
     const uint32_t* q = ANY ? C.shadowQueue : C.queue[level & 1];
@@ -2286,7 +2324,7 @@ __global__ void __launch_bounds__(128) k_wave_trace_group(WaveCtx C, int level) 
     uint32_t poolBase = 0u, poolLeft = 0u;
     bool more = true;
     while (true) {
-        const uint32_t i = group_take(!r.active, gl, gw, lane, n, cursor, poolBase, poolLeft, more);
+        const uint32_t i = group_take<GW>(!r.active, gl, gw, lane, n, cursor, poolBase, poolLeft, more);
         if (i < n) {
             const uint32_t id = q[i];
             const int v = find_view_by_pixel(C.V, C.nViews, id);
@@ -2311,7 +2349,7 @@ __global__ void __launch_bounds__(128) k_wave_trace_group(WaveCtx C, int level) 
             if (!more && poolLeft == 0u) break;
             continue;
         }
-        if (group_round<ANY>(r, nodes, tris, stack, triList, gl, gw * 8u, rc, err)) {
+        if (group_round<ANY, GW>(r, nodes, tris, stack, triList, gl, gw * GW, rc, err)) {
             if (gl == 0u) {
                 if (ANY) {
                     rc.shadow++;
@@ -2712,16 +2750,17 @@ __global__ void __launch_bounds__(128, kWalkMinBlocks) k_reuse_visibility(const 
     flush_counts(V[0].P.counters, rc, err, KERNEL, V[0].P.countWork, KERNEL);
 }
 
-/* The pass's visibility queries walked eight lanes per query (k_wave_trace_group's walk); chosen
- * with the wavefront's group traversal (grisSetWaveRefill(ctx, 2)). */
-template <int KERNEL>
+/* The pass's visibility queries walked GW lanes per query (k_wave_trace_group's walk); chosen
+ * with the wavefront's group traversal (grisSetWaveRefill(ctx, 2 or 3)). */
+template <int KERNEL, int GW>
 __global__ void __launch_bounds__(128) k_reuse_visibility_group(const ViewEntry* __restrict__ V, int nViews, ReuseCtx R,
                                                                int which) {
+    constexpr uint32_t kGroups = 128u / GW;
     const uint32_t n = R.counts[2 * which];
     uint32_t* cursor = R.counts + 2 * which + 1;
-    __shared__ uint32_t sStack[16][kGroupStack];
-    __shared__ uint32_t sTris[16][kGroupTris];
-    const uint32_t lane = threadIdx.x & 31u, gl = lane & 7u, gw = lane >> 3, g = threadIdx.x >> 3;
+    __shared__ uint32_t sStack[kGroups][kGroupStack];
+    __shared__ uint32_t sTris[kGroups][kGroupTris];
+    const uint32_t lane = threadIdx.x & 31u, gl = lane % GW, gw = lane / GW, g = threadIdx.x / GW;
     uint32_t* stack = sStack[g];
     uint32_t* triList = sTris[g];
     RayCount rc = ray_count();
@@ -2733,7 +2772,7 @@ __global__ void __launch_bounds__(128) k_reuse_visibility_group(const ViewEntry*
     uint32_t poolBase = 0u, poolLeft = 0u;
     bool more = true;
     while (true) {
-        const uint32_t i = group_take(!r.active, gl, gw, lane, n, cursor, poolBase, poolLeft, more);
+        const uint32_t i = group_take<GW>(!r.active, gl, gw, lane, n, cursor, poolBase, poolLeft, more);
         if (i < n) {
             const float4 a = R.q[2 * (uint64_t)i], b = R.q[2 * (uint64_t)i + 1];
             const uint32_t slot = __float_as_uint(b.w);
@@ -2748,7 +2787,7 @@ __global__ void __launch_bounds__(128) k_reuse_visibility_group(const ViewEntry*
             if (!more && poolLeft == 0u) break;
             continue;
         }
-        if (group_round<true>(r, nodes, tris, stack, triList, gl, gw * 8u, rc, err)) {
+        if (group_round<true, GW>(r, nodes, tris, stack, triList, gl, gw * GW, rc, err)) {
             if (gl == 0u) {
                 rc.shadow++;
                 if (!r.found) R.ps[r.id] |= kRsVisible;
@@ -3054,8 +3093,8 @@ cudaError_t enqueue_batch(const BatchShape& sh, void* dViews, const void* hViews
             const int gridShade = sm * (wl.shadeBlocksPerSM > 0 ? wl.shadeBlocksPerSM : 8);
             const int gridTrace = sm * (wl.traceBlocksPerSM > 0 ? wl.traceBlocksPerSM : 16);
             const int gridCoop = sm * 4;   /* sparse levels: 4 blocks of 4 warps per SM, 17.9 KB shared each */
-            /* eight lanes per ray (refill mode 2), where every view's tree fits the group stack */
-            const bool group = wl.refill == 2 && sh.maxBvhDepth <= kGroupMaxDepth;
+            /* eight or four lanes per ray (refill mode 2 or 3), where every view's tree fits the group stack */
+            const int group = sh.maxBvhDepth > kGroupMaxDepth ? 0 : wl.refill == 2 ? 8 : wl.refill == 3 ? 4 : 0;
             /* timer slots 4..8: begin, extend, shade, shadow, post */
             auto mark = [&](int slot, bool begin) { if (timer) timer->mark(slot, begin, stream); };
             if (guide) {
@@ -3078,7 +3117,8 @@ cudaError_t enqueue_batch(const BatchShape& sh, void* dViews, const void* hViews
                 mark(4, false);
                 for (int level = 1; level < sh.maxDepth; level++) {
                     mark(5, true);
-                    if (group) { k_wave_trace_group<false><<<gridTrace, 128, 0, stream>>>(C, level); k_wave_trace_coop<false><<<gridCoop, 128, 0, stream>>>(C, level); }
+                    if (group == 8) { k_wave_trace_group<false, 8><<<gridTrace, 128, 0, stream>>>(C, level); k_wave_trace_coop<false><<<gridCoop, 128, 0, stream>>>(C, level); }
+                else if (group == 4) { k_wave_trace_group<false, 4><<<gridTrace, 128, 0, stream>>>(C, level); k_wave_trace_coop<false><<<gridCoop, 128, 0, stream>>>(C, level); }
                     else if (wl.refill) { k_wave_trace_refill<false><<<gridTrace, 128, 0, stream>>>(C, level); k_wave_trace_coop<false><<<gridCoop, 128, 0, stream>>>(C, level); }
                     else k_wave_extend<<<gridTrace, 128, 0, stream>>>(C, level);
                     mark(5, false);
@@ -3086,7 +3126,8 @@ cudaError_t enqueue_batch(const BatchShape& sh, void* dViews, const void* hViews
                     k_gwave_shade<<<gridShade, 128, 0, stream>>>(C, level);
                     mark(6, false);
                     mark(7, true);
-                    if (group) { k_wave_trace_group<true><<<gridTrace, 128, 0, stream>>>(C, level); k_wave_trace_coop<true><<<gridCoop, 128, 0, stream>>>(C, level); }
+                    if (group == 8) { k_wave_trace_group<true, 8><<<gridTrace, 128, 0, stream>>>(C, level); k_wave_trace_coop<true><<<gridCoop, 128, 0, stream>>>(C, level); }
+                else if (group == 4) { k_wave_trace_group<true, 4><<<gridTrace, 128, 0, stream>>>(C, level); k_wave_trace_coop<true><<<gridCoop, 128, 0, stream>>>(C, level); }
                     else if (wl.refill) { k_wave_trace_refill<true><<<gridTrace, 128, 0, stream>>>(C, level); k_wave_trace_coop<true><<<gridCoop, 128, 0, stream>>>(C, level); }
                     else k_wave_shadow<<<gridTrace, 128, 0, stream>>>(C, level);
                     mark(7, false);
@@ -3110,7 +3151,8 @@ cudaError_t enqueue_batch(const BatchShape& sh, void* dViews, const void* hViews
             mark(4, false);
             for (int level = 1; level < sh.maxDepth; level++) {
                 mark(5, true);
-                if (group) { k_wave_trace_group<false><<<gridTrace, 128, 0, stream>>>(C, level); k_wave_trace_coop<false><<<gridCoop, 128, 0, stream>>>(C, level); }
+                if (group == 8) { k_wave_trace_group<false, 8><<<gridTrace, 128, 0, stream>>>(C, level); k_wave_trace_coop<false><<<gridCoop, 128, 0, stream>>>(C, level); }
+                else if (group == 4) { k_wave_trace_group<false, 4><<<gridTrace, 128, 0, stream>>>(C, level); k_wave_trace_coop<false><<<gridCoop, 128, 0, stream>>>(C, level); }
                 else if (wl.refill) { k_wave_trace_refill<false><<<gridTrace, 128, 0, stream>>>(C, level); k_wave_trace_coop<false><<<gridCoop, 128, 0, stream>>>(C, level); }
                 else k_wave_extend<<<gridTrace, 128, 0, stream>>>(C, level);
                 mark(5, false);
@@ -3118,7 +3160,8 @@ cudaError_t enqueue_batch(const BatchShape& sh, void* dViews, const void* hViews
                 k_wave_shade<<<gridShade, 128, 0, stream>>>(C, level);
                 mark(6, false);
                 mark(7, true);
-                if (group) { k_wave_trace_group<true><<<gridTrace, 128, 0, stream>>>(C, level); k_wave_trace_coop<true><<<gridCoop, 128, 0, stream>>>(C, level); }
+                if (group == 8) { k_wave_trace_group<true, 8><<<gridTrace, 128, 0, stream>>>(C, level); k_wave_trace_coop<true><<<gridCoop, 128, 0, stream>>>(C, level); }
+                else if (group == 4) { k_wave_trace_group<true, 4><<<gridTrace, 128, 0, stream>>>(C, level); k_wave_trace_coop<true><<<gridCoop, 128, 0, stream>>>(C, level); }
                 else if (wl.refill) { k_wave_trace_refill<true><<<gridTrace, 128, 0, stream>>>(C, level); k_wave_trace_coop<true><<<gridCoop, 128, 0, stream>>>(C, level); }
                 else k_wave_shadow<<<gridTrace, 128, 0, stream>>>(C, level);
                 mark(7, false);
@@ -3150,13 +3193,14 @@ reuse:
         if (e != cudaSuccess) return e;
     }
     const int gridVis = current_sm_count() * (wl.traceBlocksPerSM > 0 ? wl.traceBlocksPerSM : 16);
-    const bool visGroup = wl.refill == 2 && sh.maxBvhDepth <= kGroupMaxDepth;
+    const int visGroup = sh.maxBvhDepth > kGroupMaxDepth ? 0 : wl.refill == 2 ? 8 : wl.refill == 3 ? 4 : 0;
     if (split && (passes & 2)) {
         if (timer) timer->mark(2, true, stream);
         if (guide) k_reuse_temporal_prepare<true><<<tiles, blk, 0, stream>>>(V, n, R);
         else k_reuse_temporal_prepare<false><<<tiles, blk, 0, stream>>>(V, n, R);
         if (timer) timer->mark(GRIS_SLOT_REUSE_VIS_TEMPORAL, true, stream);
-        if (visGroup) k_reuse_visibility_group<2><<<gridVis, 128, 0, stream>>>(V, n, R, 0);
+        if (visGroup == 8) k_reuse_visibility_group<2, 8><<<gridVis, 128, 0, stream>>>(V, n, R, 0);
+        else if (visGroup == 4) k_reuse_visibility_group<2, 4><<<gridVis, 128, 0, stream>>>(V, n, R, 0);
         else k_reuse_visibility<2><<<gridVis, 128, 0, stream>>>(V, n, R, 0);
         if (timer) timer->mark(GRIS_SLOT_REUSE_VIS_TEMPORAL, false, stream);
         k_reuse_temporal_finish<<<tiles, blk, 0, stream>>>(V, n, R);
@@ -3167,7 +3211,8 @@ reuse:
         if (guide) k_reuse_spatial_prepare<true><<<tiles, blk, 0, stream>>>(V, n, R);
         else k_reuse_spatial_prepare<false><<<tiles, blk, 0, stream>>>(V, n, R);
         if (timer) timer->mark(GRIS_SLOT_REUSE_VIS_SPATIAL, true, stream);
-        if (visGroup) k_reuse_visibility_group<3><<<gridVis, 128, 0, stream>>>(V, n, R, 1);
+        if (visGroup == 8) k_reuse_visibility_group<3, 8><<<gridVis, 128, 0, stream>>>(V, n, R, 1);
+        else if (visGroup == 4) k_reuse_visibility_group<3, 4><<<gridVis, 128, 0, stream>>>(V, n, R, 1);
         else k_reuse_visibility<3><<<gridVis, 128, 0, stream>>>(V, n, R, 1);
         if (timer) timer->mark(GRIS_SLOT_REUSE_VIS_SPATIAL, false, stream);
         if (guide) k_reuse_spatial_finish<true><<<tiles, blk, 0, stream>>>(V, n, R);

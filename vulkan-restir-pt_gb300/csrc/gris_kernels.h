@@ -112,7 +112,7 @@ struct WaveLaunch {
     int traceBlocksPerSM = 16;
     int shadeBlocksPerSM = 8;
     int refill = 0;   /* 1: the resident traversal kernels (lanes take new rays while others walk);
-                         2: eight lanes per ray (groups take new rays while others walk) */
+                         2 / 3: eight / four lanes per ray (groups take new rays while others walk) */
 };
 
 struct BatchShape {

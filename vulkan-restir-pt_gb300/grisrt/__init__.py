@@ -550,7 +550,7 @@ class Context:
                    "grisSetWaveLaunch")
 
     def set_wave_refill(self, mode):
-        """0 one lane per ray, 1 one lane per ray with refill (True), 2 eight lanes per ray."""
+        """0 one lane per ray, 1 one lane per ray with refill (True), 2 / 3 eight / four lanes per ray."""
         self.check(load().grisSetWaveRefill(self.h, int(mode)), "grisSetWaveRefill")
 
     def set_work_counting(self, enable):
