@@ -411,7 +411,9 @@ bool build_bvh(const GrisSceneDesc& d, BvhHost& out, std::string& err) {
             if (e < -126) e = -126;
             while (!quantise_axis(pf, e, clo[a], chi[a], valid, q[a])) {
                 e++;
-                if (e > 127) { err = "BVH quantisation failed (scene extent too large)"; return false; }
+                /* scales up to 2^28 keep scale / |direction| finite for every ray (|1/d| <= 1e30),
+                 * which the walk's near/far plane selection needs (boxes up to 6.8e10 wide) */
+                if (e > 28) { err = "BVH quantisation failed (scene extent too large)"; return false; }
             }
             memcpy(&W[a], &pf, 4);
             ew |= q[a].e << (8 * a);

@@ -1868,6 +1868,7 @@ GD CoopHit coop_walk(const uint32_t* __restrict__ nodes, const float* __restrict
     const float idx = 1.0f / ((dx > tiny || dx < -tiny) ? dx : (dx < 0.0f ? -tiny : tiny));
     const float idy = 1.0f / ((dy > tiny || dy < -tiny) ? dy : (dy < 0.0f ? -tiny : tiny));
     const float idz = 1.0f / ((dz > tiny || dz < -tiny) ? dz : (dz < 0.0f ? -tiny : tiny));
+    const uint32_t oct = (dx < 0.0f ? 1u : 0u) | (dy < 0.0f ? 2u : 0u) | (dz < 0.0f ? 4u : 0u);
     CoopHit best;
     best.found = false; best.t = tmax; best.u = 0.0f; best.v = 0.0f; best.inst = kInvalidHit; best.tri = kInvalidHit;
     if (ox != ox || oy != oy || oz != oz || dx != dx || dy != dy || dz != dz) return best;   /* as GrisTraversal::init */
@@ -1884,24 +1885,12 @@ GD CoopHit coop_walk(const uint32_t* __restrict__ nodes, const float* __restrict
             const uint4 w0 = __ldg(N + 0), w1 = __ldg(N + 1), w2 = __ldg(N + 2), w3 = __ldg(N + 3), w4 = __ldg(N + 4);
             const uint32_t W[20] = {w0.x, w0.y, w0.z, w0.w, w1.x, w1.y, w1.z, w1.w, w2.x, w2.y,
                                     w2.z, w2.w, w3.x, w3.y, w3.z, w3.w, w4.x, w4.y, w4.z, w4.w};
-            const uint32_t meta = gris_byte(W[6 + (s >> 2)], (int)(s & 3u));
+            const uint32_t meta = gris_byte((s >> 2) ? W[7] : W[6], (int)(s & 3u));
             if (meta != 0u) {
-                const float px = gris_u2f(W[0]), py = gris_u2f(W[1]), pz = gris_u2f(W[2]);
-                const uint32_t e = W[3], imask = e >> 24;
-                const float sx = gris_u2f((e & 0xffu) << 23), sy = gris_u2f(((e >> 8) & 0xffu) << 23),
-                            sz = gris_u2f(((e >> 16) & 0xffu) << 23);
-                const float ax = sx * idx, ay = sy * idy, az = sz * idz;
-                const float bx = (px - ox) * idx, by = (py - oy) * idy, bz = (pz - oz) * idz;
-                const int wi = (int)(s >> 2), bi = (int)(s & 3u);
-                const float lx = gris_fma((float)gris_byte(W[8 + wi], bi), ax, bx);
-                const float ly = gris_fma((float)gris_byte(W[10 + wi], bi), ay, by);
-                const float lz = gris_fma((float)gris_byte(W[12 + wi], bi), az, bz);
-                const float hx = gris_fma((float)gris_byte(W[14 + wi], bi), ax, bx);
-                const float hy = gris_fma((float)gris_byte(W[16 + wi], bi), ay, by);
-                const float hz = gris_fma((float)gris_byte(W[18 + wi], bi), az, bz);
-                const float tn = gris_fmax(gris_fmax(gris_fmin(lx, hx), gris_fmin(ly, hy)), gris_fmax(gris_fmin(lz, hz), tmin));
-                const float tf = gris_fmin(gris_fmin(gris_fmax(lx, hx), gris_fmax(ly, hy)), gris_fmin(gris_fmax(lz, hz), best.t));
-                if (tn <= tf) {
+                const uint32_t imask = W[3] >> 24;
+                GrisNodeRay nr;
+                gris_node_ray(W, ox, oy, oz, idx, idy, idz, oct, nr);
+                if (gris_slot_hit(nr, (int)s, tmin, best.t)) {
                     if (imask & (1u << s)) { inner = true; child = W[4] + (uint32_t)__popc(imask & ((1u << s) - 1u)); }
                     else { triCnt = (meta >> 5) & 3u; triFirst = W[5] + (meta & 31u); }
                 }
@@ -2199,28 +2188,15 @@ GD bool group_round(GroupRay& r, const uint32_t* __restrict__ nodes, const float
         const uint4 w0 = __ldg(N + 0), w1 = __ldg(N + 1), w2 = __ldg(N + 2), w3 = __ldg(N + 3), w4 = __ldg(N + 4);
         const uint32_t W[20] = {w0.x, w0.y, w0.z, w0.w, w1.x, w1.y, w1.z, w1.w, w2.x, w2.y,
                                 w2.z, w2.w, w3.x, w3.y, w3.z, w3.w, w4.x, w4.y, w4.z, w4.w};
-        const float px = gris_u2f(W[0]), py = gris_u2f(W[1]), pz = gris_u2f(W[2]);
-        const uint32_t e = W[3], imask = e >> 24;
-        const float sx = gris_u2f((e & 0xffu) << 23), sy = gris_u2f(((e >> 8) & 0xffu) << 23),
-                    sz = gris_u2f(((e >> 16) & 0xffu) << 23);
-        const float ax = sx * r.idx, ay = sy * r.idy, az = sz * r.idz;
-        const float bx = (px - r.ox) * r.idx, by = (py - r.oy) * r.idy, bz = (pz - r.oz) * r.idz;
+        const uint32_t imask = W[3] >> 24;
+        GrisNodeRay nr;
+        gris_node_ray(W, r.ox, r.oy, r.oz, r.idx, r.idy, r.idz, r.oct, nr);
 #pragma unroll
         for (uint32_t j = 0; j < kPer; j++) {
             const uint32_t s = gl + GW * j;
-            const bool hi = (s >> 2) != 0u;                 /* the slot's word of each byte array, chosen */
-            const int bi = (int)(s & 3u);                   /* without a run-time index into W */
-            const uint32_t meta = gris_byte(hi ? W[7] : W[6], bi);
+            const uint32_t meta = gris_byte((s >> 2) ? W[7] : W[6], (int)(s & 3u));   /* selects, no run-time index */
             if (meta == 0u) continue;
-            const float lx = gris_fma((float)gris_byte(hi ? W[9] : W[8], bi), ax, bx);
-            const float ly = gris_fma((float)gris_byte(hi ? W[11] : W[10], bi), ay, by);
-            const float lz = gris_fma((float)gris_byte(hi ? W[13] : W[12], bi), az, bz);
-            const float hx = gris_fma((float)gris_byte(hi ? W[15] : W[14], bi), ax, bx);
-            const float hy = gris_fma((float)gris_byte(hi ? W[17] : W[16], bi), ay, by);
-            const float hz = gris_fma((float)gris_byte(hi ? W[19] : W[18], bi), az, bz);
-            const float tn = gris_fmax(gris_fmax(gris_fmin(lx, hx), gris_fmin(ly, hy)), gris_fmax(gris_fmin(lz, hz), r.tmin));
-            const float tf = gris_fmin(gris_fmin(gris_fmax(lx, hx), gris_fmax(ly, hy)), gris_fmin(gris_fmax(lz, hz), r.t));
-            if (tn <= tf) {
+            if (gris_slot_hit(nr, (int)s, r.tmin, r.t)) {
                 if (imask & (1u << s)) { inner[j] = true; child[j] = W[4] + (uint32_t)__popc(imask & ((1u << s) - 1u)); }
                 else { triCnt[j] = (meta >> 5) & 3u; triFirst[j] = W[5] + (meta & 31u); }
             }
