@@ -167,8 +167,7 @@ def parse():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-autotune", action="store_true")
     ap.add_argument("--wave", default=None,
-                    help="with --no-autotune: the wavefront launch as TRACE,SHADE[,refill|group|group4] blocks per SM "
-                         "(e.g. 16,16,refill; group / group4: eight / four lanes per ray), "
+                    help="with --no-autotune: the wavefront launch as TRACE,SHADE[,refill] blocks per SM (e.g. 16,16,refill), "
                          "the form the autotuner picks, so that a profiler run can skip the tuning frames")
     ap.add_argument("--no-graphs", action="store_true")
     ap.add_argument("--launch-mode", default="grid", choices=["persistent", "grid"])
@@ -816,7 +815,7 @@ def main():
     if args.wave:
         parts = args.wave.split(",")
         ctx.set_wave_launch(int(parts[0]), int(parts[1]))
-        ctx.set_wave_refill({"refill": 1, "group": 2, "group4": 3}.get(parts[2], 0) if len(parts) > 2 else 0)
+        ctx.set_wave_refill(len(parts) > 2 and parts[2] == "refill")
     ctx.set_graphs(not args.no_graphs)
     scenes = [G.Scene(ctx, v.hs) for v in views]
     stats = [sc.stats() for sc in scenes]
@@ -846,8 +845,7 @@ def main():
         names = (["megakernel"] + ["wavefront t%d s%d" % (t, s) for t in (8, 16, 32) for s in (4, 8, 16)] +
                  ["wavefront refill t%d s16" % t for t in (4, 8, 16)])
         tune = {"chosen": "megakernel" if r.pathForm == G.PATH_MEGAKERNEL else
-                "wavefront%s t%d s%d" % ({1: " refill", 2: " group", 3: " group4"}.get(r.refill, ""), r.traceBlocksPerSM,
-                                         r.shadeBlocksPerSM),
+                "wavefront%s t%d s%d" % (" refill" if r.refill else "", r.traceBlocksPerSM, r.shadeBlocksPerSM),
                 "ms": {names[i]: round(r.candidateMs[i], 3) for i in range(r.candidates)}}
         form = r.pathForm
     else:
@@ -927,8 +925,8 @@ def main():
             for k in ("nodes", "tris"):
                 work[pas][k] = max(0, work[pas][k] - work[vis][k])
         slots += ["reuse_vis_temporal", "reuse_vis_spatial"]
-    refill = (tune is not None and (" refill" in tune["chosen"] or " group" in tune["chosen"])) or (
-        tune is None and bool(args.wave) and (args.wave.endswith("refill") or "group" in args.wave))
+    refill = (tune is not None and " refill" in tune["chosen"]) or (tune is None and bool(args.wave) and
+                                                                    args.wave.endswith("refill"))
     launches_per_frame = kernel_launches_per_frame(prof, slots, K, wave, refill)
 
     # ---------------- end to end through the C ABI with host buffers

@@ -434,17 +434,12 @@ int grisSetPathForm(GrisContext* ctx, int form);
 int grisSetGraphs(GrisContext* ctx, int enable);
 /* Grid sizes of the wavefront kernels, in 128-thread blocks per SM (defaults 16 and 8). */
 int grisSetWaveLaunch(GrisContext* ctx, int traceBlocksPerSM, int shadeBlocksPerSM);
-/* The wavefront's traversal kernels: 0 one lane per ray over the level's queue; 1 one lane per ray,
- * every lane kept busy (a lane whose ray is finished takes the next ray while the others of its
- * warp still walk); 2 / 3 eight / four lanes per ray (each round a group tests the eight child
- * boxes of one node side by side, or up to eight of the triangles its last node hit), groups
- * taking new rays while the others walk, also for the reuse passes' visibility queries, where
- * every view's BVH is at most 27 levels deep (else mode 1). In modes 1-3 a bounce level with fewer
- * than 8,192 rays is walked one ray per warp (each round 4 nodes and up to 32 triangles). Same
- * results in every mode. */
-int grisSetWaveRefill(GrisContext* ctx, int mode);
+/* 1: the wavefront's traversal kernels keep every lane busy (a lane whose ray is finished takes
+ * the next ray while the others of its warp still walk), and a bounce level with fewer than 8,192
+ * rays is walked one ray per warp (each round 4 nodes and up to 32 triangles); same results. */
+int grisSetWaveRefill(GrisContext* ctx, int enable);
 /* Times candidate configurations — the megakernel path tracer, the wavefront one with trace
- * grids of 8/16/32 and shading grids of 4/8/16 blocks per SM, the wavefront one with the
+ * grids of 8/16/32 and shading grids of 4/8/16 blocks per SM, and the wavefront one with the
  * refilling traversal kernels at 4/8/16 blocks per SM — over `frames` frames each on the given
  * views (those frames are rendered: reservoirs and output change), keeps the fastest in the
  * context and reports it. */
@@ -454,7 +449,7 @@ typedef struct GrisTuneResult {
     int candidates;
     double msPerFrame;            /* of the chosen configuration */
     double candidateMs[16];       /* per candidate, in the order above */
-    int refill;                   /* the chosen wavefront's traversal (grisSetWaveRefill's mode) */
+    int refill;                   /* the chosen wavefront uses the refilling traversal kernels */
 } GrisTuneResult;
 int grisBatchCreate(GrisContext* ctx, uint32_t nViews, const GrisScene* const* scenes, const uint32_t* widths,
                     const uint32_t* heights, GrisBatch** out);

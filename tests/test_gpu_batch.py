@@ -42,11 +42,9 @@ def setup():
     (G.PATH_WAVEFRONT, True, (16, 8), False), (G.PATH_WAVEFRONT, False, (16, 8), False),
     (G.PATH_WAVEFRONT, True, (8, 4), False), (G.PATH_WAVEFRONT, True, (32, 16), False),
     (G.PATH_WAVEFRONT, True, (8, 16), True), (G.PATH_WAVEFRONT, False, (2, 8), True),
-    (G.PATH_WAVEFRONT, True, (8, 16), 2), (G.PATH_WAVEFRONT, False, (2, 8), 3),
     (G.PATH_MEGAKERNEL, True, (16, 8), False), (G.PATH_MEGAKERNEL, False, (16, 8), False)],
     ids=["wavefront-graph", "wavefront-eager", "wavefront-small-grids", "wavefront-large-grids", "wavefront-refill",
-         "wavefront-refill-eager-tiny-grid", "wavefront-group", "wavefront-group4-eager-tiny-grid", "megakernel-graph",
-         "megakernel-eager"])
+         "wavefront-refill-eager-tiny-grid", "megakernel-graph", "megakernel-eager"])
 def test_batch_views_match_oracle(setup, form, graphs, wave, refill):
     ctx, hss, scenes, seqs, settings, want = setup
     ctx.set_path_form(form)

@@ -74,16 +74,16 @@ def test_c1_box_256_8_frames_full_parity():
 
 @pytest.mark.parametrize("kind", [1, 2], ids=["c2_plain", "c4_glossy"])
 def test_c2_1080p_full_parity(kind):
-    """The wavefront traversals (one lane per ray over the queue; one lane per ray with refill;
-    eight and four lanes per ray with refill, also for the reuse passes' visibility queries) each
-    against the oracle on the full frame."""
+    """Both wavefront traversals (one lane per ray over the level's queue; the resident walks that
+    refill lanes, with the one-ray-per-warp walk of sparse levels) against the oracle on the full
+    frame."""
     W, H = 1920, 1080
     hs = G.HostScene(kind, seed=1, grid=512, spheres=2000)
     assert hs.triangle_count() > 1_100_000
     cams, prevs = G.sequence_cameras(hs, 3, W, H, seed=1, orbit_frames=60)
     st = G.Settings.make(maxDepth=8, spatialRadius=20.0, cap=20)
     want, oc = run_oracle(hs, cams, prevs, st, W, H)
-    for refill in (0, 1, 2, 3):
+    for refill in (0, 1):
         got, gc = run_gpu(hs, cams, prevs, st, W, H, refill=refill)
         assert_same(got, want, 3, ("resv", "temp", "out"))
         assert gc[:3] == oc[:3], refill

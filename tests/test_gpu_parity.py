@@ -58,11 +58,8 @@ def gpu_sequence(ctx, hs, cams, prevs, st, W, H, mode=(G.PATH_WAVEFRONT, G.LAUNC
 
 
 MODES = [(G.PATH_WAVEFRONT, G.LAUNCH_GRID), (G.PATH_MEGAKERNEL, G.LAUNCH_GRID), (G.PATH_MEGAKERNEL, G.LAUNCH_PERSISTENT),
-         (G.PATH_WAVEFRONT, G.LAUNCH_GRID, 1),   # refilling wavefront: sparse levels walked one ray per warp
-         (G.PATH_WAVEFRONT, G.LAUNCH_GRID, 2),   # eight lanes per ray (here the reuse passes' visibility queries)
-         (G.PATH_WAVEFRONT, G.LAUNCH_GRID, 3)]   # four lanes per ray
-MODE_IDS = ["wavefront", "megakernel-grid", "megakernel-persistent", "wavefront-refill", "wavefront-group",
-            "wavefront-group4"]
+         (G.PATH_WAVEFRONT, G.LAUNCH_GRID, 1)]   # refilling wavefront: sparse levels walked one ray per warp
+MODE_IDS = ["wavefront", "megakernel-grid", "megakernel-persistent", "wavefront-refill"]
 
 
 @pytest.mark.parametrize("mode", MODES, ids=MODE_IDS)

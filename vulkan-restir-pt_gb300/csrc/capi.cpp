@@ -360,9 +360,9 @@ int grisSetWaveLaunch(GrisContext* ctx, int traceBlocksPerSM, int shadeBlocksPer
     return GRIS_OK;
 }
 
-int grisSetWaveRefill(GrisContext* ctx, int mode) {
-    if (!ctx || mode < 0 || mode > 3) return GRIS_ERR_INVALID_ARGUMENT;
-    ctx->waveLaunch.refill = mode;
+int grisSetWaveRefill(GrisContext* ctx, int enable) {
+    if (!ctx) return GRIS_ERR_INVALID_ARGUMENT;
+    ctx->waveLaunch.refill = enable != 0;
     return GRIS_OK;
 }
 
@@ -451,7 +451,6 @@ int grisSceneCreate(GrisContext* ctx, const GrisSceneDesc* d, GrisScene** out) {
     UP(d->lightTable, d->lightTableCount, &s->view.table);
     UP(s->bvh.nodes.data(), (uint64_t)s->bvh.nodes.size(), &s->view.nodes);
     UP(s->bvh.tris.data(), (uint64_t)s->bvh.tris.size(), &s->view.tris);
-    s->view.bvhDepth = s->bvh.maxDepth;
 #undef UP
     if (rc == GRIS_OK) {
         cudaError_t e = cudaStreamSynchronize(ctx->stream);

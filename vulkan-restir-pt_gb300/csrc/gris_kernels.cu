@@ -2081,269 +2081,6 @@ __global__ void __launch_bounds__(128, kWalkMinBlocks) k_wave_trace_refill(WaveC
     flush_counts(C.counters, rc, err, 1, C.countWork, ANY ? 1 : 0);
 }
 
-/* ------------------------------------------------------- several lanes per ray (4 or 8) */
-/* The walk of full queues with a group of GW lanes per ray (GW = 8: four rays per warp; GW = 4:
- * eight). Each round a group either tests up to eight of the triangles its last node hit (8 / GW
- * per lane, tmax = the best t so far, the best reduced over the group) or visits the node on top
- * of its stack — lane l tests child slots l, l + GW, ... with the walker's box test, the hit inner
- * children are pushed nearest on top and the hit leaves' triangles listed. The node's 80 bytes are
- * read by the group's lanes at the same addresses (one transaction per 16 bytes for the group),
- * the box tests run side by side, and a warp's rays take new rays from a pool the warp refills by
- * one atomic. The closest hit is the lexicographic minimum of (t, instanceIdx, triangleIdx) over
- * the accepted triangles whatever the visiting order, and an any-hit query asks only whether one
- * exists, so the results are the per-lane walk's, bit for bit (the node and triangle counts depend
- * on the order). */
-constexpr uint32_t kGroupStack = 192;   /* node indices per group: 7 per level of a tree up to 27 deep */
-constexpr uint32_t kGroupTris = 24;     /* a node's leaf triangles: 8 slots x 3 */
-constexpr uint32_t kGroupMaxDepth = (kGroupStack - 1u) / 7u;
-
-struct GroupRay {
-    float ox, oy, oz, dx, dy, dz, idx, idy, idz, tmin;
-    uint32_t oct;
-    float t, u, v;
-    uint32_t inst, tri;
-    bool found, active;
-    uint32_t sp, triLeft, triPos;
-    uint32_t id;
-};
-
-GD void group_ray_init(GroupRay& r, float ox, float oy, float oz, float dx, float dy, float dz, float tmin, float tmax,
-                       uint32_t* stack, uint32_t gl) {
-    const float tiny = 1e-30f;
-    r.ox = ox; r.oy = oy; r.oz = oz; r.dx = dx; r.dy = dy; r.dz = dz; r.tmin = tmin;
-    r.idx = 1.0f / ((dx > tiny || dx < -tiny) ? dx : (dx < 0.0f ? -tiny : tiny));
-    r.idy = 1.0f / ((dy > tiny || dy < -tiny) ? dy : (dy < 0.0f ? -tiny : tiny));
-    r.idz = 1.0f / ((dz > tiny || dz < -tiny) ? dz : (dz < 0.0f ? -tiny : tiny));
-    r.oct = (dx < 0.0f ? 1u : 0u) | (dy < 0.0f ? 2u : 0u) | (dz < 0.0f ? 4u : 0u);
-    r.t = tmax; r.u = 0.0f; r.v = 0.0f; r.inst = kInvalidHit; r.tri = kInvalidHit; r.found = false;
-    /* a ray with a NaN coordinate hits nothing (as GrisTraversal::init): no walk */
-    const bool nan = ox != ox || oy != oy || oz != oz || dx != dx || dy != dy || dz != dz;
-    r.sp = nan ? 0u : 1u;
-    if (!nan && gl == 0u) stack[0] = 0u;
-    r.triLeft = 0u; r.triPos = 0u;
-    r.active = true;
-}
-
-/* (t, inst, tri) lexicographically below the held best, or the held best empty */
-GD bool group_better(bool okB, float tB, uint32_t iB, uint32_t rB, bool okA, float tA, uint32_t iA, uint32_t rA) {
-    return okB && (!okA || tB < tA || (tB == tA && (iB < iA || (iB == iA && rB < rA))));
-}
-
-/* One round of every group of the warp (all 32 lanes call it; the lanes of a group hold the same
- * ray state). Returns true in the lanes of a group whose walk ended this round. */
-template <bool ANY, int GW>
-GD bool group_round(GroupRay& r, const uint32_t* __restrict__ nodes, const float* __restrict__ tris, uint32_t* stack,
-                    uint32_t* triList, uint32_t gl, uint32_t groupShift, RayCount& rc, int& err) {
-    constexpr uint32_t kPer = 8u / GW;                    /* child slots and batch triangles per lane */
-    constexpr uint32_t kMask = (1u << GW) - 1u;
-    const bool doTri = r.active && r.triLeft > 0u;
-    const bool doNode = r.active && !doTri && r.sp > 0u;
-    bool ended = r.active && !doTri && r.sp == 0u;
-    /* ---- up to eight pending triangles */
-    bool ok = false;
-    float t = 0.0f, u = 0.0f, v = 0.0f;
-    uint32_t inst = kInvalidHit, tri = kInvalidHit;
-    if (doTri) {
-#pragma unroll
-        for (uint32_t j = 0; j < kPer; j++) {
-            const uint32_t k = gl + GW * j;
-            if (k < r.triLeft) {
-                const float4* T4 =
-                    reinterpret_cast<const float4*>(tris + (uint64_t)triList[r.triPos + k] * GRIS_TRI_FLOATS);
-                const float4 t0 = __ldg(T4 + 0), t1 = __ldg(T4 + 1), t2 = __ldg(T4 + 2);
-                const float TT[12] = {t0.x, t0.y, t0.z, t0.w, t1.x, t1.y, t1.z, t1.w, t2.x, t2.y, t2.z, t2.w};
-                const uint32_t ik = gris_f2u(TT[3]), rk = gris_f2u(TT[7]);
-                rc.work.tris++;
-                float tk, uk, vk;
-                const bool okk = gris_tri_test(TT, r.ox, r.oy, r.oz, r.dx, r.dy, r.dz, r.tmin, r.t, &tk, &uk, &vk);
-                if (group_better(okk, tk, ik, rk, ok, t, inst, tri)) { ok = true; t = tk; u = uk; v = vk; inst = ik; tri = rk; }
-            }
-        }
-    }
-    if constexpr (ANY) {
-        const unsigned b = __ballot_sync(0xffffffffu, ok);
-        if (doTri && ((b >> groupShift) & kMask)) { r.found = true; ended = true; }
-    } else {
-#pragma unroll
-        for (uint32_t off = GW / 2; off > 0u; off >>= 1) {   /* the group's best accepted triangle, in all its lanes */
-            const bool ok2 = __shfl_xor_sync(0xffffffffu, ok, off);
-            const float t2_ = __shfl_xor_sync(0xffffffffu, t, off), u2 = __shfl_xor_sync(0xffffffffu, u, off),
-                        v2 = __shfl_xor_sync(0xffffffffu, v, off);
-            const uint32_t i2 = __shfl_xor_sync(0xffffffffu, inst, off), r2 = __shfl_xor_sync(0xffffffffu, tri, off);
-            if (group_better(ok2, t2_, i2, r2, ok, t, inst, tri)) { ok = true; t = t2_; u = u2; v = v2; inst = i2; tri = r2; }
-        }
-        if (doTri && ok) {
-            const bool keyLess = inst < r.inst || (inst == r.inst && tri < r.tri);
-            if (t < r.t || (t == r.t && keyLess)) { r.found = true; r.t = t; r.u = u; r.v = v; r.inst = inst; r.tri = tri; }
-        }
-    }
-    if (doTri) { r.triPos += 8u; r.triLeft = r.triLeft > 8u ? r.triLeft - 8u : 0u; }
-    /* ---- the node on top of the stack: lane l tests child slots l + GW j */
-    bool inner[kPer];
-    uint32_t child[kPer], triCnt[kPer], triFirst[kPer];
-#pragma unroll
-    for (uint32_t j = 0; j < kPer; j++) { inner[j] = false; child[j] = 0u; triCnt[j] = 0u; triFirst[j] = 0u; }
-    if (doNode) {
-        const uint4* N = reinterpret_cast<const uint4*>(nodes + (uint64_t)stack[r.sp - 1u] * GRIS_NODE_WORDS);
-        const uint4 w0 = __ldg(N + 0), w1 = __ldg(N + 1), w2 = __ldg(N + 2), w3 = __ldg(N + 3), w4 = __ldg(N + 4);
-        const uint32_t W[20] = {w0.x, w0.y, w0.z, w0.w, w1.x, w1.y, w1.z, w1.w, w2.x, w2.y,
-                                w2.z, w2.w, w3.x, w3.y, w3.z, w3.w, w4.x, w4.y, w4.z, w4.w};
-        const uint32_t imask = W[3] >> 24;
-        GrisNodeRay nr;
-        gris_node_ray(W, r.ox, r.oy, r.oz, r.idx, r.idy, r.idz, r.oct, nr);
-#pragma unroll
-        for (uint32_t j = 0; j < kPer; j++) {
-            const uint32_t s = gl + GW * j;
-            const uint32_t meta = gris_byte((s >> 2) ? W[7] : W[6], (int)(s & 3u));   /* selects, no run-time index */
-            if (meta == 0u) continue;
-            if (gris_slot_hit(nr, (int)s, r.tmin, r.t)) {
-                if (imask & (1u << s)) { inner[j] = true; child[j] = W[4] + (uint32_t)__popc(imask & ((1u << s) - 1u)); }
-                else { triCnt[j] = (meta >> 5) & 3u; triFirst[j] = W[5] + (meta & 31u); }
-            }
-        }
-    }
-    uint32_t gin = 0u, mine = 0u;
-#pragma unroll
-    for (uint32_t j = 0; j < kPer; j++) {
-        gin |= ((__ballot_sync(0xffffffffu, inner[j]) >> groupShift) & kMask) << (GW * j);
-        mine += triCnt[j];
-    }
-    uint32_t incl = mine;
-#pragma unroll
-    for (uint32_t d = 1u; d < (uint32_t)GW; d <<= 1) {
-        const uint32_t x = __shfl_up_sync(0xffffffffu, incl, d, GW);
-        if (gl >= d) incl += x;
-    }
-    const uint32_t total = __shfl_sync(0xffffffffu, incl, GW - 1, GW);
-    if (doNode) {
-        r.sp -= 1u;
-        /* positions along the ray's octant order: the nearest child ends on top */
-        uint32_t pm = 0u;
-#pragma unroll
-        for (uint32_t q = 0; q < 8u; q++)
-            if ((gin >> q) & 1u) pm |= 1u << (q ^ r.oct);
-        const uint32_t nIn = (uint32_t)__popc(gin);
-        if (r.sp + nIn > kGroupStack) {
-            err = 1;                                      /* not reached: the host checks the tree depth */
-            ended = true;
-        } else {
-#pragma unroll
-            for (uint32_t j = 0; j < kPer; j++)
-                if (inner[j]) stack[r.sp + (uint32_t)__popc(pm >> (((gl + GW * j) ^ r.oct) + 1u))] = child[j];
-            r.sp += nIn;
-        }
-        uint32_t at = incl - mine;
-#pragma unroll
-        for (uint32_t j = 0; j < kPer; j++)
-            for (uint32_t k = 0; k < triCnt[j]; k++) triList[at++] = triFirst[j] + k;
-        r.triLeft = total;
-        r.triPos = 0u;
-        if (gl == 0u) rc.work.nodes++;
-    }
-    __syncwarp();
-    return ended;
-}
-
-/* The warp's pool of ray indices: groups whose walk ended take the next indices; when the pool
- * runs short one atomic takes 32 / GW * 2 more from the queue's cursor. Returns the index given
- * to this lane's group (or n: none). All lanes call it. */
-template <int GW>
-GD uint32_t group_take(bool idle, uint32_t gl, uint32_t gw, uint32_t lane, uint32_t n, uint32_t* cursor,
-                       uint32_t& poolBase, uint32_t& poolLeft, bool& more) {
-    constexpr uint32_t kLeaders = GW == 8 ? 0x01010101u : 0x11111111u;
-    constexpr uint32_t kFetch = 64u / GW;                 /* two rounds of the warp's groups */
-    const unsigned need = __ballot_sync(0xffffffffu, idle && gl == 0u) & kLeaders;
-    if (!need || (!more && poolLeft == 0u)) return n;
-    const uint32_t nNeed = (uint32_t)__popc(need);
-    uint32_t newBase = n, newValid = 0u;
-    if (poolLeft < nNeed && more) {
-        uint32_t b = 0u;
-        if (lane == 0u) b = atomicAdd(cursor, kFetch);
-        newBase = __shfl_sync(0xffffffffu, b, 0);
-        newValid = newBase < n ? min(kFetch, n - newBase) : 0u;
-        if (newBase + kFetch >= n) more = false;
-    }
-    const uint32_t k = (uint32_t)__popc(need & ((1u << (gw * GW)) - 1u));
-    uint32_t i = n;
-    if (idle && ((need >> (gw * GW)) & 1u)) {
-        if (k < poolLeft) i = poolBase + k;
-        else if (k - poolLeft < newValid) i = newBase + (k - poolLeft);
-    }
-    if (nNeed <= poolLeft) { poolBase += nNeed; poolLeft -= nNeed; }
-    else {
-        const uint32_t used = nNeed - poolLeft;
-        if (used < newValid) { poolBase = newBase + used; poolLeft = newValid - used; }
-        else { poolLeft = 0u; }
-    }
-    return i;
-}
-
-/* the level's closest hits (ANY = false) or shadow queries (ANY = true), GW lanes per ray */
-template <bool ANY, int GW>
-__global__ void __launch_bounds__(128) k_wave_trace_group(WaveCtx C, int level) {
-    constexpr uint32_t kGroups = 128u / GW;
-    const uint32_t n = ANY ? C.counts[256 + level] : C.counts[level];
-    if (n < kCoopMaxRays) return;                         /* k_wave_trace_coop takes a sparse level */
-    __shared__ uint32_t sStack[kGroups][kGroupStack];
-    __shared__ uint32_t sTris[kGroups][kGroupTris];
-    const uint32_t lane = threadIdx.x & 31u, gl = lane % GW, gw = lane / GW, g = threadIdx.x / GW;
-    uint32_t* stack = sStack[g];
-    uint32_t* triList = sTris[g];
-    const uint32_t* q = ANY ? C.shadowQueue : C.queue[level & 1];
-    uint32_t* cursor = C.counts + (ANY ? 1280 : 1024) + level;
-    RayCount rc = ray_count();
-    int err = 0;
-    GroupRay r;
-    r.active = false;
-    const uint32_t* nodes = nullptr;
-    const float* tris = nullptr;
-    uint32_t poolBase = 0u, poolLeft = 0u;
-    bool more = true;
-    while (true) {
-        const uint32_t i = group_take<GW>(!r.active, gl, gw, lane, n, cursor, poolBase, poolLeft, more);
-        if (i < n) {
-            const uint32_t id = q[i];
-            const int v = find_view_by_pixel(C.V, C.nViews, id);
-            nodes = C.V[v].P.sc.nodes;
-            tris = C.V[v].P.sc.tris;
-            if (ANY) {
-                const uint4* w = C.nee[id].w;
-                const uint4 a = w[0], d4 = w[4], r3 = w[3];
-                group_ray_init(r, __uint_as_float(a.x), __uint_as_float(a.y), __uint_as_float(a.z), __uint_as_float(d4.x),
-                               __uint_as_float(d4.y), __uint_as_float(d4.z), kMinRayDistance,
-                               __uint_as_float(r3.w) - kMinRayDistance, stack, gl);
-            } else {
-                const uint4* w = C.state[id].w;
-                const uint4 a = w[4], b = w[5];
-                group_ray_init(r, __uint_as_float(a.x), __uint_as_float(a.y), __uint_as_float(a.z), __uint_as_float(b.x),
-                               __uint_as_float(b.y), __uint_as_float(b.z), kMinRayDistance, kMaxRayDistance, stack, gl);
-            }
-            r.id = id;
-        }
-        __syncwarp();
-        if (__ballot_sync(0xffffffffu, r.active) == 0u) {
-            if (!more && poolLeft == 0u) break;
-            continue;
-        }
-        if (group_round<ANY, GW>(r, nodes, tris, stack, triList, gl, gw * GW, rc, err)) {
-            if (gl == 0u) {
-                if (ANY) {
-                    rc.shadow++;
-                    C.blocked[r.id] = r.found ? 1 : 0;
-                } else {
-                    rc.closest++;
-                    Isec h;
-                    if (r.found) { h.bx = r.u; h.by = r.v; h.inst = r.inst; h.tri = r.tri; }
-                    else { h.bx = 0.0f; h.by = 0.0f; h.inst = kInvalidHit; h.tri = 0u; }
-                    C.hit[r.id] = h;
-                }
-            }
-            r.active = false;
-        }
-    }
-    flush_counts(C.counters, rc, err, 1, C.countWork, ANY ? 1 : 0);
-}
-
 /* shade() of the level's paths: the end, the next level, or a shadow query */
 __global__ void __launch_bounds__(128) k_wave_shade(WaveCtx C, int level) {
     const uint32_t n = C.counts[level];
@@ -2726,54 +2463,6 @@ __global__ void __launch_bounds__(128, kWalkMinBlocks) k_reuse_visibility(const 
     flush_counts(V[0].P.counters, rc, err, KERNEL, V[0].P.countWork, KERNEL);
 }
 
-/* The pass's visibility queries walked GW lanes per query (k_wave_trace_group's walk); chosen
- * with the wavefront's group traversal (grisSetWaveRefill(ctx, 2 or 3)). */
-template <int KERNEL, int GW>
-__global__ void __launch_bounds__(128) k_reuse_visibility_group(const ViewEntry* __restrict__ V, int nViews, ReuseCtx R,
-                                                               int which) {
-    constexpr uint32_t kGroups = 128u / GW;
-    const uint32_t n = R.counts[2 * which];
-    uint32_t* cursor = R.counts + 2 * which + 1;
-    __shared__ uint32_t sStack[kGroups][kGroupStack];
-    __shared__ uint32_t sTris[kGroups][kGroupTris];
-    const uint32_t lane = threadIdx.x & 31u, gl = lane % GW, gw = lane / GW, g = threadIdx.x / GW;
-    uint32_t* stack = sStack[g];
-    uint32_t* triList = sTris[g];
-    RayCount rc = ray_count();
-    int err = 0;
-    GroupRay r;
-    r.active = false;
-    const uint32_t* nodes = nullptr;
-    const float* tris = nullptr;
-    uint32_t poolBase = 0u, poolLeft = 0u;
-    bool more = true;
-    while (true) {
-        const uint32_t i = group_take<GW>(!r.active, gl, gw, lane, n, cursor, poolBase, poolLeft, more);
-        if (i < n) {
-            const float4 a = R.q[2 * (uint64_t)i], b = R.q[2 * (uint64_t)i + 1];
-            const uint32_t slot = __float_as_uint(b.w);
-            const int v = find_view_by_pixel(V, nViews, slot % R.P);
-            nodes = V[v].P.sc.nodes;
-            tris = V[v].P.sc.tris;
-            group_ray_init(r, a.x, a.y, a.z, b.x, b.y, b.z, kMinRayDistance, a.w, stack, gl);
-            r.id = slot;
-        }
-        __syncwarp();
-        if (__ballot_sync(0xffffffffu, r.active) == 0u) {
-            if (!more && poolLeft == 0u) break;
-            continue;
-        }
-        if (group_round<true, GW>(r, nodes, tris, stack, triList, gl, gw * GW, rc, err)) {
-            if (gl == 0u) {
-                rc.shadow++;
-                if (!r.found) R.ps[r.id] |= kRsVisible;
-            }
-            r.active = false;
-        }
-    }
-    flush_counts(V[0].P.counters, rc, err, KERNEL, V[0].P.countWork, KERNEL);
-}
-
 /* ------------------------------------------------------------------ guided wavefront */
 using GuidedTracer = PathTracerT<true, true>;
 
@@ -3023,7 +2712,6 @@ BatchShape fill_view_table(const BatchView* views, int n, void* hViews, unsigned
         if ((int)bv.set.maxDepth > sh.maxDepth) sh.maxDepth = (int)bv.set.maxDepth;
         if (bv.set.misWeights) sh.pairwise = true;
         if (bv.set.spatialNeighbors > sh.maxNeighbours) sh.maxNeighbours = bv.set.spatialNeighbors;
-        if (bv.scene.bvhDepth > sh.maxBvhDepth) sh.maxBvhDepth = bv.scene.bvhDepth;
     }
     return sh;
 }
@@ -3069,8 +2757,6 @@ cudaError_t enqueue_batch(const BatchShape& sh, void* dViews, const void* hViews
             const int gridShade = sm * (wl.shadeBlocksPerSM > 0 ? wl.shadeBlocksPerSM : 8);
             const int gridTrace = sm * (wl.traceBlocksPerSM > 0 ? wl.traceBlocksPerSM : 16);
             const int gridCoop = sm * 4;   /* sparse levels: 4 blocks of 4 warps per SM, 17.9 KB shared each */
-            /* eight or four lanes per ray (refill mode 2 or 3), where every view's tree fits the group stack */
-            const int group = sh.maxBvhDepth > kGroupMaxDepth ? 0 : wl.refill == 2 ? 8 : wl.refill == 3 ? 4 : 0;
             /* timer slots 4..8: begin, extend, shade, shadow, post */
             auto mark = [&](int slot, bool begin) { if (timer) timer->mark(slot, begin, stream); };
             if (guide) {
@@ -3093,18 +2779,14 @@ cudaError_t enqueue_batch(const BatchShape& sh, void* dViews, const void* hViews
                 mark(4, false);
                 for (int level = 1; level < sh.maxDepth; level++) {
                     mark(5, true);
-                    if (group == 8) { k_wave_trace_group<false, 8><<<gridTrace, 128, 0, stream>>>(C, level); k_wave_trace_coop<false><<<gridCoop, 128, 0, stream>>>(C, level); }
-                else if (group == 4) { k_wave_trace_group<false, 4><<<gridTrace, 128, 0, stream>>>(C, level); k_wave_trace_coop<false><<<gridCoop, 128, 0, stream>>>(C, level); }
-                    else if (wl.refill) { k_wave_trace_refill<false><<<gridTrace, 128, 0, stream>>>(C, level); k_wave_trace_coop<false><<<gridCoop, 128, 0, stream>>>(C, level); }
+                    if (wl.refill) { k_wave_trace_refill<false><<<gridTrace, 128, 0, stream>>>(C, level); k_wave_trace_coop<false><<<gridCoop, 128, 0, stream>>>(C, level); }
                     else k_wave_extend<<<gridTrace, 128, 0, stream>>>(C, level);
                     mark(5, false);
                     mark(6, true);
                     k_gwave_shade<<<gridShade, 128, 0, stream>>>(C, level);
                     mark(6, false);
                     mark(7, true);
-                    if (group == 8) { k_wave_trace_group<true, 8><<<gridTrace, 128, 0, stream>>>(C, level); k_wave_trace_coop<true><<<gridCoop, 128, 0, stream>>>(C, level); }
-                else if (group == 4) { k_wave_trace_group<true, 4><<<gridTrace, 128, 0, stream>>>(C, level); k_wave_trace_coop<true><<<gridCoop, 128, 0, stream>>>(C, level); }
-                    else if (wl.refill) { k_wave_trace_refill<true><<<gridTrace, 128, 0, stream>>>(C, level); k_wave_trace_coop<true><<<gridCoop, 128, 0, stream>>>(C, level); }
+                    if (wl.refill) { k_wave_trace_refill<true><<<gridTrace, 128, 0, stream>>>(C, level); k_wave_trace_coop<true><<<gridCoop, 128, 0, stream>>>(C, level); }
                     else k_wave_shadow<<<gridTrace, 128, 0, stream>>>(C, level);
                     mark(7, false);
                     mark(9, true);
@@ -3127,18 +2809,14 @@ cudaError_t enqueue_batch(const BatchShape& sh, void* dViews, const void* hViews
             mark(4, false);
             for (int level = 1; level < sh.maxDepth; level++) {
                 mark(5, true);
-                if (group == 8) { k_wave_trace_group<false, 8><<<gridTrace, 128, 0, stream>>>(C, level); k_wave_trace_coop<false><<<gridCoop, 128, 0, stream>>>(C, level); }
-                else if (group == 4) { k_wave_trace_group<false, 4><<<gridTrace, 128, 0, stream>>>(C, level); k_wave_trace_coop<false><<<gridCoop, 128, 0, stream>>>(C, level); }
-                else if (wl.refill) { k_wave_trace_refill<false><<<gridTrace, 128, 0, stream>>>(C, level); k_wave_trace_coop<false><<<gridCoop, 128, 0, stream>>>(C, level); }
+                if (wl.refill) { k_wave_trace_refill<false><<<gridTrace, 128, 0, stream>>>(C, level); k_wave_trace_coop<false><<<gridCoop, 128, 0, stream>>>(C, level); }
                 else k_wave_extend<<<gridTrace, 128, 0, stream>>>(C, level);
                 mark(5, false);
                 mark(6, true);
                 k_wave_shade<<<gridShade, 128, 0, stream>>>(C, level);
                 mark(6, false);
                 mark(7, true);
-                if (group == 8) { k_wave_trace_group<true, 8><<<gridTrace, 128, 0, stream>>>(C, level); k_wave_trace_coop<true><<<gridCoop, 128, 0, stream>>>(C, level); }
-                else if (group == 4) { k_wave_trace_group<true, 4><<<gridTrace, 128, 0, stream>>>(C, level); k_wave_trace_coop<true><<<gridCoop, 128, 0, stream>>>(C, level); }
-                else if (wl.refill) { k_wave_trace_refill<true><<<gridTrace, 128, 0, stream>>>(C, level); k_wave_trace_coop<true><<<gridCoop, 128, 0, stream>>>(C, level); }
+                if (wl.refill) { k_wave_trace_refill<true><<<gridTrace, 128, 0, stream>>>(C, level); k_wave_trace_coop<true><<<gridCoop, 128, 0, stream>>>(C, level); }
                 else k_wave_shadow<<<gridTrace, 128, 0, stream>>>(C, level);
                 mark(7, false);
                 mark(8, true);
@@ -3169,15 +2847,12 @@ reuse:
         if (e != cudaSuccess) return e;
     }
     const int gridVis = current_sm_count() * (wl.traceBlocksPerSM > 0 ? wl.traceBlocksPerSM : 16);
-    const int visGroup = sh.maxBvhDepth > kGroupMaxDepth ? 0 : wl.refill == 2 ? 8 : wl.refill == 3 ? 4 : 0;
     if (split && (passes & 2)) {
         if (timer) timer->mark(2, true, stream);
         if (guide) k_reuse_temporal_prepare<true><<<tiles, blk, 0, stream>>>(V, n, R);
         else k_reuse_temporal_prepare<false><<<tiles, blk, 0, stream>>>(V, n, R);
         if (timer) timer->mark(GRIS_SLOT_REUSE_VIS_TEMPORAL, true, stream);
-        if (visGroup == 8) k_reuse_visibility_group<2, 8><<<gridVis, 128, 0, stream>>>(V, n, R, 0);
-        else if (visGroup == 4) k_reuse_visibility_group<2, 4><<<gridVis, 128, 0, stream>>>(V, n, R, 0);
-        else k_reuse_visibility<2><<<gridVis, 128, 0, stream>>>(V, n, R, 0);
+        k_reuse_visibility<2><<<gridVis, 128, 0, stream>>>(V, n, R, 0);
         if (timer) timer->mark(GRIS_SLOT_REUSE_VIS_TEMPORAL, false, stream);
         k_reuse_temporal_finish<<<tiles, blk, 0, stream>>>(V, n, R);
         if (timer) timer->mark(2, false, stream);
@@ -3187,9 +2862,7 @@ reuse:
         if (guide) k_reuse_spatial_prepare<true><<<tiles, blk, 0, stream>>>(V, n, R);
         else k_reuse_spatial_prepare<false><<<tiles, blk, 0, stream>>>(V, n, R);
         if (timer) timer->mark(GRIS_SLOT_REUSE_VIS_SPATIAL, true, stream);
-        if (visGroup == 8) k_reuse_visibility_group<3, 8><<<gridVis, 128, 0, stream>>>(V, n, R, 1);
-        else if (visGroup == 4) k_reuse_visibility_group<3, 4><<<gridVis, 128, 0, stream>>>(V, n, R, 1);
-        else k_reuse_visibility<3><<<gridVis, 128, 0, stream>>>(V, n, R, 1);
+        k_reuse_visibility<3><<<gridVis, 128, 0, stream>>>(V, n, R, 1);
         if (timer) timer->mark(GRIS_SLOT_REUSE_VIS_SPATIAL, false, stream);
         if (guide) k_reuse_spatial_finish<true><<<tiles, blk, 0, stream>>>(V, n, R);
         else k_reuse_spatial_finish<false><<<tiles, blk, 0, stream>>>(V, n, R);

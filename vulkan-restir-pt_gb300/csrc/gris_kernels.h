@@ -24,7 +24,6 @@ struct DeviceSceneView {
     const uint32_t* nodes;
     const float* tris;
     float boxMin[3], boxMax[3];   /* bounds of the world-space triangles */
-    uint32_t bvhDepth;            /* levels of the 8-wide BVH */
 };
 
 /* Receives a mark before (begin = true) and after each kernel launch, on the launch stream. */
@@ -111,8 +110,7 @@ size_t view_entry_bytes();
 struct WaveLaunch {
     int traceBlocksPerSM = 16;
     int shadeBlocksPerSM = 8;
-    int refill = 0;   /* 1: the resident traversal kernels (lanes take new rays while others walk);
-                         2 / 3: eight / four lanes per ray (groups take new rays while others walk) */
+    int refill = 0;   /* 1: the resident traversal kernels (lanes take new rays while others walk) */
 };
 
 struct BatchShape {
@@ -121,7 +119,6 @@ struct BatchShape {
     int maxDepth;
     bool pairwise = false;   /* some view uses the pairwise MIS weights */
     uint32_t maxNeighbours = 0;   /* largest spatialNeighbors of the views */
-    uint32_t maxBvhDepth = 0;     /* deepest BVH of the views */
 };
 
 /* Writes the view table of a frame into hViews (pinned host memory). */

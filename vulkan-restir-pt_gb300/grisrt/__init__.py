@@ -549,9 +549,8 @@ class Context:
         self.check(load().grisSetWaveLaunch(self.h, int(trace_blocks_per_sm), int(shade_blocks_per_sm)),
                    "grisSetWaveLaunch")
 
-    def set_wave_refill(self, mode):
-        """0 one lane per ray, 1 one lane per ray with refill (True), 2 / 3 eight / four lanes per ray."""
-        self.check(load().grisSetWaveRefill(self.h, int(mode)), "grisSetWaveRefill")
+    def set_wave_refill(self, enable):
+        self.check(load().grisSetWaveRefill(self.h, int(enable)), "grisSetWaveRefill")
 
     def set_work_counting(self, enable):
         self.check(load().grisSetWorkCounting(self.h, int(enable)), "grisSetWorkCounting")
