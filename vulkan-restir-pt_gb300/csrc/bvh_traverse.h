@@ -339,76 +339,71 @@ struct GrisTraversal {
         return false;
     }
 
-    /* false: the walk is over (found / best* hold the result). A step visits the node chosen by
-     * the previous step (its child boxes; the hit leaves' triangles become pending), tests up to
-     * kTris pending triangles (0: all of them), and once none is pending chooses the next node.
-     * The order of the box and triangle tests, and so every result and count, is the same for
-     * every kTris; a small kTris only spreads a node's triangles over several steps, so that the
-     * lanes of a warp whose nodes hit few triangles do not wait for the lane whose node hit many. */
-    template <int kTris = 0, bool kPrefetch = false, class Stack>
-    GRIS_HDM bool step(const uint32_t* __restrict__ nodes, const float* __restrict__ tris, bool skipInst0, int* err,
-                       Stack& stack) {
-        if (haveNode) {
-            const uint32_t* N = nodes + (uint64_t)nodeIdx * GRIS_NODE_WORDS;
+    /* Visits the node chosen last (nodeIdx): its child boxes; the hit leaves' triangles become
+     * pending (triBase / triHits) and the hit inner children the current group (the previous
+     * group, if any slots of it remain, pushed). false: the stack overflowed (*err = 1). */
+    template <bool kPrefetch = false, class Stack>
+    GRIS_HDM bool visit_node(const uint32_t* __restrict__ nodes, int* err, Stack& stack, bool prefetchOk) {
+        const uint32_t* N = nodes + (uint64_t)nodeIdx * GRIS_NODE_WORDS;
 #ifdef __CUDA_ARCH__
-            uint4 w0 = __ldg(reinterpret_cast<const uint4*>(N) + 0);
-            uint4 w1 = __ldg(reinterpret_cast<const uint4*>(N) + 1);
-            uint4 w2 = __ldg(reinterpret_cast<const uint4*>(N) + 2);
-            uint4 w3 = __ldg(reinterpret_cast<const uint4*>(N) + 3);
-            uint4 w4 = __ldg(reinterpret_cast<const uint4*>(N) + 4);
-            uint32_t W[20] = {w0.x, w0.y, w0.z, w0.w, w1.x, w1.y, w1.z, w1.w, w2.x, w2.y,
-                              w2.z, w2.w, w3.x, w3.y, w3.z, w3.w, w4.x, w4.y, w4.z, w4.w};
+        uint4 w0 = __ldg(reinterpret_cast<const uint4*>(N) + 0);
+        uint4 w1 = __ldg(reinterpret_cast<const uint4*>(N) + 1);
+        uint4 w2 = __ldg(reinterpret_cast<const uint4*>(N) + 2);
+        uint4 w3 = __ldg(reinterpret_cast<const uint4*>(N) + 3);
+        uint4 w4 = __ldg(reinterpret_cast<const uint4*>(N) + 4);
+        uint32_t W[20] = {w0.x, w0.y, w0.z, w0.w, w1.x, w1.y, w1.z, w1.w, w2.x, w2.y,
+                          w2.z, w2.w, w3.x, w3.y, w3.z, w3.w, w4.x, w4.y, w4.z, w4.w};
 #else
-            uint32_t W[20];
-            for (int i = 0; i < 20; i++) W[i] = N[i];
+        uint32_t W[20];
+        for (int i = 0; i < 20; i++) W[i] = N[i];
 #endif
-            visits++;
-            GrisNodeRay nr;
-            gris_node_ray(W, ox, oy, oz, idx, idy, idz, oct, nr);
-            const uint32_t imask = W[3] >> 24;
-            uint32_t innerHits = 0, leafHits = 0;
-#pragma unroll
-            for (int s = 0; s < 8; s++) {
-                uint32_t meta = gris_byte(W[6 + (s >> 2)], s & 3);
-                if (meta == 0) continue;
-                if (!gris_slot_hit(nr, s, tmin, bestT)) continue;
-                if (imask & (1u << s)) innerHits |= 1u << (s ^ oct);
-                else {
-                    uint32_t cnt = (meta >> 5) & 3u, off = meta & 31u;
-                    leafHits |= ((1u << cnt) - 1u) << off;
-                }
-            }
-            triBase = W[5];
-            triHits = leafHits;
-            if (innerHits) {
-                if (grpHits && !stack.push(grpBase, grpHits | (grpImask << 8))) { *err = 1; return false; }
-                grpBase = W[4]; grpHits = innerHits; grpImask = imask;
-            }
-            haveNode = false;
+        visits++;
+        GrisNodeRay nr;
+        gris_node_ray(W, ox, oy, oz, idx, idy, idz, oct, nr);
+        const uint32_t imask = W[3] >> 24;
+        uint32_t innerHits = 0, leafHits = 0;
 #ifdef __CUDA_ARCH__
-            if (kPrefetch && kTris > 0 && triHits) {
-                /* the node visited after this one's triangles is known already (the group's first
-                 * remaining slot, or the top group of the stack): fetch it towards L1 while the
-                 * triangles are tested */
-                uint32_t nb = grpBase, nm = grpHits | (grpImask << 8);
-                if (grpHits || stack.peek(nb, nm)) {
-                    const uint32_t sl = (uint32_t)gris_ffs(nm & 0xffu) ^ oct;
-                    const uint32_t nxt = nb + (uint32_t)gris_popc((nm >> 8) & ((1u << sl) - 1u));
-                    const char* p = reinterpret_cast<const char*>(nodes + (uint64_t)nxt * GRIS_NODE_WORDS);
-                    asm volatile("prefetch.global.L1 [%0];" :: "l"(p));
-                    asm volatile("prefetch.global.L1 [%0];" :: "l"(p + 4 * GRIS_NODE_WORDS - 1));
-                }
-            }
+#pragma unroll
 #endif
+        for (int s = 0; s < 8; s++) {
+            uint32_t meta = gris_byte(W[6 + (s >> 2)], s & 3);
+            if (meta == 0) continue;
+            if (!gris_slot_hit(nr, s, tmin, bestT)) continue;
+            if (imask & (1u << s)) innerHits |= 1u << (s ^ oct);
+            else {
+                uint32_t cnt = (meta >> 5) & 3u, off = meta & 31u;
+                leafHits |= ((1u << cnt) - 1u) << off;
+            }
         }
-        if (kTris == 0) {
-            while (triHits)
-                if (test_next_triangle(tris, skipInst0)) return false;
-        } else {
-            for (int k = 0; k < kTris && triHits; k++)
-                if (test_next_triangle(tris, skipInst0)) return false;
-            if (triHits) return true;
+        triBase = W[5];
+        triHits = leafHits;
+        if (innerHits) {
+            if (grpHits && !stack.push(grpBase, grpHits | (grpImask << 8))) { *err = 1; return false; }
+            grpBase = W[4]; grpHits = innerHits; grpImask = imask;
         }
+        haveNode = false;
+#ifdef __CUDA_ARCH__
+        if (kPrefetch && prefetchOk && triHits) {
+            /* the node visited after this one's triangles is known already (the group's first
+             * remaining slot, or the top group of the stack): fetch it towards L1 while the
+             * triangles are tested */
+            uint32_t nb = grpBase, nm = grpHits | (grpImask << 8);
+            if (grpHits || stack.peek(nb, nm)) {
+                const uint32_t sl = (uint32_t)gris_ffs(nm & 0xffu) ^ oct;
+                const uint32_t nxt = nb + (uint32_t)gris_popc((nm >> 8) & ((1u << sl) - 1u));
+                const char* p = reinterpret_cast<const char*>(nodes + (uint64_t)nxt * GRIS_NODE_WORDS);
+                asm volatile("prefetch.global.L1 [%0];" :: "l"(p));
+                asm volatile("prefetch.global.L1 [%0];" :: "l"(p + 4 * GRIS_NODE_WORDS - 1));
+            }
+        }
+#endif
+        return true;
+    }
+
+    /* Chooses the next node: the nearest remaining slot of the current group, else of the group
+     * on top of the stack. false: none is left (the walk is over). */
+    template <class Stack>
+    GRIS_HDM bool choose_next(Stack& stack) {
         if (grpHits == 0) {
             uint32_t b, m;
             if (!stack.pop(b, m)) return false;
@@ -420,6 +415,37 @@ struct GrisTraversal {
         nodeIdx = grpBase + (uint32_t)gris_popc(grpImask & ((1u << slot) - 1u));
         haveNode = true;
         return true;
+    }
+
+    /* false: the walk is over (found / best* hold the result). A step visits the node chosen by
+     * the previous step (its child boxes; the hit leaves' triangles become pending), tests up to
+     * kTris pending triangles (0: all of them), and once none is pending chooses the next node.
+     * The order of the box and triangle tests, and so every result and count, is the same for
+     * every kTris; a small kTris only spreads a node's triangles over several steps, so that the
+     * lanes of a warp whose nodes hit few triangles do not wait for the lane whose node hit many. */
+    template <int kTris = 0, bool kPrefetch = false, class Stack>
+    GRIS_HDM bool step(const uint32_t* __restrict__ nodes, const float* __restrict__ tris, bool skipInst0, int* err,
+                       Stack& stack) {
+        if (haveNode && !visit_node<kPrefetch>(nodes, err, stack, kTris > 0)) return false;
+        if (kTris == 0) {
+            while (triHits)
+                if (test_next_triangle(tris, skipInst0)) return false;
+        } else {
+            for (int k = 0; k < kTris && triHits; k++)
+                if (test_next_triangle(tris, skipInst0)) return false;
+            if (triHits) return true;
+        }
+        return choose_next(stack);
+    }
+
+    /* The node half of a phased walk, for a walk with no triangle pending: chooses the next node
+     * if none is chosen and visits it. false: the walk is over. Alternated with
+     * test_next_triangle() while triangles are pending, the walk makes the same box and triangle
+     * tests in the same order as step(). */
+    template <class Stack>
+    GRIS_HDM bool advance(const uint32_t* __restrict__ nodes, int* err, Stack& stack) {
+        if (!haveNode && !choose_next(stack)) return false;
+        return visit_node<false>(nodes, err, stack, false);
     }
 
     GRIS_HDM void result(GrisRayHit* hit, GrisWork* work) const {
