@@ -438,16 +438,6 @@ struct GrisTraversal {
         return choose_next(stack);
     }
 
-    /* The node half of a phased walk, for a walk with no triangle pending: chooses the next node
-     * if none is chosen and visits it. false: the walk is over. Alternated with
-     * test_next_triangle() while triangles are pending, the walk makes the same box and triangle
-     * tests in the same order as step(). */
-    template <class Stack>
-    GRIS_HDM bool advance(const uint32_t* __restrict__ nodes, int* err, Stack& stack) {
-        if (!haveNode && !choose_next(stack)) return false;
-        return visit_node<false>(nodes, err, stack, false);
-    }
-
     GRIS_HDM void result(GrisRayHit* hit, GrisWork* work) const {
         if (work) { work->nodes += visits; work->tris += tests; }
         if (found) { hit->t = bestT; hit->u = bestU; hit->v = bestV; hit->inst = bestInst; hit->tri = bestTri; }

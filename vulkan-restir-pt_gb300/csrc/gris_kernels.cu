@@ -1852,30 +1852,7 @@ constexpr int kWalkTrisClosest = GRIS_WALK_TRIS_CLOSEST, kWalkTrisAny = GRIS_WAL
 #define GRIS_WALK_PREFETCH 0
 #endif
 constexpr bool kWalkPrefetch = GRIS_WALK_PREFETCH != 0;
-/* Phased walks (resident kernels): each round a warp either visits nodes (the lanes with no
- * triangle pending) or tests one pending triangle per lane (the lanes with some), the latter when
- * at least GRIS_WALK_PHASED / 32 of its walking lanes have triangles pending; 0: step() rounds
- * (a node and its triangles per round). The tests of each walk and their order are step()'s. */
-#ifndef GRIS_WALK_PHASED
-#define GRIS_WALK_PHASED 0
-#endif
-constexpr uint32_t kWalkPhased = GRIS_WALK_PHASED;
 
-/* One round of a resident walk; true in the lanes whose walk ended this round. All lanes call
- * it (the phased form takes warp votes). */
-template <bool ANY, int kTris, class Stack>
-GD bool walk_round(GrisTraversal<ANY>& tr, bool active, const uint32_t* __restrict__ nodes,
-                   const float* __restrict__ tris, int& err, Stack& stack) {
-    if constexpr (kWalkPhased > 0u) {
-        const bool pending = active && tr.triHits != 0u;
-        const uint32_t nt = (uint32_t)__popc(__ballot_sync(0xffffffffu, pending));
-        const uint32_t na = (uint32_t)__popc(__ballot_sync(0xffffffffu, active));
-        if (nt * 32u >= na * kWalkPhased) return pending && tr.test_next_triangle(tris, false);
-        return active && !pending && !tr.advance(nodes, &err, stack);
-    } else {
-        return active && !tr.template step<kTris, kWalkPrefetch>(nodes, tris, false, &err, stack);
-    }
-}
 constexpr uint32_t kCoopMaxRays = 8192;
 constexpr uint32_t kCoopStack = 1024;      /* node indices per warp (pushes are at most 32 per round) */
 constexpr uint32_t kCoopTris = 96;         /* triangles per round: 4 nodes x 8 slots x 3 */
@@ -2086,7 +2063,7 @@ __global__ void __launch_bounds__(128, kWalkMinBlocks) k_wave_trace_refill(WaveC
             if (!more) break;
             continue;
         }
-        if (walk_round<ANY, (ANY ? kWalkTrisAny : kWalkTrisClosest)>(tr, active, nodes, tris, err, stack)) {
+        if (active && !tr.template step<(ANY ? kWalkTrisAny : kWalkTrisClosest), kWalkPrefetch>(nodes, tris, false, &err, stack)) {
             GrisRayHit h;
             tr.result(&h, &rc.work);
             if (ANY) {
@@ -2476,7 +2453,7 @@ __global__ void __launch_bounds__(128, kWalkMinBlocks) k_reuse_visibility(const 
             if (!more) break;
             continue;
         }
-        if (walk_round<true, kWalkTrisAny>(tr, active, nodes, tris, err, stack)) {
+        if (active && !tr.template step<kWalkTrisAny, kWalkPrefetch>(nodes, tris, false, &err, stack)) {
             GrisRayHit h;
             tr.result(&h, &rc.work);
             rc.shadow++;
