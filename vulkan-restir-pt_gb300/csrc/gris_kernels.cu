@@ -1852,6 +1852,11 @@ constexpr int kWalkTrisClosest = GRIS_WALK_TRIS_CLOSEST, kWalkTrisAny = GRIS_WAL
 #define GRIS_WALK_PREFETCH 0
 #endif
 constexpr bool kWalkPrefetch = GRIS_WALK_PREFETCH != 0;
+/* idle lanes of a warp at which the resident walks take new rays (one atomic per refill) */
+#ifndef GRIS_WALK_REFILL_IDLE
+#define GRIS_WALK_REFILL_IDLE 8
+#endif
+constexpr int kWalkRefillIdle = GRIS_WALK_REFILL_IDLE;
 
 constexpr uint32_t kCoopMaxRays = 8192;
 constexpr uint32_t kCoopStack = 1024;      /* node indices per warp (pushes are at most 32 per round) */
@@ -2030,7 +2035,7 @@ __global__ void __launch_bounds__(128, kWalkMinBlocks) k_wave_trace_refill(WaveC
     bool active = false, more = true;
     while (true) {
         unsigned idle = __ballot_sync(0xffffffffu, !active);
-        if (more && __popc(idle) >= 8) {
+        if (more && __popc(idle) >= kWalkRefillIdle) {
             uint32_t take = (uint32_t)__popc(idle), leader = __ffs(idle) - 1, base = 0;
             if (lane == leader) base = atomicAdd(cursor, take);
             base = __shfl_sync(0xffffffffu, base, leader);
@@ -2429,7 +2434,7 @@ __global__ void __launch_bounds__(128, kWalkMinBlocks) k_reuse_visibility(const 
     bool active = false, more = n > 0u;
     while (true) {
         unsigned idle = __ballot_sync(0xffffffffu, !active);
-        if (more && __popc(idle) >= 8) {
+        if (more && __popc(idle) >= kWalkRefillIdle) {
             const uint32_t take = (uint32_t)__popc(idle), leader = __ffs(idle) - 1;
             uint32_t base = 0;
             if (lane == leader) base = atomicAdd(cursor, take);
