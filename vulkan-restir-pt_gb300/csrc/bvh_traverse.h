@@ -138,6 +138,40 @@ GRIS_HD float gris_qf(uint32_t w, int i) {
 #endif
 }
 
+/* Three-operand max / min (one instruction on the device; the same value as the nested pair,
+ * NaN operands ignored alike). */
+GRIS_HD float gris_fmax3(float a, float b, float c) {
+#ifdef __CUDA_ARCH__
+    float r;
+    asm("max.f32 %0, %1, %2, %3;" : "=f"(r) : "f"(a), "f"(b), "f"(c));
+    return r;
+#else
+    return gris_fmax(gris_fmax(a, b), c);
+#endif
+}
+GRIS_HD float gris_fmin3(float a, float b, float c) {
+#ifdef __CUDA_ARCH__
+    float r;
+    asm("min.f32 %0, %1, %2, %3;" : "=f"(r) : "f"(a), "f"(b), "f"(c));
+    return r;
+#else
+    return gris_fmin(gris_fmin(a, b), c);
+#endif
+}
+
+/* The near and far planes' bytes as floats: by byte permute (gris_qf) or by conversion, chosen per
+ * plane kind (GRIS_BOX_CONVERT: bit 0 near planes, bit 1 far planes converted), to balance the
+ * integer and conversion pipes. Both are exact. */
+#ifndef GRIS_BOX_CONVERT
+#define GRIS_BOX_CONVERT 0
+#endif
+GRIS_HD float gris_qf_near(uint32_t w, int i) {
+    return (GRIS_BOX_CONVERT & 1) ? (float)gris_byte(w, i) : gris_qf(w, i);
+}
+GRIS_HD float gris_qf_far(uint32_t w, int i) {
+    return (GRIS_BOX_CONVERT & 2) ? (float)gris_byte(w, i) : gris_qf(w, i);
+}
+
 /* A node's planes for one ray: the origin terms b = (p - o) / d, the scales a = scale / d and
  * the words of the near and far quantised planes per axis ([axis][word]). */
 struct GrisNodeRay {
@@ -175,14 +209,14 @@ GRIS_HD void gris_node_ray(const uint32_t* W, float ox, float oy, float oz, floa
 GRIS_HD bool gris_slot_hit(const GrisNodeRay& nr, int s, float tmin, float tmax) {
     const bool w = (s >> 2) != 0;
     const int b = s & 3;
-    const float nx = gris_fma(gris_qf(w ? nr.nw[0][1] : nr.nw[0][0], b), nr.ax, nr.bx);
-    const float ny = gris_fma(gris_qf(w ? nr.nw[1][1] : nr.nw[1][0], b), nr.ay, nr.by);
-    const float nz = gris_fma(gris_qf(w ? nr.nw[2][1] : nr.nw[2][0], b), nr.az, nr.bz);
-    const float fx = gris_fma(gris_qf(w ? nr.fw[0][1] : nr.fw[0][0], b), nr.ax, nr.bx);
-    const float fy = gris_fma(gris_qf(w ? nr.fw[1][1] : nr.fw[1][0], b), nr.ay, nr.by);
-    const float fz = gris_fma(gris_qf(w ? nr.fw[2][1] : nr.fw[2][0], b), nr.az, nr.bz);
-    const float tn = gris_fmax(gris_fmax(nx, ny), gris_fmax(nz, tmin));
-    const float tf = gris_fmin(gris_fmin(fx, fy), gris_fmin(fz, tmax));
+    const float nx = gris_fma(gris_qf_near(w ? nr.nw[0][1] : nr.nw[0][0], b), nr.ax, nr.bx);
+    const float ny = gris_fma(gris_qf_near(w ? nr.nw[1][1] : nr.nw[1][0], b), nr.ay, nr.by);
+    const float nz = gris_fma(gris_qf_near(w ? nr.nw[2][1] : nr.nw[2][0], b), nr.az, nr.bz);
+    const float fx = gris_fma(gris_qf_far(w ? nr.fw[0][1] : nr.fw[0][0], b), nr.ax, nr.bx);
+    const float fy = gris_fma(gris_qf_far(w ? nr.fw[1][1] : nr.fw[1][0], b), nr.ay, nr.by);
+    const float fz = gris_fma(gris_qf_far(w ? nr.fw[2][1] : nr.fw[2][0], b), nr.az, nr.bz);
+    const float tn = gris_fmax3(gris_fmax(nx, ny), nz, tmin);
+    const float tf = gris_fmin3(gris_fmin(fx, fy), fz, tmax);
     return tn <= tf;
 }
 
