@@ -163,7 +163,7 @@ GRIS_HD float gris_fmin3(float a, float b, float c) {
  * plane kind (GRIS_BOX_CONVERT: bit 0 near planes, bit 1 far planes converted), to balance the
  * integer and conversion pipes. Both are exact. */
 #ifndef GRIS_BOX_CONVERT
-#define GRIS_BOX_CONVERT 0
+#define GRIS_BOX_CONVERT 2
 #endif
 GRIS_HD float gris_qf_near(uint32_t w, int i) {
     return (GRIS_BOX_CONVERT & 1) ? (float)gris_byte(w, i) : gris_qf(w, i);

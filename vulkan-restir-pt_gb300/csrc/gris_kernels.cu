@@ -2088,7 +2088,11 @@ __global__ void __launch_bounds__(128, kWalkMinBlocks) k_wave_trace_refill(WaveC
 }
 
 /* shade() of the level's paths: the end, the next level, or a shadow query */
-__global__ void __launch_bounds__(128) k_wave_shade(WaveCtx C, int level) {
+/* resident blocks of 128 threads per SM asked of the compiler for the shading kernels (0: none) */
+#ifndef GRIS_WAVE_SHADE_MIN_BLOCKS
+#define GRIS_WAVE_SHADE_MIN_BLOCKS 0
+#endif
+__global__ void __launch_bounds__(128, GRIS_WAVE_SHADE_MIN_BLOCKS) k_wave_shade(WaveCtx C, int level) {
     const uint32_t n = C.counts[level];
     const uint32_t* q = C.queue[level & 1];
     for (uint32_t i0 = blockIdx.x * blockDim.x; i0 < n; i0 += gridDim.x * blockDim.x) {
@@ -2139,7 +2143,7 @@ __global__ void __launch_bounds__(128) k_wave_shadow(WaveCtx C, int level) {
 }
 
 /* post() of the paths that made a shadow query */
-__global__ void __launch_bounds__(128) k_wave_post(WaveCtx C, int level) {
+__global__ void __launch_bounds__(128, GRIS_WAVE_SHADE_MIN_BLOCKS) k_wave_post(WaveCtx C, int level) {
     const uint32_t n = C.counts[256 + level];
     for (uint32_t i0 = blockIdx.x * blockDim.x; i0 < n; i0 += gridDim.x * blockDim.x) {
         uint32_t i = i0 + threadIdx.x;
