@@ -130,8 +130,12 @@ int grisBatchCreate(GrisContext* ctx, uint32_t n, const GrisScene* const* scenes
     alloc((void**)&b->wave.queue[0], P * 4, false);
     alloc((void**)&b->wave.queue[1], P * 4, false);
     alloc((void**)&b->wave.shadowQueue, P * 4, false);
+    alloc(&b->wave.ray, P * 32, false);
     alloc((void**)&b->wave.counts, 1536 * 4, true);
     b->wave.capacity = P;
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&b->wave.aux, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&b->wave.evFork, cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&b->wave.evJoin, cudaEventDisableTiming);
     alloc(&b->dViews, view_entry_bytes() * n, false);
     for (int i = 0; i < 2 && e == cudaSuccess; i++) {
         e = cudaMallocHost(&b->hViews[i], view_entry_bytes() * n);
@@ -154,6 +158,9 @@ int grisBatchDestroy(GrisBatch* b) {
     drop_graphs(b);
     if (b->guideBlock) cudaFree(b->guideBlock);
     if (b->wave.reuse.block) cudaFree(b->wave.reuse.block);
+    if (b->wave.aux) { cudaStreamSynchronize(b->wave.aux); cudaStreamDestroy(b->wave.aux); }
+    if (b->wave.evFork) cudaEventDestroy(b->wave.evFork);
+    if (b->wave.evJoin) cudaEventDestroy(b->wave.evJoin);
     for (void* p : b->allocations) cudaFree(p);
     for (int i = 0; i < 2; i++) {
         if (b->hViews[i]) cudaFreeHost(b->hViews[i]);

@@ -261,6 +261,24 @@ struct PathTracerT {
         return post(P, false) ? kNext : kEnd;
     }
 
+    /* The ray post() continues the path with, computed ahead of it from the state shade() leaves
+     * (unguided paths): Russian roulette and the BSDF sample draw the same numbers in post() and
+     * read nothing the shadow query's answer changes (throughput, the material, the surface, wo),
+     * so the next bounce's closest hit can be traced while the shadow query is. false: post()
+     * will end the path. */
+    GD bool next_ray(const PassCtx& P, V3& o, V3& d) const {
+        uint32_t r = rng;
+        if (bounce > 4) {
+            float pdfTerminate = fmaxf(1.0f - luminance(throughput) * P.set.rrScale, 0.0f);
+            if (sample1f(r) < pdfTerminate) return false;
+        }
+        BsdfSample s2;
+        if (!sampleBSDF(mat, surf.albedo, surf.norm, wo, sample3f(r), s2) || s2.pdf < 1e-6f) return false;
+        d = s2.wi;
+        o = surf.pos + d * 1e-4f;
+        return true;
+    }
+
     /* second part: the NEE contribution (when shade() sampled a light), Russian roulette, BSDF
      * sampling; true = the path continues */
     GD bool post(const PassCtx& P, bool shadowed, const guide::Lobes* L = nullptr, float mix = 0.0f) {
@@ -1668,12 +1686,13 @@ GD void load_wave(const WaveRec* __restrict__ src, T& t) {
     t.s.wi = v3s(0.0f); t.s.bsdf = v3s(0.0f);
     t.surf.isLight = false;
 }
+/* extra: bit 2 = the path's next ray is queued already (set by shade(), checked by post()) */
 template <class T>
-GD void save_nee(NeeRec* __restrict__ dst, const T& t) {
+GD void save_nee(NeeRec* __restrict__ dst, const T& t, uint32_t extra = 0u) {
     dst->w[0] = make_uint4(__float_as_uint(t.surf.pos.x), __float_as_uint(t.surf.pos.y), __float_as_uint(t.surf.pos.z),
                            __float_as_uint(t.resvRandSample));
     dst->w[1] = make_uint4(__float_as_uint(t.surf.norm.x), __float_as_uint(t.surf.norm.y), __float_as_uint(t.surf.norm.z),
-                           (t.isThisVertexConnectible ? 1u : 0u) | (t.nee ? 2u : 0u));
+                           (t.isThisVertexConnectible ? 1u : 0u) | (t.nee ? 2u : 0u) | extra);
     dst->w[2] = make_uint4(__float_as_uint(t.surf.albedo.x), __float_as_uint(t.surf.albedo.y), __float_as_uint(t.surf.albedo.z), t.lightId);
     dst->w[3] = u4f(t.lightRadiance.x, t.lightRadiance.y, t.lightRadiance.z, t.lightDist);
     dst->w[4] = u4f(t.lightDir.x, t.lightDir.y, t.lightDir.z, t.lightPdf);
@@ -1703,6 +1722,7 @@ struct WaveCtx {
     unsigned char* blocked;
     uint32_t* queue[2];
     uint32_t* shadowQueue;
+    uint4* ray;         /* per path: the next closest-hit ray, origin.xyz | dir.xyz (2 x uint4) */
     uint32_t* counts;   /* [level] paths, [256 + level] shadow queries, [512 + level] post() calls and
                            [768 + level] guided vertices of the level (guided batches) */
     unsigned long long* counters;
@@ -1763,20 +1783,32 @@ GD void guide_finish_record(const WaveCtx& C, const T& t, uint32_t id) {
     }
 }
 
-/* After a bounce's post(): the next level or the end of the path. */
+GD void store_ray(const WaveCtx& C, uint32_t id, V3 o, V3 d) {
+    C.ray[2 * (uint64_t)id] = u4f(o.x, o.y, o.z, 0.0f);
+    C.ray[2 * (uint64_t)id + 1] = u4f(d.x, d.y, d.z, 0.0f);
+}
+
+/* After a bounce's post(): the next level (the state saved; with `queue`, the path's next ray
+ * stored for the closest-hit walk and the path pushed by the caller) or the end of the path.
+ * Returns whether the path continues. */
 template <class T>
-GD void wave_continue(const WaveCtx& C, const PassCtx& P, T& t, uint32_t id, bool cont, int level, bool& push) {
+GD bool wave_continue(const WaveCtx& C, const PassCtx& P, T& t, uint32_t id, bool cont, int level, bool& push,
+                      bool queue = true) {
     push = false;
     if (cont) {
         t.bounce++;
         if (t.bounce < (int)P.set.maxDepth) {
             save_wave(C.state + id, t);
-            push = true;
-            return;
+            if (queue) {
+                store_ray(C, id, t.ray.ori, t.ray.dir);
+                push = true;
+            }
+            return true;
         }
     }
     t.end(P);
     guide_finish_record(C, t, id);
+    return false;
 }
 
 /* level 0: begin() + the primary vertex for every pixel of every view */
@@ -1806,8 +1838,7 @@ __global__ void __launch_bounds__(128) k_wave_extend(WaveCtx C, int level) {
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i - threadIdx.x < n; i += gridDim.x * blockDim.x) {
         if (i < n) {
             uint32_t id = q[i];
-            const uint4* w = C.state[id].w;
-            uint4 a = w[4], b = w[5];
+            const uint4 a = C.ray[2 * (uint64_t)id], b = C.ray[2 * (uint64_t)id + 1];
             V3 o = v3(__uint_as_float(a.x), __uint_as_float(a.y), __uint_as_float(a.z));
             V3 d = v3(__uint_as_float(b.x), __uint_as_float(b.y), __uint_as_float(b.z));
             int v = find_view_by_pixel(C.V, C.nViews, id);
@@ -1986,8 +2017,7 @@ __global__ void __launch_bounds__(128) k_wave_trace_coop(WaveCtx C, int level) {
             d[0] = __uint_as_float(d4.x); d[1] = __uint_as_float(d4.y); d[2] = __uint_as_float(d4.z);
             tmax = __uint_as_float(r3.w) - kMinRayDistance;
         } else {
-            const uint4* wv = C.state[id].w;
-            const uint4 a = wv[4], b = wv[5];
+            const uint4 a = C.ray[2 * (uint64_t)id], b = C.ray[2 * (uint64_t)id + 1];
             o[0] = __uint_as_float(a.x); o[1] = __uint_as_float(a.y); o[2] = __uint_as_float(a.z);
             d[0] = __uint_as_float(b.x); d[1] = __uint_as_float(b.y); d[2] = __uint_as_float(b.z);
             tmax = kMaxRayDistance;
@@ -2054,8 +2084,7 @@ __global__ void __launch_bounds__(128, kWalkMinBlocks) k_wave_trace_refill(WaveC
                         tr.init(__uint_as_float(a.x), __uint_as_float(a.y), __uint_as_float(a.z), __uint_as_float(d4.x),
                                 __uint_as_float(d4.y), __uint_as_float(d4.z), kMinRayDistance, dist - kMinRayDistance);
                     } else {
-                        const uint4* w = C.state[id].w;
-                        uint4 a = w[4], b = w[5];
+                        const uint4 a = C.ray[2 * (uint64_t)id], b = C.ray[2 * (uint64_t)id + 1];
                         tr.init(__uint_as_float(a.x), __uint_as_float(a.y), __uint_as_float(a.z), __uint_as_float(b.x),
                                 __uint_as_float(b.y), __uint_as_float(b.z), kMinRayDistance, kMaxRayDistance);
                     }
@@ -2110,8 +2139,13 @@ __global__ void __launch_bounds__(128, GRIS_WAVE_SHADE_MIN_BLOCKS) k_wave_shade(
             t.mat = load_material(P.sc, t.surf.matIndex);
             int r = t.shade(P, C.hit[id]);
             if (r == PathTracer::kShadow) {
+                /* the next bounce's ray now, so that its closest hit is traced while the shadow
+                 * query is; post() continues the path with the same ray and checks the queueing */
+                V3 o, d;
+                pushNext = level + 1 < (int)P.set.maxDepth && t.next_ray(P, o, d);
+                if (pushNext) store_ray(C, id, o, d);
                 save_wave(C.state + id, t);
-                save_nee(C.nee + id, t);
+                save_nee(C.nee + id, t, pushNext ? 4u : 0u);
                 pushShadow = true;
             } else {
                 wave_continue(C, P, t, id, r == PathTracer::kNext, level, pushNext);
@@ -2143,26 +2177,27 @@ __global__ void __launch_bounds__(128) k_wave_shadow(WaveCtx C, int level) {
 }
 
 /* post() of the paths that made a shadow query */
+/* post() of the level's NEE vertices. Their next rays were queued by shade() (next_ray): here
+ * the path's state moves on to the next level or the path ends; a disagreement with shade()'s
+ * queueing (not expected: both decisions read the same state and numbers) raises bit 3 of the
+ * error word. */
 __global__ void __launch_bounds__(128, GRIS_WAVE_SHADE_MIN_BLOCKS) k_wave_post(WaveCtx C, int level) {
     const uint32_t n = C.counts[256 + level];
-    for (uint32_t i0 = blockIdx.x * blockDim.x; i0 < n; i0 += gridDim.x * blockDim.x) {
-        uint32_t i = i0 + threadIdx.x;
-        bool push = false;
-        uint32_t id = 0;
-        if (i < n) {
-            id = C.shadowQueue[i];
-            int v; uint32_t x, y;
-            path_coords(C, id, v, x, y);
-            const PassCtx& P = C.V[v].P;
-            PathTracer t;
-            load_wave(C.state + id, t);
-            load_nee(C.nee + id, t);
-            t.ix = x; t.iy = y; t.bounce = level;
-            t.mat = load_material(P.sc, t.surf.matIndex);
-            bool cont = t.post(P, C.blocked[id] != 0);
-            wave_continue(C, P, t, id, cont, level, push);
-        }
-        warp_push(C.queue[(level + 1) & 1], C.counts + level + 1, push, id);
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const uint32_t id = C.shadowQueue[i];
+        int v; uint32_t x, y;
+        path_coords(C, id, v, x, y);
+        const PassCtx& P = C.V[v].P;
+        PathTracer t;
+        load_wave(C.state + id, t);
+        load_nee(C.nee + id, t);
+        const bool queued = (C.nee[id].w[1].w & 4u) != 0u;
+        t.ix = x; t.iy = y; t.bounce = level;
+        t.mat = load_material(P.sc, t.surf.matIndex);
+        bool cont = t.post(P, C.blocked[id] != 0);
+        bool unused;
+        if (wave_continue(C, P, t, id, cont, level, unused, false) != queued)
+            atomicOr(C.counters + GRIS_COUNTER_ERROR, 8ull);
     }
 }
 
@@ -2663,7 +2698,7 @@ size_t guide_wave_bytes_per_path() {
     return sizeof(uint32_t) + (9 + guide::kRaw + 18 + 9 + guide::kRaw) * sizeof(float);
 }
 
-size_t wave_bytes_per_path() { return sizeof(WaveRec) + sizeof(NeeRec) + sizeof(Isec) + 1 + 3 * sizeof(uint32_t); }
+size_t wave_bytes_per_path() { return sizeof(WaveRec) + sizeof(NeeRec) + sizeof(Isec) + 1 + 3 * sizeof(uint32_t) + 32; }
 
 static size_t reuse_up(size_t n) { return (n + 255) & ~(size_t)255; }
 size_t reuse_bytes(uint64_t pixels, uint32_t slots) {
@@ -2754,6 +2789,7 @@ cudaError_t enqueue_batch(const BatchShape& sh, void* dViews, const void* hViews
             C.blocked = wb.blocked;
             C.queue[0] = wb.queue[0]; C.queue[1] = wb.queue[1];
             C.shadowQueue = wb.shadowQueue;
+            C.ray = reinterpret_cast<uint4*>(wb.ray);
             C.counts = wb.counts;
             C.counters = counters;
             C.countWork = countWork;
@@ -2817,22 +2853,42 @@ cudaError_t enqueue_batch(const BatchShape& sh, void* dViews, const void* hViews
             mark(4, true);
             k_wave_begin<<<(pixels + 127) / 128, 128, 0, stream>>>(C);
             mark(4, false);
+            /* Level L's closest hits (queued by shade(L - 1), NEE vertices' next rays included)
+             * run beside level L - 1's shadow queries and post() on a second stream (a fork and a
+             * join in the captured graph); with a kernel timer everything runs in order on one
+             * stream. */
+            const bool fork = wb.aux != nullptr && timer == nullptr;
+            auto shadow_post = [&](int lv, cudaStream_t s) {
+                mark(7, true);
+                if (wl.refill) { k_wave_trace_refill<true><<<gridTrace, 128, 0, s>>>(C, lv); k_wave_trace_coop<true><<<gridCoop, 128, 0, s>>>(C, lv); }
+                else k_wave_shadow<<<gridTrace, 128, 0, s>>>(C, lv);
+                mark(7, false);
+                mark(8, true);
+                k_wave_post<<<gridShade, 128, 0, s>>>(C, lv);
+                mark(8, false);
+            };
             for (int level = 1; level < sh.maxDepth; level++) {
+                const bool prev = level > 1;
+                if (prev && fork) {
+                    if ((e = cudaEventRecord(wb.evFork, stream)) != cudaSuccess) return e;
+                    if ((e = cudaStreamWaitEvent(wb.aux, wb.evFork, 0)) != cudaSuccess) return e;
+                    shadow_post(level - 1, wb.aux);
+                }
                 mark(5, true);
                 if (wl.refill) { k_wave_trace_refill<false><<<gridTrace, 128, 0, stream>>>(C, level); k_wave_trace_coop<false><<<gridCoop, 128, 0, stream>>>(C, level); }
                 else k_wave_extend<<<gridTrace, 128, 0, stream>>>(C, level);
                 mark(5, false);
+                if (prev && fork) {
+                    if ((e = cudaEventRecord(wb.evJoin, wb.aux)) != cudaSuccess) return e;
+                    if ((e = cudaStreamWaitEvent(stream, wb.evJoin, 0)) != cudaSuccess) return e;
+                } else if (prev) {
+                    shadow_post(level - 1, stream);
+                }
                 mark(6, true);
                 k_wave_shade<<<gridShade, 128, 0, stream>>>(C, level);
                 mark(6, false);
-                mark(7, true);
-                if (wl.refill) { k_wave_trace_refill<true><<<gridTrace, 128, 0, stream>>>(C, level); k_wave_trace_coop<true><<<gridCoop, 128, 0, stream>>>(C, level); }
-                else k_wave_shadow<<<gridTrace, 128, 0, stream>>>(C, level);
-                mark(7, false);
-                mark(8, true);
-                k_wave_post<<<gridShade, 128, 0, stream>>>(C, level);
-                mark(8, false);
             }
+            if (sh.maxDepth > 1) shadow_post(sh.maxDepth - 1, stream);
         } else {
             k_batch_pass<PathTask, 1><<<tiles, blk, 0, stream>>>(V, n);
         }

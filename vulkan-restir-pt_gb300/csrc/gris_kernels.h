@@ -88,8 +88,12 @@ struct WaveBuffers {
     unsigned char* blocked;
     uint32_t* queue[2];
     uint32_t* shadowQueue;
+    void* ray;          /* 32 B per path: the next closest-hit ray */
     uint32_t* counts;   /* 1536 words */
     uint64_t capacity;
+    /* a second stream and two events (null: the frame's kernels run in order on one stream) */
+    cudaStream_t aux;
+    cudaEvent_t evFork, evJoin;
     /* guided batches only (null otherwise): post queue, guide inputs / outputs per guided
      * vertex, training record per path, frame state (4 words) */
     uint32_t* postQueue;
