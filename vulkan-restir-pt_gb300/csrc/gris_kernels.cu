@@ -266,22 +266,22 @@ struct PathTracerT {
      * read nothing the shadow query's answer changes (throughput, the material, the surface, wo),
      * so the next bounce's closest hit can be traced while the shadow query is. false: post()
      * will end the path. */
-    GD bool next_ray(const PassCtx& P, V3& o, BsdfSample& s2) const {
+    GD bool next_ray(const PassCtx& P, V3& o, V3& d) const {
         uint32_t r = rng;
         if (bounce > 4) {
             float pdfTerminate = fmaxf(1.0f - luminance(throughput) * P.set.rrScale, 0.0f);
             if (sample1f(r) < pdfTerminate) return false;
         }
+        BsdfSample s2;
         if (!sampleBSDF(mat, surf.albedo, surf.norm, wo, sample3f(r), s2) || s2.pdf < 1e-6f) return false;
-        o = surf.pos + s2.wi * 1e-4f;
+        d = s2.wi;
+        o = surf.pos + d * 1e-4f;
         return true;
     }
 
     /* second part: the NEE contribution (when shade() sampled a light), Russian roulette, BSDF
-     * sampling; true = the path continues. pre: the BSDF sample next_ray() drew (its random
-     * numbers are drawn again here, the sample taken from pre) */
-    GD bool post(const PassCtx& P, bool shadowed, const guide::Lobes* L = nullptr, float mix = 0.0f,
-                 const BsdfSample* pre = nullptr) {
+     * sampling; true = the path continues */
+    GD bool post(const PassCtx& P, bool shadowed, const guide::Lobes* L = nullptr, float mix = 0.0f) {
         if (nee) {
             if (!shadowed && lightPdf > 1e-6f) {
                 float bsdfPdf = absDot(surf.norm, lightDir) * kPiInv;
@@ -328,9 +328,6 @@ struct PathTracerT {
                 if (!sampleBSDF(mat, surf.albedo, surf.norm, wo, sample3f(rng), s) || s.pdf < 1e-6f) return false;
                 pdfHit = s.pdf;
             }
-        } else if (pre) {
-            (void)sample3f(rng);
-            s = *pre;
         } else {
             if (!sampleBSDF(mat, surf.albedo, surf.norm, wo, sample3f(rng), s) || s.pdf < 1e-6f) return false;
         }
@@ -1625,10 +1622,7 @@ __global__ void __launch_bounds__(128, GridMinBlocks<KERNEL>::value) k_batch_pas
 /* Path state between kernels, per path id: the loop-carried members of PathTracer (17 x 16 B)
  * and the part of a bounce carried from shade() to post() across the shadow query (6 x 16 B). */
 struct WaveRec { uint4 w[17]; };
-/* [0..5] the light sample and vertex (save_nee); [6..7] the BSDF sample shade() drew ahead for a
- * queued next ray (wi, pdf | bsdf, type), which post() reuses */
-struct NeeRec { uint4 w[8]; };
-static_assert(sizeof(WaveRec) == kWaveStateBytes && sizeof(NeeRec) == kWaveNeeBytes, "wavefront record sizes");
+struct NeeRec { uint4 w[6]; };
 
 GD uint4 u4f(float a, float b, float c, float d) {
     return make_uint4(__float_as_uint(a), __float_as_uint(b), __float_as_uint(c), __float_as_uint(d));
@@ -2147,17 +2141,11 @@ __global__ void __launch_bounds__(128, GRIS_WAVE_SHADE_MIN_BLOCKS) k_wave_shade(
             if (r == PathTracer::kShadow) {
                 /* the next bounce's ray now, so that its closest hit is traced while the shadow
                  * query is; post() continues the path with the same ray and checks the queueing */
-                V3 o;
-                BsdfSample s2;
-                pushNext = level + 1 < (int)P.set.maxDepth && t.next_ray(P, o, s2);
+                V3 o, d;
+                pushNext = level + 1 < (int)P.set.maxDepth && t.next_ray(P, o, d);
+                if (pushNext) store_ray(C, id, o, d);
                 save_wave(C.state + id, t);
                 save_nee(C.nee + id, t, pushNext ? 4u : 0u);
-                if (pushNext) {
-                    store_ray(C, id, o, s2.wi);
-                    C.nee[id].w[6] = u4f(s2.wi.x, s2.wi.y, s2.wi.z, s2.pdf);
-                    C.nee[id].w[7] = make_uint4(__float_as_uint(s2.bsdf.x), __float_as_uint(s2.bsdf.y),
-                                                __float_as_uint(s2.bsdf.z), s2.type);
-                }
                 pushShadow = true;
             } else {
                 wave_continue(C, P, t, id, r == PathTracer::kNext, level, pushNext);
@@ -2204,17 +2192,9 @@ __global__ void __launch_bounds__(128, GRIS_WAVE_SHADE_MIN_BLOCKS) k_wave_post(W
         load_wave(C.state + id, t);
         load_nee(C.nee + id, t);
         const bool queued = (C.nee[id].w[1].w & 4u) != 0u;
-        BsdfSample pre;
-        if (queued) {
-            const uint4 a = C.nee[id].w[6], b = C.nee[id].w[7];
-            pre.wi = v3(__uint_as_float(a.x), __uint_as_float(a.y), __uint_as_float(a.z));
-            pre.pdf = __uint_as_float(a.w);
-            pre.bsdf = v3(__uint_as_float(b.x), __uint_as_float(b.y), __uint_as_float(b.z));
-            pre.type = b.w;
-        }
         t.ix = x; t.iy = y; t.bounce = level;
         t.mat = load_material(P.sc, t.surf.matIndex);
-        bool cont = t.post(P, C.blocked[id] != 0, nullptr, 0.0f, queued ? &pre : nullptr);
+        bool cont = t.post(P, C.blocked[id] != 0);
         bool unused;
         if (wave_continue(C, P, t, id, cont, level, unused, false) != queued)
             atomicOr(C.counters + GRIS_COUNTER_ERROR, 8ull);

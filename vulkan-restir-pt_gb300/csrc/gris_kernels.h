@@ -81,9 +81,6 @@ size_t reuse_bytes(uint64_t pixels, uint32_t slots);
 void reuse_carve(ReuseBuffers& r, void* block, uint64_t pixels, uint32_t slots);
 
 /* Device buffers of the wavefront path tracer, for up to `capacity` paths (pixels of a batch). */
-/* bytes per path of the wavefront's path state and NEE record */
-constexpr size_t kWaveStateBytes = 272, kWaveNeeBytes = 128;
-
 struct WaveBuffers {
     void* state;
     void* nee;
