@@ -38,7 +38,9 @@ extern "C" {
 #define GRIS_ERR_OUT_OF_MEMORY (-3)
 #define GRIS_ERR_UNSUPPORTED (-4)
 #define GRIS_ERR_DEVICE_FAULT (-5)   /* a kernel raised its error word: bit 0 the traversal stack limit,
-                                        bit 1 a bounded tensor-core wait ran out */
+                                        bit 1 a bounded tensor-core wait ran out, bit 2 the drain wait
+                                        after it ran out too, bit 3 the wavefront's post() disagreed
+                                        with the next ray shade() queued ahead of it */
 #define GRIS_ERR_TOO_LARGE (-6)
 
 /* ---------------------------------------------------------------- layouts */

@@ -2119,7 +2119,7 @@ __global__ void __launch_bounds__(128, kWalkMinBlocks) k_wave_trace_refill(WaveC
 /* shade() of the level's paths: the end, the next level, or a shadow query */
 /* resident blocks of 128 threads per SM asked of the compiler for the shading kernels (0: none) */
 #ifndef GRIS_WAVE_SHADE_MIN_BLOCKS
-#define GRIS_WAVE_SHADE_MIN_BLOCKS 0
+#define GRIS_WAVE_SHADE_MIN_BLOCKS 4
 #endif
 __global__ void __launch_bounds__(128, GRIS_WAVE_SHADE_MIN_BLOCKS) k_wave_shade(WaveCtx C, int level) {
     const uint32_t n = C.counts[level];
