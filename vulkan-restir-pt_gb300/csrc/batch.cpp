@@ -133,9 +133,7 @@ int grisBatchCreate(GrisContext* ctx, uint32_t n, const GrisScene* const* scenes
     alloc(&b->wave.ray, P * 32, false);
     alloc((void**)&b->wave.counts, 1536 * 4, true);
     b->wave.capacity = P;
-    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&b->wave.aux, cudaStreamNonBlocking);
-    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&b->wave.evFork, cudaEventDisableTiming);
-    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&b->wave.evJoin, cudaEventDisableTiming);
+    if (e == cudaSuccess) e = wave_streams_create(b->wave);
     alloc(&b->dViews, view_entry_bytes() * n, false);
     for (int i = 0; i < 2 && e == cudaSuccess; i++) {
         e = cudaMallocHost(&b->hViews[i], view_entry_bytes() * n);
@@ -158,9 +156,7 @@ int grisBatchDestroy(GrisBatch* b) {
     drop_graphs(b);
     if (b->guideBlock) cudaFree(b->guideBlock);
     if (b->wave.reuse.block) cudaFree(b->wave.reuse.block);
-    if (b->wave.aux) { cudaStreamSynchronize(b->wave.aux); cudaStreamDestroy(b->wave.aux); }
-    if (b->wave.evFork) cudaEventDestroy(b->wave.evFork);
-    if (b->wave.evJoin) cudaEventDestroy(b->wave.evJoin);
+    wave_streams_destroy(b->wave);
     for (void* p : b->allocations) cudaFree(p);
     for (int i = 0; i < 2; i++) {
         if (b->hViews[i]) cudaFreeHost(b->hViews[i]);

@@ -93,9 +93,7 @@ struct WaveScratch {
         for (void* p : allocations) cudaFree(p);
         allocations.clear();
         if (wb.reuse.block) cudaFree(wb.reuse.block);
-        if (wb.aux) { cudaStreamSynchronize(wb.aux); cudaStreamDestroy(wb.aux); }
-        if (wb.evFork) cudaEventDestroy(wb.evFork);
-        if (wb.evJoin) cudaEventDestroy(wb.evJoin);
+        grisrt::wave_streams_destroy(wb);
         for (int i = 0; i < 2; i++) {
             if (hViews[i]) cudaFreeHost(hViews[i]);
             if (staged[i]) cudaEventDestroy(staged[i]);
@@ -616,9 +614,7 @@ int grisPassRender(GrisContext* ctx, const GrisScene* s, const GrisPassBindings*
             alloc((void**)&w.wb.shadowQueue, P * 4);
             alloc(&w.wb.ray, P * 32);
             alloc((void**)&w.wb.counts, 1536 * 4);
-            if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&w.wb.aux, cudaStreamNonBlocking);
-            if (e == cudaSuccess) e = cudaEventCreateWithFlags(&w.wb.evFork, cudaEventDisableTiming);
-            if (e == cudaSuccess) e = cudaEventCreateWithFlags(&w.wb.evJoin, cudaEventDisableTiming);
+            if (e == cudaSuccess) e = grisrt::wave_streams_create(w.wb);
             alloc(&w.dViews, grisrt::view_entry_bytes());
             for (int i = 0; i < 2 && e == cudaSuccess; i++) {
                 e = cudaMallocHost(&w.hViews[i], grisrt::view_entry_bytes());

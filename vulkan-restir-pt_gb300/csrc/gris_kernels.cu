@@ -755,8 +755,14 @@ struct TemporalTaskT {
     Isec prevIsec;
     Ray3 prevRay;
     uint32_t pidx;
+    /* deferred (set by the caller): begin() reads nothing of this frame's path tracing — the
+     * current reservoir is neither loaded nor copied; copy reports a pixel whose current
+     * reservoir goes to the temporary one unmerged (the three-launch form's finish kernel copies
+     * it), so that the pass's shifts and queries can run beside the path tracer */
+    bool deferred = false, copy = false;
 
     GD void finish(const PassCtx& P) {
+        if (deferred) { copy = true; return; }
         resvResetIfInvalid(resv);
         store_resv(P.b.reservoirTemp, idx, resv);
     }
@@ -777,7 +783,7 @@ struct TemporalTaskT {
         resvRng = ~rng;
         V3 pos = ray.ori + ray.dir * (depth - 1e-4f);
         idx = (uint64_t)iy * W + ix;
-        resv = load_resv(P.b.reservoirThis, idx, n);
+        if (!deferred) resv = load_resv(P.b.reservoirThis, idx, n);
         dstIsec.bx = uv.x; dstIsec.by = uv.y; dstIsec.inst = kSpecialHit; dstIsec.tri = 0u;
         if (P.set.temporalReuse) {
             src = resv_zero();
@@ -2217,7 +2223,8 @@ __global__ void __launch_bounds__(128, GRIS_WAVE_SHADE_MIN_BLOCKS) k_wave_post(W
  *            reservoir, or the spatial reservoir, final shading and running mean.
  * Same operations on the same values in the same order as the per-pixel kernels: results bit for
  * bit identical, ray counts equal. Slot k of pixel p (batch pixel id) lives at k * R.P + p. */
-constexpr uint8_t kRsEntry = 1u, kRsMerge = 2u, kRsQuery = 4u, kRsVisible = 8u, kRsBadWeight = 16u, kRsActive = 128u;
+constexpr uint8_t kRsEntry = 1u, kRsMerge = 2u, kRsQuery = 4u, kRsVisible = 8u, kRsBadWeight = 16u, kRsCopy = 32u,
+                  kRsActive = 128u;
 
 struct ReuseCtx {
     float4* pa;          /* weight if visible, source M, shifted Jacobian, shifted pdf */
@@ -2266,8 +2273,9 @@ __global__ void __launch_bounds__(128, kReusePrepareBlocks) k_reuse_temporal_pre
     if (x < P.b.width && y < P.b.height) {
         const uint32_t pix = V[v].pixelBase + y * P.b.width + x;
         TemporalTaskT<kGuide> task;
+        task.deferred = true;
         uint8_t state = 0;
-        if (task.begin(P, x, y, rc, err)) {   /* false: nothing to merge, the temporary reservoir is written */
+        if (task.begin(P, x, y, rc, err)) {   /* false: nothing to merge (copy: the finish kernel copies) */
             const guide::Lobes* Lp = nullptr;
             guide::Lobes L;
             if constexpr (kGuide) {
@@ -2283,6 +2291,8 @@ __global__ void __launch_bounds__(128, kReusePrepareBlocks) k_reuse_temporal_pre
             R.pa[pix] = make_float4(q.rw, task.src.sampleCount, q.jac, q.pdf);
             R.pb[pix] = make_float4(q.F.x, q.F.y, q.F.z, 0.0f);
             R.pn[pix] = task.pidx;
+        } else if (task.copy) {
+            state = kRsCopy;
         }
         R.ps[pix] = state;
     }
@@ -2299,9 +2309,14 @@ __global__ void __launch_bounds__(128, kReuseFinishBlocks) k_reuse_temporal_fini
     if (x >= P.b.width || y >= P.b.height) return;
     const uint32_t pix = V[v].pixelBase + y * P.b.width + x;
     const uint8_t state = R.ps[pix];
-    if (!(state & kRsEntry)) return;
+    if (!(state & (kRsEntry | kRsCopy))) return;
     const uint64_t idx = (uint64_t)y * P.b.width + x, npx = (uint64_t)P.b.width * P.b.height;
     Resv resv = load_resv(P.b.reservoirThis, idx, npx);
+    if (!(state & kRsEntry)) {               /* no temporal neighbour: the current reservoir as is */
+        resvResetIfInvalid(resv);
+        store_resv(P.b.reservoirTemp, idx, resv);
+        return;
+    }
     const float4 a = R.pa[pix];
     const bool visible = (state & kRsVisible) != 0u;
     const float w = visible ? a.x : 0.0f;   /* the source's weight: 0 unless the segment is visible */
@@ -2698,6 +2713,21 @@ size_t guide_wave_bytes_per_path() {
     return sizeof(uint32_t) + (9 + guide::kRaw + 18 + 9 + guide::kRaw) * sizeof(float);
 }
 
+cudaError_t wave_streams_create(WaveBuffers& wb) {
+    cudaError_t e = cudaStreamCreateWithFlags(&wb.aux, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&wb.aux2, cudaStreamNonBlocking);
+    for (cudaEvent_t* ev : {&wb.evFork, &wb.evJoin, &wb.evTemporal, &wb.evTemporalDone})
+        if (e == cudaSuccess) e = cudaEventCreateWithFlags(ev, cudaEventDisableTiming);
+    return e;
+}
+
+void wave_streams_destroy(WaveBuffers& wb) {
+    for (cudaStream_t* s : {&wb.aux, &wb.aux2})
+        if (*s) { cudaStreamSynchronize(*s); cudaStreamDestroy(*s); *s = nullptr; }
+    for (cudaEvent_t* ev : {&wb.evFork, &wb.evJoin, &wb.evTemporal, &wb.evTemporalDone})
+        if (*ev) { cudaEventDestroy(*ev); *ev = nullptr; }
+}
+
 size_t wave_bytes_per_path() { return sizeof(WaveRec) + sizeof(NeeRec) + sizeof(Isec) + 1 + 3 * sizeof(uint32_t) + 32; }
 
 static size_t reuse_up(size_t n) { return (n + 255) & ~(size_t)255; }
@@ -2777,6 +2807,37 @@ cudaError_t enqueue_batch(const BatchShape& sh, void* dViews, const void* hViews
         if (timer) timer->mark(0, true, stream);
         k_batch_gbuffer<<<tiles, blk, 0, stream>>>(V, n);
         if (timer) timer->mark(0, false, stream);
+    }
+    /* the three-launch form of the reuse passes where its buffers fit the frame */
+    const bool split = wb.reuse.slots > 0u && !sh.pairwise && sh.maxNeighbours <= wb.reuse.slots &&
+                       (uint64_t)sh.pixels <= wb.reuse.capacity && (passes & 6);
+    ReuseCtx R;
+    memset(&R, 0, sizeof(R));
+    if (split) {
+        R.pa = reinterpret_cast<float4*>(wb.reuse.pa);
+        R.pb = reinterpret_cast<float4*>(wb.reuse.pb);
+        R.pn = wb.reuse.pn;
+        R.ps = wb.reuse.ps;
+        R.q = reinterpret_cast<float4*>(wb.reuse.q);
+        R.counts = wb.reuse.counts;
+        R.P = pixels;
+        R.qCap = (uint64_t)pixels * wb.reuse.slots;
+        e = cudaMemsetAsync(wb.reuse.counts, 0, 4 * sizeof(uint32_t), stream);
+        if (e != cudaSuccess) return e;
+    }
+    const int gridVis = current_sm_count() * (wl.traceBlocksPerSM > 0 ? wl.traceBlocksPerSM : 16);
+    /* The temporal pass's prepare kernel and its visibility walk read the G-buffers and the
+     * previous frame's reservoirs, nothing of this frame's path tracing (the current reservoir
+     * is merged, or copied, by the finish kernel): with a side stream they run beside the path
+     * tracer, joined before the finish kernel. Guided batches keep the order (their shifts read
+     * the guide's mixture of this frame). */
+    const bool earlyTemporal = split && (passes & 2) && !guide && wb.aux2 != nullptr && timer == nullptr;
+    if (earlyTemporal) {
+        if ((e = cudaEventRecord(wb.evTemporal, stream)) != cudaSuccess) return e;
+        if ((e = cudaStreamWaitEvent(wb.aux2, wb.evTemporal, 0)) != cudaSuccess) return e;
+        k_reuse_temporal_prepare<false><<<tiles, blk, 0, wb.aux2>>>(V, n, R);
+        k_reuse_visibility<2><<<gridVis, 128, 0, wb.aux2>>>(V, n, R, 0);
+        if ((e = cudaEventRecord(wb.evTemporalDone, wb.aux2)) != cudaSuccess) return e;
     }
     if (passes & 1) {
         if (timer) timer->mark(1, true, stream);
@@ -2895,31 +2956,17 @@ cudaError_t enqueue_batch(const BatchShape& sh, void* dViews, const void* hViews
         if (timer) timer->mark(1, false, stream);
     }
 reuse:
-    /* the three-launch form of the reuse passes where its buffers fit the frame */
-    const bool split = wb.reuse.slots > 0u && !sh.pairwise && sh.maxNeighbours <= wb.reuse.slots &&
-                       (uint64_t)sh.pixels <= wb.reuse.capacity && (passes & 6);
-    ReuseCtx R;
-    memset(&R, 0, sizeof(R));
-    if (split) {
-        R.pa = reinterpret_cast<float4*>(wb.reuse.pa);
-        R.pb = reinterpret_cast<float4*>(wb.reuse.pb);
-        R.pn = wb.reuse.pn;
-        R.ps = wb.reuse.ps;
-        R.q = reinterpret_cast<float4*>(wb.reuse.q);
-        R.counts = wb.reuse.counts;
-        R.P = pixels;
-        R.qCap = (uint64_t)pixels * wb.reuse.slots;
-        e = cudaMemsetAsync(wb.reuse.counts, 0, 4 * sizeof(uint32_t), stream);
-        if (e != cudaSuccess) return e;
-    }
-    const int gridVis = current_sm_count() * (wl.traceBlocksPerSM > 0 ? wl.traceBlocksPerSM : 16);
     if (split && (passes & 2)) {
         if (timer) timer->mark(2, true, stream);
-        if (guide) k_reuse_temporal_prepare<true><<<tiles, blk, 0, stream>>>(V, n, R);
-        else k_reuse_temporal_prepare<false><<<tiles, blk, 0, stream>>>(V, n, R);
-        if (timer) timer->mark(GRIS_SLOT_REUSE_VIS_TEMPORAL, true, stream);
-        k_reuse_visibility<2><<<gridVis, 128, 0, stream>>>(V, n, R, 0);
-        if (timer) timer->mark(GRIS_SLOT_REUSE_VIS_TEMPORAL, false, stream);
+        if (earlyTemporal) {
+            if ((e = cudaStreamWaitEvent(stream, wb.evTemporalDone, 0)) != cudaSuccess) return e;
+        } else {
+            if (guide) k_reuse_temporal_prepare<true><<<tiles, blk, 0, stream>>>(V, n, R);
+            else k_reuse_temporal_prepare<false><<<tiles, blk, 0, stream>>>(V, n, R);
+            if (timer) timer->mark(GRIS_SLOT_REUSE_VIS_TEMPORAL, true, stream);
+            k_reuse_visibility<2><<<gridVis, 128, 0, stream>>>(V, n, R, 0);
+            if (timer) timer->mark(GRIS_SLOT_REUSE_VIS_TEMPORAL, false, stream);
+        }
         k_reuse_temporal_finish<<<tiles, blk, 0, stream>>>(V, n, R);
         if (timer) timer->mark(2, false, stream);
     }

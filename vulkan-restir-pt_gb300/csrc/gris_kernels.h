@@ -91,9 +91,11 @@ struct WaveBuffers {
     void* ray;          /* 32 B per path: the next closest-hit ray */
     uint32_t* counts;   /* 1536 words */
     uint64_t capacity;
-    /* a second stream and two events (null: the frame's kernels run in order on one stream) */
-    cudaStream_t aux;
-    cudaEvent_t evFork, evJoin;
+    /* two more streams and their events (null: the frame's kernels run in order on one stream):
+     * aux for a bounce's shadow queries beside the next bounce's closest hits, aux2 for the
+     * temporal pass's shifts and visibility walk beside the path tracer */
+    cudaStream_t aux, aux2;
+    cudaEvent_t evFork, evJoin, evTemporal, evTemporalDone;
     /* guided batches only (null otherwise): post queue, guide inputs / outputs per guided
      * vertex, training record per path, frame state (4 words) */
     uint32_t* postQueue;
@@ -105,6 +107,9 @@ struct WaveBuffers {
     float* gPrimOut;
     ReuseBuffers reuse;  /* the reuse passes' three-launch form (slots = 0: not used) */
 };
+/* the side streams and events of WaveBuffers (destroy waits for the streams' work) */
+cudaError_t wave_streams_create(WaveBuffers& wb);
+void wave_streams_destroy(WaveBuffers& wb);
 /* bytes per path of the guided-batch buffers */
 size_t guide_wave_bytes_per_path();
 size_t wave_bytes_per_path();
