@@ -1894,6 +1894,11 @@ constexpr bool kWalkPrefetch = GRIS_WALK_PREFETCH != 0;
 #define GRIS_WALK_REFILL_IDLE 8
 #endif
 constexpr int kWalkRefillIdle = GRIS_WALK_REFILL_IDLE;
+/* preferred shared-memory carveout of the resident walks in percent (-1: the driver's choice) */
+#ifndef GRIS_WALK_CARVEOUT
+#define GRIS_WALK_CARVEOUT -1
+#endif
+constexpr int kWalkCarveout = GRIS_WALK_CARVEOUT;
 
 constexpr uint32_t kCoopMaxRays = 8192;
 constexpr uint32_t kCoopStack = 1024;      /* node indices per warp (pushes are at most 32 per round) */
@@ -2826,6 +2831,17 @@ cudaError_t enqueue_batch(const BatchShape& sh, void* dViews, const void* hViews
         if (e != cudaSuccess) return e;
     }
     const int gridVis = current_sm_count() * (wl.traceBlocksPerSM > 0 ? wl.traceBlocksPerSM : 16);
+    if (kWalkCarveout >= 0) {
+        /* the resident walks' preferred shared-memory carveout (percent of the maximum): what is
+         * not shared memory is L1, which caches the nodes and triangles */
+        once_per_device(kDeviceKeyWalkCarveout, []() {
+            cudaError_t c = cudaFuncSetAttribute(k_wave_trace_refill<false>, cudaFuncAttributePreferredSharedMemoryCarveout, kWalkCarveout);
+            if (c == cudaSuccess) c = cudaFuncSetAttribute(k_wave_trace_refill<true>, cudaFuncAttributePreferredSharedMemoryCarveout, kWalkCarveout);
+            if (c == cudaSuccess) c = cudaFuncSetAttribute(k_reuse_visibility<2>, cudaFuncAttributePreferredSharedMemoryCarveout, kWalkCarveout);
+            if (c == cudaSuccess) c = cudaFuncSetAttribute(k_reuse_visibility<3>, cudaFuncAttributePreferredSharedMemoryCarveout, kWalkCarveout);
+            return c == cudaSuccess ? 1 : -1;
+        });
+    }
     /* The temporal pass's prepare kernel and its visibility walk read the G-buffers and the
      * previous frame's reservoirs, nothing of this frame's path tracing (the current reservoir
      * is merged, or copied, by the finish kernel): with a side stream they run beside the path

@@ -65,6 +65,7 @@ enum {
     kDeviceKeyGuideTcAttr = 4,      /* dynamic shared memory attribute of the tcgen05 inference kernel */
     kDeviceKeyGuideGradAttr = 5,    /* ... of the gradient kernel */
     kDeviceKeyGuideGradTcAttr = 6,  /* ... of the tcgen05 gradient kernel */
+    kDeviceKeyWalkCarveout = 7,     /* shared-memory carveout of the resident traversal kernels */
 };
 int once_per_device(int key, int (*f)());
 /* SM count of the current device (cached; 1 if it cannot be read). */
