@@ -1894,9 +1894,11 @@ constexpr bool kWalkPrefetch = GRIS_WALK_PREFETCH != 0;
 #define GRIS_WALK_REFILL_IDLE 8
 #endif
 constexpr int kWalkRefillIdle = GRIS_WALK_REFILL_IDLE;
-/* preferred shared-memory carveout of the resident walks in percent (-1: the driver's choice) */
+/* preferred shared-memory carveout of the resident walks in percent (-1: the driver's choice);
+ * 28% holds their 7 blocks of 8 KB and leaves the rest of the 256 KB to L1 (C2: 0.3% faster than
+ * the driver's choice, 3% faster than 100%) */
 #ifndef GRIS_WALK_CARVEOUT
-#define GRIS_WALK_CARVEOUT -1
+#define GRIS_WALK_CARVEOUT 28
 #endif
 constexpr int kWalkCarveout = GRIS_WALK_CARVEOUT;
 
