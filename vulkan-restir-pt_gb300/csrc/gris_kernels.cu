@@ -2844,19 +2844,24 @@ cudaError_t enqueue_batch(const BatchShape& sh, void* dViews, const void* hViews
             return c == cudaSuccess ? 1 : -1;
         });
     }
-    /* The temporal pass's prepare kernel and its visibility walk read the G-buffers and the
-     * previous frame's reservoirs, nothing of this frame's path tracing (the current reservoir
-     * is merged, or copied, by the finish kernel): with a side stream they run beside the path
-     * tracer, joined before the finish kernel. Guided batches keep the order (their shifts read
-     * the guide's mixture of this frame). */
-    const bool earlyTemporal = split && (passes & 2) && !guide && wb.aux2 != nullptr && timer == nullptr;
-    if (earlyTemporal) {
-        if ((e = cudaEventRecord(wb.evTemporal, stream)) != cudaSuccess) return e;
-        if ((e = cudaStreamWaitEvent(wb.aux2, wb.evTemporal, 0)) != cudaSuccess) return e;
-        k_reuse_temporal_prepare<false><<<tiles, blk, 0, wb.aux2>>>(V, n, R);
+    /* The temporal pass's prepare kernel and its visibility walk read the G-buffers, the
+     * previous frame's reservoirs and, in a guided batch, the guide's mixture at the primary
+     * vertices — nothing of this frame's path tracing (the current reservoir is merged, or
+     * copied, by the finish kernel): with a side stream they run beside the path tracer (from
+     * the G-buffer on, or from the primary vertices' inference on in a guided batch), joined
+     * before the finish kernel. */
+    const bool earlyTemporal = split && (passes & 2) && wb.aux2 != nullptr && timer == nullptr &&
+                               (!guide || (passes & 1));
+    auto early_temporal = [&]() -> cudaError_t {
+        cudaError_t x = cudaEventRecord(wb.evTemporal, stream);
+        if (x == cudaSuccess) x = cudaStreamWaitEvent(wb.aux2, wb.evTemporal, 0);
+        if (x != cudaSuccess) return x;
+        if (guide) k_reuse_temporal_prepare<true><<<tiles, blk, 0, wb.aux2>>>(V, n, R);
+        else k_reuse_temporal_prepare<false><<<tiles, blk, 0, wb.aux2>>>(V, n, R);
         k_reuse_visibility<2><<<gridVis, 128, 0, wb.aux2>>>(V, n, R, 0);
-        if ((e = cudaEventRecord(wb.evTemporalDone, wb.aux2)) != cudaSuccess) return e;
-    }
+        return cudaEventRecord(wb.evTemporalDone, wb.aux2);
+    };
+    if (earlyTemporal && !guide && (e = early_temporal()) != cudaSuccess) return e;
     if (passes & 1) {
         if (timer) timer->mark(1, true, stream);
         if (pathForm == GRIS_PATH_WAVEFRONT) {
@@ -2899,6 +2904,7 @@ cudaError_t enqueue_batch(const BatchShape& sh, void* dViews, const void* hViews
                     if (e != cudaSuccess) return e;
                 }
                 mark(9, false);
+                if (earlyTemporal && (e = early_temporal()) != cudaSuccess) return e;
                 mark(4, true);
                 k_gwave_begin<<<(pixels + 127) / 128, 128, 0, stream>>>(C);
                 mark(4, false);
@@ -2910,9 +2916,17 @@ cudaError_t enqueue_batch(const BatchShape& sh, void* dViews, const void* hViews
                     mark(6, true);
                     k_gwave_shade<<<gridShade, 128, 0, stream>>>(C, level);
                     mark(6, false);
+                    /* the level's shadow queries beside the guide's inference (post() needs both);
+                     * in order on one stream under the kernel timer */
+                    const bool gfork = wb.aux != nullptr && timer == nullptr;
+                    cudaStream_t ss = gfork ? wb.aux : stream;
+                    if (gfork) {
+                        if ((e = cudaEventRecord(wb.evFork, stream)) != cudaSuccess) return e;
+                        if ((e = cudaStreamWaitEvent(wb.aux, wb.evFork, 0)) != cudaSuccess) return e;
+                    }
                     mark(7, true);
-                    if (wl.refill) { k_wave_trace_refill<true><<<gridTrace, 128, 0, stream>>>(C, level); k_wave_trace_coop<true><<<gridCoop, 128, 0, stream>>>(C, level); }
-                    else k_wave_shadow<<<gridTrace, 128, 0, stream>>>(C, level);
+                    if (wl.refill) { k_wave_trace_refill<true><<<gridTrace, 128, 0, ss>>>(C, level); k_wave_trace_coop<true><<<gridCoop, 128, 0, ss>>>(C, level); }
+                    else k_wave_shadow<<<gridTrace, 128, 0, ss>>>(C, level);
                     mark(7, false);
                     mark(9, true);
                     guide::FwdArgs fa;
@@ -2922,6 +2936,10 @@ cudaError_t enqueue_batch(const BatchShape& sh, void* dViews, const void* hViews
                     e = guide::launch_forward(fa, stream);
                     if (e != cudaSuccess) return e;
                     mark(9, false);
+                    if (gfork) {
+                        if ((e = cudaEventRecord(wb.evJoin, wb.aux)) != cudaSuccess) return e;
+                        if ((e = cudaStreamWaitEvent(stream, wb.evJoin, 0)) != cudaSuccess) return e;
+                    }
                     mark(8, true);
                     k_gwave_post<<<gridShade, 128, 0, stream>>>(C, level);
                     mark(8, false);
