@@ -70,9 +70,11 @@ def alg_bytes(slot, w, px):
       temporal     traversal + 24+4+24 B G-buffer + 2 x 96 B reservoir reads + 96 B write + surface fetches
       spatial      traversal + 4 x 24 B G-buffer + 4 x 96 B reservoir reads + 96 B write + 32 B output r/w
                    + surface fetches
-      wave_begin   24 B G-buffer read + a path record write + a 4 B queue entry per pixel
+      wave_begin   24 B G-buffer read + a path record write + its 32 B next ray + a 4 B queue
+                   entry per pixel
       wave_extend  per ray: 32 B ray + 16 B hit + 4 B queue entry, plus traversal
-      wave_shade   per path: record read and write + 16 B hit + a surface fetch + 4 B queue entry
+      wave_shade   per path: record read and write + 16 B hit + a surface fetch + 32 B next ray +
+                   4 B queue entry; per shadow query: its 96 B record + 4 B queue entry
       wave_shadow  per shadow ray: 48 B query + 1 B verdict + 4 B queue entry, plus traversal
       wave_post    per shadow query: record read and write + query read + verdict + queue entry
     The reuse passes in three launches (prepare, visibility walk, finish; w["split"] true):
@@ -84,7 +86,7 @@ def alg_bytes(slot, w, px):
       reuse_vis_*  per query: 32 B queue entry + 1 B verdict read and written, plus traversal"""
     trav = w["nodes"] * NODE_BYTES + w["tris"] * TRI_BYTES
     r = w["rays"]
-    per_px = {"gbuffer": 28, "path_trace": 120, "temporal": 340, "spatial": 608, "wave_begin": 24 + WAVE_STATE + 4}
+    per_px = {"gbuffer": 28, "path_trace": 120, "temporal": 340, "spatial": 608, "wave_begin": 24 + WAVE_STATE + 32 + 4}
     if slot in ("temporal", "spatial") and w.get("split"):
         extra = 2 * 37 + 96 if slot == "temporal" else 2 * 37 * w["neighbours"] + 120
         return trav + (per_px[slot] + extra) * px + SURFACE_BYTES * r + 32 * w["queries"]
@@ -97,7 +99,7 @@ def alg_bytes(slot, w, px):
     if slot == "wave_extend":
         return trav + 52 * r
     if slot == "wave_shade":
-        return w["paths"] * (2 * WAVE_STATE + 16 + SURFACE_BYTES + 4)
+        return w["paths"] * (2 * WAVE_STATE + 16 + SURFACE_BYTES + 32 + 4) + w["shadow_paths"] * (NEE_STATE + 4)
     if slot == "wave_shadow":
         return trav + 53 * r
     if slot == "wave_post":
