@@ -163,3 +163,48 @@ def test_batch_graph_follows_the_mis_weights_setting():
     batch.close()
     scene.close()
     ctx.close()
+
+
+@pytest.mark.parametrize("guided", [False, True], ids=["plain", "guided"])
+def test_overlapped_frame_equals_the_frame_in_order(guided):
+    """A wavefront frame forks onto side streams (a bounce's closest hits beside the previous
+    bounce's shadow queries and post(); the temporal pass's shifts and visibility walk beside the
+    path tracer). With the kernel timer on everything runs in order on one stream. Both must give
+    the same buffers bit for bit, through captured graphs and eager launches, on a frame whose
+    bounce levels are full (the resident walks) with temporal history, and raise no error bit
+    (bit 3: post() disagreeing with the next ray queued ahead of it)."""
+    hs = G.HostScene(2, seed=21, grid=48, spheres=60)
+    W, H = 176, 120
+    cams, prevs = G.sequence_cameras(hs, 4, W, H, seed=5)
+    st = G.Settings.make(maxDepth=8, spatialRadius=20.0)
+    keys = {"resv": G.BUF_RESERVOIR, "temp": G.BUF_TEMP, "out": G.BUF_OUTPUT}
+    runs = []
+    for graphs, profiling in ((True, False), (False, False), (False, True)):
+        ctx = G.Context(0)
+        ctx.set_path_form(G.PATH_WAVEFRONT)
+        ctx.set_wave_refill(True)
+        ctx.set_graphs(graphs)
+        ctx.set_profiling(profiling)
+        scene = G.Scene(ctx, hs)
+        batch = G.Batch(ctx, [scene], [(W, H)])
+        guide = None
+        if guided:   # untrained (training folds gradients with float atomics: not bit-reproducible)
+            guide = G.Guide(ctx, G.GuideConfig.make(seed=3, train=False))
+            batch.set_guide(guide)
+        ctx.counters(reset=True)
+        got = []
+        for f in range(4):
+            batch.render([cams[f]], [prevs[f]], [st])
+            got.append({k: batch.download(0, b).tobytes() for k, b in keys.items()})
+        ctx.sync()
+        assert ctx.counters()[3] == 0
+        runs.append(got)
+        batch.close()
+        if guide is not None:
+            guide.close()
+        scene.close()
+        ctx.close()
+    for f in range(4):
+        for k in keys:
+            assert runs[0][f][k] == runs[2][f][k], ("graphs vs in order", f, k)
+            assert runs[1][f][k] == runs[2][f][k], ("eager vs in order", f, k)
