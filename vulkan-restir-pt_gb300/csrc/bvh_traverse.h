@@ -76,13 +76,6 @@ GRIS_HD float gris_fmax(float a, float b) {
     return __builtin_fmaxf(a, b);
 #endif
 }
-GRIS_HD float gris_fabs(float a) {
-#ifdef __CUDA_ARCH__
-    return fabsf(a);
-#else
-    return __builtin_fabsf(a);
-#endif
-}
 GRIS_HD float gris_u2f(uint32_t u) {
 #ifdef __CUDA_ARCH__
     return __uint_as_float(u);
@@ -120,18 +113,9 @@ GRIS_HD bool gris_tri_test(const float* T, float ox, float oy, float oz, float d
     float pvx = dy * e2z - dz * e2y, pvy = dz * e2x - dx * e2z, pvz = dx * e2y - dy * e2x;
     float det = (e1x * pvx + e1y * pvy) + e1z * pvz;
     if (det == 0.0f) return false;
-    float tvx = ox - T[0], tvy = oy - T[1], tvz = oz - T[2];
-    float un = (tvx * pvx + tvy * pvy) + tvz * pvz;
-    /* u = un * (1 / det) is negative when un and det differ in sign; with |un| >= 1e-20 and
-     * |det| <= 1e8 it is below -1e-28 (a normal number, not a -0 that would pass u >= 0), so the
-     * test below rejects it: reject before the division */
-#ifndef GRIS_TRI_EARLY_OUT
-#define GRIS_TRI_EARLY_OUT 1
-#endif
-    if (GRIS_TRI_EARLY_OUT && (un < 0.0f) != (det < 0.0f) && gris_fabs(un) >= 1e-20f && gris_fabs(det) <= 1e8f)
-        return false;
     float inv = 1.0f / det;
-    float u = un * inv;
+    float tvx = ox - T[0], tvy = oy - T[1], tvz = oz - T[2];
+    float u = ((tvx * pvx + tvy * pvy) + tvz * pvz) * inv;
     if (!(u >= 0.0f) || !(u <= 1.0f)) return false;
     float qvx = tvy * e1z - tvz * e1y, qvy = tvz * e1x - tvx * e1z, qvz = tvx * e1y - tvy * e1x;
     float v = ((dx * qvx + dy * qvy) + dz * qvz) * inv;

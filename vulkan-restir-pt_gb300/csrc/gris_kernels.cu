@@ -1261,9 +1261,9 @@ constexpr int kGbufShared = GRIS_GBUFFER_SHARED_ENTRIES;
 using GbufStack = std::conditional_t<(kGbufShared > 0), GrisShortStack<kGbufShared>, GrisArrayStack>;
 
 /* The G-buffer walk's stack for thread `tid` of a 128-thread block (slab: the block's shared array). */
-template <int K>
-GD void gbuffer_stack_bind(GrisShortStack<K>& stack, uint32_t* slab, uint32_t tid) { stack.bind(slab, tid, 128u); }
-GD void gbuffer_stack_bind(GrisArrayStack&, uint32_t*, uint32_t) {}
+GD void gbuffer_stack_bind(GbufStack& stack, uint32_t* slab, uint32_t tid) {
+    if constexpr (kGbufShared > 0) stack.bind(slab, tid, 128u);
+}
 
 template <class Stack>
 GD uint32_t gbuffer_pixel(const GBufCtx& G, uint32_t x, uint32_t y, int& err, GrisWork& work, Stack& stack) {
