@@ -20,7 +20,6 @@
  * pair) and k_wave_post; k_gwave_* are the guided stages.
  */
 #include <cuda_fp16.h>
-#include <type_traits>
 #include <cooperative_groups.h>
 #include <cuda_runtime.h>
 
@@ -1252,34 +1251,14 @@ struct GBufCtx {
 GD uint32_t packUnorm1(float c) { return (uint32_t)floorf(fminf(fmaxf(c, 0.0f), 1.0f) * 255.0f + 0.5f); }
 
 /* One pixel of the G-buffer; returns 1 (a primary ray was cast). */
-/* Entries of the G-buffer walk's stack held in shared memory (after two in registers; 0: the
- * whole stack in one local-memory array, as gris_bvh_trace keeps it). */
-#ifndef GRIS_GBUFFER_SHARED_ENTRIES
-#define GRIS_GBUFFER_SHARED_ENTRIES 8
-#endif
-constexpr int kGbufShared = GRIS_GBUFFER_SHARED_ENTRIES;
-using GbufStack = std::conditional_t<(kGbufShared > 0), GrisShortStack<kGbufShared>, GrisArrayStack>;
-
-/* The G-buffer walk's stack for thread `tid` of a 128-thread block (slab: the block's shared array). */
-GD void gbuffer_stack_bind(GbufStack& stack, uint32_t* slab, uint32_t tid) {
-    if constexpr (kGbufShared > 0) stack.bind(slab, tid, 128u);
-}
-
-template <class Stack>
-GD uint32_t gbuffer_pixel(const GBufCtx& G, uint32_t x, uint32_t y, int& err, GrisWork& work, Stack& stack) {
+GD uint32_t gbuffer_pixel(const GBufCtx& G, uint32_t x, uint32_t y, int& err, GrisWork& work) {
     const DevScene& sc = G.sc;
     uint64_t p = (uint64_t)y * G.b.width + x;
     V2 uv = v2(((float)x + 0.5f) / (float)G.b.width, ((float)y + 0.5f) / (float)G.b.height);
     Ray3 ray = pinholeCameraSampleRay(G.cam, v2(uv.x, 1.0f - uv.y));
     GrisRayHit h;
-    /* gris_bvh_trace<false> with the caller's stack (the light instance skipped: the G-buffer is
-     * rasterised without lights) */
-    GrisTraversal<false> tr;
-    stack.reset();
-    tr.init(ray.ori.x, ray.ori.y, ray.ori.z, ray.dir.x, ray.dir.y, ray.dir.z, kMinRayDistance, kMaxRayDistance);
-    while (tr.step(sc.nodes, sc.tris, true, &err, stack)) {}
-    tr.result(&h, &work);
-    bool hit = tr.found;
+    bool hit = gris_bvh_trace<false>(sc.nodes, sc.tris, ray.ori.x, ray.ori.y, ray.ori.z, ray.dir.x, ray.dir.y,
+                                      ray.dir.z, kMinRayDistance, kMaxRayDistance, true, &h, &err, &work);
     float4* dnOut = reinterpret_cast<float4*>(G.b.depthNormal) + p;
     uint2* amOut = reinterpret_cast<uint2*>(G.b.albedoMatId) + p;
     __half2* mvOut = reinterpret_cast<__half2*>(G.b.motion) + p;
@@ -1352,10 +1331,7 @@ __global__ void __launch_bounds__(128) k_gbuffer(GBufCtx G) {
     int err = 0;
     uint32_t primary = 0;
     GrisWork work; work.nodes = 0u; work.tris = 0u;
-    __shared__ uint32_t sStack[2 * (kGbufShared > 0 ? kGbufShared : 1) * 128];
-    GbufStack stack;
-    gbuffer_stack_bind(stack, sStack, threadIdx.y * blockDim.x + threadIdx.x);
-    if (x < G.b.width && y < G.b.height) primary = gbuffer_pixel(G, x, y, err, work, stack);
+    if (x < G.b.width && y < G.b.height) primary = gbuffer_pixel(G, x, y, err, work);
     flush_gbuffer_counts(G.counters, primary, err, work, G.countWork);
 }
 
@@ -1628,10 +1604,7 @@ __global__ void __launch_bounds__(128) k_batch_gbuffer(const ViewEntry* __restri
     int err = 0;
     uint32_t primary = 0;
     GrisWork work; work.nodes = 0u; work.tris = 0u;
-    __shared__ uint32_t sStack[2 * (kGbufShared > 0 ? kGbufShared : 1) * 128];
-    GbufStack stack;
-    gbuffer_stack_bind(stack, sStack, threadIdx.y * blockDim.x + threadIdx.x);
-    if (x < G.b.width && y < G.b.height) primary = gbuffer_pixel(G, x, y, err, work, stack);
+    if (x < G.b.width && y < G.b.height) primary = gbuffer_pixel(G, x, y, err, work);
     flush_gbuffer_counts(G.counters, primary, err, work, G.countWork);
 }
 
