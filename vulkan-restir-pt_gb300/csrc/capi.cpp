@@ -116,6 +116,8 @@ struct GrisContext {
     int useGraphs = 1;
     grisrt::WaveLaunch waveLaunch;
     double* dReduce = nullptr;      /* relMSE partial sums (allocated on first use) */
+    void* diSplit = nullptr;        /* the DI spatial pass's three-launch scratch (grown on demand) */
+    uint64_t diSplitPixels = 0;
     Profiler prof;
     std::string err;
 };
@@ -267,6 +269,7 @@ int grisDestroy(GrisContext* ctx) {
     if (ctx->stream) cudaStreamSynchronize(ctx->stream);
     ctx->wave.release();
     if (ctx->dReduce) cudaFree(ctx->dReduce);
+    if (ctx->diSplit) cudaFree(ctx->diSplit);
     cudaFree(ctx->dCounters);
     cudaFreeHost(ctx->hCounters);
     if (ctx->stream) cudaStreamDestroy(ctx->stream);
@@ -732,8 +735,22 @@ int grisPassDI(GrisContext* ctx, const GrisScene* s, const GrisDIBindings* b, co
     if (!grisrt::scene_device(s, &view, &dev)) return fail(ctx, GRIS_ERR_INVALID_ARGUMENT, "scene has no device copy");
     if (dev != ctx->device) return fail(ctx, GRIS_ERR_INVALID_ARGUMENT, "scene lives on another device");
     cudaSetDevice(ctx->device);
+    /* the spatial pass in three launches (reconnection shift) wants its scratch: grown here,
+     * outside a stream capture (inside one the single spatial kernel runs) */
+    const uint64_t px = (uint64_t)b->width * b->height;
+    cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+    cudaStreamIsCapturing(ctx->stream, &cap);
+    if ((passes & 4) && set->spatialReuse && set->shiftType == GRIS_DI_SHIFT_RECONNECTION && ctx->diSplitPixels < px &&
+        cap == cudaStreamCaptureStatusNone) {
+        cudaStreamSynchronize(ctx->stream);
+        if (ctx->diSplit) cudaFree(ctx->diSplit);
+        ctx->diSplit = nullptr;
+        ctx->diSplitPixels = 0;
+        if (cudaMalloc(&ctx->diSplit, grisrt::di_split_bytes_per_pixel() * px + 256) == cudaSuccess) ctx->diSplitPixels = px;
+        else ctx->diSplit = nullptr;
+    }
     GRIS_CK(ctx, grisrt::launch_di(view, *b, *cam, *prevCam, *set, passes & 7, ctx->dCounters, ctx->countWork,
-                                   &ctx->prof, ctx->stream));
+                                   &ctx->prof, ctx->stream, ctx->diSplit, ctx->diSplitPixels));
     return GRIS_OK;
 }
 

@@ -24,6 +24,7 @@
 
 #include "gris_device.cuh"
 #include "gris_kernels.h"
+#include "grisrt_internal.h"
 #include "ray_query.cuh"
 
 namespace grisrt {
@@ -502,9 +503,174 @@ __global__ void __launch_bounds__(128, 8) k_di_spatial(DICtx P) {
     flush_counts(P.counters, rc, err, 6, P.countWork);
 }
 
+/* ------------------------------------------------------------------ spatial pass in three launches */
+/* With the reconnection shift the spatial pass runs as prepare (per pixel: the ten neighbours'
+ * shifts up to their visibility queries, di_spatial_shift, each neighbour's record kept in slot k
+ * of pixel p at k * P + p and its query appended to a queue of slots), the refilling any-hit walk
+ * of that queue (a visible segment sets its slot's verdict) and finish (the merges in neighbour
+ * order with the verdicts, the final occlusion test, the cap and the running mean): the
+ * operations of k_di_spatial in the same order, each query answered as traceVisibility answers
+ * it. A warp's queries no longer wait for the longest walk among them. */
+struct DISplit {
+    float4* from;        /* per pixel: its primary vertex */
+    uint32_t* mq;        /* per pixel: neighbour records | query bits << 8 */
+    float4* recA;        /* per slot: W if visible, merge draw, Jacobian, pdf */
+    uint2* recB;         /* per slot: source M, source pixel */
+    float4* recTo;       /* per slot: the light vertex the query looks at */
+    uint8_t* vis;        /* per slot: 1 = visible */
+    uint32_t* queue;     /* query slots */
+    uint32_t* counts;    /* [0] queries, [1] the walk's cursor */
+    uint64_t P;          /* pixels */
+};
+
+__global__ void __launch_bounds__(128, 8) k_di_spatial_prepare(DICtx P, DISplit S) {
+    const uint32_t x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y * blockDim.y + threadIdx.y;
+    const uint64_t idx = (uint64_t)y * P.b.width + x;
+    uint32_t queries = 0u;
+    if (x < P.b.width && y < P.b.height) {
+        DIPixel px;
+        uint32_t m = 0u;
+        if (di_pixel(P, x, y, px)) {
+            uint32_t rng = makeSeed2(P.cam.seed, x, y) ^ 2u;
+            DINeighbour nb[kDINeighbours];
+            di_spatial_shift(P, px, -px.ray.dir, rng, nb, m, queries);
+            S.from[idx] = make_float4(px.surf.pos.x, px.surf.pos.y, px.surf.pos.z, 0.0f);
+            for (uint32_t i = 0; i < m; i++) {
+                const uint64_t s = (uint64_t)i * S.P + idx;
+                S.recA[s] = make_float4(nb[i].Wv, nb[i].u, nb[i].jac, nb[i].pdf);
+                S.recB[s] = make_uint2(nb[i].M, nb[i].q);
+                S.recTo[s] = make_float4(nb[i].to.x, nb[i].to.y, nb[i].to.z, 0.0f);
+                S.vis[s] = 0u;
+            }
+        }
+        S.mq[idx] = m | (queries << 8);
+    }
+    /* the lane's queries at the warp's exclusive prefix, one atomic per warp */
+    const uint32_t lane = (threadIdx.y * blockDim.x + threadIdx.x) & 31u;
+    const uint32_t c = (uint32_t)__popc(queries);
+    uint32_t incl = c;
+    for (uint32_t d = 1; d < 32; d <<= 1) {
+        const uint32_t v = __shfl_up_sync(0xffffffffu, incl, d);
+        if (lane >= d) incl += v;
+    }
+    const uint32_t total = __shfl_sync(0xffffffffu, incl, 31);
+    uint32_t base = 0u;
+    if (lane == 31u && total) base = atomicAdd(S.counts, total);
+    base = __shfl_sync(0xffffffffu, base, 31);
+    uint32_t at = base + incl - c;
+    for (uint32_t pending = queries; pending; pending &= pending - 1u)
+        S.queue[at++] = (uint32_t)((uint64_t)(__ffs(pending) - 1) * S.P + idx);
+}
+
+constexpr int kDIWalkShared = 8;   /* walk stack entries in shared memory (after two in registers) */
+constexpr int kDIWalkTris = 2;     /* leaf triangles tested per step */
+
+__global__ void __launch_bounds__(128, 7) k_di_visibility(DICtx P, DISplit S) {
+    const uint32_t n = S.counts[0];
+    uint32_t* cursor = S.counts + 1;
+    const uint32_t lane = threadIdx.x & 31u;
+    RayCount rc = ray_count();
+    int err = 0;
+    GrisTraversal<true> tr;
+    __shared__ uint32_t sStack[2 * kDIWalkShared * 128];
+    GrisShortStack<kDIWalkShared> stack;
+    stack.bind(sStack, threadIdx.x, 128u);
+    uint32_t slot = 0u;
+    bool active = false, more = true;
+    while (true) {
+        const unsigned idle = __ballot_sync(0xffffffffu, !active);
+        if (more && __popc(idle) >= 8) {
+            const uint32_t take = (uint32_t)__popc(idle), leader = __ffs(idle) - 1;
+            uint32_t base = 0;
+            if (lane == leader) base = atomicAdd(cursor, take);
+            base = __shfl_sync(0xffffffffu, base, leader);
+            if (!active) {
+                const uint32_t i = base + (uint32_t)__popc(idle & ((1u << lane) - 1u));
+                if (i < n) {
+                    slot = S.queue[i];
+                    const float4 f = S.from[slot % S.P], t = S.recTo[slot];
+                    /* traceVisibility's segment: from the pixel to the light vertex */
+                    const V3 from = v3(f.x, f.y, f.z), to = v3(t.x, t.y, t.z);
+                    const V3 d = normalize3(to - from);
+                    stack.reset();
+                    tr.init(from.x, from.y, from.z, d.x, d.y, d.z, kMinRayDistance,
+                            distance3(to, from) - kMinRayDistance);
+                    active = true;
+                }
+            }
+            if (base + take >= n) more = false;
+        }
+        if (__ballot_sync(0xffffffffu, active) == 0u) {
+            if (!more) break;
+            continue;
+        }
+        if (active && !tr.template step<kDIWalkTris>(P.sc.nodes, P.sc.tris, false, &err, stack)) {
+            GrisRayHit h;
+            tr.result(&h, &rc.work);
+            rc.shadow++;
+            if (!tr.found) S.vis[slot] = 1u;
+            active = false;
+        }
+    }
+    flush_counts(P.counters, rc, err, 6, P.countWork);
+}
+
+__global__ void __launch_bounds__(128, 8) k_di_spatial_finish(DICtx P, DISplit S) {
+    RayCount rc = ray_count();
+    int err = 0;
+    const uint32_t x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y * blockDim.y + threadIdx.y;
+    if (x >= P.b.width || y >= P.b.height) return;
+    const int W = (int)P.b.width, H = (int)P.b.height;
+    const uint64_t n = (uint64_t)W * (uint64_t)H, idx = (uint64_t)y * W + x;
+    DIPixel px;
+    V3 color = v3s(0.0f);
+    if (di_pixel(P, x, y, px)) {
+        const V3 wo = -px.ray.dir;
+        DIResv r = load_di(P.b.reservoirTemp, idx, n);
+        const uint32_t mq = S.mq[idx], m = mq & 0xffu, queries = mq >> 8;
+        DINeighbour nb[kDINeighbours];
+        uint32_t visible = 0u;
+        for (uint32_t i = 0; i < m; i++) {
+            const uint64_t s = (uint64_t)i * S.P + idx;
+            const float4 a = S.recA[s];
+            const uint2 b = S.recB[s];
+            nb[i].Wv = a.x; nb[i].u = a.y; nb[i].jac = a.z; nb[i].pdf = a.w;
+            nb[i].M = b.x; nb[i].q = b.y;
+            if (((queries >> i) & 1u) && S.vis[s]) visible |= 1u << i;
+        }
+        di_spatial_merge(P, nb, m, visible, r);
+        di_occlude(P, r, px.surf.pos, rc, err);
+        di_cap(r, kDICap);
+        if (!di_usable(r)) di_clear(r);
+        store_di(P.b.reservoirThis, idx, r);
+        if (di_usable(r) && r.s.isec.inst != kInvalidHit) {
+            Surf ls = surf_zero();
+            loadSurfaceInfo(P.sc, r.s.isec, ls);
+            V3 wi = normalize3(ls.pos - px.surf.pos);
+            if (r.M > 0u) {
+                Mat mat = load_material(P.sc, px.surf.matIndex);
+                V3 Li = r.s.Li * evalBSDF(mat, px.surf.albedo, px.surf.norm, wo, wi) * satDot(px.surf.norm, wi) / r.s.pdf;
+                if (!isBlack(Li)) color = Li / luminance(Li) * r.W / (float)r.M;
+            }
+        }
+        color = clampColor(color);
+    }
+    float frameCount = (float)(P.cam.frameIndex & kCameraFrameIndexMask);
+    float4* out = reinterpret_cast<float4*>(P.b.directOutput) + idx;
+    float4 o = *out;
+    V3 acc = (v3(o.x, o.y, o.z) * frameCount + color) / (frameCount + 1.0f);
+    *out = make_float4(acc.x, acc.y, acc.z, 1.0f);
+    flush_counts(P.counters, rc, err, 6, P.countWork);
+}
+
+size_t di_split_bytes_per_pixel() {
+    return sizeof(float4) + sizeof(uint32_t) +
+           kDINeighbours * (sizeof(float4) + sizeof(uint2) + sizeof(float4) + 1 + sizeof(uint32_t));
+}
+
 cudaError_t launch_di(const DeviceSceneView& scene, const GrisDIBindings& b, const GrisCamera& cam,
                       const GrisCamera& prevCam, const GrisDISettings& set, int passes, unsigned long long* counters,
-                      int countWork, KernelTimer* timer, cudaStream_t stream) {
+                      int countWork, KernelTimer* timer, cudaStream_t stream, void* split, uint64_t splitPixels) {
     DICtx P;
     P.sc = to_dev(scene);
     P.cam = make_cam(cam);
@@ -526,7 +692,30 @@ cudaError_t launch_di(const DeviceSceneView& scene, const GrisDIBindings& b, con
     }
     if (passes & 4) {
         if (timer) timer->mark(GRIS_SLOT_DI_SPATIAL, true, stream);
-        k_di_spatial<<<grid, block, 0, stream>>>(P);
+        const uint64_t px = (uint64_t)b.width * b.height;
+        const bool phased = set.spatialReuse && set.shiftType == GRIS_DI_SHIFT_RECONNECTION;
+        if (phased && split && splitPixels >= px) {
+            /* carve the scratch: per pixel from, mq; per slot recA, recTo, recB, vis, queue */
+            DISplit S;
+            unsigned char* c = reinterpret_cast<unsigned char*>(split);
+            const uint64_t slots = (uint64_t)kDINeighbours * px;
+            S.counts = reinterpret_cast<uint32_t*>(c); c += 256;
+            S.from = reinterpret_cast<float4*>(c); c += px * sizeof(float4);
+            S.recA = reinterpret_cast<float4*>(c); c += slots * sizeof(float4);
+            S.recTo = reinterpret_cast<float4*>(c); c += slots * sizeof(float4);
+            S.recB = reinterpret_cast<uint2*>(c); c += slots * sizeof(uint2);
+            S.mq = reinterpret_cast<uint32_t*>(c); c += px * sizeof(uint32_t);
+            S.queue = reinterpret_cast<uint32_t*>(c); c += slots * sizeof(uint32_t);
+            S.vis = reinterpret_cast<uint8_t*>(c);
+            S.P = px;
+            cudaError_t e = cudaMemsetAsync(S.counts, 0, 2 * sizeof(uint32_t), stream);
+            if (e != cudaSuccess) return e;
+            k_di_spatial_prepare<<<grid, block, 0, stream>>>(P, S);
+            k_di_visibility<<<current_sm_count() * 16, 128, 0, stream>>>(P, S);
+            k_di_spatial_finish<<<grid, block, 0, stream>>>(P, S);
+        } else {
+            k_di_spatial<<<grid, block, 0, stream>>>(P);
+        }
         if (timer) timer->mark(GRIS_SLOT_DI_SPATIAL, false, stream);
     }
     return cudaGetLastError();

@@ -39,9 +39,13 @@ cudaError_t launch_gris(const DeviceSceneView& scene, const GrisPassBindings& b,
                         const GrisCamera& prevCam, const GrisSettings& set, int passes, unsigned long long* counters,
                         int countWork, KernelTimer* timer, cudaStream_t stream, int launchMode = GRIS_LAUNCH_PERSISTENT);
 /* ReSTIR DI (TestReSTIR::render): passes bit 0 candidates, bit 1 temporal, bit 2 spatial */
+/* split: scratch of di_split_bytes_per_pixel() * splitPixels + 256 bytes for the spatial pass in
+ * three launches (null or too small: the single spatial kernel) */
 cudaError_t launch_di(const DeviceSceneView& scene, const GrisDIBindings& b, const GrisCamera& cam,
                       const GrisCamera& prevCam, const GrisDISettings& set, int passes, unsigned long long* counters,
-                      int countWork, KernelTimer* timer, cudaStream_t stream);
+                      int countWork, KernelTimer* timer, cudaStream_t stream, void* split = nullptr,
+                      uint64_t splitPixels = 0);
+size_t di_split_bytes_per_pixel();
 /* presentation pass (post_proc.frag): composition, tone mapping, gamma, UNORM8 */
 cudaError_t launch_post(const GrisPostBindings& b, const GrisPostSettings& set, cudaStream_t stream);
 /* converged image: FP64 sums of independent paths per pixel; relMSE / MSE reduction */
