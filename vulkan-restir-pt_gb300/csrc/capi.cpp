@@ -735,13 +735,14 @@ int grisPassDI(GrisContext* ctx, const GrisScene* s, const GrisDIBindings* b, co
     if (!grisrt::scene_device(s, &view, &dev)) return fail(ctx, GRIS_ERR_INVALID_ARGUMENT, "scene has no device copy");
     if (dev != ctx->device) return fail(ctx, GRIS_ERR_INVALID_ARGUMENT, "scene lives on another device");
     cudaSetDevice(ctx->device);
-    /* the spatial pass in three launches (reconnection shift) wants its scratch: grown here,
-     * outside a stream capture (inside one the single spatial kernel runs) */
+    /* the candidates pass and the spatial pass (reconnection shift) in three launches want their
+     * scratch (one block, used by one pass at a time): grown here, outside a stream capture
+     * (inside one the single kernels run) */
     const uint64_t px = (uint64_t)b->width * b->height;
     cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
     cudaStreamIsCapturing(ctx->stream, &cap);
-    if ((passes & 4) && set->spatialReuse && set->shiftType == GRIS_DI_SHIFT_RECONNECTION && ctx->diSplitPixels < px &&
-        cap == cudaStreamCaptureStatusNone) {
+    const bool split = (passes & 1) || ((passes & 4) && set->spatialReuse && set->shiftType == GRIS_DI_SHIFT_RECONNECTION);
+    if (split && ctx->diSplitPixels < px && cap == cudaStreamCaptureStatusNone) {
         cudaStreamSynchronize(ctx->stream);
         if (ctx->diSplit) cudaFree(ctx->diSplit);
         ctx->diSplit = nullptr;

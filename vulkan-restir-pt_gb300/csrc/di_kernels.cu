@@ -92,8 +92,18 @@ GD void store_di(GrisDIReservoir* buf, uint64_t i, const DIResv& r) {
 /* sampleLi (di_reservoir.glsl:78-174): the light and / or BSDF candidate streamed into `resv`
  * (one draw of resvRng per candidate), then the chosen sample's Li scaled by W / w and M = 1.
  * The candidates' own colour sum is never used by the pass and is not formed. */
+/* The candidates' two ray queries, answered on the spot (DITraceInline) or by the walks of the
+ * candidates pass in three launches (DITraceQueue / DITraceAnswer, below). */
+struct DITraceInline {
+    RayCount& rc;
+    int& err;
+    GD bool shadow(const DICtx& P, V3 o, V3 d, float tmax) { return traceShadowCall(P.sc, o, kMinRayDistance, d, tmax, rc, err); }
+    GD Isec closest(const DICtx& P, V3 o, V3 d) { return traceClosestHitCall(P.sc, o, d, kMinRayDistance, kMaxRayDistance, rc, err); }
+};
+
+template <class Tracer>
 GD void di_sample_li(const DICtx& P, const Surf& surf, const Mat& mat, V3 wo, uint32_t rng, uint32_t& resvRng,
-                     DIResv& resv, RayCount& rc, int& err) {
+                     DIResv& resv, Tracer& tracer) {
     DISample ps = di_zero().s;
     ps.rng = rng;
     V4 lr = sample4f(rng);
@@ -101,7 +111,7 @@ GD void di_sample_li(const DICtx& P, const Surf& surf, const Mat& mat, V3 wo, ui
     if (P.set.sampleType != GRIS_DI_SAMPLE_BSDF && !isBSDFDelta(mat)) {
         V3 wi = v3s(0.0f); float dist = 0.0f, pdf = 0.0f, jac = 0.0f; V2 bary = v2(0.0f, 0.0f); uint32_t id = 0u;
         V3 Le = sampleLightByPower(P.sc, surf.pos, wi, dist, pdf, jac, bary, id, lr);
-        bool shadowed = traceShadowCall(P.sc, surf.pos, kMinRayDistance, wi, dist - kMinRayDistance, rc, err);
+        bool shadowed = tracer.shadow(P, surf.pos, wi, dist - kMinRayDistance);
         if (!shadowed && pdf > 1e-6f) {
             float w = MISWeight(pdf, evalPdf(mat, surf.norm, wo, wi));
             if (P.set.sampleType == GRIS_DI_SAMPLE_LIGHT) w = 1.0f;
@@ -117,7 +127,7 @@ GD void di_sample_li(const DICtx& P, const Surf& surf, const Mat& mat, V3 wo, ui
     ps.isLight = 0u;
     BsdfSample s = bs_zero();
     if (P.set.sampleType != GRIS_DI_SAMPLE_LIGHT && sampleBSDF(mat, surf.albedo, surf.norm, wo, sr, s) && s.pdf > 1e-6f) {
-        Isec isec = traceClosestHitCall(P.sc, surf.pos, s.wi, kMinRayDistance, kMaxRayDistance, rc, err);
+        Isec isec = tracer.closest(P, surf.pos, s.wi);
         if (isec.inst != kInvalidHit) {
             Surf hit = surf_zero();
             loadSurfaceInfo(P.sc, isec, hit);
@@ -156,7 +166,8 @@ GD void di_replay(const DICtx& P, DIResv& dst, const Surf& ds, const DIResv& src
     Mat mat = load_material(P.sc, ds.matIndex);
     DIResv rr = di_zero();
     di_clear(rr);
-    di_sample_li(P, ds, mat, wo, src.s.rng, rng, rr, rc, err);
+    DITraceInline tracer{rc, err};
+    di_sample_li(P, ds, mat, wo, src.s.rng, rng, rr, tracer);
     if (rr.s.isec.inst != kInvalidHit) {
         Surf rs = surf_zero();
         loadSurfaceInfo(P.sc, rr.s.isec, rs);
@@ -260,7 +271,8 @@ __global__ void __launch_bounds__(128, 8) k_di_candidates(DICtx P) {
         uint32_t resvRng = ~rng;
         DIResv r = di_zero();
         di_clear(r);
-        di_sample_li(P, px.surf, load_material(P.sc, px.surf.matIndex), -px.ray.dir, rng, resvRng, r, rc, err);
+        DITraceInline tracer{rc, err};
+        di_sample_li(P, px.surf, load_material(P.sc, px.surf.matIndex), -px.ray.dir, rng, resvRng, r, tracer);
         store_di(P.b.reservoirThis, (uint64_t)y * P.b.width + x, r);
     }
     flush_counts(P.counters, rc, err, 4, P.countWork);
@@ -663,6 +675,142 @@ __global__ void __launch_bounds__(128, 8) k_di_spatial_finish(DICtx P, DISplit S
     flush_counts(P.counters, rc, err, 6, P.countWork);
 }
 
+/* The candidates pass in three launches: prepare (per pixel the light and BSDF samples, their
+ * shadow and closest-hit queries appended to two queues), the resident walks of the two queues,
+ * and finish (the same samples drawn again, the walks' answers in place of the inline queries,
+ * the candidate stream as before). */
+struct DICandidates {
+    float4* qS;          /* shadow queries: origin | tmax, direction | pixel */
+    float4* qC;          /* closest-hit queries: origin | 0, direction | pixel */
+    uint8_t* blocked;    /* per pixel: the shadow query's answer */
+    Isec* hit;           /* per pixel: the closest-hit query's answer */
+    uint32_t* counts;    /* [0] shadow queries, [1] cursor, [2] closest-hit queries, [3] cursor */
+};
+struct DITraceQueue {
+    bool wantS = false, wantC = false;
+    float4 s0, s1, c0, c1;
+    uint32_t pix;
+    GD bool shadow(const DICtx&, V3 o, V3 d, float tmax) {
+        wantS = true;
+        s0 = make_float4(o.x, o.y, o.z, tmax); s1 = make_float4(d.x, d.y, d.z, __uint_as_float(pix));
+        return true;   /* the prepare pass draws the same numbers whatever the answer */
+    }
+    GD Isec closest(const DICtx&, V3 o, V3 d) {
+        wantC = true;
+        c0 = make_float4(o.x, o.y, o.z, 0.0f); c1 = make_float4(d.x, d.y, d.z, __uint_as_float(pix));
+        Isec r; r.bx = 0.0f; r.by = 0.0f; r.inst = kInvalidHit; r.tri = 0u;
+        return r;
+    }
+};
+struct DITraceAnswer {
+    const DICandidates& Q;
+    uint32_t pix;
+    GD bool shadow(const DICtx&, V3, V3, float) { return Q.blocked[pix] != 0u; }
+    GD Isec closest(const DICtx&, V3, V3) { return Q.hit[pix]; }
+};
+
+/* appends `want` lanes' records to a queue, one atomic per warp (all lanes call) */
+GD void di_push(float4* q, uint32_t* count, bool want, float4 a, float4 b) {
+    const unsigned m = __ballot_sync(0xffffffffu, want);
+    if (!m) return;
+    const uint32_t lane = (threadIdx.y * blockDim.x + threadIdx.x) & 31u, leader = (uint32_t)__ffs(m) - 1u;
+    uint32_t base = 0u;
+    if (lane == leader) base = atomicAdd(count, (uint32_t)__popc(m));
+    base = __shfl_sync(0xffffffffu, base, leader);
+    if (want) {
+        const uint32_t i = base + (uint32_t)__popc(m & ((1u << lane) - 1u));
+        q[2 * (uint64_t)i] = a;
+        q[2 * (uint64_t)i + 1] = b;
+    }
+}
+
+__global__ void __launch_bounds__(128, 8) k_di_candidates_prepare(DICtx P, DICandidates Q) {
+    const uint32_t x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y * blockDim.y + threadIdx.y;
+    DITraceQueue tr;
+    tr.pix = y * P.b.width + x;
+    DIPixel px;
+    if (x < P.b.width && y < P.b.height && di_pixel(P, x, y, px)) {
+        uint32_t rng = makeSeed2(P.cam.seed, x, y);
+        uint32_t resvRng = ~rng;
+        DIResv r = di_zero();
+        di_clear(r);
+        di_sample_li(P, px.surf, load_material(P.sc, px.surf.matIndex), -px.ray.dir, rng, resvRng, r, tr);
+    }
+    di_push(Q.qS, Q.counts + 0, tr.wantS, tr.s0, tr.s1);
+    di_push(Q.qC, Q.counts + 2, tr.wantC, tr.c0, tr.c1);
+}
+
+/* the resident walk of a candidates queue (ANY: shadow queries; else closest hits) */
+template <bool ANY>
+__global__ void __launch_bounds__(128, 7) k_di_candidates_walk(DICtx P, DICandidates Q) {
+    const uint32_t n = Q.counts[ANY ? 0 : 2];
+    uint32_t* cursor = Q.counts + (ANY ? 1 : 3);
+    const float4* q = ANY ? Q.qS : Q.qC;
+    const uint32_t lane = threadIdx.x & 31u;
+    RayCount rc = ray_count();
+    int err = 0;
+    GrisTraversal<ANY> tr;
+    __shared__ uint32_t sStack[2 * kDIWalkShared * 128];
+    GrisShortStack<kDIWalkShared> stack;
+    stack.bind(sStack, threadIdx.x, 128u);
+    uint32_t pix = 0u;
+    bool active = false, more = true;
+    while (true) {
+        const unsigned idle = __ballot_sync(0xffffffffu, !active);
+        if (more && __popc(idle) >= 8) {
+            const uint32_t take = (uint32_t)__popc(idle), leader = __ffs(idle) - 1;
+            uint32_t base = 0;
+            if (lane == leader) base = atomicAdd(cursor, take);
+            base = __shfl_sync(0xffffffffu, base, leader);
+            if (!active) {
+                const uint32_t i = base + (uint32_t)__popc(idle & ((1u << lane) - 1u));
+                if (i < n) {
+                    const float4 a = q[2 * (uint64_t)i], b = q[2 * (uint64_t)i + 1];
+                    pix = __float_as_uint(b.w);
+                    stack.reset();
+                    tr.init(a.x, a.y, a.z, b.x, b.y, b.z, kMinRayDistance, ANY ? a.w : kMaxRayDistance);
+                    active = true;
+                }
+            }
+            if (base + take >= n) more = false;
+        }
+        if (__ballot_sync(0xffffffffu, active) == 0u) {
+            if (!more) break;
+            continue;
+        }
+        if (active && !tr.template step<(ANY ? kDIWalkTris : 0)>(P.sc.nodes, P.sc.tris, false, &err, stack)) {
+            GrisRayHit h;
+            tr.result(&h, &rc.work);
+            if (ANY) {
+                rc.shadow++;
+                Q.blocked[pix] = tr.found ? 1u : 0u;
+            } else {
+                rc.closest++;
+                Isec r;
+                if (tr.found) { r.bx = h.u; r.by = h.v; r.inst = h.inst; r.tri = h.tri; }
+                else { r.bx = 0.0f; r.by = 0.0f; r.inst = kInvalidHit; r.tri = 0u; }
+                Q.hit[pix] = r;
+            }
+            active = false;
+        }
+    }
+    flush_counts(P.counters, rc, err, 4, P.countWork);
+}
+
+__global__ void __launch_bounds__(128, 8) k_di_candidates_finish(DICtx P, DICandidates Q) {
+    uint32_t x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y * blockDim.y + threadIdx.y;
+    DIPixel px;
+    if (x < P.b.width && y < P.b.height && di_pixel(P, x, y, px)) {
+        uint32_t rng = makeSeed2(P.cam.seed, x, y);
+        uint32_t resvRng = ~rng;
+        DIResv r = di_zero();
+        di_clear(r);
+        DITraceAnswer tr{Q, y * P.b.width + x};
+        di_sample_li(P, px.surf, load_material(P.sc, px.surf.matIndex), -px.ray.dir, rng, resvRng, r, tr);
+        store_di(P.b.reservoirThis, (uint64_t)y * P.b.width + x, r);
+    }
+}
+
 size_t di_split_bytes_per_pixel() {
     return sizeof(float4) + sizeof(uint32_t) +
            kDINeighbours * (sizeof(float4) + sizeof(uint2) + sizeof(float4) + 1 + sizeof(uint32_t));
@@ -680,9 +828,28 @@ cudaError_t launch_di(const DeviceSceneView& scene, const GrisDIBindings& b, con
     P.counters = counters;
     P.countWork = countWork;
     dim3 block(16, 8), grid((b.width + 15) / 16, (b.height + 7) / 8);
+    const uint64_t npx = (uint64_t)b.width * b.height;
     if (passes & 1) {
         if (timer) timer->mark(GRIS_SLOT_DI_CANDIDATES, true, stream);
-        k_di_candidates<<<grid, block, 0, stream>>>(P);
+        if (split && splitPixels >= npx) {
+            /* the scratch as two queues of 32-byte queries, the answers per pixel */
+            DICandidates Q;
+            unsigned char* c = reinterpret_cast<unsigned char*>(split);
+            Q.counts = reinterpret_cast<uint32_t*>(c); c += 256;
+            Q.qS = reinterpret_cast<float4*>(c); c += npx * 2 * sizeof(float4);
+            Q.qC = reinterpret_cast<float4*>(c); c += npx * 2 * sizeof(float4);
+            Q.hit = reinterpret_cast<Isec*>(c); c += npx * sizeof(Isec);
+            Q.blocked = reinterpret_cast<uint8_t*>(c);
+            cudaError_t e = cudaMemsetAsync(Q.counts, 0, 4 * sizeof(uint32_t), stream);
+            if (e != cudaSuccess) return e;
+            const int gridWalk = current_sm_count() * 16;
+            k_di_candidates_prepare<<<grid, block, 0, stream>>>(P, Q);
+            k_di_candidates_walk<true><<<gridWalk, 128, 0, stream>>>(P, Q);
+            k_di_candidates_walk<false><<<gridWalk, 128, 0, stream>>>(P, Q);
+            k_di_candidates_finish<<<grid, block, 0, stream>>>(P, Q);
+        } else {
+            k_di_candidates<<<grid, block, 0, stream>>>(P);
+        }
         if (timer) timer->mark(GRIS_SLOT_DI_CANDIDATES, false, stream);
     }
     if (passes & 2) {

@@ -39,8 +39,8 @@ cudaError_t launch_gris(const DeviceSceneView& scene, const GrisPassBindings& b,
                         const GrisCamera& prevCam, const GrisSettings& set, int passes, unsigned long long* counters,
                         int countWork, KernelTimer* timer, cudaStream_t stream, int launchMode = GRIS_LAUNCH_PERSISTENT);
 /* ReSTIR DI (TestReSTIR::render): passes bit 0 candidates, bit 1 temporal, bit 2 spatial */
-/* split: scratch of di_split_bytes_per_pixel() * splitPixels + 256 bytes for the spatial pass in
- * three launches (null or too small: the single spatial kernel) */
+/* split: scratch of di_split_bytes_per_pixel() * splitPixels + 256 bytes for the candidates and
+ * spatial passes in three launches (null or too small: their single kernels) */
 cudaError_t launch_di(const DeviceSceneView& scene, const GrisDIBindings& b, const GrisCamera& cam,
                       const GrisCamera& prevCam, const GrisDISettings& set, int passes, unsigned long long* counters,
                       int countWork, KernelTimer* timer, cudaStream_t stream, void* split = nullptr,
