@@ -515,15 +515,14 @@ __global__ void __launch_bounds__(128, 8) k_di_spatial(DICtx P) {
     flush_counts(P.counters, rc, err, 6, P.countWork);
 }
 
-/* ------------------------------------------------------------------ spatial pass as five launches */
+/* ------------------------------------------------------------------ spatial pass in three launches */
 /* With the reconnection shift the spatial pass runs as prepare (per pixel: the ten neighbours'
  * shifts up to their visibility queries, di_spatial_shift, each neighbour's record kept in slot k
  * of pixel p at k * P + p and its query appended to a queue of slots), the refilling any-hit walk
- * of that queue (a visible segment sets its slot's verdict), merge (the merges in neighbour order
- * with the verdicts, the final occlusion query queued), the same walk of those queries, and final
- * (the occlusion verdict, the cap and the running mean): the operations of k_di_spatial in the
- * same order, each query answered as traceVisibility answers it. A warp's queries no longer wait
- * for the longest walk among them. */
+ * of that queue (a visible segment sets its slot's verdict) and finish (the merges in neighbour
+ * order with the verdicts, the final occlusion test, the cap and the running mean): the
+ * operations of k_di_spatial in the same order, each query answered as traceVisibility answers
+ * it. A warp's queries no longer wait for the longest walk among them. */
 struct DISplit {
     float4* from;        /* per pixel: its primary vertex */
     uint32_t* mq;        /* per pixel: neighbour records | query bits << 8 */
@@ -628,15 +627,17 @@ __global__ void __launch_bounds__(128, 7) k_di_visibility(DICtx P, DISplit S) {
     flush_counts(P.counters, rc, err, 6, P.countWork);
 }
 
-/* the merges in neighbour order with the verdicts; the merged reservoir is kept in the current
- * one and the final occlusion query (di_occlude's) appended to the emptied queue, slot p */
-__global__ void __launch_bounds__(128, 8) k_di_spatial_merge(DICtx P, DISplit S) {
+__global__ void __launch_bounds__(128, 8) k_di_spatial_finish(DICtx P, DISplit S) {
+    RayCount rc = ray_count();
+    int err = 0;
     const uint32_t x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y * blockDim.y + threadIdx.y;
+    if (x >= P.b.width || y >= P.b.height) return;
     const int W = (int)P.b.width, H = (int)P.b.height;
     const uint64_t n = (uint64_t)W * (uint64_t)H, idx = (uint64_t)y * W + x;
-    bool query = false;
     DIPixel px;
-    if (x < P.b.width && y < P.b.height && di_pixel(P, x, y, px)) {
+    V3 color = v3s(0.0f);
+    if (di_pixel(P, x, y, px)) {
+        const V3 wo = -px.ray.dir;
         DIResv r = load_di(P.b.reservoirTemp, idx, n);
         const uint32_t mq = S.mq[idx], m = mq & 0xffu, queries = mq >> 8;
         DINeighbour nb[kDINeighbours];
@@ -650,38 +651,7 @@ __global__ void __launch_bounds__(128, 8) k_di_spatial_merge(DICtx P, DISplit S)
             if (((queries >> i) & 1u) && S.vis[s]) visible |= 1u << i;
         }
         di_spatial_merge(P, nb, m, visible, r);
-        store_di(P.b.reservoirThis, idx, r);
-        if (di_usable(r) && r.s.isec.inst != kInvalidHit) {   /* di_occlude's query */
-            Surf ls = surf_zero();
-            loadSurfaceInfo(P.sc, r.s.isec, ls);
-            S.recTo[idx] = make_float4(ls.pos.x, ls.pos.y, ls.pos.z, 0.0f);
-            S.vis[idx] = 0u;
-            query = true;
-        }
-    }
-    const uint32_t lane = (threadIdx.y * blockDim.x + threadIdx.x) & 31u;
-    const unsigned qm = __ballot_sync(0xffffffffu, query);
-    if (qm) {
-        const uint32_t leader = (uint32_t)__ffs(qm) - 1u;
-        uint32_t base = 0u;
-        if (lane == leader) base = atomicAdd(S.counts, (uint32_t)__popc(qm));
-        base = __shfl_sync(0xffffffffu, base, leader);
-        if (query) S.queue[base + (uint32_t)__popc(qm & ((1u << lane) - 1u))] = (uint32_t)idx;
-    }
-}
-
-/* di_occlude with the walk's verdict, the cap, the running mean (di_spatial.comp:21-26) */
-__global__ void __launch_bounds__(128, 8) k_di_spatial_final(DICtx P, DISplit S) {
-    const uint32_t x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y * blockDim.y + threadIdx.y;
-    if (x >= P.b.width || y >= P.b.height) return;
-    const int W = (int)P.b.width, H = (int)P.b.height;
-    const uint64_t n = (uint64_t)W * (uint64_t)H, idx = (uint64_t)y * W + x;
-    DIPixel px;
-    V3 color = v3s(0.0f);
-    if (di_pixel(P, x, y, px)) {
-        const V3 wo = -px.ray.dir;
-        DIResv r = load_di(P.b.reservoirThis, idx, n);
-        if (di_usable(r) && r.s.isec.inst != kInvalidHit && !S.vis[idx]) r.W = 0.0f;
+        di_occlude(P, r, px.surf.pos, rc, err);
         di_cap(r, kDICap);
         if (!di_usable(r)) di_clear(r);
         store_di(P.b.reservoirThis, idx, r);
@@ -702,6 +672,7 @@ __global__ void __launch_bounds__(128, 8) k_di_spatial_final(DICtx P, DISplit S)
     float4 o = *out;
     V3 acc = (v3(o.x, o.y, o.z) * frameCount + color) / (frameCount + 1.0f);
     *out = make_float4(acc.x, acc.y, acc.z, 1.0f);
+    flush_counts(P.counters, rc, err, 6, P.countWork);
 }
 
 /* The candidates pass in three launches: prepare (per pixel the light and BSDF samples, their
@@ -906,14 +877,9 @@ cudaError_t launch_di(const DeviceSceneView& scene, const GrisDIBindings& b, con
             S.P = px;
             cudaError_t e = cudaMemsetAsync(S.counts, 0, 2 * sizeof(uint32_t), stream);
             if (e != cudaSuccess) return e;
-            const int gridWalk = current_sm_count() * 16;
             k_di_spatial_prepare<<<grid, block, 0, stream>>>(P, S);
-            k_di_visibility<<<gridWalk, 128, 0, stream>>>(P, S);
-            /* the queue again, for the final occlusion queries (slot = pixel) */
-            if ((e = cudaMemsetAsync(S.counts, 0, 2 * sizeof(uint32_t), stream)) != cudaSuccess) return e;
-            k_di_spatial_merge<<<grid, block, 0, stream>>>(P, S);
-            k_di_visibility<<<gridWalk, 128, 0, stream>>>(P, S);
-            k_di_spatial_final<<<grid, block, 0, stream>>>(P, S);
+            k_di_visibility<<<current_sm_count() * 16, 128, 0, stream>>>(P, S);
+            k_di_spatial_finish<<<grid, block, 0, stream>>>(P, S);
         } else {
             k_di_spatial<<<grid, block, 0, stream>>>(P);
         }
