@@ -184,8 +184,15 @@ GD void di_replay(const DICtx& P, DIResv& dst, const Surf& ds, const DIResv& src
 
 /* reconnection (di_reservoir.glsl:211-287): the source's light vertex seen from the destination
  * (one visibility ray), Jacobian (|cos| / d^2)_dst / jacobian_src. */
-GD void di_reconnect(const DICtx& P, DIResv& dst, const Surf& ds, DIResv src, V3 wo, uint32_t& rng, RayCount& rc,
-                     int& err) {
+/* the reconnection's visibility query, answered on the spot */
+struct DIVisInline {
+    RayCount& rc;
+    int& err;
+    GD bool visible(const DICtx& P, V3 from, V3 to) { return traceVisibility(P.sc, from, to, rc, err); }
+};
+
+template <class Vis>
+GD void di_reconnect(const DICtx& P, DIResv& dst, const Surf& ds, DIResv src, V3 wo, uint32_t& rng, Vis& vis) {
     Mat mat = load_material(P.sc, ds.matIndex);
     DISample ss = src.s;
     Surf lv = surf_zero();
@@ -199,7 +206,7 @@ GD void di_reconnect(const DICtx& P, DIResv& dst, const Surf& ds, DIResv src, V3
     float pHat = 0.0f, dstPdf = 0.0f;
     if (ss.isec.inst != kInvalidHit && dist > 1e-4f) {
         if (cosT > 0.0f && !isnan(jac) && ss.jac > 0.0f) {
-            if (traceVisibility(P.sc, ds.pos, lv.pos, rc, err)) {
+            if (vis.visible(P, ds.pos, lv.pos)) {
                 ok = true;
                 if (!isnan(ss.pdf) && ss.pdf > 1e-6f) {
                     V3 Li = src.s.Li * evalBSDF(mat, ds.albedo, ds.norm, wo, wi) * satDot(ds.norm, wi) / ss.pdf;
@@ -226,8 +233,12 @@ GD void di_reconnect(const DICtx& P, DIResv& dst, const Surf& ds, DIResv src, V3
 /* DIReservoirReuseAndMerge (di_reservoir.glsl:289-296) */
 GD void di_reuse(const DICtx& P, DIResv& dst, const Surf& ds, const DIResv& src, V3 wo, uint32_t& rng, RayCount& rc,
                  int& err) {
-    if (P.set.shiftType == GRIS_DI_SHIFT_RECONNECTION) di_reconnect(P, dst, ds, src, wo, rng, rc, err);
-    else if (P.set.shiftType == GRIS_DI_SHIFT_REPLAY) di_replay(P, dst, ds, src, wo, rng, rc, err);
+    if (P.set.shiftType == GRIS_DI_SHIFT_RECONNECTION) {
+        DIVisInline vis{rc, err};
+        di_reconnect(P, dst, ds, src, wo, rng, vis);
+    } else if (P.set.shiftType == GRIS_DI_SHIFT_REPLAY) {
+        di_replay(P, dst, ds, src, wo, rng, rc, err);
+    }
 }
 
 /* The final sample's visibility in both reuse passes (di_temporal.glsl:76-85, di_spatial.glsl:84-93). */
@@ -279,6 +290,27 @@ __global__ void __launch_bounds__(128, 8) k_di_candidates(DICtx P) {
 }
 
 /* findPreviousReservoir (di_temporal.glsl:9-34) + temporalReuse (:36-90) */
+/* The temporal neighbour of pixel (x, y) (di_temporal.glsl:36-74: reprojection, the previous
+ * G-buffer's checks): true with its reservoir in src when it is found and usable. */
+GD bool di_temporal_source(const DICtx& P, uint32_t x, uint32_t y, const DIPixel& px, DIResv& src) {
+    const int W = (int)P.b.width, H = (int)P.b.height;
+    const uint64_t n = (uint64_t)W * (uint64_t)H, idx = (uint64_t)y * W + x;
+    float2 motion = __half22float2(reinterpret_cast<const __half2*>(P.b.motion)[idx]);
+    V2 puv = v2(px.uv.x + motion.x, px.uv.y + motion.y);
+    if ((P.cam.frameIndex & kCameraClearFlag) != 0u || puv.x < 0.0f || puv.y < 0.0f || puv.x > 1.0f || puv.y > 1.0f)
+        return false;
+    int qx = (int)(puv.x * (float)P.cam.w), qy = (int)(puv.y * (float)P.cam.h);
+    float pdepth = 0.0f; V3 pn = v3s(0.0f), palb = v3s(0.0f); int pmm = 0;
+    float4 pdn = texture_bilinear(reinterpret_cast<const float4*>(P.b.depthNormalPrev), W, H, puv);
+    uint2 pam = fetch_am(reinterpret_cast<const uint2*>(P.b.albedoMatIdPrev), W, H, qx, qy);
+    if (!unpackGBuffer(pdn, pam, pdepth, pn, palb, pmm)) return false;
+    Ray3 pray = pinholeCameraSampleRay(P.prev, v2(puv.x, 1.0f - puv.y));
+    V3 ppos = pray.ori + pray.dir * (pdepth - 1e-4f);
+    if (pmm != px.matMeshId || dot3(pn, px.surf.norm) < 0.95f || distance3(px.surf.pos, ppos) > 0.5f) return false;
+    src = load_di(P.b.reservoirPrev, (uint64_t)((uint32_t)P.cam.w * (uint32_t)qy + (uint32_t)qx), n);
+    return di_usable(src);
+}
+
 __global__ void __launch_bounds__(128, 8) k_di_temporal(DICtx P) {
     RayCount rc = ray_count();
     int err = 0;
@@ -287,25 +319,11 @@ __global__ void __launch_bounds__(128, 8) k_di_temporal(DICtx P) {
     if (x < P.b.width && y < P.b.height && di_pixel(P, x, y, px)) {
         const int W = (int)P.b.width, H = (int)P.b.height;
         const uint64_t n = (uint64_t)W * (uint64_t)H, idx = (uint64_t)y * W + x;
-        float2 motion = __half22float2(reinterpret_cast<const __half2*>(P.b.motion)[idx]);
         uint32_t resvRng = ~(makeSeed2(P.cam.seed, x, y) ^ 1u);
         DIResv r = load_di(P.b.reservoirThis, idx, n);
         if (P.set.temporalReuse) {
-            V2 puv = v2(px.uv.x + motion.x, px.uv.y + motion.y);
-            if ((P.cam.frameIndex & kCameraClearFlag) == 0u && !(puv.x < 0.0f || puv.y < 0.0f || puv.x > 1.0f || puv.y > 1.0f)) {
-                int qx = (int)(puv.x * (float)P.cam.w), qy = (int)(puv.y * (float)P.cam.h);
-                float pdepth = 0.0f; V3 pn = v3s(0.0f), palb = v3s(0.0f); int pmm = 0;
-                float4 pdn = texture_bilinear(reinterpret_cast<const float4*>(P.b.depthNormalPrev), W, H, puv);
-                uint2 pam = fetch_am(reinterpret_cast<const uint2*>(P.b.albedoMatIdPrev), W, H, qx, qy);
-                if (unpackGBuffer(pdn, pam, pdepth, pn, palb, pmm)) {
-                    Ray3 pray = pinholeCameraSampleRay(P.prev, v2(puv.x, 1.0f - puv.y));
-                    V3 ppos = pray.ori + pray.dir * (pdepth - 1e-4f);
-                    if (!(pmm != px.matMeshId || dot3(pn, px.surf.norm) < 0.95f || distance3(px.surf.pos, ppos) > 0.5f)) {
-                        DIResv src = load_di(P.b.reservoirPrev, (uint64_t)((uint32_t)P.cam.w * (uint32_t)qy + (uint32_t)qx), n);
-                        if (di_usable(src)) di_reuse(P, r, px.surf, src, -px.ray.dir, resvRng, rc, err);
-                    }
-                }
-            }
+            DIResv src;
+            if (di_temporal_source(P, x, y, px, src)) di_reuse(P, r, px.surf, src, -px.ray.dir, resvRng, rc, err);
             di_occlude(P, r, px.surf.pos, rc, err);
         }
         di_cap(r, kDICap);
@@ -675,6 +693,93 @@ __global__ void __launch_bounds__(128, 8) k_di_spatial_finish(DICtx P, DISplit S
     flush_counts(P.counters, rc, err, 6, P.countWork);
 }
 
+/* The temporal pass in five launches (reconnection shift, temporal reuse on): prepare (per pixel
+ * the temporal neighbour and its reconnection up to the visibility query, queued, slot = pixel),
+ * its walk, merge (the reconnection with the walk's verdict, the merge, the final occlusion query
+ * queued), its walk and final (the occlusion verdict, the cap): k_di_temporal's operations in the
+ * same order. */
+struct DIVisQueue {
+    DISplit& S;
+    uint64_t idx;
+    bool want;
+    GD bool visible(const DICtx&, V3 from, V3 to) {
+        S.from[idx] = make_float4(from.x, from.y, from.z, 0.0f);
+        S.recTo[idx] = make_float4(to.x, to.y, to.z, 0.0f);
+        S.vis[idx] = 0u;
+        want = true;
+        return false;   /* the prepare pass's own merge is not kept */
+    }
+};
+struct DIVisAnswer {
+    const DISplit& S;
+    uint64_t idx;
+    GD bool visible(const DICtx&, V3, V3) { return S.vis[idx] != 0u; }
+};
+
+/* appends `want` lanes' pixels to the split queue, one atomic per warp (all lanes call) */
+GD void di_push_slot(DISplit& S, bool want, uint32_t slot) {
+    const unsigned m = __ballot_sync(0xffffffffu, want);
+    if (!m) return;
+    const uint32_t lane = (threadIdx.y * blockDim.x + threadIdx.x) & 31u, leader = (uint32_t)__ffs(m) - 1u;
+    uint32_t base = 0u;
+    if (lane == leader) base = atomicAdd(S.counts, (uint32_t)__popc(m));
+    base = __shfl_sync(0xffffffffu, base, leader);
+    if (want) S.queue[base + (uint32_t)__popc(m & ((1u << lane) - 1u))] = slot;
+}
+
+__global__ void __launch_bounds__(128, 8) k_di_temporal_prepare(DICtx P, DISplit S) {
+    const uint32_t x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y * blockDim.y + threadIdx.y;
+    const uint64_t idx = (uint64_t)y * P.b.width + x;
+    DIVisQueue vis{S, idx, false};
+    DIPixel px;
+    if (x < P.b.width && y < P.b.height && di_pixel(P, x, y, px)) {
+        uint32_t resvRng = ~(makeSeed2(P.cam.seed, x, y) ^ 1u);
+        DIResv r = load_di(P.b.reservoirThis, idx, (uint64_t)P.b.width * P.b.height);
+        DIResv src;
+        if (di_temporal_source(P, x, y, px, src)) di_reconnect(P, r, px.surf, src, -px.ray.dir, resvRng, vis);
+    }
+    di_push_slot(S, vis.want, (uint32_t)idx);
+}
+
+__global__ void __launch_bounds__(128, 8) k_di_temporal_merge(DICtx P, DISplit S) {
+    const uint32_t x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y * blockDim.y + threadIdx.y;
+    const uint64_t n = (uint64_t)P.b.width * P.b.height, idx = (uint64_t)y * P.b.width + x;
+    bool query = false;
+    DIPixel px;
+    if (x < P.b.width && y < P.b.height && di_pixel(P, x, y, px)) {
+        uint32_t resvRng = ~(makeSeed2(P.cam.seed, x, y) ^ 1u);
+        DIResv r = load_di(P.b.reservoirThis, idx, n);
+        DIResv src;
+        if (di_temporal_source(P, x, y, px, src)) {
+            DIVisAnswer vis{S, idx};
+            di_reconnect(P, r, px.surf, src, -px.ray.dir, resvRng, vis);
+        }
+        store_di(P.b.reservoirTemp, idx, r);
+        if (di_usable(r) && r.s.isec.inst != kInvalidHit) {   /* di_occlude's query */
+            Surf ls = surf_zero();
+            loadSurfaceInfo(P.sc, r.s.isec, ls);
+            S.from[idx] = make_float4(px.surf.pos.x, px.surf.pos.y, px.surf.pos.z, 0.0f);
+            S.recTo[idx] = make_float4(ls.pos.x, ls.pos.y, ls.pos.z, 0.0f);
+            S.vis[idx] = 0u;
+            query = true;
+        }
+    }
+    di_push_slot(S, query, (uint32_t)idx);
+}
+
+__global__ void __launch_bounds__(128, 8) k_di_temporal_final(DICtx P, DISplit S) {
+    const uint32_t x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y * blockDim.y + threadIdx.y;
+    if (x >= P.b.width || y >= P.b.height) return;
+    const uint64_t n = (uint64_t)P.b.width * P.b.height, idx = (uint64_t)y * P.b.width + x;
+    DIPixel px;
+    if (!di_pixel(P, x, y, px)) return;
+    DIResv r = load_di(P.b.reservoirTemp, idx, n);
+    if (di_usable(r) && r.s.isec.inst != kInvalidHit && !S.vis[idx]) r.W = 0.0f;
+    di_cap(r, kDICap);
+    if (!di_usable(r)) di_clear(r);
+    store_di(P.b.reservoirTemp, idx, r);
+}
+
 /* The candidates pass in three launches: prepare (per pixel the light and BSDF samples, their
  * shadow and closest-hit queries appended to two queues), the resident walks of the two queues,
  * and finish (the same samples drawn again, the walks' answers in place of the inline queries,
@@ -829,9 +934,28 @@ cudaError_t launch_di(const DeviceSceneView& scene, const GrisDIBindings& b, con
     P.countWork = countWork;
     dim3 block(16, 8), grid((b.width + 15) / 16, (b.height + 7) / 8);
     const uint64_t npx = (uint64_t)b.width * b.height;
+    const bool haveSplit = split && splitPixels >= npx;
+    const int gridWalk = current_sm_count() * 16;
+    /* the reuse passes' carving of the scratch: per pixel from, mq; per slot recA, recTo, recB,
+     * vis, queue (slot k of pixel p at k * P + p; the temporal pass uses slot p only) */
+    DISplit S;
+    memset(&S, 0, sizeof(S));
+    if (haveSplit) {
+        unsigned char* c = reinterpret_cast<unsigned char*>(split);
+        const uint64_t slots = (uint64_t)kDINeighbours * npx;
+        S.counts = reinterpret_cast<uint32_t*>(c); c += 256;
+        S.from = reinterpret_cast<float4*>(c); c += npx * sizeof(float4);
+        S.recA = reinterpret_cast<float4*>(c); c += slots * sizeof(float4);
+        S.recTo = reinterpret_cast<float4*>(c); c += slots * sizeof(float4);
+        S.recB = reinterpret_cast<uint2*>(c); c += slots * sizeof(uint2);
+        S.mq = reinterpret_cast<uint32_t*>(c); c += npx * sizeof(uint32_t);
+        S.queue = reinterpret_cast<uint32_t*>(c); c += slots * sizeof(uint32_t);
+        S.vis = reinterpret_cast<uint8_t*>(c);
+        S.P = npx;
+    }
     if (passes & 1) {
         if (timer) timer->mark(GRIS_SLOT_DI_CANDIDATES, true, stream);
-        if (split && splitPixels >= npx) {
+        if (haveSplit) {
             /* the scratch as two queues of 32-byte queries, the answers per pixel */
             DICandidates Q;
             unsigned char* c = reinterpret_cast<unsigned char*>(split);
@@ -842,7 +966,6 @@ cudaError_t launch_di(const DeviceSceneView& scene, const GrisDIBindings& b, con
             Q.blocked = reinterpret_cast<uint8_t*>(c);
             cudaError_t e = cudaMemsetAsync(Q.counts, 0, 4 * sizeof(uint32_t), stream);
             if (e != cudaSuccess) return e;
-            const int gridWalk = current_sm_count() * 16;
             k_di_candidates_prepare<<<grid, block, 0, stream>>>(P, Q);
             k_di_candidates_walk<true><<<gridWalk, 128, 0, stream>>>(P, Q);
             k_di_candidates_walk<false><<<gridWalk, 128, 0, stream>>>(P, Q);
@@ -854,27 +977,24 @@ cudaError_t launch_di(const DeviceSceneView& scene, const GrisDIBindings& b, con
     }
     if (passes & 2) {
         if (timer) timer->mark(GRIS_SLOT_DI_TEMPORAL, true, stream);
-        k_di_temporal<<<grid, block, 0, stream>>>(P);
+        if (haveSplit && set.temporalReuse && set.shiftType == GRIS_DI_SHIFT_RECONNECTION) {
+            cudaError_t e = cudaMemsetAsync(S.counts, 0, 2 * sizeof(uint32_t), stream);
+            if (e != cudaSuccess) return e;
+            k_di_temporal_prepare<<<grid, block, 0, stream>>>(P, S);
+            k_di_visibility<<<gridWalk, 128, 0, stream>>>(P, S);
+            if ((e = cudaMemsetAsync(S.counts, 0, 2 * sizeof(uint32_t), stream)) != cudaSuccess) return e;
+            k_di_temporal_merge<<<grid, block, 0, stream>>>(P, S);
+            k_di_visibility<<<gridWalk, 128, 0, stream>>>(P, S);
+            k_di_temporal_final<<<grid, block, 0, stream>>>(P, S);
+        } else {
+            k_di_temporal<<<grid, block, 0, stream>>>(P);
+        }
         if (timer) timer->mark(GRIS_SLOT_DI_TEMPORAL, false, stream);
     }
     if (passes & 4) {
         if (timer) timer->mark(GRIS_SLOT_DI_SPATIAL, true, stream);
-        const uint64_t px = (uint64_t)b.width * b.height;
         const bool phased = set.spatialReuse && set.shiftType == GRIS_DI_SHIFT_RECONNECTION;
-        if (phased && split && splitPixels >= px) {
-            /* carve the scratch: per pixel from, mq; per slot recA, recTo, recB, vis, queue */
-            DISplit S;
-            unsigned char* c = reinterpret_cast<unsigned char*>(split);
-            const uint64_t slots = (uint64_t)kDINeighbours * px;
-            S.counts = reinterpret_cast<uint32_t*>(c); c += 256;
-            S.from = reinterpret_cast<float4*>(c); c += px * sizeof(float4);
-            S.recA = reinterpret_cast<float4*>(c); c += slots * sizeof(float4);
-            S.recTo = reinterpret_cast<float4*>(c); c += slots * sizeof(float4);
-            S.recB = reinterpret_cast<uint2*>(c); c += slots * sizeof(uint2);
-            S.mq = reinterpret_cast<uint32_t*>(c); c += px * sizeof(uint32_t);
-            S.queue = reinterpret_cast<uint32_t*>(c); c += slots * sizeof(uint32_t);
-            S.vis = reinterpret_cast<uint8_t*>(c);
-            S.P = px;
+        if (phased && haveSplit) {
             cudaError_t e = cudaMemsetAsync(S.counts, 0, 2 * sizeof(uint32_t), stream);
             if (e != cudaSuccess) return e;
             k_di_spatial_prepare<<<grid, block, 0, stream>>>(P, S);
