@@ -741,8 +741,7 @@ int grisPassDI(GrisContext* ctx, const GrisScene* s, const GrisDIBindings* b, co
     const uint64_t px = (uint64_t)b->width * b->height;
     cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
     cudaStreamIsCapturing(ctx->stream, &cap);
-    const bool split = (passes & 1) || (((passes & 4) || ((passes & 2) && set->temporalReuse)) &&
-                                        set->shiftType == GRIS_DI_SHIFT_RECONNECTION);
+    const bool split = (passes & 1) || ((passes & 4) && set->spatialReuse && set->shiftType == GRIS_DI_SHIFT_RECONNECTION);
     if (split && ctx->diSplitPixels < px && cap == cudaStreamCaptureStatusNone) {
         cudaStreamSynchronize(ctx->stream);
         if (ctx->diSplit) cudaFree(ctx->diSplit);

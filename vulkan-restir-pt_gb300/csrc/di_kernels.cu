@@ -693,93 +693,6 @@ __global__ void __launch_bounds__(128, 8) k_di_spatial_finish(DICtx P, DISplit S
     flush_counts(P.counters, rc, err, 6, P.countWork);
 }
 
-/* The temporal pass in five launches (reconnection shift, temporal reuse on): prepare (per pixel
- * the temporal neighbour and its reconnection up to the visibility query, queued, slot = pixel),
- * its walk, merge (the reconnection with the walk's verdict, the merge, the final occlusion query
- * queued), its walk and final (the occlusion verdict, the cap): k_di_temporal's operations in the
- * same order. */
-struct DIVisQueue {
-    DISplit& S;
-    uint64_t idx;
-    bool want;
-    GD bool visible(const DICtx&, V3 from, V3 to) {
-        S.from[idx] = make_float4(from.x, from.y, from.z, 0.0f);
-        S.recTo[idx] = make_float4(to.x, to.y, to.z, 0.0f);
-        S.vis[idx] = 0u;
-        want = true;
-        return false;   /* the prepare pass's own merge is not kept */
-    }
-};
-struct DIVisAnswer {
-    const DISplit& S;
-    uint64_t idx;
-    GD bool visible(const DICtx&, V3, V3) { return S.vis[idx] != 0u; }
-};
-
-/* appends `want` lanes' pixels to the split queue, one atomic per warp (all lanes call) */
-GD void di_push_slot(DISplit& S, bool want, uint32_t slot) {
-    const unsigned m = __ballot_sync(0xffffffffu, want);
-    if (!m) return;
-    const uint32_t lane = (threadIdx.y * blockDim.x + threadIdx.x) & 31u, leader = (uint32_t)__ffs(m) - 1u;
-    uint32_t base = 0u;
-    if (lane == leader) base = atomicAdd(S.counts, (uint32_t)__popc(m));
-    base = __shfl_sync(0xffffffffu, base, leader);
-    if (want) S.queue[base + (uint32_t)__popc(m & ((1u << lane) - 1u))] = slot;
-}
-
-__global__ void __launch_bounds__(128, 8) k_di_temporal_prepare(DICtx P, DISplit S) {
-    const uint32_t x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y * blockDim.y + threadIdx.y;
-    const uint64_t idx = (uint64_t)y * P.b.width + x;
-    DIVisQueue vis{S, idx, false};
-    DIPixel px;
-    if (x < P.b.width && y < P.b.height && di_pixel(P, x, y, px)) {
-        uint32_t resvRng = ~(makeSeed2(P.cam.seed, x, y) ^ 1u);
-        DIResv r = load_di(P.b.reservoirThis, idx, (uint64_t)P.b.width * P.b.height);
-        DIResv src;
-        if (di_temporal_source(P, x, y, px, src)) di_reconnect(P, r, px.surf, src, -px.ray.dir, resvRng, vis);
-    }
-    di_push_slot(S, vis.want, (uint32_t)idx);
-}
-
-__global__ void __launch_bounds__(128, 8) k_di_temporal_merge(DICtx P, DISplit S) {
-    const uint32_t x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y * blockDim.y + threadIdx.y;
-    const uint64_t n = (uint64_t)P.b.width * P.b.height, idx = (uint64_t)y * P.b.width + x;
-    bool query = false;
-    DIPixel px;
-    if (x < P.b.width && y < P.b.height && di_pixel(P, x, y, px)) {
-        uint32_t resvRng = ~(makeSeed2(P.cam.seed, x, y) ^ 1u);
-        DIResv r = load_di(P.b.reservoirThis, idx, n);
-        DIResv src;
-        if (di_temporal_source(P, x, y, px, src)) {
-            DIVisAnswer vis{S, idx};
-            di_reconnect(P, r, px.surf, src, -px.ray.dir, resvRng, vis);
-        }
-        store_di(P.b.reservoirTemp, idx, r);
-        if (di_usable(r) && r.s.isec.inst != kInvalidHit) {   /* di_occlude's query */
-            Surf ls = surf_zero();
-            loadSurfaceInfo(P.sc, r.s.isec, ls);
-            S.from[idx] = make_float4(px.surf.pos.x, px.surf.pos.y, px.surf.pos.z, 0.0f);
-            S.recTo[idx] = make_float4(ls.pos.x, ls.pos.y, ls.pos.z, 0.0f);
-            S.vis[idx] = 0u;
-            query = true;
-        }
-    }
-    di_push_slot(S, query, (uint32_t)idx);
-}
-
-__global__ void __launch_bounds__(128, 8) k_di_temporal_final(DICtx P, DISplit S) {
-    const uint32_t x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y * blockDim.y + threadIdx.y;
-    if (x >= P.b.width || y >= P.b.height) return;
-    const uint64_t n = (uint64_t)P.b.width * P.b.height, idx = (uint64_t)y * P.b.width + x;
-    DIPixel px;
-    if (!di_pixel(P, x, y, px)) return;
-    DIResv r = load_di(P.b.reservoirTemp, idx, n);
-    if (di_usable(r) && r.s.isec.inst != kInvalidHit && !S.vis[idx]) r.W = 0.0f;
-    di_cap(r, kDICap);
-    if (!di_usable(r)) di_clear(r);
-    store_di(P.b.reservoirTemp, idx, r);
-}
-
 /* The candidates pass in three launches: prepare (per pixel the light and BSDF samples, their
  * shadow and closest-hit queries appended to two queues), the resident walks of the two queues,
  * and finish (the same samples drawn again, the walks' answers in place of the inline queries,
@@ -936,8 +849,8 @@ cudaError_t launch_di(const DeviceSceneView& scene, const GrisDIBindings& b, con
     const uint64_t npx = (uint64_t)b.width * b.height;
     const bool haveSplit = split && splitPixels >= npx;
     const int gridWalk = current_sm_count() * 16;
-    /* the reuse passes' carving of the scratch: per pixel from, mq; per slot recA, recTo, recB,
-     * vis, queue (slot k of pixel p at k * P + p; the temporal pass uses slot p only) */
+    /* the spatial pass's carving of the scratch: per pixel from, mq; per slot recA, recTo, recB,
+     * vis, queue (slot k of pixel p at k * P + p) */
     DISplit S;
     memset(&S, 0, sizeof(S));
     if (haveSplit) {
@@ -977,18 +890,7 @@ cudaError_t launch_di(const DeviceSceneView& scene, const GrisDIBindings& b, con
     }
     if (passes & 2) {
         if (timer) timer->mark(GRIS_SLOT_DI_TEMPORAL, true, stream);
-        if (haveSplit && set.temporalReuse && set.shiftType == GRIS_DI_SHIFT_RECONNECTION) {
-            cudaError_t e = cudaMemsetAsync(S.counts, 0, 2 * sizeof(uint32_t), stream);
-            if (e != cudaSuccess) return e;
-            k_di_temporal_prepare<<<grid, block, 0, stream>>>(P, S);
-            k_di_visibility<<<gridWalk, 128, 0, stream>>>(P, S);
-            if ((e = cudaMemsetAsync(S.counts, 0, 2 * sizeof(uint32_t), stream)) != cudaSuccess) return e;
-            k_di_temporal_merge<<<grid, block, 0, stream>>>(P, S);
-            k_di_visibility<<<gridWalk, 128, 0, stream>>>(P, S);
-            k_di_temporal_final<<<grid, block, 0, stream>>>(P, S);
-        } else {
-            k_di_temporal<<<grid, block, 0, stream>>>(P);
-        }
+        k_di_temporal<<<grid, block, 0, stream>>>(P);
         if (timer) timer->mark(GRIS_SLOT_DI_TEMPORAL, false, stream);
     }
     if (passes & 4) {
@@ -998,7 +900,7 @@ cudaError_t launch_di(const DeviceSceneView& scene, const GrisDIBindings& b, con
             cudaError_t e = cudaMemsetAsync(S.counts, 0, 2 * sizeof(uint32_t), stream);
             if (e != cudaSuccess) return e;
             k_di_spatial_prepare<<<grid, block, 0, stream>>>(P, S);
-            k_di_visibility<<<current_sm_count() * 16, 128, 0, stream>>>(P, S);
+            k_di_visibility<<<gridWalk, 128, 0, stream>>>(P, S);
             k_di_spatial_finish<<<grid, block, 0, stream>>>(P, S);
         } else {
             k_di_spatial<<<grid, block, 0, stream>>>(P);
