@@ -690,7 +690,12 @@ def run_di(args, rank, world, local):
     work = ctx.kernel_profile(reset=True)
     ctx.set_work_counting(False)
     slots = ["gbuffer", "di_candidates", "di_temporal", "di_spatial"]
-    launches = sum(prof[s]["launches"] for s in slots)
+    # the library's kernels per profiled pass: the candidates pass is four launches (prepare, the
+    # two walks, finish) and the spatial pass with the reconnection shift three (prepare, walk,
+    # finish); the G-buffer and the temporal pass one each
+    per_pass = {"di_candidates": 4,
+                "di_spatial": 3 if (di.spatialReuse and di.shiftType == G.DI_SHIFT_RECONNECTION) else 1}
+    launches = sum(prof[s]["launches"] * per_pass.get(s, 1) for s in slots)
     # end to end: the direct output into pinned host memory every frame
     lib = G.load()
     out_host = torch.empty((W * H * 4,), dtype=torch.float32, pin_memory=True)
