@@ -121,8 +121,6 @@ int grisBatchCreate(GrisContext* ctx, uint32_t n, const GrisScene* const* scenes
     alloc((void**)&b->motion, P * 4, true);
     alloc((void**)&b->temp, P * sizeof(GrisReservoir), true);
     alloc((void**)&b->output, P * 16, true);
-    size_t per = wave_bytes_per_path();
-    (void)per;
     alloc(&b->wave.state, P * 272, false);
     alloc(&b->wave.nee, P * 96, false);
     alloc(&b->wave.hit, P * 16, false);

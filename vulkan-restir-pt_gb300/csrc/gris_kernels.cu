@@ -2716,10 +2716,6 @@ __global__ void __launch_bounds__(128) k_gwave_post(WaveCtx C, int level) {
     }
 }
 
-size_t guide_wave_bytes_per_path() {
-    return sizeof(uint32_t) + (9 + guide::kRaw + 18 + 9 + guide::kRaw) * sizeof(float);
-}
-
 cudaError_t wave_streams_create(WaveBuffers& wb) {
     cudaError_t e = cudaStreamCreateWithFlags(&wb.aux, cudaStreamNonBlocking);
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&wb.aux2, cudaStreamNonBlocking);
@@ -2735,7 +2731,6 @@ void wave_streams_destroy(WaveBuffers& wb) {
         if (*ev) { cudaEventDestroy(*ev); *ev = nullptr; }
 }
 
-size_t wave_bytes_per_path() { return sizeof(WaveRec) + sizeof(NeeRec) + sizeof(Isec) + 1 + 3 * sizeof(uint32_t) + 32; }
 
 static size_t reuse_up(size_t n) { return (n + 255) & ~(size_t)255; }
 size_t reuse_bytes(uint64_t pixels, uint32_t slots) {

@@ -114,9 +114,6 @@ struct WaveBuffers {
 /* the side streams and events of WaveBuffers (destroy waits for the streams' work) */
 cudaError_t wave_streams_create(WaveBuffers& wb);
 void wave_streams_destroy(WaveBuffers& wb);
-/* bytes per path of the guided-batch buffers */
-size_t guide_wave_bytes_per_path();
-size_t wave_bytes_per_path();
 size_t view_entry_bytes();
 
 /* Grid sizes of the wavefront kernels, in blocks of 128 threads per SM. */
