@@ -2242,6 +2242,7 @@ struct ReuseCtx {
     uint32_t* counts;    /* [0] temporal queries, [1] their cursor, [2] spatial queries, [3] their cursor */
     uint32_t P;          /* slot stride = pixels of the batch */
     uint64_t qCap;       /* queries the queue holds */
+    uint32_t tile0;      /* first tile of the launch (the spatial pass runs in two halves of the tiles) */
 };
 
 /* Appends the visibility query of `q` (traceVisibility's ray: from -> to, tmin = MinRayDistance,
@@ -2350,9 +2351,10 @@ __global__ void __launch_bounds__(128, kReuseFinishBlocks) k_reuse_temporal_fini
 template <bool kGuide>
 __global__ void __launch_bounds__(128, kReusePrepareBlocks) k_reuse_spatial_prepare(const ViewEntry* __restrict__ V, int n,
                                                                                     ReuseCtx R) {
-    const int v = find_view_by_tile(V, n, blockIdx.x);
+    const uint32_t tb = blockIdx.x + R.tile0;
+    const int v = find_view_by_tile(V, n, tb);
     const PassCtx& P = V[v].P;
-    const uint32_t t = blockIdx.x - V[v].tileBase;
+    const uint32_t t = tb - V[v].tileBase;
     const uint32_t x = (t % V[v].tilesX) * 16u + threadIdx.x, y = (t / V[v].tilesX) * 8u + threadIdx.y;
     RayCount rc = ray_count();
     int err = 0;
@@ -2428,9 +2430,10 @@ __global__ void __launch_bounds__(128, kReusePrepareBlocks) k_reuse_spatial_prep
 template <bool kGuide>
 __global__ void __launch_bounds__(128, kReuseFinishBlocks) k_reuse_spatial_finish(const ViewEntry* __restrict__ V, int n,
                                                                                    ReuseCtx R) {
-    const int v = find_view_by_tile(V, n, blockIdx.x);
+    const uint32_t tb = blockIdx.x + R.tile0;
+    const int v = find_view_by_tile(V, n, tb);
     const PassCtx& P = V[v].P;
-    const uint32_t t = blockIdx.x - V[v].tileBase;
+    const uint32_t t = tb - V[v].tileBase;
     const uint32_t x = (t % V[v].tilesX) * 16u + threadIdx.x, y = (t / V[v].tilesX) * 8u + threadIdx.y;
     RayCount rc = ray_count();
     int err = 0;
@@ -3003,13 +3006,54 @@ reuse:
     }
     if (split && (passes & 4)) {
         if (timer) timer->mark(3, true, stream);
-        if (guide) k_reuse_spatial_prepare<true><<<tiles, blk, 0, stream>>>(V, n, R);
-        else k_reuse_spatial_prepare<false><<<tiles, blk, 0, stream>>>(V, n, R);
-        if (timer) timer->mark(GRIS_SLOT_REUSE_VIS_SPATIAL, true, stream);
-        k_reuse_visibility<3><<<gridVis, 128, 0, stream>>>(V, n, R, 1);
-        if (timer) timer->mark(GRIS_SLOT_REUSE_VIS_SPATIAL, false, stream);
-        if (guide) k_reuse_spatial_finish<true><<<tiles, blk, 0, stream>>>(V, n, R);
-        else k_reuse_spatial_finish<false><<<tiles, blk, 0, stream>>>(V, n, R);
+        auto prepare = [&](const ReuseCtx& r, uint32_t nt, cudaStream_t s) {
+            if (guide) k_reuse_spatial_prepare<true><<<nt, blk, 0, s>>>(V, n, r);
+            else k_reuse_spatial_prepare<false><<<nt, blk, 0, s>>>(V, n, r);
+        };
+        auto finish = [&](const ReuseCtx& r, uint32_t nt, cudaStream_t s) {
+            if (guide) k_reuse_spatial_finish<true><<<nt, blk, 0, s>>>(V, n, r);
+            else k_reuse_spatial_finish<false><<<nt, blk, 0, s>>>(V, n, r);
+        };
+        if (wb.aux2 != nullptr && timer == nullptr && tiles >= 2) {
+            /* Two halves of the tiles, pipelined: the first half's walk and merges on the side
+             * stream beside the second half's shifts and walk. Each half queues its queries in its
+             * own part of the queue (counts [2..3] and [4..5]); a pixel's records and verdicts
+             * belong to its half alone, and the shifts read only the temporal pass's output. */
+            const uint32_t tA = tiles / 2;
+            uint64_t pixA = 0;
+            const ViewEntry* H = reinterpret_cast<const ViewEntry*>(hViews);
+            for (int v = 0, t = 0; v < n && (uint32_t)t < tA; v++) {
+                const uint32_t W = H[v].P.b.width, Hh = H[v].P.b.height, tx = H[v].tilesX;
+                const uint32_t tv = tx * ((Hh + 7u) / 8u);
+                for (uint32_t k = 0; k < tv && (uint32_t)t < tA; k++, t++) {
+                    const uint32_t x0 = (k % tx) * 16u, y0 = (k / tx) * 8u;
+                    pixA += (uint64_t)min(16u, W - x0) * min(8u, Hh - y0);
+                }
+            }
+            ReuseCtx RA = R, RB = R;
+            RA.qCap = pixA * wb.reuse.slots;
+            RB.q = R.q + 2 * RA.qCap;
+            RB.qCap = R.qCap - RA.qCap;
+            RB.counts = R.counts + 2;
+            RB.tile0 = tA;
+            if ((e = cudaMemsetAsync(R.counts + 4, 0, 2 * sizeof(uint32_t), stream)) != cudaSuccess) return e;
+            prepare(RA, tA, stream);
+            if ((e = cudaEventRecord(wb.evTemporal, stream)) != cudaSuccess) return e;
+            if ((e = cudaStreamWaitEvent(wb.aux2, wb.evTemporal, 0)) != cudaSuccess) return e;
+            k_reuse_visibility<3><<<gridVis, 128, 0, wb.aux2>>>(V, n, RA, 1);
+            finish(RA, tA, wb.aux2);
+            if ((e = cudaEventRecord(wb.evTemporalDone, wb.aux2)) != cudaSuccess) return e;
+            prepare(RB, tiles - tA, stream);
+            k_reuse_visibility<3><<<gridVis, 128, 0, stream>>>(V, n, RB, 1);
+            finish(RB, tiles - tA, stream);
+            if ((e = cudaStreamWaitEvent(stream, wb.evTemporalDone, 0)) != cudaSuccess) return e;
+        } else {
+            prepare(R, tiles, stream);
+            if (timer) timer->mark(GRIS_SLOT_REUSE_VIS_SPATIAL, true, stream);
+            k_reuse_visibility<3><<<gridVis, 128, 0, stream>>>(V, n, R, 1);
+            if (timer) timer->mark(GRIS_SLOT_REUSE_VIS_SPATIAL, false, stream);
+            finish(R, tiles, stream);
+        }
         if (timer) timer->mark(3, false, stream);
     }
     if (split) return cudaGetLastError();
