@@ -1666,7 +1666,9 @@ GD void save_wave(WaveRec* __restrict__ dst, const T& t) {
     if constexpr (T::kAccumulate) w[16] = make_uint4(__float_as_uint(t.accAll.x), __float_as_uint(t.accAll.y),
                                                      __float_as_uint(t.accAll.z), 0u);
     if constexpr (T::kGuided) w[16].w = t.rec;
-    for (int i = 0; i < 17; i++) dst->w[i] = w[i];
+    /* word 16 carries only the accumulating and guided tracers' state (load_wave reads it only there) */
+    constexpr int kWords = T::kAccumulate ? 17 : 16;
+    for (int i = 0; i < kWords; i++) dst->w[i] = w[i];
 }
 template <class T>
 GD void load_wave(const WaveRec* __restrict__ src, T& t) {
