@@ -608,8 +608,8 @@ int grisPassRender(GrisContext* ctx, const GrisScene* s, const GrisPassBindings*
                 if (e == cudaSuccess) w.allocations.push_back(*p);
             };
             size_t P = (size_t)pixels;
-            alloc(&w.wb.state, P * 272);
-            alloc(&w.wb.nee, P * 96);
+            alloc(&w.wb.state, P * grisrt::kWaveStateBytes);
+            alloc(&w.wb.nee, P * grisrt::kWaveNeeBytes);
             alloc(&w.wb.hit, P * 16);
             alloc((void**)&w.wb.blocked, P);
             alloc((void**)&w.wb.queue[0], P * 4);

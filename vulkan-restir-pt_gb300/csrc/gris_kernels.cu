@@ -1627,30 +1627,37 @@ __global__ void __launch_bounds__(128, GridMinBlocks<KERNEL>::value) k_batch_pas
 /* ------------------------------------------------------------------ wavefront path tracer */
 /* Path state between kernels, per path id: the loop-carried members of PathTracer (17 x 16 B)
  * and the part of a bounce carried from shade() to post() across the shadow query (6 x 16 B). */
-struct WaveRec { uint4 w[17]; };
+struct WaveRec { uint4 w[16]; };
 struct NeeRec { uint4 w[6]; };
+static_assert(sizeof(WaveRec) == kWaveStateBytes && sizeof(NeeRec) == kWaveNeeBytes, "wavefront record sizes");
 
 GD uint4 u4f(float a, float b, float c, float d) {
     return make_uint4(__float_as_uint(a), __float_as_uint(b), __float_as_uint(c), __float_as_uint(d));
 }
-GD void ps_to_words(const PathSample& p, uint4* w) {
-    w[0] = make_uint4(__float_as_uint(p.rcIsec.bx), __float_as_uint(p.rcIsec.by), p.rcIsec.inst, p.rcIsec.tri);
-    w[1] = make_uint4(__float_as_uint(p.rcLi.x), __float_as_uint(p.rcLi.y), __float_as_uint(p.rcLi.z), p.rcRng);
-    w[2] = make_uint4(__float_as_uint(p.rcWi.x), __float_as_uint(p.rcWi.y), __float_as_uint(p.rcWi.z), p.flags);
-    w[3] = u4f(p.pad0, p.pad1, p.rcPrevSamplePdf, p.rcJacobian);
-    w[4] = make_uint4(__float_as_uint(p.F.x), __float_as_uint(p.F.y), __float_as_uint(p.F.z), p.primaryRng);
+/* The two path samples of a wavefront record in 9 words: their pad fields, always 0 in the path
+ * tracer, are left out (18 32-bit fields each). */
+GD void ps_put18(const PathSample& p, uint32_t* u) {
+    u[0] = __float_as_uint(p.rcIsec.bx); u[1] = __float_as_uint(p.rcIsec.by); u[2] = p.rcIsec.inst; u[3] = p.rcIsec.tri;
+    u[4] = __float_as_uint(p.rcLi.x); u[5] = __float_as_uint(p.rcLi.y); u[6] = __float_as_uint(p.rcLi.z); u[7] = p.rcRng;
+    u[8] = __float_as_uint(p.rcWi.x); u[9] = __float_as_uint(p.rcWi.y); u[10] = __float_as_uint(p.rcWi.z); u[11] = p.flags;
+    u[12] = __float_as_uint(p.rcPrevSamplePdf); u[13] = __float_as_uint(p.rcJacobian);
+    u[14] = __float_as_uint(p.F.x); u[15] = __float_as_uint(p.F.y); u[16] = __float_as_uint(p.F.z); u[17] = p.primaryRng;
 }
-GD void ps_from_words(PathSample& p, const uint4* w) {
-    p.rcIsec.bx = __uint_as_float(w[0].x); p.rcIsec.by = __uint_as_float(w[0].y); p.rcIsec.inst = w[0].z; p.rcIsec.tri = w[0].w;
-    p.rcLi = v3(__uint_as_float(w[1].x), __uint_as_float(w[1].y), __uint_as_float(w[1].z)); p.rcRng = w[1].w;
-    p.rcWi = v3(__uint_as_float(w[2].x), __uint_as_float(w[2].y), __uint_as_float(w[2].z)); p.flags = w[2].w;
-    p.pad0 = __uint_as_float(w[3].x); p.pad1 = __uint_as_float(w[3].y);
-    p.rcPrevSamplePdf = __uint_as_float(w[3].z); p.rcJacobian = __uint_as_float(w[3].w);
-    p.F = v3(__uint_as_float(w[4].x), __uint_as_float(w[4].y), __uint_as_float(w[4].z)); p.primaryRng = w[4].w;
+GD void ps_get18(PathSample& p, const uint32_t* u) {
+    p.rcIsec.bx = __uint_as_float(u[0]); p.rcIsec.by = __uint_as_float(u[1]); p.rcIsec.inst = u[2]; p.rcIsec.tri = u[3];
+    p.rcLi = v3(__uint_as_float(u[4]), __uint_as_float(u[5]), __uint_as_float(u[6])); p.rcRng = u[7];
+    p.rcWi = v3(__uint_as_float(u[8]), __uint_as_float(u[9]), __uint_as_float(u[10])); p.flags = u[11];
+    p.pad0 = 0.0f; p.pad1 = 0.0f;
+    p.rcPrevSamplePdf = __uint_as_float(u[12]); p.rcJacobian = __uint_as_float(u[13]);
+    p.F = v3(__uint_as_float(u[14]), __uint_as_float(u[15]), __uint_as_float(u[16])); p.primaryRng = u[17];
 }
+
+/* A path's wavefront record: [0..5] the tracer's scalars and ray, [6..14] the path sample and the
+ * stream's sample, [15] the accumulating / guided tracers' extra state (only they write and read
+ * it). */
 template <class T>
 GD void save_wave(WaveRec* __restrict__ dst, const T& t) {
-    uint4 w[17];
+    uint4 w[16];
     w[0] = make_uint4(t.rng, t.sampleState | (t.lastSampleState << 8) | ((t.isLastVertexConnectible ? 1u : 0u) << 16),
                       t.surf.matIndex, t.s.type);
     w[1] = u4f(t.throughput.x, t.throughput.y, t.throughput.z, t.s.pdf);
@@ -1660,26 +1667,30 @@ GD void save_wave(WaveRec* __restrict__ dst, const T& t) {
     float pdfHit = 0.0f;
     if constexpr (T::kGuided) pdfHit = t.pdfHit;
     w[5] = u4f(t.ray.dir.x, t.ray.dir.y, t.ray.dir.z, pdfHit);
-    ps_to_words(t.pathSample, w + 6);
-    ps_to_words(t.stream.ps, w + 11);
-    w[16] = make_uint4(0u, 0u, 0u, 0u);
-    if constexpr (T::kAccumulate) w[16] = make_uint4(__float_as_uint(t.accAll.x), __float_as_uint(t.accAll.y),
+    uint32_t u[36];
+    ps_put18(t.pathSample, u);
+    ps_put18(t.stream.ps, u + 18);
+#pragma unroll
+    for (int i = 0; i < 9; i++) w[6 + i] = make_uint4(u[4 * i], u[4 * i + 1], u[4 * i + 2], u[4 * i + 3]);
+    w[15] = make_uint4(0u, 0u, 0u, 0u);
+    if constexpr (T::kAccumulate) w[15] = make_uint4(__float_as_uint(t.accAll.x), __float_as_uint(t.accAll.y),
                                                      __float_as_uint(t.accAll.z), 0u);
-    if constexpr (T::kGuided) w[16].w = t.rec;
-    /* word 16 carries only the accumulating and guided tracers' state (load_wave reads it only there) */
-    constexpr int kWords = T::kAccumulate ? 17 : 16;
+    if constexpr (T::kGuided) w[15].w = t.rec;
+    constexpr int kWords = T::kAccumulate ? 16 : 15;
+#pragma unroll
     for (int i = 0; i < kWords; i++) dst->w[i] = w[i];
 }
 template <class T>
 GD void load_wave(const WaveRec* __restrict__ src, T& t) {
-    uint4 w[17];
-    for (int i = 0; i < 16; i++) w[i] = src->w[i];
+    uint4 w[16];
+#pragma unroll
+    for (int i = 0; i < 15; i++) w[i] = src->w[i];
     if constexpr (T::kAccumulate) {
-        w[16] = src->w[16];
-        t.accAll = v3(__uint_as_float(w[16].x), __uint_as_float(w[16].y), __uint_as_float(w[16].z));
+        w[15] = src->w[15];
+        t.accAll = v3(__uint_as_float(w[15].x), __uint_as_float(w[15].y), __uint_as_float(w[15].z));
         t.accCand = v3s(0.0f);
     }
-    if constexpr (T::kGuided) { t.rec = w[16].w; t.pdfHit = __uint_as_float(w[5].w); t.thrSampled = v3s(0.0f); }
+    if constexpr (T::kGuided) { t.rec = w[15].w; t.pdfHit = __uint_as_float(w[5].w); t.thrSampled = v3s(0.0f); }
     t.rng = w[0].x;
     t.sampleState = w[0].y & 0xffu; t.lastSampleState = (w[0].y >> 8) & 0xffu; t.isLastVertexConnectible = (w[0].y >> 16) & 1u;
     t.surf.matIndex = w[0].z; t.s.type = w[0].w;
@@ -1688,8 +1699,11 @@ GD void load_wave(const WaveRec* __restrict__ src, T& t) {
     t.lastPos = v3(__uint_as_float(w[3].x), __uint_as_float(w[3].y), __uint_as_float(w[3].z)); t.stream.sumWeight = __uint_as_float(w[3].w);
     t.ray.ori = v3(__uint_as_float(w[4].x), __uint_as_float(w[4].y), __uint_as_float(w[4].z)); t.stream.sampleCount = w[4].w;
     t.ray.dir = v3(__uint_as_float(w[5].x), __uint_as_float(w[5].y), __uint_as_float(w[5].z));
-    ps_from_words(t.pathSample, w + 6);
-    ps_from_words(t.stream.ps, w + 11);
+    uint32_t u[36];
+#pragma unroll
+    for (int i = 0; i < 9; i++) { u[4 * i] = w[6 + i].x; u[4 * i + 1] = w[6 + i].y; u[4 * i + 2] = w[6 + i].z; u[4 * i + 3] = w[6 + i].w; }
+    ps_get18(t.pathSample, u);
+    ps_get18(t.stream.ps, u + 18);
     t.wo = -t.ray.dir;   /* wo = -ray.dir holds at every bounce boundary */
     t.s.wi = v3s(0.0f); t.s.bsdf = v3s(0.0f);
     t.surf.isLight = false;
