@@ -59,8 +59,8 @@ METRICS = {
 UNIT = "frames/s"
 NODE_BYTES, TRI_BYTES = 80, 48
 SURFACE_BYTES = 264   # per closest hit shaded: 3 vertices (96) + transform and inverse-transpose (128) + offsets (8) + material (32)
-WAVE_STATE = 240      # one path's wavefront record as the plain tracer reads and writes it (15 x 16 B;
-                      # the accumulating and guided tracers add a 16th)
+WAVE_STATE = 248      # one path's wavefront record, the mean of the 240 B the plain tracer reads (15 x 16 B)
+                      # and the 256 B it writes (16 x 16 B: whole 32-byte sectors)
 NEE_STATE = 96        # one shadow query's record (6 x 16 B)
 
 

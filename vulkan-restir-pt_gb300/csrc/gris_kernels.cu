@@ -1652,9 +1652,9 @@ GD void ps_get18(PathSample& p, const uint32_t* u) {
     p.F = v3(__uint_as_float(u[14]), __uint_as_float(u[15]), __uint_as_float(u[16])); p.primaryRng = u[17];
 }
 
-/* A path's wavefront record: [0..5] the tracer's scalars and ray, [6..14] the path sample and the
- * stream's sample, [15] the accumulating / guided tracers' extra state (only they write and read
- * it). */
+/* A path's wavefront record (256 bytes, 8 whole sectors): [0..5] the tracer's scalars and ray,
+ * [6..14] the path sample and the stream's sample, [15] the accumulating / guided tracers' extra
+ * state (zero for the plain tracer, which does not read it). */
 template <class T>
 GD void save_wave(WaveRec* __restrict__ dst, const T& t) {
     uint4 w[16];
@@ -1676,9 +1676,10 @@ GD void save_wave(WaveRec* __restrict__ dst, const T& t) {
     if constexpr (T::kAccumulate) w[15] = make_uint4(__float_as_uint(t.accAll.x), __float_as_uint(t.accAll.y),
                                                      __float_as_uint(t.accAll.z), 0u);
     if constexpr (T::kGuided) w[15].w = t.rec;
-    constexpr int kWords = T::kAccumulate ? 16 : 15;
+    /* all 16 words, so that every 32-byte sector of the record is written whole (a partly written
+     * sector costs the L2 a read-merge when it goes to DRAM) */
 #pragma unroll
-    for (int i = 0; i < kWords; i++) dst->w[i] = w[i];
+    for (int i = 0; i < 16; i++) dst->w[i] = w[i];
 }
 template <class T>
 GD void load_wave(const WaveRec* __restrict__ src, T& t) {
