@@ -73,8 +73,7 @@ def alg_bytes(slot, w, px):
                    + surface fetches
       wave_begin   24 B G-buffer read + a path record write + its 32 B next ray + a 4 B queue
                    entry per pixel
-      wave_extend  per ray: 32 B ray + a 32 B hit record (16 B hit, written as a whole sector) + 4 B
-                   queue entry, plus traversal
+      wave_extend  per ray: 32 B ray + 16 B hit + 4 B queue entry, plus traversal
       wave_shade   per path: record read and write + 16 B hit + a surface fetch + 32 B next ray +
                    4 B queue entry; per shadow query: its 96 B record + 4 B queue entry
       wave_shadow  per shadow ray: 48 B query + 1 B verdict + 4 B queue entry, plus traversal
@@ -99,7 +98,7 @@ def alg_bytes(slot, w, px):
     if slot == "wave_begin":
         return per_px[slot] * px
     if slot == "wave_extend":
-        return trav + 68 * r
+        return trav + 52 * r
     if slot == "wave_shade":
         return w["paths"] * (2 * WAVE_STATE + 16 + SURFACE_BYTES + 32 + 4) + w["shadow_paths"] * (NEE_STATE + 4)
     if slot == "wave_shadow":

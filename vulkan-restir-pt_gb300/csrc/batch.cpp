@@ -123,7 +123,7 @@ int grisBatchCreate(GrisContext* ctx, uint32_t n, const GrisScene* const* scenes
     alloc((void**)&b->output, P * 16, true);
     alloc(&b->wave.state, P * kWaveStateBytes, false);
     alloc(&b->wave.nee, P * kWaveNeeBytes, false);
-    alloc(&b->wave.hit, P * kWaveHitBytes, false);
+    alloc(&b->wave.hit, P * 16, false);
     alloc((void**)&b->wave.blocked, P, false);
     alloc((void**)&b->wave.queue[0], P * 4, false);
     alloc((void**)&b->wave.queue[1], P * 4, false);

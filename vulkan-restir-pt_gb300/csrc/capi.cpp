@@ -610,7 +610,7 @@ int grisPassRender(GrisContext* ctx, const GrisScene* s, const GrisPassBindings*
             size_t P = (size_t)pixels;
             alloc(&w.wb.state, P * grisrt::kWaveStateBytes);
             alloc(&w.wb.nee, P * grisrt::kWaveNeeBytes);
-            alloc(&w.wb.hit, P * grisrt::kWaveHitBytes);
+            alloc(&w.wb.hit, P * 16);
             alloc((void**)&w.wb.blocked, P);
             alloc((void**)&w.wb.queue[0], P * 4);
             alloc((void**)&w.wb.queue[1], P * 4);

@@ -1629,20 +1629,7 @@ __global__ void __launch_bounds__(128, GridMinBlocks<KERNEL>::value) k_batch_pas
  * and the part of a bounce carried from shade() to post() across the shadow query (6 x 16 B). */
 struct WaveRec { uint4 w[16]; };
 struct NeeRec { uint4 w[6]; };
-struct HitRec { uint4 w[2]; };
-static_assert(sizeof(WaveRec) == kWaveStateBytes && sizeof(NeeRec) == kWaveNeeBytes && sizeof(HitRec) == kWaveHitBytes,
-              "wavefront record sizes");
-/* the hit written as a whole sector (a half-written sector costs a read-merge when it leaves L2) */
-GD void store_hit(HitRec* hit, const Isec& h) {
-    hit->w[0] = make_uint4(__float_as_uint(h.bx), __float_as_uint(h.by), h.inst, h.tri);
-    hit->w[1] = make_uint4(0u, 0u, 0u, 0u);
-}
-GD Isec load_hit(const HitRec* hit) {
-    const uint4 a = hit->w[0];
-    Isec h;
-    h.bx = __uint_as_float(a.x); h.by = __uint_as_float(a.y); h.inst = a.z; h.tri = a.w;
-    return h;
-}
+static_assert(sizeof(WaveRec) == kWaveStateBytes && sizeof(NeeRec) == kWaveNeeBytes, "wavefront record sizes");
 
 GD uint4 u4f(float a, float b, float c, float d) {
     return make_uint4(__float_as_uint(a), __float_as_uint(b), __float_as_uint(c), __float_as_uint(d));
@@ -1754,7 +1741,7 @@ struct WaveCtx {
     uint32_t totalPixels;
     WaveRec* state;
     NeeRec* nee;
-    HitRec* hit;        /* per path: the closest hit of its current ray (32 bytes: one whole sector) */
+    Isec* hit;
     unsigned char* blocked;
     uint32_t* queue[2];
     uint32_t* shadowQueue;
@@ -1878,7 +1865,7 @@ __global__ void __launch_bounds__(128) k_wave_extend(WaveCtx C, int level) {
             V3 o = v3(__uint_as_float(a.x), __uint_as_float(a.y), __uint_as_float(a.z));
             V3 d = v3(__uint_as_float(b.x), __uint_as_float(b.y), __uint_as_float(b.z));
             int v = find_view_by_pixel(C.V, C.nViews, id);
-            store_hit(C.hit + id, traceClosestHit(C.V[v].P.sc, o, d, kMinRayDistance, kMaxRayDistance, rc, err));
+            C.hit[id] = traceClosestHit(C.V[v].P.sc, o, d, kMinRayDistance, kMaxRayDistance, rc, err);
         }
     }
     flush_counts(C.counters, rc, err, 1, C.countWork, 0);
@@ -2076,7 +2063,7 @@ __global__ void __launch_bounds__(128) k_wave_trace_coop(WaveCtx C, int level) {
                 Isec r;
                 if (h.found) { r.bx = h.u; r.by = h.v; r.inst = h.inst; r.tri = h.tri; }
                 else { r.bx = 0.0f; r.by = 0.0f; r.inst = kInvalidHit; r.tri = 0u; }
-                store_hit(C.hit + id, r);
+                C.hit[id] = r;
             }
         }
         __syncwarp();
@@ -2151,7 +2138,7 @@ __global__ void __launch_bounds__(128, kWalkMinBlocks) k_wave_trace_refill(WaveC
                 Isec r;
                 if (tr.found) { r.bx = h.u; r.by = h.v; r.inst = h.inst; r.tri = h.tri; }
                 else { r.bx = 0.0f; r.by = 0.0f; r.inst = kInvalidHit; r.tri = 0u; }
-                store_hit(C.hit + id, r);
+                C.hit[id] = r;
             }
             active = false;
         }
@@ -2180,7 +2167,7 @@ __global__ void __launch_bounds__(128, GRIS_WAVE_SHADE_MIN_BLOCKS) k_wave_shade(
             load_wave(C.state + id, t);
             t.ix = x; t.iy = y; t.bounce = level;
             t.mat = load_material(P.sc, t.surf.matIndex);
-            int r = t.shade(P, load_hit(C.hit + id));
+            int r = t.shade(P, C.hit[id]);
             if (r == PathTracer::kShadow) {
                 /* the next bounce's ray now, so that its closest hit is traced while the shadow
                  * query is; post() continues the path with the same ray and checks the queueing */
@@ -2684,7 +2671,7 @@ __global__ void __launch_bounds__(128) k_gwave_shade(WaveCtx C, int level) {
             load_wave(C.state + id, t);
             t.ix = x; t.iy = y; t.bounce = level;
             t.mat = load_material(P.sc, t.surf.matIndex);
-            int r = t.shade(P, load_hit(C.hit + id));
+            int r = t.shade(P, C.hit[id]);
             if (r == GuidedTracer::kShadow || r == GuidedTracer::kPost) {
                 pushGuide = guide_eligible(t, P);
                 if (pushGuide) {
@@ -2897,7 +2884,7 @@ cudaError_t enqueue_batch(const BatchShape& sh, void* dViews, const void* hViews
             C.V = V; C.nViews = n; C.totalPixels = pixels;
             C.state = reinterpret_cast<WaveRec*>(wb.state);
             C.nee = reinterpret_cast<NeeRec*>(wb.nee);
-            C.hit = reinterpret_cast<HitRec*>(wb.hit);
+            C.hit = reinterpret_cast<Isec*>(wb.hit);
             C.blocked = wb.blocked;
             C.queue[0] = wb.queue[0]; C.queue[1] = wb.queue[1];
             C.shadowQueue = wb.shadowQueue;

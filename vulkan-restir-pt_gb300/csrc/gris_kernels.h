@@ -86,7 +86,7 @@ void reuse_carve(ReuseBuffers& r, void* block, uint64_t pixels, uint32_t slots);
 
 /* Device buffers of the wavefront path tracer, for up to `capacity` paths (pixels of a batch). */
 /* bytes per path of the wavefront's path record and NEE record */
-constexpr size_t kWaveStateBytes = 256, kWaveNeeBytes = 96, kWaveHitBytes = 32;
+constexpr size_t kWaveStateBytes = 256, kWaveNeeBytes = 96;
 
 struct WaveBuffers {
     void* state;
