@@ -236,8 +236,7 @@ int grisBatchRender(GrisContext* ctx, GrisBatch* b, const GrisCamera* cams, cons
                 e = cudaStreamEndCapture(st, &graph);
                 if (e == cudaSuccess) e = ee;
             }
-            /* the captured kernels keep their streams' priorities (the temporal pass's shifts low) */
-            if (e == cudaSuccess) e = cudaGraphInstantiate(&g.exec, graph, cudaGraphInstantiateFlagUseNodePriority);
+            if (e == cudaSuccess) e = cudaGraphInstantiate(&g.exec, graph, 0);
             if (graph) cudaGraphDestroy(graph);
             if (e != cudaSuccess) return ctx_fail(ctx, GRIS_ERR_CUDA, std::string("graph capture: ") + cudaGetErrorString(e));
             g.pathForm = form; g.maxDepth = sh.maxDepth; g.pixels = sh.pixels; g.tiles = sh.tiles;

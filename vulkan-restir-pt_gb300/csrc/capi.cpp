@@ -243,15 +243,6 @@ size_t grisSizeof(int which) {
     return 0;
 }
 
-/* The context's stream at the device's highest priority: a frame's path tracing and reuse passes
- * run there (and on a side stream of the same priority), while the temporal pass's shifts run on
- * a low-priority side stream and take the SMs the frame's critical path leaves idle. */
-static cudaError_t create_context_stream(cudaStream_t* s) {
-    int least = 0, greatest = 0;
-    if (cudaDeviceGetStreamPriorityRange(&least, &greatest) != cudaSuccess) greatest = 0;
-    return cudaStreamCreateWithPriority(s, cudaStreamNonBlocking, greatest);
-}
-
 int grisCreate(int device, GrisContext** out) {
     if (!out) return GRIS_ERR_INVALID_ARGUMENT;
     *out = nullptr;
@@ -261,7 +252,7 @@ int grisCreate(int device, GrisContext** out) {
     if (device < 0 || device >= count) return GRIS_ERR_INVALID_ARGUMENT;
     GrisContext* ctx = new GrisContext();
     ctx->device = device;
-    if (cudaSetDevice(device) != cudaSuccess || create_context_stream(&ctx->stream) != cudaSuccess ||
+    if (cudaSetDevice(device) != cudaSuccess || cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking) != cudaSuccess ||
         cudaMalloc(&ctx->dCounters, GRIS_NUM_COUNTERS * sizeof(unsigned long long)) != cudaSuccess ||
         cudaMallocHost(&ctx->hCounters, GRIS_NUM_COUNTERS * sizeof(unsigned long long)) != cudaSuccess ||
         cudaMemset(ctx->dCounters, 0, GRIS_NUM_COUNTERS * sizeof(unsigned long long)) != cudaSuccess) {

@@ -2737,12 +2737,8 @@ __global__ void __launch_bounds__(128) k_gwave_post(WaveCtx C, int level) {
 }
 
 cudaError_t wave_streams_create(WaveBuffers& wb) {
-    /* aux at the context stream's (highest) priority: it carries critical-path work; aux2 at the
-     * lowest: the temporal pass's shifts beside the path tracer fill the SMs it leaves idle */
-    int least = 0, greatest = 0;
-    if (cudaDeviceGetStreamPriorityRange(&least, &greatest) != cudaSuccess) least = greatest = 0;
-    cudaError_t e = cudaStreamCreateWithPriority(&wb.aux, cudaStreamNonBlocking, greatest);
-    if (e == cudaSuccess) e = cudaStreamCreateWithPriority(&wb.aux2, cudaStreamNonBlocking, least);
+    cudaError_t e = cudaStreamCreateWithFlags(&wb.aux, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&wb.aux2, cudaStreamNonBlocking);
     for (cudaEvent_t* ev : {&wb.evFork, &wb.evJoin, &wb.evTemporal, &wb.evTemporalDone})
         if (e == cudaSuccess) e = cudaEventCreateWithFlags(ev, cudaEventDisableTiming);
     return e;
@@ -3035,7 +3031,7 @@ reuse:
             if (guide) k_reuse_spatial_finish<true><<<nt, blk, 0, s>>>(V, n, r);
             else k_reuse_spatial_finish<false><<<nt, blk, 0, s>>>(V, n, r);
         };
-        if (wb.aux != nullptr && timer == nullptr && tiles >= 2) {
+        if (wb.aux2 != nullptr && timer == nullptr && tiles >= 2) {
             /* Two halves of the tiles, pipelined: the first half's walk and merges on the side
              * stream beside the second half's shifts and walk. Each half queues its queries in its
              * own part of the queue (counts [2..3] and [4..5]); a pixel's records and verdicts
@@ -3059,15 +3055,15 @@ reuse:
             RB.tile0 = tA;
             if ((e = cudaMemsetAsync(R.counts + 4, 0, 2 * sizeof(uint32_t), stream)) != cudaSuccess) return e;
             prepare(RA, tA, stream);
-            if ((e = cudaEventRecord(wb.evFork, stream)) != cudaSuccess) return e;
-            if ((e = cudaStreamWaitEvent(wb.aux, wb.evFork, 0)) != cudaSuccess) return e;
-            k_reuse_visibility<3><<<gridVis, 128, 0, wb.aux>>>(V, n, RA, 1);
-            finish(RA, tA, wb.aux);
-            if ((e = cudaEventRecord(wb.evJoin, wb.aux)) != cudaSuccess) return e;
+            if ((e = cudaEventRecord(wb.evTemporal, stream)) != cudaSuccess) return e;
+            if ((e = cudaStreamWaitEvent(wb.aux2, wb.evTemporal, 0)) != cudaSuccess) return e;
+            k_reuse_visibility<3><<<gridVis, 128, 0, wb.aux2>>>(V, n, RA, 1);
+            finish(RA, tA, wb.aux2);
+            if ((e = cudaEventRecord(wb.evTemporalDone, wb.aux2)) != cudaSuccess) return e;
             prepare(RB, tiles - tA, stream);
             k_reuse_visibility<3><<<gridVis, 128, 0, stream>>>(V, n, RB, 1);
             finish(RB, tiles - tA, stream);
-            if ((e = cudaStreamWaitEvent(stream, wb.evJoin, 0)) != cudaSuccess) return e;
+            if ((e = cudaStreamWaitEvent(stream, wb.evTemporalDone, 0)) != cudaSuccess) return e;
         } else {
             prepare(R, tiles, stream);
             if (timer) timer->mark(GRIS_SLOT_REUSE_VIS_SPATIAL, true, stream);

@@ -99,9 +99,8 @@ struct WaveBuffers {
     uint32_t* counts;   /* 1536 words */
     uint64_t capacity;
     /* two more streams and their events (null: the frame's kernels run in order on one stream):
-     * aux (high priority) for a bounce's shadow queries beside the next bounce's closest hits and
-     * for one half of the spatial pass, aux2 (low priority) for the temporal pass's shifts and
-     * visibility walk beside the path tracer */
+     * aux for a bounce's shadow queries beside the next bounce's closest hits, aux2 for the
+     * temporal pass's shifts and visibility walk beside the path tracer */
     cudaStream_t aux, aux2;
     cudaEvent_t evFork, evJoin, evTemporal, evTemporalDone;
     /* guided batches only (null otherwise): post queue, guide inputs / outputs per guided
