@@ -12,7 +12,8 @@
  * src/util/AliasTable.h compiled directly.
  *
  * Definitions where the reference is implementation-defined (the same in the compiled
- * reference harness and the CUDA kernels): ray queries are exact Moller-Trumbore over
+ * reference harness and the CUDA kernels): ray queries are exact Moller-Trumbore (cross and dot
+ * products fused, one rounding per fma) over
  * world-space triangles (closest hit = smallest t, then smallest (instance, triangle));
  * the G-buffer is a primary ray per pixel centre that ignores the light instance;
  * texture() is bilinear / repeat / 8-bit sub-texel weights; robust (zero) out-of-range
@@ -115,18 +116,24 @@ template <typename T> static inline T at(const std::vector<T>& v, uint64_t i) {
 }
 
 /* ------------------------------------------------------------------ ray queries (semantics in the file header) */
+/* cross and dot products with one rounding per fused step: a*b - c*d = fma(a, b, -(c*d)),
+ * a.b = fma(a.z, b.z, fma(a.y, b.y, a.x*b.x)) */
+static inline F3 crossF(const F3& a, const F3& b) {
+    return F3(fmaf(a.y, b.z, -(a.z * b.y)), fmaf(a.z, b.x, -(a.x * b.z)), fmaf(a.x, b.y, -(a.y * b.x)));
+}
+static inline float dotF(const F3& a, const F3& b) { return fmaf(a.z, b.z, fmaf(a.y, b.y, a.x * b.x)); }
 static inline bool hitTriangle(const Tri& T, const F3& o, const F3& d, float tmin, float tmax, float& t, float& u, float& v) {
-    F3 pv = cross(d, T.e2);
-    float det = dot(T.e1, pv);
+    F3 pv = crossF(d, T.e2);
+    float det = dotF(T.e1, pv);
     if (det == 0.0f) return false;
     float inv = 1.0f / det;
     F3 tv = o - T.v0;
-    u = dot(tv, pv) * inv;
+    u = dotF(tv, pv) * inv;
     if (!(u >= 0.0f) || !(u <= 1.0f)) return false;
-    F3 qv = cross(tv, T.e1);
-    v = dot(d, qv) * inv;
+    F3 qv = crossF(tv, T.e1);
+    v = dotF(d, qv) * inv;
     if (!(v >= 0.0f) || !(u + v <= 1.0f)) return false;
-    t = dot(T.e2, qv) * inv;
+    t = dotF(T.e2, qv) * inv;
     if (!(t >= tmin) || !(t <= tmax)) return false;
     return true;
 }

@@ -7,7 +7,8 @@
  *
  *   - traceClosestHit / traceShadow / traceVisibility (reference: src/shader/ray_query.glsl:6-70,
  *     hardware ray queries) as a brute-force loop over every triangle of the scene with
- *     the project's ray/triangle test (Moller-Trumbore, two-sided, t in [tmin, tmax]) and a
+ *     the project's ray/triangle test (Moller-Trumbore with its cross and dot products fused,
+ *     two-sided, t in [tmin, tmax]) and a
  *     deterministic tie-break: smallest t, then smallest (instanceIdx, triangleIdx).
  *     Instance 0 is the light geometry (src/Scene.cpp:455-479, 525-541).
  *   - the scene's storage buffers bound to caller arrays, and binary16 conversions for the
@@ -44,19 +45,25 @@ struct WTri { vec3 v0, e1, e2; uint inst, tri; };
 static std::vector<WTri> g_tris;
 static unsigned long long g_ray_counts[4];   /* closest, shadow, gbuffer, unused */
 
+/* cross and dot products with one rounding per fused step: a*b - c*d = fma(a, b, -(c*d)),
+ * a.b = fma(a.z, b.z, fma(a.y, b.y, a.x*b.x)) */
+static inline vec3 gref_cross(const vec3& a, const vec3& b) {
+    return vec3(__builtin_fmaf(a.y, b.z, -(a.z * b.y)), __builtin_fmaf(a.z, b.x, -(a.x * b.z)), __builtin_fmaf(a.x, b.y, -(a.y * b.x)));
+}
+static inline float gref_dot(const vec3& a, const vec3& b) { return __builtin_fmaf(a.z, b.z, __builtin_fmaf(a.y, b.y, a.x * b.x)); }
 static inline bool gref_tri_hit(const WTri& T, const vec3& o, const vec3& d, float tmin, float tmax,
                                 float& t, float& u, float& v) {
-    vec3 pv = cross(d, T.e2);
-    float det = dot(T.e1, pv);
+    vec3 pv = gref_cross(d, T.e2);
+    float det = gref_dot(T.e1, pv);
     if (det == 0.0f) return false;
     float inv = 1.0f / det;
     vec3 tv = o - T.v0;
-    u = dot(tv, pv) * inv;
+    u = gref_dot(tv, pv) * inv;
     if (!(u >= 0.0f) || !(u <= 1.0f)) return false;
-    vec3 qv = cross(tv, T.e1);
-    v = dot(d, qv) * inv;
+    vec3 qv = gref_cross(tv, T.e1);
+    v = gref_dot(d, qv) * inv;
     if (!(v >= 0.0f) || !(u + v <= 1.0f)) return false;
-    t = dot(T.e2, qv) * inv;
+    t = gref_dot(T.e2, qv) * inv;
     if (!(t >= tmin) || !(t <= tmax)) return false;
     return true;
 }

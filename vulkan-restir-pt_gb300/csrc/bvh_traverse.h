@@ -16,8 +16,8 @@
  *   [8..19] qlo_x[8] qlo_y[8] qlo_z[8] qhi_x[8] qhi_y[8] qhi_z[8] (bytes)
  * Triangle = 12 x f32: v0.xyz, instanceIdx | e1.xyz, triangleIdx | e2.xyz, 0  (e = v - v0).
  *
- * Hit semantics (the same everywhere in this project): Moller-Trumbore, two-sided, hits with t
- * in [tmin, tmax]; the closest hit is the smallest t, ties broken by the smaller
+ * Hit semantics (the same everywhere in this project): Moller-Trumbore with its cross and dot
+ * products fused (gris_tri_test), two-sided, hits with t in [tmin, tmax]; the closest hit is the smallest t, ties broken by the smaller
  * (instanceIdx, triangleIdx). Box tests only decide what is visited; boxes are padded and
  * rounded outward at build time so that every triangle the test would accept is reached.
  *
@@ -105,22 +105,25 @@ GRIS_HD int gris_ffs(uint32_t x) {   /* index of the lowest set bit; x != 0 */
 #endif
 }
 
-/* The project's ray/triangle test (exact IEEE sequence; no fused operations). */
+/* The project's ray/triangle test. Every cross product a*b - c*d is fma(a, b, -(c*d)) and every
+ * dot product a.x*b.x + a.y*b.y + a.z*b.z is fma(a.z, b.z, fma(a.y, b.y, a.x*b.x)): fused
+ * operations written out (each rounded once, the same on the host and the device), the rest of
+ * the sequence plain IEEE single precision. */
 GRIS_HD bool gris_tri_test(const float* T, float ox, float oy, float oz, float dx, float dy, float dz,
                            float tmin, float tmax, float* tOut, float* uOut, float* vOut) {
     float e1x = T[4], e1y = T[5], e1z = T[6];
     float e2x = T[8], e2y = T[9], e2z = T[10];
-    float pvx = dy * e2z - dz * e2y, pvy = dz * e2x - dx * e2z, pvz = dx * e2y - dy * e2x;
-    float det = (e1x * pvx + e1y * pvy) + e1z * pvz;
+    float pvx = gris_fma(dy, e2z, -(dz * e2y)), pvy = gris_fma(dz, e2x, -(dx * e2z)), pvz = gris_fma(dx, e2y, -(dy * e2x));
+    float det = gris_fma(e1z, pvz, gris_fma(e1y, pvy, e1x * pvx));
     if (det == 0.0f) return false;
     float inv = 1.0f / det;
     float tvx = ox - T[0], tvy = oy - T[1], tvz = oz - T[2];
-    float u = ((tvx * pvx + tvy * pvy) + tvz * pvz) * inv;
+    float u = gris_fma(tvz, pvz, gris_fma(tvy, pvy, tvx * pvx)) * inv;
     if (!(u >= 0.0f) || !(u <= 1.0f)) return false;
-    float qvx = tvy * e1z - tvz * e1y, qvy = tvz * e1x - tvx * e1z, qvz = tvx * e1y - tvy * e1x;
-    float v = ((dx * qvx + dy * qvy) + dz * qvz) * inv;
+    float qvx = gris_fma(tvy, e1z, -(tvz * e1y)), qvy = gris_fma(tvz, e1x, -(tvx * e1z)), qvz = gris_fma(tvx, e1y, -(tvy * e1x));
+    float v = gris_fma(dz, qvz, gris_fma(dy, qvy, dx * qvx)) * inv;
     if (!(v >= 0.0f) || !(u + v <= 1.0f)) return false;
-    float t = ((e2x * qvx + e2y * qvy) + e2z * qvz) * inv;
+    float t = gris_fma(e2z, qvz, gris_fma(e2y, qvy, e2x * qvx)) * inv;
     if (!(t >= tmin) || !(t <= tmax)) return false;
     *tOut = t; *uOut = u; *vOut = v;
     return true;
