@@ -169,13 +169,15 @@ def test_batch_graph_follows_the_mis_weights_setting():
 def test_overlapped_frame_equals_the_frame_in_order(guided):
     """A wavefront frame forks onto side streams (a bounce's closest hits beside the previous
     bounce's shadow queries and post(); the temporal pass's shifts and visibility walk beside the
-    path tracer). With the kernel timer on everything runs in order on one stream. Both must give
-    the same buffers bit for bit, through captured graphs and eager launches, on a frame whose
-    bounce levels are full (the resident walks) with temporal history, and raise no error bit
-    (bit 3: post() disagreeing with the next ray queued ahead of it)."""
+    path tracer; the spatial pass in two halves of the batch's tiles, from 2,048 tiles). With the
+    kernel timer on everything runs in order on one stream. Both must give the same buffers bit
+    for bit, through captured graphs and eager launches, on frames whose bounce levels are full
+    (the resident walks) with temporal history, and raise no error bit (bit 3: post() disagreeing
+    with the next ray queued ahead of it). Two views of 1,425 and 1,024 tiles: the halves meet
+    inside the first view."""
     hs = G.HostScene(2, seed=21, grid=48, spheres=60)
-    W, H = 176, 120
-    cams, prevs = G.sequence_cameras(hs, 4, W, H, seed=5)
+    sizes = [(400, 450), (512, 256)]
+    seq = [G.sequence_cameras(hs, 4, W, H, seed=5 + i) for i, (W, H) in enumerate(sizes)]
     st = G.Settings.make(maxDepth=8, spatialRadius=20.0)
     keys = {"resv": G.BUF_RESERVOIR, "temp": G.BUF_TEMP, "out": G.BUF_OUTPUT}
     runs = []
@@ -186,7 +188,7 @@ def test_overlapped_frame_equals_the_frame_in_order(guided):
         ctx.set_graphs(graphs)
         ctx.set_profiling(profiling)
         scene = G.Scene(ctx, hs)
-        batch = G.Batch(ctx, [scene], [(W, H)])
+        batch = G.Batch(ctx, [scene, scene], sizes)
         guide = None
         if guided:   # untrained (training folds gradients with float atomics: not bit-reproducible)
             guide = G.Guide(ctx, G.GuideConfig.make(seed=3, train=False))
@@ -194,8 +196,8 @@ def test_overlapped_frame_equals_the_frame_in_order(guided):
         ctx.counters(reset=True)
         got = []
         for f in range(4):
-            batch.render([cams[f]], [prevs[f]], [st])
-            got.append({k: batch.download(0, b).tobytes() for k, b in keys.items()})
+            batch.render([s[0][f] for s in seq], [s[1][f] for s in seq], [st, st])
+            got.append({(v, k): batch.download(v, b).tobytes() for v in range(2) for k, b in keys.items()})
         ctx.sync()
         assert ctx.counters()[3] == 0
         runs.append(got)
@@ -205,6 +207,6 @@ def test_overlapped_frame_equals_the_frame_in_order(guided):
         scene.close()
         ctx.close()
     for f in range(4):
-        for k in keys:
+        for k in runs[0][f]:
             assert runs[0][f][k] == runs[2][f][k], ("graphs vs in order", f, k)
             assert runs[1][f][k] == runs[2][f][k], ("eager vs in order", f, k)

@@ -1920,6 +1920,12 @@ constexpr int kWalkRefillIdle = GRIS_WALK_REFILL_IDLE;
 constexpr int kWalkCarveout = GRIS_WALK_CARVEOUT;
 
 constexpr uint32_t kCoopMaxRays = 8192;
+/* tiles of 16 x 8 pixels from which the spatial pass runs in two pipelined halves (below, a
+ * frame's launches and stream joins cost more than the overlap saves) */
+#ifndef GRIS_SPATIAL_HALVES_MIN_TILES
+#define GRIS_SPATIAL_HALVES_MIN_TILES 2048
+#endif
+constexpr uint32_t kSpatialHalvesMinTiles = GRIS_SPATIAL_HALVES_MIN_TILES;
 constexpr uint32_t kCoopStack = 1024;      /* node indices per warp (pushes are at most 32 per round) */
 constexpr uint32_t kCoopTris = 96;         /* triangles per round: 4 nodes x 8 slots x 3 */
 constexpr uint32_t kCoopMaxRounds = 1u << 20;
@@ -3031,7 +3037,7 @@ reuse:
             if (guide) k_reuse_spatial_finish<true><<<nt, blk, 0, s>>>(V, n, r);
             else k_reuse_spatial_finish<false><<<nt, blk, 0, s>>>(V, n, r);
         };
-        if (wb.aux2 != nullptr && timer == nullptr && tiles >= 2) {
+        if (wb.aux2 != nullptr && timer == nullptr && tiles >= kSpatialHalvesMinTiles) {
             /* Two halves of the tiles, pipelined: the first half's walk and merges on the side
              * stream beside the second half's shifts and walk. Each half queues its queries in its
              * own part of the queue (counts [2..3] and [4..5]); a pixel's records and verdicts
