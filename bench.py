@@ -20,7 +20,11 @@ launch configuration picked by grisBatchAutotune first).
           timed events;
   e2e     frames/s through the C ABI from the host: the per-frame cameras and settings come
           from host memory and every view's RGBA32F radiance is read back into pinned host
-          memory each frame, wall-clock timed;
+          memory each frame, wall-clock timed with the same L2 flush before every frame (on the
+          library's stream, its time included); the readback is pipelined
+          (grisFrameDownloadAsync / grisBatchDownloadAsync: staged on the device after the frame,
+          copied to the host beside the next frame, waited for before the next readback and
+          after the last frame);
   roofline  the kernel with the largest share of the frame: its algorithmic bytes per launch
           (BVH nodes x 80 B + triangles x 48 B + per-ray / per-pixel record bytes, counted on the
           same frames) over its average CUDA-event launch time (a separate profiled pass, eager
@@ -258,7 +262,7 @@ def make_views(args, frames, scene_lib=None):
         return G.Settings.make(shiftType=2, rrScale=1.0, temporalReuse=True, spatialReuse=True, cap=20,
                                maxDepth=depth, spatialNeighbors=3, spatialRadius=20.0)
     common = {"spatial_neighbors": 3, "spatial_radius_px": 20.0, "cap": 20, "shift": "hybrid",
-              "l2": "flushed between frames (256 MiB write outside the timed events)"}
+              "l2": "flushed between frames (256 MiB write; outside the timed events, inside the e2e wall clock)"}
     if args.workload == "c1":
         hs = G.HostScene(0, seed=args.seed, lib=scene_lib)
         st = G.Settings.make(shiftType=2, rrScale=1.0, temporalReuse=True, spatialReuse=True, cap=20, maxDepth=3,
@@ -604,7 +608,7 @@ def run_di(args, rank, world, local):
                               args.di_temporal),
               "width": W, "height": H, "triangles": hs.triangle_count(), "di_shift": args.di_shift,
               "di_sample": args.di_sample, "di_temporal": args.di_temporal,
-              "l2": "flushed between frames (256 MiB write outside the timed events)"}
+              "l2": "flushed between frames (256 MiB write; outside the timed events, inside the e2e wall clock)"}
     metric = METRICS["di"]
     if args.impl == "reference":
         if rank != 0:
@@ -697,16 +701,21 @@ def run_di(args, rank, world, local):
     per_pass = {"di_candidates": 4,
                 "di_spatial": 3 if (di.spatialReuse and di.shiftType == G.DI_SHIFT_RECONNECTION) else 1}
     launches = sum(prof[s]["launches"] * per_pass.get(s, 1) for s in slots)
-    # end to end: the direct output into pinned host memory every frame
-    lib = G.load()
+    # end to end: the direct output into pinned host memory every frame (pipelined as in the GRIS
+    # workloads: a frame's copy to the host runs beside the next frame)
     out_host = torch.empty((W * H * 4,), dtype=torch.float32, pin_memory=True)
     barrier()
     t0 = time.perf_counter()
-    for _ in range(K):
+    for k in range(K):
+        with torch.cuda.stream(stream):   # L2 flushed between frames here too, inside the wall clock
+            flush.zero_()
         frame.render_di(scene, cams[fi], prevs[fi], di)
-        ctx.check(lib.grisFrameDownload(ctx.h, frame.handle, G.BUF_DIRECT_OUTPUT, 0,
-                                        ctypes.c_void_p(out_host.data_ptr()), W * H * 16), "grisFrameDownload")
+        if k > 0:
+            ctx.download_wait()
+        frame.download_async(G.BUF_DIRECT_OUTPUT, (out_host.data_ptr(), W * H * 16))
         fi += 1
+    ctx.download_wait()
+    ctx.sync()
     barrier()
     e2e_s = max_over_ranks(time.perf_counter() - t0, "cuda")
     e2e = {"value": aggregate_rate(K, e2e_s, world), "unit": UNIT, "h2d_bytes_per_step": 2 * 352 + 16,
@@ -940,23 +949,25 @@ def main():
     # ---------------- end to end through the C ABI with host buffers
     out_host = torch.empty((px * 4,), dtype=torch.float32, pin_memory=True)
     lib = G.load()
-    offs, o = [], 0
-    for v in views:
-        offs.append(o)
-        o += v.w * v.h * 16
     barrier()
     t0 = time.perf_counter()
-    for _ in range(K):
+    for k in range(K):
+        with torch.cuda.stream(stream):   # L2 flushed between frames here too, inside the wall clock
+            flush.zero_()
         render(fi)
-        # every view's radiance into pinned host memory through the C ABI (copy + wait)
-        for vi, v in enumerate(views):
-            ptr = out_host.data_ptr() + offs[vi]
-            if batch is not None:
-                batch.download(vi, G.BUF_OUTPUT, out=(ptr, v.w * v.h * 16))
-            else:
-                ctx.check(lib.grisFrameDownload(ctx.h, frame.handle, G.BUF_OUTPUT, 0, ctypes.c_void_p(ptr),
-                                                v.w * v.h * 16), "grisFrameDownload")
+        # every view's radiance into pinned host memory through the C ABI, pipelined: the previous
+        # frame's copies are waited for once this frame is queued, then this frame's are queued
+        # (staged on the device after the frame, copied to the host beside the next frame)
+        if k > 0:
+            ctx.download_wait()
+        if batch is not None:   # the views' outputs are contiguous: one staged copy for all of them
+            batch.download_async(G.BATCH_ALL_VIEWS, G.BUF_OUTPUT, (out_host.data_ptr(), px * 16))
+        else:
+            ctx.check(lib.grisFrameDownloadAsync(ctx.h, frame.handle, G.BUF_OUTPUT, 0, ctypes.c_void_p(out_host.data_ptr()),
+                                                 px * 16), "grisFrameDownloadAsync")
         fi += 1
+    ctx.download_wait()
+    ctx.sync()
     barrier()
     e2e_s = max_over_ranks(time.perf_counter() - t0, "cuda")
     e2e = {"value": aggregate_rate(K, e2e_s, world), "unit": UNIT, "h2d_bytes_per_step": n * (2 * 352 + 64),

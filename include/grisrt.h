@@ -459,11 +459,16 @@ int grisBatchDestroy(GrisBatch* batch);
 /* cams, prevCams, settings: nViews entries each (filmSize must match the view's size). */
 int grisBatchRender(GrisContext* ctx, GrisBatch* batch, const GrisCamera* cams, const GrisCamera* prevCams,
                     const GrisSettings* settings);
-/* which / slot as in grisFrameGetBuffer, for one view. */
+/* which / slot as in grisFrameGetBuffer, for one view; view = GRIS_BATCH_ALL_VIEWS gives the
+ * buffer of every view at once (the views' pixels one after another, in view order). */
+#define GRIS_BATCH_ALL_VIEWS 0xffffffffu
 int grisBatchGetBuffer(const GrisBatch* batch, uint32_t view, int which, int slot, void** devPtr, size_t* bytes);
 /* Copies one view's buffer to host memory on the context stream and waits for it. */
 int grisBatchDownload(GrisContext* ctx, const GrisBatch* batch, uint32_t view, int which, int slot, void* host,
                       size_t bytes);
+/* The pipelined form (grisFrameDownloadAsync): returns at once, complete after grisDownloadWait. */
+int grisBatchDownloadAsync(GrisContext* ctx, const GrisBatch* batch, uint32_t view, int which, int slot, void* host,
+                           size_t bytes);
 /* Attaches a guide (NULL detaches it): the batch's path tracing then guides the vertices after
  * each path's reconnection vertex and, when the guide trains, runs its Adam steps on the
  * frame's records after each frame (wavefront path form only). */
@@ -484,6 +489,16 @@ int grisFrameRender(GrisContext* ctx, const GrisScene* scene, GrisFrame* frame, 
  * slot: 0 = the slot the last grisFrameRender wrote (current), 1 = the other one. */
 int grisFrameGetBuffer(const GrisFrame* frame, int which, int slot, void** devPtr, size_t* bytes);
 int grisFrameDownload(GrisContext* ctx, const GrisFrame* frame, int which, int slot, void* host, size_t bytes);
+/* Pipelined downloads (no counterpart in the reference, which presents its image on the GPU):
+ * the buffer is copied on the context stream into a library-owned device staging area (a
+ * device-to-device copy after the work queued so far), and from there to `host` on a separate
+ * copy stream, so that the next frame's kernels, queued right after, run while the copy to host
+ * proceeds. Returns at once; `host` holds the data after grisDownloadWait. Any number of
+ * downloads may be queued between two waits (the staging area grows; growing waits for the
+ * downloads in flight). `host` should be pinned (page-locked) for the copy to overlap. */
+int grisFrameDownloadAsync(GrisContext* ctx, const GrisFrame* frame, int which, int slot, void* host, size_t bytes);
+/* Waits for every download queued by grisFrameDownloadAsync / grisBatchDownloadAsync. */
+int grisDownloadWait(GrisContext* ctx);
 int grisFrameUpload(GrisContext* ctx, GrisFrame* frame, int which, int slot, const void* host, size_t bytes);
 
 /* ---------------------------------------------------------------- ReSTIR DI (direct lighting)

@@ -210,3 +210,78 @@ def test_overlapped_frame_equals_the_frame_in_order(guided):
         for k in runs[0][f]:
             assert runs[0][f][k] == runs[2][f][k], ("graphs vs in order", f, k)
             assert runs[1][f][k] == runs[2][f][k], ("eager vs in order", f, k)
+
+
+def test_pipelined_downloads_equal_the_waiting_ones():
+    """grisFrameDownloadAsync / grisBatchDownloadAsync: each frame's buffers staged after the frame
+    and copied to the host beside the next one equal what the waiting download reads after that
+    frame, for a frame and for a two-view batch, with several downloads queued between waits (the
+    staging area reused from its start and grown) and the next frames queued behind them."""
+    torch = pytest.importorskip("torch")
+    hs = G.HostScene(1, seed=3, grid=24, spheres=12)
+    W, H = 160, 120
+    cams, prevs = G.sequence_cameras(hs, 4, W, H, seed=9)
+    st = G.Settings.make(maxDepth=4, spatialRadius=20.0)
+    ctx = G.Context(0)
+    scene = G.Scene(ctx, hs)
+    keys = (G.BUF_OUTPUT, G.BUF_RESERVOIR)
+    # frame API: per frame the output (307 KB) and the reservoirs (1.8 MB) into pinned buffers,
+    # two frames' copies queued between waits (the 2-MB staging area is reused from its start)
+    frame = G.Frame(ctx, W, H)
+    want = []
+    for f in range(4):
+        frame.render(scene, cams[f], prevs[f], st)
+        want.append([frame.download(k).tobytes() for k in keys])
+    frame.close()
+    frame = G.Frame(ctx, W, H)
+    hosts = []
+    for f in range(4):
+        frame.render(scene, cams[f], prevs[f], st)
+        if f > 0 and f % 2 == 0:
+            ctx.download_wait()
+        bufs = []
+        for k in keys:
+            n = len(want[f][keys.index(k)])
+            b = torch.zeros(n, dtype=torch.uint8, pin_memory=True)
+            frame.download_async(k, (b.data_ptr(), n))
+            bufs.append(b)
+        hosts.append(bufs)
+    ctx.download_wait()
+    for f in range(4):
+        assert [b.numpy().tobytes() for b in hosts[f]] == want[f], ("frame", f)
+    frame.close()
+    # batch API: two views, their downloads of a frame queued before the next frame; the second
+    # view's reservoirs (3.9 MB) make the staging area grow once the copies in flight are done
+    sizes = [(W, H), (256, 160)]
+    seqs = [G.sequence_cameras(hs, 3, w, h, seed=11 + i) for i, (w, h) in enumerate(sizes)]
+    runs = []
+    for pipelined in (False, True):
+        batch = G.Batch(ctx, [scene, scene], sizes)
+        got = []
+        for f in range(3):
+            batch.render([s[0][f] for s in seqs], [s[1][f] for s in seqs], [st, st])
+            if pipelined:
+                bufs = []
+                for v, (w, h) in enumerate(sizes):
+                    for k, per in ((G.BUF_OUTPUT, 16), (G.BUF_RESERVOIR, 96)):
+                        b = torch.zeros(w * h * per, dtype=torch.uint8, pin_memory=True)
+                        batch.download_async(v, k, (b.data_ptr(), w * h * per))
+                        bufs.append(b)
+                got.append(bufs)
+            else:
+                got.append([batch.download(v, k).tobytes() for v in range(2) for k in keys])
+        # every view's output at once (GRIS_BATCH_ALL_VIEWS), pipelined and waiting
+        total = sum(w * h for (w, h) in sizes) * 16
+        allv = torch.zeros(total, dtype=torch.uint8, pin_memory=True)
+        batch.download_async(G.BATCH_ALL_VIEWS, G.BUF_OUTPUT, (allv.data_ptr(), total))
+        ctx.download_wait()
+        ctx.sync()
+        assert allv.numpy().tobytes() == batch.download(G.BATCH_ALL_VIEWS, G.BUF_OUTPUT).tobytes()
+        assert allv.numpy().tobytes() == b"".join(batch.download(v, G.BUF_OUTPUT).tobytes() for v in range(2))
+        if pipelined:
+            got = [[b.numpy().tobytes() for b in bufs] for bufs in got]
+        runs.append(got)
+        batch.close()
+    assert runs[0] == runs[1]
+    scene.close()
+    ctx.close()

@@ -262,10 +262,12 @@ int grisBatchRender(GrisContext* ctx, GrisBatch* b, const GrisCamera* cams, cons
 }
 
 int grisBatchGetBuffer(const GrisBatch* b, uint32_t view, int which, int slot, void** devPtr, size_t* bytes) {
-    if (!b || !devPtr || view >= b->n || slot < 0 || slot > 1) return GRIS_ERR_INVALID_ARGUMENT;
+    if (!b || !devPtr || (view >= b->n && view != GRIS_BATCH_ALL_VIEWS) || slot < 0 || slot > 1)
+        return GRIS_ERR_INVALID_ARGUMENT;
     int j = (b->next ^ 1) ^ slot;
-    size_t n = (size_t)b->w[view] * b->h[view];
-    uint64_t o = b->base[view];
+    const bool all = view == GRIS_BATCH_ALL_VIEWS;
+    size_t n = all ? (size_t)b->pixels : (size_t)b->w[view] * b->h[view];
+    uint64_t o = all ? 0 : b->base[view];
     void* p = nullptr;
     size_t sz = 0;
     switch (which) {
@@ -371,6 +373,15 @@ int grisBatchDownload(GrisContext* ctx, const GrisBatch* b, uint32_t view, int w
     if (e == cudaSuccess) e = cudaStreamSynchronize(ctx_stream(ctx));
     if (e != cudaSuccess) return ctx_fail(ctx, GRIS_ERR_CUDA, std::string("grisBatchDownload: ") + cudaGetErrorString(e));
     return GRIS_OK;
+}
+
+int grisBatchDownloadAsync(GrisContext* ctx, const GrisBatch* b, uint32_t view, int which, int slot, void* host,
+                           size_t bytes) {
+    void* p = nullptr;
+    size_t sz = 0;
+    if (!ctx || !host || grisBatchGetBuffer(b, view, which, slot, &p, &sz) != GRIS_OK || bytes != sz)
+        return ctx_fail(ctx, GRIS_ERR_INVALID_ARGUMENT, "bad download request");
+    return ctx_download_async(ctx, p, host, sz, "grisBatchDownloadAsync");
 }
 
 }  /* extern "C" */

@@ -119,6 +119,11 @@ struct GrisContext {
     void* diSplit = nullptr;        /* the DI spatial pass's three-launch scratch (grown on demand) */
     uint64_t diSplitPixels = 0;
     Profiler prof;
+    /* pipelined downloads: a staging area, the copy stream and its two events (created on first use) */
+    cudaStream_t copyStream = nullptr;
+    cudaEvent_t evStaged = nullptr, evCopied = nullptr;
+    char* staging = nullptr;
+    size_t stagingBytes = 0, stagingUsed = 0;
     std::string err;
 };
 
@@ -213,6 +218,41 @@ int grisrt::ctx_path_form(GrisContext* ctx) { return ctx->pathForm; }
 grisrt::KernelTimer* grisrt::ctx_timer(GrisContext* ctx) { return &ctx->prof; }
 int grisrt::ctx_fail(GrisContext* ctx, int code, const std::string& msg) { return fail(ctx, code, msg); }
 bool grisrt::ctx_graphs(GrisContext* ctx) { return ctx->useGraphs && !ctx->prof.enabled; }
+
+int grisrt::ctx_download_async(GrisContext* ctx, const void* dev, void* host, size_t bytes, const char* what) {
+    cudaSetDevice(ctx->device);
+    cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+    GRIS_CK(ctx, cudaStreamIsCapturing(ctx->stream, &cap));
+    if (cap != cudaStreamCaptureStatusNone) return fail(ctx, GRIS_ERR_INVALID_ARGUMENT, std::string(what) + ": stream is capturing");
+    if (!ctx->copyStream) {
+        GRIS_CK(ctx, cudaStreamCreateWithFlags(&ctx->copyStream, cudaStreamNonBlocking));
+        GRIS_CK(ctx, cudaEventCreateWithFlags(&ctx->evStaged, cudaEventDisableTiming));
+        GRIS_CK(ctx, cudaEventCreateWithFlags(&ctx->evCopied, cudaEventDisableTiming));
+    }
+    const size_t need = (bytes + 255) & ~(size_t)255;
+    if (ctx->stagingUsed + need > ctx->stagingBytes) {
+        /* every staged region is free once the copies to host are done (each waited for its
+         * device-to-device copy); then the area is reused from its start, or replaced */
+        GRIS_CK(ctx, cudaEventSynchronize(ctx->evCopied));
+        ctx->stagingUsed = 0;
+        if (need > ctx->stagingBytes) {
+            if (ctx->staging) GRIS_CK(ctx, cudaFree(ctx->staging));
+            ctx->staging = nullptr;
+            ctx->stagingBytes = 0;
+            const size_t sz = std::max(need, (size_t)2 << 20);
+            GRIS_CK(ctx, cudaMalloc(&ctx->staging, sz));
+            ctx->stagingBytes = sz;
+        }
+    }
+    char* st = ctx->staging + ctx->stagingUsed;
+    ctx->stagingUsed += need;
+    GRIS_CK(ctx, cudaMemcpyAsync(st, dev, bytes, cudaMemcpyDeviceToDevice, ctx->stream));
+    GRIS_CK(ctx, cudaEventRecord(ctx->evStaged, ctx->stream));
+    GRIS_CK(ctx, cudaStreamWaitEvent(ctx->copyStream, ctx->evStaged, 0));
+    GRIS_CK(ctx, cudaMemcpyAsync(host, st, bytes, cudaMemcpyDeviceToHost, ctx->copyStream));
+    GRIS_CK(ctx, cudaEventRecord(ctx->evCopied, ctx->copyStream));
+    return GRIS_OK;
+}
 grisrt::WaveLaunch grisrt::ctx_wave_launch(GrisContext* ctx) { return ctx->waveLaunch; }
 void grisrt::ctx_set_tuning(GrisContext* ctx, int pathForm, grisrt::WaveLaunch wl) { ctx->pathForm = pathForm; ctx->waveLaunch = wl; }
 
@@ -270,6 +310,10 @@ int grisDestroy(GrisContext* ctx) {
     ctx->wave.release();
     if (ctx->dReduce) cudaFree(ctx->dReduce);
     if (ctx->diSplit) cudaFree(ctx->diSplit);
+    if (ctx->copyStream) { cudaStreamSynchronize(ctx->copyStream); cudaStreamDestroy(ctx->copyStream); }
+    if (ctx->evStaged) cudaEventDestroy(ctx->evStaged);
+    if (ctx->evCopied) cudaEventDestroy(ctx->evCopied);
+    if (ctx->staging) cudaFree(ctx->staging);
     cudaFree(ctx->dCounters);
     cudaFreeHost(ctx->hCounters);
     if (ctx->stream) cudaStreamDestroy(ctx->stream);
@@ -851,6 +895,22 @@ int grisFrameDownload(GrisContext* ctx, const GrisFrame* f, int which, int slot,
     cudaSetDevice(ctx->device);
     GRIS_CK(ctx, cudaMemcpyAsync(host, p, sz, cudaMemcpyDeviceToHost, ctx->stream));
     GRIS_CK(ctx, cudaStreamSynchronize(ctx->stream));
+    return GRIS_OK;
+}
+
+int grisFrameDownloadAsync(GrisContext* ctx, const GrisFrame* f, int which, int slot, void* host, size_t bytes) {
+    void* p; size_t sz;
+    int rc = grisFrameGetBuffer(f, which, slot, &p, &sz);
+    if (rc != GRIS_OK || !ctx || !host || bytes != sz) return fail(ctx, GRIS_ERR_INVALID_ARGUMENT, "bad download request");
+    return grisrt::ctx_download_async(ctx, p, host, sz, "grisFrameDownloadAsync");
+}
+
+int grisDownloadWait(GrisContext* ctx) {
+    if (!ctx) return GRIS_ERR_INVALID_ARGUMENT;
+    if (!ctx->copyStream) return GRIS_OK;
+    cudaSetDevice(ctx->device);
+    GRIS_CK(ctx, cudaEventSynchronize(ctx->evCopied));
+    ctx->stagingUsed = 0;
     return GRIS_OK;
 }
 

@@ -40,6 +40,9 @@ int ctx_count_work(GrisContext* ctx);
 int ctx_path_form(GrisContext* ctx);
 KernelTimer* ctx_timer(GrisContext* ctx);
 int ctx_fail(GrisContext* ctx, int code, const std::string& msg);
+/* a pipelined download (grisFrameDownloadAsync): device-to-device into the staging area on the
+ * context stream, then to host on the copy stream */
+int ctx_download_async(GrisContext* ctx, const void* dev, void* host, size_t bytes, const char* what);
 struct WaveLaunch;
 namespace guide { struct GuideDevice; }
 guide::GuideDevice guide_device(const GrisGuide* g);

@@ -214,7 +214,7 @@ EXPORTS = [
     "grisNoAllocReadError", "grisMeasureL2Bandwidth",
     "grisFrameCreate", "grisFrameDestroy", "grisFrameRender", "grisFrameGetBuffer", "grisFrameDownload",
     "grisFrameUpload", "grisSetPathForm", "grisBatchCreate", "grisBatchDestroy", "grisBatchRender", "grisBatchGetBuffer",
-    "grisBatchDownload", "grisSetGraphs", "grisSetWaveLaunch", "grisBatchAutotune",
+    "grisBatchDownload", "grisFrameDownloadAsync", "grisBatchDownloadAsync", "grisDownloadWait", "grisSetGraphs", "grisSetWaveLaunch", "grisBatchAutotune",
     "grisReadKernelProfile", "grisConvergedAccumulate", "grisRelMSE",
     "grisGuideCreate", "grisGuideDestroy", "grisGuideParamCount", "grisGuideSetParams", "grisGuideGetParams",
     "grisGuideSetTraining", "grisGuideForward", "grisGuideGradient", "grisGuideTrainStep", "grisBatchSetGuide",
@@ -281,6 +281,9 @@ def load(path=None):
         "grisBatchRender": (i32, [vp, vp, ctypes.POINTER(Camera), ctypes.POINTER(Camera), ctypes.POINTER(Settings)]),
         "grisBatchGetBuffer": (i32, [vp, u32, i32, i32, ctypes.POINTER(vp), ctypes.POINTER(ctypes.c_size_t)]),
         "grisBatchDownload": (i32, [vp, vp, u32, i32, i32, vp, ctypes.c_size_t]),
+        "grisFrameDownloadAsync": (i32, [vp, vp, i32, i32, vp, ctypes.c_size_t]),
+        "grisBatchDownloadAsync": (i32, [vp, vp, u32, i32, i32, vp, ctypes.c_size_t]),
+        "grisDownloadWait": (i32, [vp]),
         "grisSetGraphs": (i32, [vp, i32]),
         "grisGuideCreate": (i32, [vp, ctypes.POINTER(GuideConfig), ctypes.POINTER(vp)]),
         "grisGuideDestroy": (i32, [vp]),
@@ -488,6 +491,10 @@ class Context:
     def stream(self):
         return load().grisGetStream(self.h)
 
+    def download_wait(self):
+        """Waits for the pipelined downloads queued so far (grisDownloadWait)."""
+        self.check(load().grisDownloadWait(self.h), "grisDownloadWait")
+
     def l2_bandwidth(self, nbytes=48 << 20, reps=20):
         """L2 read bandwidth in GB/s (grisMeasureL2Bandwidth)."""
         g = ctypes.c_double()
@@ -627,6 +634,7 @@ class Scene:
 
 
 BUF_DEPTH_NORMAL, BUF_ALBEDO_MATID, BUF_MOTION, BUF_RESERVOIR, BUF_TEMP, BUF_OUTPUT = range(6)
+BATCH_ALL_VIEWS = 0xFFFFFFFF   # a batch buffer of every view at once, in view order
 BUF_DI_RESERVOIR, BUF_DI_TEMP, BUF_DIRECT_OUTPUT = 6, 7, 8
 _BUF_DTYPE = {0: (np.float32, 4), 1: (np.uint32, 2), 2: (np.uint16, 2), 3: (RESERVOIR, None),
               4: (RESERVOIR, None), 5: (np.float32, 4), 6: (DI_RESERVOIR, None), 7: (DI_RESERVOIR, None),
@@ -668,6 +676,13 @@ class Frame:
         self.ctx.check(load().grisFrameDownload(self.ctx.h, self.handle, which, slot, arr.ctypes.data, arr.nbytes),
                        "grisFrameDownload")
         return arr
+
+    def download_async(self, which, out, slot=0):
+        """Queues a pipelined copy into the caller's host buffer `out` = (pointer, bytes); complete
+        after Context.download_wait() (grisFrameDownloadAsync)."""
+        ptr, nbytes = out
+        self.ctx.check(load().grisFrameDownloadAsync(self.ctx.h, self.handle, which, slot, ctypes.c_void_p(ptr), nbytes),
+                       "grisFrameDownloadAsync")
 
     def close(self):
         if self.handle:
@@ -786,15 +801,23 @@ class Batch:
     def download(self, view, which, slot=0, out=None):
         """Copies one view's buffer to the host (waits on the context stream)."""
         dt, ch = _BUF_DTYPE[which]
-        w, h = self.sizes[view]
+        px = sum(w * h for (w, h) in self.sizes) if view == BATCH_ALL_VIEWS else self.sizes[view][0] * self.sizes[view][1]
         if out is None:
-            out = np.zeros((w * h, ch) if ch else w * h, dtype=dt)
+            out = np.zeros((px, ch) if ch else px, dtype=dt)
             ptr, nbytes = out.ctypes.data, out.nbytes
         else:   # caller-provided host buffer (e.g. pinned): (pointer, bytes)
             ptr, nbytes = out
         self.ctx.check(load().grisBatchDownload(self.ctx.h, self.handle, view, which, slot, ctypes.c_void_p(ptr), nbytes),
                        "grisBatchDownload")
         return out
+
+    def download_async(self, view, which, out, slot=0):
+        """Queues a pipelined copy of one view's buffer into the caller's host buffer `out` =
+        (pointer, bytes), pinned for the copy to overlap the next frame; complete after
+        Context.download_wait() (grisBatchDownloadAsync)."""
+        ptr, nbytes = out
+        self.ctx.check(load().grisBatchDownloadAsync(self.ctx.h, self.handle, view, which, slot, ctypes.c_void_p(ptr),
+                                                     nbytes), "grisBatchDownloadAsync")
 
     def close(self):
         if self.handle:
