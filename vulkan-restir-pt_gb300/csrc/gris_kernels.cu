@@ -1326,6 +1326,14 @@ GD void flush_gbuffer_counts(unsigned long long* counters, uint32_t primary, int
     }
 }
 
+/* resident blocks of 128 threads per SM asked of the compiler for the batch G-buffer kernel
+ * (0: no request). At C2: 7 blocks (72 registers) 0.546 ms per frame, none (80 registers, 6
+ * blocks) 0.583 ms, 8 blocks (64 registers, spills) 0.591 ms. The single-view kernel k_gbuffer
+ * (the DI frame's G-buffer) measured slower with 7 (0.551 against 0.530 ms) and keeps none. */
+#ifndef GRIS_GBUFFER_MIN_BLOCKS
+#define GRIS_GBUFFER_MIN_BLOCKS 7
+#endif
+
 __global__ void __launch_bounds__(128) k_gbuffer(GBufCtx G) {
     uint32_t x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y * blockDim.y + threadIdx.y;
     int err = 0;
@@ -1596,7 +1604,7 @@ GD int find_view_by_pixel(const ViewEntry* V, int n, uint32_t id) {
 }
 
 /* G-buffer, temporal and spatial passes over every view: one 16 x 8 block per tile. */
-__global__ void __launch_bounds__(128) k_batch_gbuffer(const ViewEntry* __restrict__ V, int n) {
+__global__ void __launch_bounds__(128, GRIS_GBUFFER_MIN_BLOCKS) k_batch_gbuffer(const ViewEntry* __restrict__ V, int n) {
     int v = find_view_by_tile(V, n, blockIdx.x);
     const GBufCtx& G = V[v].G;
     uint32_t t = blockIdx.x - V[v].tileBase;
