@@ -271,6 +271,14 @@ GD bool di_pixel(const DICtx& P, uint32_t ix, uint32_t iy, DIPixel& px) {
     return true;
 }
 
+/* resident blocks of 128 threads per SM asked of the compiler for the DI kernels that walk their
+ * queries inline (the temporal pass, the spatial pass's finish with the final occlusion test).
+ * At 1080p: 8 blocks (64 registers; their spills stay in L1) 188.1 frames/s, 7 blocks 186.7,
+ * 6 blocks 184.1. */
+#ifndef GRIS_DI_INLINE_WALK_BLOCKS
+#define GRIS_DI_INLINE_WALK_BLOCKS 8
+#endif
+
 /* ------------------------------------------------------------------ kernels */
 __global__ void __launch_bounds__(128, 8) k_di_candidates(DICtx P) {
     RayCount rc = ray_count();
@@ -311,7 +319,7 @@ GD bool di_temporal_source(const DICtx& P, uint32_t x, uint32_t y, const DIPixel
     return di_usable(src);
 }
 
-__global__ void __launch_bounds__(128, 8) k_di_temporal(DICtx P) {
+__global__ void __launch_bounds__(128, GRIS_DI_INLINE_WALK_BLOCKS) k_di_temporal(DICtx P) {
     RayCount rc = ray_count();
     int err = 0;
     uint32_t x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y * blockDim.y + threadIdx.y;
@@ -645,7 +653,7 @@ __global__ void __launch_bounds__(128, 7) k_di_visibility(DICtx P, DISplit S) {
     flush_counts(P.counters, rc, err, 6, P.countWork);
 }
 
-__global__ void __launch_bounds__(128, 8) k_di_spatial_finish(DICtx P, DISplit S) {
+__global__ void __launch_bounds__(128, GRIS_DI_INLINE_WALK_BLOCKS) k_di_spatial_finish(DICtx P, DISplit S) {
     RayCount rc = ray_count();
     int err = 0;
     const uint32_t x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y * blockDim.y + threadIdx.y;
