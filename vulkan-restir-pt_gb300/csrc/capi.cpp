@@ -118,6 +118,7 @@ struct GrisContext {
     double* dReduce = nullptr;      /* relMSE partial sums (allocated on first use) */
     void* diSplit = nullptr;        /* the DI spatial pass's three-launch scratch (grown on demand) */
     uint64_t diSplitPixels = 0;
+    grisrt::DISide diSide{nullptr, nullptr, nullptr};   /* the DI candidates pass's side stream */
     Profiler prof;
     /* pipelined downloads: a staging area, the copy stream and its two events (created on first use) */
     cudaStream_t copyStream = nullptr;
@@ -310,6 +311,9 @@ int grisDestroy(GrisContext* ctx) {
     ctx->wave.release();
     if (ctx->dReduce) cudaFree(ctx->dReduce);
     if (ctx->diSplit) cudaFree(ctx->diSplit);
+    if (ctx->diSide.aux) { cudaStreamSynchronize(ctx->diSide.aux); cudaStreamDestroy(ctx->diSide.aux); }
+    if (ctx->diSide.evFork) cudaEventDestroy(ctx->diSide.evFork);
+    if (ctx->diSide.evJoin) cudaEventDestroy(ctx->diSide.evJoin);
     if (ctx->copyStream) { cudaStreamSynchronize(ctx->copyStream); cudaStreamDestroy(ctx->copyStream); }
     if (ctx->evStaged) cudaEventDestroy(ctx->evStaged);
     if (ctx->evCopied) cudaEventDestroy(ctx->evCopied);
@@ -794,8 +798,22 @@ int grisPassDI(GrisContext* ctx, const GrisScene* s, const GrisDIBindings* b, co
         if (cudaMalloc(&ctx->diSplit, grisrt::di_split_bytes_per_pixel() * px + 256) == cudaSuccess) ctx->diSplitPixels = px;
         else ctx->diSplit = nullptr;
     }
+    if (split && !ctx->diSide.aux && cap == cudaStreamCaptureStatusNone) {
+        grisrt::DISide d{nullptr, nullptr, nullptr};
+        if (cudaStreamCreateWithFlags(&d.aux, cudaStreamNonBlocking) == cudaSuccess &&
+            cudaEventCreateWithFlags(&d.evFork, cudaEventDisableTiming) == cudaSuccess &&
+            cudaEventCreateWithFlags(&d.evJoin, cudaEventDisableTiming) == cudaSuccess) {
+            ctx->diSide = d;
+        } else {   /* without them the walks run in order */
+            if (d.aux) cudaStreamDestroy(d.aux);
+            if (d.evFork) cudaEventDestroy(d.evFork);
+            if (d.evJoin) cudaEventDestroy(d.evJoin);
+            cudaGetLastError();
+        }
+    }
     GRIS_CK(ctx, grisrt::launch_di(view, *b, *cam, *prevCam, *set, passes & 7, ctx->dCounters, ctx->countWork,
-                                   &ctx->prof, ctx->stream, ctx->diSplit, ctx->diSplitPixels));
+                                   ctx->prof.enabled ? &ctx->prof : nullptr, ctx->stream, ctx->diSplit,
+                                   ctx->diSplitPixels, ctx->diSide.aux ? &ctx->diSide : nullptr));
     return GRIS_OK;
 }
 

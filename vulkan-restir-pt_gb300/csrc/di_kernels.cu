@@ -844,7 +844,8 @@ size_t di_split_bytes_per_pixel() {
 
 cudaError_t launch_di(const DeviceSceneView& scene, const GrisDIBindings& b, const GrisCamera& cam,
                       const GrisCamera& prevCam, const GrisDISettings& set, int passes, unsigned long long* counters,
-                      int countWork, KernelTimer* timer, cudaStream_t stream, void* split, uint64_t splitPixels) {
+                      int countWork, KernelTimer* timer, cudaStream_t stream, void* split, uint64_t splitPixels,
+                      const DISide* side) {
     DICtx P;
     P.sc = to_dev(scene);
     P.cam = make_cam(cam);
@@ -888,8 +889,19 @@ cudaError_t launch_di(const DeviceSceneView& scene, const GrisDIBindings& b, con
             cudaError_t e = cudaMemsetAsync(Q.counts, 0, 4 * sizeof(uint32_t), stream);
             if (e != cudaSuccess) return e;
             k_di_candidates_prepare<<<grid, block, 0, stream>>>(P, Q);
-            k_di_candidates_walk<true><<<gridWalk, 128, 0, stream>>>(P, Q);
+            /* the two walks share nothing but the ray counters (atomics): the shadow queries on
+             * the side stream beside the closest-hit queries, joined before the finish kernel */
+            const bool fork = side != nullptr && side->aux != nullptr && timer == nullptr;
+            if (fork) {
+                if ((e = cudaEventRecord(side->evFork, stream)) != cudaSuccess) return e;
+                if ((e = cudaStreamWaitEvent(side->aux, side->evFork, 0)) != cudaSuccess) return e;
+                k_di_candidates_walk<true><<<gridWalk, 128, 0, side->aux>>>(P, Q);
+                if ((e = cudaEventRecord(side->evJoin, side->aux)) != cudaSuccess) return e;
+            } else {
+                k_di_candidates_walk<true><<<gridWalk, 128, 0, stream>>>(P, Q);
+            }
             k_di_candidates_walk<false><<<gridWalk, 128, 0, stream>>>(P, Q);
+            if (fork && (e = cudaStreamWaitEvent(stream, side->evJoin, 0)) != cudaSuccess) return e;
             k_di_candidates_finish<<<grid, block, 0, stream>>>(P, Q);
         } else {
             k_di_candidates<<<grid, block, 0, stream>>>(P);

@@ -40,11 +40,17 @@ cudaError_t launch_gris(const DeviceSceneView& scene, const GrisPassBindings& b,
                         int countWork, KernelTimer* timer, cudaStream_t stream, int launchMode = GRIS_LAUNCH_PERSISTENT);
 /* ReSTIR DI (TestReSTIR::render): passes bit 0 candidates, bit 1 temporal, bit 2 spatial */
 /* split: scratch of di_split_bytes_per_pixel() * splitPixels + 256 bytes for the candidates and
- * spatial passes in three launches (null or too small: their single kernels) */
+ * spatial passes in three launches (null or too small: their single kernels). side: a second
+ * stream and two events of the caller's, on which the candidates pass walks its shadow queries
+ * beside its closest-hit queries (null, or a kernel timer: both on `stream`, in order) */
+struct DISide {
+    cudaStream_t aux;
+    cudaEvent_t evFork, evJoin;
+};
 cudaError_t launch_di(const DeviceSceneView& scene, const GrisDIBindings& b, const GrisCamera& cam,
                       const GrisCamera& prevCam, const GrisDISettings& set, int passes, unsigned long long* counters,
                       int countWork, KernelTimer* timer, cudaStream_t stream, void* split = nullptr,
-                      uint64_t splitPixels = 0);
+                      uint64_t splitPixels = 0, const DISide* side = nullptr);
 size_t di_split_bytes_per_pixel();
 /* presentation pass (post_proc.frag): composition, tone mapping, gamma, UNORM8 */
 cudaError_t launch_post(const GrisPostBindings& b, const GrisPostSettings& set, cudaStream_t stream);
