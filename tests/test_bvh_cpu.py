@@ -22,6 +22,22 @@ def _rays(scene, n, seed, mode):
         d[np.arange(n), k] = rng.choice([-1.0, 1.0], n)
     elif mode == "grazing":
         d[:, 2] *= 1e-3
+    elif mode == "edges":
+        # towards the vertices, edge midpoints and random edge points of random triangles (world
+        # space through the instance transforms, column-major 4x4): the triangle test's u = 0,
+        # v = 0 and u + v = 1 boundaries, where its rounding decides between neighbours
+        inst = [k for k in scene.instances if int(k["indexCount"]) >= 3]
+        for i in range(n):
+            k = inst[int(rng.integers(0, len(inst)))]
+            tri = int(rng.integers(0, int(k["indexCount"]) // 3))
+            ids = scene.indices[int(k["indexOffset"]) + 3 * tri:int(k["indexOffset"]) + 3 * tri + 3]
+            P = v[ids].astype(np.float64)
+            e = int(rng.integers(0, 3))
+            s = (0.0, 0.5, 1.0, float(rng.uniform()))[int(rng.integers(0, 4))]
+            p = P[e] + s * (P[(e + 1) % 3] - P[e])
+            M = np.asarray(k["transform"], np.float64).reshape(4, 4).T
+            w = M[:3, :3] @ p + M[:3, 3]
+            d[i] = w - o[i]
     d /= np.linalg.norm(d, axis=1, keepdims=True)
     rays = np.zeros((n, 8), np.float32)
     rays[:, 0:3], rays[:, 3], rays[:, 4:7], rays[:, 7] = o, 1e-4, d, 1e7
@@ -36,7 +52,7 @@ def oracle_bf():
 
 
 @pytest.mark.parametrize("kind,grid,spheres", [(0, 0, 0), (1, 48, 60), (2, 40, 40)])
-@pytest.mark.parametrize("mode", ["random", "axis", "grazing", "short"])
+@pytest.mark.parametrize("mode", ["random", "axis", "grazing", "short", "edges"])
 def test_bvh_closest_and_any_hit_match_brute_force(kind, grid, spheres, mode, oracle_bf):
     hs = G.HostScene(kind, seed=3, grid=grid, spheres=spheres)
     bvh = G.load()
