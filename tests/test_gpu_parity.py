@@ -107,19 +107,27 @@ def test_gpu_pairwise_weights_match_oracle(case, mode, ctx, ora):
     test_gpu_matches_oracle_bit_exact(case, mode, ctx, ora)
 
 
-def test_device_traversal_matches_host(ctx):
-    """50,000 random rays, closest hit and any hit: the device walk with the resident traversal
-    kernels' short stack (two register entries, here one shared-memory entry, then the local-memory
-    overflow, so deep walks use all three) against the host walk's array stack, bit for bit."""
+@pytest.mark.parametrize("rays_kind", ["random", "edges"])
+def test_device_traversal_matches_host(ctx, rays_kind):
+    """50,000 random rays (or 20,000 aimed at triangle vertices and edges, where the fused
+    triangle test's rounding decides), closest hit and any hit: the device walk with the resident
+    traversal kernels' short stack (two register entries, here one shared-memory entry, then the
+    local-memory overflow, so deep walks use all three) against the host walk's array stack, bit
+    for bit."""
     hs = G.HostScene(1, seed=4, grid=64, spheres=100)
     scene = G.Scene(ctx, hs)
-    rng = np.random.default_rng(5)
-    n = 50000
-    rays = np.zeros((n, 8), np.float32)
-    rays[:, 0:3] = rng.uniform([-55, -55, -5], [55, 55, 25], (n, 3))
-    d = rng.normal(size=(n, 3))
-    rays[:, 4:7] = d / np.linalg.norm(d, axis=1, keepdims=True)
-    rays[:, 3], rays[:, 7] = 1e-4, 1e7
+    if rays_kind == "edges":
+        from test_bvh_cpu import _rays
+        rays = _rays(hs, 20000, 6, "edges")
+        n = len(rays)
+    else:
+        rng = np.random.default_rng(5)
+        n = 50000
+        rays = np.zeros((n, 8), np.float32)
+        rays[:, 0:3] = rng.uniform([-55, -55, -5], [55, 55, 25], (n, 3))
+        d = rng.normal(size=(n, 3))
+        rays[:, 4:7] = d / np.linalg.norm(d, axis=1, keepdims=True)
+        rays[:, 3], rays[:, 7] = 1e-4, 1e7
     import torch
     dr = torch.from_numpy(rays).cuda()
     tuv = torch.zeros((n, 4), dtype=torch.float32, device="cuda")
