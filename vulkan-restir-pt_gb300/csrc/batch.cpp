@@ -245,8 +245,10 @@ int grisBatchRender(GrisContext* ctx, GrisBatch* b, const GrisCamera* cams, cons
         }
         e = cudaGraphLaunch(g.exec, st);
     } else {
-        e = enqueue_batch(sh, b->dViews, b->hViews[k], b->wave, ctx_counters(ctx), ctx_count_work(ctx), ctx_timer(ctx), st,
-                          form, 15, wl, b->guide ? &gd : nullptr);
+        /* eager launches: the side streams as in the captured graph unless per-kernel profiling
+         * wants every kernel in order on one stream */
+        e = enqueue_batch(sh, b->dViews, b->hViews[k], b->wave, ctx_counters(ctx), ctx_count_work(ctx),
+                          ctx_profiling(ctx) ? ctx_timer(ctx) : nullptr, st, form, 15, wl, b->guide ? &gd : nullptr);
         if (e == cudaSuccess && train) {
             KernelTimer* tm = ctx_timer(ctx);
             if (tm) tm->mark(10, true, st);

@@ -219,6 +219,7 @@ int grisrt::ctx_path_form(GrisContext* ctx) { return ctx->pathForm; }
 grisrt::KernelTimer* grisrt::ctx_timer(GrisContext* ctx) { return &ctx->prof; }
 int grisrt::ctx_fail(GrisContext* ctx, int code, const std::string& msg) { return fail(ctx, code, msg); }
 bool grisrt::ctx_graphs(GrisContext* ctx) { return ctx->useGraphs && !ctx->prof.enabled; }
+bool grisrt::ctx_profiling(GrisContext* ctx) { return ctx->prof.enabled; }
 
 int grisrt::ctx_download_async(GrisContext* ctx, const void* dev, void* host, size_t bytes, const char* what) {
     cudaSetDevice(ctx->device);

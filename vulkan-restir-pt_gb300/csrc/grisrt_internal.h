@@ -49,6 +49,7 @@ guide::GuideDevice guide_device(const GrisGuide* g);
 const GrisGuideConfig& guide_config(const GrisGuide* g);
 cudaError_t guide_train_frame(GrisGuide* g, cudaStream_t st);
 bool ctx_graphs(GrisContext* ctx);            /* graphs enabled and per-kernel profiling off */
+bool ctx_profiling(GrisContext* ctx);         /* per-kernel profiling on (kernels then run in order) */
 WaveLaunch ctx_wave_launch(GrisContext* ctx);
 void ctx_set_tuning(GrisContext* ctx, int pathForm, WaveLaunch wl);
 /* Device view and device ordinal of an uploaded scene; false for a host-only scene. */
